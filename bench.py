@@ -1,0 +1,336 @@
+"""Benchmark of the explicit MPM step (USL, linear hat basis) on one GB300.
+
+Workload (default): the 3D Taylor bar -- J2 plasticity with linear hardening,
+E=117e9, nu=0.35, rho=8930, sigma_y=400e6, H=100e6, cylinder r=3.2 mm,
+L=32.4 mm, 2x2x2 particles per cell at h=0.25 mm (511,784 particles) on a
+65x65x161-node grid, -190 m/s against the z=0 wall, dt = 0.2 h/c.
+One bench step = one full USL step (P2G, grid update, G2P + F + J2) of all
+particles.  Inputs are synthetic (generated from the geometry).  The
+particle state (~160 MB) and grid (~70 MB) exceed the 129 MB L2, so no L2
+flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision f64|f32]
+  python bench.py --impl reference ...   # the CPU restatement on the host cores
+
+Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# one process per GPU: pin this rank to its GPU before any CUDA runtime starts
+if "LOCAL_RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
+    os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-updates/s"
+# Algorithmic bytes per particle per launch, FP64, 3D J2 (each persistent field
+# read once and each updated field written once; symmetric tensors counted as 6):
+#   P2G  reads x3 v3 m V sigma6                      = 14 doubles -> 112 B
+#   G2P  reads x3 v3 V0 F9 eps6 alpha ep6            = 29 doubles
+#        writes x3 v3 V F9 eps6 sigma6 alpha ep6 vm  = 36 doubles -> 520 B
+# plus the grid share (8 particles per active node): P2G 7 doubles/node, G2P 6
+# doubles/node gathered, grid update 13 doubles/node -> 600 B per particle-update.
+BYTES = {
+    "f64": {"p2g": 112 + 7, "g2p": 520 + 6, "step": 600},
+    "f32": {"p2g": 56 + 7, "g2p": 260 + 3, "step": 330},
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, precision: str):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_taylor_bar_{precision}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch_full_size:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or (dev.isdigit() and parts[0] != dev):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(name: str):
+    from jump_gb300 import scenarios
+    if name == "taylor_bar":
+        g, s, alg, data = scenarios.taylor_bar()
+        cfg = {"workload": "taylor_bar_3d_j2", "particles": int(s[0].parCount), "grid_nodes": [65, 65, 161],
+               "h_m": 2.5e-4, "particles_per_cell": 8, "material": "J2 linear hardening",
+               "dt_s": data["dt"], "l2": "inputs larger than L2 (~230 MB resident)"}
+    elif name == "two_disks":
+        g, s, alg, data = scenarios.two_disks()
+        cfg = {"workload": "two_disks_2d_elastic", "particles": int(sum(x.parCount for x in s)),
+               "grid_nodes": [21, 21], "l2": "fits in L2 (latency-bound case)"}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    scenarios.apply_dirichlet(g, data)
+    return g, s, alg, data, cfg
+
+
+def dist_init(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    backend = "nccl"
+    try:
+        import torch
+        torch.cuda.set_device(0)
+    except Exception:
+        backend = "gloo"
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def allreduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t)
+    return float(t.item())
+
+
+def cpu_sample(desc_factory, np_total, threads, target_s):
+    """Time the CPU oracle on the same workload for about target_s seconds."""
+    from oracle.oracle import OracleContext
+    ctx = OracleContext(desc_factory(), threads=threads)
+    ctx.step(1, check=False)  # first touch
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        ctx.step(1, check=False)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= target_s or steps >= 1000:
+            break
+    ctx.close()
+    return np_total * steps / el, steps, el
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from jump_gb300.engine import Descriptors
+    from oracle import oracle
+    oracle.build()
+    g, s, alg, data, cfg = workload(args.workload)
+    npart = sum(x.parCount for x in s)
+    mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"])
+    threads = oracle.max_threads()
+    ctx = oracle.OracleContext(mk(), threads=threads)
+    for _ in range(args.warmup):
+        ctx.step(1, check=False)
+    t0 = time.perf_counter()
+    ctx.step(args.steps, check=False)
+    el = time.perf_counter() - t0
+    ctx.close()
+    value = npart * args.steps / el
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (geometry-generated particles)", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full USL steps of the workload after {args.warmup} warm-up "
+                                   f"steps; C++ restatement of the Julia loops (Julia is not installed on the "
+                                   f"host), OpenMP over {threads} threads"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = dist_init(world)
+    from jump_gb300 import _capi
+    if not os.path.exists(_capi.LIB_PATH):
+        from jump_gb300 import build
+        build.build()
+    from jump_gb300.engine import Descriptors, MPMContext
+    from jump_gb300.problem import step_times
+
+    g, s, alg, data, cfg = workload(args.workload)
+    npart = sum(x.parCount for x in s)
+    mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
+                             precision=args.precision)
+    ctx = MPMContext(mk())
+    ctx.step(args.warmup)
+    sampler = ClockSampler()
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    ctx.step(args.steps)  # synchronizes the context stream before returning
+    wall = time.perf_counter() - t0
+    dev_ms = ctx.last_step_ms()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    t_max = allreduce_max(dist, dev_ms / 1e3)
+    total_updates = allreduce_sum(dist, float(npart * args.steps))
+    value = total_updates / t_max
+
+    # per-stage device times (individual launches, CUDA events on the context stream)
+    nprof = max(3, min(args.steps, 10))
+    st = ctx.profile_stages(nprof)
+    per = {k: v / nprof for k, v in st.items()}
+    dom = max(("p2g", "g2p"), key=lambda k: per[k])
+    peak, peak_kind = load_peaks()
+    bts = BYTES[args.precision][dom] * npart
+    achieved = bts / (per[dom] * 1e-3) / 1e9
+    traffic = ncu_traffic(dom, args.precision)
+    step_bytes = BYTES[args.precision]["step"] * npart
+    ctx.close()
+
+    # end to end through the public API: host arrays -> device, K steps with the
+    # EnergiesFix sums read back every step, full particle download at the end
+    e2e_ctx_t0 = time.perf_counter()
+    desc = mk()
+    c2 = MPMContext(desc)
+    for _ in range(args.steps):
+        c2.step(1)
+        c2.energies()
+    states = c2.download_all()
+    e2e_wall = time.perf_counter() - e2e_ctx_t0
+    c2.close()
+    h2d = sum(a.nbytes for a in desc._keep)
+    d2h = sum(sum(getattr(stt, k).nbytes for k in ("pos", "velocity", "volume", "F", "strain", "stress",
+                                                   "alpha", "pstrain", "vmstr")) for stt in states)
+    e2e_t = allreduce_max(dist, e2e_wall)
+    e2e_value = total_updates / e2e_t
+
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            from oracle import oracle
+            oracle.build()
+            thr = oracle.max_threads()
+            v_all, n_all, el_all = cpu_sample(lambda: Descriptors(g, s, tolerance=alg.tolerance,
+                                                                  body_force=data.get("bodyforce"),
+                                                                  dt=data["dt"]),
+                                              npart, thr, args.cpu_seconds)
+            v_one, n_one, el_one = cpu_sample(lambda: Descriptors(g, s, tolerance=alg.tolerance,
+                                                                  body_force=data.get("bodyforce"),
+                                                                  dt=data["dt"]),
+                                              npart, 1, args.cpu_seconds / 3)
+            cpu = {"value": v_all, "unit": METRIC, "cores": thr, "kind": "port",
+                   "sample": f"{n_all} USL steps of the same workload in {el_all:.1f} s (FP64 C++ "
+                             f"restatement of the reference loops, OpenMP {thr} threads); single thread: "
+                             f"{v_one:.4g} {METRIC} over {n_one} steps",
+                   "single_thread_value": v_one}
+        out = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+            "data": "synthetic (geometry-generated particles, no dataset)",
+            "config": dict(cfg, precision=args.precision,
+                           parallelism=f"replicas{world}" if world > 1 else "single-gpu"),
+            "wall_ms_per_step": 1e3 * wall / args.steps,
+            "stage_ms_per_step": per,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": bts,
+                         "step_frac": step_bytes / (t_max / args.steps) / 1e9 / peak},
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / args.steps,
+                    "d2h_bytes_per_step": d2h / args.steps + 8 * 5},
+            "gpu_launches": args.steps * (2 * len(s) + 1),
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--workload", default="taylor_bar", choices=["taylor_bar", "two_disks"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/*
+ * jump_mpm.h -- C ABI of the GB300 explicit-MPM step (USL, linear hat basis).
+ *
+ * This is the drop-in boundary for jump's explicit solid-mechanics solvers:
+ *
+ *   solve_explicit_dynamics_2D(grid::Grid2D, solids::Vector{Solid2D}, basis::LinearBasis,
+ *                              alg::USL, output, fixes, data)
+ *       SolveExplicitSolidMechanics2D.jl:335-585
+ *   solve_explicit_dynamics_3D(grid::Grid3D, solids::Vector{Solid3D}, basis::LinearBasis,
+ *                              alg::USL, output, fixes, data)
+ *       SolveExplicitSolidMechanics3D.jl:230-378
+ *
+ * A host binding (Julia ccall, Python ctypes) builds one context from the
+ * Grid/Solid/Material arrays, advances it some steps, downloads the particle
+ * state before each output/fix hook and at the end, then destroys it.
+ * Every array crossing this boundary is plain host memory owned by the
+ * caller; the library never retains a caller pointer after a call returns.
+ *
+ * Layouts follow Julia's memory layout of the reference types, so a Julia
+ * binding can pass `reinterpret`ed arrays without copies:
+ *   - Vector{SVector{d,Float64}}      -> d doubles per particle/node, AoS
+ *   - Vector{SMatrix{d,d,Float64}}    -> d*d doubles per particle, column-major
+ *   - grid.fixedNodes::Array{Int64,2} -> (d, nodeCount), column-major
+ * Node and particle indices in this ABI are 0-based; node I (1-based in the
+ * reference, Grid.jl:151,259) is element I-1 here.
+ *
+ * Every function returns an int status: MPM_OK (0) or one of MPM_ERR_*.
+ * mpm_last_error() returns a message for the last failing call of the
+ * calling thread.  A context may be used from one host thread at a time.
+ */
+#ifndef JUMP_MPM_H
+#define JUMP_MPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JUMP_MPM_ABI_VERSION 1
+
+/* status codes */
+#define MPM_OK               0
+#define MPM_ERR_ARG          1  /* invalid argument or descriptor */
+#define MPM_ERR_CUDA         2  /* a CUDA runtime call failed */
+#define MPM_ERR_NEGATIVE_J   3  /* det F <= 0 at some particle (state still advanced) */
+#define MPM_ERR_NONFINITE    4  /* NaN/Inf in a particle's velocity, position or stress */
+#define MPM_ERR_OUT_OF_GRID  5  /* a particle's cell lies outside the grid; it was frozen */
+#define MPM_ERR_TIMEOUT      6  /* a bounded device-side wait gave up */
+#define MPM_ERR_UNSUPPORTED  7  /* feature not available in this build */
+
+/* material models (Material.jl) */
+#define MPM_MAT_ELASTIC     0   /* ElasticMaterial, Material.jl:37-81 */
+#define MPM_MAT_NEOHOOKEAN  1   /* NeoHookeanMaterial, Material.jl:100-122 */
+#define MPM_MAT_J2          2   /* ElastoPlasticMaterial, Material.jl:128-275 */
+
+/* particle precision (grid accumulation is always FP64) */
+#define MPM_PREC_F64        0   /* every particle field and every operation in FP64 */
+#define MPM_PREC_F32        1   /* FP32 particle fields and arithmetic; FP64 nodes, det F, energies */
+
+typedef struct mpm_grid_desc {
+  int32_t dim;                 /* 2 (Grid2D) or 3 (Grid3D) */
+  int32_t reserved;
+  double  xmin[3];             /* Grid2D(xmin,xmax,ymin,ymax,nx,ny), Grid.jl:104 */
+  double  xmax[3];             /* Grid3D(xmin,xmax,ymin,ymax,zmin,zmax,nx,ny,nz), Grid.jl:198 */
+  int64_t nodes[3];            /* iN_x, iN_y(, iN_z): nodes per axis, >= 2 */
+  const int64_t* fixed_nodes;  /* grid.fixedNodes (dim x nodeCount, column-major), or NULL */
+} mpm_grid_desc;
+
+typedef struct mpm_material_desc {
+  int32_t type;                /* MPM_MAT_* */
+  int32_t reserved;
+  double  E, nu, density;      /* constructor arguments */
+  double  fy, k1;              /* J2 yield stress and linear hardening modulus */
+} mpm_material_desc;
+
+/* Particle arrays of one Solid2D/Solid3D (Solid.jl:67-125, 267-297), read at create time. */
+typedef struct mpm_body_desc {
+  int64_t count;                    /* parCount */
+  mpm_material_desc mat;
+  const double* pos;                /* dim   per particle */
+  const double* velocity;           /* dim   per particle */
+  const double* mass;               /* 1 */
+  const double* volume;             /* 1 */
+  const double* volume_initial;     /* 1 */
+  const double* F;                  /* dim*dim, column-major */
+  const double* strain;             /* dim*dim */
+  const double* stress;             /* dim*dim */
+  const double* alpha;              /* J2: equivalent plastic strain, or NULL (zeros) */
+  const double* pstrain;            /* J2: 3 (2D Voigt) or 9 (3D) per particle, or NULL */
+  const double* youngs;             /* optional per-particle Young's modulus, or NULL */
+} mpm_body_desc;
+
+/* Writable views for mpm_download; any pointer may be NULL to skip that field. */
+typedef struct mpm_body_view {
+  double* pos;
+  double* velocity;
+  double* volume;
+  double* F;
+  double* strain;
+  double* stress;
+  double* alpha;
+  double* pstrain;
+  double* vmstr;                    /* von Mises stress written by Elastic-3D and J2 updates */
+} mpm_body_view;
+
+typedef struct mpm_params {
+  double  dt;                  /* data["dt"] */
+  double  tolerance;           /* USL.tolerance: nodal mass cutoff in G2P, Algorithm.jl:16-18 */
+  double  body_force[3];       /* ConstantBodyForce2D/3D.g, BodyForce.jl:56-62,85-91 */
+  int32_t precision;           /* MPM_PREC_F64 or MPM_PREC_F32 */
+  int32_t contact;             /* 0: one velocity field (the reference USL); 1: one field per body
+                                  with the multi-body contact correction */
+  double  friction;            /* Coulomb coefficient for contact (2D only; 0 = frictionless) */
+  int32_t sort_interval;       /* re-sort particles by cell every N steps (0 = never) */
+  int32_t flags;               /* reserved, 0 */
+} mpm_params;
+
+typedef struct mpm_ctx mpm_ctx;
+
+/* Library identity. */
+int         mpm_abi_version(void);
+const char* mpm_last_error(void);
+
+/* Build a context: copies grid + particle arrays to device memory. */
+int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t nbodies,
+               const mpm_params* params, mpm_ctx** out);
+
+/* Advance nsteps USL steps (the body of the `while t < Tf` loop,
+   SolveExplicitSolidMechanics2D.jl:381-534).  If t_inout is not NULL,
+   *t_inout += dt once per step, in FP64, exactly like `t += dtime` (:580). */
+int mpm_step(mpm_ctx* ctx, int64_t nsteps, double* t_inout);
+
+/* Copy one body's particle state back into caller-owned host arrays
+   (original particle order, the layouts of mpm_body_desc). */
+int mpm_download(mpm_ctx* ctx, int32_t body, const mpm_body_view* out);
+
+/* Grid state after the last step: grid.mass, grid.momentum0, grid.momentum
+   and grid.force (the reference's arrays after its grid update, :429-442).
+   Each pointer may be NULL; sizes nodeCount and dim*nodeCount. */
+int mpm_download_grid(mpm_ctx* ctx, double* mass, double* momentum0, double* momentum,
+                      double* force);
+
+/* EnergiesFix quantities (Fix.jl:248-270) reduced on the device in FP64:
+   KE = sum 1/2 m v.v, SE = sum 1/2 V sigma:eps, and total momentum (dim). */
+int mpm_energies(mpm_ctx* ctx, double* ke, double* se, double* momentum);
+
+/* Snapshot / restore of the full particle state (checkpoint/resume).  With
+   buf == NULL, mpm_save stores the byte size it needs in *nbytes. */
+int mpm_save(mpm_ctx* ctx, void* buf, size_t* nbytes);
+int mpm_load(mpm_ctx* ctx, const void* buf, size_t nbytes);
+
+/* Device time of the kernels of the last mpm_step call, in milliseconds,
+   measured with CUDA events on the context's stream. */
+int mpm_last_step_ms(mpm_ctx* ctx, double* ms);
+
+/* Measurement aid (no counterpart in the reference): run nsteps steps as
+   individual launches with CUDA events between the stages and add each
+   stage's device time, in milliseconds, to stage_ms[MPM_STAGE_*]. */
+#define MPM_STAGE_RESET 0
+#define MPM_STAGE_P2G   1
+#define MPM_STAGE_GRID  2
+#define MPM_STAGE_G2P   3
+#define MPM_NUM_STAGES  4
+int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
+
+int mpm_destroy(mpm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JUMP_MPM_H */

@@ -1,0 +1,187 @@
+"""ctypes mirror of include/jump_mpm.h and the loader of the CUDA library.
+
+The structures here are the boundary a Julia ``ccall`` shim would fill from
+jump's Grid/Solid/Material objects (SolveExplicitSolidMechanics2D.jl:335,
+SolveExplicitSolidMechanics3D.jl:230).  The product library is
+``jump_gb300/lib/libjumpmpm.so``; importing this module never falls back to a
+CPU implementation: when the library is missing, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+MPM_OK = 0
+MPM_ERR_ARG = 1
+MPM_ERR_CUDA = 2
+MPM_ERR_NEGATIVE_J = 3
+MPM_ERR_NONFINITE = 4
+MPM_ERR_OUT_OF_GRID = 5
+MPM_ERR_TIMEOUT = 6
+MPM_ERR_UNSUPPORTED = 7
+
+ERR_NAMES = {
+    MPM_ERR_ARG: "MPM_ERR_ARG",
+    MPM_ERR_CUDA: "MPM_ERR_CUDA",
+    MPM_ERR_NEGATIVE_J: "MPM_ERR_NEGATIVE_J",
+    MPM_ERR_NONFINITE: "MPM_ERR_NONFINITE",
+    MPM_ERR_OUT_OF_GRID: "MPM_ERR_OUT_OF_GRID",
+    MPM_ERR_TIMEOUT: "MPM_ERR_TIMEOUT",
+    MPM_ERR_UNSUPPORTED: "MPM_ERR_UNSUPPORTED",
+}
+
+MPM_MAT_ELASTIC = 0
+MPM_MAT_NEOHOOKEAN = 1
+MPM_MAT_J2 = 2
+
+MPM_PREC_F64 = 0
+MPM_PREC_F32 = 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int64)
+
+
+class GridDesc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("reserved", C.c_int32),
+        ("xmin", C.c_double * 3),
+        ("xmax", C.c_double * 3),
+        ("nodes", C.c_int64 * 3),
+        ("fixed_nodes", _ip),
+    ]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("reserved", C.c_int32),
+        ("E", C.c_double),
+        ("nu", C.c_double),
+        ("density", C.c_double),
+        ("fy", C.c_double),
+        ("k1", C.c_double),
+    ]
+
+
+class BodyDesc(C.Structure):
+    _fields_ = [
+        ("count", C.c_int64),
+        ("mat", MaterialDesc),
+        ("pos", _dp),
+        ("velocity", _dp),
+        ("mass", _dp),
+        ("volume", _dp),
+        ("volume_initial", _dp),
+        ("F", _dp),
+        ("strain", _dp),
+        ("stress", _dp),
+        ("alpha", _dp),
+        ("pstrain", _dp),
+        ("youngs", _dp),
+    ]
+
+
+class BodyView(C.Structure):
+    _fields_ = [
+        ("pos", _dp),
+        ("velocity", _dp),
+        ("volume", _dp),
+        ("F", _dp),
+        ("strain", _dp),
+        ("stress", _dp),
+        ("alpha", _dp),
+        ("pstrain", _dp),
+        ("vmstr", _dp),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double),
+        ("tolerance", C.c_double),
+        ("body_force", C.c_double * 3),
+        ("precision", C.c_int32),
+        ("contact", C.c_int32),
+        ("friction", C.c_double),
+        ("sort_interval", C.c_int32),
+        ("flags", C.c_int32),
+    ]
+
+
+def dptr(a: np.ndarray | None):
+    """Pointer to a C-contiguous float64 array (None -> NULL)."""
+    if a is None:
+        return _dp()
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], "need C-contiguous float64"
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray | None):
+    if a is None:
+        return _ip()
+    assert a.dtype == np.int64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_ip)
+
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libjumpmpm.so")
+
+# Every symbol include/jump_mpm.h declares, with its ctypes signature.
+SIGNATURES = {
+    "mpm_abi_version": (C.c_int, []),
+    "mpm_last_error": (C.c_char_p, []),
+    "mpm_create": (C.c_int, [C.POINTER(GridDesc), C.POINTER(BodyDesc), C.c_int32,
+                             C.POINTER(Params), C.POINTER(C.c_void_p)]),
+    "mpm_step": (C.c_int, [C.c_void_p, C.c_int64, _dp]),
+    "mpm_download": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(BodyView)]),
+    "mpm_download_grid": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
+    "mpm_energies": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "mpm_save": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_size_t)]),
+    "mpm_load": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "mpm_last_step_ms": (C.c_int, [C.c_void_p, _dp]),
+    "mpm_profile_stages": (C.c_int, [C.c_void_p, C.c_int64, _dp]),
+    "mpm_destroy": (C.c_int, [C.c_void_p]),
+}
+
+STAGES = ("reset", "p2g", "grid", "g2p")
+
+_lib = None
+_lock = threading.Lock()
+
+
+class MPMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load_library(path: str):
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
+def lib():
+    """The CUDA library; raises if it has not been built (no CPU fallback)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; "
+                    "g.build()\"` (the CUDA path has no CPU fallback)")
+            _lib = load_library(LIB_PATH)
+        return _lib
+
+
+def check(code: int, L=None):
+    if code != MPM_OK:
+        L = L or lib()
+        raise MPMError(code, L.mpm_last_error().decode())

@@ -1,0 +1,575 @@
+// mpm_capi.cu -- the C ABI of include/jump_mpm.h: context lifetime, host <->
+// device layout conversion and the step loop (one captured CUDA graph per
+// USL step, replayed nsteps times on the context's stream).
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/jump_mpm.h"
+#include "mpm_internal.h"
+
+using namespace jmpm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                  \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(MPM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+int sym_slot(int dim, int i, int j) {
+  if (i == j) return i;
+  if (dim == 2) return 2;
+  int a = i < j ? i : j, b = i < j ? j : i;
+  return (a == 0 && b == 1) ? 3 : ((a == 1 && b == 2) ? 4 : 5);
+}
+
+int num_fields(int dim) { return dim == 2 ? Layout<2>::NF : Layout<3>::NF; }
+
+struct FieldIdx {
+  int X, V, M, VOL, VOL0, F, EPS, SIG, VM, ALPHA, EP, LAM, MU, S, PS;
+};
+
+template <int D>
+FieldIdx make_idx() {
+  using L = Layout<D>;
+  return FieldIdx{L::X, L::V, L::M, L::VOL, L::VOL0, L::F, L::EPS, L::SIG,
+                  L::VM, L::ALPHA, L::EP, L::LAM, L::MU, L::S, L::PS};
+}
+
+}  // namespace
+
+struct mpm_ctx {
+  int dim = 2;
+  bool f32 = false;
+  mpm_params prm{};
+  int nb = 0;
+  std::vector<int64_t> off, cnt;
+  std::vector<MatParams> mats;
+  int64_t np = 0;
+  int NF = 0;
+  size_t esz = 8;
+  FieldIdx fi{};
+  void* P = nullptr;
+  GridP g{};
+  NodeP nd{};
+  double* coords = nullptr;
+  uint8_t* fixed = nullptr;
+  double* nodebuf = nullptr;
+  float* nodebuf_f = nullptr;
+  std::vector<uint8_t> fixed_h;
+  unsigned* status = nullptr;
+  double* partial = nullptr;
+  double* red = nullptr;
+  double* staging = nullptr;
+  size_t staging_n = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double last_ms = 0.0;
+
+  PartP part(int b) const {
+    PartP pp;
+    pp.base = P;
+    pp.pitch = np;
+    pp.begin = off[b];
+    pp.count = cnt[b];
+    return pp;
+  }
+  PartP all() const {
+    PartP pp;
+    pp.base = P;
+    pp.pitch = np;
+    pp.begin = 0;
+    pp.count = np;
+    return pp;
+  }
+};
+
+namespace {
+
+void destroy_ctx(mpm_ctx* c) {
+  if (!c) return;
+  if (c->exec) cudaGraphExecDestroy(c->exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  cudaFree(c->P);
+  cudaFree(c->coords);
+  cudaFree(c->fixed);
+  cudaFree(c->nodebuf);
+  cudaFree(c->nodebuf_f);
+  cudaFree(c->status);
+  cudaFree(c->partial);
+  cudaFree(c->red);
+  cudaFree(c->staging);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+void launch_aos_to_soa(mpm_ctx* c, const PartP& pp, const double* src, int per, int f0,
+                       const CompMapH& cm) {
+  if (c->dim == 2) Launchers<2>::aos_to_soa(c->stream, pp, c->f32, src, per, f0, cm);
+  else Launchers<3>::aos_to_soa(c->stream, pp, c->f32, src, per, f0, cm);
+}
+
+void launch_soa_to_aos(mpm_ctx* c, const PartP& pp, double* dst, int per, int f0, const CompMapH& cm) {
+  if (c->dim == 2) Launchers<2>::soa_to_aos(c->stream, pp, c->f32, dst, per, f0, cm);
+  else Launchers<3>::soa_to_aos(c->stream, pp, c->f32, dst, per, f0, cm);
+}
+
+// host AoS array -> staging -> SoA fields [f0, f0 + cm.n)
+int upload(mpm_ctx* c, int b, const double* host, int per, int f0, const CompMapH& cm) {
+  size_t n = size_t(c->cnt[b]) * per;
+  if (n == 0) return MPM_OK;
+  CUDA_TRY(cudaMemcpyAsync(c->staging, host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_aos_to_soa(c, c->part(b), c->staging, per, f0, cm);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+int download(mpm_ctx* c, int b, double* host, int per, int f0, const CompMapH& cm) {
+  size_t n = size_t(c->cnt[b]) * per;
+  if (n == 0 || !host) return MPM_OK;
+  launch_soa_to_aos(c, c->part(b), c->staging, per, f0, cm);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(host, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+CompMapH ident(int n) {
+  CompMapH m{};
+  m.n = n;
+  for (int i = 0; i < n; ++i) m.src[i] = i;
+  return m;
+}
+
+// upload: symmetric slot s <- column-major entry
+CompMapH sym_from_full(int dim) {
+  CompMapH m{};
+  m.n = dim == 2 ? 3 : 6;
+  for (int j = 0; j < dim; ++j)
+    for (int i = j; i < dim; ++i) m.src[sym_slot(dim, i, j)] = i + dim * j;
+  return m;
+}
+
+// download: column-major entry <- symmetric slot
+CompMapH full_from_sym(int dim) {
+  CompMapH m{};
+  m.n = dim * dim;
+  for (int j = 0; j < dim; ++j)
+    for (int i = 0; i < dim; ++i) m.src[i + dim * j] = sym_slot(dim, i, j);
+  return m;
+}
+
+bool symmetric(const double* a, int64_t n, int dim) {
+  if (!a) return true;
+  for (int64_t p = 0; p < n; ++p)
+    for (int i = 0; i < dim; ++i)
+      for (int j = i + 1; j < dim; ++j)
+        if (a[p * dim * dim + i + dim * j] != a[p * dim * dim + j + dim * i]) return false;
+  return true;
+}
+
+// The launches of one USL step; ev (optional) gets an event recorded after each stage.
+void enqueue_step(mpm_ctx* c, cudaEvent_t* ev) {
+  const int D = c->dim;
+  const size_t acc = size_t(c->nd.nodeCount) * (1 + 2 * D);
+  cudaMemsetAsync(c->nodebuf, 0, acc * sizeof(double), c->stream);
+  if (ev) cudaEventRecord(ev[0], c->stream);
+  for (int b = 0; b < c->nb; ++b) {
+    if (D == 2) Launchers<2>::p2g(c->stream, c->g, c->nd, c->part(b), c->f32, c->prm.body_force, c->status);
+    else Launchers<3>::p2g(c->stream, c->g, c->nd, c->part(b), c->f32, c->prm.body_force, c->status);
+  }
+  if (ev) cudaEventRecord(ev[1], c->stream);
+  if (D == 2) Launchers<2>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
+  else Launchers<3>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
+  if (ev) cudaEventRecord(ev[2], c->stream);
+  for (int b = 0; b < c->nb; ++b) {
+    if (D == 2) Launchers<2>::g2p(c->stream, c->g, c->nd, c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+    else Launchers<3>::g2p(c->stream, c->g, c->nd, c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+  }
+  if (ev) cudaEventRecord(ev[3], c->stream);
+}
+
+int build_step_graph(mpm_ctx* c) {
+  if (c->exec) return MPM_OK;
+  CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(c, nullptr);
+  cudaError_t le = cudaGetLastError();
+  cudaError_t ee = cudaStreamEndCapture(c->stream, &c->graph);
+  if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(le));
+  if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
+  CUDA_TRY(cudaGraphInstantiate(&c->exec, c->graph, 0));
+  return MPM_OK;
+}
+
+int status_to_code(unsigned st) {
+  if (st & ST_OUT_OF_GRID) return fail(MPM_ERR_OUT_OF_GRID, "a particle left the grid; it was frozen in place");
+  if (st & ST_NONFINITE) return fail(MPM_ERR_NONFINITE, "non-finite particle velocity, position or stress");
+  if (st & ST_NEGATIVE_J) return fail(MPM_ERR_NEGATIVE_J, "det F <= 0 at a particle");
+  return MPM_OK;
+}
+
+int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodies, const mpm_params* prm,
+                mpm_ctx* c) {
+  const int D = gd->dim;
+  c->dim = D;
+  c->prm = *prm;
+  c->f32 = prm->precision == MPM_PREC_F32;
+  c->esz = c->f32 ? sizeof(float) : sizeof(double);
+  c->NF = num_fields(D);
+  c->fi = D == 2 ? make_idx<2>() : make_idx<3>();
+  c->nb = nbodies;
+  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&c->e0));
+  CUDA_TRY(cudaEventCreate(&c->e1));
+
+  // grid geometry, exactly as Grid2D/Grid3D build it (Grid.jl:105-107, 149-152, 199-204, 256-261)
+  int64_t nn[3] = {1, 1, 1};
+  double dx[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a) {
+    nn[a] = gd->nodes[a];
+    dx[a] = (gd->xmax[a] - gd->xmin[a]) / (double(gd->nodes[a]) - 1.0);
+    c->g.xmin[a] = gd->xmin[a];
+    c->g.dxI[a] = 1.0 / dx[a];
+    c->g.nn[a] = nn[a];
+  }
+  c->g.nx = nn[0];
+  c->g.nxy = nn[0] * nn[1];
+  c->g.nodeCount = c->g.nxy * nn[2];
+  const int64_t Nn = c->g.nodeCount;
+  std::vector<double> coords_h;
+  for (int a = 0; a < D; ++a)
+    for (int64_t i = 0; i < nn[a]; ++i) coords_h.push_back(gd->xmin[a] + double(i) * dx[a]);
+  CUDA_TRY(cudaMalloc(&c->coords, coords_h.size() * sizeof(double)));
+  CUDA_TRY(cudaMemcpy(c->coords, coords_h.data(), coords_h.size() * sizeof(double), cudaMemcpyHostToDevice));
+  int64_t o = 0;
+  for (int a = 0; a < 3; ++a) {
+    c->g.coord[a] = a < D ? c->coords + o : c->coords;
+    if (a < D) o += nn[a];
+  }
+
+  // Dirichlet mask (grid.fixedNodes, set by fix_Dirichlet_grid, Dirichlet.jl:28-78)
+  c->fixed_h.assign(Nn, 0);
+  if (gd->fixed_nodes)
+    for (int64_t i = 0; i < Nn; ++i)
+      for (int a = 0; a < D; ++a)
+        if (gd->fixed_nodes[a + D * i] == 1) c->fixed_h[i] |= uint8_t(1u << a);
+  CUDA_TRY(cudaMalloc(&c->fixed, Nn));
+  CUDA_TRY(cudaMemcpy(c->fixed, c->fixed_h.data(), Nn, cudaMemcpyHostToDevice));
+
+  // node buffers: m | p0 (D) | f (D) | vdt (D) | dv (D)
+  CUDA_TRY(cudaMalloc(&c->nodebuf, size_t(Nn) * (1 + 4 * D) * sizeof(double)));
+  CUDA_TRY(cudaMemset(c->nodebuf, 0, size_t(Nn) * (1 + 4 * D) * sizeof(double)));
+  c->nd.nodeCount = Nn;
+  c->nd.m = c->nodebuf;
+  c->nd.p0 = c->nodebuf + Nn;
+  c->nd.f = c->nodebuf + Nn * (1 + D);
+  c->nd.vdt = c->nodebuf + Nn * (1 + 2 * D);
+  c->nd.dv = c->nodebuf + Nn * (1 + 3 * D);
+  c->nd.fixed = c->fixed;
+  if (c->f32) {
+    CUDA_TRY(cudaMalloc(&c->nodebuf_f, size_t(Nn) * 2 * D * sizeof(float)));
+    CUDA_TRY(cudaMemset(c->nodebuf_f, 0, size_t(Nn) * 2 * D * sizeof(float)));
+    c->nd.vdt_f = c->nodebuf_f;
+    c->nd.dv_f = c->nodebuf_f + Nn * D;
+  }
+
+  // particles
+  int64_t maxn = 0;
+  for (int b = 0; b < nbodies; ++b) {
+    c->off.push_back(c->np);
+    c->cnt.push_back(bd[b].count);
+    c->np += bd[b].count;
+    maxn = bd[b].count > maxn ? bd[b].count : maxn;
+    const mpm_material_desc& m = bd[b].mat;
+    MatParams mp{};
+    mp.type = m.type;
+    mp.per_particle = bd[b].youngs != nullptr;
+    mp.lambda = m.E * m.nu / (1 + m.nu) / (1 - 2 * m.nu);  // Material.jl:54-55
+    mp.mu = m.E / 2 / (1 + m.nu);
+    mp.kappa = mp.lambda + mp.mu;  // Material.jl:161
+    mp.fy = m.fy;
+    mp.k1 = m.k1;
+    c->mats.push_back(mp);
+  }
+  size_t ptot = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1);
+  CUDA_TRY(cudaMalloc(&c->P, ptot * c->esz));
+  CUDA_TRY(cudaMemset(c->P, 0, ptot * c->esz));
+  c->staging_n = size_t(maxn > 0 ? maxn : 1) * 9;
+  CUDA_TRY(cudaMalloc(&c->staging, c->staging_n * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&c->status, sizeof(unsigned)));
+  CUDA_TRY(cudaMemset(c->status, 0, sizeof(unsigned)));
+  CUDA_TRY(cudaMalloc(&c->partial, size_t(kEnergyBlocks) * 5 * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&c->red, 8 * sizeof(double)));
+
+  const FieldIdx& fi = c->fi;
+  for (int b = 0; b < nbodies; ++b) {
+    const mpm_body_desc& d = bd[b];
+    int64_t n = d.count;
+    if (n == 0) continue;
+    int r;
+    if ((r = upload(c, b, d.pos, D, fi.X, ident(D)))) return r;
+    if ((r = upload(c, b, d.velocity, D, fi.V, ident(D)))) return r;
+    if ((r = upload(c, b, d.mass, 1, fi.M, ident(1)))) return r;
+    if ((r = upload(c, b, d.volume, 1, fi.VOL, ident(1)))) return r;
+    if ((r = upload(c, b, d.volume_initial, 1, fi.VOL0, ident(1)))) return r;
+    if (d.F) {
+      if ((r = upload(c, b, d.F, D * D, fi.F, ident(D * D)))) return r;
+    } else {
+      std::vector<double> I(size_t(n) * D * D, 0.0);
+      for (int64_t p = 0; p < n; ++p)
+        for (int a = 0; a < D; ++a) I[p * D * D + a * (D + 1)] = 1.0;
+      if ((r = upload(c, b, I.data(), D * D, fi.F, ident(D * D)))) return r;
+    }
+    if (d.strain && (r = upload(c, b, d.strain, D * D, fi.EPS, sym_from_full(D)))) return r;
+    if (d.stress && (r = upload(c, b, d.stress, D * D, fi.SIG, sym_from_full(D)))) return r;
+    if (d.alpha && (r = upload(c, b, d.alpha, 1, fi.ALPHA, ident(1)))) return r;
+    if (d.pstrain) {
+      if (D == 2) r = upload(c, b, d.pstrain, 3, fi.EP, ident(3));
+      else r = upload(c, b, d.pstrain, 9, fi.EP, sym_from_full(3));
+      if (r) return r;
+    }
+    if (d.youngs) {
+      std::vector<double> lm(size_t(n) * 2);
+      double nu = d.mat.nu;
+      for (int64_t p = 0; p < n; ++p) {
+        double E = d.youngs[p];
+        lm[2 * p] = E * nu / (1 + nu) / (1 - 2 * nu);
+        lm[2 * p + 1] = E / 2 / (1 + nu);
+      }
+      if ((r = upload(c, b, lm.data(), 2, fi.LAM, ident(2)))) return r;
+    }
+  }
+  return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_abi_version(void) { return JUMP_MPM_ABI_VERSION; }
+
+const char* mpm_last_error(void) { return g_err.c_str(); }
+
+int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t nbodies,
+               const mpm_params* params, mpm_ctx** out) {
+  if (!grid || !params || !out) return fail(MPM_ERR_ARG, "mpm_create: null argument");
+  *out = nullptr;
+  if (grid->dim != 2 && grid->dim != 3) return fail(MPM_ERR_ARG, "mpm_create: dim must be 2 or 3");
+  if (nbodies < 0 || (nbodies > 0 && !bodies)) return fail(MPM_ERR_ARG, "mpm_create: bad body list");
+  for (int a = 0; a < grid->dim; ++a) {
+    if (grid->nodes[a] < 2) return fail(MPM_ERR_ARG, "mpm_create: a grid axis needs at least 2 nodes");
+    if (!(grid->xmax[a] > grid->xmin[a])) return fail(MPM_ERR_ARG, "mpm_create: need xmax > xmin");
+    if (grid->nodes[a] > (int64_t(1) << 30)) return fail(MPM_ERR_ARG, "mpm_create: grid axis too large");
+  }
+  if (!(params->dt > 0.0) || !std::isfinite(params->dt)) return fail(MPM_ERR_ARG, "mpm_create: dt must be > 0");
+  if (params->precision != MPM_PREC_F64 && params->precision != MPM_PREC_F32)
+    return fail(MPM_ERR_ARG, "mpm_create: unknown precision");
+  if (params->contact) return fail(MPM_ERR_UNSUPPORTED, "mpm_create: multi-body contact is not built yet");
+  const int D = grid->dim;
+  for (int b = 0; b < nbodies; ++b) {
+    const mpm_body_desc& d = bodies[b];
+    if (d.count < 0) return fail(MPM_ERR_ARG, "mpm_create: negative particle count");
+    if (d.count > 0 && (!d.pos || !d.velocity || !d.mass || !d.volume || !d.volume_initial))
+      return fail(MPM_ERR_ARG, "mpm_create: pos, velocity, mass, volume and volume_initial are required");
+    if (d.mat.type != MPM_MAT_ELASTIC && d.mat.type != MPM_MAT_NEOHOOKEAN && d.mat.type != MPM_MAT_J2)
+      return fail(MPM_ERR_ARG, "mpm_create: unknown material type");
+    if (!symmetric(d.strain, d.count, D) || !symmetric(d.stress, d.count, D))
+      return fail(MPM_ERR_ARG, "mpm_create: strain and stress must be symmetric");
+    if (D == 3 && !symmetric(d.pstrain, d.count, 3))
+      return fail(MPM_ERR_ARG, "mpm_create: pstrain must be symmetric");
+  }
+  mpm_ctx* c = new mpm_ctx();
+  int r = create_impl(grid, bodies, nbodies, params, c);
+  if (r != MPM_OK) {
+    std::string msg = g_err;
+    destroy_ctx(c);
+    g_err = msg;
+    return r;
+  }
+  *out = c;
+  return MPM_OK;
+}
+
+int mpm_step(mpm_ctx* c, int64_t nsteps, double* t_inout) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_step: null context");
+  if (nsteps < 0) return fail(MPM_ERR_ARG, "mpm_step: nsteps < 0");
+  int r = build_step_graph(c);
+  if (r) return r;
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  CUDA_TRY(cudaEventRecord(c->e0, c->stream));
+  for (int64_t k = 0; k < nsteps; ++k) {
+    CUDA_TRY(cudaGraphLaunch(c->exec, c->stream));
+    if (t_inout) *t_inout += c->prm.dt;
+  }
+  CUDA_TRY(cudaEventRecord(c->e1, c->stream));
+  unsigned st = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  c->last_ms = ms;
+  return status_to_code(st);
+}
+
+int mpm_download(mpm_ctx* c, int32_t body, const mpm_body_view* v) {
+  if (!c || !v) return fail(MPM_ERR_ARG, "mpm_download: null argument");
+  if (body < 0 || body >= c->nb) return fail(MPM_ERR_ARG, "mpm_download: body index out of range");
+  const int D = c->dim;
+  const FieldIdx& fi = c->fi;
+  int r;
+  if ((r = download(c, body, v->pos, D, fi.X, ident(D)))) return r;
+  if ((r = download(c, body, v->velocity, D, fi.V, ident(D)))) return r;
+  if ((r = download(c, body, v->volume, 1, fi.VOL, ident(1)))) return r;
+  if ((r = download(c, body, v->F, D * D, fi.F, ident(D * D)))) return r;
+  if ((r = download(c, body, v->strain, D * D, fi.EPS, full_from_sym(D)))) return r;
+  if ((r = download(c, body, v->stress, D * D, fi.SIG, full_from_sym(D)))) return r;
+  if ((r = download(c, body, v->alpha, 1, fi.ALPHA, ident(1)))) return r;
+  if (D == 2) r = download(c, body, v->pstrain, 3, fi.EP, ident(3));
+  else r = download(c, body, v->pstrain, 9, fi.EP, full_from_sym(3));
+  if (r) return r;
+  if ((r = download(c, body, v->vmstr, 1, fi.VM, ident(1)))) return r;
+  return MPM_OK;
+}
+
+int mpm_download_grid(mpm_ctx* c, double* mass, double* momentum0, double* momentum, double* force) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_download_grid: null context");
+  const int D = c->dim;
+  const int64_t Nn = c->g.nodeCount;
+  std::vector<double> h(size_t(Nn) * (1 + 2 * D));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cudaMemcpy(h.data(), c->nodebuf, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  const double* m = h.data();
+  const double* p0 = m + Nn;
+  const double* f = p0 + Nn * D;
+  const double dt = c->prm.dt;
+  for (int64_t i = 0; i < Nn; ++i) {
+    if (mass) mass[i] = m[i];
+    for (int a = 0; a < D; ++a) {
+      double q0 = p0[a * Nn + i], fa = f[a * Nn + i];
+      double q = q0 + fa * dt;  // grid update (:430), then the Dirichlet mask (:433-441)
+      if (c->fixed_h[i] & (1u << a)) {
+        q0 = 0.0;
+        q = 0.0;
+      }
+      if (momentum0) momentum0[D * i + a] = q0;
+      if (momentum) momentum[D * i + a] = q;
+      if (force) force[D * i + a] = fa;
+    }
+  }
+  return MPM_OK;
+}
+
+int mpm_energies(mpm_ctx* c, double* ke, double* se, double* momentum) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_energies: null context");
+  const int D = c->dim;
+  double out[5] = {0, 0, 0, 0, 0};
+  if (c->np > 0) {
+    if (D == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, c->red);
+    else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, c->red);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, c->red, (2 + D) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  if (ke) *ke = out[0];
+  if (se) *se = out[1];
+  if (momentum)
+    for (int a = 0; a < D; ++a) momentum[a] = out[2 + a];
+  return MPM_OK;
+}
+
+// snapshot layout: 4 x int64 header (magic, dim, precision, particle count) + particle SoA
+static const int64_t kMagic = 0x4d504d4a554d5031LL;
+
+int mpm_save(mpm_ctx* c, void* buf, size_t* nbytes) {
+  if (!c || !nbytes) return fail(MPM_ERR_ARG, "mpm_save: null argument");
+  size_t body = size_t(c->NF) * size_t(c->np) * c->esz;
+  size_t need = 4 * sizeof(int64_t) + body;
+  if (!buf) {
+    *nbytes = need;
+    return MPM_OK;
+  }
+  if (*nbytes < need) return fail(MPM_ERR_ARG, "mpm_save: buffer too small");
+  int64_t hdr[4] = {kMagic, c->dim, c->f32 ? 1 : 0, c->np};
+  std::memcpy(buf, hdr, sizeof(hdr));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (body) CUDA_TRY(cudaMemcpy(static_cast<char*>(buf) + sizeof(hdr), c->P, body, cudaMemcpyDeviceToHost));
+  *nbytes = need;
+  return MPM_OK;
+}
+
+int mpm_load(mpm_ctx* c, const void* buf, size_t nbytes) {
+  if (!c || !buf) return fail(MPM_ERR_ARG, "mpm_load: null argument");
+  size_t body = size_t(c->NF) * size_t(c->np) * c->esz;
+  int64_t hdr[4];
+  if (nbytes != sizeof(hdr) + body) return fail(MPM_ERR_ARG, "mpm_load: size does not match this context");
+  std::memcpy(hdr, buf, sizeof(hdr));
+  if (hdr[0] != kMagic || hdr[1] != c->dim || hdr[2] != (c->f32 ? 1 : 0) || hdr[3] != c->np)
+    return fail(MPM_ERR_ARG, "mpm_load: snapshot belongs to a different configuration");
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (body) CUDA_TRY(cudaMemcpy(c->P, static_cast<const char*>(buf) + sizeof(hdr), body, cudaMemcpyHostToDevice));
+  return MPM_OK;
+}
+
+int mpm_last_step_ms(mpm_ctx* c, double* ms) {
+  if (!c || !ms) return fail(MPM_ERR_ARG, "mpm_last_step_ms: null argument");
+  *ms = c->last_ms;
+  return MPM_OK;
+}
+
+int mpm_profile_stages(mpm_ctx* c, int64_t nsteps, double* stage_ms) {
+  if (!c || !stage_ms || nsteps < 0) return fail(MPM_ERR_ARG, "mpm_profile_stages: bad argument");
+  cudaEvent_t ev[5];
+  for (int i = 0; i < 5; ++i) CUDA_TRY(cudaEventCreate(&ev[i]));
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  int rc = MPM_OK;
+  for (int64_t k = 0; k < nsteps && rc == MPM_OK; ++k) {
+    cudaEventRecord(ev[4], c->stream);
+    enqueue_step(c, ev);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+      rc = fail(MPM_ERR_CUDA, std::string("mpm_profile_stages: ") + cudaGetErrorString(e));
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[4], ev[0]);
+    stage_ms[MPM_STAGE_RESET] += ms;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    stage_ms[MPM_STAGE_P2G] += ms;
+    cudaEventElapsedTime(&ms, ev[1], ev[2]);
+    stage_ms[MPM_STAGE_GRID] += ms;
+    cudaEventElapsedTime(&ms, ev[2], ev[3]);
+    stage_ms[MPM_STAGE_G2P] += ms;
+  }
+  for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
+  if (rc != MPM_OK) return rc;
+  unsigned st = 0;
+  CUDA_TRY(cudaMemcpy(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  return status_to_code(st);
+}
+
+int mpm_destroy(mpm_ctx* c) {
+  if (c) {
+    cudaStreamSynchronize(c->stream);
+    destroy_ctx(c);
+  }
+  return MPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+// mpm_common.cuh -- device data layout and shared device helpers of the
+// GB300 explicit-MPM step (USL, linear hat basis).
+//
+// Particle state is one SoA allocation of NF fields x pitch elements
+// (field-major), in the particle precision R (double or float).  Bodies
+// occupy contiguous particle ranges.  Node state is FP64 SoA over a dense
+// grid (nodeCount = nx*ny*nz, node index i + nx*j + nx*ny*k, 0-based).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace jmpm {
+
+// status bits raised by kernels (atomicOr), mapped to MPM_ERR_* by the host
+enum : unsigned { ST_OUT_OF_GRID = 1u, ST_NEGATIVE_J = 2u, ST_NONFINITE = 4u };
+
+// Field indices of the particle SoA.  Symmetric tensors are stored as
+// 2D: (xx, yy, xy); 3D: (xx, yy, zz, xy, yz, xz).
+template <int D>
+struct Layout {
+  static constexpr int S = (D == 2) ? 3 : 6;   // symmetric tensor components
+  static constexpr int PS = (D == 2) ? 3 : 6;  // plastic strain components
+  static constexpr int X = 0;
+  static constexpr int V = D;
+  static constexpr int M = 2 * D;
+  static constexpr int VOL = 2 * D + 1;
+  static constexpr int VOL0 = 2 * D + 2;
+  static constexpr int F = 2 * D + 3;          // D*D, column-major
+  static constexpr int EPS = F + D * D;
+  static constexpr int SIG = EPS + S;
+  static constexpr int VM = SIG + S;
+  static constexpr int ALPHA = VM + 1;
+  static constexpr int EP = ALPHA + 1;
+  static constexpr int LAM = EP + PS;          // per-particle Lame constants (optional)
+  static constexpr int MU = LAM + 1;
+  static constexpr int NF = MU + 1;
+};
+
+// symmetric index (i, j) -> storage slot
+template <int D>
+__host__ __device__ constexpr int sym(int i, int j) {
+  if (i == j) return i;
+  if (D == 2) return 2;
+  int a = i < j ? i : j, b = i < j ? j : i;
+  return (a == 0 && b == 1) ? 3 : ((a == 1 && b == 2) ? 4 : 5);
+}
+
+struct MatParams {
+  int type;        // MPM_MAT_*
+  int per_particle;  // 1: use the LAM/MU particle fields
+  double lambda, mu, kappa, fy, k1;
+};
+
+// Grid description shared by all kernels.
+struct GridP {
+  double xmin[3];
+  double dxI[3];
+  int64_t nn[3];       // nodes per axis
+  int64_t nx, nxy, nodeCount;
+  const double* coord[3];  // node coordinate per axis (xmin + i*dx, Grid.jl:149-152)
+};
+
+// Node arrays (FP64).  Accumulators m, p0 (D), f (D); grid-update outputs
+// vdt = (p/m)*dt and dv = (p - p0)/m (D each, zero where m <= tolerance).
+struct NodeP {
+  double* m;
+  double* p0;   // D * nodeCount, component-major
+  double* f;
+  double* vdt;
+  double* dv;
+  float* vdt_f;  // FP32 copies for the FP32 particle path
+  float* dv_f;
+  const uint8_t* fixed;  // bit a set: dof a is fixed (grid.fixedNodes)
+  int64_t nodeCount;
+};
+
+struct PartP {
+  void* base;      // R*, NF * pitch
+  int64_t pitch;   // elements per field
+  int64_t begin;   // first particle of this launch
+  int64_t count;   // particles of this launch
+};
+
+__device__ __forceinline__ bool is_zero_bits(double x) {
+  return (__double_as_longlong(x) << 1) == 0;
+}
+__device__ __forceinline__ bool is_zero_bits(float x) {
+  return (__float_as_uint(x) << 1) == 0;
+}
+__device__ __forceinline__ bool is_neg_bits(double x) { return __double_as_longlong(x) < 0; }
+__device__ __forceinline__ bool is_neg_bits(float x) { return int(__float_as_uint(x)) < 0; }
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+__device__ __forceinline__ bool finite_bits(float x) {
+  return ((__float_as_uint(x) >> 23) & 0xff) != 0xff;
+}
+
+// -sign(delta) * dxI, selected with integer ops (Basis.jl:247-248, sign(0) = 0)
+template <class R>
+__device__ __forceinline__ R neg_sign_scale(R delta, R dxI) {
+  if (is_zero_bits(delta)) return R(0);
+  return is_neg_bits(delta) ? dxI : -dxI;
+}
+
+// exact-rounding helpers (no contraction) for the shape functions, so the
+// hat values are bit-identical to the reference's `1.0 - abs(x)*dxI`
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ int floor_to_int(double t) { return __double2int_rd(t); }
+__device__ __forceinline__ int floor_to_int(float t) { return __float2int_rd(t); }
+
+// Per-axis linear hat values and gradient factors of one particle.
+template <int D, class R>
+struct Hat {
+  int c[D];      // 0-based cell per axis
+  R Nl[D], Nh[D];  // hat value at the lower / upper node
+  R gl[D], gh[D];  // -sign(x - x_node) * dxI
+};
+
+// getAdjacentGridPoints + 1D factors of getShapeAndGradient
+// (Basis.jl:63-78, 104-137, 219-251, 292-332).  False if outside the grid.
+template <int D, class R>
+__device__ __forceinline__ bool hat(const GridP& g, const R* x, Hat<D, R>& h) {
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    R xmin = R(g.xmin[a]), dxI = R(g.dxI[a]);
+    R t = add_rn(mul_rn(sub_rn(x[a], xmin), dxI), R(1));
+    int i1 = floor_to_int(t);  // 1-based base node
+    if (i1 < 1 || i1 > int(g.nn[a] - 1)) return false;
+    int c = i1 - 1;
+    h.c[a] = c;
+    R xl = R(g.coord[a][c]), xh = R(g.coord[a][c + 1]);
+    R dl = sub_rn(x[a], xl), dh = sub_rn(x[a], xh);
+    h.Nl[a] = sub_rn(R(1), mul_rn(fabs(dl), dxI));
+    h.Nh[a] = sub_rn(R(1), mul_rn(fabs(dh), dxI));
+    h.gl[a] = neg_sign_scale(dl, dxI);
+    h.gh[a] = neg_sign_scale(dh, dxI);
+  }
+  return true;
+}
+
+// Corner k of the stencil in the reference's nearPoints order:
+// bit 0 -> +x, bit 1 -> +y, bit 2 -> +z.  N and grad N with the reference's
+// products: N = (Nx*Ny)*Nz, dN/dx = (Ny*Nz)*(-sign*dxI), ...
+template <int D, class R>
+struct Corners {
+  R N[1 << D];
+  R dN[1 << D][D];
+  int64_t node[1 << D];
+};
+
+template <int D, class R>
+__device__ __forceinline__ void corners(const GridP& g, const Hat<D, R>& h, Corners<D, R>& cr) {
+  int64_t base = int64_t(h.c[0]) + g.nx * int64_t(h.c[1]);
+  if (D == 3) base += g.nxy * int64_t(h.c[D == 3 ? 2 : 0]);
+  if (D == 2) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      int bx = k & 1, by = (k >> 1) & 1;
+      R Nx = bx ? h.Nh[0] : h.Nl[0];
+      R Ny = by ? h.Nh[1] : h.Nl[1];
+      R gx = bx ? h.gh[0] : h.gl[0];
+      R gy = by ? h.gh[1] : h.gl[1];
+      cr.N[k] = mul_rn(Nx, Ny);
+      cr.dN[k][0] = mul_rn(Ny, gx);
+      cr.dN[k][1] = mul_rn(Nx, gy);
+      cr.node[k] = base + bx + g.nx * by;
+    }
+  } else {
+    R NxNy[4], NyNz[4], NxNz[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int b0 = q & 1, b1 = (q >> 1) & 1;
+      NxNy[q] = mul_rn(b0 ? h.Nh[0] : h.Nl[0], b1 ? h.Nh[1] : h.Nl[1]);
+      NyNz[q] = mul_rn(b0 ? h.Nh[1] : h.Nl[1], b1 ? h.Nh[D - 1] : h.Nl[D - 1]);
+      NxNz[q] = mul_rn(b0 ? h.Nh[0] : h.Nl[0], b1 ? h.Nh[D - 1] : h.Nl[D - 1]);
+    }
+#pragma unroll
+    for (int k = 0; k < (1 << D); ++k) {
+      int bx = k & 1, by = (k >> 1) & 1, bz = (k >> 2) & 1;
+      R Nz = bz ? h.Nh[D - 1] : h.Nl[D - 1];
+      R gx = bx ? h.gh[0] : h.gl[0];
+      R gy = by ? h.gh[1] : h.gl[1];
+      R gz = bz ? h.gh[D - 1] : h.gl[D - 1];
+      R nxny = NxNy[bx + 2 * by];
+      cr.N[k] = mul_rn(nxny, Nz);
+      cr.dN[k][0] = mul_rn(NyNz[by + 2 * bz], gx);
+      cr.dN[k][1] = mul_rn(NxNz[bx + 2 * bz], gy);
+      cr.dN[k][D - 1] = mul_rn(nxny, gz);
+      cr.node[k] = base + bx + g.nx * by + g.nxy * bz;
+    }
+  }
+}
+
+}  // namespace jmpm

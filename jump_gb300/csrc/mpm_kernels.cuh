@@ -1,0 +1,461 @@
+// mpm_kernels.cuh -- kernels of one USL step (SolveExplicitSolidMechanics2D.jl:381-534,
+// 3D lifted the same way) for D = 2, 3 and particle precision R = double | float.
+//
+//   p2g        P2G: nodal mass, momentum and force (:391-423), FP64 atomics at L2
+//   grid       grid update + Dirichlet mask (:429-442), and the nodal velocities
+//              the G2P needs, computed once per node instead of per particle
+//   g2p        G2P + velocity gradient + F/J/volume + update_stress! (:485-533)
+//              fused in one per-particle pass
+//   energies   EnergiesFix sums (Fix.jl:248-270)
+#pragma once
+
+#include "mpm_common.cuh"
+#include "../../include/jump_mpm.h"
+
+namespace jmpm {
+
+template <class R>
+__device__ __forceinline__ R* field(const PartP& pp, int f, int64_t p) {
+  return static_cast<R*>(pp.base) + int64_t(f) * pp.pitch + p;
+}
+
+// ---------------------------------------------------------------------------
+// P2G
+template <int D, class R, bool GRAV>
+__global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
+                                                  double gz, unsigned* status) {
+  using L = Layout<D>;
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  int64_t p = pp.begin + t;
+  R x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
+  Hat<D, R> h;
+  if (!hat<D, R>(g, x, h)) {
+    atomicOr(status, ST_OUT_OF_GRID);
+    return;
+  }
+  Corners<D, R> cr;
+  corners<D, R>(g, h, cr);
+  R m = *field<R>(pp, L::M, p);
+  R V = *field<R>(pp, L::VOL, p);
+  R v[D], ms[L::S];
+#pragma unroll
+  for (int a = 0; a < D; ++a) v[a] = *field<R>(pp, L::V + a, p);
+#pragma unroll
+  for (int c = 0; c < L::S; ++c) ms[c] = -V * *field<R>(pp, L::SIG + c, p);  // -V sigma
+  R mg[3] = {R(0), R(0), R(0)};
+  if (GRAV) {
+    mg[0] = m * R(gx);
+    mg[1] = m * R(gy);
+    if (D == 3) mg[2] = m * R(gz);
+  }
+  const int64_t Nn = nd.nodeCount;
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) {
+    int64_t n = cr.node[k];
+    R N = cr.N[k];
+    R Nm = N * m;
+    atomicAdd(nd.m + n, double(Nm));
+#pragma unroll
+    for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, double(Nm * v[a]));
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      R fa = ms[sym<D>(a, 0)] * cr.dN[k][0];
+#pragma unroll
+      for (int j = 1; j < D; ++j) fa += ms[sym<D>(a, j)] * cr.dN[k][j];
+      if (GRAV) fa += mg[a] * N;
+      atomicAdd(nd.f + a * Nn + n, double(fa));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Grid update (:429-442) + nodal velocities for G2P.
+template <int D, bool F32COPY>
+__global__ void __launch_bounds__(256) grid_kernel(NodeP nd, double dt, double tol) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= nd.nodeCount) return;
+  const int64_t Nn = nd.nodeCount;
+  double m = nd.m[i];
+  if (!(m > tol)) {
+    // empty or near-empty node: G2P skips it (:510); no FP64 work here
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      nd.vdt[a * Nn + i] = 0.0;
+      nd.dv[a * Nn + i] = 0.0;
+      if (F32COPY) {
+        nd.vdt_f[a * Nn + i] = 0.f;
+        nd.dv_f[a * Nn + i] = 0.f;
+      }
+    }
+    return;
+  }
+  unsigned fx = nd.fixed[i];
+  double vdt[D], dv[D];
+  const bool live = true;
+  double invM = 1.0 / m;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    double p0 = nd.p0[a * Nn + i];
+    double p = __dadd_rn(p0, __dmul_rn(nd.f[a * Nn + i], dt));  // p = p0 + f*dt
+    if (fx & (1u << a)) {
+      p0 = 0.0;
+      p = 0.0;
+    }
+    vdt[a] = live ? (p * invM) * dt : 0.0;
+    dv[a] = live ? (p - p0) * invM : 0.0;
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    nd.vdt[a * Nn + i] = vdt[a];
+    nd.dv[a * Nn + i] = dv[a];
+    if (F32COPY) {
+      nd.vdt_f[a * Nn + i] = float(vdt[a]);
+      nd.dv_f[a * Nn + i] = float(dv[a]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Constitutive updates (update_stress!, Material.jl).  eps/sig symmetric storage.
+template <int D, class R>
+__device__ __forceinline__ void elastic(R lam, R mu, const R* eps, R* sig) {
+  // lambda*(tr eps)*I + 2.0*mu*eps   (Material.jl:68-72, 80)
+  R tr = (D == 2) ? eps[0] + eps[1] : (eps[0] + eps[1]) + eps[2];
+  R lt = lam * tr;
+  R tmu = R(2) * mu;
+#pragma unroll
+  for (int c = 0; c < Layout<D>::S; ++c) sig[c] = tmu * eps[c] + (c < D ? lt : R(0));
+}
+
+template <int D, class R>
+__device__ __forceinline__ void neohookean(R lam, R mu, const R* F, double J, R* sig) {
+  // (1/J)*( mu*(F*F' - I) + lambda*log(J)*I )   (Material.jl:119-122)
+  R ll = R(double(lam) * log(J));
+  R iJ = R(1.0 / J);
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      R s = F[i] * F[j];
+#pragma unroll
+      for (int k = 1; k < D; ++k) s += F[i + D * k] * F[j + D * k];
+      R v = (i == j) ? mu * (s - R(1)) + ll : mu * s;
+      sig[sym<D>(i, j)] = iJ * v;
+    }
+}
+
+template <class R>
+__device__ __forceinline__ R sqr(R a) {
+  return a * a;
+}
+
+// J2 radial return, 3D (Material.jl:228-275)
+template <class R>
+__device__ __forceinline__ void j2_3d(R lam, R mu, R kappa, R fy, R k1, const R* eps, R* sig,
+                                      R* alpha, R* ep, R* vm) {
+  (void)lam;
+  R tr = (eps[0] + eps[1]) + eps[2];
+  R tt = R(0.333333333) * tr;
+  R tmu = R(2) * mu;
+  R s[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) s[c] = tmu * ((c < 3 ? eps[c] - tt : eps[c]) - ep[c]);
+  // sqrt(s11^2 + s22^2 + s33^2 + 2.0*(s12^2 + s23^2 + s13^2))
+  R ns = sqrt(((sqr(s[0]) + sqr(s[1])) + sqr(s[2])) + R(2) * ((sqr(s[3]) + sqr(s[4])) + sqr(s[5])));
+  R kt = kappa * tr;
+  R a0 = *alpha;
+  R f_trial = ns - (k1 * a0 + fy);
+  R sg[6];
+  if (f_trial <= R(0)) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sg[c] = s[c] + (c < 3 ? kt : R(0));
+  } else {
+    R inv = R(1) / ns;
+    R lamp = ((ns - k1 * a0) - fy) / (tmu + k1);
+    a0 += lamp;
+    R cc = tmu * lamp;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      R nrm = inv * s[c];
+      ep[c] += lamp * nrm;
+      sg[c] = (s[c] + (c < 3 ? kt : R(0))) - cc * nrm;
+    }
+    *alpha = a0;
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) sig[c] = sg[c];
+  R ts = R(0.333333333) * ((sg[0] + sg[1]) + sg[2]);
+  R d0 = sg[0] - ts, d1 = sg[1] - ts, d2 = sg[2] - ts;
+  // sqrt(d11^2 + d22^2 + d33^2 + 2*(d12^2 + d13^2 + d23^2))
+  *vm = sqrt(((sqr(d0) + sqr(d1)) + sqr(d2)) + R(2) * ((sqr(sg[3]) + sqr(sg[5])) + sqr(sg[4])));
+}
+
+// J2 radial return, 2D Voigt [xx, yy, 2xy] (Material.jl:174-225)
+template <class R>
+__device__ __forceinline__ void j2_2d(R lam, R mu, R kappa, R fy, R k1, const R* eps, R* sig,
+                                      R* alpha, R* ep, R* vm) {
+  (void)lam;
+  R e0 = eps[0], e1 = eps[1], e2 = R(2) * eps[2];
+  // epsilon_dev = I_dev * epsilon, I_dev = [.5 -.5 0; -.5 .5 0; 0 0 1]
+  R ed0 = R(0.5) * e0 + R(-0.5) * e1;
+  R ed1 = R(-0.5) * e0 + R(0.5) * e1;
+  R ed2 = e2;
+  R tmu = R(2) * mu;
+  // s_trial = diag(1,1,.5) * 2mu*(ed - ep)
+  R s0 = tmu * (ed0 - ep[0]);
+  R s1 = tmu * (ed1 - ep[1]);
+  R s2 = R(0.5) * (tmu * (ed2 - ep[2]));
+  R ns = sqrt((sqr(s0) + sqr(s1)) + R(2) * sqr(s2));
+  R kt = kappa * (e0 + e1);
+  R a0 = *alpha;
+  R f_trial = ns - (k1 * a0 + fy);
+  R g0 = kt + s0, g1 = kt + s1, g2 = s2;
+  if (!(f_trial <= R(0))) {
+    R inv = R(1) / ns;
+    R n0 = inv * s0, n1 = inv * s1, n2 = inv * s2;
+    R lamp = ((ns - k1 * a0) - fy) / (tmu + k1);
+    a0 += lamp;
+    ep[0] += lamp * n0;
+    ep[1] += lamp * n1;
+    ep[2] += lamp * (R(2) * n2);  // Iinv = diag(1,1,2)
+    R cc = tmu * lamp;
+    g0 -= cc * n0;
+    g1 -= cc * n1;
+    g2 -= cc * n2;
+    *alpha = a0;
+  }
+  sig[0] = g0;
+  sig[1] = g1;
+  sig[2] = g2;
+  R d0 = R(0.5) * g0 + R(-0.5) * g1;
+  R d1 = R(-0.5) * g0 + R(0.5) * g1;
+  *vm = sqrt((sqr(d0) + sqr(d1)) + R(2) * sqr(g2));
+}
+
+template <int D>
+__device__ __forceinline__ double det_d(const double* A) {
+  if (D == 2) return A[0] * A[3] - A[2] * A[1];
+  const double* x0 = A;
+  const double* x1 = A + 3;
+  const double* x2 = A + 6;
+  double c0 = x1[1] * x2[2] - x1[2] * x2[1];
+  double c1 = x1[2] * x2[0] - x1[0] * x2[2];
+  double c2 = x1[0] * x2[1] - x1[1] * x2[0];
+  return (x0[0] * c0 + x0[1] * c1) + x0[2] * c2;
+}
+
+// ---------------------------------------------------------------------------
+// G2P + kinematics + stress, one thread per particle.
+template <int D, class R, int MAT>
+__global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, double dt,
+                                                  unsigned* status) {
+  using L = Layout<D>;
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  int64_t p = pp.begin + t;
+  R x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
+  Hat<D, R> h;
+  if (!hat<D, R>(g, x, h)) {
+    atomicOr(status, ST_OUT_OF_GRID);
+    return;
+  }
+  Corners<D, R> cr;
+  corners<D, R>(g, h, cr);
+  R v[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) v[a] = *field<R>(pp, L::V + a, p);
+  R Ldt[D][D];
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int j = 0; j < D; ++j) Ldt[a][j] = R(0);
+  const R* vdt_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.vdt) : reinterpret_cast<const R*>(nd.vdt_f);
+  const R* dv_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.dv) : reinterpret_cast<const R*>(nd.dv_f);
+  const int64_t Nn = nd.nodeCount;
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) {
+    int64_t n = cr.node[k];
+    R N = cr.N[k];
+    R vd[D], dvv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      vd[a] = __ldg(vdt_n + a * Nn + n);
+      dvv[a] = __ldg(dv_n + a * Nn + n);
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      v[a] += N * dvv[a];
+      x[a] += N * vd[a];
+#pragma unroll
+      for (int j = 0; j < D; ++j) Ldt[a][j] += vd[a] * cr.dN[k][j];
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    *field<R>(pp, L::X + a, p) = x[a];
+    *field<R>(pp, L::V + a, p) = v[a];
+  }
+  // F <- F (I + L dt)   (:523)
+  R F[D * D], Fn[D * D];
+#pragma unroll
+  for (int c = 0; c < D * D; ++c) F[c] = *field<R>(pp, L::F + c, p);
+#pragma unroll
+  for (int j = 0; j < D; ++j)
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      R s = F[i] * (Ldt[0][j] + (j == 0 ? R(1) : R(0)));
+#pragma unroll
+      for (int k = 1; k < D; ++k) s += F[i + D * k] * (Ldt[k][j] + (j == k ? R(1) : R(0)));
+      Fn[i + D * j] = s;
+    }
+  double Fd[D * D];
+#pragma unroll
+  for (int c = 0; c < D * D; ++c) {
+    Fd[c] = double(Fn[c]);
+    *field<R>(pp, L::F + c, p) = Fn[c];
+  }
+  double J = det_d<D>(Fd);  // det F in FP64 for both precisions
+  *field<R>(pp, L::VOL, p) = R(J * double(*field<R>(pp, L::VOL0, p)));
+  // strain += dt * 0.5*(L + L')
+  R eps[L::S];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      int c = sym<D>(i, j);
+      R e = *field<R>(pp, L::EPS + c, p);
+      e += (i == j) ? Ldt[i][i] : R(0.5) * (Ldt[i][j] + Ldt[j][i]);
+      eps[c] = e;
+      *field<R>(pp, L::EPS + c, p) = e;
+    }
+  R lam = R(mp.lambda), mu = R(mp.mu), kappa = R(mp.kappa);
+  if (mp.per_particle) {
+    lam = *field<R>(pp, L::LAM, p);
+    mu = *field<R>(pp, L::MU, p);
+    kappa = lam + mu;
+  }
+  R sig[L::S];
+  if (MAT == MPM_MAT_ELASTIC) {
+    if (D == 3) {
+      // vmStr of the incoming stress (Material.jl:78-79)
+      R so[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) so[c] = *field<R>(pp, L::SIG + c, p);
+      *field<R>(pp, L::VM, p) =
+          sqrt(((sqr(so[0]) + sqr(so[1])) + sqr(so[2])) + R(2) * ((sqr(so[3]) + sqr(so[5])) + sqr(so[4])));
+    }
+    elastic<D, R>(lam, mu, eps, sig);
+  } else if (MAT == MPM_MAT_NEOHOOKEAN) {
+    neohookean<D, R>(lam, mu, Fn, J, sig);
+  } else {
+    R alpha = *field<R>(pp, L::ALPHA, p);
+    R ep[L::PS];
+#pragma unroll
+    for (int c = 0; c < L::PS; ++c) ep[c] = *field<R>(pp, L::EP + c, p);
+    R vm;
+    if (D == 3)
+      j2_3d<R>(lam, mu, kappa, R(mp.fy), R(mp.k1), eps, sig, &alpha, ep, &vm);
+    else
+      j2_2d<R>(lam, mu, kappa, R(mp.fy), R(mp.k1), eps, sig, &alpha, ep, &vm);
+    *field<R>(pp, L::ALPHA, p) = alpha;
+#pragma unroll
+    for (int c = 0; c < L::PS; ++c) *field<R>(pp, L::EP + c, p) = ep[c];
+    *field<R>(pp, L::VM, p) = vm;
+  }
+  bool fin = true;
+#pragma unroll
+  for (int c = 0; c < L::S; ++c) {
+    *field<R>(pp, L::SIG + c, p) = sig[c];
+    fin &= finite_bits(sig[c]);
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) fin &= finite_bits(x[a]) & finite_bits(v[a]);
+  unsigned st = (J > 0.0 ? 0u : ST_NEGATIVE_J) | (fin ? 0u : ST_NONFINITE);
+  if (st) atomicOr(status, st);
+}
+
+// ---------------------------------------------------------------------------
+// EnergiesFix sums: per-block partials [KE, SE, P_0..P_{D-1}], then one block
+// folds the partials in a fixed order (deterministic).
+template <int D, class R>
+__global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial) {
+  using L = Layout<D>;
+  constexpr int NQ = 2 + D;
+  double q[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) q[k] = 0.0;
+  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < pp.count;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    int64_t p = pp.begin + t;
+    double m = *field<R>(pp, L::M, p);
+    double vv = 0.0;
+    double v[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      v[a] = *field<R>(pp, L::V + a, p);
+      vv += v[a] * v[a];
+    }
+    q[0] += 0.5 * m * vv;
+    double se = 0.0;
+#pragma unroll
+    for (int c = 0; c < L::S; ++c) {
+      double w = (c < D) ? 1.0 : 2.0;  // off-diagonal entries appear twice in sigma:eps
+      se += w * double(*field<R>(pp, L::SIG + c, p)) * double(*field<R>(pp, L::EPS + c, p));
+    }
+    q[1] += 0.5 * double(*field<R>(pp, L::VOL, p)) * se;
+#pragma unroll
+    for (int a = 0; a < D; ++a) q[2 + a] += m * v[a];
+  }
+  __shared__ double sh[NQ][256];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] = q[k];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) partial[int64_t(blockIdx.x) * NQ + k] = sh[k][0];
+}
+
+template <int NQ>
+__global__ void fold_kernel(const double* partial, int nblocks, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int k = 0; k < NQ; ++k) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partial[int64_t(b) * NQ + k];
+    out[k] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// AoS (host layout, FP64) <-> SoA (device fields, precision R).
+struct CompMap {
+  int n;          // components moved per particle
+  int src[9];     // AoS component for each SoA field (upload) / SoA field for each AoS entry
+};
+
+template <class R>
+__global__ void aos_to_soa_kernel(PartP pp, const double* src, int per, int f0, CompMap cm) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  for (int c = 0; c < cm.n; ++c)
+    *field<R>(pp, f0 + c, pp.begin + t) = R(src[t * per + cm.src[c]]);
+}
+
+template <class R>
+__global__ void soa_to_aos_kernel(PartP pp, double* dst, int per, int f0, CompMap cm) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  for (int c = 0; c < cm.n; ++c) dst[t * per + c] = double(*field<R>(pp, f0 + cm.src[c], pp.begin + t));
+}
+
+}  // namespace jmpm

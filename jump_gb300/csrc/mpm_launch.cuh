@@ -1,0 +1,90 @@
+// mpm_launch.cuh -- definitions of Launchers<D>; included once per dimension.
+#pragma once
+
+#include "mpm_internal.h"
+#include "mpm_kernels.cuh"
+
+namespace jmpm {
+
+static inline unsigned blocks_for(int64_t n, int threads) {
+  return unsigned((n + threads - 1) / threads);
+}
+
+static inline CompMap to_dev(const CompMapH& h) {
+  CompMap c;
+  c.n = h.n;
+  for (int i = 0; i < 9; ++i) c.src[i] = h.src[i];
+  return c;
+}
+
+template <int D>
+void Launchers<D>::p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
+                       const double* grav, unsigned* status) {
+  if (pp.count <= 0) return;
+  bool has_g = grav[0] != 0.0 || grav[1] != 0.0 || (D == 3 && grav[2] != 0.0);
+  unsigned nb = blocks_for(pp.count, 256);
+  if (f32) {
+    if (has_g) p2g_kernel<D, float, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+    else p2g_kernel<D, float, false><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+  } else {
+    if (has_g) p2g_kernel<D, double, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+    else p2g_kernel<D, double, false><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+  }
+}
+
+template <int D>
+void Launchers<D>::grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy) {
+  unsigned nb = blocks_for(nd.nodeCount, 256);
+  if (f32copy) grid_kernel<D, true><<<nb, 256, 0, s>>>(nd, dt, tol);
+  else grid_kernel<D, false><<<nb, 256, 0, s>>>(nd, dt, tol);
+}
+
+template <int D>
+void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
+                       const MatParams& mp, double dt, unsigned* status) {
+  if (pp.count <= 0) return;
+  unsigned nb = blocks_for(pp.count, 256);
+#define JMPM_G2P(R, M) g2p_kernel<D, R, M><<<nb, 256, 0, s>>>(g, nd, pp, mp, dt, status)
+  if (f32) {
+    switch (mp.type) {
+      case MPM_MAT_ELASTIC: JMPM_G2P(float, MPM_MAT_ELASTIC); break;
+      case MPM_MAT_NEOHOOKEAN: JMPM_G2P(float, MPM_MAT_NEOHOOKEAN); break;
+      default: JMPM_G2P(float, MPM_MAT_J2); break;
+    }
+  } else {
+    switch (mp.type) {
+      case MPM_MAT_ELASTIC: JMPM_G2P(double, MPM_MAT_ELASTIC); break;
+      case MPM_MAT_NEOHOOKEAN: JMPM_G2P(double, MPM_MAT_NEOHOOKEAN); break;
+      default: JMPM_G2P(double, MPM_MAT_J2); break;
+    }
+  }
+#undef JMPM_G2P
+}
+
+template <int D>
+void Launchers<D>::energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,
+                            double* out) {
+  if (f32) energies_kernel<D, float><<<nblocks, 256, 0, s>>>(pp, partial);
+  else energies_kernel<D, double><<<nblocks, 256, 0, s>>>(pp, partial);
+  fold_kernel<2 + D><<<1, 32, 0, s>>>(partial, nblocks, out);
+}
+
+template <int D>
+void Launchers<D>::aos_to_soa(cudaStream_t s, const PartP& pp, bool f32, const double* src, int per,
+                              int f0, const CompMapH& cm) {
+  if (pp.count <= 0) return;
+  unsigned nb = blocks_for(pp.count, 256);
+  if (f32) aos_to_soa_kernel<float><<<nb, 256, 0, s>>>(pp, src, per, f0, to_dev(cm));
+  else aos_to_soa_kernel<double><<<nb, 256, 0, s>>>(pp, src, per, f0, to_dev(cm));
+}
+
+template <int D>
+void Launchers<D>::soa_to_aos(cudaStream_t s, const PartP& pp, bool f32, double* dst, int per, int f0,
+                              const CompMapH& cm) {
+  if (pp.count <= 0) return;
+  unsigned nb = blocks_for(pp.count, 256);
+  if (f32) soa_to_aos_kernel<float><<<nb, 256, 0, s>>>(pp, dst, per, f0, to_dev(cm));
+  else soa_to_aos_kernel<double><<<nb, 256, 0, s>>>(pp, dst, per, f0, to_dev(cm));
+}
+
+}  // namespace jmpm

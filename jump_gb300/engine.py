@@ -1,0 +1,214 @@
+"""Context objects over the C ABI (include/jump_mpm.h).
+
+``build_descriptors`` turns the host mirror of jump's types (Grid2D/3D,
+Solid2D/3D, materials, USL, a constant body force) into the ABI's
+descriptors; ``MPMContext`` owns one device context of the CUDA library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from .algorithm import USL, ConstantBodyForce2D, ConstantBodyForce3D
+from .material import ElastoPlasticMaterial, RigidMaterial
+
+PRECISIONS = {"f64": _capi.MPM_PREC_F64, "f32": _capi.MPM_PREC_F32}
+
+
+def colmajor(a: np.ndarray) -> np.ndarray:
+    """(n, d, d) with a[p, i, j] = A_ij  ->  flat column-major per particle."""
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).transpose(0, 2, 1))
+
+
+def from_colmajor(flat: np.ndarray, n: int, d: int) -> np.ndarray:
+    return flat.reshape(n, d, d).transpose(0, 2, 1)
+
+
+class Descriptors:
+    """Descriptors plus the numpy arrays they point into (kept alive here)."""
+
+    def __init__(self, grid, solids, tolerance=0.0, body_force=None, dt=0.0, precision="f64",
+                 contact=False, friction=0.0, sort_interval=0):
+        d = grid.dim
+        self.dim = d
+        self._keep = []
+        g = _capi.GridDesc()
+        g.dim = d
+        g.xmin[0], g.xmin[1] = grid.xmin, grid.ymin
+        g.xmax[0], g.xmax[1] = grid.xmax, grid.ymax
+        g.nodes[0], g.nodes[1] = grid.nodeCountX, grid.nodeCountY
+        if d == 3:
+            g.xmin[2], g.xmax[2], g.nodes[2] = grid.zmin, grid.zmax, grid.nodeCountZ
+        else:
+            g.nodes[2] = 1
+        fixed = np.ascontiguousarray(np.asarray(grid.fixedNodes, dtype=np.int64).T)  # (Nn, d)
+        self._keep.append(fixed)
+        g.fixed_nodes = _capi.iptr(fixed)
+        self.grid = g
+        bodies = (_capi.BodyDesc * max(1, len(solids)))()
+        for s, sol in enumerate(solids):
+            if isinstance(sol.mat, RigidMaterial) or getattr(sol, "rigid", False):
+                raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED,
+                                     "rigid solids are not supported by the accelerated USL path")
+            b = bodies[s]
+            b.count = sol.parCount
+            m = sol.mat
+            b.mat.type = m.kind
+            b.mat.E, b.mat.nu, b.mat.density = m.E, m.nu, m.density
+            b.mat.fy, b.mat.k1 = getattr(m, "fy", 0.0), getattr(m, "k1", 0.0)
+            arrs = {
+                "pos": np.ascontiguousarray(sol.pos, dtype=np.float64),
+                "velocity": np.ascontiguousarray(sol.velocity, dtype=np.float64),
+                "mass": np.ascontiguousarray(sol.mass, dtype=np.float64),
+                "volume": np.ascontiguousarray(sol.volume, dtype=np.float64),
+                "volume_initial": np.ascontiguousarray(sol.volumeInitial, dtype=np.float64),
+                "F": colmajor(sol.deformationGradient),
+                "strain": colmajor(sol.strain),
+                "stress": colmajor(sol.stress),
+            }
+            if isinstance(m, ElastoPlasticMaterial):
+                arrs["alpha"] = np.ascontiguousarray(m.alpha[: sol.parCount], dtype=np.float64)
+                if d == 2:
+                    arrs["pstrain"] = np.ascontiguousarray(m.pstrain[: sol.parCount], dtype=np.float64)
+                else:
+                    arrs["pstrain"] = colmajor(m.pstrain_3D[: sol.parCount])
+            if getattr(sol, "youngs", None) is not None:
+                arrs["youngs"] = np.ascontiguousarray(sol.youngs, dtype=np.float64)
+            for k, v in arrs.items():
+                self._keep.append(v)
+                setattr(b, k, _capi.dptr(v))
+        self.bodies = bodies
+        self.nbodies = len(solids)
+        p = _capi.Params()
+        p.dt = float(dt)
+        p.tolerance = float(tolerance)
+        bf = np.zeros(3)
+        if body_force is not None:
+            g_ = np.asarray(getattr(body_force, "g", body_force), dtype=np.float64).ravel()
+            bf[: g_.size] = g_
+        p.body_force[0], p.body_force[1], p.body_force[2] = bf
+        p.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        p.contact = 1 if contact else 0
+        p.friction = float(friction)
+        p.sort_interval = int(sort_interval)
+        p.flags = 0
+        self.params = p
+
+
+class BodyState:
+    """Host arrays one body downloads into (the reference layouts)."""
+
+    def __init__(self, n: int, d: int):
+        self.n, self.d = n, d
+        self.pos = np.zeros((n, d))
+        self.velocity = np.zeros((n, d))
+        self.volume = np.zeros(n)
+        self.F = np.zeros(n * d * d)
+        self.strain = np.zeros(n * d * d)
+        self.stress = np.zeros(n * d * d)
+        self.alpha = np.zeros(n)
+        self.pstrain = np.zeros(n * (3 if d == 2 else 9))
+        self.vmstr = np.zeros(n)
+
+    def view(self) -> _capi.BodyView:
+        v = _capi.BodyView()
+        for k in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr"):
+            setattr(v, k, _capi.dptr(getattr(self, k)))
+        return v
+
+    def matrices(self):
+        n, d = self.n, self.d
+        return (from_colmajor(self.F, n, d), from_colmajor(self.strain, n, d),
+                from_colmajor(self.stress, n, d))
+
+
+class _ContextBase:
+    """Shared driver logic for the CUDA context and the CPU oracle."""
+
+    def __init__(self, desc: Descriptors):
+        self.desc = desc
+        self.dim = desc.dim
+        self.counts = [desc.bodies[s].count for s in range(desc.nbodies)]
+
+    def download_body(self, s: int) -> BodyState:
+        st = BodyState(self.counts[s], self.dim)
+        self._download(s, st.view())
+        return st
+
+    def download_all(self):
+        return [self.download_body(s) for s in range(len(self.counts))]
+
+
+class MPMContext(_ContextBase):
+    """One device context of libjumpmpm.so."""
+
+    def __init__(self, desc: Descriptors):
+        super().__init__(desc)
+        self.L = _capi.lib()
+        h = C.c_void_p()
+        _capi.check(self.L.mpm_create(C.byref(desc.grid), desc.bodies, desc.nbodies,
+                                      C.byref(desc.params), C.byref(h)), self.L)
+        self.h = h
+
+    def step(self, nsteps: int, t: float | None = None, check: bool = True):
+        tt = C.c_double(0.0 if t is None else t)
+        rc = self.L.mpm_step(self.h, int(nsteps), C.byref(tt))
+        if check:
+            _capi.check(rc, self.L)
+        return tt.value if t is not None else rc
+
+    def _download(self, s, view):
+        _capi.check(self.L.mpm_download(self.h, int(s), C.byref(view)), self.L)
+
+    def download_grid(self, nn: int):
+        d = self.dim
+        m, p0, p, f = np.zeros(nn), np.zeros((nn, d)), np.zeros((nn, d)), np.zeros((nn, d))
+        _capi.check(self.L.mpm_download_grid(self.h, _capi.dptr(m), _capi.dptr(p0), _capi.dptr(p),
+                                             _capi.dptr(f)), self.L)
+        return m, p0, p, f
+
+    def energies(self):
+        ke, se = C.c_double(), C.c_double()
+        mom = np.zeros(3)
+        _capi.check(self.L.mpm_energies(self.h, C.byref(ke), C.byref(se), _capi.dptr(mom)), self.L)
+        return ke.value, se.value, mom[: self.dim]
+
+    def save(self) -> bytes:
+        n = C.c_size_t(0)
+        _capi.check(self.L.mpm_save(self.h, None, C.byref(n)), self.L)
+        buf = C.create_string_buffer(n.value)
+        _capi.check(self.L.mpm_save(self.h, buf, C.byref(n)), self.L)
+        return buf.raw
+
+    def load(self, data: bytes):
+        _capi.check(self.L.mpm_load(self.h, data, len(data)), self.L)
+
+    def last_step_ms(self) -> float:
+        ms = C.c_double()
+        _capi.check(self.L.mpm_last_step_ms(self.h, C.byref(ms)), self.L)
+        return ms.value
+
+    def profile_stages(self, nsteps: int) -> dict:
+        """Device ms per stage summed over nsteps steps (individual launches, CUDA events)."""
+        out = np.zeros(len(_capi.STAGES))
+        _capi.check(self.L.mpm_profile_stages(self.h, int(nsteps), _capi.dptr(out)), self.L)
+        return dict(zip(_capi.STAGES, out.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mpm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

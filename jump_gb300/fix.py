@@ -1,0 +1,110 @@
+"""Fixes: per-interval recorders called by the solver (Fix.jl:29-357).
+
+``compute(fix, t)`` and ``closeFile(fix)`` keep the reference semantics and
+text formats.  EnergiesFix can also be fed device-reduced sums
+(``record``), which lets the solver skip a full particle download when no
+other hook needs the particle arrays.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+
+class FixBase:
+    needs_particles = True
+
+    def close(self):
+        f = getattr(self, "file", None)
+        if f is not None and not f.closed:
+            f.close()
+
+
+class EmptyFix(FixBase):
+    """Fix.jl:34-35, 208-212: does nothing."""
+    needs_particles = False
+
+    def compute(self, time):
+        pass
+
+
+def _open_fresh(filename):
+    if os.path.isfile(filename):
+        os.remove(filename)
+    d = os.path.dirname(filename)
+    if d:
+        os.makedirs(d, exist_ok=True)
+    return open(filename, "a")
+
+
+class EnergiesFix(FixBase):
+    """KE = sum 1/2 m v.v and SE = sum 1/2 V sum(sigma .* eps), one line per call
+    (Fix.jl:104-117, 248-270)."""
+    needs_particles = False
+
+    def __init__(self, solids, filename):
+        self.solids = solids
+        self.file = _open_fresh(filename)
+        self.kinEnergy, self.strEnergy, self.recordTime = [], [], []
+
+    def compute(self, time):
+        KE = 0.0
+        SE = 0.0
+        for solid in self.solids:
+            v = solid.velocity
+            KE += float(np.sum(0.5 * solid.mass * np.einsum("pi,pi->p", v, v)))
+            SE += float(np.sum(0.5 * solid.volume * np.einsum("pij,pij->p", solid.stress, solid.strain)))
+        self.record(time, KE, SE)
+
+    def record(self, time, KE, SE):
+        self.kinEnergy.append(KE)
+        self.strEnergy.append(SE)
+        self.recordTime.append(time)
+        self.file.write(f"{time} {KE} {SE}\n")
+
+
+class DisplacementFix(FixBase):
+    """Position minus initial position of the particle found at ``point``
+    (Fix.jl:37-102, 214-218)."""
+
+    def __init__(self, solids, point, dir):
+        point = np.asarray(point, dtype=np.float64)
+        self.solids = solids
+        self.index = None
+        for s, solid in enumerate(solids):
+            dist = np.sqrt(np.sum((solid.pos - point[None, :]) ** 2, axis=1))
+            hit = np.nonzero(dist < 1e-10)[0]
+            if hit.size:
+                self.index = (s, int(hit[0]))
+                break
+        if self.index is None:
+            raise ValueError("No particle with that position found\n")
+        self.file = _open_fresh(os.path.join(dir, "recorded-position.txt"))
+
+    def compute(self, time):
+        s, p = self.index
+        solid = self.solids[s]
+        x = solid.pos[p] - solid.pos0[p]
+        self.file.write(f"{time} {x[0]} {x[1]}\n")
+
+
+def compute(fixes, time):
+    """compute(fix, t) on one fix or a list of fixes."""
+    if isinstance(fixes, FixBase):
+        fixes.compute(time)
+        return
+    for f in fixes:
+        f.compute(time)
+
+
+def closeFile(fixes):
+    if isinstance(fixes, FixBase):
+        fixes.close()
+        return
+    for f in fixes:
+        f.close()
+
+
+def as_list(fixes):
+    return [fixes] if isinstance(fixes, FixBase) else list(fixes)

@@ -1,0 +1,89 @@
+"""Material types of jump's explicit step (Material.jl:29-172), host side.
+
+Only the parameters and per-particle state live here; the constitutive
+updates themselves (update_stress!, Material.jl:68-275) run in the fused
+grid-to-particle kernel.  ``lambda`` is a Python keyword, so the Lame
+constant is stored as ``lambda_`` and also reachable as ``getattr(m, "lambda")``.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _capi
+
+
+class MaterialType:
+    kind = None
+    density = 0.0
+
+    def __getattr__(self, name):
+        if name == "lambda":
+            return self.lambda_
+        raise AttributeError(name)
+
+
+def _lame(E, nu):
+    lam = E * nu / (1 + nu) / (1 - 2 * nu)  # Material.jl:54
+    mu = E / 2 / (1 + nu)  # Material.jl:55
+    return lam, mu
+
+
+class RigidMaterial(MaterialType):
+    """RigidMaterial(density), Material.jl:29-31 (not supported by the solver)."""
+
+    def __init__(self, density):
+        self.density = float(density)
+
+
+class ElasticMaterial(MaterialType):
+    """ElasticMaterial(E,nu,density,Gf,l,parCount) or ElasticMaterial(E,nu,rho,parCount),
+    Material.jl:37-64."""
+    kind = _capi.MPM_MAT_ELASTIC
+
+    def __init__(self, E, nu, density, *rest):
+        if len(rest) == 3:
+            Gf, l0, parCount = rest
+        elif len(rest) == 1:
+            Gf, l0, parCount = 0.0, 0.0, rest[0]
+        else:
+            raise TypeError("ElasticMaterial(E,nu,density,Gf,l,parCount) or (E,nu,rho,parCount)")
+        self.E, self.nu, self.density = float(E), float(nu), float(density)
+        self.lambda_, self.mu = _lame(self.E, self.nu)
+        self.Gf, self.l0 = float(Gf), float(l0)
+        self.fac = 0.5 / self.E
+        self.vmStr = np.zeros(int(parCount))
+        self.dam = np.zeros(int(parCount))
+        self.c_dil = math.sqrt((self.lambda_ + 2 * self.mu) / self.density)
+        self.fy = 0.0
+        self.k1 = 0.0
+
+
+class NeoHookeanMaterial(MaterialType):
+    """NeoHookeanMaterial(E,nu,density,parCount), Material.jl:100-117."""
+    kind = _capi.MPM_MAT_NEOHOOKEAN
+
+    def __init__(self, E, nu, density, parCount):
+        self.E, self.nu, self.density = float(E), float(nu), float(density)
+        self.lambda_, self.mu = _lame(self.E, self.nu)
+        self.vmStr = np.zeros(int(parCount))
+        self.fy = 0.0
+        self.k1 = 0.0
+
+
+class ElastoPlasticMaterial(MaterialType):
+    """J2 plasticity with linear hardening, ElastoPlasticMaterial(E,nu,density,fy,k1,parCount),
+    Material.jl:128-171.  State per particle: alpha, pstrain (2D Voigt) and pstrain_3D."""
+    kind = _capi.MPM_MAT_J2
+
+    def __init__(self, E, nu, density, fy, k1, parCount):
+        self.E, self.nu, self.density = float(E), float(nu), float(density)
+        self.lambda_, self.mu = _lame(self.E, self.nu)
+        self.kappa = self.lambda_ + self.mu  # Material.jl:161 (kept as in the reference)
+        self.fy, self.k1 = float(fy), float(k1)
+        n = int(parCount)
+        self.pstrain = np.zeros((n, 3))
+        self.alpha = np.zeros(n)
+        self.vmStr = np.zeros(n)
+        self.pstrain_3D = np.zeros((n, 3, 3))

@@ -1,0 +1,125 @@
+"""solve_explicit_dynamics_2D / 3D for USL + LinearBasis: the drop-in for
+Problem.solve_explicit_dynamics_2D (SolveExplicitSolidMechanics2D.jl:335-585)
+and solve_explicit_dynamics_3D (SolveExplicitSolidMechanics3D.jl:230-378).
+
+The time loop, the hook schedule and the in-place mutation of ``solids`` and
+``grid`` follow the reference; the step itself runs in libjumpmpm.so.
+Steps between two hooks run on the device without host round trips.  Before
+each hook the particle arrays are downloaded into ``solids`` (skipped when
+the only hooks are EmptyFix/EnergiesFix and a non-writing output, in which case
+the energies are reduced on the device).  The per-step ``@printf`` of the 2D
+reference (:375) is not reproduced.
+
+Extra ``data`` keys (all optional): "precision" ("f64" | "f32"),
+"contact" (bool) with "friction" (float), "sort_interval" (int).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _capi
+from .algorithm import USL, LinearBasis
+from .dirichlet import fix_Dirichlet_grid
+from .engine import Descriptors, MPMContext
+from .fix import EnergiesFix, as_list, closeFile
+from .material import ElastoPlasticMaterial, ElasticMaterial
+
+
+def step_times(t: float, Tf: float, dt: float):
+    """The `t` of every iteration of `while t < Tf ... t += dtime` (:373, :580)."""
+    ts = []
+    while t < Tf:
+        ts.append(t)
+        t += dt
+    return ts
+
+
+def write_back(solids, states):
+    """Copy downloaded body states into the Solid objects (in place, like the reference)."""
+    for solid, st in zip(solids, states):
+        F, eps, sig = st.matrices()
+        solid.pos[:] = st.pos
+        solid.velocity[:] = st.velocity
+        solid.volume[:] = st.volume
+        solid.deformationGradient[:] = F
+        solid.strain[:] = eps
+        solid.stress[:] = sig
+        m = solid.mat
+        n = solid.parCount
+        if isinstance(m, ElastoPlasticMaterial):
+            m.alpha[:n] = st.alpha
+            if solid.dim == 2:
+                m.pstrain[:n] = st.pstrain.reshape(n, 3)
+            else:
+                m.pstrain_3D[:n] = st.pstrain.reshape(n, 3, 3).transpose(0, 2, 1)
+            m.vmStr[:n] = st.vmstr
+        elif isinstance(m, ElasticMaterial) and solid.dim == 3:
+            m.vmStr[:n] = st.vmstr
+
+
+def _solve(dim, grid, solids, basis, alg, output, fixes, data):
+    if not isinstance(basis, LinearBasis):
+        raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED, "the accelerated path supports LinearBasis only")
+    if not isinstance(alg, USL):
+        raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED, "the accelerated path supports USL only")
+    if grid.dim != dim or any(s.dim != dim for s in solids):
+        raise ValueError(f"solve_explicit_dynamics_{dim}D needs a Grid{dim}D and Solid{dim}D objects")
+    Tf = float(data["total_time"])
+    dt = float(data["dt"])
+    t = float(data["time"])
+    bodyforce = data["bodyforce"] if dim == 2 else data.get("bodyforce")
+    ghostcell = "ghostcell" in data
+    fix_Dirichlet_grid(grid, data, ghostcell=ghostcell)
+
+    desc = Descriptors(grid, solids, tolerance=alg.tolerance, body_force=bodyforce, dt=dt,
+                       precision=data.get("precision", "f64"), contact=bool(data.get("contact", False)),
+                       friction=float(data.get("friction", 0.0)),
+                       sort_interval=int(data.get("sort_interval", 0)))
+    fl = as_list(fixes)
+    need_particles = output.needs_particles or any(f.needs_particles for f in fl)
+    times = step_times(t, Tf, dt)
+    interval = max(1, int(output.interval))
+    lims = list(grid.lengths)
+    ncells = [grid.nodeCountX, grid.nodeCountY] + ([grid.nodeCountZ] if dim == 3 else [])
+    ctx = MPMContext(desc)
+    try:
+        done = 0
+        nsteps = len(times)
+        while done < nsteps:
+            # next hook step: the first counter >= done with counter % interval == 0
+            nxt = ((done + interval - 1) // interval) * interval
+            run = min(nsteps, nxt + 1) - done
+            ctx.step(run)
+            done += run
+            counter = done - 1
+            if counter % interval == 0:
+                th = times[counter]
+                if need_particles:
+                    write_back(solids, ctx.download_all())
+                    output.plot(solids, lims, ncells, counter)
+                    for f in fl:
+                        f.compute(th)
+                else:
+                    ke, se, _ = ctx.energies()
+                    for f in fl:
+                        if isinstance(f, EnergiesFix):
+                            f.record(th, ke, se)
+        write_back(solids, ctx.download_all())
+        m, p0, p, f = ctx.download_grid(grid.nodeCount)
+        grid.mass[:] = m
+        grid.momentum0[:] = p0
+        grid.momentum[:] = p
+        grid.force[:] = f
+    finally:
+        ctx.close()
+    closeFile(fixes)
+
+
+def solve_explicit_dynamics_2D(grid, solids, basis, alg, output, fixes, data):
+    """USL explicit dynamics on a Grid2D (SolveExplicitSolidMechanics2D.jl:335)."""
+    return _solve(2, grid, solids, basis, alg, output, fixes, data)
+
+
+def solve_explicit_dynamics_3D(grid, solids, basis, alg, output, fixes, data):
+    """USL explicit dynamics on a Grid3D (SolveExplicitSolidMechanics3D.jl:230)."""
+    return _solve(3, grid, solids, basis, alg, output, fixes, data)

@@ -1,0 +1,46 @@
+"""Run a workload for a few USL steps, for profiling the step kernels.
+
+  python -m jump_gb300.profile_step [--workload taylor_bar] [--precision f64]
+                                    [--warmup 2] [--steps 2] [--h 2.5e-4]
+
+Launch order per step: p2g_kernel, grid_kernel, g2p_kernel (one each per body),
+after the aos_to_soa upload launches of context creation.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+from . import scenarios
+from .engine import Descriptors, MPMContext
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="taylor_bar", choices=["taylor_bar", "two_disks", "cantilever"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--h", type=float, default=2.5e-4)
+    a = ap.parse_args()
+    if a.workload == "taylor_bar":
+        g, s, alg, data = scenarios.taylor_bar(h=a.h)
+    elif a.workload == "two_disks":
+        g, s, alg, data = scenarios.two_disks()
+    else:
+        g, s, alg, data = scenarios.cantilever()
+    scenarios.apply_dirichlet(g, data)
+    ctx = MPMContext(Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"),
+                                 dt=data["dt"], precision=a.precision))
+    ctx.step(a.warmup)
+    t0 = time.perf_counter()
+    ctx.step(a.steps)
+    dt = time.perf_counter() - t0
+    n = sum(x.parCount for x in s)
+    print(f"{a.workload} {a.precision}: {n} particles, {a.steps} steps, {1e3 * dt / max(a.steps, 1):.3f} ms/step, "
+          f"device {ctx.last_step_ms() / max(a.steps, 1):.3f} ms/step")
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

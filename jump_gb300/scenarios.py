@@ -1,0 +1,134 @@
+"""Problem set-ups of the benchmark workloads, written like jump's driver
+scripts (Main_TwoDisks.jl:40-116, Main_TaylorBar.jl, Main_VibratingBeam.jl)
+on the mirrored types.  Each returns (grid, solids, alg, data); inputs are
+synthetic, generated from the stated geometry with seeded randomness.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .algorithm import USL, ConstantBodyForce2D, ConstantBodyForce3D
+from .dirichlet import fix_Dirichlet_grid
+from .grid import Grid2D, Grid3D
+from .material import ElasticMaterial, ElastoPlasticMaterial, NeoHookeanMaterial
+from .solid import (Solid2D, Solid3D, assign_velocity, buildParticleForCircle,
+                    buildParticleForCylinder, buildParticleForRectangle)
+
+
+def _scale(solid, off, d):
+    vol = off ** d
+    solid.mass *= vol  # solid.mass .*= dx*dx  (Main_TwoDisks.jl:69-71)
+    solid.volume[:] = vol
+    solid.volumeInitial[:] = vol
+
+
+def two_disks(nodes: int = 21, ppc: int = 2, radius: float = 0.2, speed: float = 0.1,
+              E: float = 1000.0, nu: float = 0.3, rho: float = 1000.0, dt: float = 1e-3,
+              total_time: float = 3.0, fixed_boundary: bool = True, material: str = "elastic",
+              centers=((0.2, 0.2), (0.8, 0.8))):
+    """Two elastic disks colliding on [0,1]^2 (Main_TwoDisks.jl:40-116, linear basis)."""
+    grid = Grid2D(0.0, 1.0, 0.0, 1.0, nodes, nodes)
+    off = grid.dx / ppc
+    c1 = buildParticleForCircle(list(centers[0]), radius, off)
+    c2 = buildParticleForCircle(list(centers[1]), radius, off)
+    if material == "elastic":
+        mat = ElasticMaterial(E, nu, rho, 0, 0, len(c1))
+        mats = (mat, mat)
+    elif material == "neohookean":
+        mats = (NeoHookeanMaterial(E, nu, rho, len(c1)), NeoHookeanMaterial(E, nu, rho, len(c2)))
+    else:
+        mats = (ElastoPlasticMaterial(E, nu, rho, 1.0, 10.0, len(c1)),
+                ElastoPlasticMaterial(E, nu, rho, 1.0, 10.0, len(c2)))
+    s1, s2 = Solid2D(c1, mats[0]), Solid2D(c2, mats[1])
+    for s in (s1, s2):
+        _scale(s, off, 2)
+    assign_velocity(s1, [speed, speed])
+    assign_velocity(s2, [-speed, -speed])
+    data = {"total_time": total_time, "dt": dt, "time": 0.0,
+            "bodyforce": ConstantBodyForce2D([0.0, 0.0])}
+    if fixed_boundary:
+        data["dirichlet_grid"] = [("bottom", (1, 1)), ("top", (1, 1)), ("left", (1, 1)), ("right", (1, 1))]
+    return grid, [s1, s2], USL(1e-9), data
+
+
+def taylor_bar(h: float = 2.5e-4, ppc: int = 2, radius: float = 3.2e-3, length: float = 32.4e-3,
+               width: float = 16e-3, height: float = 40e-3, gap: float = 0.0, speed: float = 190.0,
+               E: float = 117e9, nu: float = 0.35, rho: float = 8930.0, fy: float = 400e6,
+               k1: float = 100e6, cfl: float = 0.2):
+    """Copper Taylor bar along z striking a rigid wall at z = 0 (J2, linear hardening).
+
+    Grid cells of size h over width x width x height, a cylinder of the given
+    radius and length built with buildParticleForCylinder (Solid.jl:447-465,
+    half-length argument) at ppc particles per cell and axis, the z = 0 face
+    fixed in z (the wall), dt = cfl*h/c with c the dilatational wave speed.
+    """
+    nx = int(round(width / h)) + 1
+    nz = int(round(height / h)) + 1
+    grid = Grid3D(0.0, width, 0.0, width, 0.0, height, nx, nx, nz)
+    off = h / ppc
+    center = [0.5 * width, 0.5 * width, gap + 0.5 * length]
+    coords = buildParticleForCylinder(center, radius, 0.5 * length, off, off, axis=2)
+    mat = ElastoPlasticMaterial(E, nu, rho, fy, k1, len(coords))
+    s = Solid3D(coords, mat)
+    _scale(s, off, 3)
+    assign_velocity(s, [0.0, 0.0, -speed])
+    c = math.sqrt((mat.lambda_ + 2 * mat.mu) / rho)
+    dt = cfl * h / c
+    data = {"total_time": 80e-6, "dt": dt, "time": 0.0,
+            "bodyforce": ConstantBodyForce3D([0.0, 0.0, 0.0]),
+            "dirichlet_grid": [("front", (0, 0, 1))]}
+    # Nodal-mass cutoff of 1e-3 particle masses: with USL(0.) near-empty nodes at
+    # the mushrooming impact face give runaway velocities after ~110 steps.
+    return grid, [s], USL(1e-3 * float(s.mass[0])), data
+
+
+def cantilever(h: float = 0.0625, ppc: int = 4, length: float = 4.0, depth: float = 1.0,
+               E_range=(0.5e6, 2e6), nu: float = 0.3, rho: float = 1050.0, g: float = -10.0,
+               dt: float = 1e-4, seed: int = 0):
+    """A 4 m x 1 m neo-Hookean beam clamped at x = 0 under gravity, with a
+    per-particle Young's modulus drawn log-uniform in E_range (seeded)."""
+    nx = int(round(4.5 / h)) + 1
+    ny = int(round(4.0 / h)) + 1
+    grid = Grid2D(0.0, 4.5, 0.0, 4.0, nx, ny)
+    off = h / ppc
+    coords = buildParticleForRectangle([0.5 * length, 2.5], length, depth, off)
+    mat = NeoHookeanMaterial(math.sqrt(E_range[0] * E_range[1]), nu, rho, len(coords))
+    s = Solid2D(coords, mat)
+    _scale(s, off, 2)
+    rng = np.random.default_rng(seed)
+    s.youngs = np.exp(rng.uniform(math.log(E_range[0]), math.log(E_range[1]), len(coords)))
+    data = {"total_time": 2000 * dt, "dt": dt, "time": 0.0,
+            "bodyforce": ConstantBodyForce2D([0.0, g]),
+            "dirichlet_grid": [("left", (1, 1))]}
+    return grid, [s], USL(1e-9), data
+
+
+def ensemble_member(i: int, seed: int = 0):
+    """Instance i of the seeded two-disk ensemble: radii in [0.1, 0.25],
+    20..80 cells per axis, 4 particles per cell, E in [500, 5000], speed in
+    [0.05, 0.2], dt = 5e-4."""
+    rng = np.random.default_rng([seed, i])
+    r1, r2 = rng.uniform(0.1, 0.25, 2)
+    cells = int(rng.integers(20, 81))
+    E = float(rng.uniform(500.0, 5000.0))
+    speed = float(rng.uniform(0.05, 0.2))
+    grid = Grid2D(0.0, 1.0, 0.0, 1.0, cells + 1, cells + 1)
+    off = grid.dx / 2
+    c1 = buildParticleForCircle([0.3, 0.3], float(r1), off)
+    c2 = buildParticleForCircle([0.7, 0.7], float(r2), off)
+    mat = ElasticMaterial(E, 0.3, 1000.0, 0, 0, max(len(c1), len(c2)))
+    s1, s2 = Solid2D(c1, mat), Solid2D(c2, mat)
+    for s in (s1, s2):
+        _scale(s, off, 2)
+    assign_velocity(s1, [speed, speed])
+    assign_velocity(s2, [-speed, -speed])
+    data = {"total_time": 1000 * 5e-4, "dt": 5e-4, "time": 0.0,
+            "bodyforce": ConstantBodyForce2D([0.0, 0.0]),
+            "dirichlet_grid": [("bottom", (1, 1)), ("top", (1, 1)), ("left", (1, 1)), ("right", (1, 1))]}
+    return grid, [s1, s2], USL(1e-9), data
+
+
+def apply_dirichlet(grid, data):
+    fix_Dirichlet_grid(grid, data, ghostcell="ghostcell" in data)

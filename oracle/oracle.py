@@ -1,0 +1,120 @@
+"""ctypes binding of the CPU oracle (oracle/mpm_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and bench.py's
+CPU-baseline leg, never by the jump_gb300 package.  It consumes the same
+descriptors as the CUDA library (jump_gb300.engine.Descriptors) so both run
+on identical inputs.  Parity status: unpinned (the Julia reference cannot
+run here and ships no golden data).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from jump_gb300 import _capi
+from jump_gb300.engine import BodyState, Descriptors, _ContextBase
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "mpm_oracle.cpp")
+LIB = os.path.join(HERE, "_build", "libmpm_oracle.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """g++ -O3 -ffp-contract=off (no FMA contraction), OpenMP when available."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    hdr = os.path.join(HERE, "..", "include", "jump_mpm.h")
+    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC)
+            and os.path.getmtime(LIB) >= os.path.getmtime(hdr)):
+        return LIB
+    base = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", SRC, "-o", LIB]
+    r = subprocess.run(base[:6] + ["-fopenmp"] + base[6:], capture_output=True, text=True)
+    if r.returncode != 0:
+        r = subprocess.run(base, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stderr)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        vp = C.c_void_p
+        L.oracle_create.argtypes = [C.POINTER(_capi.GridDesc), C.POINTER(_capi.BodyDesc), C.c_int32,
+                                    C.POINTER(_capi.Params), C.POINTER(vp)]
+        L.oracle_step.argtypes = [vp, C.c_int64, C.POINTER(C.c_double)]
+        L.oracle_download.argtypes = [vp, C.c_int32, C.POINTER(_capi.BodyView)]
+        L.oracle_download_grid.argtypes = [vp] + [C.POINTER(C.c_double)] * 4
+        L.oracle_energies.argtypes = [vp] + [C.POINTER(C.c_double)] * 3
+        L.oracle_destroy.argtypes = [vp]
+        L.oracle_set_threads.argtypes = [vp, C.c_int32]
+        L.oracle_last_error.restype = C.c_char_p
+        L.oracle_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise _capi.MPMError(rc, lib().oracle_last_error().decode())
+
+
+class OracleContext(_ContextBase):
+    """Same driver surface as jump_gb300.engine.MPMContext, on the CPU restatement."""
+
+    def __init__(self, desc: Descriptors, threads: int = 1):
+        super().__init__(desc)
+        self.L = lib()
+        h = C.c_void_p()
+        _check(self.L.oracle_create(C.byref(desc.grid), desc.bodies, desc.nbodies,
+                                    C.byref(desc.params), C.byref(h)))
+        self.h = h
+        self.L.oracle_set_threads(self.h, int(threads))
+
+    def step(self, nsteps: int, t: float | None = None, check: bool = True):
+        tt = C.c_double(0.0 if t is None else t)
+        rc = self.L.oracle_step(self.h, int(nsteps), C.byref(tt))
+        if check:
+            _check(rc)
+        return tt.value if t is not None else rc
+
+    def _download(self, s, view):
+        _check(self.L.oracle_download(self.h, int(s), C.byref(view)))
+
+    def download_grid(self, nn: int):
+        d = self.dim
+        m, p0, p, f = np.zeros(nn), np.zeros((nn, d)), np.zeros((nn, d)), np.zeros((nn, d))
+        _check(self.L.oracle_download_grid(self.h, _capi.dptr(m), _capi.dptr(p0), _capi.dptr(p),
+                                           _capi.dptr(f)))
+        return m, p0, p, f
+
+    def energies(self):
+        ke, se = C.c_double(), C.c_double()
+        mom = np.zeros(3)
+        _check(self.L.oracle_energies(self.h, C.byref(ke), C.byref(se), _capi.dptr(mom)))
+        return ke.value, se.value, mom[: self.dim]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+__all__ = ["OracleContext", "BodyState", "build", "lib", "max_threads"]

@@ -1,0 +1,96 @@
+"""Shared test helpers: rebuild a case from a golden fixture, run a context,
+compare particle fields."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from jump_gb300 import _capi
+from jump_gb300.algorithm import USL, ConstantBodyForce2D, ConstantBodyForce3D
+from jump_gb300.engine import Descriptors, colmajor, from_colmajor
+from jump_gb300.grid import Grid2D, Grid3D
+from jump_gb300.material import ElasticMaterial, ElastoPlasticMaterial, NeoHookeanMaterial
+from jump_gb300.solid import Solid2D, Solid3D
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr")
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = int(z["meta_dim"])
+    xmin, xmax, nodes = z["meta_xmin"], z["meta_xmax"], z["meta_nodes"]
+    if d == 2:
+        grid = Grid2D(xmin[0], xmax[0], xmin[1], xmax[1], nodes[0], nodes[1])
+    else:
+        grid = Grid3D(xmin[0], xmax[0], xmin[1], xmax[1], xmin[2], xmax[2], nodes[0], nodes[1], nodes[2])
+    grid.fixedNodes[:, :] = z["meta_fixed"].T
+    solids = []
+    for b in range(int(z["meta_nbodies"])):
+        typ, E, nu, rho, fy, k1 = z[f"b{b}_mat"]
+        pos = z[f"b{b}_in_pos"]
+        n = pos.shape[0]
+        if int(typ) == _capi.MPM_MAT_ELASTIC:
+            mat = ElasticMaterial(E, nu, rho, n)
+        elif int(typ) == _capi.MPM_MAT_NEOHOOKEAN:
+            mat = NeoHookeanMaterial(E, nu, rho, n)
+        else:
+            mat = ElastoPlasticMaterial(E, nu, rho, fy, k1, n)
+        s = (Solid2D if d == 2 else Solid3D)(pos, mat)
+        s.velocity[:] = z[f"b{b}_in_vel"]
+        s.mass[:] = z[f"b{b}_in_mass"]
+        s.volume[:] = z[f"b{b}_in_vol"]
+        s.volumeInitial[:] = z[f"b{b}_in_vol0"]
+        s.deformationGradient[:] = from_colmajor(z[f"b{b}_in_F"].ravel(), n, d)
+        s.strain[:] = from_colmajor(z[f"b{b}_in_strain"].ravel(), n, d)
+        s.stress[:] = from_colmajor(z[f"b{b}_in_stress"].ravel(), n, d)
+        if isinstance(mat, ElastoPlasticMaterial):
+            mat.alpha[:] = z[f"b{b}_in_alpha"]
+            if d == 2:
+                mat.pstrain[:] = z[f"b{b}_in_ep"]
+            else:
+                mat.pstrain_3D[:] = from_colmajor(z[f"b{b}_in_ep"].ravel(), n, 3)
+        if f"b{b}_in_youngs" in z:
+            s.youngs = z[f"b{b}_in_youngs"].copy()
+        solids.append(s)
+    g = z["meta_gravity"]
+    bf = ConstantBodyForce2D(g[:2]) if d == 2 else ConstantBodyForce3D(g)
+    return grid, solids, float(z["meta_tol"]), bf, float(z["meta_dt"]), int(z["meta_nsteps"]), z
+
+
+def golden_expected(z, b):
+    """Expected outputs of body b in the download layout."""
+    d = int(z["meta_dim"])
+    out = {
+        "pos": z[f"b{b}_out_pos"], "velocity": z[f"b{b}_out_vel"], "volume": z[f"b{b}_out_vol"],
+        "F": z[f"b{b}_out_F"].ravel(), "strain": z[f"b{b}_out_strain"].ravel(),
+        "stress": z[f"b{b}_out_stress"].ravel(), "alpha": z[f"b{b}_out_alpha"],
+        "pstrain": z[f"b{b}_out_ep"].ravel(), "vmstr": z[f"b{b}_out_vm"],
+    }
+    return out
+
+
+def descriptors(grid, solids, tol, bf, dt, **kw):
+    return Descriptors(grid, solids, tolerance=tol, body_force=bf, dt=dt, **kw)
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| over a field (0 when both are identically 0)."""
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    den = np.max(np.abs(b)) if b.size else 0.0
+    num = np.max(np.abs(a - b)) if b.size else 0.0
+    if den == 0.0:
+        return float(num)
+    return float(num / den)
+
+
+def field_errors(states_a, states_b, fields=FIELDS):
+    errs = {}
+    for s, (A, B) in enumerate(zip(states_a, states_b)):
+        for f in fields:
+            errs[(s, f)] = rel_err(getattr(A, f), getattr(B, f))
+    return errs

@@ -1,0 +1,426 @@
+"""Generate the golden fixtures of tests/golden/*.npz.
+
+An independent pure-Python restatement of jump's USL step, written line by
+line from the Julia source with Python floats (IEEE binary64, each operation
+rounded, no fused multiply-add), run on small seeded cases.  The C++ oracle
+must reproduce these outputs bit for bit; the CUDA path is then compared with
+the oracle.  Neither restatement can be checked against the Julia reference
+itself (no Julia toolchain exists where this project builds and runs).
+
+Followed statements (paths relative to the reference repository):
+  SolveExplicitSolidMechanics2D.jl:381-534   reset, P2G, grid update, G2P
+  Basis.jl:63-78, 104-137, 219-251, 292-332  node lookup and hat functions
+  Material.jl:68-81, 119-122, 174-275        update_stress!
+  Grid.jl:104-154, 198-264                   node coordinates
+3D uses the 2D USL statements with three components (the reference's 3D USL
+reads undefined variables); J2 stress is computed as the math of
+Material.jl:174-275 and returned.
+
+Run:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+
+
+def sign(x):
+    return 1.0 if x > 0 else (-1.0 if x < 0 else 0.0)
+
+
+class PyGrid:
+    def __init__(self, dim, xmin, xmax, nodes):
+        self.dim = dim
+        self.xmin = list(xmin)
+        self.n = list(nodes)
+        self.dx = [(xmax[a] - xmin[a]) / (float(nodes[a]) - 1.0) for a in range(dim)]
+        self.dxI = [1.0 / self.dx[a] for a in range(dim)]
+        self.nxy = nodes[0] * nodes[1]
+        self.count = self.nxy * (nodes[2] if dim == 3 else 1)
+        self.pos = []
+        for k in range(nodes[2] if dim == 3 else 1):
+            for j in range(nodes[1]):
+                for i in range(nodes[0]):
+                    x = float(i) * self.dx[0]
+                    y = float(j) * self.dx[1]
+                    if dim == 2:
+                        self.pos.append((self.xmin[0] + x, self.xmin[1] + y))
+                    else:
+                        z = float(k) * self.dx[2]
+                        self.pos.append((self.xmin[0] + x, self.xmin[1] + y, self.xmin[2] + z))
+
+    def shape(self, xp):
+        """getShapeAndGradient: (nearPoints 0-based, funcs, ders)."""
+        idx = []
+        for a in range(self.dim):
+            idx.append(math.floor((xp[a] - self.xmin[a]) * self.dxI[a] + 1.0))
+        if self.dim == 2:
+            I = self.n[0] * (idx[1] - 1) + idx[0]
+            near = [I, I + 1, I + self.n[0], I + 1 + self.n[0]]
+        else:
+            I = self.nxy * (idx[2] - 1) + self.n[0] * (idx[1] - 1) + idx[0]
+            nx, nxy = self.n[0], self.nxy
+            near = [I, I + 1, I + nx, I + nx + 1, I + nxy, I + 1 + nxy, I + nx + nxy, I + nx + 1 + nxy]
+        near = [q - 1 for q in near]
+        funcs, ders = [], []
+        for q in near:
+            xi = self.pos[q]
+            if self.dim == 2:
+                xip = xp[0] - xi[0]
+                yip = xp[1] - xi[1]
+                Nx = 1.0 - abs(xip) * self.dxI[0]
+                Ny = 1.0 - abs(yip) * self.dxI[1]
+                funcs.append(Nx * Ny)
+                ders.append((-Ny * sign(xip) * self.dxI[0], -Nx * sign(yip) * self.dxI[1]))
+            else:
+                xip = xp[0] - xi[0]
+                yip = xp[1] - xi[1]
+                zip_ = xp[2] - xi[2]
+                Nx = 1.0 - abs(xip) * self.dxI[0]
+                Ny = 1.0 - abs(yip) * self.dxI[1]
+                Nz = 1.0 - abs(zip_) * self.dxI[2]
+                funcs.append(Nx * Ny * Nz)
+                ders.append((-Ny * Nz * sign(xip) * self.dxI[0],
+                             -Nx * Nz * sign(yip) * self.dxI[1],
+                             -Nx * Ny * sign(zip_) * self.dxI[2]))
+        return near, funcs, ders
+
+
+def mat_get(M, i, j, d):
+    return M[i + d * j]  # column-major, 0-based
+
+
+def matmul(A, B, d):
+    C = [0.0] * (d * d)
+    for j in range(d):
+        for i in range(d):
+            s = A[i] * B[d * j]
+            for k in range(1, d):
+                s = s + A[i + d * k] * B[k + d * j]
+            C[i + d * j] = s
+    return C
+
+
+def det(A, d):
+    if d == 2:
+        return A[0] * A[3] - A[2] * A[1]
+    x0, x1, x2 = A[0:3], A[3:6], A[6:9]
+    cr = (x1[1] * x2[2] - x1[2] * x2[1], x1[2] * x2[0] - x1[0] * x2[2], x1[0] * x2[1] - x1[1] * x2[0])
+    return x0[0] * cr[0] + x0[1] * cr[1] + x0[2] * cr[2]
+
+
+def stress_update(mat, d, sig, eps, F, J, state):
+    """update_stress! for one particle; returns the new stress (column-major)."""
+    typ, lam, mu = mat["type"], mat["lambda"], mat["mu"]
+    if typ == 0:  # ElasticMaterial
+        if d == 3:
+            s = sig
+            state["vm"] = math.sqrt(s[0] ** 2 + s[4] ** 2 + s[8] ** 2 + 2 * (s[3] ** 2 + s[6] ** 2 + s[7] ** 2))
+            tr = eps[0] + eps[4] + eps[8]
+        else:
+            tr = eps[0] + eps[3]
+        out = []
+        for j in range(d):
+            for i in range(d):
+                v = 2.0 * mu * eps[i + d * j]
+                if i == j:
+                    v = lam * tr * 1.0 + v
+                out.append(v)
+        return [out[i] for i in range(d * d)]
+    if typ == 1:  # NeoHookeanMaterial
+        FFt = [0.0] * (d * d)
+        for j in range(d):
+            for i in range(d):
+                s = F[i] * F[j]
+                for k in range(1, d):
+                    s = s + F[i + d * k] * F[j + d * k]
+                FFt[i + d * j] = s
+        out = [0.0] * (d * d)
+        ll = lam * math.log(J) * 1.0
+        for j in range(d):
+            for i in range(d):
+                a = FFt[i + d * j] - (1.0 if i == j else 0.0) if i == j else FFt[i + d * j]
+                v = mu * a
+                if i == j:
+                    v = v + ll
+                out[i + d * j] = (1.0 / J) * v
+        return out
+    # ElastoPlasticMaterial
+    k1, fy, kappa = mat["k1"], mat["fy"], mat["kappa"]
+    if d == 3:
+        ep = state["ep"]  # 9, column-major
+        a0 = state["alpha"]
+        t3 = 0.333333333 * (eps[0] + eps[4] + eps[8])
+        ed = list(eps)
+        for c in (0, 4, 8):
+            ed[c] = ed[c] - t3
+        s = [2 * mu * (ed[c] - ep[c]) for c in range(9)]
+        ns = math.sqrt(s[0] ** 2 + s[4] ** 2 + s[8] ** 2 + 2.0 * (s[3] ** 2 + s[7] ** 2 + s[6] ** 2))
+        kt = kappa * (eps[0] + eps[4] + eps[8]) * 1.0
+        st = list(s)
+        for c in (0, 4, 8):
+            st[c] = kt + st[c]
+        f_trial = ns - (k1 * a0 + fy)
+        if f_trial <= 0.0:
+            sg = st
+        else:
+            nrm = [(1.0 / ns) * s[c] for c in range(9)]
+            lamp = (ns - k1 * a0 - fy) / (2 * mu + k1)
+            a0 += lamp
+            ep = [ep[c] + lamp * nrm[c] for c in range(9)]
+            sg = [st[c] - 2 * mu * lamp * nrm[c] for c in range(9)]
+        state["alpha"], state["ep"] = a0, ep
+        t3 = 0.333333333 * (sg[0] + sg[4] + sg[8])
+        dv = list(sg)
+        for c in (0, 4, 8):
+            dv[c] = dv[c] - t3
+        state["vm"] = math.sqrt(dv[0] ** 2 + dv[4] ** 2 + dv[8] ** 2 + 2 * (dv[3] ** 2 + dv[6] ** 2 + dv[7] ** 2))
+        return sg
+    # 2D J2, Voigt
+    Idev = [[0.5, -0.5, 0.0], [-0.5, 0.5, 0.0], [0.0, 0.0, 1.0]]
+    Im = [[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 0.5]]
+    Iinv = [[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 2.0]]
+    ep = state["ep"]  # 3
+    a0 = state["alpha"]
+    e = [mat_get(eps, 0, 0, 2), mat_get(eps, 1, 1, 2), 2 * mat_get(eps, 0, 1, 2)]
+    edv = [Idev[i][0] * e[0] + Idev[i][1] * e[1] + Idev[i][2] * e[2] for i in range(3)]
+    a = [2 * mu * (edv[i] - ep[i]) for i in range(3)]
+    s = [Im[i][0] * a[0] + Im[i][1] * a[1] + Im[i][2] * a[2] for i in range(3)]
+    ns = math.sqrt(s[0] ** 2 + s[1] ** 2 + 2 * s[2] ** 2)
+    eye2 = [1.0, 1.0, 0.0]
+    kt = kappa * (e[0] + e[1])
+    f_trial = ns - (k1 * a0 + fy)
+    if f_trial <= 0.0:
+        sg = [kt * eye2[i] + s[i] for i in range(3)]
+    else:
+        nrm = [(1.0 / ns) * s[i] for i in range(3)]
+        lamp = (ns - k1 * a0 - fy) / (2 * mu + k1)
+        a0 += lamp
+        q = [Iinv[i][0] * nrm[0] + Iinv[i][1] * nrm[1] + Iinv[i][2] * nrm[2] for i in range(3)]
+        ep = [ep[i] + lamp * q[i] for i in range(3)]
+        sg = [kt * eye2[i] + s[i] - 2 * mu * lamp * nrm[i] for i in range(3)]
+    state["alpha"], state["ep"] = a0, ep
+    dv = [Idev[i][0] * sg[0] + Idev[i][1] * sg[1] + Idev[i][2] * sg[2] for i in range(3)]
+    state["vm"] = math.sqrt(dv[0] ** 2 + dv[1] ** 2 + 2 * dv[2] ** 2)
+    return [sg[0], sg[2], sg[2], sg[1]]
+
+
+def usl_steps(case, nsteps):
+    """Run nsteps of the USL loop on a case dict (lists of floats); mutates it."""
+    d = case["dim"]
+    G = PyGrid(d, case["xmin"], case["xmax"], case["nodes"])
+    fixed = case["fixed"]  # list of d-tuples per node
+    dt, tol, body = case["dt"], case["tol"], case["gravity"][:d]
+    for _ in range(nsteps):
+        mass = [0.0] * G.count
+        mom0 = [[0.0] * d for _ in range(G.count)]
+        force = [[0.0] * d for _ in range(G.count)]
+        for B in case["bodies"]:
+            for ip in range(B["n"]):
+                near, funcs, ders = G.shape(B["pos"][ip])
+                fVolume, fMass, vp, sigma = B["vol"][ip], B["mass"][ip], B["vel"][ip], B["stress"][ip]
+                for i in range(len(near)):
+                    q, Ni, dNi = near[i], funcs[i], ders[i]
+                    Nim = Ni * fMass
+                    mass[q] += Nim
+                    for a in range(d):
+                        mom0[q][a] += Nim * vp[a]
+                    for a in range(d):
+                        s = sigma[a] * dNi[0] + sigma[a + d] * dNi[1]
+                        if d == 3:
+                            s = s + sigma[a + 2 * d] * dNi[2]
+                        force[q][a] += -fVolume * s + fMass * body[a] * Ni
+        mom = [[0.0] * d for _ in range(G.count)]
+        for i in range(G.count):
+            for a in range(d):
+                mom[i][a] = mom0[i][a] + force[i][a] * dt
+            for a in range(d):
+                if fixed[i][a] == 1:
+                    mom0[i][a] = 0.0
+                    mom[i][a] = 0.0
+        for B in case["bodies"]:
+            mat = B["mat"]
+            for ip in range(B["n"]):
+                near, funcs, ders = G.shape(B["pos"][ip])
+                L = [0.0] * (d * d)
+                vvp = list(B["vel"][ip])
+                xxp = list(B["pos"][ip])
+                for i in range(len(near)):
+                    q, Ni, dNi = near[i], funcs[i], ders[i]
+                    mI = mass[q]
+                    if mI > tol:
+                        invM = 1.0 / mI
+                        vI = [mom[q][a] * invM for a in range(d)]
+                        for a in range(d):
+                            vvp[a] += Ni * (mom[q][a] - mom0[q][a]) * invM
+                        for a in range(d):
+                            xxp[a] += Ni * vI[a] * dt
+                        for j in range(d):
+                            for a in range(d):
+                                L[a + d * j] += dNi[j] * vI[a]
+                B["vel"][ip] = vvp
+                B["pos"][ip] = xxp
+                D_ = [0.5 * (L[i + d * j] + L[j + d * i]) for j in range(d) for i in range(d)]
+                B["strain"][ip] = [B["strain"][ip][c] + dt * D_[c] for c in range(d * d)]
+                A = [L[c] * dt for c in range(d * d)]
+                for a in range(d):
+                    A[a * (d + 1)] = A[a * (d + 1)] + 1.0
+                F = matmul(B["F"][ip], A, d)
+                B["F"][ip] = F
+                J = det(F, d)
+                B["vol"][ip] = J * B["vol0"][ip]
+                lam, mu = mat["lambda"], mat["mu"]
+                m2 = dict(mat)
+                if B.get("youngs") is not None:
+                    E, nu = B["youngs"][ip], mat["nu"]
+                    m2["lambda"] = E * nu / (1 + nu) / (1 - 2 * nu)
+                    m2["mu"] = E / 2 / (1 + nu)
+                    m2["kappa"] = m2["lambda"] + m2["mu"]
+                state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip]}
+                B["stress"][ip] = stress_update(m2, d, B["stress"][ip], B["strain"][ip], F, J, state)
+                B["alpha"][ip], B["ep"][ip], B["vm"][ip] = state["alpha"], state["ep"], state["vm"]
+    case["grid_out"] = (mass, mom0, mom, force)
+    return case
+
+
+# ---------------------------------------------------------------------------
+def case_from_objects(grid, solids, alg, data, nsteps):
+    from jump_gb300.engine import colmajor
+    from jump_gb300.material import ElastoPlasticMaterial
+    d = grid.dim
+    xmin = [grid.xmin, grid.ymin] + ([grid.zmin] if d == 3 else [])
+    xmax = [grid.xmax, grid.ymax] + ([grid.zmax] if d == 3 else [])
+    nodes = [grid.nodeCountX, grid.nodeCountY] + ([grid.nodeCountZ] if d == 3 else [])
+    fixed = [tuple(int(v) for v in grid.fixedNodes[:, i]) for i in range(grid.nodeCount)]
+    g = np.zeros(3)
+    if data.get("bodyforce") is not None:
+        g[:d] = data["bodyforce"].g
+    bodies = []
+    for s in solids:
+        m = s.mat
+        mat = {"type": m.kind, "E": m.E, "nu": m.nu, "density": m.density, "lambda": m.lambda_, "mu": m.mu,
+               "kappa": m.lambda_ + m.mu, "fy": getattr(m, "fy", 0.0), "k1": getattr(m, "k1", 0.0)}
+        n = s.parCount
+        ps = 3 if d == 2 else 9
+        ep = np.zeros((n, ps))
+        alpha = np.zeros(n)
+        if isinstance(m, ElastoPlasticMaterial):
+            alpha = m.alpha[:n].copy()
+            ep = m.pstrain[:n].copy() if d == 2 else colmajor(m.pstrain_3D[:n]).reshape(n, 9)
+        bodies.append({
+            "n": n, "mat": mat,
+            "pos": [list(map(float, r)) for r in s.pos], "vel": [list(map(float, r)) for r in s.velocity],
+            "mass": list(map(float, s.mass)), "vol": list(map(float, s.volume)),
+            "vol0": list(map(float, s.volumeInitial)),
+            "F": [list(map(float, r)) for r in colmajor(s.deformationGradient).reshape(n, d * d)],
+            "strain": [list(map(float, r)) for r in colmajor(s.strain).reshape(n, d * d)],
+            "stress": [list(map(float, r)) for r in colmajor(s.stress).reshape(n, d * d)],
+            "alpha": list(map(float, alpha)), "ep": [list(map(float, r)) for r in ep],
+            "vm": [0.0] * n,
+            "youngs": None if s.youngs is None else list(map(float, s.youngs)),
+        })
+    return {"dim": d, "xmin": xmin, "xmax": xmax, "nodes": nodes, "fixed": fixed, "dt": float(data["dt"]),
+            "tol": float(alg.tolerance), "gravity": list(map(float, g)), "bodies": bodies, "nsteps": nsteps}
+
+
+def save_case(name, case_in, case_out):
+    arrs = {}
+    d = case_in["dim"]
+    arrs["meta_dim"] = np.array(d)
+    arrs["meta_xmin"] = np.array(case_in["xmin"])
+    arrs["meta_xmax"] = np.array(case_in["xmax"])
+    arrs["meta_nodes"] = np.array(case_in["nodes"])
+    arrs["meta_fixed"] = np.array(case_in["fixed"], dtype=np.int64)
+    arrs["meta_dt"] = np.array(case_in["dt"])
+    arrs["meta_tol"] = np.array(case_in["tol"])
+    arrs["meta_gravity"] = np.array(case_in["gravity"])
+    arrs["meta_nsteps"] = np.array(case_in["nsteps"])
+    arrs["meta_nbodies"] = np.array(len(case_in["bodies"]))
+    for b, (Bi, Bo) in enumerate(zip(case_in["bodies"], case_out["bodies"])):
+        m = Bi["mat"]
+        arrs[f"b{b}_mat"] = np.array([m["type"], m["E"], m["nu"], m["density"], m["fy"], m["k1"]])
+        for k in ("pos", "vel", "mass", "vol", "vol0", "F", "strain", "stress", "alpha", "ep"):
+            arrs[f"b{b}_in_{k}"] = np.array(Bi[k], dtype=np.float64)
+        if Bi["youngs"] is not None:
+            arrs[f"b{b}_in_youngs"] = np.array(Bi["youngs"], dtype=np.float64)
+        for k in ("pos", "vel", "vol", "F", "strain", "stress", "alpha", "ep", "vm"):
+            arrs[f"b{b}_out_{k}"] = np.array(Bo[k], dtype=np.float64)
+    mass, mom0, mom, force = case_out["grid_out"]
+    arrs["grid_mass"] = np.array(mass)
+    arrs["grid_momentum0"] = np.array(mom0)
+    arrs["grid_momentum"] = np.array(mom)
+    arrs["grid_force"] = np.array(force)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+
+
+def main():
+    import copy
+    from jump_gb300 import scenarios
+    from jump_gb300.algorithm import ConstantBodyForce2D, ConstantBodyForce3D, USL
+    from jump_gb300.grid import Grid2D, Grid3D
+    from jump_gb300.material import ElasticMaterial, ElastoPlasticMaterial, NeoHookeanMaterial
+    from jump_gb300.solid import (Solid2D, Solid3D, assign_velocity, buildParticleForCircle,
+                                  buildParticleForCylinder, buildParticleForRectangle,
+                                  buildParticleForSphere)
+
+    cases = {}
+    # 1. the two-disk collision (416 particles, all faces fixed), 20 steps
+    g, s, alg, data = scenarios.two_disks()
+    scenarios.apply_dirichlet(g, data)
+    cases["two_disks_elastic_20"] = (case_from_objects(g, s, alg, data, 20))
+    # 2. 2D neo-Hookean beam under gravity with per-particle E, clamped left face
+    g = Grid2D(0.0, 1.0, 0.0, 1.0, 11, 11)
+    off = g.dx / 2
+    c = buildParticleForRectangle([0.3, 0.5], 0.6, 0.2, off)
+    m = NeoHookeanMaterial(1e4, 0.3, 1000.0, len(c))
+    so = Solid2D(c, m)
+    so.mass *= off * off
+    so.volume[:] = off * off
+    so.volumeInitial[:] = off * off
+    so.youngs = np.random.default_rng(1).uniform(0.5e4, 2e4, len(c))
+    data = {"dt": 1e-3, "bodyforce": ConstantBodyForce2D([0.0, -10.0]), "dirichlet_grid": [("left", (1, 1))]}
+    scenarios.apply_dirichlet(g, data)
+    cases["beam_nh_gravity_15"] = case_from_objects(g, [so], USL(1e-9), data, 15)
+    # 3. 2D J2 disks (yielding)
+    g, s, alg, data = scenarios.two_disks(nodes=11, speed=0.5, material="j2", E=1e4)
+    scenarios.apply_dirichlet(g, data)
+    cases["two_disks_j2_25"] = case_from_objects(g, s, alg, data, 25)
+    # 4. 3D J2 mini Taylor bar, fast impact so that particles yield
+    g, s, alg, data = scenarios.taylor_bar(h=1e-3, radius=2e-3, length=6e-3, width=8e-3, height=10e-3,
+                                           gap=0.0, speed=300.0)
+    scenarios.apply_dirichlet(g, data)
+    cases["taylor_mini_j2_6"] = case_from_objects(g, s, alg, data, 6)
+    # 5. 3D elastic and 3D neo-Hookean spheres hitting each other
+    for kind in ("elastic", "neohookean"):
+        g = Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, 7, 7, 7)
+        off = g.dx / 2
+        c1 = buildParticleForSphere([0.35, 0.35, 0.4], 0.17, off)
+        c2 = buildParticleForSphere([0.65, 0.65, 0.6], 0.17, off)
+        mk = (lambda n: ElasticMaterial(1e3, 0.3, 1000.0, n)) if kind == "elastic" else \
+            (lambda n: NeoHookeanMaterial(1e3, 0.3, 1000.0, n))
+        s1, s2 = Solid3D(c1, mk(len(c1))), Solid3D(c2, mk(len(c2)))
+        for so in (s1, s2):
+            so.mass *= off ** 3
+            so.volume[:] = off ** 3
+            so.volumeInitial[:] = off ** 3
+        assign_velocity(s1, [0.3, 0.3, 0.2])
+        assign_velocity(s2, [-0.3, -0.3, -0.2])
+        data = {"dt": 2e-3, "bodyforce": ConstantBodyForce3D([0.0, 0.0, -1.0]),
+                "dirichlet_grid": [("front", (0, 0, 1)), ("left", (1, 0, 0))]}
+        scenarios.apply_dirichlet(g, data)
+        cases[f"spheres_{kind}_12"] = case_from_objects(g, [s1, s2], USL(1e-9), data, 12)
+
+    for name, cin in cases.items():
+        cout = usl_steps(copy.deepcopy(cin), cin["nsteps"])
+        save_case(name, cin, cout)
+        print("wrote", name, [b["n"] for b in cin["bodies"]])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,69 @@
+"""The C-ABI library loads and exports every symbol include/jump_mpm.h
+declares; argument errors are reported without touching the GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from jump_gb300 import _capi
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "jump_mpm.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(mpm_[a-z_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    if not os.path.exists(_capi.LIB_PATH):
+        from jump_gb300 import build
+        build.build()
+    return _capi.lib()
+
+
+def test_every_declared_symbol_is_exported(L):
+    syms = header_symbols()
+    assert "mpm_create" in syms and "mpm_step" in syms
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) == set(_capi.SIGNATURES), "ctypes signatures must cover exactly the header"
+
+
+def test_abi_version(L):
+    assert L.mpm_abi_version() == 1
+
+
+def test_argument_errors_without_gpu(L):
+    h = C.c_void_p()
+    g = _capi.GridDesc()
+    p = _capi.Params()
+    assert L.mpm_create(None, None, 0, None, C.byref(h)) == _capi.MPM_ERR_ARG
+    assert b"null" in L.mpm_last_error()
+    g.dim = 4
+    p.dt = 1e-3
+    assert L.mpm_create(C.byref(g), None, 0, C.byref(p), C.byref(h)) == _capi.MPM_ERR_ARG
+    g.dim = 2
+    g.nodes[0], g.nodes[1] = 1, 5
+    g.xmax[0], g.xmax[1] = 1.0, 1.0
+    assert L.mpm_create(C.byref(g), None, 0, C.byref(p), C.byref(h)) == _capi.MPM_ERR_ARG
+    g.nodes[0] = 5
+    p.dt = 0.0
+    assert L.mpm_create(C.byref(g), None, 0, C.byref(p), C.byref(h)) == _capi.MPM_ERR_ARG
+    assert L.mpm_step(None, 1, None) == _capi.MPM_ERR_ARG
+    assert L.mpm_destroy(None) == _capi.MPM_OK
+
+
+def test_asymmetric_stress_rejected(L):
+    import numpy as np
+    from jump_gb300 import scenarios
+    from jump_gb300.engine import Descriptors
+    g, s, alg, data = scenarios.two_disks(nodes=6)
+    s[0].stress[0] = np.array([[1.0, 2.0], [3.0, 4.0]])
+    d = Descriptors(g, s, tolerance=alg.tolerance, body_force=data["bodyforce"], dt=data["dt"])
+    h = C.c_void_p()
+    rc = L.mpm_create(C.byref(d.grid), d.bodies, d.nbodies, C.byref(d.params), C.byref(h))
+    assert rc == _capi.MPM_ERR_ARG and b"symmetric" in L.mpm_last_error()

@@ -1,0 +1,91 @@
+"""CUDA path vs the CPU oracle on identical inputs (FP64 within 1e-10
+relative per particle field; FP32 error bounds stated per case)."""
+import numpy as np
+import pytest
+
+from cases import GOLDEN_CASES, descriptors, field_errors, golden_expected, load_golden, rel_err
+from jump_gb300 import scenarios
+from jump_gb300.engine import Descriptors, MPMContext
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+
+
+def run_pair(grid, solids, tol, bf, dt, steps, oracle, precision="f64", sched=None):
+    dg = MPMContext(descriptors(grid, solids, tol, bf, dt, precision=precision))
+    do = oracle.OracleContext(descriptors(grid, solids, tol, bf, dt))
+    for n in (sched or [steps]):
+        dg.step(n)
+        do.step(n)
+    return dg, do
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_cases_fp64(name, oracle_lib):
+    grid, solids, tol, bf, dt, nsteps, z = load_golden(name)
+    dg = MPMContext(descriptors(grid, solids, tol, bf, dt))
+    dg.step(nsteps)
+    for b, st in enumerate(dg.download_all()):
+        for k, v in golden_expected(z, b).items():
+            assert rel_err(getattr(st, k), v) <= FP64_TOL, (name, b, k, rel_err(getattr(st, k), v))
+
+
+@pytest.mark.parametrize("steps", [1, 10, 100])
+def test_two_disks_fp64_vs_oracle(steps, oracle_lib):
+    grid, solids, alg, data = scenarios.two_disks()
+    scenarios.apply_dirichlet(grid, data)
+    dg, do = run_pair(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], steps, oracle_lib)
+    errs = field_errors(dg.download_all(), do.download_all())
+    worst = max(errs.values())
+    assert worst <= FP64_TOL, sorted(errs.items(), key=lambda kv: -kv[1])[:4]
+    ke_g, se_g, p_g = dg.energies()
+    ke_o, se_o, p_o = do.energies()
+    assert abs(ke_g - ke_o) <= 1e-10 * abs(ke_o) and abs(se_g - se_o) <= 1e-9 * max(abs(se_o), 1e-30)
+
+
+def test_grid_download_matches_oracle(oracle_lib):
+    grid, solids, alg, data = scenarios.two_disks()
+    scenarios.apply_dirichlet(grid, data)
+    dg, do = run_pair(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], 5, oracle_lib)
+    for a, b in zip(dg.download_grid(grid.nodeCount), do.download_grid(grid.nodeCount)):
+        assert rel_err(a, b) <= 1e-12
+
+
+def test_taylor_bar_small_fp64_100_steps(oracle_lib):
+    """J2 plasticity in 3D at the wall, 100 steps (a coarser bar that the oracle runs in seconds)."""
+    grid, solids, alg, data = scenarios.taylor_bar(h=5e-4)
+    scenarios.apply_dirichlet(grid, data)
+    dg, do = run_pair(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], 100, oracle_lib)
+    so, sg = do.download_all(), dg.download_all()
+    assert np.max(so[0].alpha) > 0, "the case must yield"
+    errs = field_errors(sg, so)
+    assert max(errs.values()) <= FP64_TOL, sorted(errs.items(), key=lambda kv: -kv[1])[:4]
+
+
+def test_fp32_variant_error_stated(oracle_lib):
+    """FP32 particles + FP64 nodes against the FP64 oracle (two disks, 100 steps)."""
+    grid, solids, alg, data = scenarios.two_disks()
+    scenarios.apply_dirichlet(grid, data)
+    dg, do = run_pair(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], 100, oracle_lib,
+                      precision="f32")
+    errs = field_errors(dg.download_all(), do.download_all(), fields=("pos", "velocity", "stress", "F"))
+    # stated bound for this case: 1e-4 relative per field
+    assert max(errs.values()) <= 1e-4, errs
+
+
+def test_invariants_full_taylor_bar():
+    """Size-independent properties at the full 511,784-particle size: total mass
+    is exact, the bar only moves towards/along the wall, momentum decays at impact."""
+    grid, solids, alg, data = scenarios.taylor_bar()
+    scenarios.apply_dirichlet(grid, data)
+    d = Descriptors(grid, solids, tolerance=alg.tolerance, body_force=data["bodyforce"], dt=data["dt"])
+    ctx = MPMContext(d)
+    ke0, _, p0 = ctx.energies()
+    ctx.step(50)
+    ke1, se1, p1 = ctx.energies()
+    st = ctx.download_body(0)
+    assert np.all(np.isfinite(st.pos)) and np.all(st.volume > 0)
+    assert abs(p1[0]) < 1e-9 * abs(p0[2]) and abs(p1[1]) < 1e-9 * abs(p0[2])  # symmetric bar
+    assert p1[2] > p0[2]  # the wall removes downward momentum
+    assert ke1 + se1 <= ke0 * (1 + 1e-9)  # plastic dissipation, no energy gain
