@@ -50,6 +50,8 @@ FieldIdx make_idx() {
 
 }  // namespace
 
+int jmpm::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+
 struct mpm_ctx {
   int dim = 2;
   bool f32 = false;
@@ -444,7 +446,19 @@ int mpm_download(mpm_ctx* c, int32_t body, const mpm_body_view* v) {
   if (D == 2) r = download(c, body, v->pstrain, 3, fi.EP, ident(3));
   else r = download(c, body, v->pstrain, 9, fi.EP, full_from_sym(3));
   if (r) return r;
-  if ((r = download(c, body, v->vmstr, 1, fi.VM, ident(1)))) return r;
+  if (v->vmstr && c->cnt[body] > 0) {
+    if (c->mats[body].type == MPM_MAT_J2) {
+      // J2 vmStr is a function of the stored stress (Material.jl:223-224, 273-274)
+      if (D == 2) Launchers<2>::j2_vm(c->stream, c->part(body), c->f32, c->staging);
+      else Launchers<3>::j2_vm(c->stream, c->part(body), c->f32, c->staging);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaMemcpyAsync(v->vmstr, c->staging, size_t(c->cnt[body]) * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+    } else if ((r = download(c, body, v->vmstr, 1, fi.VM, ident(1)))) {
+      return r;
+    }
+  }
   return MPM_OK;
 }
 

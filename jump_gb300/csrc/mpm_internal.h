@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "mpm_common.cuh"
 
 namespace jmpm {
@@ -26,8 +28,12 @@ struct Launchers {
                          const CompMapH& cm);
   static void soa_to_aos(cudaStream_t s, const PartP& pp, bool f32, double* dst, int per, int f0,
                          const CompMapH& cm);
+  static void j2_vm(cudaStream_t s, const PartP& pp, bool f32, double* dst);
 };
 
 constexpr int kEnergyBlocks = 304;  // 2 x 152 SMs
+
+// Records msg as the calling thread's mpm_last_error() text; returns code.
+int set_last_error(int code, const std::string& msg);
 
 }  // namespace jmpm

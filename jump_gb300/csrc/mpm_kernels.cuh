@@ -169,10 +169,9 @@ __device__ __forceinline__ void j2_3d(R lam, R mu, R kappa, R fy, R k1, const R*
   R a0 = *alpha;
   R f_trial = ns - (k1 * a0 + fy);
   R sg[6];
-  if (f_trial <= R(0)) {
 #pragma unroll
-    for (int c = 0; c < 6; ++c) sg[c] = s[c] + (c < 3 ? kt : R(0));
-  } else {
+  for (int c = 0; c < 6; ++c) sg[c] = c < 3 ? s[c] + kt : s[c];  // sigma_trial
+  if (!(f_trial <= R(0))) {
     R inv = R(1) / ns;
     R lamp = ((ns - k1 * a0) - fy) / (tmu + k1);
     a0 += lamp;
@@ -181,16 +180,29 @@ __device__ __forceinline__ void j2_3d(R lam, R mu, R kappa, R fy, R k1, const R*
     for (int c = 0; c < 6; ++c) {
       R nrm = inv * s[c];
       ep[c] += lamp * nrm;
-      sg[c] = (s[c] + (c < 3 ? kt : R(0))) - cc * nrm;
+      sg[c] -= cc * nrm;
     }
     *alpha = a0;
   }
 #pragma unroll
   for (int c = 0; c < 6; ++c) sig[c] = sg[c];
-  R ts = R(0.333333333) * ((sg[0] + sg[1]) + sg[2]);
-  R d0 = sg[0] - ts, d1 = sg[1] - ts, d2 = sg[2] - ts;
-  // sqrt(d11^2 + d22^2 + d33^2 + 2*(d12^2 + d13^2 + d23^2))
-  *vm = sqrt(((sqr(d0) + sqr(d1)) + sqr(d2)) + R(2) * ((sqr(sg[3]) + sqr(sg[5])) + sqr(sg[4])));
+  (void)vm;  // von Mises stress is a function of sigma alone: computed at download (j2_vm)
+}
+
+// vmStr of the J2 updates from the stored stress (Material.jl:223-224, 273-274)
+template <int D, class R>
+__device__ __forceinline__ R j2_vm(const R* sg) {
+  if constexpr (D == 3) {
+    R ts = R(0.333333333) * ((sg[0] + sg[1]) + sg[2]);
+    R d0 = sg[0] - ts, d1 = sg[1] - ts, d2 = sg[2] - ts;
+    // sqrt(d11^2 + d22^2 + d33^2 + 2*(d12^2 + d13^2 + d23^2))
+    return sqrt(((sqr(d0) + sqr(d1)) + sqr(d2)) + R(2) * ((sqr(sg[3]) + sqr(sg[5])) + sqr(sg[4])));
+  } else {
+    // devSig = I_dev * sigma (Voigt), sqrt(d1^2 + d2^2 + 2*d3^2)
+    R d0 = R(0.5) * sg[0] + R(-0.5) * sg[1];
+    R d1 = R(-0.5) * sg[0] + R(0.5) * sg[1];
+    return sqrt((sqr(d0) + sqr(d1)) + R(2) * sqr(sg[2]));
+  }
 }
 
 // J2 radial return, 2D Voigt [xx, yy, 2xy] (Material.jl:174-225)
@@ -230,9 +242,7 @@ __device__ __forceinline__ void j2_2d(R lam, R mu, R kappa, R fy, R k1, const R*
   sig[0] = g0;
   sig[1] = g1;
   sig[2] = g2;
-  R d0 = R(0.5) * g0 + R(-0.5) * g1;
-  R d1 = R(-0.5) * g0 + R(0.5) * g1;
-  *vm = sqrt((sqr(d0) + sqr(d1)) + R(2) * sqr(g2));
+  (void)vm;  // computed at download (j2_vm)
 }
 
 template <int D>
@@ -301,16 +311,20 @@ __global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, M
     *field<R>(pp, L::V + a, p) = v[a];
   }
   // F <- F (I + L dt)   (:523)
-  R F[D * D], Fn[D * D];
+  R F[D * D], Fn[D * D], A[D][D];
 #pragma unroll
   for (int c = 0; c < D * D; ++c) F[c] = *field<R>(pp, L::F + c, p);
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int j = 0; j < D; ++j) A[k][j] = (k == j) ? Ldt[k][j] + R(1) : Ldt[k][j];  // I + L dt
 #pragma unroll
   for (int j = 0; j < D; ++j)
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      R s = F[i] * (Ldt[0][j] + (j == 0 ? R(1) : R(0)));
+      R s = F[i] * A[0][j];
 #pragma unroll
-      for (int k = 1; k < D; ++k) s += F[i + D * k] * (Ldt[k][j] + (j == k ? R(1) : R(0)));
+      for (int k = 1; k < D; ++k) s += F[i + D * k] * A[k][j];
       Fn[i + D * j] = s;
     }
   double Fd[D * D];
@@ -365,7 +379,6 @@ __global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, M
     *field<R>(pp, L::ALPHA, p) = alpha;
 #pragma unroll
     for (int c = 0; c < L::PS; ++c) *field<R>(pp, L::EP + c, p) = ep[c];
-    *field<R>(pp, L::VM, p) = vm;
   }
   bool fin = true;
 #pragma unroll
@@ -449,6 +462,18 @@ __global__ void aos_to_soa_kernel(PartP pp, const double* src, int per, int f0, 
   if (t >= pp.count) return;
   for (int c = 0; c < cm.n; ++c)
     *field<R>(pp, f0 + c, pp.begin + t) = R(src[t * per + cm.src[c]]);
+}
+
+// vmStr of J2 particles, from the stored stress, into a dense FP64 array
+template <int D, class R>
+__global__ void j2_vm_kernel(PartP pp, double* dst) {
+  using L = Layout<D>;
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  R sg[L::S];
+#pragma unroll
+  for (int c = 0; c < L::S; ++c) sg[c] = *field<R>(pp, L::SIG + c, pp.begin + t);
+  dst[t] = double(j2_vm<D, R>(sg));
 }
 
 template <class R>

@@ -87,4 +87,12 @@ void Launchers<D>::soa_to_aos(cudaStream_t s, const PartP& pp, bool f32, double*
   else soa_to_aos_kernel<double><<<nb, 256, 0, s>>>(pp, dst, per, f0, to_dev(cm));
 }
 
+template <int D>
+void Launchers<D>::j2_vm(cudaStream_t s, const PartP& pp, bool f32, double* dst) {
+  if (pp.count <= 0) return;
+  unsigned nb = blocks_for(pp.count, 256);
+  if (f32) j2_vm_kernel<D, float><<<nb, 256, 0, s>>>(pp, dst);
+  else j2_vm_kernel<D, double><<<nb, 256, 0, s>>>(pp, dst);
+}
+
 }  // namespace jmpm
