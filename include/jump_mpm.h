@@ -167,6 +167,31 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
 
 int mpm_destroy(mpm_ctx* ctx);
 
+/* No counterpart in the reference.  EnergiesFix sums (as mpm_energies) for
+   callers that cannot call cudaMalloc where they need them -- e.g. inside a
+   CUDA stream capture, where allocation is not permitted, or in a host
+   program whose device memory belongs to another allocator -- and that hold
+   the particle arrays in their own device memory.  It allocates nothing: its
+   scratch (one partial sum per 1024 particles) is a fixed static device array
+   that every GPU loading this library keeps until the process exits.
+     count     particles, 0 .. MPM_STATIC_MAX_PARTICLES (larger: MPM_ERR_ARG)
+     mass, volume          device arrays of count doubles
+     velocity              device, dim*count doubles, component-major (v_a at a*count)
+     stress, strain        device, symmetric components, component-major:
+                           2D (xx, yy, xy), 3D (xx, yy, zz, xy, yz, xz)
+     out       device, 2+dim doubles: KE, SE, momentum
+     stream    a cudaStream_t of this process, or NULL for the default stream
+   The work is enqueued on `stream` and the call returns without waiting.
+   The first call on each device looks up the scratch array's device address
+   (cudaGetSymbolAddress) with that device current, so make that first call
+   before any stream capture.  Calls share the one scratch array: calls that
+   overlap on the GPU (other streams, other threads) race and must be
+   serialised by the caller. */
+#define MPM_STATIC_MAX_PARTICLES 4194304
+int mpm_energies_static(int32_t dim, int64_t count, const double* mass, const double* velocity,
+                        const double* volume, const double* stress, const double* strain, double* out,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

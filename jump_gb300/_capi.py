@@ -145,6 +145,8 @@ SIGNATURES = {
     "mpm_last_step_ms": (C.c_int, [C.c_void_p, _dp]),
     "mpm_profile_stages": (C.c_int, [C.c_void_p, C.c_int64, _dp]),
     "mpm_destroy": (C.c_int, [C.c_void_p]),
+    "mpm_energies_static": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 STAGES = ("reset", "p2g", "grid", "g2p")
