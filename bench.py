@@ -224,7 +224,7 @@ def run_ours(args):
     g, s, alg, data, cfg = workload(args.workload)
     npart = sum(x.parCount for x in s)
     mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
-                             precision=args.precision)
+                             precision=args.precision, sort_interval=args.sort_interval)
     ctx = MPMContext(mk())
     ctx.step(args.warmup)
     sampler = ClockSampler()
@@ -294,7 +294,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
             "data": "synthetic (geometry-generated particles, no dataset)",
-            "config": dict(cfg, precision=args.precision,
+            "config": dict(cfg, precision=args.precision, sort_interval=args.sort_interval,
                            parallelism=f"replicas{world}" if world > 1 else "single-gpu"),
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "stage_ms_per_step": per,
@@ -320,6 +320,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--sort-interval", type=int, default=0,
+                    help="counting-sort particles by cell every N steps (0: never)")
     ap.add_argument("--workload", default="taylor_bar", choices=["taylor_bar", "two_disks"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")

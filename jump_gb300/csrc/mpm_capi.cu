@@ -63,7 +63,14 @@ struct mpm_ctx {
   int NF = 0;
   size_t esz = 8;
   FieldIdx fi{};
-  void* P = nullptr;
+  void* P = nullptr;          // particle SoA in use
+  void* Palt = nullptr;       // the other buffer of the counting sort (sort_interval > 0)
+  int64_t* orig = nullptr;    // orig[slot]: original (creation-order) index of the particle in slot
+  int64_t* orig_alt = nullptr;
+  int cur = 0;                // which physical buffer P is (selects the captured graph)
+  SortP sp{};
+  uint32_t ncells = 0;
+  int64_t since_sort = 0;
   GridP g{};
   NodeP nd{};
   double* coords = nullptr;
@@ -78,8 +85,8 @@ struct mpm_ctx {
   size_t staging_n = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph[2] = {nullptr, nullptr};       // one step, per physical buffer
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
   double last_ms = 0.0;
 
   PartP part(int b) const {
@@ -104,9 +111,19 @@ namespace {
 
 void destroy_ctx(mpm_ctx* c) {
   if (!c) return;
-  if (c->exec) cudaGraphExecDestroy(c->exec);
-  if (c->graph) cudaGraphDestroy(c->graph);
+  for (int i = 0; i < 2; ++i) {
+    if (c->exec[i]) cudaGraphExecDestroy(c->exec[i]);
+    if (c->graph[i]) cudaGraphDestroy(c->graph[i]);
+  }
   cudaFree(c->P);
+  cudaFree(c->Palt);
+  cudaFree(c->orig);
+  cudaFree(c->orig_alt);
+  cudaFree(c->sp.key);
+  cudaFree(c->sp.rank);
+  cudaFree(c->sp.count);
+  cudaFree(c->sp.offset);
+  cudaFree(c->sp.blocksum);
   cudaFree(c->coords);
   cudaFree(c->fixed);
   cudaFree(c->nodebuf);
@@ -127,9 +144,29 @@ void launch_aos_to_soa(mpm_ctx* c, const PartP& pp, const double* src, int per, 
   else Launchers<3>::aos_to_soa(c->stream, pp, c->f32, src, per, f0, cm);
 }
 
+// device SoA -> host AoS in original particle order (through orig[])
 void launch_soa_to_aos(mpm_ctx* c, const PartP& pp, double* dst, int per, int f0, const CompMapH& cm) {
-  if (c->dim == 2) Launchers<2>::soa_to_aos(c->stream, pp, c->f32, dst, per, f0, cm);
-  else Launchers<3>::soa_to_aos(c->stream, pp, c->f32, dst, per, f0, cm);
+  if (c->dim == 2) Launchers<2>::soa_to_aos_perm(c->stream, pp, c->f32, c->orig, dst, per, f0, cm);
+  else Launchers<3>::soa_to_aos_perm(c->stream, pp, c->f32, c->orig, dst, per, f0, cm);
+}
+
+// Counting sort of all particles by (body, cell) into the other buffer; swaps buffers.
+int enqueue_sort(mpm_ctx* c) {
+  if (!c->Palt || c->np == 0) return MPM_OK;
+  CUDA_TRY(cudaMemsetAsync(c->sp.count, 0, size_t(c->sp.nkeys) * sizeof(uint32_t), c->stream));
+  for (int b = 0; b < c->nb; ++b) {
+    uint32_t base = uint32_t(b) * (c->ncells + 1);
+    if (c->dim == 2) Launchers<2>::sort_keys(c->stream, c->g, c->part(b), c->f32, base, c->ncells, c->sp);
+    else Launchers<3>::sort_keys(c->stream, c->g, c->part(b), c->f32, base, c->ncells, c->sp);
+  }
+  Launchers<2>::scan(c->stream, c->sp.count, c->sp.offset, c->sp.blocksum, c->sp.nkeys);
+  Launchers<2>::sort_scatter(c->stream, c->f32, c->P, c->Palt, c->np, c->NF, c->sp, c->orig, c->orig_alt);
+  CUDA_TRY(cudaGetLastError());
+  std::swap(c->P, c->Palt);
+  std::swap(c->orig, c->orig_alt);
+  c->cur ^= 1;
+  c->since_sort = 0;
+  return MPM_OK;
 }
 
 // host AoS array -> staging -> SoA fields [f0, f0 + cm.n)
@@ -208,15 +245,17 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev) {
   if (ev) cudaEventRecord(ev[3], c->stream);
 }
 
+// The step graph of the buffer currently in use (captured on first use).
 int build_step_graph(mpm_ctx* c) {
-  if (c->exec) return MPM_OK;
+  const int k = c->cur;
+  if (c->exec[k]) return MPM_OK;
   CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   enqueue_step(c, nullptr);
   cudaError_t le = cudaGetLastError();
-  cudaError_t ee = cudaStreamEndCapture(c->stream, &c->graph);
+  cudaError_t ee = cudaStreamEndCapture(c->stream, &c->graph[k]);
   if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(le));
   if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
-  CUDA_TRY(cudaGraphInstantiate(&c->exec, c->graph, 0));
+  CUDA_TRY(cudaGraphInstantiate(&c->exec[k], c->graph[k], 0));
   return MPM_OK;
 }
 
@@ -313,6 +352,27 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   size_t ptot = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1);
   CUDA_TRY(cudaMalloc(&c->P, ptot * c->esz));
   CUDA_TRY(cudaMemset(c->P, 0, ptot * c->esz));
+  {
+    // identity permutation: slot i holds particle i until the first sort
+    std::vector<int64_t> iota(size_t(c->np > 0 ? c->np : 1));
+    for (size_t i = 0; i < iota.size(); ++i) iota[i] = int64_t(i);
+    CUDA_TRY(cudaMalloc(&c->orig, iota.size() * sizeof(int64_t)));
+    CUDA_TRY(cudaMemcpy(c->orig, iota.data(), iota.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  }
+  c->ncells = 1;
+  for (int a = 0; a < D; ++a) c->ncells *= uint32_t(nn[a] - 1);
+  if (prm->sort_interval > 0 && c->np > 0) {
+    // second particle buffer + key/rank/count arrays of the counting sort
+    CUDA_TRY(cudaMalloc(&c->Palt, ptot * c->esz));
+    CUDA_TRY(cudaMalloc(&c->orig_alt, size_t(c->np) * sizeof(int64_t)));
+    c->sp.nkeys = int64_t(nbodies) * (int64_t(c->ncells) + 1);
+    CUDA_TRY(cudaMalloc(&c->sp.key, size_t(c->np) * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&c->sp.rank, size_t(c->np) * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&c->sp.count, size_t(c->sp.nkeys) * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&c->sp.offset, size_t(c->sp.nkeys) * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&c->sp.blocksum, size_t((c->sp.nkeys + 1023) / 1024) * sizeof(uint32_t)));
+    c->since_sort = prm->sort_interval;  // sort before the first step
+  }
   c->staging_n = size_t(maxn > 0 ? maxn : 1) * 9;
   CUDA_TRY(cudaMalloc(&c->staging, c->staging_n * sizeof(double)));
   CUDA_TRY(cudaMalloc(&c->status, sizeof(unsigned)));
@@ -380,6 +440,13 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
     if (!(grid->xmax[a] > grid->xmin[a])) return fail(MPM_ERR_ARG, "mpm_create: need xmax > xmin");
     if (grid->nodes[a] > (int64_t(1) << 30)) return fail(MPM_ERR_ARG, "mpm_create: grid axis too large");
   }
+  {
+    int64_t cells = 1;
+    for (int a = 0; a < grid->dim; ++a) cells *= grid->nodes[a] - 1;
+    if (params->sort_interval > 0 && int64_t(nbodies) * (cells + 1) >= (int64_t(1) << 32))
+      return fail(MPM_ERR_ARG, "mpm_create: too many (body, cell) keys for the particle sort");
+  }
+  if (params->sort_interval < 0) return fail(MPM_ERR_ARG, "mpm_create: sort_interval < 0");
   if (!(params->dt > 0.0) || !std::isfinite(params->dt)) return fail(MPM_ERR_ARG, "mpm_create: dt must be > 0");
   if (params->precision != MPM_PREC_F64 && params->precision != MPM_PREC_F32)
     return fail(MPM_ERR_ARG, "mpm_create: unknown precision");
@@ -412,12 +479,14 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
 int mpm_step(mpm_ctx* c, int64_t nsteps, double* t_inout) {
   if (!c) return fail(MPM_ERR_ARG, "mpm_step: null context");
   if (nsteps < 0) return fail(MPM_ERR_ARG, "mpm_step: nsteps < 0");
-  int r = build_step_graph(c);
-  if (r) return r;
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CUDA_TRY(cudaEventRecord(c->e0, c->stream));
   for (int64_t k = 0; k < nsteps; ++k) {
-    CUDA_TRY(cudaGraphLaunch(c->exec, c->stream));
+    int r;
+    if (c->Palt && c->since_sort >= c->prm.sort_interval && (r = enqueue_sort(c))) return r;
+    if ((r = build_step_graph(c))) return r;
+    CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
+    ++c->since_sort;
     if (t_inout) *t_inout += c->prm.dt;
   }
   CUDA_TRY(cudaEventRecord(c->e1, c->stream));
@@ -449,8 +518,8 @@ int mpm_download(mpm_ctx* c, int32_t body, const mpm_body_view* v) {
   if (v->vmstr && c->cnt[body] > 0) {
     if (c->mats[body].type == MPM_MAT_J2) {
       // J2 vmStr is a function of the stored stress (Material.jl:223-224, 273-274)
-      if (D == 2) Launchers<2>::j2_vm(c->stream, c->part(body), c->f32, c->staging);
-      else Launchers<3>::j2_vm(c->stream, c->part(body), c->f32, c->staging);
+      if (D == 2) Launchers<2>::j2_vm_perm(c->stream, c->part(body), c->f32, c->orig, c->staging);
+      else Launchers<3>::j2_vm_perm(c->stream, c->part(body), c->f32, c->orig, c->staging);
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaMemcpyAsync(v->vmstr, c->staging, size_t(c->cnt[body]) * sizeof(double),
                                cudaMemcpyDeviceToHost, c->stream));
@@ -508,13 +577,15 @@ int mpm_energies(mpm_ctx* c, double* ke, double* se, double* momentum) {
   return MPM_OK;
 }
 
-// snapshot layout: 4 x int64 header (magic, dim, precision, particle count) + particle SoA
-static const int64_t kMagic = 0x4d504d4a554d5031LL;
+// snapshot layout: 4 x int64 header (magic, dim, precision, particle count),
+// the particle SoA in slot order, then orig[slot] (the slot -> particle map)
+static const int64_t kMagic = 0x4d504d4a554d5032LL;
 
 int mpm_save(mpm_ctx* c, void* buf, size_t* nbytes) {
   if (!c || !nbytes) return fail(MPM_ERR_ARG, "mpm_save: null argument");
   size_t body = size_t(c->NF) * size_t(c->np) * c->esz;
-  size_t need = 4 * sizeof(int64_t) + body;
+  size_t perm = size_t(c->np) * sizeof(int64_t);
+  size_t need = 4 * sizeof(int64_t) + body + perm;
   if (!buf) {
     *nbytes = need;
     return MPM_OK;
@@ -523,7 +594,9 @@ int mpm_save(mpm_ctx* c, void* buf, size_t* nbytes) {
   int64_t hdr[4] = {kMagic, c->dim, c->f32 ? 1 : 0, c->np};
   std::memcpy(buf, hdr, sizeof(hdr));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
-  if (body) CUDA_TRY(cudaMemcpy(static_cast<char*>(buf) + sizeof(hdr), c->P, body, cudaMemcpyDeviceToHost));
+  char* p = static_cast<char*>(buf) + sizeof(hdr);
+  if (body) CUDA_TRY(cudaMemcpy(p, c->P, body, cudaMemcpyDeviceToHost));
+  if (perm) CUDA_TRY(cudaMemcpy(p + body, c->orig, perm, cudaMemcpyDeviceToHost));
   *nbytes = need;
   return MPM_OK;
 }
@@ -531,13 +604,16 @@ int mpm_save(mpm_ctx* c, void* buf, size_t* nbytes) {
 int mpm_load(mpm_ctx* c, const void* buf, size_t nbytes) {
   if (!c || !buf) return fail(MPM_ERR_ARG, "mpm_load: null argument");
   size_t body = size_t(c->NF) * size_t(c->np) * c->esz;
+  size_t perm = size_t(c->np) * sizeof(int64_t);
   int64_t hdr[4];
-  if (nbytes != sizeof(hdr) + body) return fail(MPM_ERR_ARG, "mpm_load: size does not match this context");
+  if (nbytes != sizeof(hdr) + body + perm) return fail(MPM_ERR_ARG, "mpm_load: size does not match this context");
   std::memcpy(hdr, buf, sizeof(hdr));
   if (hdr[0] != kMagic || hdr[1] != c->dim || hdr[2] != (c->f32 ? 1 : 0) || hdr[3] != c->np)
     return fail(MPM_ERR_ARG, "mpm_load: snapshot belongs to a different configuration");
   CUDA_TRY(cudaStreamSynchronize(c->stream));
-  if (body) CUDA_TRY(cudaMemcpy(c->P, static_cast<const char*>(buf) + sizeof(hdr), body, cudaMemcpyHostToDevice));
+  const char* p = static_cast<const char*>(buf) + sizeof(hdr);
+  if (body) CUDA_TRY(cudaMemcpy(c->P, p, body, cudaMemcpyHostToDevice));
+  if (perm) CUDA_TRY(cudaMemcpy(c->orig, p + body, perm, cudaMemcpyHostToDevice));
   return MPM_OK;
 }
 

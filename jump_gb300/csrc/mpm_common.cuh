@@ -82,6 +82,16 @@ struct PartP {
   int64_t count;   // particles of this launch
 };
 
+// Buffers of the counting sort by (body, cell).
+struct SortP {
+  uint32_t* key;       // per particle
+  uint32_t* rank;      // per particle: arrival rank inside its key
+  uint32_t* count;     // per key, zeroed before the key pass
+  uint32_t* offset;    // per key, exclusive scan of count
+  uint32_t* blocksum;  // per 1024-key scan block
+  int64_t nkeys;
+};
+
 __device__ __forceinline__ bool is_zero_bits(double x) {
   return (__double_as_longlong(x) << 1) == 0;
 }
@@ -95,6 +105,28 @@ __device__ __forceinline__ bool finite_bits(double x) {
 }
 __device__ __forceinline__ bool finite_bits(float x) {
   return ((__float_as_uint(x) >> 23) & 0xff) != 0xff;
+}
+
+// Exact float -> double on the integer pipe (the hardware conversion issues on
+// the FP64 pipe, which runs at 1/64 of the FP32 rate on this GPU).  Normal
+// numbers and zeros are repacked bit for bit; subnormals, Inf and NaN take the
+// hardware conversion.
+__device__ __forceinline__ double to_f64(float f) {
+  unsigned u = __float_as_uint(f);
+  unsigned e = u & 0x7f800000u;
+  if (e == 0u || e == 0x7f800000u) {
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double(int(u & 0x80000000u), 0);
+    return double(f);
+  }
+  unsigned hi = (u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + 0x38000000u);
+  return __hiloint2double(int(hi), int(u << 29));
+}
+__device__ __forceinline__ double to_f64(double d) { return d; }
+
+// x > 0 for a double, decided on the integer pipe
+__device__ __forceinline__ bool positive_bits(double x) {
+  long long b = __double_as_longlong(x);
+  return b > 0 && ((b >> 52) & 0x7ff) != 0x7ff;
 }
 
 // -sign(delta) * dxI, selected with integer ops (Basis.jl:247-248, sign(0) = 0)

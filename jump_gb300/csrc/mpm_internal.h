@@ -29,6 +29,16 @@ struct Launchers {
   static void soa_to_aos(cudaStream_t s, const PartP& pp, bool f32, double* dst, int per, int f0,
                          const CompMapH& cm);
   static void j2_vm(cudaStream_t s, const PartP& pp, bool f32, double* dst);
+  // downloads in original particle order through the permutation orig[slot]
+  static void soa_to_aos_perm(cudaStream_t s, const PartP& pp, bool f32, const int64_t* orig, double* dst,
+                              int per, int f0, const CompMapH& cm);
+  static void j2_vm_perm(cudaStream_t s, const PartP& pp, bool f32, const int64_t* orig, double* dst);
+  // counting sort by (body, cell)
+  static void sort_keys(cudaStream_t s, const GridP& g, const PartP& pp, bool f32, uint32_t body_base,
+                        uint32_t ncells, const SortP& sp);
+  static void scan(cudaStream_t s, const uint32_t* in, uint32_t* out, uint32_t* blocksum, int64_t n);
+  static void sort_scatter(cudaStream_t s, bool f32, const void* src, void* dst, int64_t pitch, int nf,
+                           const SortP& sp, const int64_t* orig_src, int64_t* orig_dst);
 };
 
 constexpr int kEnergyBlocks = 304;  // 2 x 152 SMs

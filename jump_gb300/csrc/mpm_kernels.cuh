@@ -25,48 +25,89 @@ template <int D, class R, bool GRAV>
 __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
                                                   double gz, unsigned* status) {
   using L = Layout<D>;
+  constexpr int NV = 1 + 2 * D;  // per node: m, p0 (D), f (D)
+  constexpr bool WARP_SUM = sizeof(R) == 4;
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  // lanes of this warp holding a particle (a contiguous low range)
+  const unsigned mask = __ballot_sync(0xffffffffu, t < pp.count);
   if (t >= pp.count) return;
   int64_t p = pp.begin + t;
   R x[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
   Hat<D, R> h;
-  if (!hat<D, R>(g, x, h)) {
+  const bool ok = hat<D, R>(g, x, h);
+  if (!ok) {
     atomicOr(status, ST_OUT_OF_GRID);
-    return;
+    if (!WARP_SUM) return;
   }
   Corners<D, R> cr;
-  corners<D, R>(g, h, cr);
-  R m = *field<R>(pp, L::M, p);
-  R V = *field<R>(pp, L::VOL, p);
-  R v[D], ms[L::S];
+  R m = R(0), V = R(0), v[D], ms[L::S];
+  if (ok) {
+    corners<D, R>(g, h, cr);
+    m = *field<R>(pp, L::M, p);
+    V = *field<R>(pp, L::VOL, p);
+  }
 #pragma unroll
-  for (int a = 0; a < D; ++a) v[a] = *field<R>(pp, L::V + a, p);
+  for (int a = 0; a < D; ++a) v[a] = ok ? *field<R>(pp, L::V + a, p) : R(0);
 #pragma unroll
-  for (int c = 0; c < L::S; ++c) ms[c] = -V * *field<R>(pp, L::SIG + c, p);  // -V sigma
+  for (int c = 0; c < L::S; ++c) ms[c] = ok ? -V * *field<R>(pp, L::SIG + c, p) : R(0);  // -V sigma
   R mg[3] = {R(0), R(0), R(0)};
   if (GRAV) {
     mg[0] = m * R(gx);
     mg[1] = m * R(gy);
     if (D == 3) mg[2] = m * R(gz);
   }
+  // FP32 particles: lanes with the same base node (runs of consecutive lanes,
+  // long after the cell sort) add their contributions with a segmented
+  // shuffle reduction, and only the run's first lane issues the FP64 atomics.
+  const int lane = threadIdx.x & 31;
+  bool head = true;
+  int end = lane + 1, levels = 0;
+  if (WARP_SUM) {
+    long long key = ok ? (long long)cr.node[0] : -1ll - lane;
+    long long kprev = __shfl_up_sync(mask, key, 1);
+    head = lane == 0 || kprev != key;
+    unsigned heads = __ballot_sync(mask, head);
+    unsigned later = heads & ~((2u << lane) - 1u);
+    end = later ? __ffs(later) - 1 : 32 - __clz(mask);
+    unsigned run = __reduce_max_sync(mask, head ? unsigned(end - lane) : 0u);
+    while ((1u << levels) < run) ++levels;
+  }
   const int64_t Nn = nd.nodeCount;
 #pragma unroll
   for (int k = 0; k < (1 << D); ++k) {
-    int64_t n = cr.node[k];
-    R N = cr.N[k];
+    R val[NV];
+    R N = ok ? cr.N[k] : R(0);
     R Nm = N * m;
-    atomicAdd(nd.m + n, double(Nm));
+    val[0] = Nm;
 #pragma unroll
-    for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, double(Nm * v[a]));
+    for (int a = 0; a < D; ++a) val[1 + a] = Nm * v[a];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      R fa = ms[sym<D>(a, 0)] * cr.dN[k][0];
+      R fa = ok ? ms[sym<D>(a, 0)] * cr.dN[k][0] : R(0);
 #pragma unroll
-      for (int j = 1; j < D; ++j) fa += ms[sym<D>(a, j)] * cr.dN[k][j];
+      for (int j = 1; j < D; ++j) fa += ok ? ms[sym<D>(a, j)] * cr.dN[k][j] : R(0);
       if (GRAV) fa += mg[a] * N;
-      atomicAdd(nd.f + a * Nn + n, double(fa));
+      val[1 + D + a] = fa;
+    }
+    if (WARP_SUM) {
+      for (int l = 0; l < levels; ++l) {
+        const int off = 1 << l;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+          R o = __shfl_down_sync(mask, val[q], off);
+          if (lane + off < end) val[q] += o;
+        }
+      }
+    }
+    if (ok && head) {
+      int64_t n = cr.node[k];
+      atomicAdd(nd.m + n, to_f64(val[0]));
+#pragma unroll
+      for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, to_f64(val[1 + a]));
+#pragma unroll
+      for (int a = 0; a < D; ++a) atomicAdd(nd.f + a * Nn + n, to_f64(val[1 + D + a]));
     }
   }
 }
@@ -133,8 +174,15 @@ __device__ __forceinline__ void elastic(R lam, R mu, const R* eps, R* sig) {
 template <int D, class R>
 __device__ __forceinline__ void neohookean(R lam, R mu, const R* F, double J, R* sig) {
   // (1/J)*( mu*(F*F' - I) + lambda*log(J)*I )   (Material.jl:119-122)
-  R ll = R(double(lam) * log(J));
-  R iJ = R(1.0 / J);
+  R ll, iJ;
+  if constexpr (sizeof(R) == 8) {
+    ll = lam * log(J);
+    iJ = 1.0 / J;
+  } else {
+    // FP32 particles: J - 1 taken in FP64 keeps log(J) accurate near J = 1
+    ll = lam * log1pf(float(J - 1.0));
+    iJ = 1.0f / float(J);
+  }
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
@@ -330,11 +378,11 @@ __global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, M
   double Fd[D * D];
 #pragma unroll
   for (int c = 0; c < D * D; ++c) {
-    Fd[c] = double(Fn[c]);
+    Fd[c] = to_f64(Fn[c]);
     *field<R>(pp, L::F + c, p) = Fn[c];
   }
   double J = det_d<D>(Fd);  // det F in FP64 for both precisions
-  *field<R>(pp, L::VOL, p) = R(J * double(*field<R>(pp, L::VOL0, p)));
+  *field<R>(pp, L::VOL, p) = R(J * to_f64(*field<R>(pp, L::VOL0, p)));
   // strain += dt * 0.5*(L + L')
   R eps[L::S];
 #pragma unroll
@@ -388,7 +436,7 @@ __global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, M
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) fin &= finite_bits(x[a]) & finite_bits(v[a]);
-  unsigned st = (J > 0.0 ? 0u : ST_NEGATIVE_J) | (fin ? 0u : ST_NONFINITE);
+  unsigned st = (positive_bits(J) ? 0u : ST_NEGATIVE_J) | (fin ? 0u : ST_NONFINITE);
   if (st) atomicOr(status, st);
 }
 
@@ -481,6 +529,116 @@ __global__ void soa_to_aos_kernel(PartP pp, double* dst, int per, int f0, CompMa
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= pp.count) return;
   for (int c = 0; c < cm.n; ++c) dst[t * per + c] = double(*field<R>(pp, f0 + cm.src[c], pp.begin + t));
+}
+
+}  // namespace jmpm
+
+// ---------------------------------------------------------------------------
+// Counting sort of particles by (body, cell).  key = body * ncells + cell
+// (cell linear index x-fastest; a particle outside the grid gets its body's
+// last bucket, ncells).  Order inside a cell is the atomic arrival order.
+namespace jmpm {
+
+template <int D, class R>
+__global__ void __launch_bounds__(256) sort_keys_kernel(GridP g, PartP pp, uint32_t body_base, uint32_t ncells,
+                                                        SortP sp) {
+  using L = Layout<D>;
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  int64_t p = pp.begin + t;
+  uint32_t cell = 0;
+  bool inside = true;
+  int64_t stride = 1;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    R xa = *field<R>(pp, L::X + a, p);
+    R tt = add_rn(mul_rn(sub_rn(xa, R(g.xmin[a])), R(g.dxI[a])), R(1));
+    int i1 = floor_to_int(tt);
+    if (i1 < 1 || i1 > int(g.nn[a] - 1)) inside = false;
+    cell += uint32_t(int64_t(i1 - 1) * stride);
+    stride *= (g.nn[a] - 1);
+  }
+  uint32_t key = body_base + (inside ? cell : ncells);
+  sp.key[p] = key;
+  sp.rank[p] = atomicAdd(sp.count + key, 1u);
+}
+
+// exclusive scan, three passes: per-1024 block scan, scan of block sums, add
+static __global__ void __launch_bounds__(1024) scan_blocks_kernel(const uint32_t* in, uint32_t* out, uint32_t* blocksum,
+                                                           int64_t n) {
+  __shared__ uint32_t sh[1024];
+  int64_t i = int64_t(blockIdx.x) * 1024 + threadIdx.x;
+  uint32_t v = i < n ? in[i] : 0u;
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    uint32_t add = threadIdx.x >= off ? sh[threadIdx.x - off] : 0u;
+    __syncthreads();
+    sh[threadIdx.x] += add;
+    __syncthreads();
+  }
+  if (i < n) out[i] = sh[threadIdx.x] - v;
+  if (threadIdx.x == 1023) blocksum[blockIdx.x] = sh[1023];
+}
+
+static __global__ void __launch_bounds__(1024) scan_sums_kernel(uint32_t* blocksum, int64_t nb) {
+  __shared__ uint32_t sh[1024];
+  uint32_t carry = 0;
+  for (int64_t base = 0; base < nb; base += 1024) {
+    int64_t i = base + threadIdx.x;
+    uint32_t v = i < nb ? blocksum[i] : 0u;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      uint32_t add = threadIdx.x >= off ? sh[threadIdx.x - off] : 0u;
+      __syncthreads();
+      sh[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (i < nb) blocksum[i] = carry + sh[threadIdx.x] - v;
+    uint32_t tot = sh[1023];
+    __syncthreads();
+    carry += tot;
+  }
+}
+
+static __global__ void __launch_bounds__(1024) scan_add_kernel(uint32_t* out, const uint32_t* blocksum, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * 1024 + threadIdx.x;
+  if (i < n) out[i] += blocksum[blockIdx.x];
+}
+
+// move every field of particle p to slot offset[key] + rank, and carry its original index
+template <class R>
+__global__ void __launch_bounds__(256) sort_scatter_kernel(const R* __restrict__ src, R* __restrict__ dst,
+                                                           int64_t pitch, int nf, SortP sp,
+                                                           const int64_t* __restrict__ orig_src,
+                                                           int64_t* __restrict__ orig_dst) {
+  int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= pitch) return;
+  int64_t d = int64_t(sp.offset[sp.key[p]]) + sp.rank[p];
+  for (int f = 0; f < nf; ++f) dst[int64_t(f) * pitch + d] = src[int64_t(f) * pitch + p];
+  orig_dst[d] = orig_src[p];
+}
+
+// download in original order: dst[(orig[slot] - first) * per + c] = field[slot]
+template <class R>
+__global__ void soa_to_aos_perm_kernel(PartP pp, const int64_t* __restrict__ orig, double* dst, int per, int f0,
+                                       CompMap cm) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  int64_t o = orig[pp.begin + t] - pp.begin;
+  for (int c = 0; c < cm.n; ++c) dst[o * per + c] = double(*field<R>(pp, f0 + cm.src[c], pp.begin + t));
+}
+
+template <int D, class R>
+__global__ void j2_vm_perm_kernel(PartP pp, const int64_t* __restrict__ orig, double* dst) {
+  using L = Layout<D>;
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  R sg[L::S];
+#pragma unroll
+  for (int c = 0; c < L::S; ++c) sg[c] = *field<R>(pp, L::SIG + c, pp.begin + t);
+  dst[orig[pp.begin + t] - pp.begin] = double(j2_vm<D, R>(sg));
 }
 
 }  // namespace jmpm

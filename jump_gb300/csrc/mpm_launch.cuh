@@ -88,6 +88,54 @@ void Launchers<D>::soa_to_aos(cudaStream_t s, const PartP& pp, bool f32, double*
 }
 
 template <int D>
+void Launchers<D>::soa_to_aos_perm(cudaStream_t s, const PartP& pp, bool f32, const int64_t* orig, double* dst,
+                                   int per, int f0, const CompMapH& cm) {
+  if (pp.count <= 0) return;
+  unsigned nb = blocks_for(pp.count, 256);
+  if (f32) soa_to_aos_perm_kernel<float><<<nb, 256, 0, s>>>(pp, orig, dst, per, f0, to_dev(cm));
+  else soa_to_aos_perm_kernel<double><<<nb, 256, 0, s>>>(pp, orig, dst, per, f0, to_dev(cm));
+}
+
+template <int D>
+void Launchers<D>::j2_vm_perm(cudaStream_t s, const PartP& pp, bool f32, const int64_t* orig, double* dst) {
+  if (pp.count <= 0) return;
+  unsigned nb = blocks_for(pp.count, 256);
+  if (f32) j2_vm_perm_kernel<D, float><<<nb, 256, 0, s>>>(pp, orig, dst);
+  else j2_vm_perm_kernel<D, double><<<nb, 256, 0, s>>>(pp, orig, dst);
+}
+
+template <int D>
+void Launchers<D>::sort_keys(cudaStream_t s, const GridP& g, const PartP& pp, bool f32, uint32_t body_base,
+                             uint32_t ncells, const SortP& sp) {
+  if (pp.count <= 0) return;
+  unsigned nb = blocks_for(pp.count, 256);
+  if (f32) sort_keys_kernel<D, float><<<nb, 256, 0, s>>>(g, pp, body_base, ncells, sp);
+  else sort_keys_kernel<D, double><<<nb, 256, 0, s>>>(g, pp, body_base, ncells, sp);
+}
+
+template <int D>
+void Launchers<D>::scan(cudaStream_t s, const uint32_t* in, uint32_t* out, uint32_t* blocksum, int64_t n) {
+  if (n <= 0) return;
+  unsigned nb = blocks_for(n, 1024);
+  scan_blocks_kernel<<<nb, 1024, 0, s>>>(in, out, blocksum, n);
+  scan_sums_kernel<<<1, 1024, 0, s>>>(blocksum, nb);
+  scan_add_kernel<<<nb, 1024, 0, s>>>(out, blocksum, n);
+}
+
+template <int D>
+void Launchers<D>::sort_scatter(cudaStream_t s, bool f32, const void* src, void* dst, int64_t pitch, int nf,
+                                const SortP& sp, const int64_t* orig_src, int64_t* orig_dst) {
+  if (pitch <= 0) return;
+  unsigned nb = blocks_for(pitch, 256);
+  if (f32)
+    sort_scatter_kernel<float><<<nb, 256, 0, s>>>(static_cast<const float*>(src), static_cast<float*>(dst), pitch,
+                                                  nf, sp, orig_src, orig_dst);
+  else
+    sort_scatter_kernel<double><<<nb, 256, 0, s>>>(static_cast<const double*>(src), static_cast<double*>(dst),
+                                                   pitch, nf, sp, orig_src, orig_dst);
+}
+
+template <int D>
 void Launchers<D>::j2_vm(cudaStream_t s, const PartP& pp, bool f32, double* dst) {
   if (pp.count <= 0) return;
   unsigned nb = blocks_for(pp.count, 256);

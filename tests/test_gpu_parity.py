@@ -89,3 +89,51 @@ def test_invariants_full_taylor_bar():
     assert abs(p1[0]) < 1e-9 * abs(p0[2]) and abs(p1[1]) < 1e-9 * abs(p0[2])  # symmetric bar
     assert p1[2] > p0[2]  # the wall removes downward momentum
     assert ke1 + se1 <= ke0 * (1 + 1e-9)  # plastic dissipation, no energy gain
+
+
+@pytest.mark.parametrize("interval", [1, 7])
+def test_cell_sort_keeps_parity(interval, oracle_lib):
+    """Counting sort by (body, cell) every `interval` steps: downloads come back in
+    the original particle order and match the oracle to FP64 tolerance."""
+    grid, solids, alg, data = scenarios.two_disks()
+    scenarios.apply_dirichlet(grid, data)
+    dg = MPMContext(descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"],
+                                sort_interval=interval))
+    do = oracle_lib.OracleContext(descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"]))
+    for n in (3, 17, 30):
+        dg.step(n)
+        do.step(n)
+    errs = field_errors(dg.download_all(), do.download_all())
+    assert max(errs.values()) <= FP64_TOL, sorted(errs.items(), key=lambda kv: -kv[1])[:4]
+
+
+def test_cell_sort_taylor_bar_fp64_and_fp32(oracle_lib):
+    grid, solids, alg, data = scenarios.taylor_bar(h=5e-4)
+    scenarios.apply_dirichlet(grid, data)
+    mk = lambda **kw: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], **kw)
+    do = oracle_lib.OracleContext(mk())
+    d64 = MPMContext(mk(sort_interval=5))
+    d32 = MPMContext(mk(sort_interval=5, precision="f32"))
+    for c in (do, d64, d32):
+        c.step(40)
+    so = do.download_all()
+    e64 = field_errors(d64.download_all(), so)
+    assert max(e64.values()) <= FP64_TOL, sorted(e64.items(), key=lambda kv: -kv[1])[:4]
+    e32 = field_errors(d32.download_all(), so, fields=("pos", "velocity", "stress", "F"))
+    # stated FP32 bound for this case: 1e-3 relative per field (stress near the yield surface)
+    assert max(e32.values()) <= 1e-3, e32
+
+
+def test_save_load_roundtrip_with_sort():
+    grid, solids, alg, data = scenarios.two_disks()
+    scenarios.apply_dirichlet(grid, data)
+    mk = lambda: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], sort_interval=3)
+    a = MPMContext(mk())
+    a.step(8)
+    snap = a.save()
+    a.step(11)
+    b = MPMContext(mk())
+    b.load(snap)
+    b.step(11)
+    for x, y in zip(a.download_all(), b.download_all()):
+        assert rel_err(x.pos, y.pos) <= 1e-12 and rel_err(x.stress, y.stress) <= 1e-10
