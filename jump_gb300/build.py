@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + [
 ]
 
 SOURCES = ["mpm_k2d.cu", "mpm_k3d.cu", "mpm_capi.cu", "mpm_static.cu"]
-HEADERS = ["mpm_common.cuh", "mpm_kernels.cuh", "mpm_launch.cuh", "mpm_internal.h"]
+HEADERS = ["mpm_common.cuh", "mpm_kernels.cuh", "mpm_launch.cuh", "mpm_internal.h", "mpm_sparse.cuh"]
 
 
 def nvcc() -> str:

@@ -75,6 +75,7 @@ struct mpm_ctx {
   NodeP nd{};
   double* coords = nullptr;
   uint8_t* fixed = nullptr;
+  uint32_t* blockbuf = nullptr;  // node-block flags | list | count
   double* nodebuf = nullptr;
   float* nodebuf_f = nullptr;
   std::vector<uint8_t> fixed_h;
@@ -128,6 +129,7 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->fixed);
   cudaFree(c->nodebuf);
   cudaFree(c->nodebuf_f);
+  cudaFree(c->blockbuf);
   cudaFree(c->status);
   cudaFree(c->partial);
   cudaFree(c->red);
@@ -227,8 +229,10 @@ bool symmetric(const double* a, int64_t n, int dim) {
 // The launches of one USL step; ev (optional) gets an event recorded after each stage.
 void enqueue_step(mpm_ctx* c, cudaEvent_t* ev) {
   const int D = c->dim;
-  const size_t acc = size_t(c->nd.nodeCount) * (1 + 2 * D);
-  cudaMemsetAsync(c->nodebuf, 0, acc * sizeof(double), c->stream);
+  // reset (:381-385): only the blocks the previous step touched hold non-zeros
+  if (D == 2) Launchers<2>::clear(c->stream, c->nd);
+  else Launchers<3>::clear(c->stream, c->nd);
+  cudaMemsetAsync(c->nd.bcount, 0, sizeof(uint32_t), c->stream);
   if (ev) cudaEventRecord(ev[0], c->stream);
   for (int b = 0; b < c->nb; ++b) {
     if (D == 2) Launchers<2>::p2g(c->stream, c->g, c->nd, c->part(b), c->f32, c->prm.body_force, c->status);
@@ -324,6 +328,21 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   c->nd.vdt = c->nodebuf + Nn * (1 + 2 * D);
   c->nd.dv = c->nodebuf + Nn * (1 + 3 * D);
   c->nd.fixed = c->fixed;
+  {
+    // node blocks of 64 (4x4x4 / 8x8) and their flag/list arrays
+    const int B = D == 2 ? 8 : 4;
+    c->nd.nblk = 1;
+    for (int a = 0; a < 3; ++a) {
+      c->nd.nn[a] = nn[a];
+      c->nd.nb[a] = a < D ? (nn[a] + B - 1) / B : 1;
+      c->nd.nblk *= c->nd.nb[a];
+    }
+    CUDA_TRY(cudaMalloc(&c->blockbuf, size_t(2 * c->nd.nblk + 1) * sizeof(uint32_t)));
+    CUDA_TRY(cudaMemset(c->blockbuf, 0, size_t(2 * c->nd.nblk + 1) * sizeof(uint32_t)));
+    c->nd.bflag = c->blockbuf;
+    c->nd.blist = c->blockbuf + c->nd.nblk;
+    c->nd.bcount = c->blockbuf + 2 * c->nd.nblk;
+  }
   if (c->f32) {
     CUDA_TRY(cudaMalloc(&c->nodebuf_f, size_t(Nn) * 2 * D * sizeof(float)));
     CUDA_TRY(cudaMemset(c->nodebuf_f, 0, size_t(Nn) * 2 * D * sizeof(float)));

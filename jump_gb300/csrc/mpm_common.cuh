@@ -73,6 +73,13 @@ struct NodeP {
   float* dv_f;
   const uint8_t* fixed;  // bit a set: dof a is fixed (grid.fixedNodes)
   int64_t nodeCount;
+  int64_t nn[3];         // nodes per axis (1 for the unused axis in 2D)
+  // active node blocks (64 nodes each, see mpm_sparse.cuh)
+  uint32_t* bflag;       // per block, set by P2G
+  uint32_t* blist;       // listed blocks of the current step
+  uint32_t* bcount;      // length of blist (device)
+  int64_t nb[3];         // blocks per axis
+  int64_t nblk;
 };
 
 struct PartP {

@@ -19,7 +19,10 @@ template <int D>
 struct Launchers {
   static void p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
                   const double* grav, unsigned* status);
+  // compaction of the flagged node blocks + grid update over them
   static void grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy);
+  // zero the accumulators of the blocks listed by the previous grid stage
+  static void clear(cudaStream_t s, const NodeP& nd);
   static void g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
                   const MatParams& mp, double dt, unsigned* status);
   static void energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,

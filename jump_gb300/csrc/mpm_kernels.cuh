@@ -10,6 +10,7 @@
 #pragma once
 
 #include "mpm_common.cuh"
+#include "mpm_sparse.cuh"
 #include "../../include/jump_mpm.h"
 
 namespace jmpm {
@@ -102,6 +103,7 @@ __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, d
       }
     }
     if (ok && head) {
+      if (k == 0) mark_blocks<D>(nd, h.c);
       int64_t n = cr.node[k];
       atomicAdd(nd.m + n, to_f64(val[0]));
 #pragma unroll
@@ -113,11 +115,9 @@ __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, d
 }
 
 // ---------------------------------------------------------------------------
-// Grid update (:429-442) + nodal velocities for G2P.
+// Grid update (:429-442) + nodal velocities for G2P, for node i.
 template <int D, bool F32COPY>
-__global__ void __launch_bounds__(256) grid_kernel(NodeP nd, double dt, double tol) {
-  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= nd.nodeCount) return;
+__device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt, double tol) {
   const int64_t Nn = nd.nodeCount;
   double m = nd.m[i];
   if (!(m > tol)) {
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) grid_kernel(NodeP nd, double dt, double t
     }
     return;
   }
-  unsigned fx = nd.fixed[i];
+  const unsigned fx = nd.fixed[i];
   double vdt[D], dv[D];
   const bool live = true;
   double invM = 1.0 / m;
@@ -156,6 +156,16 @@ __global__ void __launch_bounds__(256) grid_kernel(NodeP nd, double dt, double t
       nd.vdt_f[a * Nn + i] = float(vdt[a]);
       nd.dv_f[a * Nn + i] = float(dv[a]);
     }
+  }
+}
+
+// grid update over the nodes of the listed blocks
+template <int D, bool F32COPY>
+__global__ void __launch_bounds__(256) grid_kernel(NodeP nd, double dt, double tol) {
+  const int64_t work = int64_t(*nd.bcount) * 64;
+  for (int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < work; w += int64_t(gridDim.x) * blockDim.x) {
+    int64_t i = block_node<D>(nd, nd.blist[w >> 6], int(w & 63));
+    if (i >= 0) grid_node<D, F32COPY>(nd, i, dt, tol);
   }
 }
 

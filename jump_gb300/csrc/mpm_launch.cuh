@@ -32,11 +32,22 @@ void Launchers<D>::p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
   }
 }
 
+// sparse grid stages: a fixed grid of CTAs strides over the listed blocks
+static inline unsigned sparse_ctas(const NodeP& nd) {
+  int64_t most = (nd.nblk * 64 + 255) / 256;
+  return unsigned(most < 152 * 8 ? (most > 0 ? most : 1) : 152 * 8);
+}
+
 template <int D>
 void Launchers<D>::grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy) {
-  unsigned nb = blocks_for(nd.nodeCount, 256);
-  if (f32copy) grid_kernel<D, true><<<nb, 256, 0, s>>>(nd, dt, tol);
-  else grid_kernel<D, false><<<nb, 256, 0, s>>>(nd, dt, tol);
+  compact_blocks_kernel<<<blocks_for(nd.nblk, 256), 256, 0, s>>>(nd);
+  if (f32copy) grid_kernel<D, true><<<sparse_ctas(nd), 256, 0, s>>>(nd, dt, tol);
+  else grid_kernel<D, false><<<sparse_ctas(nd), 256, 0, s>>>(nd, dt, tol);
+}
+
+template <int D>
+void Launchers<D>::clear(cudaStream_t s, const NodeP& nd) {
+  clear_blocks_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd);
 }
 
 template <int D>
