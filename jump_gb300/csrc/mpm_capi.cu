@@ -76,6 +76,9 @@ struct mpm_ctx {
   double* coords = nullptr;
   uint8_t* fixed = nullptr;
   uint32_t* blockbuf = nullptr;  // node-block flags | list | count
+  ContactP cp{};                 // contact mode: per-body node fields
+  double* contactbuf = nullptr;
+  float* contactbuf_f = nullptr;
   double* nodebuf = nullptr;
   float* nodebuf_f = nullptr;
   std::vector<uint8_t> fixed_h;
@@ -130,6 +133,8 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->nodebuf);
   cudaFree(c->nodebuf_f);
   cudaFree(c->blockbuf);
+  cudaFree(c->contactbuf);
+  cudaFree(c->contactbuf_f);
   cudaFree(c->status);
   cudaFree(c->partial);
   cudaFree(c->red);
@@ -229,22 +234,32 @@ bool symmetric(const double* a, int64_t n, int dim) {
 // The launches of one USL step; ev (optional) gets an event recorded after each stage.
 void enqueue_step(mpm_ctx* c, cudaEvent_t* ev) {
   const int D = c->dim;
+  const bool contact = c->prm.contact != 0;
+  // node field of body b: its own in contact mode, else the shared one
+  auto field_of = [&](int b) -> const NodeP& { return contact ? c->cp.body[b] : c->nd; };
   // reset (:381-385): only the blocks the previous step touched hold non-zeros
-  if (D == 2) Launchers<2>::clear(c->stream, c->nd);
-  else Launchers<3>::clear(c->stream, c->nd);
+  for (int b = 0; b < (contact ? c->nb : 1); ++b) {
+    if (D == 2) Launchers<2>::clear(c->stream, field_of(b));
+    else Launchers<3>::clear(c->stream, field_of(b));
+  }
   cudaMemsetAsync(c->nd.bcount, 0, sizeof(uint32_t), c->stream);
   if (ev) cudaEventRecord(ev[0], c->stream);
   for (int b = 0; b < c->nb; ++b) {
-    if (D == 2) Launchers<2>::p2g(c->stream, c->g, c->nd, c->part(b), c->f32, c->prm.body_force, c->status);
-    else Launchers<3>::p2g(c->stream, c->g, c->nd, c->part(b), c->f32, c->prm.body_force, c->status);
+    if (D == 2) Launchers<2>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
+    else Launchers<3>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
   }
   if (ev) cudaEventRecord(ev[1], c->stream);
-  if (D == 2) Launchers<2>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
-  else Launchers<3>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
+  if (contact) {
+    if (D == 2) Launchers<2>::contact_grid(c->stream, c->nd, c->cp, c->prm.dt, c->prm.tolerance, c->f32);
+    else Launchers<3>::contact_grid(c->stream, c->nd, c->cp, c->prm.dt, c->prm.tolerance, c->f32);
+  } else {
+    if (D == 2) Launchers<2>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
+    else Launchers<3>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
+  }
   if (ev) cudaEventRecord(ev[2], c->stream);
   for (int b = 0; b < c->nb; ++b) {
-    if (D == 2) Launchers<2>::g2p(c->stream, c->g, c->nd, c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
-    else Launchers<3>::g2p(c->stream, c->g, c->nd, c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+    if (D == 2) Launchers<2>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+    else Launchers<3>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
   }
   if (ev) cudaEventRecord(ev[3], c->stream);
 }
@@ -342,6 +357,33 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     c->nd.bflag = c->blockbuf;
     c->nd.blist = c->blockbuf + c->nd.nblk;
     c->nd.bcount = c->blockbuf + 2 * c->nd.nblk;
+  }
+  if (prm->contact) {
+    // per body: m | p0 (D) | f (D) | normal (D) | vdt (D) | dv (D), sharing mask and block list
+    const size_t per = size_t(1 + 5 * D);
+    CUDA_TRY(cudaMalloc(&c->contactbuf, size_t(Nn) * per * nbodies * sizeof(double)));
+    CUDA_TRY(cudaMemset(c->contactbuf, 0, size_t(Nn) * per * nbodies * sizeof(double)));
+    if (c->f32) {
+      CUDA_TRY(cudaMalloc(&c->contactbuf_f, size_t(Nn) * 2 * D * nbodies * sizeof(float)));
+      CUDA_TRY(cudaMemset(c->contactbuf_f, 0, size_t(Nn) * 2 * D * nbodies * sizeof(float)));
+    }
+    c->cp.nb = nbodies;
+    c->cp.friction = prm->friction;
+    for (int b = 0; b < nbodies; ++b) {
+      NodeP f = c->nd;
+      double* base = c->contactbuf + size_t(Nn) * per * b;
+      f.m = base;
+      f.p0 = base + Nn;
+      f.f = base + Nn * (1 + D);
+      f.nrm = base + Nn * (1 + 2 * D);
+      f.vdt = base + Nn * (1 + 3 * D);
+      f.dv = base + Nn * (1 + 4 * D);
+      if (c->f32) {
+        f.vdt_f = c->contactbuf_f + size_t(Nn) * 2 * D * b;
+        f.dv_f = f.vdt_f + Nn * D;
+      }
+      c->cp.body[b] = f;
+    }
   }
   if (c->f32) {
     CUDA_TRY(cudaMalloc(&c->nodebuf_f, size_t(Nn) * 2 * D * sizeof(float)));
@@ -469,7 +511,10 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
   if (!(params->dt > 0.0) || !std::isfinite(params->dt)) return fail(MPM_ERR_ARG, "mpm_create: dt must be > 0");
   if (params->precision != MPM_PREC_F64 && params->precision != MPM_PREC_F32)
     return fail(MPM_ERR_ARG, "mpm_create: unknown precision");
-  if (params->contact) return fail(MPM_ERR_UNSUPPORTED, "mpm_create: multi-body contact is not built yet");
+  if (params->contact && nbodies > kMaxContactBodies)
+    return fail(MPM_ERR_ARG, "mpm_create: contact mode supports at most " + std::to_string(kMaxContactBodies) +
+                                 " bodies");
+  if (params->contact && !(params->friction >= 0.0)) return fail(MPM_ERR_ARG, "mpm_create: friction < 0");
   const int D = grid->dim;
   for (int b = 0; b < nbodies; ++b) {
     const mpm_body_desc& d = bodies[b];
@@ -556,6 +601,25 @@ int mpm_download_grid(mpm_ctx* c, double* mass, double* momentum0, double* momen
   const int64_t Nn = c->g.nodeCount;
   std::vector<double> h(size_t(Nn) * (1 + 2 * D));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (c->prm.contact) {
+    // contact mode: the grid holds the system mass sum_b m_b; the single-field
+    // momentum and force arrays are not formed (zeros), as in the FEMP solvers
+    std::vector<double> mb(static_cast<size_t>(Nn));
+    for (int64_t i = 0; i < Nn; ++i) h[i] = 0.0;
+    for (int b = 0; b < c->nb; ++b) {
+      CUDA_TRY(cudaMemcpy(mb.data(), c->cp.body[b].m, size_t(Nn) * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int64_t i = 0; i < Nn; ++i) h[i] += mb[i];
+    }
+    for (int64_t i = 0; i < Nn; ++i) {
+      if (mass) mass[i] = h[i];
+      for (int a = 0; a < D; ++a) {
+        if (momentum0) momentum0[D * i + a] = 0.0;
+        if (momentum) momentum[D * i + a] = 0.0;
+        if (force) force[D * i + a] = 0.0;
+      }
+    }
+    return MPM_OK;
+  }
   CUDA_TRY(cudaMemcpy(h.data(), c->nodebuf, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
   const double* m = h.data();
   const double* p0 = m + Nn;

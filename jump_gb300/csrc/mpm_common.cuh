@@ -80,6 +80,15 @@ struct NodeP {
   uint32_t* bcount;      // length of blist (device)
   int64_t nb[3];         // blocks per axis
   int64_t nblk;
+  double* nrm;           // contact mode: per-body normals sum m_p grad N (D), else nullptr
+};
+
+// Contact mode: one node field per body (SolveExplicitFEMP2DContact.jl:33-52).
+constexpr int kMaxContactBodies = 4;
+struct ContactP {
+  int nb;
+  double friction;
+  NodeP body[kMaxContactBodies];
 };
 
 struct PartP {

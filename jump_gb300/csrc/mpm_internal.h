@@ -23,6 +23,9 @@ struct Launchers {
   static void grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy);
   // zero the accumulators of the blocks listed by the previous grid stage
   static void clear(cudaStream_t s, const NodeP& nd);
+  // contact mode: compaction + per-node grid update of every body field + correction
+  static void contact_grid(cudaStream_t s, const NodeP& nd, const ContactP& cp, double dt, double tol,
+                           bool f32copy);
   static void g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
                   const MatParams& mp, double dt, unsigned* status);
   static void energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,

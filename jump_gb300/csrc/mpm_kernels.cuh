@@ -26,8 +26,9 @@ template <int D, class R, bool GRAV>
 __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
                                                   double gz, unsigned* status) {
   using L = Layout<D>;
-  constexpr int NV = 1 + 2 * D;  // per node: m, p0 (D), f (D)
+  constexpr int NV = 1 + 3 * D;  // per node: m, p0 (D), f (D), normal (D, contact mode)
   constexpr bool WARP_SUM = sizeof(R) == 4;
+  const bool NRM = nd.nrm != nullptr;
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   // lanes of this warp holding a particle (a contiguous low range)
   const unsigned mask = __ballot_sync(0xffffffffu, t < pp.count);
@@ -92,11 +93,17 @@ __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, d
       if (GRAV) fa += mg[a] * N;
       val[1 + D + a] = fa;
     }
+    // normals of the contact correction: sum m_p grad N (SolveExplicitFEMP2DContact.jl:237)
+    if (NRM)
+#pragma unroll
+      for (int a = 0; a < D; ++a) val[1 + 2 * D + a] = ok ? m * cr.dN[k][a] : R(0);
     if (WARP_SUM) {
+      const int nv = NRM ? NV : 1 + 2 * D;
       for (int l = 0; l < levels; ++l) {
         const int off = 1 << l;
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
+          if (q >= nv) break;
           R o = __shfl_down_sync(mask, val[q], off);
           if (lane + off < end) val[q] += o;
         }
@@ -110,7 +117,121 @@ __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, d
       for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, to_f64(val[1 + a]));
 #pragma unroll
       for (int a = 0; a < D; ++a) atomicAdd(nd.f + a * Nn + n, to_f64(val[1 + D + a]));
+      if (NRM)
+#pragma unroll
+        for (int a = 0; a < D; ++a) atomicAdd(nd.nrm + a * Nn + n, to_f64(val[1 + 2 * D + a]));
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Contact mode grid update: one field per body, system sums, and the
+// multi-body correction at nodes two bodies share
+// (SolveExplicitFEMP2DContact.jl:248-266, 305-387; SolveExplicitFEMP3DContact.jl:424-517).
+template <int D, bool F32COPY>
+__device__ __forceinline__ void contact_node(const ContactP& cp, int64_t i, double dt, double tol) {
+  const int64_t Nn = cp.body[0].nodeCount;
+  const unsigned fx = cp.body[0].fixed[i];
+  double mb[kMaxContactBodies], v[kMaxContactBodies][D], v0[kMaxContactBodies][D];
+  double mS = 0.0, pS[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) pS[a] = 0.0;
+  int s1 = -1, s2 = -1;
+#pragma unroll
+  for (int b = 0; b < kMaxContactBodies; ++b) {
+    if (b >= cp.nb) break;
+    const NodeP& nd = cp.body[b];
+    double m = nd.m[i];
+    mb[b] = m;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double p0 = nd.p0[a * Nn + i];
+      double p = __dadd_rn(p0, __dmul_rn(nd.f[a * Nn + i], dt));  // p = p0 + f*dt
+      pS[a] += p;                                                // system momentum, before BCs
+      v0[b][a] = p0;
+      v[b][a] = p;
+    }
+    mS += m;
+    if (m > 0.0) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        v0[b][a] = v0[b][a] / m;
+        v[b][a] = v[b][a] / m;
+      }
+      if (s1 < 0) s1 = b;
+      else if (s2 < 0) s2 = b;
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+      if (fx & (1u << a)) {
+        v0[b][a] = 0.0;
+        v[b][a] = 0.0;
+      }
+  }
+  if (s2 >= 0) {
+    // common normal n = (n1 - n2)/|n1 - n2|; body 1 uses n, body 2 uses -n
+    double n[D], nn = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      n[a] = cp.body[s1].nrm[a * Nn + i] - cp.body[s2].nrm[a * Nn + i];
+      nn += n[a] * n[a];
+    }
+    nn = sqrt(nn);
+#pragma unroll
+    for (int a = 0; a < D; ++a) n[a] = n[a] / nn;
+#pragma unroll
+    for (int is = 0; is < 2; ++is) {
+      const int s = is == 0 ? s1 : s2;
+      double nI[D], dvv[D], D1 = 0.0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        nI[a] = is == 0 ? n[a] : -n[a];
+        dvv[a] = v[s][a] - pS[a] / mS;
+        D1 += dvv[a] * nI[a];
+      }
+      if (D1 > 0.0) {  // approaching
+        // Coulomb branch; with no tangential slip (C1 == 0) the reference's
+        // (muPrime/|C1|) is 0/0, whose limit is the normal-only update below
+        if (D == 2 && cp.friction > 0.0 && (dvv[0] * nI[1] - dvv[1] * nI[0]) != 0.0) {
+          double C1 = dvv[0] * nI[1] - dvv[1] * nI[0];
+          double absC1 = fabs(C1);
+          double mup = fmin(cp.friction, absC1 / D1);
+          double t0 = nI[0] + (mup / absC1) * (nI[1] * C1);
+          double t1 = nI[D - 1] + (mup / absC1) * (-nI[0] * C1);
+          v[s][0] = v[s][0] - D1 * t0;
+          v[s][D - 1] = v[s][D - 1] - D1 * t1;
+        } else {
+#pragma unroll
+          for (int a = 0; a < D; ++a) v[s][a] = v[s][a] - D1 * nI[a];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < kMaxContactBodies; ++b) {
+    if (b >= cp.nb) break;
+    const NodeP& nd = cp.body[b];
+    const bool live = mb[b] > tol;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double vd = live ? v[b][a] * dt : 0.0;
+      double dd = live ? v[b][a] - v0[b][a] : 0.0;
+      nd.vdt[a * Nn + i] = vd;
+      nd.dv[a * Nn + i] = dd;
+      if (F32COPY) {
+        nd.vdt_f[a * Nn + i] = float(vd);
+        nd.dv_f[a * Nn + i] = float(dd);
+      }
+    }
+  }
+}
+
+template <int D, bool F32COPY>
+__global__ void __launch_bounds__(256) contact_grid_kernel(NodeP nd, ContactP cp, double dt, double tol) {
+  const int64_t work = int64_t(*nd.bcount) * 64;
+  for (int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < work; w += int64_t(gridDim.x) * blockDim.x) {
+    int64_t i = block_node<D>(nd, nd.blist[w >> 6], int(w & 63));
+    if (i >= 0) contact_node<D, F32COPY>(cp, i, dt, tol);
   }
 }
 

@@ -46,6 +46,14 @@ void Launchers<D>::grid(cudaStream_t s, const NodeP& nd, double dt, double tol, 
 }
 
 template <int D>
+void Launchers<D>::contact_grid(cudaStream_t s, const NodeP& nd, const ContactP& cp, double dt, double tol,
+                                bool f32copy) {
+  compact_blocks_kernel<<<blocks_for(nd.nblk, 256), 256, 0, s>>>(nd);
+  if (f32copy) contact_grid_kernel<D, true><<<sparse_ctas(nd), 256, 0, s>>>(nd, cp, dt, tol);
+  else contact_grid_kernel<D, false><<<sparse_ctas(nd), 256, 0, s>>>(nd, cp, dt, tol);
+}
+
+template <int D>
 void Launchers<D>::clear(cudaStream_t s, const NodeP& nd) {
   clear_blocks_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd);
 }

@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(256) clear_blocks_kernel(NodeP nd) {
     for (int a = 0; a < D; ++a) {
       nd.p0[a * Nn + i] = 0.0;
       nd.f[a * Nn + i] = 0.0;
+      if (nd.nrm) nd.nrm[a * Nn + i] = 0.0;
     }
   }
 }

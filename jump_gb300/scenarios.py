@@ -132,3 +132,39 @@ def ensemble_member(i: int, seed: int = 0):
 
 def apply_dirichlet(grid, data):
     fix_Dirichlet_grid(grid, data, ghostcell="ghostcell" in data)
+
+
+def sphere_plate(h: float = 5e-4, ppc: int = 2, radius: float = 5e-3, speed: float = 50.0,
+                 E_sphere: float = 200e9, rho_sphere: float = 7800.0, E_plate: float = 5e9,
+                 rho_plate: float = 1200.0, nu: float = 0.3, plate=(20e-3, 20e-3, 4e-3), margin: float = 2e-3,
+                 cfl: float = 0.2, gap=None):
+    """An elastic steel sphere striking a neo-Hookean plate (two bodies, contact mode).
+
+    The plate rests on the z = 0 face (fixed in z); the sphere starts one cell
+    above it (``gap``, default one cell).  Contact uses one velocity field per body with the frictionless
+    normal correction.  The plate density is not given by the workload
+    description; 1200 kg/m^3 is used.
+    """
+    from .material import ElasticMaterial
+    from .solid import buildParticleForBlock, buildParticleForSphere
+    wx, wy, tz = plate
+    gap = h if gap is None else gap
+    lx = wx + 2 * margin
+    lz = tz + 2 * radius + h + 2 * margin
+    nx = int(round(lx / h)) + 1
+    nz = int(round(lz / h)) + 1
+    grid = Grid3D(0.0, lx, 0.0, lx, 0.0, (nz - 1) * h, nx, nx, nz)
+    off = h / ppc
+    cs = buildParticleForSphere([0.5 * lx, 0.5 * lx, tz + gap + radius], radius, off)
+    cp = buildParticleForBlock([0.5 * lx, 0.5 * lx, 0.5 * tz], wx, wy, tz, off)
+    ms = ElasticMaterial(E_sphere, nu, rho_sphere, len(cs))
+    mp = NeoHookeanMaterial(E_plate, nu, rho_plate, len(cp))
+    s1, s2 = Solid3D(cs, ms), Solid3D(cp, mp)
+    for s in (s1, s2):
+        _scale(s, off, 3)
+    assign_velocity(s1, [0.0, 0.0, -speed])
+    c = math.sqrt((ms.lambda_ + 2 * ms.mu) / rho_sphere)
+    data = {"total_time": 1e-4, "dt": cfl * h / c, "time": 0.0,
+            "bodyforce": ConstantBodyForce3D([0.0, 0.0, 0.0]),
+            "dirichlet_grid": [("front", (0, 0, 1))], "contact": True, "friction": 0.0}
+    return grid, [s1, s2], USL(1e-3 * float(s2.mass[0])), data

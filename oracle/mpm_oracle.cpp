@@ -583,7 +583,9 @@ void step_contact(Ctx<D>& c) {
       for (int a = 0; a < D; ++a) dv[a] = velo1[a] - c.sysp[D * i + a] / g.mass[i];
       for (int a = 0; a < D; ++a) D1 += dv[a] * nI[a];
       if (D1 > 0) {
-        if (D == 2 && fric > 0) {
+        // Coulomb branch (:376-380); with no tangential slip (C1 == 0) its
+        // (muPrime/|C1|) is 0/0 in the reference, whose limit is the normal-only update
+        if (D == 2 && fric > 0 && (dv[0] * nI[1] - dv[1] * nI[0]) != 0.0) {
           double C1 = dv[0] * nI[1] - dv[1] * nI[0];
           double absC1 = std::fabs(C1);
           double mup = std::min(fric, absC1 / D1);
