@@ -167,6 +167,49 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
 
 int mpm_destroy(mpm_ctx* ctx);
 
+/* ---------------------------------------------------------------------------
+ * Batched ensembles (no counterpart in the reference, which solves one
+ * problem per call): many independent problems -- each what one
+ * solve_explicit_dynamics_2D/3D call would take -- advance together in one
+ * persistent launch.  Each CTA takes problems from a work queue (largest
+ * first) and runs all requested steps of a problem before taking the next.
+ * All problems share the dimension, the precision and the material model
+ * type (parameters may differ); contact mode and sorting are not available.
+ * ------------------------------------------------------------------------- */
+#define MPM_BATCH_MAX_BODIES 4
+
+typedef struct mpm_instance_desc {
+  mpm_grid_desc grid;
+  const mpm_body_desc* bodies;  /* 1 .. MPM_BATCH_MAX_BODIES */
+  int32_t nbodies;
+  int32_t reserved;
+  double dt;
+  double tolerance;
+  double body_force[3];
+} mpm_instance_desc;
+
+typedef struct mpm_batch mpm_batch;
+
+int mpm_batch_create(const mpm_instance_desc* instances, int32_t ninstances, int32_t precision,
+                     mpm_batch** out);
+/* every problem advances nsteps steps (one launch) */
+int mpm_batch_step(mpm_batch* batch, int64_t nsteps);
+/* per problem MPM_OK or MPM_ERR_* of the last mpm_batch_step */
+int mpm_batch_status(mpm_batch* batch, int32_t* status);
+int mpm_batch_download(mpm_batch* batch, int32_t instance, int32_t body, const mpm_body_view* out);
+/* EnergiesFix sums per problem: out[i*(2+dim) + {0: KE, 1: SE, 2..: momentum}] */
+int mpm_batch_energies(mpm_batch* batch, double* out);
+/* launch shape: threads per CTA (multiple of 32, <= 1024) and CTAs per SM */
+int mpm_batch_set_launch(mpm_batch* batch, int32_t threads, int32_t ctas_per_sm);
+/* Autotuner: times probe_steps steps of every launch shape that fits (on a
+   scratch copy of the particles, the batch state is not advanced), keeps the
+   fastest and returns it and its device time per step. */
+int mpm_batch_tune(mpm_batch* batch, int64_t probe_steps, int32_t* threads, int32_t* ctas_per_sm,
+                   double* ms_per_step);
+/* device time of the last mpm_batch_step, milliseconds */
+int mpm_batch_last_ms(mpm_batch* batch, double* ms);
+int mpm_batch_destroy(mpm_batch* batch);
+
 /* No counterpart in the reference.  EnergiesFix sums (as mpm_energies) for
    callers that cannot call cudaMalloc where they need them -- e.g. inside a
    CUDA stream capture, where allocation is not permitted, or in a host

@@ -147,7 +147,28 @@ SIGNATURES = {
     "mpm_destroy": (C.c_int, [C.c_void_p]),
     "mpm_energies_static": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mpm_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "mpm_batch_step": (C.c_int, [C.c_void_p, C.c_int64]),
+    "mpm_batch_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "mpm_batch_download": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "mpm_batch_energies": (C.c_int, [C.c_void_p, _dp]),
+    "mpm_batch_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "mpm_batch_tune": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp]),
+    "mpm_batch_last_ms": (C.c_int, [C.c_void_p, _dp]),
+    "mpm_batch_destroy": (C.c_int, [C.c_void_p]),
 }
+
+
+class InstanceDesc(C.Structure):
+    _fields_ = [
+        ("grid", GridDesc),
+        ("bodies", C.POINTER(BodyDesc)),
+        ("nbodies", C.c_int32),
+        ("reserved", C.c_int32),
+        ("dt", C.c_double),
+        ("tolerance", C.c_double),
+        ("body_force", C.c_double * 3),
+    ]
 
 STAGES = ("reset", "p2g", "grid", "g2p")
 

@@ -1,0 +1,642 @@
+// mpm_batch.cu -- batched ensembles: many independent USL problems advance in
+// one persistent launch.
+//
+// Layout: the particles of every problem (and of every body inside a
+// problem) are contiguous ranges of one SoA allocation; node arrays of every
+// problem are packed one after another; InstanceP is the per-problem offset
+// table.  A CTA takes a problem from a work queue (problems ordered by
+// particle count, largest first), runs all requested steps of it -- reset,
+// P2G, grid update, G2P + stress, with __syncthreads between the stages --
+// and takes the next one.  Nothing but the queue counter is shared between
+// CTAs, and there is one launch for all problems and all steps.  Node data a
+// stage reads was written earlier in the same launch, so it is loaded through
+// L2 (__ldcg), never through the read-only path.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/jump_mpm.h"
+#include "mpm_internal.h"
+#include "mpm_kernels.cuh"
+
+using namespace jmpm;
+
+namespace {
+
+int fail(int code, const std::string& msg) { return set_last_error(code, msg); }
+
+#define BATCH_TRY(x)                                                                 \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(MPM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+struct InstanceP {
+  GridP g;
+  NodeP nd;
+  int64_t pbegin, pcount;  // all particles of the problem
+  int nb;
+  int64_t bbeg[MPM_BATCH_MAX_BODIES], bcnt[MPM_BATCH_MAX_BODIES];
+  MatParams mp[MPM_BATCH_MAX_BODIES];
+  double dt, tol, grav[3];
+};
+
+template <int D, class R, int MAT, bool GRAV>
+__global__ void batch_kernel(const InstanceP* __restrict__ inst, const int* __restrict__ order, int ninst,
+                             int* next, int64_t nsteps, void* P, int64_t pitch, unsigned* status) {
+  __shared__ int sh_q;
+  constexpr bool F32 = sizeof(R) == 4;
+  for (;;) {
+    if (threadIdx.x == 0) sh_q = atomicAdd(next, 1);
+    __syncthreads();
+    const int q = sh_q;
+    __syncthreads();  // every thread has read sh_q before thread 0 overwrites it
+    if (q >= ninst) return;
+    const int id = order[q];
+    const InstanceP& I = inst[id];
+    const PartP all{P, pitch, I.pbegin, I.pcount};
+    unsigned* st = status + id;
+    const int64_t Nn = I.nd.nodeCount;
+    for (int64_t s = 0; s < nsteps; ++s) {
+      // reset (:381-385)
+      for (int64_t i = threadIdx.x; i < Nn; i += blockDim.x) {
+        I.nd.m[i] = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          I.nd.p0[a * Nn + i] = 0.0;
+          I.nd.f[a * Nn + i] = 0.0;
+        }
+      }
+      __syncthreads();
+      // P2G; every thread runs the same number of iterations (warp-synchronous FP32 path)
+      for (int64_t base = 0; base < I.pcount; base += blockDim.x)
+        p2g_particle<D, R, GRAV>(I.g, I.nd, all, base + threadIdx.x, I.grav[0], I.grav[1], I.grav[2], st);
+      __syncthreads();
+      for (int64_t i = threadIdx.x; i < Nn; i += blockDim.x) grid_node<D, F32, true>(I.nd, i, I.dt, I.tol);
+      __syncthreads();
+      for (int b = 0; b < I.nb; ++b) {
+        const PartP pb{P, pitch, I.bbeg[b], I.bcnt[b]};
+        for (int64_t t = threadIdx.x; t < pb.count; t += blockDim.x)
+          g2p_particle<D, R, MAT, true>(I.g, I.nd, pb, t, I.mp[b], I.dt, st);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// EnergiesFix sums of every problem: one CTA per problem, fixed reduction order
+template <int D, class R>
+__global__ void __launch_bounds__(256) batch_energies_kernel(const InstanceP* __restrict__ inst, void* P,
+                                                             int64_t pitch, double* out) {
+  using L = Layout<D>;
+  constexpr int NQ = 2 + D;
+  const InstanceP& I = inst[blockIdx.x];
+  const PartP pp{P, pitch, I.pbegin, I.pcount};
+  double q[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) q[k] = 0.0;
+  for (int64_t t = threadIdx.x; t < pp.count; t += blockDim.x) {
+    int64_t p = pp.begin + t;
+    double m = double(*field<R>(pp, L::M, p)), vv = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double va = double(*field<R>(pp, L::V + a, p));
+      vv += va * va;
+      q[2 + a] += m * va;
+    }
+    q[0] += 0.5 * m * vv;
+    double se = 0.0;
+#pragma unroll
+    for (int c = 0; c < L::S; ++c)
+      se += (c < D ? 1.0 : 2.0) * double(*field<R>(pp, L::SIG + c, p)) * double(*field<R>(pp, L::EPS + c, p));
+    q[1] += 0.5 * double(*field<R>(pp, L::VOL, p)) * se;
+  }
+  __shared__ double sh[NQ][256];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] = q[k];
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) out[int64_t(blockIdx.x) * NQ + k] = sh[k][0];
+}
+
+int sym_slot(int dim, int i, int j) {
+  if (i == j) return i;
+  if (dim == 2) return 2;
+  int a = i < j ? i : j, b = i < j ? j : i;
+  return (a == 0 && b == 1) ? 3 : ((a == 1 && b == 2) ? 4 : 5);
+}
+
+CompMapH ident(int n) {
+  CompMapH m{};
+  m.n = n;
+  for (int i = 0; i < n; ++i) m.src[i] = i;
+  return m;
+}
+
+CompMapH sym_from_full(int dim) {
+  CompMapH m{};
+  m.n = dim == 2 ? 3 : 6;
+  for (int j = 0; j < dim; ++j)
+    for (int i = j; i < dim; ++i) m.src[sym_slot(dim, i, j)] = i + dim * j;
+  return m;
+}
+
+CompMapH full_from_sym(int dim) {
+  CompMapH m{};
+  m.n = dim * dim;
+  for (int j = 0; j < dim; ++j)
+    for (int i = 0; i < dim; ++i) m.src[i + dim * j] = sym_slot(dim, i, j);
+  return m;
+}
+
+}  // namespace
+
+struct mpm_batch {
+  int dim = 2;
+  bool f32 = false;
+  int mat = MPM_MAT_ELASTIC;
+  bool grav = false;
+  int ninst = 0;
+  int64_t np = 0;
+  int NF = 0;
+  size_t esz = 8;
+  void* P = nullptr;
+  double* nodebuf = nullptr;
+  float* nodebuf_f = nullptr;
+  uint8_t* fixed = nullptr;
+  double* coords = nullptr;
+  std::vector<InstanceP> inst;
+  InstanceP* d_inst = nullptr;
+  int* d_order = nullptr;
+  int* d_next = nullptr;
+  unsigned* d_status = nullptr;
+  double* d_energy = nullptr;
+  double* staging = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double last_ms = 0.0;
+  int threads = 256;
+  int ctas_per_sm = 0;  // 0: as many as fit
+  int sms = 1;
+
+  PartP body(int i, int b) const { return PartP{P, np, inst[i].bbeg[b], inst[i].bcnt[b]}; }
+};
+
+namespace {
+
+void destroy_batch(mpm_batch* b) {
+  if (!b) return;
+  cudaFree(b->P);
+  cudaFree(b->nodebuf);
+  cudaFree(b->nodebuf_f);
+  cudaFree(b->fixed);
+  cudaFree(b->coords);
+  cudaFree(b->d_inst);
+  cudaFree(b->d_order);
+  cudaFree(b->d_next);
+  cudaFree(b->d_status);
+  cudaFree(b->d_energy);
+  cudaFree(b->staging);
+  if (b->e0) cudaEventDestroy(b->e0);
+  if (b->e1) cudaEventDestroy(b->e1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+template <int D, class R, int MAT, bool GRAV>
+int launch_t(mpm_batch* b, void* P, int64_t nsteps, int threads, int per_sm) {
+  auto kern = batch_kernel<D, R, MAT, GRAV>;
+  cudaFuncAttributes attr;
+  BATCH_TRY(cudaFuncGetAttributes(&attr, kern));
+  if (threads > attr.maxThreadsPerBlock)
+    return fail(MPM_ERR_ARG, "mpm_batch: " + std::to_string(threads) + " threads per CTA exceed this kernel's limit " +
+                                 std::to_string(attr.maxThreadsPerBlock));
+  int occ = 0;
+  BATCH_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0));
+  if (occ < 1) return fail(MPM_ERR_ARG, "mpm_batch: launch shape does not fit on an SM");
+  int per = per_sm > 0 ? std::min(per_sm, occ) : occ;
+  BATCH_TRY(cudaMemsetAsync(b->d_next, 0, sizeof(int), b->stream));
+  kern<<<b->sms * per, threads, 0, b->stream>>>(b->d_inst, b->d_order, b->ninst, b->d_next, nsteps, P, b->np,
+                                                b->d_status);
+  BATCH_TRY(cudaGetLastError());
+  return MPM_OK;
+}
+
+template <int D, class R>
+int launch_m(mpm_batch* b, void* P, int64_t n, int th, int per) {
+  switch (b->mat) {
+    case MPM_MAT_ELASTIC:
+      return b->grav ? launch_t<D, R, MPM_MAT_ELASTIC, true>(b, P, n, th, per)
+                     : launch_t<D, R, MPM_MAT_ELASTIC, false>(b, P, n, th, per);
+    case MPM_MAT_NEOHOOKEAN:
+      return b->grav ? launch_t<D, R, MPM_MAT_NEOHOOKEAN, true>(b, P, n, th, per)
+                     : launch_t<D, R, MPM_MAT_NEOHOOKEAN, false>(b, P, n, th, per);
+    default:
+      return b->grav ? launch_t<D, R, MPM_MAT_J2, true>(b, P, n, th, per)
+                     : launch_t<D, R, MPM_MAT_J2, false>(b, P, n, th, per);
+  }
+}
+
+int launch(mpm_batch* b, void* P, int64_t nsteps, int threads, int per_sm) {
+  if (b->dim == 2)
+    return b->f32 ? launch_m<2, float>(b, P, nsteps, threads, per_sm)
+                  : launch_m<2, double>(b, P, nsteps, threads, per_sm);
+  return b->f32 ? launch_m<3, float>(b, P, nsteps, threads, per_sm)
+                : launch_m<3, double>(b, P, nsteps, threads, per_sm);
+}
+
+int upload(mpm_batch* b, const PartP& pp, const double* host, int per, int f0, const CompMapH& cm) {
+  size_t n = size_t(pp.count) * per;
+  if (n == 0 || !host) return MPM_OK;
+  BATCH_TRY(cudaMemcpyAsync(b->staging, host, n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  if (b->dim == 2) Launchers<2>::aos_to_soa(b->stream, pp, b->f32, b->staging, per, f0, cm);
+  else Launchers<3>::aos_to_soa(b->stream, pp, b->f32, b->staging, per, f0, cm);
+  BATCH_TRY(cudaGetLastError());
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  return MPM_OK;
+}
+
+int download(mpm_batch* b, const PartP& pp, double* host, int per, int f0, const CompMapH& cm) {
+  size_t n = size_t(pp.count) * per;
+  if (n == 0 || !host) return MPM_OK;
+  if (b->dim == 2) Launchers<2>::soa_to_aos(b->stream, pp, b->f32, b->staging, per, f0, cm);
+  else Launchers<3>::soa_to_aos(b->stream, pp, b->f32, b->staging, per, f0, cm);
+  BATCH_TRY(cudaGetLastError());
+  BATCH_TRY(cudaMemcpyAsync(host, b->staging, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  return MPM_OK;
+}
+
+template <int D>
+int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
+  using L = Layout<D>;
+  b->NF = L::NF;
+  int64_t maxbody = 1, nodes = 0, ncoord = 0;
+  for (int i = 0; i < n; ++i) {
+    int64_t nn = 1;
+    for (int a = 0; a < D; ++a) {
+      nn *= in[i].grid.nodes[a];
+      ncoord += in[i].grid.nodes[a];
+    }
+    nodes += nn;
+    for (int k = 0; k < in[i].nbodies; ++k) {
+      b->np += in[i].bodies[k].count;
+      maxbody = std::max(maxbody, in[i].bodies[k].count);
+    }
+  }
+  const size_t ptot = size_t(b->NF) * size_t(b->np > 0 ? b->np : 1);
+  BATCH_TRY(cudaMalloc(&b->P, ptot * b->esz));
+  BATCH_TRY(cudaMemset(b->P, 0, ptot * b->esz));
+  BATCH_TRY(cudaMalloc(&b->nodebuf, size_t(nodes) * (1 + 4 * D) * sizeof(double)));
+  BATCH_TRY(cudaMemset(b->nodebuf, 0, size_t(nodes) * (1 + 4 * D) * sizeof(double)));
+  if (b->f32) BATCH_TRY(cudaMalloc(&b->nodebuf_f, size_t(nodes) * 2 * D * sizeof(float)));
+  BATCH_TRY(cudaMalloc(&b->fixed, size_t(nodes)));
+  BATCH_TRY(cudaMalloc(&b->coords, size_t(ncoord) * sizeof(double)));
+  BATCH_TRY(cudaMalloc(&b->staging, size_t(maxbody) * 9 * sizeof(double)));
+  BATCH_TRY(cudaMalloc(&b->d_status, size_t(n) * sizeof(unsigned)));
+  BATCH_TRY(cudaMemset(b->d_status, 0, size_t(n) * sizeof(unsigned)));
+  BATCH_TRY(cudaMalloc(&b->d_energy, size_t(n) * (2 + D) * sizeof(double)));
+  BATCH_TRY(cudaMalloc(&b->d_next, sizeof(int)));
+  std::vector<uint8_t> fixed_h(static_cast<size_t>(nodes), 0);
+  std::vector<double> coords_h;
+  int64_t noff = 0, poff = 0;
+  b->inst.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const mpm_instance_desc& d = in[i];
+    InstanceP I{};
+    int64_t nn[3] = {1, 1, 1};
+    double dx[3] = {0, 0, 0};
+    for (int a = 0; a < D; ++a) {
+      nn[a] = d.grid.nodes[a];
+      dx[a] = (d.grid.xmax[a] - d.grid.xmin[a]) / (double(d.grid.nodes[a]) - 1.0);  // Grid.jl:105
+      I.g.xmin[a] = d.grid.xmin[a];
+      I.g.dxI[a] = 1.0 / dx[a];
+      I.g.nn[a] = nn[a];
+    }
+    I.g.nx = nn[0];
+    I.g.nxy = nn[0] * nn[1];
+    I.g.nodeCount = I.g.nxy * nn[2];
+    for (int a = 0; a < 3; ++a) {
+      I.g.coord[a] = b->coords + coords_h.size();
+      if (a < D)
+        for (int64_t k = 0; k < nn[a]; ++k) coords_h.push_back(d.grid.xmin[a] + double(k) * dx[a]);
+    }
+    const int64_t Nn = I.g.nodeCount;
+    if (d.grid.fixed_nodes)
+      for (int64_t k = 0; k < Nn; ++k)
+        for (int a = 0; a < D; ++a)
+          if (d.grid.fixed_nodes[a + D * k] == 1) fixed_h[size_t(noff + k)] |= uint8_t(1u << a);
+    NodeP& nd = I.nd;
+    nd.nodeCount = Nn;
+    double* base = b->nodebuf + size_t(noff) * (1 + 4 * D);
+    nd.m = base;
+    nd.p0 = base + Nn;
+    nd.f = base + Nn * (1 + D);
+    nd.vdt = base + Nn * (1 + 2 * D);
+    nd.dv = base + Nn * (1 + 3 * D);
+    if (b->f32) {
+      nd.vdt_f = b->nodebuf_f + size_t(noff) * 2 * D;
+      nd.dv_f = nd.vdt_f + Nn * D;
+    }
+    nd.fixed = b->fixed + noff;
+    for (int a = 0; a < 3; ++a) nd.nn[a] = nn[a];
+    I.pbegin = poff;
+    I.nb = d.nbodies;
+    for (int k = 0; k < d.nbodies; ++k) {
+      const mpm_material_desc& m = d.bodies[k].mat;
+      I.bbeg[k] = poff;
+      I.bcnt[k] = d.bodies[k].count;
+      poff += d.bodies[k].count;
+      MatParams& mp = I.mp[k];
+      mp.type = m.type;
+      mp.per_particle = d.bodies[k].youngs != nullptr;
+      mp.lambda = m.E * m.nu / (1 + m.nu) / (1 - 2 * m.nu);  // Material.jl:54-55
+      mp.mu = m.E / 2 / (1 + m.nu);
+      mp.kappa = mp.lambda + mp.mu;
+      mp.fy = m.fy;
+      mp.k1 = m.k1;
+    }
+    I.pcount = poff - I.pbegin;
+    I.dt = d.dt;
+    I.tol = d.tolerance;
+    for (int a = 0; a < 3; ++a) I.grav[a] = a < D ? d.body_force[a] : 0.0;
+    b->inst[i] = I;
+    noff += Nn;
+  }
+  BATCH_TRY(cudaMemcpy(b->fixed, fixed_h.data(), fixed_h.size(), cudaMemcpyHostToDevice));
+  BATCH_TRY(cudaMemcpy(b->coords, coords_h.data(), coords_h.size() * sizeof(double), cudaMemcpyHostToDevice));
+  BATCH_TRY(cudaMalloc(&b->d_inst, size_t(n) * sizeof(InstanceP)));
+  BATCH_TRY(cudaMemcpy(b->d_inst, b->inst.data(), size_t(n) * sizeof(InstanceP), cudaMemcpyHostToDevice));
+  // work queue order: largest problem first
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->inst[x].pcount > b->inst[y].pcount; });
+  BATCH_TRY(cudaMalloc(&b->d_order, size_t(n) * sizeof(int)));
+  BATCH_TRY(cudaMemcpy(b->d_order, order.data(), size_t(n) * sizeof(int), cudaMemcpyHostToDevice));
+  // particles
+  for (int i = 0; i < n; ++i) {
+    for (int k = 0; k < in[i].nbodies; ++k) {
+      const mpm_body_desc& d = in[i].bodies[k];
+      const PartP pp = b->body(i, k);
+      if (d.count == 0) continue;
+      int r;
+      if ((r = upload(b, pp, d.pos, D, L::X, ident(D)))) return r;
+      if ((r = upload(b, pp, d.velocity, D, L::V, ident(D)))) return r;
+      if ((r = upload(b, pp, d.mass, 1, L::M, ident(1)))) return r;
+      if ((r = upload(b, pp, d.volume, 1, L::VOL, ident(1)))) return r;
+      if ((r = upload(b, pp, d.volume_initial, 1, L::VOL0, ident(1)))) return r;
+      if (d.F) {
+        if ((r = upload(b, pp, d.F, D * D, L::F, ident(D * D)))) return r;
+      } else {
+        std::vector<double> I(size_t(d.count) * D * D, 0.0);
+        for (int64_t p = 0; p < d.count; ++p)
+          for (int a = 0; a < D; ++a) I[p * D * D + a * (D + 1)] = 1.0;
+        if ((r = upload(b, pp, I.data(), D * D, L::F, ident(D * D)))) return r;
+      }
+      if ((r = upload(b, pp, d.strain, D * D, L::EPS, sym_from_full(D)))) return r;
+      if ((r = upload(b, pp, d.stress, D * D, L::SIG, sym_from_full(D)))) return r;
+      if ((r = upload(b, pp, d.alpha, 1, L::ALPHA, ident(1)))) return r;
+      if (d.pstrain) {
+        r = D == 2 ? upload(b, pp, d.pstrain, 3, L::EP, ident(3)) : upload(b, pp, d.pstrain, 9, L::EP, sym_from_full(3));
+        if (r) return r;
+      }
+      if (d.youngs) {
+        std::vector<double> lm(size_t(d.count) * 2);
+        double nu = d.mat.nu;
+        for (int64_t p = 0; p < d.count; ++p) {
+          double E = d.youngs[p];
+          lm[2 * p] = E * nu / (1 + nu) / (1 - 2 * nu);
+          lm[2 * p + 1] = E / 2 / (1 + nu);
+        }
+        if ((r = upload(b, pp, lm.data(), 2, L::LAM, ident(2)))) return r;
+      }
+    }
+  }
+  return MPM_OK;
+}
+
+template <int D>
+int energies_t(mpm_batch* b, double* out) {
+  if (b->f32) batch_energies_kernel<D, float><<<b->ninst, 256, 0, b->stream>>>(b->d_inst, b->P, b->np, b->d_energy);
+  else batch_energies_kernel<D, double><<<b->ninst, 256, 0, b->stream>>>(b->d_inst, b->P, b->np, b->d_energy);
+  BATCH_TRY(cudaGetLastError());
+  BATCH_TRY(cudaMemcpyAsync(out, b->d_energy, size_t(b->ninst) * (2 + D) * sizeof(double), cudaMemcpyDeviceToHost,
+                            b->stream));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  return MPM_OK;
+}
+
+int status_code(unsigned st) {
+  if (st & ST_OUT_OF_GRID) return MPM_ERR_OUT_OF_GRID;
+  if (st & ST_NONFINITE) return MPM_ERR_NONFINITE;
+  if (st & ST_NEGATIVE_J) return MPM_ERR_NEGATIVE_J;
+  return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t precision, mpm_batch** out) {
+  if (!instances || !out || n < 1) return fail(MPM_ERR_ARG, "mpm_batch_create: need at least one problem");
+  *out = nullptr;
+  if (precision != MPM_PREC_F64 && precision != MPM_PREC_F32)
+    return fail(MPM_ERR_ARG, "mpm_batch_create: unknown precision");
+  const int D = instances[0].grid.dim;
+  if (D != 2 && D != 3) return fail(MPM_ERR_ARG, "mpm_batch_create: dim must be 2 or 3");
+  int mat = -1;
+  bool grav = false;
+  for (int i = 0; i < n; ++i) {
+    const mpm_instance_desc& d = instances[i];
+    if (d.grid.dim != D) return fail(MPM_ERR_ARG, "mpm_batch_create: all problems must share the dimension");
+    for (int a = 0; a < D; ++a) {
+      if (d.grid.nodes[a] < 2 || d.grid.nodes[a] > (1 << 20))
+        return fail(MPM_ERR_ARG, "mpm_batch_create: bad node count");
+      if (!(d.grid.xmax[a] > d.grid.xmin[a])) return fail(MPM_ERR_ARG, "mpm_batch_create: need xmax > xmin");
+    }
+    if (!(d.dt > 0.0)) return fail(MPM_ERR_ARG, "mpm_batch_create: dt must be > 0");
+    if (d.nbodies < 1 || d.nbodies > MPM_BATCH_MAX_BODIES || !d.bodies)
+      return fail(MPM_ERR_ARG, "mpm_batch_create: 1 to MPM_BATCH_MAX_BODIES bodies per problem");
+    for (int a = 0; a < D; ++a) grav = grav || d.body_force[a] != 0.0;
+    for (int k = 0; k < d.nbodies; ++k) {
+      const mpm_body_desc& bd = d.bodies[k];
+      if (bd.count < 0) return fail(MPM_ERR_ARG, "mpm_batch_create: negative particle count");
+      if (bd.count > 0 && (!bd.pos || !bd.velocity || !bd.mass || !bd.volume || !bd.volume_initial))
+        return fail(MPM_ERR_ARG, "mpm_batch_create: pos, velocity, mass, volume and volume_initial are required");
+      if (bd.mat.type != MPM_MAT_ELASTIC && bd.mat.type != MPM_MAT_NEOHOOKEAN && bd.mat.type != MPM_MAT_J2)
+        return fail(MPM_ERR_ARG, "mpm_batch_create: unknown material type");
+      if (mat >= 0 && bd.mat.type != mat)
+        return fail(MPM_ERR_ARG, "mpm_batch_create: all bodies of a batch must use the same material model");
+      mat = bd.mat.type;
+    }
+  }
+  mpm_batch* b = new mpm_batch();
+  b->dim = D;
+  b->f32 = precision == MPM_PREC_F32;
+  b->esz = b->f32 ? sizeof(float) : sizeof(double);
+  b->mat = mat < 0 ? MPM_MAT_ELASTIC : mat;
+  b->grav = grav;
+  b->ninst = n;
+  int dev = 0, r = MPM_OK;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->e1);
+  if (e != cudaSuccess) r = fail(MPM_ERR_CUDA, std::string("mpm_batch_create: ") + cudaGetErrorString(e));
+  if (r == MPM_OK) r = D == 2 ? create_t<2>(instances, n, b) : create_t<3>(instances, n, b);
+  if (r != MPM_OK) {
+    std::string msg = mpm_last_error();
+    destroy_batch(b);
+    set_last_error(r, msg);
+    return r;
+  }
+  *out = b;
+  return MPM_OK;
+}
+
+int mpm_batch_step(mpm_batch* b, int64_t nsteps) {
+  if (!b || nsteps < 0) return fail(MPM_ERR_ARG, "mpm_batch_step: bad argument");
+  BATCH_TRY(cudaMemsetAsync(b->d_status, 0, size_t(b->ninst) * sizeof(unsigned), b->stream));
+  BATCH_TRY(cudaEventRecord(b->e0, b->stream));
+  int r = nsteps > 0 ? launch(b, b->P, nsteps, b->threads, b->ctas_per_sm) : MPM_OK;
+  if (r) return r;
+  BATCH_TRY(cudaEventRecord(b->e1, b->stream));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  float ms = 0.f;
+  BATCH_TRY(cudaEventElapsedTime(&ms, b->e0, b->e1));
+  b->last_ms = ms;
+  std::vector<unsigned> st(static_cast<size_t>(b->ninst));
+  BATCH_TRY(cudaMemcpy(st.data(), b->d_status, st.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
+  unsigned all = 0;
+  for (unsigned s : st) all |= s;
+  r = status_code(all);
+  if (r != MPM_OK) return fail(r, "mpm_batch_step: a problem reported a failure (see mpm_batch_status)");
+  return MPM_OK;
+}
+
+int mpm_batch_status(mpm_batch* b, int32_t* status) {
+  if (!b || !status) return fail(MPM_ERR_ARG, "mpm_batch_status: null argument");
+  std::vector<unsigned> st(static_cast<size_t>(b->ninst));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  BATCH_TRY(cudaMemcpy(st.data(), b->d_status, st.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < b->ninst; ++i) status[i] = status_code(st[i]);
+  return MPM_OK;
+}
+
+int mpm_batch_download(mpm_batch* b, int32_t instance, int32_t body, const mpm_body_view* v) {
+  if (!b || !v) return fail(MPM_ERR_ARG, "mpm_batch_download: null argument");
+  if (instance < 0 || instance >= b->ninst || body < 0 || body >= b->inst[instance].nb)
+    return fail(MPM_ERR_ARG, "mpm_batch_download: index out of range");
+  const int D = b->dim;
+  const PartP pp = b->body(instance, body);
+  const int X = 0, V = D, VOL = 2 * D + 1, F = 2 * D + 3, EPS = F + D * D, S = D == 2 ? 3 : 6;
+  const int SIG = EPS + S, VM = SIG + S, ALPHA = VM + 1, EP = ALPHA + 1;
+  int r;
+  if ((r = download(b, pp, v->pos, D, X, ident(D)))) return r;
+  if ((r = download(b, pp, v->velocity, D, V, ident(D)))) return r;
+  if ((r = download(b, pp, v->volume, 1, VOL, ident(1)))) return r;
+  if ((r = download(b, pp, v->F, D * D, F, ident(D * D)))) return r;
+  if ((r = download(b, pp, v->strain, D * D, EPS, full_from_sym(D)))) return r;
+  if ((r = download(b, pp, v->stress, D * D, SIG, full_from_sym(D)))) return r;
+  if ((r = download(b, pp, v->alpha, 1, ALPHA, ident(1)))) return r;
+  if ((r = D == 2 ? download(b, pp, v->pstrain, 3, EP, ident(3)) : download(b, pp, v->pstrain, 9, EP, full_from_sym(3))))
+    return r;
+  if (v->vmstr && pp.count > 0) {
+    if (b->inst[instance].mp[body].type == MPM_MAT_J2) {
+      if (D == 2) Launchers<2>::j2_vm(b->stream, pp, b->f32, b->staging);
+      else Launchers<3>::j2_vm(b->stream, pp, b->f32, b->staging);
+      BATCH_TRY(cudaGetLastError());
+      BATCH_TRY(cudaMemcpyAsync(v->vmstr, b->staging, size_t(pp.count) * sizeof(double), cudaMemcpyDeviceToHost,
+                                b->stream));
+      BATCH_TRY(cudaStreamSynchronize(b->stream));
+    } else if ((r = download(b, pp, v->vmstr, 1, VM, ident(1)))) {
+      return r;
+    }
+  }
+  return MPM_OK;
+}
+
+int mpm_batch_energies(mpm_batch* b, double* out) {
+  if (!b || !out) return fail(MPM_ERR_ARG, "mpm_batch_energies: null argument");
+  return b->dim == 2 ? energies_t<2>(b, out) : energies_t<3>(b, out);
+}
+
+int mpm_batch_set_launch(mpm_batch* b, int32_t threads, int32_t ctas_per_sm) {
+  if (!b || threads < 32 || threads > 1024 || threads % 32 != 0 || ctas_per_sm < 0)
+    return fail(MPM_ERR_ARG, "mpm_batch_set_launch: threads must be a multiple of 32 in [32, 1024]");
+  b->threads = threads;
+  b->ctas_per_sm = ctas_per_sm;
+  return MPM_OK;
+}
+
+int mpm_batch_tune(mpm_batch* b, int64_t probe_steps, int32_t* threads, int32_t* ctas_per_sm, double* ms_per_step) {
+  if (!b || probe_steps < 1) return fail(MPM_ERR_ARG, "mpm_batch_tune: bad argument");
+  const size_t bytes = size_t(b->NF) * size_t(b->np > 0 ? b->np : 1) * b->esz;
+  void* scratch = nullptr;
+  BATCH_TRY(cudaMalloc(&scratch, bytes));
+  const int th_list[] = {64, 128, 256, 512, 1024};
+  const int cta_list[] = {1, 2, 4, 8, 16};
+  double best = 1e300;
+  int bt = b->threads, bc = b->ctas_per_sm;
+  int rc = MPM_OK;
+  for (int th : th_list) {
+    for (int cps : cta_list) {
+      cudaMemcpyAsync(scratch, b->P, bytes, cudaMemcpyDeviceToDevice, b->stream);
+      cudaEventRecord(b->e0, b->stream);
+      int r = launch(b, scratch, probe_steps, th, cps);
+      cudaEventRecord(b->e1, b->stream);
+      cudaError_t e = cudaStreamSynchronize(b->stream);
+      if (e != cudaSuccess) {
+        rc = fail(MPM_ERR_CUDA, std::string("mpm_batch_tune: ") + cudaGetErrorString(e));
+        break;
+      }
+      if (r != MPM_OK) continue;  // shape does not fit this kernel
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, b->e0, b->e1);
+      if (ms < best) {
+        best = ms;
+        bt = th;
+        bc = cps;
+      }
+    }
+    if (rc != MPM_OK) break;
+  }
+  cudaFree(scratch);
+  if (rc != MPM_OK) return rc;
+  b->threads = bt;
+  b->ctas_per_sm = bc;
+  if (threads) *threads = bt;
+  if (ctas_per_sm) *ctas_per_sm = bc;
+  if (ms_per_step) *ms_per_step = best / double(probe_steps);
+  BATCH_TRY(cudaMemsetAsync(b->d_status, 0, size_t(b->ninst) * sizeof(unsigned), b->stream));
+  return MPM_OK;
+}
+
+int mpm_batch_last_ms(mpm_batch* b, double* ms) {
+  if (!b || !ms) return fail(MPM_ERR_ARG, "mpm_batch_last_ms: null argument");
+  *ms = b->last_ms;
+  return MPM_OK;
+}
+
+int mpm_batch_destroy(mpm_batch* b) {
+  if (b) {
+    cudaStreamSynchronize(b->stream);
+    destroy_batch(b);
+  }
+  return MPM_OK;
+}
+
+}  // extern "C"

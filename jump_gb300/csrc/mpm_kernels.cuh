@@ -21,15 +21,15 @@ __device__ __forceinline__ R* field(const PartP& pp, int f, int64_t p) {
 }
 
 // ---------------------------------------------------------------------------
-// P2G
+// P2G of particle pp.begin + t.  All 32 lanes of a warp call it together
+// (t consecutive across the warp); lanes with t >= pp.count do nothing.
 template <int D, class R, bool GRAV>
-__global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
-                                                  double gz, unsigned* status) {
+__device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
+                                             double gx, double gy, double gz, unsigned* status) {
   using L = Layout<D>;
   constexpr int NV = 1 + 3 * D;  // per node: m, p0 (D), f (D), normal (D, contact mode)
   constexpr bool WARP_SUM = sizeof(R) == 4;
   const bool NRM = nd.nrm != nullptr;
-  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   // lanes of this warp holding a particle (a contiguous low range)
   const unsigned mask = __ballot_sync(0xffffffffu, t < pp.count);
   if (t >= pp.count) return;
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, d
       }
     }
     if (ok && head) {
-      if (k == 0) mark_blocks<D>(nd, h.c);
+      if (k == 0 && nd.bflag) mark_blocks<D>(nd, h.c);
       int64_t n = cr.node[k];
       atomicAdd(nd.m + n, to_f64(val[0]));
 #pragma unroll
@@ -122,6 +122,12 @@ __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, d
         for (int a = 0; a < D; ++a) atomicAdd(nd.nrm + a * Nn + n, to_f64(val[1 + 2 * D + a]));
     }
   }
+}
+
+template <int D, class R, bool GRAV>
+__global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
+                                                  double gz, unsigned* status) {
+  p2g_particle<D, R, GRAV>(g, nd, pp, int64_t(blockIdx.x) * blockDim.x + threadIdx.x, gx, gy, gz, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -237,10 +243,19 @@ __global__ void __launch_bounds__(256) contact_grid_kernel(NodeP nd, ContactP cp
 
 // ---------------------------------------------------------------------------
 // Grid update (:429-442) + nodal velocities for G2P, for node i.
-template <int D, bool F32COPY>
+// Node data written earlier in the same kernel (the persistent batch kernel)
+// must be read through L2 (CG); data from an earlier launch may use the
+// read-only path.
+template <bool CG, class T>
+__device__ __forceinline__ T nload(const T* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return __ldg(p);
+}
+
+template <int D, bool F32COPY, bool CG = false>
 __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt, double tol) {
   const int64_t Nn = nd.nodeCount;
-  double m = nd.m[i];
+  double m = CG ? __ldcg(nd.m + i) : nd.m[i];
   if (!(m > tol)) {
     // empty or near-empty node: G2P skips it (:510); no FP64 work here
 #pragma unroll
@@ -260,8 +275,9 @@ __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt,
   double invM = 1.0 / m;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    double p0 = nd.p0[a * Nn + i];
-    double p = __dadd_rn(p0, __dmul_rn(nd.f[a * Nn + i], dt));  // p = p0 + f*dt
+    double p0 = CG ? __ldcg(nd.p0 + a * Nn + i) : nd.p0[a * Nn + i];
+    double fa = CG ? __ldcg(nd.f + a * Nn + i) : nd.f[a * Nn + i];
+    double p = __dadd_rn(p0, __dmul_rn(fa, dt));  // p = p0 + f*dt
     if (fx & (1u << a)) {
       p0 = 0.0;
       p = 0.0;
@@ -437,13 +453,11 @@ __device__ __forceinline__ double det_d(const double* A) {
 }
 
 // ---------------------------------------------------------------------------
-// G2P + kinematics + stress, one thread per particle.
-template <int D, class R, int MAT>
-__global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, double dt,
-                                                  unsigned* status) {
+// G2P + kinematics + stress of particle pp.begin + t (t < pp.count).
+template <int D, class R, int MAT, bool CG = false>
+__device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
+                                             const MatParams& mp, double dt, unsigned* status) {
   using L = Layout<D>;
-  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= pp.count) return;
   int64_t p = pp.begin + t;
   R x[D];
 #pragma unroll
@@ -473,8 +487,8 @@ __global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, M
     R vd[D], dvv[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      vd[a] = __ldg(vdt_n + a * Nn + n);
-      dvv[a] = __ldg(dv_n + a * Nn + n);
+      vd[a] = nload<CG>(vdt_n + a * Nn + n);
+      dvv[a] = nload<CG>(dv_n + a * Nn + n);
     }
 #pragma unroll
     for (int a = 0; a < D; ++a) {
@@ -569,6 +583,13 @@ __global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, M
   for (int a = 0; a < D; ++a) fin &= finite_bits(x[a]) & finite_bits(v[a]);
   unsigned st = (positive_bits(J) ? 0u : ST_NEGATIVE_J) | (fin ? 0u : ST_NONFINITE);
   if (st) atomicOr(status, st);
+}
+
+template <int D, class R, int MAT>
+__global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, double dt,
+                                                  unsigned* status) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t < pp.count) g2p_particle<D, R, MAT>(g, nd, pp, t, mp, dt, status);
 }
 
 // ---------------------------------------------------------------------------

@@ -105,10 +105,13 @@ def cantilever(h: float = 0.0625, ppc: int = 4, length: float = 4.0, depth: floa
     return grid, [s], USL(1e-9), data
 
 
-def ensemble_member(i: int, seed: int = 0):
+def ensemble_member(i: int, seed: int = 0, gap=None):
     """Instance i of the seeded two-disk ensemble: radii in [0.1, 0.25],
     20..80 cells per axis, 4 particles per cell, E in [500, 5000], speed in
-    [0.05, 0.2], dt = 5e-4."""
+    [0.05, 0.2], dt = 5e-4.  The disks start at (0.3, 0.3) and (0.7, 0.7), or,
+    with ``gap``, along that diagonal with their rims ``gap`` apart.  The nodal
+    mass cutoff is 1e-3 particle masses (with 1e-9 some seeded problems run
+    away once the disks collide)."""
     rng = np.random.default_rng([seed, i])
     r1, r2 = rng.uniform(0.1, 0.25, 2)
     cells = int(rng.integers(20, 81))
@@ -116,8 +119,12 @@ def ensemble_member(i: int, seed: int = 0):
     speed = float(rng.uniform(0.05, 0.2))
     grid = Grid2D(0.0, 1.0, 0.0, 1.0, cells + 1, cells + 1)
     off = grid.dx / 2
-    c1 = buildParticleForCircle([0.3, 0.3], float(r1), off)
-    c2 = buildParticleForCircle([0.7, 0.7], float(r2), off)
+    p1, p2 = (0.3, 0.3), (0.7, 0.7)
+    if gap is not None:
+        d = (float(r1) + float(r2) + gap) / math.sqrt(2.0)
+        p1, p2 = (0.5 - 0.5 * d, 0.5 - 0.5 * d), (0.5 + 0.5 * d, 0.5 + 0.5 * d)
+    c1 = buildParticleForCircle(list(p1), float(r1), off)
+    c2 = buildParticleForCircle(list(p2), float(r2), off)
     mat = ElasticMaterial(E, 0.3, 1000.0, 0, 0, max(len(c1), len(c2)))
     s1, s2 = Solid2D(c1, mat), Solid2D(c2, mat)
     for s in (s1, s2):
@@ -127,7 +134,7 @@ def ensemble_member(i: int, seed: int = 0):
     data = {"total_time": 1000 * 5e-4, "dt": 5e-4, "time": 0.0,
             "bodyforce": ConstantBodyForce2D([0.0, 0.0]),
             "dirichlet_grid": [("bottom", (1, 1)), ("top", (1, 1)), ("left", (1, 1)), ("right", (1, 1))]}
-    return grid, [s1, s2], USL(1e-9), data
+    return grid, [s1, s2], USL(1e-3 * float(s1.mass[0])), data
 
 
 def apply_dirichlet(grid, data):
