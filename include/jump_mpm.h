@@ -168,6 +168,28 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
 int mpm_destroy(mpm_ctx* ctx);
 
 /* ---------------------------------------------------------------------------
+ * Reverse mode (no counterpart in the reference): gradients of a loss on the
+ * final particle state with respect to the initial velocities and positions
+ * and to a per-particle Young's modulus, through hand-written adjoint
+ * kernels of every stage.  Built for FP64 contexts with one velocity field,
+ * no sorting and neo-Hookean bodies; otherwise MPM_ERR_UNSUPPORTED.
+ * The derivative is that of the discrete map inside the particles' current
+ * cells (the hat basis has kinks at nodes and cell faces).
+ * ------------------------------------------------------------------------- */
+/* Advance nsteps steps keeping a snapshot of the particle state every
+   `checkpoint_every` steps (and the final state) in device memory. */
+int mpm_fwd_checkpointed(mpm_ctx* ctx, int64_t nsteps, int32_t checkpoint_every);
+/* Reverse sweep over the last mpm_fwd_checkpointed run: each segment is
+   recomputed from its snapshot, then differentiated step by step.
+     x_bar, v_bar  dL/dx and dL/dv at the final step (v_bar may be NULL),
+                   all bodies in order, dim doubles per particle
+     E_bar         out: dL/dE per particle (count doubles), or NULL
+     v0_bar, x0_bar out: dL/dv, dL/dx at the initial step, or NULL
+   The context is left at the final state of the forward run. */
+int mpm_bwd(mpm_ctx* ctx, const double* x_bar, const double* v_bar, double* E_bar, double* v0_bar,
+            double* x0_bar);
+
+/* ---------------------------------------------------------------------------
  * Batched ensembles (no counterpart in the reference, which solves one
  * problem per call): many independent problems -- each what one
  * solve_explicit_dynamics_2D/3D call would take -- advance together in one

@@ -147,6 +147,8 @@ SIGNATURES = {
     "mpm_destroy": (C.c_int, [C.c_void_p]),
     "mpm_energies_static": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mpm_fwd_checkpointed": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),
+    "mpm_bwd": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
     "mpm_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "mpm_batch_step": (C.c_int, [C.c_void_p, C.c_int64]),
     "mpm_batch_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),

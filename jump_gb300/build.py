@@ -27,7 +27,8 @@ NVCC_FLAGS = ARCH + [
 ]
 
 SOURCES = ["mpm_k2d.cu", "mpm_k3d.cu", "mpm_capi.cu", "mpm_static.cu", "mpm_batch.cu"]
-HEADERS = ["mpm_common.cuh", "mpm_kernels.cuh", "mpm_launch.cuh", "mpm_internal.h", "mpm_sparse.cuh"]
+HEADERS = ["mpm_common.cuh", "mpm_kernels.cuh", "mpm_launch.cuh", "mpm_internal.h", "mpm_sparse.cuh",
+           "mpm_adjoint.cuh"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,371 @@
+// mpm_adjoint.cuh -- reverse-mode (adjoint) kernels of one USL step, FP64,
+// single velocity field, neo-Hookean bodies (the material of the inverse
+// problems this serves), D = 2, 3.
+//
+// State of a step n: (x, v, F) per particle, with sigma = NH(F; lambda_p,
+// mu_p) and V = det(F) V0 derived from F.  The forward step (mpm_kernels.cuh)
+//   P2G   m_I = sum w m_p,  p0_I = sum w m_p v_p,  f_I = sum (-V sigma g + m_p b w)
+//   grid  vdt = dt (p0 + dt f)/m,  dv = dt f/m   (free dofs of nodes with m > tol)
+//   G2P   v' = v + sum w dv,  x' = x + sum w vdt,  Ldt = sum vdt (x) g,
+//         F' = F (I + Ldt)
+// is differentiated exactly within the particles' current cells: w = N(x),
+// g = grad N(x), H = grad grad N(x) (zero diagonal for the hat product).
+// Reverse of step n, given the adjoints (x', v', F') of step n + 1:
+//   g2p_adj   F_ = F' (I + Ldt)^T,  Abar = F^T F',  scatter vdt_I += w x' + Abar g,
+//             dv_I += w v',  x_ = x' + sum (w_ g + H g_)   (w_ = x'.vdt + v'.dv,
+//             g_ = Abar^T vdt)
+//   grid_adj  p0_ = dt vdt_/m,  f_ = dt (dt vdt_ + dv_)/m,  m_ = -sum (vdt_ vdt + dv_ dv)/m
+//   p2g_adj   w_ = m_p (m_ + v.p0_ + b.f_),  v_ += m_p sum w p0_,  g_ = -V sigma^T f_,
+//             sigma_ = -V sum f_ (x) g,  V_ = -sum f_.(sigma g);  then
+//             F_ += dNH/dF^T sigma_ + V_ V0 J F^-T,  E_ += c1 lambda_ + c2 mu_
+// (c1 = dlambda/dE, c2 = dmu/dE).  Trailing underscore = adjoint.
+#pragma once
+
+#include "mpm_common.cuh"
+
+namespace jmpm {
+
+// particle adjoints, SoA (component-major) with pitch = particle count:
+// x_ (D) | v_ (D) | F_ (D*D, column-major) | E_ (1)
+template <int D>
+struct AdjLayout {
+  static constexpr int XB = 0, VB = D, FB = 2 * D, EB = 2 * D + D * D, NF = 2 * D + D * D + 1;
+};
+
+struct AdjP {
+  double* base;
+  int64_t pitch;
+};
+
+// node adjoints: vdt_ (D) | dv_ (D) accumulated by g2p_adj; m_ | p0_ (D) | f_ (D) from grid_adj
+struct NodeAdjP {
+  double* vdtb;
+  double* dvb;
+  double* mb;
+  double* p0b;
+  double* fb;
+  int64_t nodeCount;
+};
+
+// forward grid outputs recorded for step n: m | vdt (D) | dv (D), component-major
+struct GridRec {
+  const double* m;
+  const double* vdt;
+  const double* dv;
+};
+
+template <int D>
+struct CornersFull {
+  int64_t node[1 << D];
+  double N[1 << D];
+  double g[1 << D][D];
+  double H[1 << D][3];  // xy, xz, yz
+};
+
+template <int D>
+__device__ __forceinline__ void corners_full(const GridP& gp, const Hat<D, double>& h, CornersFull<D>& c) {
+  int64_t base = int64_t(h.c[0]) + gp.nx * int64_t(h.c[1]);
+  if constexpr (D == 3) base += gp.nxy * int64_t(h.c[2]);
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) {
+    const int bx = k & 1, by = (k >> 1) & 1, bz = (k >> 2) & 1;
+    const double Nx = bx ? h.Nh[0] : h.Nl[0], gx = bx ? h.gh[0] : h.gl[0];
+    const double Ny = by ? h.Nh[1] : h.Nl[1], gy = by ? h.gh[1] : h.gl[1];
+    if constexpr (D == 2) {
+      c.N[k] = Nx * Ny;
+      c.g[k][0] = gx * Ny;
+      c.g[k][1] = Nx * gy;
+      c.H[k][0] = gx * gy;
+      c.H[k][1] = c.H[k][2] = 0.0;
+      c.node[k] = base + bx + gp.nx * by;
+    } else {
+      const double Nz = bz ? h.Nh[2] : h.Nl[2], gz = bz ? h.gh[2] : h.gl[2];
+      c.N[k] = Nx * Ny * Nz;
+      c.g[k][0] = gx * Ny * Nz;
+      c.g[k][1] = Nx * gy * Nz;
+      c.g[k][2] = Nx * Ny * gz;
+      c.H[k][0] = gx * gy * Nz;
+      c.H[k][1] = gx * Ny * gz;
+      c.H[k][2] = Nx * gy * gz;
+      c.node[k] = base + bx + gp.nx * by + gp.nxy * bz;
+    }
+  }
+}
+
+// x_ += w_ g + H g_
+template <int D>
+__device__ __forceinline__ void add_shape_adj(double* xb, const CornersFull<D>& c, int k, double wb, const double* gb) {
+#pragma unroll
+  for (int a = 0; a < D; ++a) xb[a] += wb * c.g[k][a];
+  xb[0] += c.H[k][0] * gb[1];
+  xb[1] += c.H[k][0] * gb[0];
+  if constexpr (D == 3) {
+    xb[0] += c.H[k][1] * gb[2];
+    xb[2] += c.H[k][1] * gb[0];
+    xb[1] += c.H[k][2] * gb[2];
+    xb[2] += c.H[k][2] * gb[1];
+  }
+}
+
+template <int D>
+__device__ __forceinline__ double* adj(const AdjP& ad, int f, int64_t p) {
+  return ad.base + int64_t(f) * ad.pitch + p;
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, PartP pp, AdjP ad, NodeAdjP na) {
+  using L = Layout<D>;
+  using A = AdjLayout<D>;
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  const int64_t p = pp.begin + t;
+  const double* P = static_cast<const double*>(pp.base);
+  double x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = P[int64_t(L::X + a) * pp.pitch + p];
+  Hat<D, double> h;
+  if (!hat<D, double>(gp, x, h)) return;  // frozen particle: its adjoints pass through unchanged
+  CornersFull<D> c;
+  corners_full<D>(gp, h, c);
+  const int64_t Nn = na.nodeCount;
+  double vdt[1 << D][D], dv[1 << D][D];
+  double Ldt[D][D];
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int b = 0; b < D; ++b) Ldt[a][b] = 0.0;
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k)
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      vdt[k][a] = gr.vdt[a * Nn + c.node[k]];
+      dv[k][a] = gr.dv[a * Nn + c.node[k]];
+#pragma unroll
+      for (int b = 0; b < D; ++b) Ldt[a][b] += vdt[k][a] * c.g[k][b];
+    }
+  double F[D * D], Fb[D * D], xb[D], vb[D];
+#pragma unroll
+  for (int q = 0; q < D * D; ++q) {
+    F[q] = P[int64_t(L::F + q) * pp.pitch + p];
+    Fb[q] = *adj<D>(ad, A::FB + q, p);
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    xb[a] = *adj<D>(ad, A::XB + a, p);
+    vb[a] = *adj<D>(ad, A::VB + a, p);
+  }
+  // Abar = F^T F', F_ = F' A^T with A = I + Ldt (column-major F[i + D j])
+  double Ab[D][D], Fn[D * D];
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < D; ++i) s += F[i + D * k] * Fb[i + D * j];
+      Ab[k][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < D; ++j) s += Fb[i + D * j] * ((k == j ? 1.0 : 0.0) + Ldt[k][j]);
+      Fn[i + D * k] = s;
+    }
+  double xn[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) xn[a] = xb[a];
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) {
+    double wb = 0.0, gb[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) wb += xb[a] * vdt[k][a] + vb[a] * dv[k][a];
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      double s = 0.0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) s += Ab[a][b] * vdt[k][a];
+      gb[b] = s;
+    }
+    const int64_t n = c.node[k];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double s = c.N[k] * xb[a];
+#pragma unroll
+      for (int b = 0; b < D; ++b) s += Ab[a][b] * c.g[k][b];
+      atomicAdd(na.vdtb + a * Nn + n, s);
+      atomicAdd(na.dvb + a * Nn + n, c.N[k] * vb[a]);
+    }
+    add_shape_adj<D>(xn, c, k, wb, gb);
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) *adj<D>(ad, A::XB + a, p) = xn[a];
+#pragma unroll
+  for (int q = 0; q < D * D; ++q) *adj<D>(ad, A::FB + q, p) = Fn[q];
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, const uint8_t* fixed, double dt,
+                                                       double tol) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t Nn = na.nodeCount;
+  if (i >= Nn) return;
+  const double m = gr.m[i];
+  double mb = 0.0;
+  const unsigned fx = fixed[i];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    double p0b = 0.0, fb = 0.0;
+    if (m > tol && !(fx & (1u << a))) {
+      const double vdtb = na.vdtb[a * Nn + i], dvb = na.dvb[a * Nn + i];
+      p0b = dt * vdtb / m;
+      fb = (dt * dt * vdtb + dt * dvb) / m;
+      mb -= (vdtb * gr.vdt[a * Nn + i] + dvb * gr.dv[a * Nn + i]) / m;
+    }
+    na.p0b[a * Nn + i] = p0b;
+    na.fb[a * Nn + i] = fb;
+  }
+  na.mb[i] = mb;
+}
+
+template <int D>
+__device__ __forceinline__ void inv_det(const double* F, double* Fi, double& J) {
+  if constexpr (D == 2) {
+    J = F[0] * F[3] - F[2] * F[1];
+    const double iJ = 1.0 / J;
+    Fi[0] = F[3] * iJ;
+    Fi[3] = F[0] * iJ;
+    Fi[2] = -F[2] * iJ;
+    Fi[1] = -F[1] * iJ;
+  } else {
+    const double c00 = F[4] * F[8] - F[7] * F[5], c02 = F[1] * F[5] - F[4] * F[2];
+    J = F[0] * c00 - F[3] * (F[1] * F[8] - F[2] * F[7]) + F[6] * c02;
+    const double iJ = 1.0 / J;
+    // inverse via the adjugate (column-major: Fi[i + 3 j] = (F^-1)_ij)
+    Fi[0] = c00 * iJ;
+    Fi[1] = -(F[1] * F[8] - F[2] * F[7]) * iJ;
+    Fi[2] = c02 * iJ;
+    Fi[3] = -(F[3] * F[8] - F[5] * F[6]) * iJ;
+    Fi[4] = (F[0] * F[8] - F[2] * F[6]) * iJ;
+    Fi[5] = -(F[0] * F[5] - F[2] * F[3]) * iJ;
+    Fi[6] = (F[3] * F[7] - F[4] * F[6]) * iJ;
+    Fi[7] = -(F[0] * F[7] - F[1] * F[6]) * iJ;
+    Fi[8] = (F[0] * F[4] - F[1] * F[3]) * iJ;
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) p2g_adj_kernel(GridP gp, PartP pp, AdjP ad, NodeAdjP na, MatParams mp,
+                                                      double c1, double c2, double bx, double by, double bz) {
+  using L = Layout<D>;
+  using A = AdjLayout<D>;
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  const int64_t p = pp.begin + t;
+  const double* P = static_cast<const double*>(pp.base);
+  auto fld = [&](int f) { return P[int64_t(f) * pp.pitch + p]; };
+  double x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = fld(L::X + a);
+  Hat<D, double> h;
+  if (!hat<D, double>(gp, x, h)) return;
+  CornersFull<D> c;
+  corners_full<D>(gp, h, c);
+  const double mpart = fld(L::M), V = fld(L::VOL), V0 = fld(L::VOL0);
+  double v[D], sig[D][D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) v[a] = fld(L::V + a);
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int b = 0; b < D; ++b) sig[a][b] = fld(L::SIG + sym<D>(a, b));
+  const double grav[3] = {bx, by, bz};
+  double xb[D], vb[D], sb[D][D], Vb = 0.0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    xb[a] = *adj<D>(ad, A::XB + a, p);
+    vb[a] = *adj<D>(ad, A::VB + a, p);
+#pragma unroll
+    for (int b = 0; b < D; ++b) sb[a][b] = 0.0;
+  }
+  const int64_t Nn = na.nodeCount;
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) {
+    const int64_t n = c.node[k];
+    const double mb = na.mb[n];
+    double p0b[D], fb[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      p0b[a] = na.p0b[a * Nn + n];
+      fb[a] = na.fb[a * Nn + n];
+    }
+    double wb = mpart * mb, gb[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      wb += mpart * (v[a] * p0b[a] + grav[a] * fb[a]);
+      vb[a] += mpart * c.N[k] * p0b[a];
+    }
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      double s = 0.0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) s += sig[a][b] * fb[a];
+      gb[b] = -V * s;
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double sg = 0.0;
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        sb[a][b] -= V * fb[a] * c.g[k][b];
+        sg += sig[a][b] * c.g[k][b];
+      }
+      Vb -= fb[a] * sg;
+    }
+    add_shape_adj<D>(xb, c, k, wb, gb);
+  }
+  // sigma = NH(F) = (mu (F F^T - I) + lambda ln J I) / J ;  V = J V0
+  double F[D * D], Fi[D * D], J;
+#pragma unroll
+  for (int q = 0; q < D * D; ++q) F[q] = fld(L::F + q);
+  inv_det<D>(F, Fi, J);
+  double lam = mp.lambda, mu = mp.mu;
+  if (mp.per_particle) {
+    lam = fld(L::LAM);
+    mu = fld(L::MU);
+  }
+  const double lnJ = log(J), iJ = 1.0 / J;
+  double trS = 0.0, SB = 0.0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    trS += sb[a][a];
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      double Bab = 0.0;
+#pragma unroll
+      for (int q = 0; q < D; ++q) Bab += F[a + D * q] * F[b + D * q];
+      SB += sb[a][b] * (Bab - (a == b ? 1.0 : 0.0));
+    }
+  }
+  // F_ += (mu/J)[(S + S^T) F - (S:(B - I)) F^-T] + lambda trS (1 - ln J)/J F^-T + V_ V0 J F^-T
+  const double cinvT = -mu * iJ * SB + lam * trS * (1.0 - lnJ) * iJ + Vb * V0 * J;
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int q = 0; q < D; ++q) {
+      double s = 0.0;
+#pragma unroll
+      for (int b = 0; b < D; ++b) s += (sb[a][b] + sb[b][a]) * F[b + D * q];
+      *adj<D>(ad, A::FB + a + D * q, p) += mu * iJ * s + cinvT * Fi[q + D * a];
+    }
+  *adj<D>(ad, A::EB, p) += c1 * (trS * lnJ * iJ) + c2 * (SB * iJ);
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    *adj<D>(ad, A::XB + a, p) = xb[a];
+    *adj<D>(ad, A::VB + a, p) = vb[a];
+  }
+}
+
+}  // namespace jmpm

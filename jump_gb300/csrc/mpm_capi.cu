@@ -76,6 +76,16 @@ struct mpm_ctx {
   double* coords = nullptr;
   uint8_t* fixed = nullptr;
   uint32_t* blockbuf = nullptr;  // node-block flags | list | count
+  std::vector<double> nus;       // Poisson ratio per body (dlambda/dE, dmu/dE of the adjoint)
+  // reverse mode: checkpoints of mpm_fwd_checkpointed and the adjoint work buffers
+  char* ckpt = nullptr;
+  int64_t ckpt_slots = 0, adj_nsteps = -1;
+  int32_t adj_every = 0;
+  char* segbuf = nullptr;
+  int32_t segbuf_slots = 0;
+  double* gridrec = nullptr;
+  double* adjbuf = nullptr;
+  double* nodeadj = nullptr;
   ContactP cp{};                 // contact mode: per-body node fields
   double* contactbuf = nullptr;
   float* contactbuf_f = nullptr;
@@ -133,6 +143,11 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->nodebuf);
   cudaFree(c->nodebuf_f);
   cudaFree(c->blockbuf);
+  cudaFree(c->ckpt);
+  cudaFree(c->segbuf);
+  cudaFree(c->gridrec);
+  cudaFree(c->adjbuf);
+  cudaFree(c->nodeadj);
   cudaFree(c->contactbuf);
   cudaFree(c->contactbuf_f);
   cudaFree(c->status);
@@ -232,7 +247,8 @@ bool symmetric(const double* a, int64_t n, int dim) {
 }
 
 // The launches of one USL step; ev (optional) gets an event recorded after each stage.
-void enqueue_step(mpm_ctx* c, cudaEvent_t* ev) {
+// rec (optional): receives this step's grid outputs m | vdt (D) | dv (D) for the adjoint
+void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
   const int D = c->dim;
   const bool contact = c->prm.contact != 0;
   // node field of body b: its own in contact mode, else the shared one
@@ -255,6 +271,11 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev) {
   } else {
     if (D == 2) Launchers<2>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
     else Launchers<3>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
+  }
+  if (rec) {
+    const size_t Nn = size_t(c->nd.nodeCount);
+    cudaMemcpyAsync(rec, c->nd.m, Nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(rec + Nn, c->nd.vdt, 2 * D * Nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   }
   if (ev) cudaEventRecord(ev[2], c->stream);
   for (int b = 0; b < c->nb; ++b) {
@@ -409,6 +430,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     mp.fy = m.fy;
     mp.k1 = m.k1;
     c->mats.push_back(mp);
+    c->nus.push_back(m.nu);
   }
   size_t ptot = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1);
   CUDA_TRY(cudaMalloc(&c->P, ptot * c->esz));
@@ -735,6 +757,151 @@ int mpm_profile_stages(mpm_ctx* c, int64_t nsteps, double* stage_ms) {
   unsigned st = 0;
   CUDA_TRY(cudaMemcpy(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
   return status_to_code(st);
+}
+
+int mpm_fwd_checkpointed(mpm_ctx* c, int64_t nsteps, int32_t every) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: null context");
+  if (nsteps < 1 || every < 1) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: need nsteps >= 1, every >= 1");
+  if (c->f32 || c->prm.contact || c->prm.sort_interval > 0)
+    return fail(MPM_ERR_UNSUPPORTED,
+                "mpm_fwd_checkpointed: reverse mode needs FP64 particles, one velocity field and no sorting");
+  for (const MatParams& m : c->mats)
+    if (m.type != MPM_MAT_NEOHOOKEAN)
+      return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode is built for neo-Hookean bodies");
+  const size_t bytes = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1) * c->esz;
+  const int64_t slots = (nsteps + every - 1) / every + 1;  // steps 0, every, ... and the final state
+  if (slots != c->ckpt_slots) {
+    cudaFree(c->ckpt);
+    c->ckpt = nullptr;
+    c->ckpt_slots = 0;
+    CUDA_TRY(cudaMalloc(&c->ckpt, bytes * size_t(slots)));
+    c->ckpt_slots = slots;
+  }
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->ckpt, c->P, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  int r;
+  if ((r = build_step_graph(c))) return r;
+  for (int64_t k = 1; k <= nsteps; ++k) {
+    CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
+    if (k % every == 0 && k < nsteps)
+      CUDA_TRY(cudaMemcpyAsync(c->ckpt + bytes * size_t(k / every), c->P, bytes, cudaMemcpyDeviceToDevice,
+                               c->stream));
+  }
+  CUDA_TRY(cudaMemcpyAsync(c->ckpt + bytes * size_t(slots - 1), c->P, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  unsigned st = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->adj_nsteps = nsteps;
+  c->adj_every = every;
+  return status_to_code(st);
+}
+
+int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar, double* v0_bar, double* x0_bar) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_bwd: null context");
+  if (c->adj_nsteps < 1) return fail(MPM_ERR_ARG, "mpm_bwd: run mpm_fwd_checkpointed first");
+  const int D = c->dim;
+  const int every = c->adj_every;
+  const int64_t nsteps = c->adj_nsteps;
+  const int64_t Nn = c->nd.nodeCount;
+  const size_t bytes = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1) * c->esz;
+  const int ANF = D == 2 ? AdjLayout<2>::NF : AdjLayout<3>::NF;
+  const int XB = 0, VB = D, EB = 2 * D + D * D;
+  if (c->segbuf_slots < every) {
+    cudaFree(c->segbuf);
+    cudaFree(c->gridrec);
+    c->segbuf = nullptr;
+    c->gridrec = nullptr;
+    c->segbuf_slots = 0;
+    CUDA_TRY(cudaMalloc(&c->segbuf, bytes * size_t(every)));
+    CUDA_TRY(cudaMalloc(&c->gridrec, size_t(Nn) * (1 + 2 * D) * sizeof(double) * size_t(every)));
+    c->segbuf_slots = every;
+  }
+  if (!c->adjbuf) {
+    CUDA_TRY(cudaMalloc(&c->adjbuf, size_t(ANF) * size_t(c->np > 0 ? c->np : 1) * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&c->nodeadj, size_t(Nn) * (1 + 4 * D) * sizeof(double)));
+  }
+  CUDA_TRY(cudaMemsetAsync(c->adjbuf, 0, size_t(ANF) * size_t(c->np > 0 ? c->np : 1) * sizeof(double), c->stream));
+  // adjoints at the final step, per body AoS -> component-major SoA
+  auto adj_part = [&](int b) { return PartP{c->adjbuf, c->np, c->off[b], c->cnt[b]}; };
+  int64_t base = 0;
+  for (int b = 0; b < c->nb; ++b) {
+    const size_t n = size_t(c->cnt[b]) * D;
+    for (int which = 0; which < 2; ++which) {
+      const double* src = which == 0 ? x_bar : v_bar;
+      if (!src || n == 0) continue;
+      CUDA_TRY(cudaMemcpyAsync(c->staging, src + base * D, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      if (D == 2) Launchers<2>::aos_to_soa(c->stream, adj_part(b), false, c->staging, D, which == 0 ? XB : VB, ident(D));
+      else Launchers<3>::aos_to_soa(c->stream, adj_part(b), false, c->staging, D, which == 0 ? XB : VB, ident(D));
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    base += c->cnt[b];
+  }
+  const AdjP ad{c->adjbuf, c->np};
+  NodeAdjP na;
+  na.nodeCount = Nn;
+  na.vdtb = c->nodeadj;
+  na.dvb = c->nodeadj + Nn * D;
+  na.mb = c->nodeadj + Nn * 2 * D;
+  na.p0b = c->nodeadj + Nn * (1 + 2 * D);
+  na.fb = c->nodeadj + Nn * (1 + 3 * D);
+  const int64_t nseg = c->ckpt_slots - 1;
+  void* Pwork = c->P;
+  for (int64_t seg = nseg - 1; seg >= 0; --seg) {
+    const int64_t n0 = seg * every;
+    const int len = int(std::min<int64_t>(every, nsteps - n0));
+    // recompute the segment from its checkpoint, recording each step's state and grid
+    CUDA_TRY(cudaMemcpyAsync(Pwork, c->ckpt + bytes * size_t(seg), bytes, cudaMemcpyDeviceToDevice, c->stream));
+    for (int j = 0; j < len; ++j) {
+      CUDA_TRY(cudaMemcpyAsync(c->segbuf + bytes * size_t(j), Pwork, bytes, cudaMemcpyDeviceToDevice, c->stream));
+      enqueue_step(c, nullptr, c->gridrec + size_t(Nn) * (1 + 2 * D) * size_t(j));
+    }
+    // reverse sweep over the segment
+    for (int j = len - 1; j >= 0; --j) {
+      const double* rec = c->gridrec + size_t(Nn) * (1 + 2 * D) * size_t(j);
+      const GridRec gr{rec, rec + Nn, rec + Nn * (1 + D)};
+      CUDA_TRY(cudaMemsetAsync(c->nodeadj, 0, size_t(Nn) * 2 * D * sizeof(double), c->stream));
+      for (int b = 0; b < c->nb; ++b) {
+        const PartP ps{c->segbuf + bytes * size_t(j), c->np, c->off[b], c->cnt[b]};
+        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
+        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
+      }
+      if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
+      else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
+      for (int b = 0; b < c->nb; ++b) {
+        const PartP ps{c->segbuf + bytes * size_t(j), c->np, c->off[b], c->cnt[b]};
+        const double nu = c->nus[b];
+        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);  // dlambda/dE, dmu/dE
+        if (D == 2) Launchers<2>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
+        else Launchers<3>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
+      }
+      CUDA_TRY(cudaGetLastError());
+    }
+  }
+  // gradients in original particle order (no sorting in reverse mode)
+  base = 0;
+  for (int b = 0; b < c->nb; ++b) {
+    const int64_t n = c->cnt[b];
+    struct Out {
+      double* dst;
+      int per, f0;
+    } outs[3] = {{E_bar ? E_bar + base : nullptr, 1, EB},
+                 {v0_bar ? v0_bar + base * D : nullptr, D, VB},
+                 {x0_bar ? x0_bar + base * D : nullptr, D, XB}};
+    for (const Out& o : outs) {
+      if (!o.dst || n == 0) continue;
+      if (D == 2) Launchers<2>::soa_to_aos(c->stream, adj_part(b), false, c->staging, o.per, o.f0, ident(o.per));
+      else Launchers<3>::soa_to_aos(c->stream, adj_part(b), false, c->staging, o.per, o.f0, ident(o.per));
+      CUDA_TRY(cudaMemcpyAsync(o.dst, c->staging, size_t(n) * o.per * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    base += n;
+  }
+  // leave the context at the final state of the forward run
+  CUDA_TRY(cudaMemcpyAsync(c->P, c->ckpt + bytes * size_t(c->ckpt_slots - 1), bytes, cudaMemcpyDeviceToDevice,
+                           c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
 }
 
 int mpm_destroy(mpm_ctx* c) {

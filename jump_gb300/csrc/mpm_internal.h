@@ -7,6 +7,7 @@
 #include <string>
 
 #include "mpm_common.cuh"
+#include "mpm_adjoint.cuh"
 
 namespace jmpm {
 
@@ -23,6 +24,13 @@ struct Launchers {
   static void grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy);
   // zero the accumulators of the blocks listed by the previous grid stage
   static void clear(cudaStream_t s, const NodeP& nd);
+  // adjoint of one step (mpm_adjoint.cuh), FP64 particles
+  static void g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, const PartP& pp, const AdjP& ad,
+                      const NodeAdjP& na);
+  static void grid_adj(cudaStream_t s, const GridRec& gr, const NodeAdjP& na, const uint8_t* fixed, double dt,
+                       double tol);
+  static void p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, const AdjP& ad, const NodeAdjP& na,
+                      const MatParams& mp, double c1, double c2, const double* grav);
   // contact mode: compaction + per-node grid update of every body field + correction
   static void contact_grid(cudaStream_t s, const NodeP& nd, const ContactP& cp, double dt, double tol,
                            bool f32copy);

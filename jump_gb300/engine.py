@@ -190,6 +190,24 @@ class MPMContext(_ContextBase):
         _capi.check(self.L.mpm_last_step_ms(self.h, C.byref(ms)), self.L)
         return ms.value
 
+    def fwd_checkpointed(self, nsteps: int, every: int):
+        """nsteps steps keeping a snapshot every `every` steps (reverse mode)."""
+        _capi.check(self.L.mpm_fwd_checkpointed(self.h, int(nsteps), int(every)), self.L)
+
+    def bwd(self, x_bar: np.ndarray, v_bar: np.ndarray | None = None) -> dict:
+        """Reverse sweep of the last fwd_checkpointed run.  x_bar/v_bar: dL/dx, dL/dv
+        at the final step, (total particles, dim).  Returns dL/dE per particle and
+        dL/dv, dL/dx at the initial step."""
+        n = sum(self.counts)
+        xb = np.ascontiguousarray(x_bar, dtype=np.float64).reshape(n, self.dim)
+        vb = None if v_bar is None else np.ascontiguousarray(v_bar, dtype=np.float64).reshape(n, self.dim)
+        E = np.zeros(n)
+        v0 = np.zeros((n, self.dim))
+        x0 = np.zeros((n, self.dim))
+        _capi.check(self.L.mpm_bwd(self.h, _capi.dptr(xb), _capi.dptr(vb), _capi.dptr(E), _capi.dptr(v0),
+                                   _capi.dptr(x0)), self.L)
+        return {"E": E, "v0": v0, "x0": x0}
+
     def profile_stages(self, nsteps: int) -> dict:
         """Device ms per stage summed over nsteps steps (individual launches, CUDA events)."""
         out = np.zeros(len(_capi.STAGES))

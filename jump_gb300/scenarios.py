@@ -175,3 +175,24 @@ def sphere_plate(h: float = 5e-4, ppc: int = 2, radius: float = 5e-3, speed: flo
             "bodyforce": ConstantBodyForce3D([0.0, 0.0, 0.0]),
             "dirichlet_grid": [("front", (0, 0, 1))], "contact": True, "friction": 0.0}
     return grid, [s1, s2], USL(1e-3 * float(s2.mass[0])), data
+
+
+def block_3d(h: float = 0.125, ppc: int = 2, size=(1.0, 0.25, 0.25), E_range=(0.5e6, 2e6), nu: float = 0.3,
+             rho: float = 1050.0, g: float = -10.0, dt: float = 1e-4, seed: int = 0):
+    """A neo-Hookean block clamped at x = 0 sagging under gravity, with a
+    per-particle Young's modulus (log-uniform, seeded): the 3D counterpart of
+    the cantilever inverse problem."""
+    from .solid import buildParticleForBlock
+    lx, ly, lz = size
+    nx, ny, nz = int(round((lx + 0.25) / h)) + 1, int(round((ly + 0.75) / h)) + 1, int(round((lz + 0.25) / h)) + 1
+    grid = Grid3D(0.0, (nx - 1) * h, 0.0, (ny - 1) * h, 0.0, (nz - 1) * h, nx, ny, nz)
+    off = h / ppc
+    coords = buildParticleForBlock([0.5 * lx, 0.5 + 0.5 * ly, 0.125 + 0.5 * lz], lx, ly, lz, off)
+    mat = NeoHookeanMaterial(math.sqrt(E_range[0] * E_range[1]), nu, rho, len(coords))
+    s = Solid3D(coords, mat)
+    _scale(s, off, 3)
+    rng = np.random.default_rng(seed)
+    s.youngs = np.exp(rng.uniform(math.log(E_range[0]), math.log(E_range[1]), len(coords)))
+    data = {"total_time": 200 * dt, "dt": dt, "time": 0.0, "bodyforce": ConstantBodyForce3D([0.0, g, 0.0]),
+            "dirichlet_grid": [("left", (1, 1, 1))]}
+    return grid, [s], USL(1e-9), data
