@@ -83,6 +83,10 @@ struct mpm_ctx {
   int32_t adj_every = 0;
   char* segbuf = nullptr;
   int32_t segbuf_slots = 0;
+  // captured reverse segment (recompute + reverse sweep), per segment length
+  cudaGraph_t seg_graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t seg_exec[2] = {nullptr, nullptr};
+  int seg_len[2] = {0, 0};
   double* gridrec = nullptr;
   double* adjbuf = nullptr;
   double* nodeadj = nullptr;
@@ -143,6 +147,10 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->nodebuf);
   cudaFree(c->nodebuf_f);
   cudaFree(c->blockbuf);
+  for (int i = 0; i < 2; ++i) {
+    if (c->seg_exec[i]) cudaGraphExecDestroy(c->seg_exec[i]);
+    if (c->seg_graph[i]) cudaGraphDestroy(c->seg_graph[i]);
+  }
   cudaFree(c->ckpt);
   cudaFree(c->segbuf);
   cudaFree(c->gridrec);
@@ -807,6 +815,13 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
   const int ANF = D == 2 ? AdjLayout<2>::NF : AdjLayout<3>::NF;
   const int XB = 0, VB = D, EB = 2 * D + D * D;
   if (c->segbuf_slots < every) {
+    for (int i = 0; i < 2; ++i) {  // captured segments point into the old buffers
+      if (c->seg_exec[i]) cudaGraphExecDestroy(c->seg_exec[i]);
+      if (c->seg_graph[i]) cudaGraphDestroy(c->seg_graph[i]);
+      c->seg_exec[i] = nullptr;
+      c->seg_graph[i] = nullptr;
+      c->seg_len[i] = 0;
+    }
     cudaFree(c->segbuf);
     cudaFree(c->gridrec);
     c->segbuf = nullptr;
@@ -846,20 +861,17 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
   na.fb = c->nodeadj + Nn * (1 + 3 * D);
   const int64_t nseg = c->ckpt_slots - 1;
   void* Pwork = c->P;
-  for (int64_t seg = nseg - 1; seg >= 0; --seg) {
-    const int64_t n0 = seg * every;
-    const int len = int(std::min<int64_t>(every, nsteps - n0));
-    // recompute the segment from its checkpoint, recording each step's state and grid
-    CUDA_TRY(cudaMemcpyAsync(Pwork, c->ckpt + bytes * size_t(seg), bytes, cudaMemcpyDeviceToDevice, c->stream));
+  // One segment: recompute `len` steps from the state in P, recording each
+  // step's particle state and grid outputs, then the reverse sweep over them.
+  auto enqueue_segment = [&](int len) {
     for (int j = 0; j < len; ++j) {
-      CUDA_TRY(cudaMemcpyAsync(c->segbuf + bytes * size_t(j), Pwork, bytes, cudaMemcpyDeviceToDevice, c->stream));
+      cudaMemcpyAsync(c->segbuf + bytes * size_t(j), Pwork, bytes, cudaMemcpyDeviceToDevice, c->stream);
       enqueue_step(c, nullptr, c->gridrec + size_t(Nn) * (1 + 2 * D) * size_t(j));
     }
-    // reverse sweep over the segment
     for (int j = len - 1; j >= 0; --j) {
       const double* rec = c->gridrec + size_t(Nn) * (1 + 2 * D) * size_t(j);
       const GridRec gr{rec, rec + Nn, rec + Nn * (1 + D)};
-      CUDA_TRY(cudaMemsetAsync(c->nodeadj, 0, size_t(Nn) * 2 * D * sizeof(double), c->stream));
+      cudaMemsetAsync(c->nodeadj, 0, size_t(Nn) * 2 * D * sizeof(double), c->stream);
       for (int b = 0; b < c->nb; ++b) {
         const PartP ps{c->segbuf + bytes * size_t(j), c->np, c->off[b], c->cnt[b]};
         if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
@@ -874,9 +886,43 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
         if (D == 2) Launchers<2>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
         else Launchers<3>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
       }
-      CUDA_TRY(cudaGetLastError());
     }
+  };
+  // captured once per segment length (full segments, and a shorter last one)
+  auto segment_exec = [&](int len, cudaGraphExec_t* out) -> int {
+    for (int i = 0; i < 2; ++i)
+      if (c->seg_exec[i] && c->seg_len[i] == len) {
+        *out = c->seg_exec[i];
+        return MPM_OK;
+      }
+    int slot = c->seg_exec[0] ? 1 : 0;
+    if (c->seg_exec[slot]) {
+      cudaGraphExecDestroy(c->seg_exec[slot]);
+      cudaGraphDestroy(c->seg_graph[slot]);
+      c->seg_exec[slot] = nullptr;
+      c->seg_graph[slot] = nullptr;
+    }
+    CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_segment(len);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ee = cudaStreamEndCapture(c->stream, &c->seg_graph[slot]);
+    if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_bwd launch: ") + cudaGetErrorString(le));
+    if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_bwd capture: ") + cudaGetErrorString(ee));
+    CUDA_TRY(cudaGraphInstantiate(&c->seg_exec[slot], c->seg_graph[slot], 0));
+    c->seg_len[slot] = len;
+    *out = c->seg_exec[slot];
+    return MPM_OK;
+  };
+  for (int64_t seg = nseg - 1; seg >= 0; --seg) {
+    const int64_t n0 = seg * every;
+    const int len = int(std::min<int64_t>(every, nsteps - n0));
+    CUDA_TRY(cudaMemcpyAsync(Pwork, c->ckpt + bytes * size_t(seg), bytes, cudaMemcpyDeviceToDevice, c->stream));
+    cudaGraphExec_t ex = nullptr;
+    int r = segment_exec(len, &ex);
+    if (r) return r;
+    CUDA_TRY(cudaGraphLaunch(ex, c->stream));
   }
+  CUDA_TRY(cudaGetLastError());
   // gradients in original particle order (no sorting in reverse mode)
   base = 0;
   for (int b = 0; b < c->nb; ++b) {
