@@ -126,19 +126,34 @@ def workload(name: str):
     return g, s, alg, data, cfg
 
 
-def dist_init(world):
+def dist_init(world, backend=None):
+    """One process per GPU (torchrun env): NCCL when this rank sees a GPU, else gloo."""
     if world <= 1:
         return None
     import torch.distributed as dist
     os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-    backend = "nccl"
-    try:
-        import torch
-        torch.cuda.set_device(0)
-    except Exception:
-        backend = "gloo"
+    if backend is None:
+        backend = "nccl"
+        try:
+            import torch
+            torch.cuda.set_device(0)
+        except Exception:
+            backend = "gloo"
     dist.init_process_group(backend=backend)
     return dist
+
+
+def shard(n: int, rank: int, world: int) -> list[int]:
+    """Problems of an ensemble that rank runs: every world-th one from rank, so
+    ranks get the seeded size mix alike; together the ranks cover 0..n-1 once."""
+    return list(range(rank, n, world))
+
+
+def aggregate(dist, device_s: float, units: float):
+    """Whole-job throughput: units summed over ranks / the slowest rank's time."""
+    t_max = allreduce_max(dist, device_s)
+    total = allreduce_sum(dist, units)
+    return t_max, total, total / t_max
 
 
 def allreduce_max(dist, x: float) -> float:
@@ -237,9 +252,7 @@ def run_ours(args):
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
-    t_max = allreduce_max(dist, dev_ms / 1e3)
-    total_updates = allreduce_sum(dist, float(npart * args.steps))
-    value = total_updates / t_max
+    t_max, total_updates, value = aggregate(dist, dev_ms / 1e3, float(npart * args.steps))
 
     # per-stage device times (individual launches, CUDA events on the context stream)
     nprof = max(3, min(args.steps, 10))
@@ -321,20 +334,33 @@ def run_ensemble(args):
     from jump_gb300 import scenarios
     from jump_gb300.batch import Ensemble
     from jump_gb300.engine import Descriptors, MPMContext
-    n, steps = args.instances, args.solve_steps
-    probs = [scenarios.ensemble_member(i) for i in range(n)]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = dist_init(world)
+    n, steps = args.instances * world, args.solve_steps  # --instances per GPU: weak scaling
+    mine = shard(n, rank, world)  # problems are independent: no collective on the data path
+    probs = [scenarios.ensemble_member(i) for i in mine]
     ens = Ensemble(probs, precision=args.precision)
     tune = ens.tune(probe_steps=10)
     ens.step(2)  # warm-up (advances every problem 2 steps)
     sampler = ClockSampler()
+    if dist is not None:
+        dist.barrier()
     t0 = time.perf_counter()
     ens.step(steps)
     wall = time.perf_counter() - t0
+    if dist is not None:
+        dist.barrier()
     clocks = sampler.stop()
-    dev = ens.last_ms() / 1e3
-    batched = n / dev
-    npart = ens.particles
+    dev, _, batched = aggregate(dist, ens.last_ms() / 1e3, float(len(mine)))
+    npart = allreduce_sum(dist, float(ens.particles))
     ens.close()
+    if rank != 0 or world > 1:
+        if rank == 0:
+            print(json.dumps(ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks, None, world)))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     sample = list(range(0, n, max(1, n // 32)))[:32]
     t_one = 0.0
     for i in sample:
@@ -348,16 +374,24 @@ def run_ensemble(args):
         t_one += time.perf_counter() - t1
         c.close()
     one_by_one = n / (t_one * n / len(sample))
-    out = {"metric": "solves/s", "value": batched, "unit": "solves/s", "n_gpus": 1, "steps": steps,
+    print(json.dumps(ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks,
+                                   (one_by_one, len(sample)), world)))
+
+
+def ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks, one_by_one, world):
+    out = {"metric": "solves/s", "value": batched, "unit": "solves/s", "n_gpus": world, "steps": steps,
            "warmup": 2, "ms_per_step": 1e3 * dev / steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": args.precision, "data": "synthetic (seeded ensemble)",
            "config": {"workload": "two_disk_ensemble_2d", "instances": n, "steps_per_solve": steps,
-                      "particles": npart, "launch": tune},
-           "particle_updates_per_s": npart * steps / dev, "wall_s": wall,
-           "one_by_one": {"value": one_by_one, "unit": "solves/s", "sample": len(sample),
-                          "how": "same problems, one context each, step graph replayed per step"},
-           "speedup_vs_one_by_one": batched / one_by_one, "clocks": clocks}
-    print(json.dumps(out))
+                      "particles": int(npart), "launch": tune,
+                      "parallelism": f"problems sharded over {world} ranks" if world > 1 else "single-gpu"},
+           "particle_updates_per_s": npart * steps / dev, "wall_s": wall, "clocks": clocks}
+    if one_by_one is not None:
+        v, ns = one_by_one
+        out["one_by_one"] = {"value": v, "unit": "solves/s", "sample": ns,
+                             "how": "same problems, one context each, step graph replayed per step"}
+        out["speedup_vs_one_by_one"] = batched / v
+    return out
 
 
 def run_adjoint(args):
