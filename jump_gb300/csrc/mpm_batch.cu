@@ -144,11 +144,20 @@ CompMapH ident(int n) {
   return m;
 }
 
-CompMapH sym_from_full(int dim) {
+// upload of a symmetric matrix; mirrored entries that differ set `bit` in *flag
+CompMapH sym_from_full(int dim, unsigned* flag = nullptr, unsigned bit = 0) {
   CompMapH m{};
   m.n = dim == 2 ? 3 : 6;
   for (int j = 0; j < dim; ++j)
     for (int i = j; i < dim; ++i) m.src[sym_slot(dim, i, j)] = i + dim * j;
+  for (int j = 0; j < dim; ++j)
+    for (int i = j + 1; i < dim; ++i) {
+      m.ca[m.nchk] = i + dim * j;
+      m.cb[m.nchk] = j + dim * i;
+      ++m.nchk;
+    }
+  m.flag = flag;
+  m.bit = bit;
   return m;
 }
 
@@ -405,11 +414,11 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
           for (int a = 0; a < D; ++a) I[p * D * D + a * (D + 1)] = 1.0;
         if ((r = upload(b, pp, I.data(), D * D, L::F, ident(D * D)))) return r;
       }
-      if ((r = upload(b, pp, d.strain, D * D, L::EPS, sym_from_full(D)))) return r;
-      if ((r = upload(b, pp, d.stress, D * D, L::SIG, sym_from_full(D)))) return r;
+      if ((r = upload(b, pp, d.strain, D * D, L::EPS, sym_from_full(D, b->d_status, ST_ASYM_STRESS)))) return r;
+      if ((r = upload(b, pp, d.stress, D * D, L::SIG, sym_from_full(D, b->d_status, ST_ASYM_STRESS)))) return r;
       if ((r = upload(b, pp, d.alpha, 1, L::ALPHA, ident(1)))) return r;
       if (d.pstrain) {
-        r = D == 2 ? upload(b, pp, d.pstrain, 3, L::EP, ident(3)) : upload(b, pp, d.pstrain, 9, L::EP, sym_from_full(3));
+        r = D == 2 ? upload(b, pp, d.pstrain, 3, L::EP, ident(3)) : upload(b, pp, d.pstrain, 9, L::EP, sym_from_full(3, b->d_status, ST_ASYM_PSTRAIN));
         if (r) return r;
       }
       if (d.youngs) {
@@ -424,6 +433,12 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       }
     }
   }
+  // the uploads compared the mirrored entries of every symmetric input (flag: problem 0's status word)
+  unsigned st = 0;
+  BATCH_TRY(cudaMemcpy(&st, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (st & ST_ASYM_STRESS) return fail(MPM_ERR_ARG, "mpm_batch_create: strain and stress must be symmetric");
+  if (st & ST_ASYM_PSTRAIN) return fail(MPM_ERR_ARG, "mpm_batch_create: pstrain must be symmetric");
+  BATCH_TRY(cudaMemset(b->d_status, 0, sizeof(unsigned)));
   return MPM_OK;
 }
 

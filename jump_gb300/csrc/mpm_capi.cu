@@ -227,12 +227,21 @@ CompMapH ident(int n) {
   return m;
 }
 
-// upload: symmetric slot s <- column-major entry
-CompMapH sym_from_full(int dim) {
+// upload: symmetric slot s <- column-major entry; with a flag, entries (i, j)
+// and (j, i) are compared on the device and `bit` is set when they differ
+CompMapH sym_from_full(int dim, unsigned* flag = nullptr, unsigned bit = 0) {
   CompMapH m{};
   m.n = dim == 2 ? 3 : 6;
   for (int j = 0; j < dim; ++j)
     for (int i = j; i < dim; ++i) m.src[sym_slot(dim, i, j)] = i + dim * j;
+  for (int j = 0; j < dim; ++j)
+    for (int i = j + 1; i < dim; ++i) {
+      m.ca[m.nchk] = i + dim * j;
+      m.cb[m.nchk] = j + dim * i;
+      ++m.nchk;
+    }
+  m.flag = flag;
+  m.bit = bit;
   return m;
 }
 
@@ -243,15 +252,6 @@ CompMapH full_from_sym(int dim) {
   for (int j = 0; j < dim; ++j)
     for (int i = 0; i < dim; ++i) m.src[i + dim * j] = sym_slot(dim, i, j);
   return m;
-}
-
-bool symmetric(const double* a, int64_t n, int dim) {
-  if (!a) return true;
-  for (int64_t p = 0; p < n; ++p)
-    for (int i = 0; i < dim; ++i)
-      for (int j = i + 1; j < dim; ++j)
-        if (a[p * dim * dim + i + dim * j] != a[p * dim * dim + j + dim * i]) return false;
-  return true;
 }
 
 // The launches of one USL step; ev (optional) gets an event recorded after each stage.
@@ -490,12 +490,14 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
         for (int a = 0; a < D; ++a) I[p * D * D + a * (D + 1)] = 1.0;
       if ((r = upload(c, b, I.data(), D * D, fi.F, ident(D * D)))) return r;
     }
-    if (d.strain && (r = upload(c, b, d.strain, D * D, fi.EPS, sym_from_full(D)))) return r;
-    if (d.stress && (r = upload(c, b, d.stress, D * D, fi.SIG, sym_from_full(D)))) return r;
+    if (d.strain && (r = upload(c, b, d.strain, D * D, fi.EPS, sym_from_full(D, c->status, ST_ASYM_STRESS))))
+      return r;
+    if (d.stress && (r = upload(c, b, d.stress, D * D, fi.SIG, sym_from_full(D, c->status, ST_ASYM_STRESS))))
+      return r;
     if (d.alpha && (r = upload(c, b, d.alpha, 1, fi.ALPHA, ident(1)))) return r;
     if (d.pstrain) {
       if (D == 2) r = upload(c, b, d.pstrain, 3, fi.EP, ident(3));
-      else r = upload(c, b, d.pstrain, 9, fi.EP, sym_from_full(3));
+      else r = upload(c, b, d.pstrain, 9, fi.EP, sym_from_full(3, c->status, ST_ASYM_PSTRAIN));
       if (r) return r;
     }
     if (d.youngs) {
@@ -509,6 +511,12 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
       if ((r = upload(c, b, lm.data(), 2, fi.LAM, ident(2)))) return r;
     }
   }
+  // the uploads compared the mirrored entries of every symmetric input
+  unsigned st = 0;
+  CUDA_TRY(cudaMemcpy(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (st & ST_ASYM_STRESS) return fail(MPM_ERR_ARG, "mpm_create: strain and stress must be symmetric");
+  if (st & ST_ASYM_PSTRAIN) return fail(MPM_ERR_ARG, "mpm_create: pstrain must be symmetric");
+  CUDA_TRY(cudaMemset(c->status, 0, sizeof(unsigned)));
   return MPM_OK;
 }
 
@@ -553,10 +561,6 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
       return fail(MPM_ERR_ARG, "mpm_create: pos, velocity, mass, volume and volume_initial are required");
     if (d.mat.type != MPM_MAT_ELASTIC && d.mat.type != MPM_MAT_NEOHOOKEAN && d.mat.type != MPM_MAT_J2)
       return fail(MPM_ERR_ARG, "mpm_create: unknown material type");
-    if (!symmetric(d.strain, d.count, D) || !symmetric(d.stress, d.count, D))
-      return fail(MPM_ERR_ARG, "mpm_create: strain and stress must be symmetric");
-    if (D == 3 && !symmetric(d.pstrain, d.count, 3))
-      return fail(MPM_ERR_ARG, "mpm_create: pstrain must be symmetric");
   }
   mpm_ctx* c = new mpm_ctx();
   int r = create_impl(grid, bodies, nbodies, params, c);

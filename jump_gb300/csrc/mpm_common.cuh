@@ -13,7 +13,10 @@
 namespace jmpm {
 
 // status bits raised by kernels (atomicOr), mapped to MPM_ERR_* by the host
-enum : unsigned { ST_OUT_OF_GRID = 1u, ST_NEGATIVE_J = 2u, ST_NONFINITE = 4u };
+enum : unsigned { ST_OUT_OF_GRID = 1u, ST_NEGATIVE_J = 2u, ST_NONFINITE = 4u,
+                  // set only while uploading: a strain/stress or 3D plastic strain input
+                  // whose mirrored entries differ
+                  ST_ASYM_STRESS = 8u, ST_ASYM_PSTRAIN = 16u };
 
 // Field indices of the particle SoA.  Symmetric tensors are stored as
 // 2D: (xx, yy, xy); 3D: (xx, yy, zz, xy, yz, xz).

@@ -14,6 +14,10 @@ namespace jmpm {
 struct CompMapH {
   int n;
   int src[9];
+  int nchk;         // upload: mirrored pairs (ca[k], cb[k]) that must be equal
+  int ca[3], cb[3];
+  unsigned bit;     // set in *flag when a pair differs
+  unsigned* flag;
 };
 
 template <int D>

@@ -641,12 +641,21 @@ __global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial
 
 template <int NQ>
 __global__ void fold_kernel(const double* partial, int nblocks, double* out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int k = 0; k < NQ; ++k) {
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partial[int64_t(b) * NQ + k];
-    out[k] = s;
-  }
+  // one warp: lane l sums blocks l, l+32, ... then a fixed shuffle tree, so the
+  // result does not depend on timing
+  int lane = threadIdx.x;
+  double acc[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) acc[k] = 0.0;
+  for (int b = lane; b < nblocks; b += 32)
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) acc[k] += partial[int64_t(b) * NQ + k];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k)
+    for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) out[k] = acc[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -654,6 +663,12 @@ __global__ void fold_kernel(const double* partial, int nblocks, double* out) {
 struct CompMap {
   int n;          // components moved per particle
   int src[9];     // AoS component for each SoA field (upload) / SoA field for each AoS entry
+  // upload only: pairs of AoS components that must be equal (the mirrored
+  // entries of a symmetric matrix); any pair that differs sets `bit` in *flag
+  int nchk;
+  int ca[3], cb[3];
+  unsigned bit;
+  unsigned* flag;
 };
 
 template <class R>
@@ -662,6 +677,9 @@ __global__ void aos_to_soa_kernel(PartP pp, const double* src, int per, int f0, 
   if (t >= pp.count) return;
   for (int c = 0; c < cm.n; ++c)
     *field<R>(pp, f0 + c, pp.begin + t) = R(src[t * per + cm.src[c]]);
+  bool asym = false;
+  for (int k = 0; k < cm.nchk; ++k) asym |= src[t * per + cm.ca[k]] != src[t * per + cm.cb[k]];
+  if (asym && cm.flag) atomicOr(cm.flag, cm.bit);
 }
 
 // vmStr of J2 particles, from the stored stress, into a dense FP64 array

@@ -14,6 +14,13 @@ static inline CompMap to_dev(const CompMapH& h) {
   CompMap c;
   c.n = h.n;
   for (int i = 0; i < 9; ++i) c.src[i] = h.src[i];
+  c.nchk = h.nchk;
+  for (int i = 0; i < 3; ++i) {
+    c.ca[i] = h.ca[i];
+    c.cb[i] = h.cb[i];
+  }
+  c.bit = h.bit;
+  c.flag = h.flag;
   return c;
 }
 

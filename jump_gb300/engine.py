@@ -132,13 +132,19 @@ class _ContextBase:
         self.dim = desc.dim
         self.counts = [desc.bodies[s].count for s in range(desc.nbodies)]
 
-    def download_body(self, s: int) -> BodyState:
-        st = BodyState(self.counts[s], self.dim)
+    def download_body(self, s: int, into: BodyState | None = None) -> BodyState:
+        """Body s's state, into `into` (reused host arrays) or new arrays."""
+        st = BodyState(self.counts[s], self.dim) if into is None else into
+        if st.n != self.counts[s] or st.d != self.dim:
+            raise ValueError("download_body: state arrays of the wrong size")
         self._download(s, st.view())
         return st
 
-    def download_all(self):
-        return [self.download_body(s) for s in range(len(self.counts))]
+    def download_all(self, into: list | None = None):
+        """Every body's state; pass the list a previous call returned to reuse its arrays."""
+        if into is None:
+            return [self.download_body(s) for s in range(len(self.counts))]
+        return [self.download_body(s, st) for s, st in enumerate(into)]
 
 
 class MPMContext(_ContextBase):

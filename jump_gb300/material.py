@@ -12,6 +12,7 @@ import math
 import numpy as np
 
 from . import _capi
+from .arrays import matrix_array
 
 
 class MaterialType:
@@ -86,4 +87,4 @@ class ElastoPlasticMaterial(MaterialType):
         self.pstrain = np.zeros((n, 3))
         self.alpha = np.zeros(n)
         self.vmStr = np.zeros(n)
-        self.pstrain_3D = np.zeros((n, 3, 3))
+        self.pstrain_3D = matrix_array(n, 3)

@@ -85,6 +85,7 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
     try:
         done = 0
         nsteps = len(times)
+        states = None  # host arrays of the downloads, reused from hook to hook
         while done < nsteps:
             # next hook step: the first counter >= done with counter % interval == 0
             nxt = ((done + interval - 1) // interval) * interval
@@ -95,7 +96,8 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
             if counter % interval == 0:
                 th = times[counter]
                 if need_particles:
-                    write_back(solids, ctx.download_all())
+                    states = ctx.download_all(states)
+                    write_back(solids, states)
                     output.plot(solids, lims, ncells, counter)
                     for f in fl:
                         f.compute(th)
@@ -104,7 +106,7 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
                     for f in fl:
                         if isinstance(f, EnergiesFix):
                             f.record(th, ke, se)
-        write_back(solids, ctx.download_all())
+        write_back(solids, ctx.download_all(states))
         m, p0, p, f = ctx.download_grid(grid.nodeCount)
         grid.mass[:] = m
         grid.momentum0[:] = p0

@@ -3,8 +3,8 @@
 
 Particle fields keep the reference's names.  Vectors are (parCount, d) numpy
 arrays and matrices (parCount, d, d) with ``A[p, i, j]`` the (i, j) entry;
-the C ABI receives the matrices transposed per particle, which is the
-column-major layout of a Julia ``SMatrix``.
+their memory is column-major per particle (the layout of a Julia
+``SMatrix``, which the C ABI reads), so they pass to the library uncopied.
 
 Extension beyond the reference: ``youngs`` (None or a parCount array) gives
 a per-particle Young's modulus, used by inverse problems that recover E per
@@ -17,6 +17,7 @@ import math
 
 import numpy as np
 
+from .arrays import matrix_array
 from .material import RigidMaterial
 
 
@@ -128,9 +129,9 @@ class _SolidBase:
         self.pos = coords.copy()
         self.pos0 = coords.copy()
         self.velocity = np.zeros((n, d))
-        self.deformationGradient = np.tile(np.eye(d), (n, 1, 1))
-        self.strain = np.zeros((n, d, d))
-        self.stress = np.zeros((n, d, d))
+        self.deformationGradient = matrix_array(n, d, identity=True)
+        self.strain = matrix_array(n, d)
+        self.stress = matrix_array(n, d)
         self.rigid = isinstance(mat, RigidMaterial)
         self.youngs = None
 

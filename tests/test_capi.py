@@ -55,15 +55,3 @@ def test_argument_errors_without_gpu(L):
     assert L.mpm_create(C.byref(g), None, 0, C.byref(p), C.byref(h)) == _capi.MPM_ERR_ARG
     assert L.mpm_step(None, 1, None) == _capi.MPM_ERR_ARG
     assert L.mpm_destroy(None) == _capi.MPM_OK
-
-
-def test_asymmetric_stress_rejected(L):
-    import numpy as np
-    from jump_gb300 import scenarios
-    from jump_gb300.engine import Descriptors
-    g, s, alg, data = scenarios.two_disks(nodes=6)
-    s[0].stress[0] = np.array([[1.0, 2.0], [3.0, 4.0]])
-    d = Descriptors(g, s, tolerance=alg.tolerance, body_force=data["bodyforce"], dt=data["dt"])
-    h = C.c_void_p()
-    rc = L.mpm_create(C.byref(d.grid), d.bodies, d.nbodies, C.byref(d.params), C.byref(h))
-    assert rc == _capi.MPM_ERR_ARG and b"symmetric" in L.mpm_last_error()
