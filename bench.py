@@ -375,23 +375,37 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+ENSEMBLES = {
+    # workload: (problem i, default problems per GPU, default steps per solve, config name)
+    "ensemble": ("ensemble_member", 512, 1000, "two_disk_ensemble_2d"),
+    "impact_ensemble": ("impact_member", 64, 200, "sphere_plate_impact_ensemble_3d_contact"),
+}
+
+
 def run_ensemble(args):
-    """Batched ensemble of independent two-disk problems (seeded sizes 20^2..80^2
-    cells, 4 particles per cell): solves/s of the persistent batched launch
-    against launching the same problems one after another through single
-    contexts (a stratified sample of 32 problems, scaled to the ensemble)."""
+    """Batched ensembles: solves/s of the batch (strategy and launch shape
+    autotuned) against launching the same problems one after another through
+    single contexts (a stratified sample of up to 32 problems, scaled to the
+    ensemble).  "ensemble": seeded two-disk problems (20^2..80^2 cells, 4
+    particles per cell).  "impact_ensemble": seeded sphere-on-plate impacts
+    (3D, 135,952 particles each, two velocity fields with the frictionless
+    contact correction, speed in [10, 100] m/s, plate E in [1e9, 10e9] Pa)."""
     from jump_gb300 import scenarios
     from jump_gb300.batch import Ensemble
     from jump_gb300.engine import Descriptors, MPMContext
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     dist = dist_init(world)
-    n, steps = args.instances * world, args.solve_steps  # --instances per GPU: weak scaling
+    gen_name, n_default, steps_default, cfg_name = ENSEMBLES[args.workload]
+    member = getattr(scenarios, gen_name)
+    per_gpu = args.instances if args.instances is not None else n_default
+    steps = args.solve_steps if args.solve_steps is not None else steps_default
+    n = per_gpu * world  # problems per GPU fixed: weak scaling
     mine = shard(n, rank, world)  # problems are independent: no collective on the data path
-    probs = [scenarios.ensemble_member(i) for i in mine]
+    probs = [member(i) for i in mine]
     ens = Ensemble(probs, precision=args.precision)
     tune = ens.tune(probe_steps=10)
-    ens.step(2)  # warm-up (advances every problem 2 steps)
+    ens.step(args.warmup)  # warm-up (advances every problem W steps)
     sampler = ClockSampler()
     if dist is not None:
         dist.barrier()
@@ -413,11 +427,12 @@ def run_ensemble(args):
     sample = list(range(0, n, max(1, n // 32)))[:32]
     t_one = 0.0
     for i in sample:
-        grid, solids, alg, data = scenarios.ensemble_member(i)
+        grid, solids, alg, data = member(i)
         scenarios.apply_dirichlet(grid, data)
         c = MPMContext(Descriptors(grid, solids, tolerance=alg.tolerance, body_force=data["bodyforce"],
-                                   dt=data["dt"], precision=args.precision))
-        c.step(2)
+                                   dt=data["dt"], precision=args.precision, contact=bool(data.get("contact")),
+                                   friction=float(data.get("friction", 0.0))))
+        c.step(args.warmup)
         t1 = time.perf_counter()
         c.step(steps)
         t_one += time.perf_counter() - t1
@@ -429,9 +444,9 @@ def run_ensemble(args):
 
 def ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks, one_by_one, world):
     out = {"metric": "solves/s", "value": batched, "unit": "solves/s", "n_gpus": world, "steps": steps,
-           "warmup": 2, "ms_per_step": 1e3 * dev / steps, "higher_is_better": True, "scaling": "weak",
+           "warmup": args.warmup, "ms_per_step": 1e3 * dev / steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": args.precision, "data": "synthetic (seeded ensemble)",
-           "config": {"workload": "two_disk_ensemble_2d", "instances": n, "steps_per_solve": steps,
+           "config": {"workload": ENSEMBLES[args.workload][3], "instances": n, "steps_per_solve": steps,
                       "particles": int(npart), "launch": tune,
                       "parallelism": f"problems sharded over {world} ranks" if world > 1 else "single-gpu"},
            "particle_updates_per_s": npart * steps / dev, "wall_s": wall, "clocks": clocks}
@@ -523,9 +538,12 @@ def main():
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
     ap.add_argument("--sort-interval", type=int, default=0,
                     help="counting-sort particles by cell every N steps (0: never)")
-    ap.add_argument("--workload", default="taylor_bar", choices=["taylor_bar", "two_disks", "ensemble", "adjoint"])
-    ap.add_argument("--instances", type=int, default=512, help="ensemble: number of problems")
-    ap.add_argument("--solve-steps", type=int, default=1000, help="ensemble: steps per solve")
+    ap.add_argument("--workload", default="taylor_bar",
+                    choices=["taylor_bar", "two_disks", "ensemble", "impact_ensemble", "adjoint"])
+    ap.add_argument("--instances", type=int, default=None,
+                    help="ensembles: problems per GPU (default 512 two-disk, 64 impact)")
+    ap.add_argument("--solve-steps", type=int, default=None,
+                    help="ensembles: steps per solve (default 1000 two-disk, 200 impact); adjoint: steps (2000)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -533,10 +551,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "ensemble":
+    elif args.workload in ENSEMBLES:
         run_ensemble(args)
     elif args.workload == "adjoint":
-        args.solve_steps = args.solve_steps if args.solve_steps != 1000 else 2000
+        args.solve_steps = args.solve_steps if args.solve_steps is not None else 2000
         run_adjoint(args)
     else:
         run_ours(args)

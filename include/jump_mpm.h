@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 1
+#define JUMP_MPM_ABI_VERSION 2
 
 /* status codes */
 #define MPM_OK               0
@@ -192,22 +192,36 @@ int mpm_bwd(mpm_ctx* ctx, const double* x_bar, const double* v_bar, double* E_ba
 /* ---------------------------------------------------------------------------
  * Batched ensembles (no counterpart in the reference, which solves one
  * problem per call): many independent problems -- each what one
- * solve_explicit_dynamics_2D/3D call would take -- advance together in one
- * persistent launch.  Each CTA takes problems from a work queue (largest
- * first) and runs all requested steps of a problem before taking the next.
- * All problems share the dimension, the precision and the material model
- * type (parameters may differ); contact mode and sorting are not available.
+ * solve_explicit_dynamics_2D/3D call would take -- advance together.  All
+ * problems share the dimension and the precision; sorting is not available.
+ * Two execution strategies:
+ *   MPM_BATCH_PERSISTENT  one persistent launch for all problems and all
+ *                         steps; each CTA takes problems from a work queue
+ *                         (largest first) and runs all steps of a problem.
+ *                         Needs one material model type for every body and
+ *                         no contact: the fit for many small problems.
+ *   MPM_BATCH_WIDE        one launch per stage for all problems (clear, P2G,
+ *                         block compaction, grid update, G2P) through
+ *                         per-problem and per-body offset tables, the step
+ *                         captured in a CUDA graph: the fit for problems too
+ *                         large for one CTA, problems mixing material models,
+ *                         and contact (one node field per body).
+ * mpm_batch_create picks PERSISTENT where it is allowed; mpm_batch_tune
+ * times both where both are allowed and keeps the faster.
  * ------------------------------------------------------------------------- */
 #define MPM_BATCH_MAX_BODIES 4
+#define MPM_BATCH_PERSISTENT 0
+#define MPM_BATCH_WIDE 1
 
 typedef struct mpm_instance_desc {
   mpm_grid_desc grid;
   const mpm_body_desc* bodies;  /* 1 .. MPM_BATCH_MAX_BODIES */
   int32_t nbodies;
-  int32_t reserved;
+  int32_t contact;              /* 1: one velocity field per body + contact correction */
   double dt;
   double tolerance;
   double body_force[3];
+  double friction;              /* contact: Coulomb coefficient (0: frictionless, 2D only above 0) */
 } mpm_instance_desc;
 
 typedef struct mpm_batch mpm_batch;
@@ -228,6 +242,9 @@ int mpm_batch_set_launch(mpm_batch* batch, int32_t threads, int32_t ctas_per_sm)
    fastest and returns it and its device time per step. */
 int mpm_batch_tune(mpm_batch* batch, int64_t probe_steps, int32_t* threads, int32_t* ctas_per_sm,
                    double* ms_per_step);
+/* MPM_BATCH_PERSISTENT or MPM_BATCH_WIDE (MPM_ERR_ARG where not allowed) */
+int mpm_batch_set_strategy(mpm_batch* batch, int32_t strategy);
+int mpm_batch_strategy(mpm_batch* batch, int32_t* strategy);
 /* device time of the last mpm_batch_step, milliseconds */
 int mpm_batch_last_ms(mpm_batch* batch, double* ms);
 int mpm_batch_destroy(mpm_batch* batch);

@@ -14,6 +14,8 @@ import threading
 
 import numpy as np
 
+ABI_VERSION = 2  # JUMP_MPM_ABI_VERSION of the structures below
+
 MPM_OK = 0
 MPM_ERR_ARG = 1
 MPM_ERR_CUDA = 2
@@ -39,6 +41,9 @@ MPM_MAT_J2 = 2
 
 MPM_PREC_F64 = 0
 MPM_PREC_F32 = 1
+
+MPM_BATCH_PERSISTENT = 0
+MPM_BATCH_WIDE = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int64)
@@ -156,6 +161,8 @@ SIGNATURES = {
     "mpm_batch_energies": (C.c_int, [C.c_void_p, _dp]),
     "mpm_batch_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "mpm_batch_tune": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp]),
+    "mpm_batch_set_strategy": (C.c_int, [C.c_void_p, C.c_int32]),
+    "mpm_batch_strategy": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "mpm_batch_last_ms": (C.c_int, [C.c_void_p, _dp]),
     "mpm_batch_destroy": (C.c_int, [C.c_void_p]),
 }
@@ -166,10 +173,11 @@ class InstanceDesc(C.Structure):
         ("grid", GridDesc),
         ("bodies", C.POINTER(BodyDesc)),
         ("nbodies", C.c_int32),
-        ("reserved", C.c_int32),
+        ("contact", C.c_int32),
         ("dt", C.c_double),
         ("tolerance", C.c_double),
         ("body_force", C.c_double * 3),
+        ("friction", C.c_double),
     ]
 
 STAGES = ("reset", "p2g", "grid", "g2p")
@@ -202,7 +210,11 @@ def lib():
                 raise RuntimeError(
                     f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; "
                     "g.build()\"` (the CUDA path has no CPU fallback)")
-            _lib = load_library(LIB_PATH)
+            L = load_library(LIB_PATH)
+            if L.mpm_abi_version() != ABI_VERSION:
+                raise RuntimeError(f"{LIB_PATH} has ABI version {L.mpm_abi_version()}, these bindings "
+                                   f"{ABI_VERSION}: rebuild it")
+            _lib = L
         return _lib
 
 

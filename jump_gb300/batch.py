@@ -1,12 +1,16 @@
-"""Batched ensembles: many independent problems in one persistent launch.
+"""Batched ensembles: many independent problems advanced together.
 
     ens = Ensemble([scenarios.ensemble_member(i) for i in range(512)], precision="f64")
-    ens.tune()                 # autotuned launch shape (cached per workload signature)
-    ens.step(1000)             # every problem advances 1000 steps, one launch
+    ens.tune()                 # strategy and launch shape, timed (cached per workload signature)
+    ens.step(1000)             # every problem advances 1000 steps
     ens.download(i)            # BodyState list of problem i
 
 Each problem is the (grid, solids, alg, data) a solve_explicit_dynamics_2D/3D
-call would take.  The C entry points are mpm_batch_* in include/jump_mpm.h.
+call would take; ``data["contact"]`` / ``data["friction"]`` select contact
+mode per problem.  Strategies: "persistent" (one launch for all problems and
+steps; one material model type, no contact) and "wide" (one launch per stage
+for all problems; any mix).  The C entry points are mpm_batch_* in
+include/jump_mpm.h.
 """
 from __future__ import annotations
 
@@ -46,6 +50,8 @@ class Ensemble:
             insts[i].tolerance = d.params.tolerance
             for a in range(3):
                 insts[i].body_force[a] = d.params.body_force[a]
+            insts[i].contact = 1 if data.get("contact") else 0
+            insts[i].friction = float(data.get("friction", 0.0))
             self.counts.append([d.bodies[s].count for s in range(d.nbodies)])
             self.dim = d.dim
         self._insts = insts
@@ -60,7 +66,9 @@ class Ensemble:
     def signature(self) -> str:
         """Workload key of the autotune cache: dimension, precision, sizes."""
         sizes = ",".join(str(sum(c)) for c in self.counts)
-        return f"d{self.dim}-{self.precision}-n{self.n}-" + hashlib.sha1(sizes.encode()).hexdigest()[:12]
+        kinds = ",".join(f"{int(i.contact)}" for i in self._insts)
+        return (f"d{self.dim}-{self.precision}-n{self.n}-"
+                + hashlib.sha1((sizes + "|" + kinds).encode()).hexdigest()[:12])
 
     def tune(self, probe_steps: int = 20, use_cache: bool = True):
         """Pick threads per CTA and CTAs per SM by timing them; remembered per workload."""
@@ -72,13 +80,15 @@ class Ensemble:
                 cache = json.load(open(path))
             except (OSError, ValueError):
                 cache = {}
-        if use_cache and key in cache:
+        if use_cache and key in cache and "strategy" in cache[key]:
             th, cps = cache[key]["threads"], cache[key]["ctas_per_sm"]
             _capi.check(self.L.mpm_batch_set_launch(self.h, th, cps), self.L)
+            self.set_strategy(cache[key]["strategy"])
             return dict(cache[key], cached=True)
         th, cps, ms = C.c_int32(), C.c_int32(), C.c_double()
         _capi.check(self.L.mpm_batch_tune(self.h, int(probe_steps), C.byref(th), C.byref(cps), C.byref(ms)), self.L)
-        res = {"threads": th.value, "ctas_per_sm": cps.value, "ms_per_step": ms.value}
+        res = {"threads": th.value, "ctas_per_sm": cps.value, "ms_per_step": ms.value,
+               "strategy": self.strategy}
         if use_cache:
             cache[key] = res
             try:
@@ -87,6 +97,18 @@ class Ensemble:
             except OSError:
                 pass
         return dict(res, cached=False)
+
+    STRATEGIES = {"persistent": _capi.MPM_BATCH_PERSISTENT, "wide": _capi.MPM_BATCH_WIDE}
+
+    @property
+    def strategy(self) -> str:
+        v = C.c_int32()
+        _capi.check(self.L.mpm_batch_strategy(self.h, C.byref(v)), self.L)
+        return {k: n for n, k in self.STRATEGIES.items()}[v.value]
+
+    def set_strategy(self, name: str):
+        """'persistent' (one launch for all problems and steps) or 'wide' (one launch per stage)."""
+        _capi.check(self.L.mpm_batch_set_strategy(self.h, self.STRATEGIES[name]), self.L)
 
     def set_launch(self, threads: int, ctas_per_sm: int = 0):
         _capi.check(self.L.mpm_batch_set_launch(self.h, int(threads), int(ctas_per_sm)), self.L)

@@ -1,7 +1,7 @@
-// mpm_batch.cu -- batched ensembles: many independent USL problems advance in
-// one persistent launch.
+// mpm_batch.cu -- batched ensembles: many independent USL problems advance
+// together, by one of two strategies.
 //
-// Layout: the particles of every problem (and of every body inside a
+// PERSISTENT (small problems, one material model, no contact).  Layout: the particles of every problem (and of every body inside a
 // problem) are contiguous ranges of one SoA allocation; node arrays of every
 // problem are packed one after another; InstanceP is the per-problem offset
 // table.  A CTA takes a problem from a work queue (problems ordered by
@@ -11,6 +11,11 @@
 // CTAs, and there is one launch for all problems and all steps.  Node data a
 // stage reads was written earlier in the same launch, so it is loaded through
 // L2 (__ldcg), never through the read-only path.
+//
+// WIDE (large problems, mixed materials, contact).  One launch per stage for
+// all problems (mpm_wide.cuh), the step captured once as a CUDA graph and
+// replayed.  It shares the particle SoA and, without contact, the node fields
+// of the persistent layout; contact problems get one node field per body.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -21,6 +26,7 @@
 #include "../../include/jump_mpm.h"
 #include "mpm_internal.h"
 #include "mpm_kernels.cuh"
+#include "mpm_wide.cuh"
 
 using namespace jmpm;
 
@@ -199,7 +205,29 @@ struct mpm_batch {
   int ctas_per_sm = 0;  // 0: as many as fit
   int sms = 1;
 
+  // strategy
+  bool persistent_ok = true;  // one material model type and no contact
+  int strategy = MPM_BATCH_PERSISTENT;
+  // WIDE strategy tables and node bookkeeping
+  std::vector<WideBody> wbody;
+  std::vector<WideInst> winst;
+  std::vector<WideTile> tiles;
+  WideBody* d_wbody = nullptr;
+  WideInst* d_winst = nullptr;
+  WideTile* d_tiles = nullptr;
+  int* d_blk_inst = nullptr;
+  uint32_t* d_blk = nullptr;  // flags (nblk) | list (nblk) | count (1)
+  int64_t nblk = 0;
+  double* cnodebuf = nullptr;  // contact problems: one field per body
+  float* cnodebuf_f = nullptr;
+  cudaGraph_t wgraph = nullptr;
+  cudaGraphExec_t wexec = nullptr;
+  bool nodes_dirty = false;  // the persistent kernel left node data the WIDE list does not cover
+
   PartP body(int i, int b) const { return PartP{P, np, inst[i].bbeg[b], inst[i].bcnt[b]}; }
+  uint32_t* flags() const { return d_blk; }
+  uint32_t* list() const { return d_blk + nblk; }
+  uint32_t* count() const { return d_blk + 2 * nblk; }
 };
 
 namespace {
@@ -217,6 +245,15 @@ void destroy_batch(mpm_batch* b) {
   cudaFree(b->d_status);
   cudaFree(b->d_energy);
   cudaFree(b->staging);
+  cudaFree(b->d_wbody);
+  cudaFree(b->d_winst);
+  cudaFree(b->d_tiles);
+  cudaFree(b->d_blk_inst);
+  cudaFree(b->d_blk);
+  cudaFree(b->cnodebuf);
+  cudaFree(b->cnodebuf_f);
+  if (b->wexec) cudaGraphExecDestroy(b->wexec);
+  if (b->wgraph) cudaGraphDestroy(b->wgraph);
   if (b->e0) cudaEventDestroy(b->e0);
   if (b->e1) cudaEventDestroy(b->e1);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -265,6 +302,76 @@ int launch(mpm_batch* b, void* P, int64_t nsteps, int threads, int per_sm) {
                 : launch_m<3, double>(b, P, nsteps, threads, per_sm);
 }
 
+// ---- WIDE strategy ----------------------------------------------------------
+template <int D>
+void wide_enqueue(mpm_batch* b) {
+  cudaStream_t s = b->stream;
+  const unsigned nt = unsigned(b->tiles.size());
+  const int64_t most = (b->nblk * 64 + 255) / 256;
+  const unsigned gctas = unsigned(std::max<int64_t>(1, std::min<int64_t>(most, int64_t(b->sms) * 8)));
+  // reset (:381-385) of the blocks the previous step touched
+  wide_clear_kernel<D><<<gctas, 256, 0, s>>>(b->d_winst, b->d_blk_inst, b->list(), b->count());
+  cudaMemsetAsync(b->count(), 0, sizeof(uint32_t), s);
+  if (nt) {
+    if (b->f32) wide_p2g_kernel<D, float><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
+    else wide_p2g_kernel<D, double><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
+  }
+  NodeP all{};
+  all.bflag = b->flags();
+  all.blist = b->list();
+  all.bcount = b->count();
+  all.nblk = b->nblk;
+  compact_blocks_kernel<<<unsigned((b->nblk + 255) / 256), 256, 0, s>>>(all);
+  if (b->f32) wide_grid_kernel<D, true><<<gctas, 256, 0, s>>>(b->d_winst, b->d_blk_inst, b->list(), b->count());
+  else wide_grid_kernel<D, false><<<gctas, 256, 0, s>>>(b->d_winst, b->d_blk_inst, b->list(), b->count());
+  if (nt) {
+    if (b->f32) wide_g2p_kernel<D, float><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
+    else wide_g2p_kernel<D, double><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
+  }
+}
+
+// zero every node field and the block list (after the persistent kernel, or
+// to drop the node state a timing run left)
+int wide_clean(mpm_batch* b) {
+  const int D = b->dim;
+  int64_t plain = 0, contact = 0;
+  for (const WideInst& W : b->winst) {
+    if (W.contact) contact += W.g.nodeCount * W.cp.nb;
+    else plain += W.g.nodeCount;
+  }
+  if (plain) BATCH_TRY(cudaMemsetAsync(b->nodebuf, 0, size_t(plain) * (1 + 4 * D) * sizeof(double), b->stream));
+  if (contact) BATCH_TRY(cudaMemsetAsync(b->cnodebuf, 0, size_t(contact) * (1 + 5 * D) * sizeof(double), b->stream));
+  BATCH_TRY(cudaMemsetAsync(b->d_blk, 0, size_t(2 * b->nblk + 1) * sizeof(uint32_t), b->stream));
+  b->nodes_dirty = false;
+  return MPM_OK;
+}
+
+int wide_run(mpm_batch* b, int64_t nsteps) {
+  if (b->nodes_dirty) {
+    int r = wide_clean(b);
+    if (r) return r;
+  }
+  if (!b->wexec) {
+    BATCH_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    if (b->dim == 2) wide_enqueue<2>(b);
+    else wide_enqueue<3>(b);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ee = cudaStreamEndCapture(b->stream, &b->wgraph);
+    if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_batch: kernel launch: ") + cudaGetErrorString(le));
+    if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_batch: graph capture: ") + cudaGetErrorString(ee));
+    BATCH_TRY(cudaGraphInstantiate(&b->wexec, b->wgraph, 0));
+  }
+  for (int64_t k = 0; k < nsteps; ++k) BATCH_TRY(cudaGraphLaunch(b->wexec, b->stream));
+  return MPM_OK;
+}
+
+int run_steps(mpm_batch* b, int64_t nsteps) {
+  if (nsteps <= 0) return MPM_OK;
+  if (b->strategy == MPM_BATCH_WIDE) return wide_run(b, nsteps);
+  b->nodes_dirty = true;
+  return launch(b, b->P, nsteps, b->threads, b->ctas_per_sm);
+}
+
 int upload(mpm_batch* b, const PartP& pp, const double* host, int per, int f0, const CompMapH& cm) {
   size_t n = size_t(pp.count) * per;
   if (n == 0 || !host) return MPM_OK;
@@ -291,7 +398,7 @@ template <int D>
 int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
   using L = Layout<D>;
   b->NF = L::NF;
-  int64_t maxbody = 1, nodes = 0, ncoord = 0;
+  int64_t maxbody = 1, nodes = 0, ncoord = 0, plain_nodes = 0, contact_nodes = 0;
   for (int i = 0; i < n; ++i) {
     int64_t nn = 1;
     for (int a = 0; a < D; ++a) {
@@ -299,6 +406,8 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       ncoord += in[i].grid.nodes[a];
     }
     nodes += nn;
+    if (in[i].contact) contact_nodes += nn * in[i].nbodies;
+    else plain_nodes += nn;
     for (int k = 0; k < in[i].nbodies; ++k) {
       b->np += in[i].bodies[k].count;
       maxbody = std::max(maxbody, in[i].bodies[k].count);
@@ -307,9 +416,17 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
   const size_t ptot = size_t(b->NF) * size_t(b->np > 0 ? b->np : 1);
   BATCH_TRY(cudaMalloc(&b->P, ptot * b->esz));
   BATCH_TRY(cudaMemset(b->P, 0, ptot * b->esz));
-  BATCH_TRY(cudaMalloc(&b->nodebuf, size_t(nodes) * (1 + 4 * D) * sizeof(double)));
-  BATCH_TRY(cudaMemset(b->nodebuf, 0, size_t(nodes) * (1 + 4 * D) * sizeof(double)));
-  if (b->f32) BATCH_TRY(cudaMalloc(&b->nodebuf_f, size_t(nodes) * 2 * D * sizeof(float)));
+  // per node: m | p0 (D) | f (D) | vdt (D) | dv (D); contact fields add the normals (D)
+  if (plain_nodes > 0) {
+    BATCH_TRY(cudaMalloc(&b->nodebuf, size_t(plain_nodes) * (1 + 4 * D) * sizeof(double)));
+    BATCH_TRY(cudaMemset(b->nodebuf, 0, size_t(plain_nodes) * (1 + 4 * D) * sizeof(double)));
+    if (b->f32) BATCH_TRY(cudaMalloc(&b->nodebuf_f, size_t(plain_nodes) * 2 * D * sizeof(float)));
+  }
+  if (contact_nodes > 0) {
+    BATCH_TRY(cudaMalloc(&b->cnodebuf, size_t(contact_nodes) * (1 + 5 * D) * sizeof(double)));
+    BATCH_TRY(cudaMemset(b->cnodebuf, 0, size_t(contact_nodes) * (1 + 5 * D) * sizeof(double)));
+    if (b->f32) BATCH_TRY(cudaMalloc(&b->cnodebuf_f, size_t(contact_nodes) * 2 * D * sizeof(float)));
+  }
   BATCH_TRY(cudaMalloc(&b->fixed, size_t(nodes)));
   BATCH_TRY(cudaMalloc(&b->coords, size_t(ncoord) * sizeof(double)));
   BATCH_TRY(cudaMalloc(&b->staging, size_t(maxbody) * 9 * sizeof(double)));
@@ -319,8 +436,9 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
   BATCH_TRY(cudaMalloc(&b->d_next, sizeof(int)));
   std::vector<uint8_t> fixed_h(static_cast<size_t>(nodes), 0);
   std::vector<double> coords_h;
-  int64_t noff = 0, poff = 0;
+  int64_t noff = 0, poff = 0, pnoff = 0, cnoff = 0;
   b->inst.resize(n);
+  b->winst.resize(n);
   for (int i = 0; i < n; ++i) {
     const mpm_instance_desc& d = in[i];
     InstanceP I{};
@@ -348,18 +466,56 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
           if (d.grid.fixed_nodes[a + D * k] == 1) fixed_h[size_t(noff + k)] |= uint8_t(1u << a);
     NodeP& nd = I.nd;
     nd.nodeCount = Nn;
-    double* base = b->nodebuf + size_t(noff) * (1 + 4 * D);
-    nd.m = base;
-    nd.p0 = base + Nn;
-    nd.f = base + Nn * (1 + D);
-    nd.vdt = base + Nn * (1 + 2 * D);
-    nd.dv = base + Nn * (1 + 3 * D);
-    if (b->f32) {
-      nd.vdt_f = b->nodebuf_f + size_t(noff) * 2 * D;
-      nd.dv_f = nd.vdt_f + Nn * D;
-    }
     nd.fixed = b->fixed + noff;
     for (int a = 0; a < 3; ++a) nd.nn[a] = nn[a];
+    // node blocks of the WIDE strategy (global ids blk0 ..)
+    WideInst& W = b->winst[i];
+    W.blk0 = b->nblk;
+    {
+      const int B = BlockShape<D>::B;
+      nd.nblk = 1;
+      for (int a = 0; a < 3; ++a) {
+        nd.nb[a] = a < D ? (nn[a] + B - 1) / B : 1;
+        nd.nblk *= nd.nb[a];
+      }
+      b->nblk += nd.nblk;
+    }
+    if (!d.contact) {
+      double* base = b->nodebuf + size_t(pnoff) * (1 + 4 * D);
+      nd.m = base;
+      nd.p0 = base + Nn;
+      nd.f = base + Nn * (1 + D);
+      nd.vdt = base + Nn * (1 + 2 * D);
+      nd.dv = base + Nn * (1 + 3 * D);
+      if (b->f32) {
+        nd.vdt_f = b->nodebuf_f + size_t(pnoff) * 2 * D;
+        nd.dv_f = nd.vdt_f + Nn * D;
+      }
+      pnoff += Nn;
+      W.contact = 0;
+      W.cp.nb = 1;
+      W.cp.body[0] = nd;
+    } else {
+      W.contact = 1;
+      W.cp.nb = d.nbodies;
+      W.cp.friction = d.friction;
+      for (int k = 0; k < d.nbodies; ++k) {
+        NodeP f = nd;
+        double* base = b->cnodebuf + size_t(cnoff) * (1 + 5 * D);
+        f.m = base;
+        f.p0 = base + Nn;
+        f.f = base + Nn * (1 + D);
+        f.nrm = base + Nn * (1 + 2 * D);
+        f.vdt = base + Nn * (1 + 3 * D);
+        f.dv = base + Nn * (1 + 4 * D);
+        if (b->f32) {
+          f.vdt_f = b->cnodebuf_f + size_t(cnoff) * 2 * D;
+          f.dv_f = f.vdt_f + Nn * D;
+        }
+        W.cp.body[k] = f;
+        cnoff += Nn;
+      }
+    }
     I.pbegin = poff;
     I.nb = d.nbodies;
     for (int k = 0; k < d.nbodies; ++k) {
@@ -381,7 +537,41 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
     I.tol = d.tolerance;
     for (int a = 0; a < 3; ++a) I.grav[a] = a < D ? d.body_force[a] : 0.0;
     b->inst[i] = I;
+    W.g = I.g;
+    W.dt = I.dt;
+    W.tol = I.tol;
+    for (int a = 0; a < 3; ++a) W.grav[a] = I.grav[a];
     noff += Nn;
+  }
+  // WIDE tables: block flags/list/count, block -> problem, bodies, particle tiles
+  BATCH_TRY(cudaMalloc(&b->d_blk, size_t(2 * b->nblk + 1) * sizeof(uint32_t)));
+  BATCH_TRY(cudaMemset(b->d_blk, 0, size_t(2 * b->nblk + 1) * sizeof(uint32_t)));
+  {
+    std::vector<int> blk_inst(static_cast<size_t>(b->nblk));
+    for (int i = 0; i < n; ++i) {
+      WideInst& W = b->winst[i];
+      const int nf = W.contact ? W.cp.nb : 1;
+      for (int k = 0; k < nf; ++k) W.cp.body[k].bflag = b->flags() + W.blk0;
+      for (int64_t q = 0; q < b->inst[i].nd.nblk; ++q) blk_inst[size_t(W.blk0 + q)] = i;
+      for (int k = 0; k < b->inst[i].nb; ++k) {
+        WideBody wb{};
+        wb.pp = b->body(i, k);
+        wb.nd = W.cp.body[W.contact ? k : 0];
+        wb.mp = b->inst[i].mp[k];
+        wb.inst = i;
+        const int body = int(b->wbody.size());
+        for (int64_t t = 0; t < wb.pp.count; t += 256) b->tiles.push_back(WideTile{body, t});
+        b->wbody.push_back(wb);
+      }
+    }
+    BATCH_TRY(cudaMalloc(&b->d_blk_inst, blk_inst.size() * sizeof(int) + sizeof(int)));
+    BATCH_TRY(cudaMemcpy(b->d_blk_inst, blk_inst.data(), blk_inst.size() * sizeof(int), cudaMemcpyHostToDevice));
+    BATCH_TRY(cudaMalloc(&b->d_winst, b->winst.size() * sizeof(WideInst)));
+    BATCH_TRY(cudaMemcpy(b->d_winst, b->winst.data(), b->winst.size() * sizeof(WideInst), cudaMemcpyHostToDevice));
+    BATCH_TRY(cudaMalloc(&b->d_wbody, b->wbody.size() * sizeof(WideBody) + sizeof(WideBody)));
+    BATCH_TRY(cudaMemcpy(b->d_wbody, b->wbody.data(), b->wbody.size() * sizeof(WideBody), cudaMemcpyHostToDevice));
+    BATCH_TRY(cudaMalloc(&b->d_tiles, b->tiles.size() * sizeof(WideTile) + sizeof(WideTile)));
+    BATCH_TRY(cudaMemcpy(b->d_tiles, b->tiles.data(), b->tiles.size() * sizeof(WideTile), cudaMemcpyHostToDevice));
   }
   BATCH_TRY(cudaMemcpy(b->fixed, fixed_h.data(), fixed_h.size(), cudaMemcpyHostToDevice));
   BATCH_TRY(cudaMemcpy(b->coords, coords_h.data(), coords_h.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -472,7 +662,7 @@ int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t prec
   const int D = instances[0].grid.dim;
   if (D != 2 && D != 3) return fail(MPM_ERR_ARG, "mpm_batch_create: dim must be 2 or 3");
   int mat = -1;
-  bool grav = false;
+  bool grav = false, mixed = false, any_contact = false;
   for (int i = 0; i < n; ++i) {
     const mpm_instance_desc& d = instances[i];
     if (d.grid.dim != D) return fail(MPM_ERR_ARG, "mpm_batch_create: all problems must share the dimension");
@@ -484,6 +674,12 @@ int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t prec
     if (!(d.dt > 0.0)) return fail(MPM_ERR_ARG, "mpm_batch_create: dt must be > 0");
     if (d.nbodies < 1 || d.nbodies > MPM_BATCH_MAX_BODIES || !d.bodies)
       return fail(MPM_ERR_ARG, "mpm_batch_create: 1 to MPM_BATCH_MAX_BODIES bodies per problem");
+    if (d.contact != 0 && d.contact != 1) return fail(MPM_ERR_ARG, "mpm_batch_create: contact must be 0 or 1");
+    if (d.contact && d.nbodies > kMaxContactBodies)
+      return fail(MPM_ERR_ARG, "mpm_batch_create: contact mode supports at most " +
+                                   std::to_string(kMaxContactBodies) + " bodies");
+    if (d.contact && !(d.friction >= 0.0)) return fail(MPM_ERR_ARG, "mpm_batch_create: friction < 0");
+    any_contact = any_contact || d.contact;
     for (int a = 0; a < D; ++a) grav = grav || d.body_force[a] != 0.0;
     for (int k = 0; k < d.nbodies; ++k) {
       const mpm_body_desc& bd = d.bodies[k];
@@ -492,8 +688,7 @@ int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t prec
         return fail(MPM_ERR_ARG, "mpm_batch_create: pos, velocity, mass, volume and volume_initial are required");
       if (bd.mat.type != MPM_MAT_ELASTIC && bd.mat.type != MPM_MAT_NEOHOOKEAN && bd.mat.type != MPM_MAT_J2)
         return fail(MPM_ERR_ARG, "mpm_batch_create: unknown material type");
-      if (mat >= 0 && bd.mat.type != mat)
-        return fail(MPM_ERR_ARG, "mpm_batch_create: all bodies of a batch must use the same material model");
+      mixed = mixed || (mat >= 0 && bd.mat.type != mat);
       mat = bd.mat.type;
     }
   }
@@ -504,6 +699,8 @@ int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t prec
   b->mat = mat < 0 ? MPM_MAT_ELASTIC : mat;
   b->grav = grav;
   b->ninst = n;
+  b->persistent_ok = !mixed && !any_contact;
+  b->strategy = b->persistent_ok ? MPM_BATCH_PERSISTENT : MPM_BATCH_WIDE;
   int dev = 0, r = MPM_OK;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -526,7 +723,7 @@ int mpm_batch_step(mpm_batch* b, int64_t nsteps) {
   if (!b || nsteps < 0) return fail(MPM_ERR_ARG, "mpm_batch_step: bad argument");
   BATCH_TRY(cudaMemsetAsync(b->d_status, 0, size_t(b->ninst) * sizeof(unsigned), b->stream));
   BATCH_TRY(cudaEventRecord(b->e0, b->stream));
-  int r = nsteps > 0 ? launch(b, b->P, nsteps, b->threads, b->ctas_per_sm) : MPM_OK;
+  int r = run_steps(b, nsteps);
   if (r) return r;
   BATCH_TRY(cudaEventRecord(b->e1, b->stream));
   BATCH_TRY(cudaStreamSynchronize(b->stream));
@@ -608,6 +805,7 @@ int mpm_batch_tune(mpm_batch* b, int64_t probe_steps, int32_t* threads, int32_t*
   int bt = b->threads, bc = b->ctas_per_sm;
   int rc = MPM_OK;
   for (int th : th_list) {
+    if (!b->persistent_ok) break;
     for (int cps : cta_list) {
       cudaMemcpyAsync(scratch, b->P, bytes, cudaMemcpyDeviceToDevice, b->stream);
       cudaEventRecord(b->e0, b->stream);
@@ -629,14 +827,64 @@ int mpm_batch_tune(mpm_batch* b, int64_t probe_steps, int32_t* threads, int32_t*
     }
     if (rc != MPM_OK) break;
   }
+  int bs = MPM_BATCH_PERSISTENT;
+  if (rc == MPM_OK) {
+    // WIDE: probe_steps on the batch itself, particles saved before and put back after
+    b->nodes_dirty = true;  // the persistent probes above used the node arrays
+    BATCH_TRY(cudaMemcpyAsync(scratch, b->P, bytes, cudaMemcpyDeviceToDevice, b->stream));
+    const int saved = b->strategy;
+    b->strategy = MPM_BATCH_WIDE;
+    int r = wide_run(b, 1);  // builds the step graph outside the timed region
+    if (r == MPM_OK) {
+      cudaEventRecord(b->e0, b->stream);
+      r = wide_run(b, probe_steps - 1 > 0 ? probe_steps - 1 : 1);
+      cudaEventRecord(b->e1, b->stream);
+    }
+    b->strategy = saved;
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) rc = fail(MPM_ERR_CUDA, std::string("mpm_batch_tune: ") + cudaGetErrorString(e));
+    else if (r != MPM_OK) rc = r;
+    if (rc == MPM_OK) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, b->e0, b->e1);
+      const double per = ms * double(probe_steps) / double(probe_steps - 1 > 0 ? probe_steps - 1 : 1);
+      if (per < best) {
+        best = per;
+        bs = MPM_BATCH_WIDE;
+      }
+      cudaMemcpyAsync(b->P, scratch, bytes, cudaMemcpyDeviceToDevice, b->stream);
+      rc = wide_clean(b);
+      if (rc == MPM_OK) {
+        e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) rc = fail(MPM_ERR_CUDA, std::string("mpm_batch_tune: ") + cudaGetErrorString(e));
+      }
+    }
+  }
   cudaFree(scratch);
   if (rc != MPM_OK) return rc;
+  b->strategy = bs;
   b->threads = bt;
   b->ctas_per_sm = bc;
   if (threads) *threads = bt;
   if (ctas_per_sm) *ctas_per_sm = bc;
   if (ms_per_step) *ms_per_step = best / double(probe_steps);
   BATCH_TRY(cudaMemsetAsync(b->d_status, 0, size_t(b->ninst) * sizeof(unsigned), b->stream));
+  return MPM_OK;
+}
+
+int mpm_batch_set_strategy(mpm_batch* b, int32_t strategy) {
+  if (!b || (strategy != MPM_BATCH_PERSISTENT && strategy != MPM_BATCH_WIDE))
+    return fail(MPM_ERR_ARG, "mpm_batch_set_strategy: unknown strategy");
+  if (strategy == MPM_BATCH_PERSISTENT && !b->persistent_ok)
+    return fail(MPM_ERR_ARG, "mpm_batch_set_strategy: the persistent kernel needs one material model type and no "
+                             "contact");
+  b->strategy = strategy;
+  return MPM_OK;
+}
+
+int mpm_batch_strategy(mpm_batch* b, int32_t* strategy) {
+  if (!b || !strategy) return fail(MPM_ERR_ARG, "mpm_batch_strategy: null argument");
+  *strategy = b->strategy;
   return MPM_OK;
 }
 

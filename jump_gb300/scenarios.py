@@ -177,6 +177,20 @@ def sphere_plate(h: float = 5e-4, ppc: int = 2, radius: float = 5e-3, speed: flo
     return grid, [s1, s2], USL(1e-3 * float(s2.mass[0])), data
 
 
+def impact_member(i: int, seed: int = 0, h: float = 5e-4, gap: float = 0.0):
+    """Instance i of the seeded sphere-on-plate impact ensemble: the
+    sphere_plate problem (steel sphere r = 5 mm, neo-Hookean plate 20x20x4 mm,
+    2x2x2 particles per cell, two velocity fields with the frictionless
+    contact correction) with the impact speed uniform in [10, 100] m/s and the
+    plate's Young's modulus uniform in [1e9, 10e9] Pa.  The sphere starts
+    touching the plate (``gap`` = 0) so that every step of a short solve is
+    in contact."""
+    rng = np.random.default_rng([seed, i])
+    speed = float(rng.uniform(10.0, 100.0))
+    E_plate = float(rng.uniform(1e9, 10e9))
+    return sphere_plate(h=h, speed=speed, E_plate=E_plate, gap=gap)
+
+
 def block_3d(h: float = 0.125, ppc: int = 2, size=(1.0, 0.25, 0.25), E_range=(0.5e6, 2e6), nu: float = 0.3,
              rho: float = 1050.0, g: float = -10.0, dt: float = 1e-4, seed: int = 0):
     """A neo-Hookean block clamped at x = 0 sagging under gravity, with a
