@@ -242,6 +242,18 @@ int mpm_batch_set_launch(mpm_batch* batch, int32_t threads, int32_t ctas_per_sm)
    fastest and returns it and its device time per step. */
 int mpm_batch_tune(mpm_batch* batch, int64_t probe_steps, int32_t* threads, int32_t* ctas_per_sm,
                    double* ms_per_step);
+/* Forward-mode derivative (no counterpart in the reference).  Advances every
+   problem nsteps steps exactly as mpm_batch_step (WIDE strategy) while
+   carrying, for each problem, the derivative of its state with respect to
+   one scalar s of that problem: a change of the Young's modulus of its
+   bodies, dE[i * MPM_BATCH_MAX_BODIES + k] = dE_k/ds for body k of problem
+   i (0 for bodies that do not depend on s; NULL: all 0).  Derivatives start
+   at zero at the call.  On return x_dot (or NULL) holds dx/ds of every
+   particle, problems and bodies in order, dim doubles per particle.  FP64
+   batches with elastic and neo-Hookean bodies and frictionless contact;
+   otherwise MPM_ERR_UNSUPPORTED.  The derivative is that of the discrete
+   map within the current cells and contact branches. */
+int mpm_batch_jvp(mpm_batch* batch, int64_t nsteps, const double* dE, double* x_dot);
 /* MPM_BATCH_PERSISTENT or MPM_BATCH_WIDE (MPM_ERR_ARG where not allowed) */
 int mpm_batch_set_strategy(mpm_batch* batch, int32_t strategy);
 int mpm_batch_strategy(mpm_batch* batch, int32_t* strategy);

@@ -44,6 +44,7 @@ MPM_PREC_F32 = 1
 
 MPM_BATCH_PERSISTENT = 0
 MPM_BATCH_WIDE = 1
+MPM_BATCH_MAX_BODIES = 4
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int64)
@@ -161,6 +162,7 @@ SIGNATURES = {
     "mpm_batch_energies": (C.c_int, [C.c_void_p, _dp]),
     "mpm_batch_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "mpm_batch_tune": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp]),
+    "mpm_batch_jvp": (C.c_int, [C.c_void_p, C.c_int64, _dp, _dp]),
     "mpm_batch_set_strategy": (C.c_int, [C.c_void_p, C.c_int32]),
     "mpm_batch_strategy": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "mpm_batch_last_ms": (C.c_int, [C.c_void_p, _dp]),

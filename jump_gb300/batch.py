@@ -119,6 +119,24 @@ class Ensemble:
             _capi.check(rc, self.L)
         return rc
 
+    def jvp(self, nsteps: int, dE) -> list:
+        """Advance nsteps steps (as step) and return, per problem, dx/ds of its
+        particles (bodies in order, (n, dim)), where s is one scalar per problem
+        and dE[i][k] = dE_k/ds is the change of body k's Young's modulus.
+        Forward-mode derivative through mpm_batch_jvp (FP64 batches, elastic
+        and neo-Hookean bodies, frictionless contact)."""
+        seeds = np.zeros((self.n, _capi.MPM_BATCH_MAX_BODIES))
+        for i, row in enumerate(dE):
+            seeds[i, :len(row)] = row
+        xd = np.zeros(self.particles * self.dim)
+        _capi.check(self.L.mpm_batch_jvp(self.h, int(nsteps), _capi.dptr(seeds.ravel()), _capi.dptr(xd)), self.L)
+        out, off = [], 0
+        for c in self.counts:
+            k = sum(c)
+            out.append(xd[off * self.dim:(off + k) * self.dim].reshape(k, self.dim))
+            off += k
+        return out
+
     def status(self):
         st = (C.c_int32 * self.n)()
         _capi.check(self.L.mpm_batch_status(self.h, st), self.L)

@@ -27,6 +27,7 @@
 #include "mpm_internal.h"
 #include "mpm_kernels.cuh"
 #include "mpm_wide.cuh"
+#include "mpm_tangent.cuh"
 
 using namespace jmpm;
 
@@ -210,6 +211,8 @@ struct mpm_batch {
   int strategy = MPM_BATCH_PERSISTENT;
   // WIDE strategy tables and node bookkeeping
   std::vector<WideBody> wbody;
+  std::vector<int> wbody_k;       // index of each table body within its problem
+  std::vector<double> wbody_nu;   // its Poisson ratio
   std::vector<WideInst> winst;
   std::vector<WideTile> tiles;
   WideBody* d_wbody = nullptr;
@@ -223,6 +226,16 @@ struct mpm_batch {
   cudaGraph_t wgraph = nullptr;
   cudaGraphExec_t wexec = nullptr;
   bool nodes_dirty = false;  // the persistent kernel left node data the WIDE list does not cover
+  // forward-mode derivatives (mpm_batch_jvp): tangent particle fields and node fields
+  double* tpart = nullptr;
+  double* tnodebuf = nullptr;
+  size_t tnode_doubles = 0;
+  std::vector<TanBody> tbody;
+  std::vector<TanInst> tinst;
+  TanBody* d_tbody = nullptr;
+  TanInst* d_tinst = nullptr;
+  cudaGraph_t jgraph = nullptr;
+  cudaGraphExec_t jexec = nullptr;
 
   PartP body(int i, int b) const { return PartP{P, np, inst[i].bbeg[b], inst[i].bcnt[b]}; }
   uint32_t* flags() const { return d_blk; }
@@ -254,6 +267,12 @@ void destroy_batch(mpm_batch* b) {
   cudaFree(b->cnodebuf_f);
   if (b->wexec) cudaGraphExecDestroy(b->wexec);
   if (b->wgraph) cudaGraphDestroy(b->wgraph);
+  cudaFree(b->tpart);
+  cudaFree(b->tnodebuf);
+  cudaFree(b->d_tbody);
+  cudaFree(b->d_tinst);
+  if (b->jexec) cudaGraphExecDestroy(b->jexec);
+  if (b->jgraph) cudaGraphDestroy(b->jgraph);
   if (b->e0) cudaEventDestroy(b->e0);
   if (b->e1) cudaEventDestroy(b->e1);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -362,6 +381,116 @@ int wide_run(mpm_batch* b, int64_t nsteps) {
     BATCH_TRY(cudaGraphInstantiate(&b->wexec, b->wgraph, 0));
   }
   for (int64_t k = 0; k < nsteps; ++k) BATCH_TRY(cudaGraphLaunch(b->wexec, b->stream));
+  return MPM_OK;
+}
+
+// ---- forward-mode derivatives -------------------------------------------------
+template <int D>
+void jvp_enqueue(mpm_batch* b) {
+  cudaStream_t s = b->stream;
+  const unsigned nt = unsigned(b->tiles.size());
+  const int64_t most = (b->nblk * 64 + 255) / 256;
+  const unsigned gctas = unsigned(std::max<int64_t>(1, std::min<int64_t>(most, int64_t(b->sms) * 8)));
+  wide_clear_kernel<D><<<gctas, 256, 0, s>>>(b->d_winst, b->d_blk_inst, b->list(), b->count());
+  tan_clear_kernel<D><<<gctas, 256, 0, s>>>(b->d_winst, b->d_tinst, b->d_blk_inst, b->list(), b->count());
+  cudaMemsetAsync(b->count(), 0, sizeof(uint32_t), s);
+  if (nt) {
+    wide_p2g_kernel<D, double><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
+    tan_p2g_kernel<D><<<nt, 256, 0, s>>>(b->d_wbody, b->d_tbody, b->d_winst, b->d_tiles);
+  }
+  NodeP all{};
+  all.bflag = b->flags();
+  all.blist = b->list();
+  all.bcount = b->count();
+  all.nblk = b->nblk;
+  compact_blocks_kernel<<<unsigned((b->nblk + 255) / 256), 256, 0, s>>>(all);
+  wide_grid_kernel<D, false><<<gctas, 256, 0, s>>>(b->d_winst, b->d_blk_inst, b->list(), b->count());
+  tan_grid_kernel<D><<<gctas, 256, 0, s>>>(b->d_winst, b->d_tinst, b->d_blk_inst, b->list(), b->count());
+  if (nt) {
+    // the tangent G2P reads the state the primal G2P overwrites: it goes first
+    tan_g2p_kernel<D><<<nt, 256, 0, s>>>(b->d_wbody, b->d_tbody, b->d_winst, b->d_tiles);
+    wide_g2p_kernel<D, double><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
+  }
+}
+
+// tangent buffers and tables (first call), seeds (every call)
+int jvp_setup(mpm_batch* b, const double* dE) {
+  const int D = b->dim;
+  const int NT = D == 2 ? TanLayout<2>::NT : TanLayout<3>::NT;
+  if (!b->tpart) {
+    BATCH_TRY(cudaMalloc(&b->tpart, size_t(NT) * size_t(b->np > 0 ? b->np : 1) * sizeof(double)));
+    size_t nd = 0;
+    for (const WideInst& W : b->winst)
+      nd += size_t(W.g.nodeCount) * (W.contact ? size_t(W.cp.nb) * (1 + 5 * D) : size_t(1 + 4 * D));
+    b->tnode_doubles = nd;
+    BATCH_TRY(cudaMalloc(&b->tnodebuf, (nd > 0 ? nd : 1) * sizeof(double)));
+    b->tinst.resize(b->winst.size());
+    size_t off = 0;
+    for (size_t i = 0; i < b->winst.size(); ++i) {
+      const WideInst& W = b->winst[i];
+      TanInst& T = b->tinst[i];
+      T.tcp = W.cp;
+      const int64_t Nn = W.g.nodeCount;
+      const int nf = W.contact ? W.cp.nb : 1;
+      const int per = W.contact ? 1 + 5 * D : 1 + 4 * D;
+      for (int k = 0; k < nf; ++k) {
+        NodeP f = W.cp.body[k];
+        double* base = b->tnodebuf + off;
+        f.m = base;
+        f.p0 = base + Nn;
+        f.f = base + Nn * (1 + D);
+        f.nrm = W.contact ? base + Nn * (1 + 2 * D) : nullptr;
+        f.vdt = base + Nn * (W.contact ? 1 + 3 * D : 1 + 2 * D);
+        f.dv = base + Nn * (W.contact ? 1 + 4 * D : 1 + 3 * D);
+        f.vdt_f = f.dv_f = nullptr;
+        f.bflag = nullptr;
+        T.tcp.body[k] = f;
+        off += size_t(Nn) * per;
+      }
+    }
+    BATCH_TRY(cudaMalloc(&b->d_tinst, b->tinst.size() * sizeof(TanInst)));
+    BATCH_TRY(cudaMemcpy(b->d_tinst, b->tinst.data(), b->tinst.size() * sizeof(TanInst), cudaMemcpyHostToDevice));
+    BATCH_TRY(cudaMalloc(&b->d_tbody, b->wbody.size() * sizeof(TanBody) + sizeof(TanBody)));
+  }
+  b->tbody.resize(b->wbody.size());
+  for (size_t q = 0; q < b->wbody.size(); ++q) {
+    const WideBody& wb = b->wbody[q];
+    TanBody& tb = b->tbody[q];
+    tb.tp = wb.pp;
+    tb.tp.base = b->tpart;
+    const WideInst& W = b->winst[wb.inst];
+    const int k = b->wbody_k[q];
+    tb.tnd = b->tinst[wb.inst].tcp.body[W.contact ? k : 0];
+    const double nu = b->wbody_nu[q];
+    const double e = dE ? dE[size_t(wb.inst) * MPM_BATCH_MAX_BODIES + k] : 0.0;
+    tb.dlam = e * nu / (1 + nu) / (1 - 2 * nu);  // d lambda / dE times dE (Material.jl:54)
+    tb.dmu = e / 2 / (1 + nu);                   // d mu / dE times dE (Material.jl:55)
+  }
+  BATCH_TRY(cudaMemcpyAsync(b->d_tbody, b->tbody.data(), b->tbody.size() * sizeof(TanBody), cudaMemcpyHostToDevice,
+                            b->stream));
+  // tangents start at zero: the state at the call does not depend on the scalar
+  BATCH_TRY(cudaMemsetAsync(b->tpart, 0, size_t(NT) * size_t(b->np > 0 ? b->np : 1) * sizeof(double), b->stream));
+  BATCH_TRY(cudaMemsetAsync(b->tnodebuf, 0, (b->tnode_doubles > 0 ? b->tnode_doubles : 1) * sizeof(double),
+                            b->stream));
+  return MPM_OK;
+}
+
+int jvp_run(mpm_batch* b, int64_t nsteps) {
+  if (b->nodes_dirty) {
+    int r = wide_clean(b);
+    if (r) return r;
+  }
+  if (!b->jexec) {
+    BATCH_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    if (b->dim == 2) jvp_enqueue<2>(b);
+    else jvp_enqueue<3>(b);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ee = cudaStreamEndCapture(b->stream, &b->jgraph);
+    if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_batch_jvp: kernel launch: ") + cudaGetErrorString(le));
+    if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_batch_jvp: graph capture: ") + cudaGetErrorString(ee));
+    BATCH_TRY(cudaGraphInstantiate(&b->jexec, b->jgraph, 0));
+  }
+  for (int64_t k = 0; k < nsteps; ++k) BATCH_TRY(cudaGraphLaunch(b->jexec, b->stream));
   return MPM_OK;
 }
 
@@ -562,6 +691,8 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
         const int body = int(b->wbody.size());
         for (int64_t t = 0; t < wb.pp.count; t += 256) b->tiles.push_back(WideTile{body, t});
         b->wbody.push_back(wb);
+        b->wbody_k.push_back(k);
+        b->wbody_nu.push_back(in[i].bodies[k].mat.nu);
       }
     }
     BATCH_TRY(cudaMalloc(&b->d_blk_inst, blk_inst.size() * sizeof(int) + sizeof(int)));
@@ -869,6 +1000,52 @@ int mpm_batch_tune(mpm_batch* b, int64_t probe_steps, int32_t* threads, int32_t*
   if (ctas_per_sm) *ctas_per_sm = bc;
   if (ms_per_step) *ms_per_step = best / double(probe_steps);
   BATCH_TRY(cudaMemsetAsync(b->d_status, 0, size_t(b->ninst) * sizeof(unsigned), b->stream));
+  return MPM_OK;
+}
+
+int mpm_batch_jvp(mpm_batch* b, int64_t nsteps, const double* dE, double* x_dot) {
+  if (!b || nsteps < 0) return fail(MPM_ERR_ARG, "mpm_batch_jvp: bad argument");
+  if (b->f32) return fail(MPM_ERR_UNSUPPORTED, "mpm_batch_jvp: needs an FP64 batch");
+  for (size_t q = 0; q < b->wbody.size(); ++q) {
+    const int t = b->wbody[q].mp.type;
+    if (t != MPM_MAT_ELASTIC && t != MPM_MAT_NEOHOOKEAN)
+      return fail(MPM_ERR_UNSUPPORTED, "mpm_batch_jvp: elastic and neo-Hookean bodies only");
+  }
+  for (const WideInst& W : b->winst)
+    if (W.contact && b->dim == 2 && W.cp.friction > 0.0)
+      return fail(MPM_ERR_UNSUPPORTED, "mpm_batch_jvp: frictionless contact only");
+  int r = jvp_setup(b, dE);
+  if (r) return r;
+  BATCH_TRY(cudaMemsetAsync(b->d_status, 0, size_t(b->ninst) * sizeof(unsigned), b->stream));
+  BATCH_TRY(cudaEventRecord(b->e0, b->stream));
+  if ((r = jvp_run(b, nsteps))) return r;
+  BATCH_TRY(cudaEventRecord(b->e1, b->stream));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
+  float ms = 0.f;
+  BATCH_TRY(cudaEventElapsedTime(&ms, b->e0, b->e1));
+  b->last_ms = ms;
+  if (x_dot) {
+    const int D = b->dim;
+    size_t off = 0;
+    for (int i = 0; i < b->ninst; ++i)
+      for (int k = 0; k < b->inst[i].nb; ++k) {
+        PartP tp = b->body(i, k);
+        tp.base = b->tpart;
+        if (D == 2) Launchers<2>::soa_to_aos(b->stream, tp, false, b->staging, D, TanLayout<2>::XD, ident(D));
+        else Launchers<3>::soa_to_aos(b->stream, tp, false, b->staging, D, TanLayout<3>::XD, ident(D));
+        BATCH_TRY(cudaGetLastError());
+        BATCH_TRY(cudaMemcpyAsync(x_dot + off, b->staging, size_t(tp.count) * D * sizeof(double),
+                                  cudaMemcpyDeviceToHost, b->stream));
+        BATCH_TRY(cudaStreamSynchronize(b->stream));
+        off += size_t(tp.count) * D;
+      }
+  }
+  std::vector<unsigned> st(static_cast<size_t>(b->ninst));
+  BATCH_TRY(cudaMemcpy(st.data(), b->d_status, st.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
+  unsigned all = 0;
+  for (unsigned v : st) all |= v;
+  r = status_code(all);
+  if (r != MPM_OK) return fail(r, "mpm_batch_jvp: a problem reported a failure (see mpm_batch_status)");
   return MPM_OK;
 }
 
