@@ -394,10 +394,7 @@ void jvp_enqueue(mpm_batch* b) {
   wide_clear_kernel<D><<<gctas, 256, 0, s>>>(b->d_winst, b->d_blk_inst, b->list(), b->count());
   tan_clear_kernel<D><<<gctas, 256, 0, s>>>(b->d_winst, b->d_tinst, b->d_blk_inst, b->list(), b->count());
   cudaMemsetAsync(b->count(), 0, sizeof(uint32_t), s);
-  if (nt) {
-    wide_p2g_kernel<D, double><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
-    tan_p2g_kernel<D><<<nt, 256, 0, s>>>(b->d_wbody, b->d_tbody, b->d_winst, b->d_tiles);
-  }
+  if (nt) tan_p2g_kernel<D><<<nt, 256, 0, s>>>(b->d_wbody, b->d_tbody, b->d_winst, b->d_tiles, b->d_status);
   NodeP all{};
   all.bflag = b->flags();
   all.blist = b->list();
@@ -406,11 +403,8 @@ void jvp_enqueue(mpm_batch* b) {
   compact_blocks_kernel<<<unsigned((b->nblk + 255) / 256), 256, 0, s>>>(all);
   wide_grid_kernel<D, false><<<gctas, 256, 0, s>>>(b->d_winst, b->d_blk_inst, b->list(), b->count());
   tan_grid_kernel<D><<<gctas, 256, 0, s>>>(b->d_winst, b->d_tinst, b->d_blk_inst, b->list(), b->count());
-  if (nt) {
-    // the tangent G2P reads the state the primal G2P overwrites: it goes first
-    tan_g2p_kernel<D><<<nt, 256, 0, s>>>(b->d_wbody, b->d_tbody, b->d_winst, b->d_tiles);
-    wide_g2p_kernel<D, double><<<nt, 256, 0, s>>>(b->d_wbody, b->d_winst, b->d_tiles, b->d_status);
-  }
+  // per particle: the tangent G2P reads the state the primal G2P then overwrites
+  if (nt) tan_g2p_kernel<D><<<nt, 256, 0, s>>>(b->d_wbody, b->d_tbody, b->d_winst, b->d_tiles, b->d_status);
 }
 
 // tangent buffers and tables (first call), seeds (every call)

@@ -2,20 +2,23 @@
 // batched problems that each depend on one scalar (e.g. a Young's modulus).
 //
 // Every primal quantity q of a step gets a tangent q' = dq/ds.  The primal
-// kernels run unchanged; these kernels run beside them and recompute the
-// primal intermediate values they need:
+// device functions run unchanged inside these kernels (same thread, same
+// particle), and the tangent code recomputes the primal intermediate values
+// it needs:
 //
-//   tan_p2g    after the primal P2G (P2G does not change particles):
+//   tan_p2g    the primal P2G of the particle, then (P2G does not change
+//              particles) its tangent scatter:
 //                m'_I  += m N'                        N'  = grad N . x'
 //                p0'_I += m (N' v + N v')
 //                f'_I  += -(V' sig + V sig') grad N - V sig (grad N)' + m b N'
 //                n'_I  += m (grad N)'                 (grad N)' = H x'
 //              H is the Hessian of the multilinear hat (off-diagonal only).
-//   tan_grid   after the primal grid update: the tangents of
+//   tan_grid   after the primal grid update (own launch): the tangents of
 //              p = p0 + f dt, the Dirichlet mask, vdt = p/m dt,
 //              dv = (p - p0)/m, and of the frictionless contact correction
 //              (system velocity, common normal, approach rate D1 > 0).
-//   tan_g2p    before the primal G2P (it reads the state G2P overwrites):
+//   tan_g2p    the tangent G2P from the state before the step, then the
+//              primal G2P of the same particle, which overwrites that state:
 //                x' += N' vdt + N vdt',  v' += N' dv + N dv'
 //                (L dt)' = vdt' (x) grad N + vdt (x) (grad N)'
 //                F_new' = F' (I + L dt) + F (L dt)',  J' = cof(F_new) : F_new'
@@ -83,11 +86,12 @@ __device__ __forceinline__ double& tf(const PartP& tp, int f, int64_t p) {
   return static_cast<double*>(tp.base)[int64_t(f) * tp.pitch + p];
 }
 
+// primal P2G of the particle (p2g_particle, unchanged) followed by its tangent scatter
 template <int D>
 __global__ void __launch_bounds__(256) tan_p2g_kernel(const WideBody* __restrict__ bodies,
                                                       const TanBody* __restrict__ tbodies,
                                                       const WideInst* __restrict__ inst,
-                                                      const WideTile* __restrict__ tiles) {
+                                                      const WideTile* __restrict__ tiles, unsigned* status) {
   using L = Layout<D>;
   using T = TanLayout<D>;
   __shared__ WideBody sB;
@@ -103,13 +107,17 @@ __global__ void __launch_bounds__(256) tan_p2g_kernel(const WideBody* __restrict
   if (threadIdx.x < 3) sGrav[threadIdx.x] = I->grav[threadIdx.x];
   __syncthreads();
   const int64_t t = tl.start + threadIdx.x;
+  if (sGrav[0] != 0.0 || sGrav[1] != 0.0 || sGrav[2] != 0.0)
+    p2g_particle<D, double, true>(sG, sB.nd, sB.pp, t, sGrav[0], sGrav[1], sGrav[2], status + sB.inst);
+  else
+    p2g_particle<D, double, false>(sG, sB.nd, sB.pp, t, 0.0, 0.0, 0.0, status + sB.inst);
   if (t >= sB.pp.count) return;
   const int64_t p = sB.pp.begin + t;
   double x[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) x[a] = *field<double>(sB.pp, L::X + a, p);
   Hat<D, double> h;
-  if (!hat<D, double>(sG, x, h)) return;  // the primal P2G reported it
+  if (!hat<D, double>(sG, x, h)) return;  // reported by the primal P2G
   Corners<D, double> cr;
   corners<D, double>(sG, h, cr);
   const double m = *field<double>(sB.pp, L::M, p), V = *field<double>(sB.pp, L::VOL, p);
@@ -126,6 +134,19 @@ __global__ void __launch_bounds__(256) tan_p2g_kernel(const WideBody* __restrict
     sg[c] = *field<double>(sB.pp, L::SIG + c, p);
     sd[c] = tf<D>(sT.tp, T::SD + c, p);
   }
+  // per particle: -(V' sig + V sig') and -V sig, so each corner costs two dot products
+  double A[L::S], B[L::S], mg[D], mv[D], mvd[D];
+#pragma unroll
+  for (int c = 0; c < L::S; ++c) {
+    A[c] = -(Vd * sg[c] + V * sd[c]);
+    B[c] = -V * sg[c];
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    mg[a] = m * sGrav[a];
+    mv[a] = m * v[a];
+    mvd[a] = m * vd[a];
+  }
   const NodeP& tn = sT.tnd;
   const int64_t Nn = tn.nodeCount;
 #pragma unroll
@@ -140,14 +161,14 @@ __global__ void __launch_bounds__(256) tan_p2g_kernel(const WideBody* __restrict
     const int64_t n = cr.node[k];
     atomicAdd(tn.m + n, m * Nd);
 #pragma unroll
-    for (int a = 0; a < D; ++a) atomicAdd(tn.p0 + a * Nn + n, m * (Nd * v[a] + N * vd[a]));
+    for (int a = 0; a < D; ++a) atomicAdd(tn.p0 + a * Nn + n, Nd * mv[a] + N * mvd[a]);
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      double fa = sGrav[a] * m * Nd;
+      double fa = mg[a] * Nd;
 #pragma unroll
       for (int j = 0; j < D; ++j) {
         const int c = sym<D>(a, j);
-        fa -= (Vd * sg[c] + V * sd[c]) * cr.dN[k][j] + V * sg[c] * gd[j];
+        fa += A[c] * cr.dN[k][j] + B[c] * gd[j];
       }
       atomicAdd(tn.f + a * Nn + n, fa);
     }
@@ -345,24 +366,39 @@ __device__ __forceinline__ void cofactor(const double* A, double* C) {
   }
 }
 
+// tangent G2P of the particle from the state before the step
+template <int D>
+__device__ __forceinline__ void tan_g2p_particle(const WideBody& sB, const TanBody& sT, const GridP& sG, int64_t t);
+
+// tangent G2P, then the primal G2P (g2p_particle, unchanged) of the same particle
 template <int D>
 __global__ void __launch_bounds__(256) tan_g2p_kernel(const WideBody* __restrict__ bodies,
                                                       const TanBody* __restrict__ tbodies,
                                                       const WideInst* __restrict__ inst,
-                                                      const WideTile* __restrict__ tiles) {
-  using L = Layout<D>;
-  using T = TanLayout<D>;
+                                                      const WideTile* __restrict__ tiles, unsigned* status) {
   __shared__ WideBody sB;
   __shared__ TanBody sT;
   __shared__ GridP sG;
+  __shared__ double sDt;
   const WideTile tl = tiles[blockIdx.x];
   stage(&sB, bodies + tl.body);
   stage(&sT, tbodies + tl.body);
   __syncthreads();
   stage(&sG, &inst[sB.inst].g);
+  if (threadIdx.x == 0) sDt = inst[sB.inst].dt;
   __syncthreads();
   const int64_t t = tl.start + threadIdx.x;
   if (t >= sB.pp.count) return;
+  tan_g2p_particle<D>(sB, sT, sG, t);
+  unsigned* st = status + sB.inst;
+  if (sB.mp.type == MPM_MAT_ELASTIC) g2p_particle<D, double, MPM_MAT_ELASTIC>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st);
+  else g2p_particle<D, double, MPM_MAT_NEOHOOKEAN>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st);
+}
+
+template <int D>
+__device__ __forceinline__ void tan_g2p_particle(const WideBody& sB, const TanBody& sT, const GridP& sG, int64_t t) {
+  using L = Layout<D>;
+  using T = TanLayout<D>;
   const int64_t p = sB.pp.begin + t;
   const PartP& pp = sB.pp;
   const PartP& tp = sT.tp;
