@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 2
+#define JUMP_MPM_ABI_VERSION 3
 
 /* status codes */
 #define MPM_OK               0
@@ -49,6 +49,7 @@ extern "C" {
 #define MPM_ERR_OUT_OF_GRID  5  /* a particle's cell lies outside the grid; it was frozen */
 #define MPM_ERR_TIMEOUT      6  /* a bounded device-side wait gave up */
 #define MPM_ERR_UNSUPPORTED  7  /* feature not available in this build */
+#define MPM_ERR_SOLVER       8  /* the 2D MUSL mass solve did not converge in its iteration cap */
 
 /* material models (Material.jl) */
 #define MPM_MAT_ELASTIC     0   /* ElasticMaterial, Material.jl:37-81 */
@@ -58,6 +59,12 @@ extern "C" {
 /* particle precision (grid accumulation is always FP64) */
 #define MPM_PREC_F64        0   /* every particle field and every operation in FP64 */
 #define MPM_PREC_F32        1   /* FP32 particle fields and arithmetic; FP64 nodes, det F, energies */
+
+/* Update scheme (the `alg` argument of solve_explicit_dynamics_2D/3D) */
+#define MPM_ALG_USL         0   /* USL(tolerance), SolveExplicitSolidMechanics2D.jl:335-585 */
+#define MPM_ALG_MUSL        1   /* MUSL(alpha): 2D SolveExplicitSolidMechanics2D.jl:24-329 (blended
+                                   consistent mass), 3D SolveExplicitSolidMechanics3D.jl:14-223
+                                   (lumped mass); FP64, one velocity field */
 
 typedef struct mpm_grid_desc {
   int32_t dim;                 /* 2 (Grid2D) or 3 (Grid3D) */
@@ -115,6 +122,9 @@ typedef struct mpm_params {
   double  friction;            /* Coulomb coefficient for contact (2D only; 0 = frictionless) */
   int32_t sort_interval;       /* re-sort particles by cell every N steps (0 = never) */
   int32_t flags;               /* reserved, 0 */
+  int32_t algorithm;           /* MPM_ALG_USL or MPM_ALG_MUSL */
+  int32_t reserved;
+  double  alpha;               /* MUSL.alpha: FLIP/PIC blend, Algorithm.jl:38-40 (MUSL only) */
 } mpm_params;
 
 typedef struct mpm_ctx mpm_ctx;

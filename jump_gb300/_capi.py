@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-ABI_VERSION = 2  # JUMP_MPM_ABI_VERSION of the structures below
+ABI_VERSION = 3  # JUMP_MPM_ABI_VERSION of the structures below
 
 MPM_OK = 0
 MPM_ERR_ARG = 1
@@ -24,6 +24,7 @@ MPM_ERR_NONFINITE = 4
 MPM_ERR_OUT_OF_GRID = 5
 MPM_ERR_TIMEOUT = 6
 MPM_ERR_UNSUPPORTED = 7
+MPM_ERR_SOLVER = 8
 
 ERR_NAMES = {
     MPM_ERR_ARG: "MPM_ERR_ARG",
@@ -33,6 +34,7 @@ ERR_NAMES = {
     MPM_ERR_OUT_OF_GRID: "MPM_ERR_OUT_OF_GRID",
     MPM_ERR_TIMEOUT: "MPM_ERR_TIMEOUT",
     MPM_ERR_UNSUPPORTED: "MPM_ERR_UNSUPPORTED",
+    MPM_ERR_SOLVER: "MPM_ERR_SOLVER",
 }
 
 MPM_MAT_ELASTIC = 0
@@ -41,6 +43,9 @@ MPM_MAT_J2 = 2
 
 MPM_PREC_F64 = 0
 MPM_PREC_F32 = 1
+
+MPM_ALG_USL = 0
+MPM_ALG_MUSL = 1
 
 MPM_BATCH_PERSISTENT = 0
 MPM_BATCH_WIDE = 1
@@ -115,6 +120,9 @@ class Params(C.Structure):
         ("friction", C.c_double),
         ("sort_interval", C.c_int32),
         ("flags", C.c_int32),
+        ("algorithm", C.c_int32),
+        ("reserved", C.c_int32),
+        ("alpha", C.c_double),
     ]
 
 

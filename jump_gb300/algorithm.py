@@ -17,7 +17,8 @@ class USL(AlgorithmType):
 
 
 class MUSL(AlgorithmType):
-    """Modified USL with FLIP/PIC blend ``alpha`` (Algorithm.jl:37-39); not accelerated here."""
+    """Modified USL with FLIP/PIC blend ``alpha`` (Algorithm.jl:37-39): particle
+    velocities v <- alpha v + sum N (v_I - alpha v0_I) before the kinematics."""
 
     def __init__(self, alpha):
         self.alpha = float(alpha)

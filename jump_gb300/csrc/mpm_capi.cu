@@ -94,6 +94,8 @@ struct mpm_ctx {
   double* contactbuf = nullptr;
   float* contactbuf_f = nullptr;
   double* nodebuf = nullptr;
+  double* muslbuf = nullptr;  // MUSL: 3D p2 | vg; 2D mass stencil (9) | vg | CG vectors (16)
+  CgP cg{};
   float* nodebuf_f = nullptr;
   std::vector<uint8_t> fixed_h;
   unsigned* status = nullptr;
@@ -145,6 +147,7 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->coords);
   cudaFree(c->fixed);
   cudaFree(c->nodebuf);
+  cudaFree(c->muslbuf);
   cudaFree(c->nodebuf_f);
   cudaFree(c->blockbuf);
   for (int i = 0; i < 2; ++i) {
@@ -256,7 +259,38 @@ CompMapH full_from_sym(int dim) {
 
 // The launches of one USL step; ev (optional) gets an event recorded after each stage.
 // rec (optional): receives this step's grid outputs m | vdt (D) | dv (D) for the adjoint
+// One MUSL step (mpm_musl.cuh); ev as enqueue_step.
+void enqueue_musl(mpm_ctx* c, cudaEvent_t* ev) {
+  const int D = c->dim;
+  if (D == 2) Launchers<2>::clear(c->stream, c->nd);
+  else Launchers<3>::clear(c->stream, c->nd);
+  cudaMemsetAsync(c->nd.bcount, 0, sizeof(uint32_t), c->stream);
+  if (ev) cudaEventRecord(ev[0], c->stream);
+  for (int b = 0; b < c->nb; ++b) {
+    if (D == 2) Launchers<2>::musl_p2g(c->stream, c->g, c->nd, c->part(b), c->prm.body_force, c->status);
+    else Launchers<3>::musl_p2g(c->stream, c->g, c->nd, c->part(b), c->prm.body_force, c->status);
+  }
+  if (ev) cudaEventRecord(ev[1], c->stream);
+  if (D == 2) Launchers<2>::musl_grid(c->stream, c->nd, c->cg, c->prm.dt, c->prm.alpha, c->status);
+  else Launchers<3>::musl_grid(c->stream, c->nd, c->cg, c->prm.dt, c->prm.alpha, c->status);
+  if (ev) cudaEventRecord(ev[2], c->stream);
+  for (int b = 0; b < c->nb; ++b) {
+    if (D == 2) Launchers<2>::musl_g2p1(c->stream, c->g, c->nd, c->part(b), c->prm.alpha, c->status);
+    else Launchers<3>::musl_g2p1(c->stream, c->g, c->nd, c->part(b), c->prm.alpha, c->status);
+  }
+  if (D == 3) Launchers<3>::musl_vg(c->stream, c->nd, c->prm.dt);
+  for (int b = 0; b < c->nb; ++b) {
+    if (D == 2) Launchers<2>::musl_g2p2(c->stream, c->g, c->nd, c->part(b), c->mats[b], c->status);
+    else Launchers<3>::musl_g2p2(c->stream, c->g, c->nd, c->part(b), c->mats[b], c->status);
+  }
+  if (ev) cudaEventRecord(ev[3], c->stream);
+}
+
 void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
+  if (c->prm.algorithm == MPM_ALG_MUSL) {
+    enqueue_musl(c, ev);
+    return;
+  }
   const int D = c->dim;
   const bool contact = c->prm.contact != 0;
   // node field of body b: its own in contact mode, else the shared one
@@ -311,6 +345,7 @@ int status_to_code(unsigned st) {
   if (st & ST_OUT_OF_GRID) return fail(MPM_ERR_OUT_OF_GRID, "a particle left the grid; it was frozen in place");
   if (st & ST_NONFINITE) return fail(MPM_ERR_NONFINITE, "non-finite particle velocity, position or stress");
   if (st & ST_NEGATIVE_J) return fail(MPM_ERR_NEGATIVE_J, "det F <= 0 at a particle");
+  if (st & ST_SOLVER) return fail(MPM_ERR_SOLVER, "the MUSL mass solve did not converge");
   return MPM_OK;
 }
 
@@ -412,6 +447,26 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
         f.dv_f = f.vdt_f + Nn * D;
       }
       c->cp.body[b] = f;
+    }
+  }
+  if (prm->algorithm == MPM_ALG_MUSL) {
+    // 3D: p2 (D) | vg (D); 2D: mass stencil (9) | vg (D) | CG x, r, p, q of four right-hand sides
+    const size_t per = D == 3 ? size_t(2 * D) : size_t(9 + D + 16);
+    CUDA_TRY(cudaMalloc(&c->muslbuf, size_t(Nn) * per * sizeof(double)));
+    CUDA_TRY(cudaMemset(c->muslbuf, 0, size_t(Nn) * per * sizeof(double)));
+    if (D == 3) {
+      c->nd.p2 = c->muslbuf;
+      c->nd.vg = c->muslbuf + Nn * D;
+    } else {
+      c->nd.mc = c->muslbuf;
+      c->nd.vg = c->muslbuf + Nn * 9;
+      double* v = c->muslbuf + Nn * (9 + D);
+      for (int k = 0; k < 4; ++k) {
+        c->cg.x[k] = v + Nn * (0 + k);
+        c->cg.r[k] = v + Nn * (4 + k);
+        c->cg.p[k] = v + Nn * (8 + k);
+        c->cg.q[k] = v + Nn * (12 + k);
+      }
     }
   }
   if (c->f32) {
@@ -546,6 +601,10 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
       return fail(MPM_ERR_ARG, "mpm_create: too many (body, cell) keys for the particle sort");
   }
   if (params->sort_interval < 0) return fail(MPM_ERR_ARG, "mpm_create: sort_interval < 0");
+  if (params->algorithm != MPM_ALG_USL && params->algorithm != MPM_ALG_MUSL)
+    return fail(MPM_ERR_ARG, "mpm_create: unknown algorithm");
+  if (params->algorithm == MPM_ALG_MUSL && (params->precision != MPM_PREC_F64 || params->contact))
+    return fail(MPM_ERR_UNSUPPORTED, "mpm_create: MUSL runs FP64 with one velocity field");
   if (!(params->dt > 0.0) || !std::isfinite(params->dt)) return fail(MPM_ERR_ARG, "mpm_create: dt must be > 0");
   if (params->precision != MPM_PREC_F64 && params->precision != MPM_PREC_F32)
     return fail(MPM_ERR_ARG, "mpm_create: unknown precision");
@@ -774,9 +833,9 @@ int mpm_profile_stages(mpm_ctx* c, int64_t nsteps, double* stage_ms) {
 int mpm_fwd_checkpointed(mpm_ctx* c, int64_t nsteps, int32_t every) {
   if (!c) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: null context");
   if (nsteps < 1 || every < 1) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: need nsteps >= 1, every >= 1");
-  if (c->f32 || c->prm.contact || c->prm.sort_interval > 0)
-    return fail(MPM_ERR_UNSUPPORTED,
-                "mpm_fwd_checkpointed: reverse mode needs FP64 particles, one velocity field and no sorting");
+  if (c->f32 || c->prm.contact || c->prm.sort_interval > 0 || c->prm.algorithm != MPM_ALG_USL)
+    return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode needs USL, FP64 particles, one velocity "
+                                     "field and no sorting");
   for (const MatParams& m : c->mats)
     if (m.type != MPM_MAT_NEOHOOKEAN)
       return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode is built for neo-Hookean bodies");

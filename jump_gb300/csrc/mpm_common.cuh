@@ -16,7 +16,9 @@ namespace jmpm {
 enum : unsigned { ST_OUT_OF_GRID = 1u, ST_NEGATIVE_J = 2u, ST_NONFINITE = 4u,
                   // set only while uploading: a strain/stress or 3D plastic strain input
                   // whose mirrored entries differ
-                  ST_ASYM_STRESS = 8u, ST_ASYM_PSTRAIN = 16u };
+                  ST_ASYM_STRESS = 8u, ST_ASYM_PSTRAIN = 16u,
+                  // the 2D MUSL mass solve reached its iteration cap
+                  ST_SOLVER = 32u };
 
 // Field indices of the particle SoA.  Symmetric tensors are stored as
 // 2D: (xx, yy, xy); 3D: (xx, yy, zz, xy, yz, xz).
@@ -84,6 +86,20 @@ struct NodeP {
   int64_t nb[3];         // blocks per axis
   int64_t nblk;
   double* nrm;           // contact mode: per-body normals sum m_p grad N (D), else nullptr
+  // MUSL: second momentum sum (D, lumped), velocity x dt for the velocity
+  // gradient (D), consistent-mass stencil (9 per node, 2D)
+  double* p2;
+  double* vg;
+  double* mc;
+};
+
+// 2D MUSL mass solve: CG vectors of the four right-hand sides (p0_x, p0_y,
+// dt f_x, dt f_y), nodeCount doubles each; x holds v0_x, v0_y, dv_x, dv_y.
+struct CgP {
+  double* x[4];
+  double* r[4];
+  double* p[4];
+  double* q[4];
 };
 
 // Contact mode: one node field per body (SolveExplicitFEMP2DContact.jl:33-52).

@@ -57,6 +57,18 @@ struct Launchers {
   static void scan(cudaStream_t s, const uint32_t* in, uint32_t* out, uint32_t* blocksum, int64_t n);
   static void sort_scatter(cudaStream_t s, bool f32, const void* src, void* dst, int64_t pitch, int nf,
                            const SortP& sp, const int64_t* orig_src, int64_t* orig_dst);
+  // MUSL (mpm_musl.cuh), FP64 particles.  musl_p2g: P2G (2D: with body force and
+  // the consistent mass stencil; 3D: no body force); musl_grid: compaction + grid
+  // update (3D lumped) or mass solve + node outputs (2D); musl_g2p1: velocity
+  // blend (3D: + P2G-2); musl_vg: 3D gradient velocities; musl_g2p2: kinematics.
+  static void musl_p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const double* grav,
+                       unsigned* status);
+  static void musl_grid(cudaStream_t s, const NodeP& nd, const CgP& cg, double dt, double alpha, unsigned* status);
+  static void musl_g2p1(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, double alpha,
+                        unsigned* status);
+  static void musl_vg(cudaStream_t s, const NodeP& nd, double dt);
+  static void musl_g2p2(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const MatParams& mp,
+                        unsigned* status);
 };
 
 constexpr int kEnergyBlocks = 304;  // 2 x 152 SMs

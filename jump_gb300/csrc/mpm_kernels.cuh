@@ -452,57 +452,12 @@ __device__ __forceinline__ double det_d(const double* A) {
   return (x0[0] * c0 + x0[1] * c1) + x0[2] * c2;
 }
 
-// ---------------------------------------------------------------------------
-// G2P + kinematics + stress of particle pp.begin + t (t < pp.count).
-template <int D, class R, int MAT, bool CG = false>
-__device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
-                                             const MatParams& mp, double dt, unsigned* status) {
+// F <- F (I + L dt), J, V = J V0, strain += sym(L dt), update_stress! of particle p
+// (:520-532), given L dt; fin: the particle's new x and v are finite.
+template <int D, class R, int MAT>
+__device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, const R (&Ldt)[D][D],
+                                                  const MatParams& mp, bool fin, unsigned* status) {
   using L = Layout<D>;
-  int64_t p = pp.begin + t;
-  R x[D];
-#pragma unroll
-  for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
-  Hat<D, R> h;
-  if (!hat<D, R>(g, x, h)) {
-    atomicOr(status, ST_OUT_OF_GRID);
-    return;
-  }
-  Corners<D, R> cr;
-  corners<D, R>(g, h, cr);
-  R v[D];
-#pragma unroll
-  for (int a = 0; a < D; ++a) v[a] = *field<R>(pp, L::V + a, p);
-  R Ldt[D][D];
-#pragma unroll
-  for (int a = 0; a < D; ++a)
-#pragma unroll
-    for (int j = 0; j < D; ++j) Ldt[a][j] = R(0);
-  const R* vdt_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.vdt) : reinterpret_cast<const R*>(nd.vdt_f);
-  const R* dv_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.dv) : reinterpret_cast<const R*>(nd.dv_f);
-  const int64_t Nn = nd.nodeCount;
-#pragma unroll
-  for (int k = 0; k < (1 << D); ++k) {
-    int64_t n = cr.node[k];
-    R N = cr.N[k];
-    R vd[D], dvv[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      vd[a] = nload<CG>(vdt_n + a * Nn + n);
-      dvv[a] = nload<CG>(dv_n + a * Nn + n);
-    }
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      v[a] += N * dvv[a];
-      x[a] += N * vd[a];
-#pragma unroll
-      for (int j = 0; j < D; ++j) Ldt[a][j] += vd[a] * cr.dN[k][j];
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    *field<R>(pp, L::X + a, p) = x[a];
-    *field<R>(pp, L::V + a, p) = v[a];
-  }
   // F <- F (I + L dt)   (:523)
   R F[D * D], Fn[D * D], A[D][D];
 #pragma unroll
@@ -573,16 +528,70 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
 #pragma unroll
     for (int c = 0; c < L::PS; ++c) *field<R>(pp, L::EP + c, p) = ep[c];
   }
-  bool fin = true;
 #pragma unroll
   for (int c = 0; c < L::S; ++c) {
     *field<R>(pp, L::SIG + c, p) = sig[c];
     fin &= finite_bits(sig[c]);
   }
-#pragma unroll
-  for (int a = 0; a < D; ++a) fin &= finite_bits(x[a]) & finite_bits(v[a]);
   unsigned st = (positive_bits(J) ? 0u : ST_NEGATIVE_J) | (fin ? 0u : ST_NONFINITE);
   if (st) atomicOr(status, st);
+}
+
+// ---------------------------------------------------------------------------
+// G2P + kinematics + stress of particle pp.begin + t (t < pp.count).
+template <int D, class R, int MAT, bool CG = false>
+__device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
+                                             const MatParams& mp, double dt, unsigned* status) {
+  using L = Layout<D>;
+  int64_t p = pp.begin + t;
+  R x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
+  Hat<D, R> h;
+  if (!hat<D, R>(g, x, h)) {
+    atomicOr(status, ST_OUT_OF_GRID);
+    return;
+  }
+  Corners<D, R> cr;
+  corners<D, R>(g, h, cr);
+  R v[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) v[a] = *field<R>(pp, L::V + a, p);
+  R Ldt[D][D];
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int j = 0; j < D; ++j) Ldt[a][j] = R(0);
+  const R* vdt_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.vdt) : reinterpret_cast<const R*>(nd.vdt_f);
+  const R* dv_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.dv) : reinterpret_cast<const R*>(nd.dv_f);
+  const int64_t Nn = nd.nodeCount;
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) {
+    int64_t n = cr.node[k];
+    R N = cr.N[k];
+    R vd[D], dvv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      vd[a] = nload<CG>(vdt_n + a * Nn + n);
+      dvv[a] = nload<CG>(dv_n + a * Nn + n);
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      v[a] += N * dvv[a];
+      x[a] += N * vd[a];
+#pragma unroll
+      for (int j = 0; j < D; ++j) Ldt[a][j] += vd[a] * cr.dN[k][j];
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    *field<R>(pp, L::X + a, p) = x[a];
+    *field<R>(pp, L::V + a, p) = v[a];
+  }
+  bool fin = true;
+#pragma unroll
+  for (int a = 0; a < D; ++a) fin &= finite_bits(x[a]) & finite_bits(v[a]);
+  kinematics_stress<D, R, MAT>(pp, p, Ldt, mp, fin, status);
 }
 
 template <int D, class R, int MAT>

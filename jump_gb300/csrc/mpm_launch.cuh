@@ -3,6 +3,7 @@
 
 #include "mpm_internal.h"
 #include "mpm_kernels.cuh"
+#include "mpm_musl.cuh"
 
 namespace jmpm {
 
@@ -84,6 +85,57 @@ void Launchers<D>::p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, cons
 template <int D>
 void Launchers<D>::clear(cudaStream_t s, const NodeP& nd) {
   clear_blocks_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd);
+}
+
+template <int D>
+void Launchers<D>::musl_p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const double* grav,
+                            unsigned* status) {
+  if (pp.count <= 0) return;
+  const unsigned nb = blocks_for(pp.count, 256);
+  if constexpr (D == 2) {
+    if (grav[0] != 0.0 || grav[1] != 0.0) musl2d_p2g_kernel<true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], status);
+    else musl2d_p2g_kernel<false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, status);
+  } else {
+    p2g_kernel<D, double, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
+  }
+}
+
+template <int D>
+void Launchers<D>::musl_grid(cudaStream_t s, const NodeP& nd, const CgP& cg, double dt, double alpha,
+                             unsigned* status) {
+  compact_blocks_kernel<<<blocks_for(nd.nblk, 256), 256, 0, s>>>(nd);
+  if constexpr (D == 2) {
+    musl2d_cg_kernel<<<4, 1024, 0, s>>>(nd, cg, dt, status);
+    musl2d_node_kernel<<<sparse_ctas(nd), 256, 0, s>>>(nd, cg, dt, alpha);
+  } else {
+    musl_lumped_grid_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd, dt, alpha);
+  }
+}
+
+template <int D>
+void Launchers<D>::musl_g2p1(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, double alpha,
+                             unsigned* status) {
+  if (pp.count <= 0) return;
+  musl_g2p1_kernel<D, D == 3><<<blocks_for(pp.count, 256), 256, 0, s>>>(g, nd, pp, alpha, status);
+}
+
+template <int D>
+void Launchers<D>::musl_vg(cudaStream_t s, const NodeP& nd, double dt) {
+  if constexpr (D == 3) musl_vg_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd, dt);
+}
+
+template <int D>
+void Launchers<D>::musl_g2p2(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const MatParams& mp,
+                             unsigned* status) {
+  if (pp.count <= 0) return;
+  const unsigned nb = blocks_for(pp.count, 256);
+  switch (mp.type) {
+    case MPM_MAT_ELASTIC: musl_g2p2_kernel<D, MPM_MAT_ELASTIC, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status); break;
+    case MPM_MAT_NEOHOOKEAN:
+      musl_g2p2_kernel<D, MPM_MAT_NEOHOOKEAN, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+      break;
+    default: musl_g2p2_kernel<D, MPM_MAT_J2, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status); break;
+  }
 }
 
 template <int D>

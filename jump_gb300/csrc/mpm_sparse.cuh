@@ -69,7 +69,8 @@ __device__ __forceinline__ int64_t block_node(const NodeP& nd, uint32_t blk, int
   return ix + nd.nn[0] * (iy + nd.nn[1] * iz);
 }
 
-// zero m, p0, f of the listed blocks (before the next P2G)
+// zero the accumulators (m, p0, f and, where present, normals, MUSL p2 and
+// mass stencil) of the listed blocks before the next P2G
 template <int D>
 __global__ void __launch_bounds__(256) clear_blocks_kernel(NodeP nd) {
   const int64_t Nn = nd.nodeCount;
@@ -83,7 +84,11 @@ __global__ void __launch_bounds__(256) clear_blocks_kernel(NodeP nd) {
       nd.p0[a * Nn + i] = 0.0;
       nd.f[a * Nn + i] = 0.0;
       if (nd.nrm) nd.nrm[a * Nn + i] = 0.0;
+      if (nd.p2) nd.p2[a * Nn + i] = 0.0;
     }
+    if (nd.mc)
+#pragma unroll
+      for (int o = 0; o < 9; ++o) nd.mc[o * Nn + i] = 0.0;
   }
 }
 

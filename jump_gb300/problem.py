@@ -1,6 +1,7 @@
-"""solve_explicit_dynamics_2D / 3D for USL + LinearBasis: the drop-in for
-Problem.solve_explicit_dynamics_2D (SolveExplicitSolidMechanics2D.jl:335-585)
-and solve_explicit_dynamics_3D (SolveExplicitSolidMechanics3D.jl:230-378).
+"""solve_explicit_dynamics_2D / 3D for USL or MUSL + LinearBasis: the drop-in
+for Problem.solve_explicit_dynamics_2D (USL SolveExplicitSolidMechanics2D.jl:335-585,
+MUSL :24-329) and solve_explicit_dynamics_3D (USL
+SolveExplicitSolidMechanics3D.jl:230-378, MUSL :14-223).
 
 The time loop, the hook schedule and the in-place mutation of ``solids`` and
 ``grid`` follow the reference; the step itself runs in libjumpmpm.so.
@@ -18,7 +19,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _capi
-from .algorithm import USL, LinearBasis
+from .algorithm import MUSL, USL, LinearBasis
 from .dirichlet import fix_Dirichlet_grid
 from .engine import Descriptors, MPMContext
 from .fix import EnergiesFix, as_list, closeFile
@@ -60,8 +61,9 @@ def write_back(solids, states):
 def _solve(dim, grid, solids, basis, alg, output, fixes, data):
     if not isinstance(basis, LinearBasis):
         raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED, "the accelerated path supports LinearBasis only")
-    if not isinstance(alg, USL):
-        raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED, "the accelerated path supports USL only")
+    if not isinstance(alg, (USL, MUSL)):
+        raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED, "the accelerated path supports USL and MUSL")
+    musl = isinstance(alg, MUSL)
     if grid.dim != dim or any(s.dim != dim for s in solids):
         raise ValueError(f"solve_explicit_dynamics_{dim}D needs a Grid{dim}D and Solid{dim}D objects")
     Tf = float(data["total_time"])
@@ -71,10 +73,11 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
     ghostcell = "ghostcell" in data
     fix_Dirichlet_grid(grid, data, ghostcell=ghostcell)
 
-    desc = Descriptors(grid, solids, tolerance=alg.tolerance, body_force=bodyforce, dt=dt,
+    desc = Descriptors(grid, solids, tolerance=0.0 if musl else alg.tolerance, body_force=bodyforce, dt=dt,
                        precision=data.get("precision", "f64"), contact=bool(data.get("contact", False)),
                        friction=float(data.get("friction", 0.0)),
-                       sort_interval=int(data.get("sort_interval", 0)))
+                       sort_interval=int(data.get("sort_interval", 0)),
+                       algorithm="musl" if musl else "usl", alpha=alg.alpha if musl else 1.0)
     fl = as_list(fixes)
     need_particles = output.needs_particles or any(f.needs_particles for f in fl)
     times = step_times(t, Tf, dt)
@@ -118,10 +121,10 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
 
 
 def solve_explicit_dynamics_2D(grid, solids, basis, alg, output, fixes, data):
-    """USL explicit dynamics on a Grid2D (SolveExplicitSolidMechanics2D.jl:335)."""
+    """USL or MUSL explicit dynamics on a Grid2D (SolveExplicitSolidMechanics2D.jl:335, :24)."""
     return _solve(2, grid, solids, basis, alg, output, fixes, data)
 
 
 def solve_explicit_dynamics_3D(grid, solids, basis, alg, output, fixes, data):
-    """USL explicit dynamics on a Grid3D (SolveExplicitSolidMechanics3D.jl:230)."""
+    """USL or MUSL explicit dynamics on a Grid3D (SolveExplicitSolidMechanics3D.jl:230, :14)."""
     return _solve(3, grid, solids, basis, alg, output, fixes, data)

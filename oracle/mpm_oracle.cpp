@@ -21,6 +21,8 @@
 //   energies                                  Fix.jl:248-270
 //   multi-body contact correction             SolveExplicitFEMP2DContact.jl:189-387,
 //                                             SolveExplicitFEMP3DContact.jl:388-519
+//   MUSL, 2D blended consistent mass          SolveExplicitSolidMechanics2D.jl:24-329
+//   MUSL, 3D lumped mass                      SolveExplicitSolidMechanics3D.jl:14-223
 //
 // Documented decisions where the reference cannot be followed literally:
 //  * 3D USL reads the undefined `nodalMomentum0` and `counter`
@@ -34,6 +36,9 @@
 //    published StaticArrays formula; 2x2 is a11 a22 - a12 a21.
 //  * A particle whose cell lies outside the grid (undefined behaviour in the
 //    reference, Basis.jl:71-74) is skipped and reported as an error.
+//  * The 2D MUSL solves its blended mass matrix with a banded Cholesky where the
+//    reference calls a dense `\`: the same solution up to rounding.  The MUSL
+//    steps run single-threaded.
 //  * With more than one thread, P2G runs slab-coloured (even then odd slabs
 //    of two cells along the last axis) so the node sums are re-associated;
 //    G2P results are identical for any thread count.
@@ -109,6 +114,8 @@ struct Ctx {
   // contact mode: per-body node fields (velocities after the grid update)
   std::vector<std::vector<double>> bm, bv0, bv, bnormal;
   std::vector<double> sysp;  // system momentum, D per node
+  // MUSL: nodalMomentum2 (lumped), solved velocities v0 and v (2D consistent)
+  std::vector<double> mom2, v0, gv;
 };
 
 inline double sign_of(double x) { return (x > 0) ? 1.0 : ((x < 0) ? -1.0 : 0.0); }
@@ -353,6 +360,9 @@ inline void p2g_particle(const Grid<D>& g, const Body<D>& b, int64_t ip, const d
   }
 }
 
+template <int D>
+inline void kin_stress(Body<D>& b, int64_t ip, const double* L, double dt, int* status);
+
 // G2P of one particle (:500-532).  vfield/v0field given as momenta (mode 0: reference
 // form (p - p0)/m) or as velocities (mode 1: contact fields, SolveExplicitFEMP2DContact.jl:415-426).
 template <int D>
@@ -398,6 +408,12 @@ inline void g2p_particle(const Grid<D>& g, Body<D>& b, int64_t ip, double dt, do
     b.vel[D * ip + a] = vvp[a];
     b.pos[D * ip + a] = xxp[a];
   }
+  kin_stress<D>(b, ip, L, dt, status);
+}
+
+// strain += dt D, F *= (I + L dt), J, V = J V0, update_stress! (:520-532)
+template <int D>
+inline void kin_stress(Body<D>& b, int64_t ip, const double* L, double dt, int* status) {
   double Dm[D * D];
   for (int j = 0; j < D; ++j)
     for (int i = 0; i < D; ++i) Dm[i + D * j] = 0.5 * (L[i + D * j] + L[j + D * i]);
@@ -437,8 +453,8 @@ void zero(std::vector<double>& v) {
 // P2G over every body into the given arrays; sequential or slab-coloured.
 template <int D>
 void p2g_bodies(Ctx<D>& c, const std::vector<int>& which, double* mass, double* mom0, double* force,
-                double* normal) {
-  const double* bf = c.p.body_force;
+                double* normal, const double* bf = nullptr) {
+  if (!bf) bf = c.p.body_force;
   if (c.threads <= 1) {
     for (int s : which) {
       const Body<D>& b = c.bodies[s];
@@ -519,6 +535,222 @@ void step_single(Ctx<D>& c) {
   }
   for (size_t s = 0; s < c.bodies.size(); ++s)
     g2p_body<D>(c, int(s), g.mass.data(), g.momentum0.data(), g.momentum.data(), 0);
+}
+
+// ---------------------------------------------------------------------------
+// MUSL with lumped mass, SolveExplicitSolidMechanics3D.jl:14-223.  The 3D solver
+// applies no body force, builds the velocity gradient as L_ij = dN_i vI_j
+// (SMatrix{3,3}(dNix*vIx, dNiy*vIx, dNiz*vIx, ...), :187-189), updates positions
+// with nodalMomentum and the gradient with nodalMomentum2, which carries no
+// Dirichlet condition; all as written.
+template <int D>
+void step_musl_lumped(Ctx<D>& c) {
+  Grid<D>& g = c.g;
+  const double dt = c.p.dt, alpha = c.p.alpha;
+  constexpr int S = (D == 2) ? 4 : 8;
+  zero<D>(g.mass);
+  zero<D>(g.momentum0);
+  zero<D>(c.mom2);
+  zero<D>(g.force);
+  std::vector<int> all(c.bodies.size());
+  for (size_t s = 0; s < all.size(); ++s) all[s] = int(s);
+  const double nobf[3] = {0.0, 0.0, 0.0};
+  p2g_bodies<D>(c, all, g.mass.data(), g.momentum0.data(), g.force.data(), nullptr, nobf);
+  auto bcs = [&]() {
+    for (int64_t i = 0; i < g.nodeCount; ++i)
+      for (int a = 0; a < D; ++a)
+        if (g.fixed[D * i + a] == 1) {
+          g.momentum0[D * i + a] = 0.;
+          g.momentum[D * i + a] = 0.;
+        }
+  };
+  for (int64_t i = 0; i < g.nodeCount; ++i)
+    for (int a = 0; a < D; ++a) g.momentum[D * i + a] = g.momentum0[D * i + a] + g.force[D * i + a] * dt;
+  bcs();
+  // grid to particle 1 and particle to grid 2 (:113-139), in particle order
+  int64_t near[S];
+  double N[S], dN[S * D];
+  for (auto& b : c.bodies)
+    for (int64_t ip = 0; ip < b.n; ++ip) {
+      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) {
+        c.status = MPM_ERR_OUT_OF_GRID;
+        continue;
+      }
+      double vacc[D];
+      for (int a = 0; a < D; ++a) vacc[a] = 0.;
+      for (int i = 0; i < S; ++i) {
+        const int64_t in = near[i];
+        const double mI = g.mass[in];
+        if (mI > 0) {
+          const double mii = (1 / mI) * N[i];
+          for (int a = 0; a < D; ++a)
+            vacc[a] += (g.momentum[D * in + a] - alpha * g.momentum0[D * in + a]) * mii;
+        }
+      }
+      double* vp = &b.vel[D * ip];
+      for (int a = 0; a < D; ++a) vp[a] = alpha * vp[a] + vacc[a];
+      const double mp = b.mass[ip];
+      for (int i = 0; i < S; ++i)
+        for (int a = 0; a < D; ++a) c.mom2[D * near[i] + a] += N[i] * mp * vp[a];
+    }
+  bcs();
+  // particle to grid 2 / kinematics (:162-204)
+  for (auto& b : c.bodies)
+    for (int64_t ip = 0; ip < b.n; ++ip) {
+      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) continue;
+      double L[D * D], xxp[D];
+      for (int q = 0; q < D * D; ++q) L[q] = 0.;
+      for (int a = 0; a < D; ++a) xxp[a] = b.pos[D * ip + a];
+      for (int i = 0; i < S; ++i) {
+        const int64_t in = near[i];
+        const double m = g.mass[in];
+        if (m > 0.) {
+          const double mii = 1 / m;
+          double vI[D];
+          for (int a = 0; a < D; ++a) vI[a] = mii * c.mom2[D * in + a];
+          for (int a = 0; a < D; ++a) xxp[a] += N[i] * mii * dt * g.momentum[D * in + a];
+          for (int j = 0; j < D; ++j)
+            for (int r = 0; r < D; ++r) L[r + D * j] += dN[D * i + r] * vI[j];
+        }
+      }
+      for (int a = 0; a < D; ++a) b.pos[D * ip + a] = xxp[a];
+      kin_stress<D>(b, ip, L, dt, &c.status);
+    }
+}
+
+// Banded Cholesky of the symmetric positive definite matrix whose lower band
+// (half-bandwidth w) is A[i*(w+1) + (i-j)], j = i-w .. i; in place.  The 2D MUSL's
+// blended mass matrix couples nodes at most nx+1 apart in index.
+inline bool band_cholesky(std::vector<double>& A, int64_t n, int64_t w) {
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = std::max<int64_t>(0, i - w); j <= i; ++j) {
+      double sum = A[i * (w + 1) + (i - j)];
+      for (int64_t k = std::max<int64_t>(std::max<int64_t>(0, i - w), j - w); k < j; ++k)
+        sum -= A[i * (w + 1) + (i - k)] * A[j * (w + 1) + (j - k)];
+      if (i == j) {
+        if (!(sum > 0.0)) return false;
+        A[i * (w + 1)] = std::sqrt(sum);
+      } else {
+        A[i * (w + 1) + (i - j)] = sum / A[j * (w + 1)];
+      }
+    }
+  return true;
+}
+
+inline void band_solve(const std::vector<double>& Lb, int64_t n, int64_t w, const double* b, double* x) {
+  std::vector<double> y(static_cast<size_t>(n));
+  for (int64_t i = 0; i < n; ++i) {
+    double sum = b[i];
+    for (int64_t k = std::max<int64_t>(0, i - w); k < i; ++k) sum -= Lb[i * (w + 1) + (i - k)] * y[k];
+    y[i] = sum / Lb[i * (w + 1)];
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    double sum = y[i];
+    for (int64_t k = i + 1; k <= std::min<int64_t>(n - 1, i + w); ++k) sum -= Lb[k * (w + 1) + (k - i)] * x[k];
+    x[i] = sum / Lb[i * (w + 1)];
+  }
+}
+
+// MUSL with the blended consistent mass matrix, SolveExplicitSolidMechanics2D.jl:24-329:
+// bmassMat = 0.1 Diagonal(m) + 0.9 M (M_ij = sum_p m_p N_i N_j, rows of massless nodes
+// set to 1 on the diagonal), v0 = bmassMat \ p0 and v = v0 + bmassMat \ (dt f) per
+// component (the reference's dense solve is a banded Cholesky here: same solution up to
+// rounding).  The Dirichlet update of nodalMomentum that follows is never read by the
+// particle updates, so fixed nodes do not constrain this solver; as written.
+void step_musl_consistent(Ctx<2>& c) {
+  constexpr int D = 2, S = 4;
+  Grid<2>& g = c.g;
+  const double dt = c.p.dt, alpha = c.p.alpha;
+  const int64_t n = g.nodeCount, w = g.nn[0] + 1;
+  zero<D>(g.mass);
+  zero<D>(g.momentum0);
+  zero<D>(g.force);
+  std::vector<double> Mb(static_cast<size_t>(n * (w + 1)), 0.0);
+  int64_t near[S];
+  double N[S], dN[S * D];
+  const double* body = c.p.body_force;
+  for (auto& b : c.bodies)
+    for (int64_t ip = 0; ip < b.n; ++ip) {
+      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) {
+        c.status = MPM_ERR_OUT_OF_GRID;
+        continue;
+      }
+      const double fVolume = b.vol[ip], fMass = b.mass[ip];
+      const double* vp = &b.vel[D * ip];
+      const double* sigma = &b.stress[D * D * ip];
+      for (int i = 0; i < S; ++i) {
+        const int64_t id = near[i];
+        const double Ni = N[i], Nim = Ni * fMass;
+        g.mass[id] += Nim;
+        for (int j = 0; j < S; ++j)
+          if (near[j] <= id) Mb[id * (w + 1) + (id - near[j])] += Nim * N[j];
+        for (int a = 0; a < D; ++a) g.momentum0[D * id + a] += Nim * vp[a];
+        for (int a = 0; a < D; ++a) {
+          double sa = sigma[a] * dN[D * i] + sigma[a + D] * dN[D * i + 1];
+          g.force[D * id + a] += -fVolume * sa + fMass * body[a] * Ni;
+        }
+      }
+    }
+  const double eps = 0.1;
+  for (int64_t i = 0; i < n; ++i) {
+    for (int64_t k = 0; k <= w; ++k) Mb[i * (w + 1) + k] *= (1 - eps);
+    Mb[i * (w + 1)] += eps * g.mass[i];
+    if (g.mass[i] == 0.) Mb[i * (w + 1)] = 1.0;
+  }
+  if (!band_cholesky(Mb, n, w)) {
+    c.status = MPM_ERR_SOLVER;
+    return;
+  }
+  std::vector<double> rhs(static_cast<size_t>(n)), sol(static_cast<size_t>(n));
+  for (int a = 0; a < D; ++a) {
+    for (int64_t i = 0; i < n; ++i) rhs[i] = g.momentum0[D * i + a];
+    band_solve(Mb, n, w, rhs.data(), sol.data());
+    for (int64_t i = 0; i < n; ++i) c.v0[D * i + a] = sol[i];
+    for (int64_t i = 0; i < n; ++i) rhs[i] = dt * g.force[D * i + a];
+    band_solve(Mb, n, w, rhs.data(), sol.data());
+    for (int64_t i = 0; i < n; ++i) c.gv[D * i + a] = c.v0[D * i + a] + sol[i];
+  }
+  // update grid (:168-186): nodalMomentum and the Dirichlet conditions, which no
+  // particle update below reads
+  for (int64_t i = 0; i < n; ++i) {
+    for (int a = 0; a < D; ++a) g.momentum[D * i + a] = g.momentum0[D * i + a] + g.force[D * i + a] * dt;
+    for (int a = 0; a < D; ++a)
+      if (g.fixed[D * i + a] == 1) {
+        g.momentum0[D * i + a] = 0.;
+        g.momentum[D * i + a] = 0.;
+      }
+  }
+  // grid to particle 1: velocities (:198-224)
+  for (auto& b : c.bodies)
+    for (int64_t ip = 0; ip < b.n; ++ip) {
+      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) continue;
+      double vacc[D] = {0., 0.};
+      for (int i = 0; i < S; ++i) {
+        const int64_t in = near[i];
+        if (g.mass[in] > 0)
+          for (int a = 0; a < D; ++a) vacc[a] += N[i] * (c.gv[D * in + a] - alpha * c.v0[D * in + a]);
+      }
+      double* vp = &b.vel[D * ip];
+      for (int a = 0; a < D; ++a) vp[a] = alpha * vp[a] + vacc[a];
+    }
+  // particle update 2: positions, gradient, F, stress (:245-290)
+  for (auto& b : c.bodies)
+    for (int64_t ip = 0; ip < b.n; ++ip) {
+      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) continue;
+      double L[D * D] = {0., 0., 0., 0.}, xxp[D];
+      for (int a = 0; a < D; ++a) xxp[a] = b.pos[D * ip + a];
+      for (int i = 0; i < S; ++i) {
+        const int64_t in = near[i];
+        if (g.mass[in] > 0.) {
+          const double* vI = &c.gv[D * in];
+          for (int a = 0; a < D; ++a) xxp[a] += (N[i] * vI[a]) * dt;
+          for (int j = 0; j < D; ++j)
+            for (int a = 0; a < D; ++a) L[a + D * j] += dN[D * i + j] * vI[a];
+        }
+      }
+      for (int a = 0; a < D; ++a) b.pos[D * ip + a] = xxp[a];
+      kin_stress<D>(b, ip, L, dt, &c.status);
+    }
 }
 
 // One USL step with one velocity field per body and the contact correction.
@@ -661,6 +893,11 @@ int create(const mpm_grid_desc* gd, const mpm_body_desc* bd, int nb, const mpm_p
     if (b.has_youngs) cp(b.youngs, d.youngs, 1, 0.0);
     c->bodies.push_back(std::move(b));
   }
+  if (p->algorithm == MPM_ALG_MUSL) {
+    c->mom2.assign(size_t(D) * g.nodeCount, 0.0);
+    c->v0.assign(size_t(D) * g.nodeCount, 0.0);
+    c->gv.assign(size_t(D) * g.nodeCount, 0.0);
+  }
   if (p->contact) {
     c->bm.assign(nb, std::vector<double>(g.nodeCount, 0.0));
     c->bv0.assign(nb, std::vector<double>(size_t(D) * g.nodeCount, 0.0));
@@ -684,12 +921,19 @@ template <int D>
 static int step_impl(Ctx<D>* c, int64_t nsteps, double* t) {
   c->status = MPM_OK;
   for (int64_t k = 0; k < nsteps; ++k) {
-    if (c->p.contact) step_contact<D>(*c);
-    else step_single<D>(*c);
+    if (c->p.algorithm == MPM_ALG_MUSL) {
+      if constexpr (D == 2) step_musl_consistent(*c);
+      else step_musl_lumped<D>(*c);
+    } else if (c->p.contact) {
+      step_contact<D>(*c);
+    } else {
+      step_single<D>(*c);
+    }
     if (t) *t += c->p.dt;
   }
   if (c->status == MPM_ERR_OUT_OF_GRID) return fail(c->status, "particle outside the grid");
   if (c->status == MPM_ERR_NEGATIVE_J) return fail(c->status, "det F <= 0 at a particle");
+  if (c->status == MPM_ERR_SOLVER) return fail(c->status, "MUSL mass matrix not positive definite");
   return c->status;
 }
 

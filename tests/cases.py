@@ -61,6 +61,13 @@ def load_golden(name):
     return grid, solids, float(z["meta_tol"]), bf, float(z["meta_dt"]), int(z["meta_nsteps"]), z
 
 
+def golden_kw(z):
+    """Descriptor arguments of a fixture's update scheme (USL when it names none)."""
+    if "meta_alg" in z and int(z["meta_alg"]) == 1:
+        return {"algorithm": "musl", "alpha": float(z["meta_alpha"])}
+    return {}
+
+
 def golden_expected(z, b):
     """Expected outputs of body b in the download layout."""
     d = int(z["meta_dim"])

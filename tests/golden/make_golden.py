@@ -121,7 +121,7 @@ def stress_update(mat, d, sig, eps, F, J, state):
     if typ == 0:  # ElasticMaterial
         if d == 3:
             s = sig
-            state["vm"] = math.sqrt(s[0] ** 2 + s[4] ** 2 + s[8] ** 2 + 2 * (s[3] ** 2 + s[6] ** 2 + s[7] ** 2))
+            state["vm"] = math.sqrt(s[0] * s[0] + s[4] * s[4] + s[8] * s[8] + 2 * (s[3] * s[3] + s[6] * s[6] + s[7] * s[7]))
             tr = eps[0] + eps[4] + eps[8]
         else:
             tr = eps[0] + eps[3]
@@ -161,7 +161,7 @@ def stress_update(mat, d, sig, eps, F, J, state):
         for c in (0, 4, 8):
             ed[c] = ed[c] - t3
         s = [2 * mu * (ed[c] - ep[c]) for c in range(9)]
-        ns = math.sqrt(s[0] ** 2 + s[4] ** 2 + s[8] ** 2 + 2.0 * (s[3] ** 2 + s[7] ** 2 + s[6] ** 2))
+        ns = math.sqrt(s[0] * s[0] + s[4] * s[4] + s[8] * s[8] + 2.0 * (s[3] * s[3] + s[7] * s[7] + s[6] * s[6]))
         kt = kappa * (eps[0] + eps[4] + eps[8]) * 1.0
         st = list(s)
         for c in (0, 4, 8):
@@ -180,7 +180,7 @@ def stress_update(mat, d, sig, eps, F, J, state):
         dv = list(sg)
         for c in (0, 4, 8):
             dv[c] = dv[c] - t3
-        state["vm"] = math.sqrt(dv[0] ** 2 + dv[4] ** 2 + dv[8] ** 2 + 2 * (dv[3] ** 2 + dv[6] ** 2 + dv[7] ** 2))
+        state["vm"] = math.sqrt(dv[0] * dv[0] + dv[4] * dv[4] + dv[8] * dv[8] + 2 * (dv[3] * dv[3] + dv[6] * dv[6] + dv[7] * dv[7]))
         return sg
     # 2D J2, Voigt
     Idev = [[0.5, -0.5, 0.0], [-0.5, 0.5, 0.0], [0.0, 0.0, 1.0]]
@@ -192,7 +192,7 @@ def stress_update(mat, d, sig, eps, F, J, state):
     edv = [Idev[i][0] * e[0] + Idev[i][1] * e[1] + Idev[i][2] * e[2] for i in range(3)]
     a = [2 * mu * (edv[i] - ep[i]) for i in range(3)]
     s = [Im[i][0] * a[0] + Im[i][1] * a[1] + Im[i][2] * a[2] for i in range(3)]
-    ns = math.sqrt(s[0] ** 2 + s[1] ** 2 + 2 * s[2] ** 2)
+    ns = math.sqrt(s[0] * s[0] + s[1] * s[1] + 2 * s[2] * s[2])
     eye2 = [1.0, 1.0, 0.0]
     kt = kappa * (e[0] + e[1])
     f_trial = ns - (k1 * a0 + fy)
@@ -207,7 +207,7 @@ def stress_update(mat, d, sig, eps, F, J, state):
         sg = [kt * eye2[i] + s[i] - 2 * mu * lamp * nrm[i] for i in range(3)]
     state["alpha"], state["ep"] = a0, ep
     dv = [Idev[i][0] * sg[0] + Idev[i][1] * sg[1] + Idev[i][2] * sg[2] for i in range(3)]
-    state["vm"] = math.sqrt(dv[0] ** 2 + dv[1] ** 2 + 2 * dv[2] ** 2)
+    state["vm"] = math.sqrt(dv[0] * dv[0] + dv[1] * dv[1] + 2 * dv[2] * dv[2])
     return [sg[0], sg[2], sg[2], sg[1]]
 
 
@@ -289,6 +289,169 @@ def usl_steps(case, nsteps):
     return case
 
 
+def _kinematics(B, ip, L, d, dt):
+    """strain += dt D, F *= (I + L dt), J, V, update_stress! (shared by the USL and MUSL loops)."""
+    mat = B["mat"]
+    D_ = [0.5 * (L[i + d * j] + L[j + d * i]) for j in range(d) for i in range(d)]
+    B["strain"][ip] = [B["strain"][ip][c] + dt * D_[c] for c in range(d * d)]
+    A = [L[c] * dt for c in range(d * d)]
+    for a in range(d):
+        A[a * (d + 1)] = A[a * (d + 1)] + 1.0
+    F = matmul(B["F"][ip], A, d)
+    B["F"][ip] = F
+    J = det(F, d)
+    B["vol"][ip] = J * B["vol0"][ip]
+    m2 = dict(mat)
+    if B.get("youngs") is not None:
+        E, nu = B["youngs"][ip], mat["nu"]
+        m2["lambda"] = E * nu / (1 + nu) / (1 - 2 * nu)
+        m2["mu"] = E / 2 / (1 + nu)
+        m2["kappa"] = m2["lambda"] + m2["mu"]
+    state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip]}
+    B["stress"][ip] = stress_update(m2, d, B["stress"][ip], B["strain"][ip], F, J, state)
+    B["alpha"][ip], B["ep"][ip], B["vm"][ip] = state["alpha"], state["ep"], state["vm"]
+
+
+def _cholesky_solve_band(A, n, w, rhs):
+    """Solve A x = rhs for the symmetric positive definite A given by its lower
+    band A[i][k] = A_{i,i-k}, k = 0..w: Cholesky A = L L^T (columns in ascending
+    order, so the entries outside the band, all zero, never enter a sum), then
+    forward and backward substitution."""
+    Lb = [row[:] for row in A]
+    for i in range(n):
+        for j in range(max(0, i - w), i + 1):
+            acc = Lb[i][i - j]
+            for k in range(max(0, i - w, j - w), j):
+                acc -= Lb[i][i - k] * Lb[j][j - k]
+            if i == j:
+                Lb[i][0] = math.sqrt(acc)
+            else:
+                Lb[i][i - j] = acc / Lb[j][0]
+    out = []
+    for b in rhs:
+        y = [0.0] * n
+        for i in range(n):
+            acc = b[i]
+            for k in range(max(0, i - w), i):
+                acc -= Lb[i][i - k] * y[k]
+            y[i] = acc / Lb[i][0]
+        x = [0.0] * n
+        for i in range(n - 1, -1, -1):
+            acc = y[i]
+            for k in range(i + 1, min(n - 1, i + w) + 1):
+                acc -= Lb[k][k - i] * x[k]
+            x[i] = acc / Lb[i][0]
+        out.append(x)
+    return out
+
+
+def musl_steps(case, nsteps):
+    """Run nsteps of the MUSL loop: 2D with the blended consistent mass matrix
+    (SolveExplicitSolidMechanics2D.jl:24-329, bmassMat = 0.1 Diagonal(m) + 0.9 M,
+    massless rows 1 on the diagonal; solved here by banded Cholesky), 3D with
+    lumped mass and no body force (SolveExplicitSolidMechanics3D.jl:14-223)."""
+    d = case["dim"]
+    G = PyGrid(d, case["xmin"], case["xmax"], case["nodes"])
+    fixed = case["fixed"]
+    dt, alpha, body = case["dt"], case["alpha"], case["gravity"][:d]
+    n = G.count
+    for _ in range(nsteps):
+        mass = [0.0] * n
+        mom0 = [[0.0] * d for _ in range(n)]
+        force = [[0.0] * d for _ in range(n)]
+        w = case["nodes"][0] + 1
+        band = [[0.0] * (w + 1) for _ in range(n)] if d == 2 else None
+        for B in case["bodies"]:
+            for ip in range(B["n"]):
+                near, funcs, ders = G.shape(B["pos"][ip])
+                fVolume, fMass, vp, sigma = B["vol"][ip], B["mass"][ip], B["vel"][ip], B["stress"][ip]
+                for i in range(len(near)):
+                    q, Ni, dNi = near[i], funcs[i], ders[i]
+                    Nim = Ni * fMass
+                    mass[q] += Nim
+                    if d == 2:
+                        for j in range(len(near)):
+                            if near[j] <= q:
+                                band[q][q - near[j]] += Nim * funcs[j]
+                    for a in range(d):
+                        mom0[q][a] += Nim * vp[a]
+                    for a in range(d):
+                        s = sigma[a] * dNi[0] + sigma[a + d] * dNi[1]
+                        if d == 3:
+                            s = s + sigma[a + 2 * d] * dNi[2]
+                        if d == 2:
+                            force[q][a] += -fVolume * s + fMass * body[a] * Ni
+                        else:
+                            force[q][a] += -fVolume * s  # no body force in the 3D MUSL
+        if d == 2:
+            for i in range(n):
+                for k in range(w + 1):
+                    band[i][k] *= (1 - 0.1)
+                band[i][0] += 0.1 * mass[i]
+                if mass[i] == 0.0:
+                    band[i][0] = 1.0
+            v0x, v0y, dvx, dvy = _cholesky_solve_band(
+                band, n, w, [[mom0[i][0] for i in range(n)], [mom0[i][1] for i in range(n)],
+                             [dt * force[i][0] for i in range(n)], [dt * force[i][1] for i in range(n)]])
+            v0 = [[v0x[i], v0y[i]] for i in range(n)]
+            gv = [[v0x[i] + dvx[i], v0y[i] + dvy[i]] for i in range(n)]
+        mom = [[0.0] * d for _ in range(n)]
+        for i in range(n):
+            for a in range(d):
+                mom[i][a] = mom0[i][a] + force[i][a] * dt
+            for a in range(d):
+                if fixed[i][a] == 1:
+                    mom0[i][a] = 0.0
+                    mom[i][a] = 0.0
+        mom2 = [[0.0] * d for _ in range(n)]
+        for B in case["bodies"]:
+            for ip in range(B["n"]):
+                near, funcs, ders = G.shape(B["pos"][ip])
+                acc = [0.0] * d
+                for i in range(len(near)):
+                    q, Ni = near[i], funcs[i]
+                    if mass[q] > 0:
+                        if d == 2:
+                            for a in range(d):
+                                acc[a] += Ni * (gv[q][a] - alpha * v0[q][a])
+                        else:
+                            mii = (1 / mass[q]) * Ni
+                            for a in range(d):
+                                acc[a] += (mom[q][a] - alpha * mom0[q][a]) * mii
+                B["vel"][ip] = [alpha * B["vel"][ip][a] + acc[a] for a in range(d)]
+                if d == 3:
+                    for i in range(len(near)):
+                        for a in range(d):
+                            mom2[near[i]][a] += funcs[i] * B["mass"][ip] * B["vel"][ip][a]
+        for B in case["bodies"]:
+            for ip in range(B["n"]):
+                near, funcs, ders = G.shape(B["pos"][ip])
+                L = [0.0] * (d * d)
+                xxp = list(B["pos"][ip])
+                for i in range(len(near)):
+                    q, Ni, dNi = near[i], funcs[i], ders[i]
+                    if mass[q] > 0.0:
+                        if d == 2:
+                            vI = gv[q]
+                            for a in range(d):
+                                xxp[a] += (Ni * vI[a]) * dt
+                            for j in range(d):
+                                for a in range(d):
+                                    L[a + d * j] += dNi[j] * vI[a]
+                        else:
+                            mii = 1 / mass[q]
+                            vI = [mii * mom2[q][a] for a in range(d)]
+                            for a in range(d):
+                                xxp[a] += Ni * mii * dt * mom[q][a]
+                            for j in range(d):  # L_rj = dN_r vI_j, as the 3D solver builds it
+                                for r in range(d):
+                                    L[r + d * j] += dNi[r] * vI[j]
+                B["pos"][ip] = xxp
+                _kinematics(B, ip, L, d, dt)
+    case["grid_out"] = (mass, mom0, mom, force)
+    return case
+
+
 # ---------------------------------------------------------------------------
 def case_from_objects(grid, solids, alg, data, nsteps):
     from jump_gb300.engine import colmajor
@@ -325,8 +488,10 @@ def case_from_objects(grid, solids, alg, data, nsteps):
             "vm": [0.0] * n,
             "youngs": None if s.youngs is None else list(map(float, s.youngs)),
         })
+    musl = hasattr(alg, "alpha")
     return {"dim": d, "xmin": xmin, "xmax": xmax, "nodes": nodes, "fixed": fixed, "dt": float(data["dt"]),
-            "tol": float(alg.tolerance), "gravity": list(map(float, g)), "bodies": bodies, "nsteps": nsteps}
+            "tol": 0.0 if musl else float(alg.tolerance), "gravity": list(map(float, g)), "bodies": bodies,
+            "nsteps": nsteps, "alg": 1 if musl else 0, "alpha": float(alg.alpha) if musl else 1.0}
 
 
 def save_case(name, case_in, case_out):
@@ -342,6 +507,8 @@ def save_case(name, case_in, case_out):
     arrs["meta_gravity"] = np.array(case_in["gravity"])
     arrs["meta_nsteps"] = np.array(case_in["nsteps"])
     arrs["meta_nbodies"] = np.array(len(case_in["bodies"]))
+    arrs["meta_alg"] = np.array(case_in["alg"])
+    arrs["meta_alpha"] = np.array(case_in["alpha"])
     for b, (Bi, Bo) in enumerate(zip(case_in["bodies"], case_out["bodies"])):
         m = Bi["mat"]
         arrs[f"b{b}_mat"] = np.array([m["type"], m["E"], m["nu"], m["density"], m["fy"], m["k1"]])
@@ -359,7 +526,7 @@ def save_case(name, case_in, case_out):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
 
 
-def main():
+def main(only=None):
     import copy
     from jump_gb300 import scenarios
     from jump_gb300.algorithm import ConstantBodyForce2D, ConstantBodyForce3D, USL
@@ -416,11 +583,46 @@ def main():
         scenarios.apply_dirichlet(g, data)
         cases[f"spheres_{kind}_12"] = case_from_objects(g, [s1, s2], USL(1e-9), data, 12)
 
+    # 6. MUSL: 2D touching elastic disks (consistent mass, alpha 0.99); 3D
+    #    neo-Hookean spheres colliding in one velocity field (lumped mass,
+    #    alpha 1); 3D J2 mini Taylor bar (alpha 0.99: with alpha 1 the 3D
+    #    solver's FLIP increment (p - p0)/m vanishes at the fixed wall nodes and
+    #    the bar passes the wall undeformed)
+    from jump_gb300.algorithm import MUSL
+    touch = ((0.3, 0.3), (0.3 + 0.4 / math.sqrt(2.0), 0.3 + 0.4 / math.sqrt(2.0)))
+    g, s, alg, data = scenarios.two_disks(nodes=11, centers=touch, speed=0.5)
+    scenarios.apply_dirichlet(g, data)
+    cases["two_disks_musl_15"] = case_from_objects(g, s, MUSL(0.99), data, 15)
+    g = Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, 7, 7, 7)
+    off = g.dx / 2
+    c1 = buildParticleForSphere([0.4, 0.4, 0.45], 0.17, off)
+    c2 = buildParticleForSphere([0.6, 0.6, 0.55], 0.17, off)
+    s1, s2 = Solid3D(c1, NeoHookeanMaterial(1e3, 0.3, 1000.0, len(c1))), \
+        Solid3D(c2, NeoHookeanMaterial(1e3, 0.3, 1000.0, len(c2)))
+    for so in (s1, s2):
+        so.mass *= off ** 3
+        so.volume[:] = off ** 3
+        so.volumeInitial[:] = off ** 3
+    assign_velocity(s1, [0.3, 0.3, 0.2])
+    assign_velocity(s2, [-0.3, -0.3, -0.2])
+    data = {"dt": 2e-3, "bodyforce": ConstantBodyForce3D([0.0, 0.0, -1.0]),
+            "dirichlet_grid": [("front", (0, 0, 1)), ("left", (1, 0, 0))]}
+    scenarios.apply_dirichlet(g, data)
+    cases["spheres_nh_musl_12"] = case_from_objects(g, [s1, s2], MUSL(1.0), data, 12)
+    g, s, alg, data = scenarios.taylor_bar(h=1e-3, radius=2e-3, length=6e-3, width=8e-3, height=10e-3,
+                                           gap=0.0, speed=300.0)
+    scenarios.apply_dirichlet(g, data)
+    cases["taylor_mini_musl_j2_10"] = case_from_objects(g, s, MUSL(0.99), data, 10)
+
     for name, cin in cases.items():
-        cout = usl_steps(copy.deepcopy(cin), cin["nsteps"])
+        if only and name not in only:
+            continue
+        run = musl_steps if cin["alg"] == 1 else usl_steps
+        cout = run(copy.deepcopy(cin), cin["nsteps"])
         save_case(name, cin, cout)
         print("wrote", name, [b["n"] for b in cin["bodies"]])
 
 
 if __name__ == "__main__":
-    main()
+    # optional case names: regenerate only those fixtures
+    main(sys.argv[1:])

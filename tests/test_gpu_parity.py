@@ -3,7 +3,7 @@ relative per particle field; FP32 error bounds stated per case)."""
 import numpy as np
 import pytest
 
-from cases import GOLDEN_CASES, descriptors, field_errors, golden_expected, load_golden, rel_err
+from cases import GOLDEN_CASES, descriptors, field_errors, golden_expected, golden_kw, load_golden, rel_err
 from jump_gb300 import scenarios
 from jump_gb300.engine import Descriptors, MPMContext
 
@@ -24,11 +24,13 @@ def run_pair(grid, solids, tol, bf, dt, steps, oracle, precision="f64", sched=No
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_golden_cases_fp64(name, oracle_lib):
     grid, solids, tol, bf, dt, nsteps, z = load_golden(name)
-    dg = MPMContext(descriptors(grid, solids, tol, bf, dt))
+    dg = MPMContext(descriptors(grid, solids, tol, bf, dt, **golden_kw(z)))
     dg.step(nsteps)
+    # the 2D MUSL solves its mass matrix iteratively on the device (relative residual 1e-13)
+    tol = 1e-9 if golden_kw(z) and int(z["meta_dim"]) == 2 else FP64_TOL
     for b, st in enumerate(dg.download_all()):
         for k, v in golden_expected(z, b).items():
-            assert rel_err(getattr(st, k), v) <= FP64_TOL, (name, b, k, rel_err(getattr(st, k), v))
+            assert rel_err(getattr(st, k), v) <= tol, (name, b, k, rel_err(getattr(st, k), v))
 
 
 @pytest.mark.parametrize("steps", [1, 10, 100])

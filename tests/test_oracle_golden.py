@@ -3,13 +3,13 @@
 import numpy as np
 import pytest
 
-from cases import GOLDEN_CASES, descriptors, golden_expected, load_golden, rel_err
+from cases import GOLDEN_CASES, descriptors, golden_expected, golden_kw, load_golden, rel_err
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_oracle_matches_golden_bitwise(name, oracle_lib):
     grid, solids, tol, bf, dt, nsteps, z = load_golden(name)
-    desc = descriptors(grid, solids, tol, bf, dt)
+    desc = descriptors(grid, solids, tol, bf, dt, **golden_kw(z))
     ctx = oracle_lib.OracleContext(desc)
     t = ctx.step(nsteps, t=0.0)
     assert t > 0
