@@ -46,6 +46,27 @@ BYTES = {
     "f64": {"p2g": 112 + 7, "g2p": 520 + 6, "step": 600},
     "f32": {"p2g": 56 + 7, "g2p": 260 + 3, "step": 330},
 }
+# MUSL, FP64, 3D J2: P2G as above; the G2P stage is G2P-1 (reads x3 v3 m, writes v3
+# = 80 B, + P2G-2 grid share 3 doubles/node) and G2P-2 (reads x3 v3 V0 F9 eps6 alpha
+# ep6, writes x3 V F9 eps6 sigma6 alpha ep6 vm = 496 B, + 6 doubles/node gathered)
+BYTES_MUSL = {"p2g": 112 + 7, "g2p": 80 + 3 + 496 + 6, "step": 720}
+
+
+def launches_per_run(args, nbodies):
+    """Kernels of the timed steps: USL clear + P2G per body + compaction + grid
+    update + G2P per body; MUSL adds G2P-1 per body and, in 3D, the gradient
+    velocity pass (2D: the solve and the node pass in place of the grid update);
+    a cell sort is a key pass per body, three scan passes and the scatter."""
+    per_step = 3 + 2 * nbodies if args.algorithm == "usl" else 4 + 3 * nbodies
+    sorts = args.steps // args.sort_interval if args.sort_interval > 0 else 0
+    return args.steps * per_step + sorts * (nbodies + 4)
+
+
+def scheme_kw(args):
+    """Descriptor arguments of the update scheme under test."""
+    if args.algorithm == "musl":
+        return {"algorithm": "musl", "alpha": args.alpha}
+    return {}
 
 
 def load_peaks():
@@ -234,8 +255,9 @@ def run_reference(args):
     oracle.build()
     g, s, alg, data, cfg = workload(args.workload)
     npart = sum(x.parCount for x in s)
-    mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"])
-    threads = oracle.max_threads()
+    mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
+                             **scheme_kw(args))
+    threads = oracle.max_threads() if args.algorithm == "usl" else 1  # the oracle's MUSL is single-threaded
     ctx = oracle.OracleContext(mk(), threads=threads)
     for _ in range(args.warmup):
         ctx.step(1, check=False)
@@ -248,9 +270,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (geometry-generated particles)", "config": cfg,
+        "data": "synthetic (geometry-generated particles)",
+        "config": dict(cfg, algorithm=args.algorithm if args.algorithm == "usl" else f"musl(alpha={args.alpha})"),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full USL steps of the workload after {args.warmup} warm-up "
+                         "sample": f"{args.steps} full {args.algorithm.upper()} steps of the workload after {args.warmup} warm-up "
                                    f"steps; C++ restatement of the Julia loops (Julia is not installed on the "
                                    f"host), OpenMP over {threads} threads"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -272,7 +295,7 @@ def run_ours(args):
     g, s, alg, data, cfg = workload(args.workload)
     npart = sum(x.parCount for x in s)
     mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
-                             precision=args.precision, sort_interval=args.sort_interval)
+                             precision=args.precision, sort_interval=args.sort_interval, **scheme_kw(args))
     ctx = MPMContext(mk())
     ctx.step(args.warmup)
     sampler = ClockSampler()
@@ -293,10 +316,11 @@ def run_ours(args):
     per = {k: v / nprof for k, v in st.items()}
     dom = max(("p2g", "g2p"), key=lambda k: per[k])
     peak, peak_kind = load_peaks()
-    bts = BYTES[args.precision][dom] * npart
+    table = BYTES_MUSL if args.algorithm == "musl" else BYTES[args.precision]
+    bts = table[dom] * npart
     achieved = bts / (per[dom] * 1e-3) / 1e9
     traffic = ncu_traffic(dom, args.precision)
-    step_bytes = BYTES[args.precision]["step"] * npart
+    step_bytes = table["step"] * npart
     ctx.close()
 
     # End to end through the public API.  The caller's particle arrays (inputs)
@@ -309,7 +333,8 @@ def run_ours(args):
     s_pin = pin_solids(copy.deepcopy(s))
     out_states = [pin_state(BodyState(x.parCount, x.dim)) for x in s]
     mk_pin = lambda: Descriptors(g, s_pin, tolerance=alg.tolerance, body_force=data.get("bodyforce"),
-                                 dt=data["dt"], precision=args.precision, sort_interval=args.sort_interval)
+                                 dt=data["dt"], precision=args.precision, sort_interval=args.sort_interval,
+                                 **scheme_kw(args))
     parts = {}
     e2e_ctx_t0 = time.perf_counter()
     desc = mk_pin()
@@ -335,17 +360,17 @@ def run_ours(args):
         if world == 1 and not args.no_cpu:
             from oracle import oracle
             oracle.build()
-            thr = oracle.max_threads()
+            thr = oracle.max_threads() if args.algorithm == "usl" else 1  # the oracle's MUSL is single-threaded
             v_all, n_all, el_all = cpu_sample(lambda: Descriptors(g, s, tolerance=alg.tolerance,
                                                                   body_force=data.get("bodyforce"),
-                                                                  dt=data["dt"]),
+                                                                  dt=data["dt"], **scheme_kw(args)),
                                               npart, thr, args.cpu_seconds)
             v_one, n_one, el_one = cpu_sample(lambda: Descriptors(g, s, tolerance=alg.tolerance,
                                                                   body_force=data.get("bodyforce"),
-                                                                  dt=data["dt"]),
+                                                                  dt=data["dt"], **scheme_kw(args)),
                                               npart, 1, args.cpu_seconds / 3)
             cpu = {"value": v_all, "unit": METRIC, "cores": thr, "kind": "port",
-                   "sample": f"{n_all} USL steps of the same workload in {el_all:.1f} s (FP64 C++ "
+                   "sample": f"{n_all} {args.algorithm.upper()} steps of the same workload in {el_all:.1f} s (FP64 C++ "
                              f"restatement of the reference loops, OpenMP {thr} threads); single thread: "
                              f"{v_one:.4g} {METRIC} over {n_one} steps",
                    "single_thread_value": v_one}
@@ -355,6 +380,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
             "data": "synthetic (geometry-generated particles, no dataset)",
             "config": dict(cfg, precision=args.precision, sort_interval=args.sort_interval,
+                           algorithm=args.algorithm if args.algorithm == "usl" else f"musl(alpha={args.alpha})",
                            parallelism=f"replicas{world}" if world > 1 else "single-gpu"),
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "stage_ms_per_step": per,
@@ -366,7 +392,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h / args.steps + 8 * 5, "host_memory": "pinned",
                     "how": f"create from host arrays, {args.steps} x (step + energies read), download all",
                     **parts},
-            "gpu_launches": args.steps * (2 * len(s) + 1),
+            "gpu_launches": launches_per_run(args, len(s)),
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
@@ -597,6 +623,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--algorithm", default="usl", choices=["usl", "musl"],
+                    help="update scheme: USL (the headline) or MUSL (FLIP/PIC blend --alpha)")
+    ap.add_argument("--alpha", type=float, default=1.0, help="MUSL FLIP/PIC blend")
     ap.add_argument("--sort-interval", type=int, default=0,
                     help="counting-sort particles by cell every N steps (0: never)")
     ap.add_argument("--workload", default="taylor_bar",
