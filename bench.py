@@ -210,7 +210,7 @@ def pinned_like(a: np.ndarray) -> np.ndarray:
 
 PARTICLE_ARRAYS = ("pos", "velocity", "mass", "volume", "volumeInitial", "deformationGradient", "strain",
                    "stress", "youngs")
-MATERIAL_ARRAYS = ("alpha", "pstrain", "pstrain_3D")
+MATERIAL_ARRAYS = ("alpha", "pstrain", "pstrain_3D", "alphadot")
 
 
 def pin_solids(solids):
@@ -225,7 +225,7 @@ def pin_solids(solids):
 
 
 def pin_state(st):
-    for k in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr"):
+    for k in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot"):
         setattr(st, k, pinned_like(getattr(st, k)))
     return st
 
@@ -351,7 +351,7 @@ def run_ours(args):
     c2.close()
     h2d = sum(a.nbytes for a in desc._keep)
     d2h = sum(sum(getattr(stt, k).nbytes for k in ("pos", "velocity", "volume", "F", "strain", "stress",
-                                                   "alpha", "pstrain", "vmstr")) for stt in states)
+                                                   "alpha", "pstrain", "vmstr", "alphadot")) for stt in states)
     e2e_t = allreduce_max(dist, e2e_wall)
     e2e_value = total_updates / e2e_t
 

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 3
+#define JUMP_MPM_ABI_VERSION 4
 
 /* status codes */
 #define MPM_OK               0
@@ -55,6 +55,8 @@ extern "C" {
 #define MPM_MAT_ELASTIC     0   /* ElasticMaterial, Material.jl:37-81 */
 #define MPM_MAT_NEOHOOKEAN  1   /* NeoHookeanMaterial, Material.jl:100-122 */
 #define MPM_MAT_J2          2   /* ElastoPlasticMaterial, Material.jl:128-275 */
+#define MPM_MAT_JOHNSON_COOK 3  /* JohnsonCookMaterial, Material.jl:279-330, 386-443 (3D) */
+#define MPM_MAT_VOCE        4   /* VoceMaterial, Material.jl:336-383, 445-493 (3D) */
 
 /* particle precision (grid accumulation is always FP64) */
 #define MPM_PREC_F64        0   /* every particle field and every operation in FP64 */
@@ -80,6 +82,10 @@ typedef struct mpm_material_desc {
   int32_t reserved;
   double  E, nu, density;      /* constructor arguments */
   double  fy, k1;              /* J2 yield stress and linear hardening modulus */
+  /* Johnson-Cook: yield (A + B ep^n)(1 + epdot/epsdot0)^C (C != 0) or A + B ep^n;
+     Voce: A - B exp(-C ep) (n, epsdot0 unused); both: plastic strain rate filter
+     time 1000 cellsize / sqrt((lambda + 2 mu)/density) */
+  double  A, B, C, n, epsdot0, cellsize;
 } mpm_material_desc;
 
 /* Particle arrays of one Solid2D/Solid3D (Solid.jl:67-125, 267-297), read at create time. */
@@ -97,6 +103,7 @@ typedef struct mpm_body_desc {
   const double* alpha;              /* J2: equivalent plastic strain, or NULL (zeros) */
   const double* pstrain;            /* J2: 3 (2D Voigt) or 9 (3D) per particle, or NULL */
   const double* youngs;             /* optional per-particle Young's modulus, or NULL */
+  const double* alphadot;           /* Johnson-Cook/Voce: plastic strain rate, or NULL (zeros) */
 } mpm_body_desc;
 
 /* Writable views for mpm_download; any pointer may be NULL to skip that field. */
@@ -110,6 +117,7 @@ typedef struct mpm_body_view {
   double* alpha;
   double* pstrain;
   double* vmstr;                    /* von Mises stress written by Elastic-3D and J2 updates */
+  double* alphadot;                 /* Johnson-Cook/Voce plastic strain rate, or NULL */
 } mpm_body_view;
 
 typedef struct mpm_params {

@@ -12,7 +12,8 @@ EnergiesFix, DisplacementFix), Output (OvitoOutput) and Problem
 from .algorithm import (USL, MUSL, LinearBasis, QuadBsplineBasis, CubicBsplineBasis,
                         ConstantBodyForce2D, ConstantBodyForce3D)
 from .grid import Grid2D, Grid3D, to_1D_index
-from .material import ElasticMaterial, NeoHookeanMaterial, ElastoPlasticMaterial, RigidMaterial
+from .material import (ElasticMaterial, NeoHookeanMaterial, ElastoPlasticMaterial, JohnsonCookMaterial,
+                       VoceMaterial, RigidMaterial)
 from .solid import (Solid2D, Solid3D, assign_velocity, move, julia_range, buildParticleForCircle,
                     buildParticleForRing, buildParticleForSphere, buildParticleForCylinder,
                     buildParticleForRectangle, buildParticleForBlock)

@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-ABI_VERSION = 3  # JUMP_MPM_ABI_VERSION of the structures below
+ABI_VERSION = 4  # JUMP_MPM_ABI_VERSION of the structures below
 
 MPM_OK = 0
 MPM_ERR_ARG = 1
@@ -40,6 +40,8 @@ ERR_NAMES = {
 MPM_MAT_ELASTIC = 0
 MPM_MAT_NEOHOOKEAN = 1
 MPM_MAT_J2 = 2
+MPM_MAT_JOHNSON_COOK = 3
+MPM_MAT_VOCE = 4
 
 MPM_PREC_F64 = 0
 MPM_PREC_F32 = 1
@@ -75,6 +77,12 @@ class MaterialDesc(C.Structure):
         ("density", C.c_double),
         ("fy", C.c_double),
         ("k1", C.c_double),
+        ("A", C.c_double),
+        ("B", C.c_double),
+        ("C", C.c_double),
+        ("n", C.c_double),
+        ("epsdot0", C.c_double),
+        ("cellsize", C.c_double),
     ]
 
 
@@ -93,6 +101,7 @@ class BodyDesc(C.Structure):
         ("alpha", _dp),
         ("pstrain", _dp),
         ("youngs", _dp),
+        ("alphadot", _dp),
     ]
 
 
@@ -107,6 +116,7 @@ class BodyView(C.Structure):
         ("alpha", _dp),
         ("pstrain", _dp),
         ("vmstr", _dp),
+        ("alphadot", _dp),
     ]
 
 

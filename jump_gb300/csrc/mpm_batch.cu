@@ -307,6 +307,16 @@ int launch_m(mpm_batch* b, void* P, int64_t n, int th, int per) {
     case MPM_MAT_NEOHOOKEAN:
       return b->grav ? launch_t<D, R, MPM_MAT_NEOHOOKEAN, true>(b, P, n, th, per)
                      : launch_t<D, R, MPM_MAT_NEOHOOKEAN, false>(b, P, n, th, per);
+    case MPM_MAT_JOHNSON_COOK:
+      if constexpr (D == 3)
+        return b->grav ? launch_t<D, R, MPM_MAT_JOHNSON_COOK, true>(b, P, n, th, per)
+                       : launch_t<D, R, MPM_MAT_JOHNSON_COOK, false>(b, P, n, th, per);
+      return fail(MPM_ERR_ARG, "mpm_batch: Johnson-Cook is a 3D material");
+    case MPM_MAT_VOCE:
+      if constexpr (D == 3)
+        return b->grav ? launch_t<D, R, MPM_MAT_VOCE, true>(b, P, n, th, per)
+                       : launch_t<D, R, MPM_MAT_VOCE, false>(b, P, n, th, per);
+      return fail(MPM_ERR_ARG, "mpm_batch: Voce is a 3D material");
     default:
       return b->grav ? launch_t<D, R, MPM_MAT_J2, true>(b, P, n, th, per)
                      : launch_t<D, R, MPM_MAT_J2, false>(b, P, n, th, per);
@@ -646,14 +656,7 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       I.bbeg[k] = poff;
       I.bcnt[k] = d.bodies[k].count;
       poff += d.bodies[k].count;
-      MatParams& mp = I.mp[k];
-      mp.type = m.type;
-      mp.per_particle = d.bodies[k].youngs != nullptr;
-      mp.lambda = m.E * m.nu / (1 + m.nu) / (1 - 2 * m.nu);  // Material.jl:54-55
-      mp.mu = m.E / 2 / (1 + m.nu);
-      mp.kappa = mp.lambda + mp.mu;
-      mp.fy = m.fy;
-      mp.k1 = m.k1;
+      I.mp[k] = make_mat_params(m, d.bodies[k].youngs != nullptr, d.dt);
     }
     I.pcount = poff - I.pbegin;
     I.dt = d.dt;
@@ -732,6 +735,7 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       if ((r = upload(b, pp, d.strain, D * D, L::EPS, sym_from_full(D, b->d_status, ST_ASYM_STRESS)))) return r;
       if ((r = upload(b, pp, d.stress, D * D, L::SIG, sym_from_full(D, b->d_status, ST_ASYM_STRESS)))) return r;
       if ((r = upload(b, pp, d.alpha, 1, L::ALPHA, ident(1)))) return r;
+      if ((r = upload(b, pp, d.alphadot, 1, L::ALPHAD, ident(1)))) return r;
       if (d.pstrain) {
         r = D == 2 ? upload(b, pp, d.pstrain, 3, L::EP, ident(3)) : upload(b, pp, d.pstrain, 9, L::EP, sym_from_full(3, b->d_status, ST_ASYM_PSTRAIN));
         if (r) return r;
@@ -811,7 +815,7 @@ int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t prec
       if (bd.count < 0) return fail(MPM_ERR_ARG, "mpm_batch_create: negative particle count");
       if (bd.count > 0 && (!bd.pos || !bd.velocity || !bd.mass || !bd.volume || !bd.volume_initial))
         return fail(MPM_ERR_ARG, "mpm_batch_create: pos, velocity, mass, volume and volume_initial are required");
-      if (bd.mat.type != MPM_MAT_ELASTIC && bd.mat.type != MPM_MAT_NEOHOOKEAN && bd.mat.type != MPM_MAT_J2)
+      if (!material_ok(bd.mat.type, D))
         return fail(MPM_ERR_ARG, "mpm_batch_create: unknown material type");
       mixed = mixed || (mat >= 0 && bd.mat.type != mat);
       mat = bd.mat.type;
@@ -889,6 +893,7 @@ int mpm_batch_download(mpm_batch* b, int32_t instance, int32_t body, const mpm_b
   if ((r = download(b, pp, v->strain, D * D, EPS, full_from_sym(D)))) return r;
   if ((r = download(b, pp, v->stress, D * D, SIG, full_from_sym(D)))) return r;
   if ((r = download(b, pp, v->alpha, 1, ALPHA, ident(1)))) return r;
+  if ((r = download(b, pp, v->alphadot, 1, D == 2 ? Layout<2>::ALPHAD : Layout<3>::ALPHAD, ident(1)))) return r;
   if ((r = D == 2 ? download(b, pp, v->pstrain, 3, EP, ident(3)) : download(b, pp, v->pstrain, 9, EP, full_from_sym(3))))
     return r;
   if (v->vmstr && pp.count > 0) {

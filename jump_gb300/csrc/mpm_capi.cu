@@ -38,14 +38,14 @@ int sym_slot(int dim, int i, int j) {
 int num_fields(int dim) { return dim == 2 ? Layout<2>::NF : Layout<3>::NF; }
 
 struct FieldIdx {
-  int X, V, M, VOL, VOL0, F, EPS, SIG, VM, ALPHA, EP, LAM, MU, S, PS;
+  int X, V, M, VOL, VOL0, F, EPS, SIG, VM, ALPHA, EP, LAM, MU, ALPHAD, S, PS;
 };
 
 template <int D>
 FieldIdx make_idx() {
   using L = Layout<D>;
   return FieldIdx{L::X, L::V, L::M, L::VOL, L::VOL0, L::F, L::EPS, L::SIG,
-                  L::VM, L::ALPHA, L::EP, L::LAM, L::MU, L::S, L::PS};
+                  L::VM, L::ALPHA, L::EP, L::LAM, L::MU, L::ALPHAD, L::S, L::PS};
 }
 
 }  // namespace
@@ -484,15 +484,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     c->np += bd[b].count;
     maxn = bd[b].count > maxn ? bd[b].count : maxn;
     const mpm_material_desc& m = bd[b].mat;
-    MatParams mp{};
-    mp.type = m.type;
-    mp.per_particle = bd[b].youngs != nullptr;
-    mp.lambda = m.E * m.nu / (1 + m.nu) / (1 - 2 * m.nu);  // Material.jl:54-55
-    mp.mu = m.E / 2 / (1 + m.nu);
-    mp.kappa = mp.lambda + mp.mu;  // Material.jl:161
-    mp.fy = m.fy;
-    mp.k1 = m.k1;
-    c->mats.push_back(mp);
+    c->mats.push_back(make_mat_params(m, bd[b].youngs != nullptr, prm->dt));
     c->nus.push_back(m.nu);
   }
   size_t ptot = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1);
@@ -550,6 +542,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     if (d.stress && (r = upload(c, b, d.stress, D * D, fi.SIG, sym_from_full(D, c->status, ST_ASYM_STRESS))))
       return r;
     if (d.alpha && (r = upload(c, b, d.alpha, 1, fi.ALPHA, ident(1)))) return r;
+    if (d.alphadot && (r = upload(c, b, d.alphadot, 1, fi.ALPHAD, ident(1)))) return r;
     if (d.pstrain) {
       if (D == 2) r = upload(c, b, d.pstrain, 3, fi.EP, ident(3));
       else r = upload(c, b, d.pstrain, 9, fi.EP, sym_from_full(3, c->status, ST_ASYM_PSTRAIN));
@@ -618,8 +611,8 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
     if (d.count < 0) return fail(MPM_ERR_ARG, "mpm_create: negative particle count");
     if (d.count > 0 && (!d.pos || !d.velocity || !d.mass || !d.volume || !d.volume_initial))
       return fail(MPM_ERR_ARG, "mpm_create: pos, velocity, mass, volume and volume_initial are required");
-    if (d.mat.type != MPM_MAT_ELASTIC && d.mat.type != MPM_MAT_NEOHOOKEAN && d.mat.type != MPM_MAT_J2)
-      return fail(MPM_ERR_ARG, "mpm_create: unknown material type");
+    if (!material_ok(d.mat.type, D))
+      return fail(MPM_ERR_ARG, "mpm_create: unknown material type (Johnson-Cook and Voce are 3D)");
   }
   mpm_ctx* c = new mpm_ctx();
   int r = create_impl(grid, bodies, nbodies, params, c);
@@ -669,6 +662,7 @@ int mpm_download(mpm_ctx* c, int32_t body, const mpm_body_view* v) {
   if ((r = download(c, body, v->strain, D * D, fi.EPS, full_from_sym(D)))) return r;
   if ((r = download(c, body, v->stress, D * D, fi.SIG, full_from_sym(D)))) return r;
   if ((r = download(c, body, v->alpha, 1, fi.ALPHA, ident(1)))) return r;
+  if ((r = download(c, body, v->alphadot, 1, fi.ALPHAD, ident(1)))) return r;
   if (D == 2) r = download(c, body, v->pstrain, 3, fi.EP, ident(3));
   else r = download(c, body, v->pstrain, 9, fi.EP, full_from_sym(3));
   if (r) return r;
@@ -755,7 +749,7 @@ int mpm_energies(mpm_ctx* c, double* ke, double* se, double* momentum) {
 
 // snapshot layout: 4 x int64 header (magic, dim, precision, particle count),
 // the particle SoA in slot order, then orig[slot] (the slot -> particle map)
-static const int64_t kMagic = 0x4d504d4a554d5032LL;
+static const int64_t kMagic = 0x4d504d4a554d5033LL;  // "3": particle records with the JC/Voce rate field
 
 int mpm_save(mpm_ctx* c, void* buf, size_t* nbytes) {
   if (!c || !nbytes) return fail(MPM_ERR_ARG, "mpm_save: null argument");

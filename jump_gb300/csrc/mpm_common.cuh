@@ -39,7 +39,8 @@ struct Layout {
   static constexpr int EP = ALPHA + 1;
   static constexpr int LAM = EP + PS;          // per-particle Lame constants (optional)
   static constexpr int MU = LAM + 1;
-  static constexpr int NF = MU + 1;
+  static constexpr int ALPHAD = MU + 1;        // Johnson-Cook/Voce plastic strain rate
+  static constexpr int NF = ALPHAD + 1;
 };
 
 // symmetric index (i, j) -> storage slot
@@ -55,6 +56,9 @@ struct MatParams {
   int type;        // MPM_MAT_*
   int per_particle;  // 1: use the LAM/MU particle fields
   double lambda, mu, kappa, fy, k1;
+  // Johnson-Cook / Voce: hardening constants, rate filter time 1000 cellsize /
+  // signal velocity, and the step dt it is applied with
+  double A, B, C, n, epsdot0, tav, dtime;
 };
 
 // Grid description shared by all kernels.

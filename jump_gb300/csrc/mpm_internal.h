@@ -6,10 +6,44 @@
 
 #include <string>
 
+#include <cmath>
+
+#include "../../include/jump_mpm.h"
 #include "mpm_common.cuh"
 #include "mpm_adjoint.cuh"
 
 namespace jmpm {
+
+// Kernel parameters of a material (Material.jl:37-172, 279-383): Lame constants
+// as the constructors compute them; for Johnson-Cook/Voce the rate filter time
+// 1000 cellsize / sqrt((lambda + 2 mu)/density) and the step dt.
+inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, double dt) {
+  MatParams mp{};
+  mp.type = m.type;
+  mp.per_particle = per_particle;
+  mp.lambda = m.E * m.nu / (1 + m.nu) / (1 - 2 * m.nu);  // Material.jl:54-55
+  mp.mu = m.E / 2 / (1 + m.nu);
+  mp.kappa = mp.lambda + mp.mu;  // Material.jl:161, 315
+  mp.fy = m.fy;
+  mp.k1 = m.k1;
+  mp.A = m.A;
+  mp.B = m.B;
+  mp.C = m.C;
+  mp.n = m.n;
+  mp.epsdot0 = m.epsdot0;
+  if (m.type == MPM_MAT_JOHNSON_COOK || m.type == MPM_MAT_VOCE) {
+    const double velo = std::sqrt((mp.lambda + 2 * mp.mu) / m.density);  // Material.jl:317
+    mp.tav = 1000 * m.cellsize / velo;                                   // Material.jl:428
+  }
+  mp.dtime = dt;
+  return mp;
+}
+
+// material model types a context or batch accepts in dimension dim
+inline bool material_ok(int type, int dim) {
+  if (type == MPM_MAT_ELASTIC || type == MPM_MAT_NEOHOOKEAN || type == MPM_MAT_J2) return true;
+  return dim == 3 && (type == MPM_MAT_JOHNSON_COOK || type == MPM_MAT_VOCE);
+}
 
 struct CompMapH {
   int n;

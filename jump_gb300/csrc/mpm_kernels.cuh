@@ -452,6 +452,54 @@ __device__ __forceinline__ double det_d(const double* A) {
   return (x0[0] * c0 + x0[1] * c1) + x0[2] * c2;
 }
 
+// Johnson-Cook / Voce update_stress! (Material.jl:386-443, 445-493), 3D: trial
+// stress sig + 2 mu deps, deviator with the reference's 0.333333333, radial
+// return to the yield stress of the equivalent plastic strain (and, for
+// Johnson-Cook, of the filtered plastic strain rate), that rate's update, and
+// the returned stress deviator + kappa tr(eps) I.  Symmetric storage (xx, yy,
+// zz, xy, yz, xz).
+template <class R, int MAT>
+__device__ __forceinline__ void jc_voce_3d(const MatParams& mp, R mu, R kappa, const R* sig_old, const R* deps,
+                                           const R* eps, R* sig, R* alpha, R* alphad, R* vm) {
+  const R ep = *alpha;
+  R yieldS;
+  if (ep < R(1.0e-10)) {
+    yieldS = R(mp.A);
+  } else if (MAT == MPM_MAT_JOHNSON_COOK) {
+    const R ratio = fmax(*alphad / R(mp.epsdot0), R(1));
+    const R base = R(mp.A) + R(mp.B) * pow(ep, R(mp.n));
+    yieldS = mp.C != 0.0 ? base * pow(R(1) + ratio, R(mp.C)) : base;
+  } else {
+    yieldS = R(mp.A) - R(mp.B) * exp(-R(mp.C) * ep);
+  }
+  const R Gd = mu;
+  R d[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) d[c] = sig_old[c] + R(2) * Gd * deps[c];
+  const R third = R(0.333333333) * ((d[0] + d[1]) + d[2]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) d[c] = d[c] - third;
+  const R J2 = R(1.224744871391589) *
+               sqrt(((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + R(2) * ((d[3] * d[3] + d[5] * d[5]) + d[4] * d[4]));
+  R dp = R(0);
+  if (!(J2 < yieldS)) {
+    dp = (J2 - yieldS) / (R(3) * Gd);
+    const R sc = yieldS / J2;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) d[c] = d[c] * sc;
+  }
+  *alpha = ep + dp;
+  const R tav = R(mp.tav);
+  R ad = *alphad;
+  ad = ad - ad * R(mp.dtime) / tav;
+  ad = ad + dp / tav;
+  *alphad = fmax(R(0), ad);
+  *vm = sqrt(((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + R(2) * ((d[3] * d[3] + d[5] * d[5]) + d[4] * d[4]));
+  const R p = kappa * ((eps[0] + eps[1]) + eps[2]);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? d[c] + p : d[c];
+}
+
 // F <- F (I + L dt), J, V = J V0, strain += sym(L dt), update_stress! of particle p
 // (:520-532), given L dt; fin: the particle's new x and v are finite.
 template <int D, class R, int MAT>
@@ -484,14 +532,15 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
   double J = det_d<D>(Fd);  // det F in FP64 for both precisions
   *field<R>(pp, L::VOL, p) = R(J * to_f64(*field<R>(pp, L::VOL0, p)));
   // strain += dt * 0.5*(L + L')
-  R eps[L::S];
+  R eps[L::S], deps[L::S];
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
     for (int j = i; j < D; ++j) {
       int c = sym<D>(i, j);
       R e = *field<R>(pp, L::EPS + c, p);
-      e += (i == j) ? Ldt[i][i] : R(0.5) * (Ldt[i][j] + Ldt[j][i]);
+      deps[c] = (i == j) ? Ldt[i][i] : R(0.5) * (Ldt[i][j] + Ldt[j][i]);
+      e += deps[c];
       eps[c] = e;
       *field<R>(pp, L::EPS + c, p) = e;
     }
@@ -514,6 +563,16 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
     elastic<D, R>(lam, mu, eps, sig);
   } else if (MAT == MPM_MAT_NEOHOOKEAN) {
     neohookean<D, R>(lam, mu, Fn, J, sig);
+  } else if (MAT == MPM_MAT_JOHNSON_COOK || MAT == MPM_MAT_VOCE) {
+    if constexpr (D == 3) {
+      R so[6], alpha = *field<R>(pp, L::ALPHA, p), ad = *field<R>(pp, L::ALPHAD, p), vm;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) so[c] = *field<R>(pp, L::SIG + c, p);
+      jc_voce_3d<R, MAT>(mp, mu, kappa, so, deps, eps, sig, &alpha, &ad, &vm);
+      *field<R>(pp, L::ALPHA, p) = alpha;
+      *field<R>(pp, L::ALPHAD, p) = ad;
+      *field<R>(pp, L::VM, p) = vm;
+    }
   } else {
     R alpha = *field<R>(pp, L::ALPHA, p);
     R ep[L::PS];

@@ -134,6 +134,12 @@ void Launchers<D>::musl_g2p2(cudaStream_t s, const GridP& g, const NodeP& nd, co
     case MPM_MAT_NEOHOOKEAN:
       musl_g2p2_kernel<D, MPM_MAT_NEOHOOKEAN, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
       break;
+    case MPM_MAT_JOHNSON_COOK:
+      if constexpr (D == 3) musl_g2p2_kernel<D, MPM_MAT_JOHNSON_COOK, true><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+      break;
+    case MPM_MAT_VOCE:
+      if constexpr (D == 3) musl_g2p2_kernel<D, MPM_MAT_VOCE, true><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+      break;
     default: musl_g2p2_kernel<D, MPM_MAT_J2, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status); break;
   }
 }
@@ -148,12 +154,16 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
     switch (mp.type) {
       case MPM_MAT_ELASTIC: JMPM_G2P(float, MPM_MAT_ELASTIC); break;
       case MPM_MAT_NEOHOOKEAN: JMPM_G2P(float, MPM_MAT_NEOHOOKEAN); break;
+      case MPM_MAT_JOHNSON_COOK: if constexpr (D == 3) JMPM_G2P(float, MPM_MAT_JOHNSON_COOK); break;
+      case MPM_MAT_VOCE: if constexpr (D == 3) JMPM_G2P(float, MPM_MAT_VOCE); break;
       default: JMPM_G2P(float, MPM_MAT_J2); break;
     }
   } else {
     switch (mp.type) {
       case MPM_MAT_ELASTIC: JMPM_G2P(double, MPM_MAT_ELASTIC); break;
       case MPM_MAT_NEOHOOKEAN: JMPM_G2P(double, MPM_MAT_NEOHOOKEAN); break;
+      case MPM_MAT_JOHNSON_COOK: if constexpr (D == 3) JMPM_G2P(double, MPM_MAT_JOHNSON_COOK); break;
+      case MPM_MAT_VOCE: if constexpr (D == 3) JMPM_G2P(double, MPM_MAT_VOCE); break;
       default: JMPM_G2P(double, MPM_MAT_J2); break;
     }
   }

@@ -90,6 +90,12 @@ __global__ void __launch_bounds__(256) wide_g2p_kernel(const WideBody* __restric
   switch (sB.mp.type) {
     case MPM_MAT_ELASTIC: g2p_particle<D, R, MPM_MAT_ELASTIC>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st); break;
     case MPM_MAT_NEOHOOKEAN: g2p_particle<D, R, MPM_MAT_NEOHOOKEAN>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st); break;
+    case MPM_MAT_JOHNSON_COOK:
+      if constexpr (D == 3) g2p_particle<D, R, MPM_MAT_JOHNSON_COOK>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st);
+      break;
+    case MPM_MAT_VOCE:
+      if constexpr (D == 3) g2p_particle<D, R, MPM_MAT_VOCE>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st);
+      break;
     default: g2p_particle<D, R, MPM_MAT_J2>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st); break;
   }
 }

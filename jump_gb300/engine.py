@@ -58,6 +58,8 @@ class Descriptors:
             b.mat.type = m.kind
             b.mat.E, b.mat.nu, b.mat.density = m.E, m.nu, m.density
             b.mat.fy, b.mat.k1 = getattr(m, "fy", 0.0), getattr(m, "k1", 0.0)
+            for k in ("A", "B", "C", "n", "epsdot0", "cellsize"):
+                setattr(b.mat, k, float(getattr(m, k, 0.0)))
             arrs = {
                 "pos": np.ascontiguousarray(sol.pos, dtype=np.float64),
                 "velocity": np.ascontiguousarray(sol.velocity, dtype=np.float64),
@@ -76,6 +78,9 @@ class Descriptors:
                     arrs["pstrain"] = colmajor(m.pstrain_3D[: sol.parCount])
             if getattr(sol, "youngs", None) is not None:
                 arrs["youngs"] = np.ascontiguousarray(sol.youngs, dtype=np.float64)
+            if getattr(m, "alphadot", None) is not None:  # Johnson-Cook / Voce state
+                arrs["alpha"] = np.ascontiguousarray(m.alpha[: sol.parCount], dtype=np.float64)
+                arrs["alphadot"] = np.ascontiguousarray(m.alphadot[: sol.parCount], dtype=np.float64)
             for k, v in arrs.items():
                 self._keep.append(v)
                 setattr(b, k, _capi.dptr(v))
@@ -113,10 +118,11 @@ class BodyState:
         self.alpha = np.zeros(n)
         self.pstrain = np.zeros(n * (3 if d == 2 else 9))
         self.vmstr = np.zeros(n)
+        self.alphadot = np.zeros(n)
 
     def view(self) -> _capi.BodyView:
         v = _capi.BodyView()
-        for k in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr"):
+        for k in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot"):
             setattr(v, k, _capi.dptr(getattr(self, k)))
         return v
 

@@ -73,6 +73,51 @@ class NeoHookeanMaterial(MaterialType):
         self.k1 = 0.0
 
 
+class JohnsonCookMaterial(MaterialType):
+    """JohnsonCookMaterial(E,nu,density,A,B,C,n,eps0dot,m,chi,Cp,cellsize,parCount),
+    Material.jl:279-330; 3D stress update Material.jl:386-443.  State per
+    particle: alpha (equivalent plastic strain), alphadot (its filtered rate),
+    vmStr.  m, chi and Cp enter no stress update."""
+    kind = _capi.MPM_MAT_JOHNSON_COOK
+
+    def __init__(self, E, nu, density, A, B, C, n, eps0dot, m, chi, Cp, cellsize, parCount):
+        self.E, self.nu, self.density = float(E), float(nu), float(density)
+        self.lambda_, self.mu = _lame(self.E, self.nu)
+        self.kappa = self.lambda_ + self.mu
+        self.A, self.B, self.C, self.n = float(A), float(B), float(C), float(n)
+        self.epsdot0, self.m, self.chi, self.Cp = float(eps0dot), float(m), float(chi), float(Cp)
+        self.cellsize = float(cellsize)
+        self.signal_velocity = math.sqrt((self.lambda_ + 2 * self.mu) / self.density)
+        self.delta = self.chi / (self.density * self.Cp) if self.Cp != 0 else math.inf
+        k = int(parCount)
+        self.alpha = np.zeros(k)
+        self.alphadot = np.zeros(k)
+        self.vmStr = np.zeros(k)
+        self.fy = 0.0
+        self.k1 = 0.0
+
+
+class VoceMaterial(MaterialType):
+    """VoceMaterial(E,nu,density,A,B,C,chi,Cp,cellsize,parCount), Material.jl:336-383;
+    3D stress update Material.jl:445-493 (yield A - B exp(-C alpha))."""
+    kind = _capi.MPM_MAT_VOCE
+
+    def __init__(self, E, nu, density, A, B, C, chi, Cp, cellsize, parCount):
+        self.E, self.nu, self.density = float(E), float(nu), float(density)
+        self.lambda_, self.mu = _lame(self.E, self.nu)
+        self.kappa = self.lambda_ + self.mu
+        self.A, self.B, self.C = float(A), float(B), float(C)
+        self.n, self.epsdot0 = 0.0, 0.0
+        self.chi, self.Cp, self.cellsize = float(chi), float(Cp), float(cellsize)
+        self.signal_velocity = math.sqrt((self.lambda_ + 2 * self.mu) / self.density)
+        k = int(parCount)
+        self.alpha = np.zeros(k)
+        self.alphadot = np.zeros(k)
+        self.vmStr = np.zeros(k)
+        self.fy = 0.0
+        self.k1 = 0.0
+
+
 class ElastoPlasticMaterial(MaterialType):
     """J2 plasticity with linear hardening, ElastoPlasticMaterial(E,nu,density,fy,k1,parCount),
     Material.jl:128-171.  State per particle: alpha, pstrain (2D Voigt) and pstrain_3D."""

@@ -56,6 +56,10 @@ def write_back(solids, states):
             m.vmStr[:n] = st.vmstr
         elif isinstance(m, ElasticMaterial) and solid.dim == 3:
             m.vmStr[:n] = st.vmstr
+        elif getattr(m, "alphadot", None) is not None:  # Johnson-Cook / Voce
+            m.alpha[:n] = st.alpha
+            m.alphadot[:n] = st.alphadot
+            m.vmStr[:n] = st.vmstr
 
 
 def _solve(dim, grid, solids, basis, alg, output, fixes, data):

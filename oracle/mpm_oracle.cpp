@@ -17,7 +17,7 @@
 //   3D USL (lifted from the 2D USL, see below) SolveExplicitSolidMechanics3D.jl:230-378
 //   node lookup and hat functions             Basis.jl:63-78, 104-137, 219-251, 292-332
 //   grid geometry                             Grid.jl:104-158, 198-267, 275-291
-//   constitutive updates                      Material.jl:37-81, 100-122, 128-275
+//   constitutive updates                      Material.jl:37-81, 100-122, 128-275, 279-493
 //   energies                                  Fix.jl:248-270
 //   multi-body contact correction             SolveExplicitFEMP2DContact.jl:189-387,
 //                                             SolveExplicitFEMP3DContact.jl:388-519
@@ -45,6 +45,7 @@
 
 #include "../include/jump_mpm.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -66,6 +67,9 @@ int fail(int code, const std::string& msg) {
 struct Material {
   int type = MPM_MAT_ELASTIC;
   double E = 0, nu = 0, density = 0, lambda = 0, mu = 0, kappa = 0, fy = 0, k1 = 0;
+  // Johnson-Cook / Voce (Material.jl:279-383): hardening constants, cellsize and
+  // the signal velocity sqrt((lambda + 2 mu)/density) of the rate filter
+  double A = 0, B = 0, C = 0, n = 0, epsdot0 = 0, cellsize = 0, velo = 0;
 };
 
 Material make_material(const mpm_material_desc& d) {
@@ -80,6 +84,13 @@ Material make_material(const mpm_material_desc& d) {
   m.kappa = m.lambda + m.mu;
   m.fy = d.fy;
   m.k1 = d.k1;
+  m.A = d.A;
+  m.B = d.B;
+  m.C = d.C;
+  m.n = d.n;
+  m.epsdot0 = d.epsdot0;
+  m.cellsize = d.cellsize;
+  m.velo = std::sqrt((m.lambda + 2 * m.mu) / m.density);  // Material.jl:317
   return m;
 }
 
@@ -88,7 +99,7 @@ struct Body {
   int64_t n = 0;
   Material mat;
   std::vector<double> mass, vol0, vol, pos, vel, F, strain, stress;
-  std::vector<double> alpha, pstrain, vmstr, youngs;
+  std::vector<double> alpha, pstrain, vmstr, youngs, alphadot;
   bool has_youngs = false;
 };
 
@@ -198,7 +209,49 @@ inline void matmul(const double* A, const double* B, double* C) {
 template <int D>
 void update_stress(const Material& mat, double lambda, double mu, double kappa, double* sig,
                    const double* eps, const double* F, double J, double* alpha,
-                   double* pstrain, double* vmstr) {
+                   double* pstrain, double* vmstr, const double* deps, double dtime, double* alphadot) {
+  if (D == 3 && (mat.type == MPM_MAT_JOHNSON_COOK || mat.type == MPM_MAT_VOCE)) {
+    // Material.jl:386-443 (Johnson-Cook), 445-493 (Voce); column-major 3x3
+    const double ep = *alpha;
+    double yieldStress;
+    if (ep < 1.0e-10) {
+      yieldStress = mat.A;
+    } else if (mat.type == MPM_MAT_JOHNSON_COOK) {
+      double epsdot_ratio = *alphadot / mat.epsdot0;
+      epsdot_ratio = std::max(epsdot_ratio, 1.0);
+      if (mat.C != 0) yieldStress = (mat.A + mat.B * std::pow(ep, mat.n)) * std::pow(1.0 + epsdot_ratio, mat.C);
+      else yieldStress = mat.A + mat.B * std::pow(ep, mat.n);
+    } else {
+      yieldStress = mat.A - mat.B * std::exp(-mat.C * ep);
+    }
+    const double Gd = mu;
+    double dev[9];
+    for (int k = 0; k < 9; ++k) dev[k] = sig[k] + 2.0 * Gd * deps[k];
+    const double tr = 0.333333333 * (dev[0] + dev[4] + dev[8]);
+    dev[0] -= tr;
+    dev[4] -= tr;
+    dev[8] -= tr;
+    auto sq = [](double x) { return x * x; };
+    const double J2 = 1.224744871391589 * std::sqrt(sq(dev[0]) + sq(dev[4]) + sq(dev[8]) +
+                                                    2 * (sq(dev[3]) + sq(dev[6]) + sq(dev[7])));
+    double dp = 0.0;
+    if (!(J2 < yieldStress)) {
+      dp = (J2 - yieldStress) / (3.0 * Gd);
+      for (int k = 0; k < 9; ++k) dev[k] *= (yieldStress / J2);
+    }
+    *alpha = ep + dp;
+    const double tav = 1000 * mat.cellsize / mat.velo;
+    *alphadot -= *alphadot * dtime / tav;
+    *alphadot += dp / tav;
+    *alphadot = std::max(0.0, *alphadot);
+    *vmstr = std::sqrt(sq(dev[0]) + sq(dev[4]) + sq(dev[8]) + 2 * (sq(dev[3]) + sq(dev[6]) + sq(dev[7])));
+    const double pr = kappa * (eps[0] + eps[4] + eps[8]);
+    for (int k = 0; k < 9; ++k) sig[k] = dev[k];
+    sig[0] += pr;
+    sig[4] += pr;
+    sig[8] += pr;
+    return;
+  }
   if (mat.type == MPM_MAT_ELASTIC) {
     if (D == 3) {
       // vmStr from the incoming stress (Material.jl:78-79)
@@ -440,8 +493,10 @@ inline void kin_stress(Body<D>& b, int64_t ip, const double* L, double dt, int* 
     kappa = lambda + mu;
   }
   constexpr int PS = (D == 2) ? 3 : 9;
+  double deps[D * D];  // strain_increment = dtime*D (SolveExplicitSolidMechanics3D.jl:208, 363)
+  for (int k = 0; k < D * D; ++k) deps[k] = dt * Dm[k];
   update_stress<D>(b.mat, lambda, mu, kappa, &b.stress[D * D * ip], eps, F, J, &b.alpha[ip],
-                   &b.pstrain[PS * ip], &b.vmstr[ip]);
+                   &b.pstrain[PS * ip], &b.vmstr[ip], deps, dt, &b.alphadot[ip]);
   if (!(J > 0.0) && *status == MPM_OK) *status = MPM_ERR_NEGATIVE_J;
 }
 
@@ -887,6 +942,7 @@ int create(const mpm_grid_desc* gd, const mpm_body_desc* bd, int nb, const mpm_p
     cp(b.strain, d.strain, D * D, 0.0);
     cp(b.stress, d.stress, D * D, 0.0);
     cp(b.alpha, d.alpha, 1, 0.0);
+    cp(b.alphadot, d.alphadot, 1, 0.0);
     cp(b.pstrain, d.pstrain, PS, 0.0);
     b.vmstr.assign(b.n, 0.0);
     b.has_youngs = d.youngs != nullptr;
@@ -954,6 +1010,7 @@ static int download_impl(Ctx<D>* c, int body, const mpm_body_view* v) {
   put(v->alpha, b.alpha, 1);
   put(v->pstrain, b.pstrain, PS);
   put(v->vmstr, b.vmstr, 1);
+  put(v->alphadot, b.alphadot, 1);
   return MPM_OK;
 }
 

@@ -10,13 +10,14 @@ from jump_gb300 import _capi
 from jump_gb300.algorithm import USL, ConstantBodyForce2D, ConstantBodyForce3D
 from jump_gb300.engine import Descriptors, colmajor, from_colmajor
 from jump_gb300.grid import Grid2D, Grid3D
-from jump_gb300.material import ElasticMaterial, ElastoPlasticMaterial, NeoHookeanMaterial
+from jump_gb300.material import (ElasticMaterial, ElastoPlasticMaterial, JohnsonCookMaterial, NeoHookeanMaterial,
+                                 VoceMaterial)
 from jump_gb300.solid import Solid2D, Solid3D
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 
-FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr")
+FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot")
 
 
 def load_golden(name):
@@ -37,6 +38,12 @@ def load_golden(name):
             mat = ElasticMaterial(E, nu, rho, n)
         elif int(typ) == _capi.MPM_MAT_NEOHOOKEAN:
             mat = NeoHookeanMaterial(E, nu, rho, n)
+        elif int(typ) == _capi.MPM_MAT_JOHNSON_COOK:
+            A, Bh, Ch, nh, e0, cs = z[f"b{b}_matx"]
+            mat = JohnsonCookMaterial(E, nu, rho, A, Bh, Ch, nh, e0, 0.0, 0.0, 0.0, cs, n)
+        elif int(typ) == _capi.MPM_MAT_VOCE:
+            A, Bh, Ch, nh, e0, cs = z[f"b{b}_matx"]
+            mat = VoceMaterial(E, nu, rho, A, Bh, Ch, 0.0, 0.0, cs, n)
         else:
             mat = ElastoPlasticMaterial(E, nu, rho, fy, k1, n)
         s = (Solid2D if d == 2 else Solid3D)(pos, mat)
@@ -47,6 +54,9 @@ def load_golden(name):
         s.deformationGradient[:] = from_colmajor(z[f"b{b}_in_F"].ravel(), n, d)
         s.strain[:] = from_colmajor(z[f"b{b}_in_strain"].ravel(), n, d)
         s.stress[:] = from_colmajor(z[f"b{b}_in_stress"].ravel(), n, d)
+        if isinstance(mat, (JohnsonCookMaterial, VoceMaterial)):
+            mat.alpha[:] = z[f"b{b}_in_alpha"]
+            mat.alphadot[:] = z[f"b{b}_in_alphadot"]
         if isinstance(mat, ElastoPlasticMaterial):
             mat.alpha[:] = z[f"b{b}_in_alpha"]
             if d == 2:
@@ -77,6 +87,8 @@ def golden_expected(z, b):
         "stress": z[f"b{b}_out_stress"].ravel(), "alpha": z[f"b{b}_out_alpha"],
         "pstrain": z[f"b{b}_out_ep"].ravel(), "vmstr": z[f"b{b}_out_vm"],
     }
+    if f"b{b}_out_alphadot" in z:
+        out["alphadot"] = z[f"b{b}_out_alphadot"]
     return out
 
 

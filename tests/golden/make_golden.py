@@ -116,8 +116,47 @@ def det(A, d):
 
 
 def stress_update(mat, d, sig, eps, F, J, state):
-    """update_stress! for one particle; returns the new stress (column-major)."""
+    """update_stress! for one particle; returns the new stress (column-major).
+    state carries alpha, ep, vm and, for Johnson-Cook/Voce, alphadot, the strain
+    increment deps = dt D and dt."""
     typ, lam, mu = mat["type"], mat["lambda"], mat["mu"]
+    if typ in (3, 4):  # JohnsonCookMaterial / VoceMaterial, Material.jl:386-493 (3D)
+        ep = state["alpha"]
+        if ep < 1.0e-10:
+            yieldStress = mat["A"]
+        elif typ == 3:
+            ratio = max(state["alphadot"] / mat["epsdot0"], 1.0)
+            if mat["C"] != 0:
+                yieldStress = (mat["A"] + mat["B"] * ep ** mat["n"]) * (1.0 + ratio) ** mat["C"]
+            else:
+                yieldStress = mat["A"] + mat["B"] * ep ** mat["n"]
+        else:
+            yieldStress = mat["A"] - mat["B"] * math.exp(-mat["C"] * ep)
+        Gd = mu
+        trial = [sig[k] + 2.0 * Gd * state["deps"][k] for k in range(9)]
+        third = 0.333333333 * (trial[0] + trial[4] + trial[8])
+        dev = list(trial)
+        for k in (0, 4, 8):
+            dev[k] = trial[k] - third
+        J2 = 1.224744871391589 * math.sqrt(dev[0] * dev[0] + dev[4] * dev[4] + dev[8] * dev[8] +
+                                           2 * (dev[3] * dev[3] + dev[6] * dev[6] + dev[7] * dev[7]))
+        dp = 0.0
+        if not (J2 < yieldStress):
+            dp = (J2 - yieldStress) / (3.0 * Gd)
+            dev = [x * (yieldStress / J2) for x in dev]
+        state["alpha"] = ep + dp
+        tav = 1000 * mat["cellsize"] / math.sqrt((lam + 2 * mu) / mat["density"])
+        ad = state["alphadot"]
+        ad -= ad * state["dt"] / tav
+        ad += dp / tav
+        state["alphadot"] = max(0.0, ad)
+        state["vm"] = math.sqrt(dev[0] * dev[0] + dev[4] * dev[4] + dev[8] * dev[8] +
+                                2 * (dev[3] * dev[3] + dev[6] * dev[6] + dev[7] * dev[7]))
+        p = mat["kappa"] * (eps[0] + eps[4] + eps[8])
+        out = list(dev)
+        for k in (0, 4, 8):
+            out[k] = dev[k] + p
+        return out
     if typ == 0:  # ElasticMaterial
         if d == 3:
             s = sig
@@ -282,9 +321,11 @@ def usl_steps(case, nsteps):
                     m2["lambda"] = E * nu / (1 + nu) / (1 - 2 * nu)
                     m2["mu"] = E / 2 / (1 + nu)
                     m2["kappa"] = m2["lambda"] + m2["mu"]
-                state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip]}
+                state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip],
+                         "alphadot": B["alphadot"][ip], "deps": [dt * x for x in D_], "dt": dt}
                 B["stress"][ip] = stress_update(m2, d, B["stress"][ip], B["strain"][ip], F, J, state)
                 B["alpha"][ip], B["ep"][ip], B["vm"][ip] = state["alpha"], state["ep"], state["vm"]
+                B["alphadot"][ip] = state["alphadot"]
     case["grid_out"] = (mass, mom0, mom, force)
     return case
 
@@ -307,9 +348,11 @@ def _kinematics(B, ip, L, d, dt):
         m2["lambda"] = E * nu / (1 + nu) / (1 - 2 * nu)
         m2["mu"] = E / 2 / (1 + nu)
         m2["kappa"] = m2["lambda"] + m2["mu"]
-    state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip]}
+    state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip],
+             "alphadot": B["alphadot"][ip], "deps": [dt * x for x in D_], "dt": dt}
     B["stress"][ip] = stress_update(m2, d, B["stress"][ip], B["strain"][ip], F, J, state)
     B["alpha"][ip], B["ep"][ip], B["vm"][ip] = state["alpha"], state["ep"], state["vm"]
+    B["alphadot"][ip] = state["alphadot"]
 
 
 def _cholesky_solve_band(A, n, w, rhs):
@@ -469,13 +512,19 @@ def case_from_objects(grid, solids, alg, data, nsteps):
         m = s.mat
         mat = {"type": m.kind, "E": m.E, "nu": m.nu, "density": m.density, "lambda": m.lambda_, "mu": m.mu,
                "kappa": m.lambda_ + m.mu, "fy": getattr(m, "fy", 0.0), "k1": getattr(m, "k1", 0.0)}
+        for k in ("A", "B", "C", "n", "epsdot0", "cellsize"):
+            mat[k] = float(getattr(m, k, 0.0))
         n = s.parCount
         ps = 3 if d == 2 else 9
         ep = np.zeros((n, ps))
         alpha = np.zeros(n)
+        alphadot = np.zeros(n)
         if isinstance(m, ElastoPlasticMaterial):
             alpha = m.alpha[:n].copy()
             ep = m.pstrain[:n].copy() if d == 2 else colmajor(m.pstrain_3D[:n]).reshape(n, 9)
+        elif getattr(m, "alphadot", None) is not None:
+            alpha = m.alpha[:n].copy()
+            alphadot = m.alphadot[:n].copy()
         bodies.append({
             "n": n, "mat": mat,
             "pos": [list(map(float, r)) for r in s.pos], "vel": [list(map(float, r)) for r in s.velocity],
@@ -485,7 +534,7 @@ def case_from_objects(grid, solids, alg, data, nsteps):
             "strain": [list(map(float, r)) for r in colmajor(s.strain).reshape(n, d * d)],
             "stress": [list(map(float, r)) for r in colmajor(s.stress).reshape(n, d * d)],
             "alpha": list(map(float, alpha)), "ep": [list(map(float, r)) for r in ep],
-            "vm": [0.0] * n,
+            "vm": [0.0] * n, "alphadot": list(map(float, alphadot)),
             "youngs": None if s.youngs is None else list(map(float, s.youngs)),
         })
     musl = hasattr(alg, "alpha")
@@ -512,11 +561,12 @@ def save_case(name, case_in, case_out):
     for b, (Bi, Bo) in enumerate(zip(case_in["bodies"], case_out["bodies"])):
         m = Bi["mat"]
         arrs[f"b{b}_mat"] = np.array([m["type"], m["E"], m["nu"], m["density"], m["fy"], m["k1"]])
-        for k in ("pos", "vel", "mass", "vol", "vol0", "F", "strain", "stress", "alpha", "ep"):
+        arrs[f"b{b}_matx"] = np.array([m["A"], m["B"], m["C"], m["n"], m["epsdot0"], m["cellsize"]])
+        for k in ("pos", "vel", "mass", "vol", "vol0", "F", "strain", "stress", "alpha", "ep", "alphadot"):
             arrs[f"b{b}_in_{k}"] = np.array(Bi[k], dtype=np.float64)
         if Bi["youngs"] is not None:
             arrs[f"b{b}_in_youngs"] = np.array(Bi["youngs"], dtype=np.float64)
-        for k in ("pos", "vel", "vol", "F", "strain", "stress", "alpha", "ep", "vm"):
+        for k in ("pos", "vel", "vol", "F", "strain", "stress", "alpha", "ep", "vm", "alphadot"):
             arrs[f"b{b}_out_{k}"] = np.array(Bo[k], dtype=np.float64)
     mass, mom0, mom, force = case_out["grid_out"]
     arrs["grid_mass"] = np.array(mass)
@@ -613,6 +663,22 @@ def main(only=None):
                                            gap=0.0, speed=300.0)
     scenarios.apply_dirichlet(g, data)
     cases["taylor_mini_musl_j2_10"] = case_from_objects(g, s, MUSL(0.99), data, 10)
+
+    # 7. Johnson-Cook (USL) and Voce (MUSL 0.99) mini Taylor bars: the copper of the
+    #    reference's Taylor-bar driver in SI units, cellsize one grid cell
+    from jump_gb300.material import JohnsonCookMaterial, VoceMaterial
+    for kind in ("jc", "voce"):
+        g, s, alg, data = scenarios.taylor_bar(h=1e-3, radius=2e-3, length=6e-3, width=8e-3, height=10e-3,
+                                               gap=0.0, speed=300.0)
+        n = s[0].parCount
+        if kind == "jc":
+            s[0].mat = JohnsonCookMaterial(115e9, 0.31, 8940.0, 65e6, 356e6, 0.013, 0.37, 1e-3, 0.0, 0.0, 0.0,
+                                           1e-3, n)
+        else:
+            s[0].mat = VoceMaterial(115e9, 0.31, 8940.0, 200e6, 120e6, 20.0, 0.0, 0.0, 1e-3, n)
+        scenarios.apply_dirichlet(g, data)
+        algo = USL(1e-3 * float(s[0].mass[0])) if kind == "jc" else MUSL(0.99)
+        cases[f"taylor_mini_{kind}_10"] = case_from_objects(g, s, algo, data, 10)
 
     for name, cin in cases.items():
         if only and name not in only:
