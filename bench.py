@@ -50,6 +50,9 @@ BYTES = {
 # = 80 B, + P2G-2 grid share 3 doubles/node) and G2P-2 (reads x3 v3 V0 F9 eps6 alpha
 # ep6, writes x3 V F9 eps6 sigma6 alpha ep6 vm = 496 B, + 6 doubles/node gathered)
 BYTES_MUSL = {"p2g": 112 + 7, "g2p": 80 + 3 + 496 + 6, "step": 720}
+# Johnson-Cook, FP64: G2P reads x3 v3 V0 F9 eps6 sigma6 alpha alphadot (30 doubles)
+# and writes x3 v3 V F9 eps6 sigma6 alpha alphadot vm (31 doubles) -> 488 B
+BYTES_JC = {"p2g": 112 + 7, "g2p": 488 + 6, "step": 560}
 
 
 def launches_per_run(args, nbodies):
@@ -130,12 +133,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload(name: str):
+def workload(name: str, material: str = "j2"):
     from jump_gb300 import scenarios
     if name == "taylor_bar":
         g, s, alg, data = scenarios.taylor_bar()
-        cfg = {"workload": "taylor_bar_3d_j2", "particles": int(s[0].parCount), "grid_nodes": [65, 65, 161],
-               "h_m": 2.5e-4, "particles_per_cell": 8, "material": "J2 linear hardening",
+        label = "J2 linear hardening"
+        if material == "jc":
+            # the Johnson-Cook copper of the reference's Taylor-bar driver (Main_TaylorBar.jl:43-56), SI units
+            from jump_gb300.material import JohnsonCookMaterial
+            s[0].mat = JohnsonCookMaterial(115e9, 0.31, 8940.0, 65e6, 356e6, 0.0, 0.37, 1e-3, 0.0, 0.0, 0.0,
+                                           2.5e-4, s[0].parCount)
+            label = "Johnson-Cook (A 65 MPa, B 356 MPa, n 0.37, C 0)"
+        cfg = {"workload": f"taylor_bar_3d_{material}", "particles": int(s[0].parCount), "grid_nodes": [65, 65, 161],
+               "h_m": 2.5e-4, "particles_per_cell": 8, "material": label,
                "dt_s": data["dt"], "l2": "inputs larger than L2 (~230 MB resident)"}
     elif name == "two_disks":
         g, s, alg, data = scenarios.two_disks()
@@ -253,7 +263,7 @@ def run_reference(args):
     from jump_gb300.engine import Descriptors
     from oracle import oracle
     oracle.build()
-    g, s, alg, data, cfg = workload(args.workload)
+    g, s, alg, data, cfg = workload(args.workload, args.material)
     npart = sum(x.parCount for x in s)
     mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
                              **scheme_kw(args))
@@ -292,7 +302,7 @@ def run_ours(args):
     from jump_gb300.engine import Descriptors, MPMContext
     from jump_gb300.problem import step_times
 
-    g, s, alg, data, cfg = workload(args.workload)
+    g, s, alg, data, cfg = workload(args.workload, args.material)
     npart = sum(x.parCount for x in s)
     mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
                              precision=args.precision, sort_interval=args.sort_interval, **scheme_kw(args))
@@ -316,7 +326,8 @@ def run_ours(args):
     per = {k: v / nprof for k, v in st.items()}
     dom = max(("p2g", "g2p"), key=lambda k: per[k])
     peak, peak_kind = load_peaks()
-    table = BYTES_MUSL if args.algorithm == "musl" else BYTES[args.precision]
+    table = BYTES_MUSL if args.algorithm == "musl" else (BYTES_JC if args.material == "jc" and args.precision == "f64"
+                                                         else BYTES[args.precision])
     bts = table[dom] * npart
     achieved = bts / (per[dom] * 1e-3) / 1e9
     traffic = ncu_traffic(dom, args.precision)
@@ -626,6 +637,8 @@ def main():
     ap.add_argument("--algorithm", default="usl", choices=["usl", "musl"],
                     help="update scheme: USL (the headline) or MUSL (FLIP/PIC blend --alpha)")
     ap.add_argument("--alpha", type=float, default=1.0, help="MUSL FLIP/PIC blend")
+    ap.add_argument("--material", default="j2", choices=["j2", "jc"],
+                    help="Taylor bar material: J2 linear hardening (the headline) or Johnson-Cook")
     ap.add_argument("--sort-interval", type=int, default=0,
                     help="counting-sort particles by cell every N steps (0: never)")
     ap.add_argument("--workload", default="taylor_bar",

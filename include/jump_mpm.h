@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 4
+#define JUMP_MPM_ABI_VERSION 5
 
 /* status codes */
 #define MPM_OK               0
@@ -61,6 +61,13 @@ extern "C" {
 /* particle precision (grid accumulation is always FP64) */
 #define MPM_PREC_F64        0   /* every particle field and every operation in FP64 */
 #define MPM_PREC_F32        1   /* FP32 particle fields and arithmetic; FP64 nodes, det F, energies */
+
+/* Shape functions (the `basis` argument of solve_explicit_dynamics_2D/3D) */
+#define MPM_BASIS_LINEAR        0  /* LinearBasis: hat functions, 2^dim nodes (Basis.jl:219-251, 292-332) */
+#define MPM_BASIS_QUAD_BSPLINE  1  /* QuadBsplineBasis: modified quadratic B-splines, 3^dim nodes
+                                      (Basis.jl:374-592, Bsplines.jl:18-80); grids of >= 3 nodes per axis */
+#define MPM_BASIS_CUBIC_BSPLINE 2  /* CubicBsplineBasis: modified cubic B-splines, 4^dim nodes
+                                      (Basis.jl:594-820, Bsplines.jl:86-172); grids of >= 4 nodes per axis */
 
 /* Update scheme (the `alg` argument of solve_explicit_dynamics_2D/3D) */
 #define MPM_ALG_USL         0   /* USL(tolerance), SolveExplicitSolidMechanics2D.jl:335-585 */
@@ -131,7 +138,7 @@ typedef struct mpm_params {
   int32_t sort_interval;       /* re-sort particles by cell every N steps (0 = never) */
   int32_t flags;               /* reserved, 0 */
   int32_t algorithm;           /* MPM_ALG_USL or MPM_ALG_MUSL */
-  int32_t reserved;
+  int32_t basis;               /* MPM_BASIS_LINEAR, _QUAD_BSPLINE or _CUBIC_BSPLINE */
   double  alpha;               /* MUSL.alpha: FLIP/PIC blend, Algorithm.jl:38-40 (MUSL only) */
 } mpm_params;
 

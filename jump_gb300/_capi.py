@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-ABI_VERSION = 4  # JUMP_MPM_ABI_VERSION of the structures below
+ABI_VERSION = 5  # JUMP_MPM_ABI_VERSION of the structures below
 
 MPM_OK = 0
 MPM_ERR_ARG = 1
@@ -48,6 +48,10 @@ MPM_PREC_F32 = 1
 
 MPM_ALG_USL = 0
 MPM_ALG_MUSL = 1
+
+MPM_BASIS_LINEAR = 0
+MPM_BASIS_QUAD_BSPLINE = 1
+MPM_BASIS_CUBIC_BSPLINE = 2
 
 MPM_BATCH_PERSISTENT = 0
 MPM_BATCH_WIDE = 1
@@ -131,7 +135,7 @@ class Params(C.Structure):
         ("sort_interval", C.c_int32),
         ("flags", C.c_int32),
         ("algorithm", C.c_int32),
-        ("reserved", C.c_int32),
+        ("basis", C.c_int32),
         ("alpha", C.c_double),
     ]
 

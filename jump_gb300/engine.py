@@ -30,7 +30,7 @@ class Descriptors:
     """Descriptors plus the numpy arrays they point into (kept alive here)."""
 
     def __init__(self, grid, solids, tolerance=0.0, body_force=None, dt=0.0, precision="f64",
-                 contact=False, friction=0.0, sort_interval=0, algorithm="usl", alpha=1.0):
+                 contact=False, friction=0.0, sort_interval=0, algorithm="usl", alpha=1.0, basis="linear"):
         d = grid.dim
         self.dim = d
         self._keep = []
@@ -101,6 +101,8 @@ class Descriptors:
         p.flags = 0
         p.algorithm = {"usl": _capi.MPM_ALG_USL, "musl": _capi.MPM_ALG_MUSL}[algorithm]
         p.alpha = float(alpha)
+        p.basis = {"linear": _capi.MPM_BASIS_LINEAR, "quad": _capi.MPM_BASIS_QUAD_BSPLINE,
+                   "cubic": _capi.MPM_BASIS_CUBIC_BSPLINE}[basis]
         self.params = p
 
 

@@ -113,6 +113,7 @@ struct Grid {
   std::vector<double> mass;         // 1 per node
   std::vector<double> momentum0, momentum, force;  // D per node
   std::vector<int64_t> fixed;       // D per node
+  int basis = MPM_BASIS_LINEAR;
 };
 
 template <int D>
@@ -178,6 +179,125 @@ bool shape(const Grid<D>& g, const double* xp, int64_t* near, double* N, double*
     }
   }
   return true;
+}
+
+// Modified quadratic and cubic B-splines of the normalised distance r and
+// their derivatives in r (Bsplines.jl:18-172): type 1 at the first and last
+// node of an axis, 2 at the second, 4 at the second last, 3 elsewhere.
+inline void quad_bspline(int type, double r, double& N, double& dN) {
+  N = 0.;
+  dN = 0.;
+  if (type == 1) {
+    if (r < -1.5 || r > 1.5) return;
+    if (r >= -1.5 && r <= -0.5) { N = 0.5 * r * r + 1.5 * r + 1.125; dN = r + 1.5; }
+    else if (r <= 0.) { N = 1. + r; dN = 1.; }
+    else if (r <= 0.5) { N = 1. - r; dN = -1.; }
+    else { N = 0.5 * r * r - 1.5 * r + 1.125; dN = r - 1.5; }
+  } else if (type == 2) {
+    if (r < -1.0 || r > 1.5) return;
+    if (r >= -1. && r <= -0.5) { N = 1. + r; dN = 1.; }
+    else if (r <= 0.5) { N = -r * r + 0.75; dN = -2 * r; }
+    else { N = 0.5 * r * r - 1.5 * r + 1.125; dN = r - 1.5; }
+  } else if (type == 3) {
+    if (r < -1.5 || r > 1.5) return;
+    if (r >= -1.5 && r <= -0.5) { N = 0.5 * r * r + 1.5 * r + 1.125; dN = r + 1.5; }
+    else if (r <= 0.5) { N = -r * r + 0.75; dN = -2 * r; }
+    else { N = 0.5 * r * r - 1.5 * r + 1.125; dN = r - 1.5; }
+  } else {
+    if (r < -1.5 || r > 1.) return;
+    if (r >= -1.5 && r <= -0.5) { N = 0.5 * r * r + 1.5 * r + 1.125; dN = r + 1.5; }
+    else if (r <= 0.5) { N = -r * r + 0.75; dN = -2 * r; }
+    else { N = 1. - r; dN = -1.; }
+  }
+}
+
+inline void cubic_bspline(int type, double r, double& N, double& dN) {
+  N = 0.;
+  dN = 0.;
+  const double r2 = r * r;
+  if (type == 1) {
+    if (r < -2. || r > 2.) return;
+    if (r >= -2.0 && r <= -1.0) { N = 0.16666666666666666 * r * r2 + r2 + 2 * r + 1.3333333333333333; dN = 0.5 * r2 + 2 * r + 2.; }
+    else if (-1 <= r && r <= 0.) { N = -0.16666666666666666 * r * r2 + r + 1; dN = -0.5 * r2 + 1.; }
+    else if (0 <= r && r <= 1.0) { N = 0.16666666666666666 * r * r2 - r + 1; dN = 0.5 * r2 - 1.0; }
+    else { N = -0.16666666666666666 * r * r2 + r2 - 2 * r + 1.3333333333333333; dN = -0.5 * r2 + 2 * r - 2.; }
+  } else if (type == 2) {
+    if (r < -1. || r > 2.) return;
+    if (r >= -1.0 && r <= 0.) { N = -0.3333333333333333 * r * r2 - r2 + 0.6666666666666666; dN = -r2 - 2 * r; }
+    else if (0. <= r && r <= 1.) { N = 0.5 * r * r2 - r2 + 0.6666666666666666; dN = 1.5 * r2 - 2 * r; }
+    else if (1 <= r && r <= 2.0) { N = -0.16666666666666666 * r * r2 + r2 - 2 * r + 1.3333333333333333; dN = -0.5 * r2 + 2 * r - 2; }
+  } else if (type == 3) {
+    if (r < -2. || r > 2.) return;
+    if (r >= -2.0 && r <= -1.0) { N = 0.16666666666666666 * r * r2 + r2 + 2 * r + 1.3333333333333333; dN = 0.5 * r2 + 2 * r + 2; }
+    else if (-1. <= r && r <= 0.) { N = -0.5 * r * r2 - r2 + 0.6666666666666666; dN = -1.5 * r2 - 2 * r; }
+    else if (0 <= r && r <= 1.0) { N = 0.5 * r * r2 - r2 + 0.6666666666666666; dN = 1.5 * r2 - 2 * r; }
+    else if (1. <= r && r <= 2.0) { N = -0.16666666666666666 * r * r2 + r2 - 2 * r + 1.3333333333333333; dN = -0.5 * r2 + 2 * r - 2; }
+  } else {
+    if (r < -2. || r > 1.) return;
+    if (r >= -2.0 && r <= -1.0) { N = 0.16666666666666666 * r * r2 + r2 + 2 * r + 1.3333333333333333; dN = 0.5 * r2 + 2 * r + 2; }
+    else if (-1. <= r && r <= 0.) { N = -0.5 * r * r2 - r2 + 0.6666666666666666; dN = -1.5 * r2 - 2 * r; }
+    else if (0 <= r && r <= 1.0) { N = 0.3333333333333333 * r * r2 - r2 + 0.6666666667; dN = r2 - 2 * r; }
+  }
+}
+
+constexpr int kMaxSupport = 64;
+
+// getShapeAndGradient for the B-spline bases (Basis.jl:374-592 quadratic,
+// 594-820 cubic): per axis the near nodes, then the tensor product in the
+// reference's loop order.  As written: the 3D quadratic basis measures the
+// particle from the origin (numx = xp*dxI), and every B-spline basis measures
+// y and z from (jd-1)*dy, (kd-1)*dz rather than from the grid's minimum.
+template <int D>
+int bspline_support(const Grid<D>& g, const double* xp, int64_t* near, double* N, double* dN) {
+  const int K = g.basis == MPM_BASIS_QUAD_BSPLINE ? 3 : 4;
+  int64_t f1[3];
+  double Nv[3][4], dNv[3][4];
+  for (int a = 0; a < D; ++a) {
+    const int64_t nn = g.nn[a];
+    const double num = (K == 3 && D == 3) ? xp[a] * g.dxI[a] : (xp[a] - g.xmin[a]) * g.dxI[a];
+    const double rem = num - std::floor(num);
+    const double fb = std::floor(num + 1.);
+    if (!(fb >= 1.0) || !(fb <= double(nn - 1))) return 0;
+    const int64_t ib = int64_t(fb);
+    if (K == 3) f1[a] = ib == 1 ? ib : (ib == nn - 1 ? ib - 1 : (rem < 0.5 ? ib - 1 : ib));
+    else f1[a] = ib == 1 ? 1 : (ib == nn - 1 ? ib - 2 : ib - 1);
+    for (int i = 0; i < K; ++i) {
+      const int64_t id = f1[a] + i;
+      const double r = a == 0 ? (xp[0] - g.pos[D * (id - 1)]) * g.dxI[0] : (xp[a] - double(id - 1) * g.dx[a]) * g.dxI[a];
+      const int type = (id == 1 || id == nn) ? 1 : (id == 2 ? 2 : (id == nn - 1 ? 4 : 3));
+      if (K == 3) quad_bspline(type, r, Nv[a][i], dNv[a][i]);
+      else cubic_bspline(type, r, Nv[a][i], dNv[a][i]);
+    }
+  }
+  int q = 0;
+  for (int i = 0; i < K; ++i)
+    for (int j = 0; j < K; ++j) {
+      if (D == 2) {
+        near[q] = (f1[0] + i - 1) + g.nn[0] * (f1[1] + j - 1);
+        N[q] = Nv[0][i] * Nv[1][j];
+        dN[D * q] = dNv[0][i] * g.dxI[0] * Nv[1][j];
+        dN[D * q + 1] = dNv[1][j] * g.dxI[1] * Nv[0][i];
+        ++q;
+      } else {
+        for (int k = 0; k < K; ++k) {
+          near[q] = (f1[0] + i - 1) + g.nn[0] * (f1[1] + j - 1) + g.nodeCountXY * (f1[D - 1] + k - 1);
+          N[q] = Nv[0][i] * Nv[1][j] * Nv[D - 1][k];
+          dN[D * q] = dNv[0][i] * g.dxI[0] * Nv[1][j] * Nv[D - 1][k];
+          dN[D * q + 1] = dNv[1][j] * g.dxI[1] * Nv[0][i] * Nv[D - 1][k];
+          dN[D * q + D - 1] = dNv[D - 1][k] * g.dxI[D - 1] * Nv[0][i] * Nv[1][j];
+          ++q;
+        }
+      }
+    }
+  return q;
+}
+
+// nodes, values and gradients of particle position xp for the grid's basis;
+// 0 when its cell lies outside the grid
+template <int D>
+int support(const Grid<D>& g, const double* xp, int64_t* near, double* N, double* dN) {
+  if (g.basis != MPM_BASIS_LINEAR) return bspline_support<D>(g, xp, near, N, dN);
+  return shape<D>(g, xp, near, N, dN) ? (D == 2 ? 4 : 8) : 0;
 }
 
 // 2x2 / 3x3 helpers on column-major storage: M[i + D*j] = M_ij (0-based).
@@ -383,10 +503,10 @@ void update_stress(const Material& mat, double lambda, double mu, double kappa, 
 template <int D>
 inline void p2g_particle(const Grid<D>& g, const Body<D>& b, int64_t ip, const double* body,
                          double* mass, double* mom0, double* force, double* normal, int* status) {
-  constexpr int S = (D == 2) ? 4 : 8;
-  int64_t near[S];
-  double N[S], dN[S * D];
-  if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) {
+  int64_t near[kMaxSupport];
+  double N[kMaxSupport], dN[kMaxSupport * D];
+  const int S = support<D>(g, &b.pos[D * ip], near, N, dN);
+  if (S == 0) {
     *status = MPM_ERR_OUT_OF_GRID;
     return;
   }
@@ -422,10 +542,10 @@ template <int D>
 inline void g2p_particle(const Grid<D>& g, Body<D>& b, int64_t ip, double dt, double tol,
                          const double* mass, const double* mom0, const double* mom, int velmode,
                          int* status) {
-  constexpr int S = (D == 2) ? 4 : 8;
-  int64_t near[S];
-  double N[S], dN[S * D];
-  if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) {
+  int64_t near[kMaxSupport];
+  double N[kMaxSupport], dN[kMaxSupport * D];
+  const int S = support<D>(g, &b.pos[D * ip], near, N, dN);
+  if (S == 0) {
     *status = MPM_ERR_OUT_OF_GRID;
     return;
   }
@@ -519,17 +639,22 @@ void p2g_bodies(Ctx<D>& c, const std::vector<int>& which, double* mass, double* 
     return;
   }
 #ifdef _OPENMP
-  // slabs of two cells along the last axis; even slabs, then odd slabs
+  // slabs of K cells along the last axis (K nodes per axis in a particle's
+  // support), keyed by the support's first node; even slabs, then odd slabs,
+  // so that no two particles of one pass share a node
   const int ax = D - 1;
-  int64_t ncell = c.g.nn[ax] - 1;
-  int64_t nslab = (ncell + 1) / 2;
+  const int64_t K = c.g.basis == MPM_BASIS_LINEAR ? 2 : (c.g.basis == MPM_BASIS_QUAD_BSPLINE ? 3 : 4);
+  const int64_t stride = D == 3 ? c.g.nodeCountXY : c.g.nn[0];
+  int64_t nslab = (c.g.nn[ax] + K - 1) / K;
   std::vector<std::vector<std::pair<int, int64_t>>> slabs(nslab);
+  int64_t near[kMaxSupport];
+  double Nw[kMaxSupport], dNw[kMaxSupport * D];
   for (int s : which) {
     const Body<D>& b = c.bodies[s];
     for (int64_t ip = 0; ip < b.n; ++ip) {
-      double t = std::floor((b.pos[D * ip + ax] - c.g.xmin[ax]) * c.g.dxI[ax] + 1.0);
-      int64_t k = (t >= 1.0 && t <= double(ncell)) ? int64_t(t) - 1 : 0;
-      slabs[k / 2].push_back({s, ip});
+      const int S = support<D>(c.g, &b.pos[D * ip], near, Nw, dNw);
+      const int64_t k = S > 0 ? near[0] / stride : 0;
+      slabs[k / K].push_back({s, ip});
     }
   }
   int st = MPM_OK;
@@ -602,7 +727,6 @@ template <int D>
 void step_musl_lumped(Ctx<D>& c) {
   Grid<D>& g = c.g;
   const double dt = c.p.dt, alpha = c.p.alpha;
-  constexpr int S = (D == 2) ? 4 : 8;
   zero<D>(g.mass);
   zero<D>(g.momentum0);
   zero<D>(c.mom2);
@@ -623,11 +747,12 @@ void step_musl_lumped(Ctx<D>& c) {
     for (int a = 0; a < D; ++a) g.momentum[D * i + a] = g.momentum0[D * i + a] + g.force[D * i + a] * dt;
   bcs();
   // grid to particle 1 and particle to grid 2 (:113-139), in particle order
-  int64_t near[S];
-  double N[S], dN[S * D];
+  int64_t near[kMaxSupport];
+  double N[kMaxSupport], dN[kMaxSupport * D];
   for (auto& b : c.bodies)
     for (int64_t ip = 0; ip < b.n; ++ip) {
-      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) {
+      const int S = support<D>(g, &b.pos[D * ip], near, N, dN);
+      if (S == 0) {
         c.status = MPM_ERR_OUT_OF_GRID;
         continue;
       }
@@ -652,7 +777,8 @@ void step_musl_lumped(Ctx<D>& c) {
   // particle to grid 2 / kinematics (:162-204)
   for (auto& b : c.bodies)
     for (int64_t ip = 0; ip < b.n; ++ip) {
-      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) continue;
+      const int S = support<D>(g, &b.pos[D * ip], near, N, dN);
+      if (S == 0) continue;
       double L[D * D], xxp[D];
       for (int q = 0; q < D * D; ++q) L[q] = 0.;
       for (int a = 0; a < D; ++a) xxp[a] = b.pos[D * ip + a];
@@ -713,20 +839,23 @@ inline void band_solve(const std::vector<double>& Lb, int64_t n, int64_t w, cons
 // rounding).  The Dirichlet update of nodalMomentum that follows is never read by the
 // particle updates, so fixed nodes do not constrain this solver; as written.
 void step_musl_consistent(Ctx<2>& c) {
-  constexpr int D = 2, S = 4;
+  constexpr int D = 2;
   Grid<2>& g = c.g;
   const double dt = c.p.dt, alpha = c.p.alpha;
-  const int64_t n = g.nodeCount, w = g.nn[0] + 1;
+  // nodes of one particle's support differ by at most K-1 per axis
+  const int64_t K = g.basis == MPM_BASIS_LINEAR ? 2 : (g.basis == MPM_BASIS_QUAD_BSPLINE ? 3 : 4);
+  const int64_t n = g.nodeCount, w = (K - 1) * (g.nn[0] + 1);
   zero<D>(g.mass);
   zero<D>(g.momentum0);
   zero<D>(g.force);
   std::vector<double> Mb(static_cast<size_t>(n * (w + 1)), 0.0);
-  int64_t near[S];
-  double N[S], dN[S * D];
+  int64_t near[kMaxSupport];
+  double N[kMaxSupport], dN[kMaxSupport * D];
   const double* body = c.p.body_force;
   for (auto& b : c.bodies)
     for (int64_t ip = 0; ip < b.n; ++ip) {
-      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) {
+      const int S = support<D>(g, &b.pos[D * ip], near, N, dN);
+      if (S == 0) {
         c.status = MPM_ERR_OUT_OF_GRID;
         continue;
       }
@@ -778,7 +907,8 @@ void step_musl_consistent(Ctx<2>& c) {
   // grid to particle 1: velocities (:198-224)
   for (auto& b : c.bodies)
     for (int64_t ip = 0; ip < b.n; ++ip) {
-      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) continue;
+      const int S = support<D>(g, &b.pos[D * ip], near, N, dN);
+      if (S == 0) continue;
       double vacc[D] = {0., 0.};
       for (int i = 0; i < S; ++i) {
         const int64_t in = near[i];
@@ -791,7 +921,8 @@ void step_musl_consistent(Ctx<2>& c) {
   // particle update 2: positions, gradient, F, stress (:245-290)
   for (auto& b : c.bodies)
     for (int64_t ip = 0; ip < b.n; ++ip) {
-      if (!shape<D>(g, &b.pos[D * ip], near, N, dN)) continue;
+      const int S = support<D>(g, &b.pos[D * ip], near, N, dN);
+      if (S == 0) continue;
       double L[D * D] = {0., 0., 0., 0.}, xxp[D];
       for (int a = 0; a < D; ++a) xxp[a] = b.pos[D * ip + a];
       for (int i = 0; i < S; ++i) {
@@ -896,6 +1027,7 @@ int create(const mpm_grid_desc* gd, const mpm_body_desc* bd, int nb, const mpm_p
   Ctx<D>* c = new Ctx<D>();
   c->p = *p;
   Grid<D>& g = c->g;
+  g.basis = p->basis;
   for (int a = 0; a < D; ++a) {
     g.xmin[a] = gd->xmin[a];
     g.nn[a] = gd->nodes[a];
@@ -1060,6 +1192,12 @@ int oracle_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_
   if (grid->dim != 2 && grid->dim != 3) return fail(MPM_ERR_ARG, "oracle_create: dim must be 2 or 3");
   for (int a = 0; a < grid->dim; ++a)
     if (grid->nodes[a] < 2) return fail(MPM_ERR_ARG, "oracle_create: need >= 2 nodes per axis");
+  if (params && params->basis != MPM_BASIS_LINEAR && params->basis != MPM_BASIS_QUAD_BSPLINE &&
+      params->basis != MPM_BASIS_CUBIC_BSPLINE)
+    return fail(MPM_ERR_ARG, "oracle_create: unknown basis");
+  for (int a = 0; params && a < grid->dim; ++a)
+    if (grid->nodes[a] < (params->basis == MPM_BASIS_CUBIC_BSPLINE ? 4 : 3) && params->basis != MPM_BASIS_LINEAR)
+      return fail(MPM_ERR_ARG, "oracle_create: B-spline bases need 3 (quadratic) or 4 (cubic) nodes per axis");
   Handle* h = new Handle{grid->dim, nullptr};
   if (grid->dim == 2) {
     Ctx<2>* c;

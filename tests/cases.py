@@ -72,10 +72,14 @@ def load_golden(name):
 
 
 def golden_kw(z):
-    """Descriptor arguments of a fixture's update scheme (USL when it names none)."""
+    """Descriptor arguments of a fixture's update scheme and basis (USL and the
+    linear basis when it names none)."""
+    kw = {}
     if "meta_alg" in z and int(z["meta_alg"]) == 1:
-        return {"algorithm": "musl", "alpha": float(z["meta_alpha"])}
-    return {}
+        kw.update(algorithm="musl", alpha=float(z["meta_alpha"]))
+    if "meta_basis" in z and int(z["meta_basis"]) != 0:
+        kw["basis"] = ("linear", "quad", "cubic")[int(z["meta_basis"])]
+    return kw
 
 
 def golden_expected(z, b):

@@ -34,8 +34,92 @@ def sign(x):
     return 1.0 if x > 0 else (-1.0 if x < 0 else 0.0)
 
 
+def quad_bs(t, r):
+    """Bsplines.jl:18-80: modified quadratic B-spline of type t, value and d/dr."""
+    if t == 1:
+        if r < -1.5 or r > 1.5:
+            return 0.0, 0.0
+        if -1.5 <= r <= -0.5:
+            return 0.5 * r * r + 1.5 * r + 1.125, r + 1.5
+        if r <= 0.0:
+            return 1.0 + r, 1.0
+        if r <= 0.5:
+            return 1.0 - r, -1.0
+        return 0.5 * r * r - 1.5 * r + 1.125, r - 1.5
+    if t == 2:
+        if r < -1.0 or r > 1.5:
+            return 0.0, 0.0
+        if -1.0 <= r <= -0.5:
+            return 1.0 + r, 1.0
+        if r <= 0.5:
+            return -r * r + 0.75, -2 * r
+        return 0.5 * r * r - 1.5 * r + 1.125, r - 1.5
+    if t == 3:
+        if r < -1.5 or r > 1.5:
+            return 0.0, 0.0
+        if -1.5 <= r <= -0.5:
+            return 0.5 * r * r + 1.5 * r + 1.125, r + 1.5
+        if r <= 0.5:
+            return -r * r + 0.75, -2 * r
+        return 0.5 * r * r - 1.5 * r + 1.125, r - 1.5
+    if r < -1.5 or r > 1.0:
+        return 0.0, 0.0
+    if -1.5 <= r <= -0.5:
+        return 0.5 * r * r + 1.5 * r + 1.125, r + 1.5
+    if r <= 0.5:
+        return -r * r + 0.75, -2 * r
+    return 1.0 - r, -1.0
+
+
+def cubic_bs(t, r):
+    """Bsplines.jl:86-172: modified cubic B-spline of type t, value and d/dr."""
+    r2 = r * r
+    if t == 1:
+        if r < -2.0 or r > 2.0:
+            return 0.0, 0.0
+        if -2.0 <= r <= -1.0:
+            return 0.16666666666666666 * r * r2 + r2 + 2 * r + 1.3333333333333333, 0.5 * r2 + 2 * r + 2.0
+        if -1 <= r <= 0.0:
+            return -0.16666666666666666 * r * r2 + r + 1, -0.5 * r2 + 1.0
+        if 0 <= r <= 1.0:
+            return 0.16666666666666666 * r * r2 - r + 1, 0.5 * r2 - 1.0
+        return -0.16666666666666666 * r * r2 + r2 - 2 * r + 1.3333333333333333, -0.5 * r2 + 2 * r - 2.0
+    if t == 2:
+        if r < -1.0 or r > 2.0:
+            return 0.0, 0.0
+        if -1.0 <= r <= 0.0:
+            return -0.3333333333333333 * r * r2 - r2 + 0.6666666666666666, -r2 - 2 * r
+        if 0.0 <= r <= 1.0:
+            return 0.5 * r * r2 - r2 + 0.6666666666666666, 1.5 * r2 - 2 * r
+        if 1 <= r <= 2.0:
+            return -0.16666666666666666 * r * r2 + r2 - 2 * r + 1.3333333333333333, -0.5 * r2 + 2 * r - 2
+        return 0.0, 0.0
+    if t == 3:
+        if r < -2.0 or r > 2.0:
+            return 0.0, 0.0
+        if -2.0 <= r <= -1.0:
+            return 0.16666666666666666 * r * r2 + r2 + 2 * r + 1.3333333333333333, 0.5 * r2 + 2 * r + 2
+        if -1.0 <= r <= 0.0:
+            return -0.5 * r * r2 - r2 + 0.6666666666666666, -1.5 * r2 - 2 * r
+        if 0 <= r <= 1.0:
+            return 0.5 * r * r2 - r2 + 0.6666666666666666, 1.5 * r2 - 2 * r
+        if 1.0 <= r <= 2.0:
+            return -0.16666666666666666 * r * r2 + r2 - 2 * r + 1.3333333333333333, -0.5 * r2 + 2 * r - 2
+        return 0.0, 0.0
+    if r < -2.0 or r > 1.0:
+        return 0.0, 0.0
+    if -2.0 <= r <= -1.0:
+        return 0.16666666666666666 * r * r2 + r2 + 2 * r + 1.3333333333333333, 0.5 * r2 + 2 * r + 2
+    if -1.0 <= r <= 0.0:
+        return -0.5 * r * r2 - r2 + 0.6666666666666666, -1.5 * r2 - 2 * r
+    if 0 <= r <= 1.0:
+        return 0.3333333333333333 * r * r2 - r2 + 0.6666666667, r2 - 2 * r
+    return 0.0, 0.0
+
+
 class PyGrid:
-    def __init__(self, dim, xmin, xmax, nodes):
+    def __init__(self, dim, xmin, xmax, nodes, basis=0):
+        self.basis = basis  # 0 linear, 1 quadratic B-spline, 2 cubic B-spline
         self.dim = dim
         self.xmin = list(xmin)
         self.n = list(nodes)
@@ -57,6 +141,8 @@ class PyGrid:
 
     def shape(self, xp):
         """getShapeAndGradient: (nearPoints 0-based, funcs, ders)."""
+        if self.basis:
+            return self.bspline_shape(xp)
         idx = []
         for a in range(self.dim):
             idx.append(math.floor((xp[a] - self.xmin[a]) * self.dxI[a] + 1.0))
@@ -89,6 +175,64 @@ class PyGrid:
                 ders.append((-Ny * Nz * sign(xip) * self.dxI[0],
                              -Nx * Nz * sign(yip) * self.dxI[1],
                              -Nx * Ny * sign(zip_) * self.dxI[2]))
+        return near, funcs, ders
+
+    def bspline_shape(self, xp):
+        """Basis.jl:374-820: near nodes per axis (1-based ids), boundary-typed 1D
+        B-splines, tensor product in the reference's i, j(, k) loop order.  The
+        3D quadratic basis measures x from the origin; y and z are measured
+        from (id-1)*dy and (id-1)*dz for both bases."""
+        d, K = self.dim, (3 if self.basis == 1 else 4)
+        fn = quad_bs if K == 3 else cubic_bs
+        per_axis = []
+        for a in range(d):
+            n = self.n[a]
+            num = xp[a] * self.dxI[a] if (K == 3 and d == 3) else (xp[a] - self.xmin[a]) * self.dxI[a]
+            rem = num - math.floor(num)
+            ib = math.floor(num + 1.0)
+            if K == 3:
+                if ib == 1:
+                    ids = [ib, ib + 1, ib + 2]
+                elif ib == n - 1:
+                    ids = [ib - 1, ib, ib + 1]
+                elif rem < 0.5:
+                    ids = [ib - 1, ib, ib + 1]
+                else:
+                    ids = [ib, ib + 1, ib + 2]
+            else:
+                if ib == 1:
+                    ids = [1, 2, 3, 4]
+                elif ib == n - 1:
+                    ids = [ib - 2, ib - 1, ib, ib + 1]
+                else:
+                    ids = [ib - 1, ib, ib + 1, ib + 2]
+            vals = []
+            for i in ids:
+                if a == 0:
+                    r = (xp[0] - self.pos[i - 1][0]) * self.dxI[0]
+                else:
+                    r = (xp[a] - (i - 1) * self.dx[a]) * self.dxI[a]
+                t = 1 if (i == 1 or i == n) else (2 if i == 2 else (4 if i == n - 1 else 3))
+                vals.append(fn(t, r))
+            per_axis.append((ids, vals))
+        near, funcs, ders = [], [], []
+        (ix, vx), (iy, vy) = per_axis[0], per_axis[1]
+        for i in range(K):
+            Nx, dNx = vx[i]
+            for j in range(K):
+                Ny, dNy = vy[j]
+                if d == 2:
+                    near.append(self.n[0] * (iy[j] - 1) + ix[i] - 1)
+                    funcs.append(Nx * Ny)
+                    ders.append((dNx * self.dxI[0] * Ny, dNy * self.dxI[1] * Nx))
+                else:
+                    iz, vz = per_axis[2]
+                    for k in range(K):
+                        Nz, dNz = vz[k]
+                        near.append(self.nxy * (iz[k] - 1) + self.n[0] * (iy[j] - 1) + ix[i] - 1)
+                        funcs.append(Nx * Ny * Nz)
+                        ders.append((dNx * self.dxI[0] * Ny * Nz, dNy * self.dxI[1] * Nx * Nz,
+                                     dNz * self.dxI[2] * Nx * Ny))
         return near, funcs, ders
 
 
@@ -253,7 +397,7 @@ def stress_update(mat, d, sig, eps, F, J, state):
 def usl_steps(case, nsteps):
     """Run nsteps of the USL loop on a case dict (lists of floats); mutates it."""
     d = case["dim"]
-    G = PyGrid(d, case["xmin"], case["xmax"], case["nodes"])
+    G = PyGrid(d, case["xmin"], case["xmax"], case["nodes"], case.get("basis", 0))
     fixed = case["fixed"]  # list of d-tuples per node
     dt, tol, body = case["dt"], case["tol"], case["gravity"][:d]
     for _ in range(nsteps):
@@ -394,7 +538,7 @@ def musl_steps(case, nsteps):
     massless rows 1 on the diagonal; solved here by banded Cholesky), 3D with
     lumped mass and no body force (SolveExplicitSolidMechanics3D.jl:14-223)."""
     d = case["dim"]
-    G = PyGrid(d, case["xmin"], case["xmax"], case["nodes"])
+    G = PyGrid(d, case["xmin"], case["xmax"], case["nodes"], case.get("basis", 0))
     fixed = case["fixed"]
     dt, alpha, body = case["dt"], case["alpha"], case["gravity"][:d]
     n = G.count
@@ -402,7 +546,7 @@ def musl_steps(case, nsteps):
         mass = [0.0] * n
         mom0 = [[0.0] * d for _ in range(n)]
         force = [[0.0] * d for _ in range(n)]
-        w = case["nodes"][0] + 1
+        w = (2 + case.get("basis", 0) - 1) * (case["nodes"][0] + 1)  # (K - 1)(nx + 1)
         band = [[0.0] * (w + 1) for _ in range(n)] if d == 2 else None
         for B in case["bodies"]:
             for ip in range(B["n"]):
@@ -496,7 +640,7 @@ def musl_steps(case, nsteps):
 
 
 # ---------------------------------------------------------------------------
-def case_from_objects(grid, solids, alg, data, nsteps):
+def case_from_objects(grid, solids, alg, data, nsteps, basis=0):
     from jump_gb300.engine import colmajor
     from jump_gb300.material import ElastoPlasticMaterial
     d = grid.dim
@@ -540,7 +684,8 @@ def case_from_objects(grid, solids, alg, data, nsteps):
     musl = hasattr(alg, "alpha")
     return {"dim": d, "xmin": xmin, "xmax": xmax, "nodes": nodes, "fixed": fixed, "dt": float(data["dt"]),
             "tol": 0.0 if musl else float(alg.tolerance), "gravity": list(map(float, g)), "bodies": bodies,
-            "nsteps": nsteps, "alg": 1 if musl else 0, "alpha": float(alg.alpha) if musl else 1.0}
+            "nsteps": nsteps, "alg": 1 if musl else 0, "alpha": float(alg.alpha) if musl else 1.0,
+            "basis": basis}
 
 
 def save_case(name, case_in, case_out):
@@ -557,6 +702,7 @@ def save_case(name, case_in, case_out):
     arrs["meta_nsteps"] = np.array(case_in["nsteps"])
     arrs["meta_nbodies"] = np.array(len(case_in["bodies"]))
     arrs["meta_alg"] = np.array(case_in["alg"])
+    arrs["meta_basis"] = np.array(case_in.get("basis", 0))
     arrs["meta_alpha"] = np.array(case_in["alpha"])
     for b, (Bi, Bo) in enumerate(zip(case_in["bodies"], case_out["bodies"])):
         m = Bi["mat"]
@@ -679,6 +825,46 @@ def main(only=None):
         scenarios.apply_dirichlet(g, data)
         algo = USL(1e-3 * float(s[0].mass[0])) if kind == "jc" else MUSL(0.99)
         cases[f"taylor_mini_{kind}_10"] = case_from_objects(g, s, algo, data, 10)
+
+    # 8. B-spline bases: the two-disk collision with quadratic B-splines and USL
+    #    (Main_TwoDisks.jl:53, 116); 3D neo-Hookean spheres with cubic B-splines
+    #    and USL; a 2D neo-Hookean beam under gravity with cubic B-splines and
+    #    MUSL (consistent mass, Main_VibratingBeam.jl:103); the J2 mini Taylor
+    #    bar with quadratic B-splines and MUSL 0.99 (3D lumped)
+    g, s, alg, data = scenarios.two_disks(nodes=21, centers=touch, speed=0.3)
+    scenarios.apply_dirichlet(g, data)
+    cases["two_disks_quad_12"] = case_from_objects(g, s, alg, data, 12, basis=1)
+    g = Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, 9, 9, 9)
+    off = g.dx / 2
+    c1 = buildParticleForSphere([0.4, 0.4, 0.42], 0.14, off)
+    c2 = buildParticleForSphere([0.6, 0.6, 0.58], 0.14, off)
+    s1, s2 = Solid3D(c1, NeoHookeanMaterial(1e3, 0.3, 1000.0, len(c1))), \
+        Solid3D(c2, NeoHookeanMaterial(1e3, 0.3, 1000.0, len(c2)))
+    for so in (s1, s2):
+        so.mass *= off ** 3
+        so.volume[:] = off ** 3
+        so.volumeInitial[:] = off ** 3
+    assign_velocity(s1, [0.3, 0.3, 0.2])
+    assign_velocity(s2, [-0.3, -0.3, -0.2])
+    data = {"dt": 2e-3, "bodyforce": ConstantBodyForce3D([0.0, 0.0, -1.0]),
+            "dirichlet_grid": [("front", (0, 0, 1))]}
+    scenarios.apply_dirichlet(g, data)
+    cases["spheres_nh_cubic_8"] = case_from_objects(g, [s1, s2], USL(1e-9), data, 8, basis=2)
+    g = Grid2D(0.0, 1.0, 0.0, 1.0, 11, 11)
+    off = g.dx / 2
+    c = buildParticleForRectangle([0.4, 0.5], 0.6, 0.2, off)
+    so = Solid2D(c, NeoHookeanMaterial(1e4, 0.3, 1000.0, len(c)))
+    so.mass *= off * off
+    so.volume[:] = off * off
+    so.volumeInitial[:] = off * off
+    so.velocity[:, 1] = 2.0 * (so.pos[:, 0] - 0.4)  # rotating: the 2D MUSL ignores the clamp
+    data = {"dt": 1e-3, "bodyforce": ConstantBodyForce2D([0.0, -10.0]), "dirichlet_grid": [("left", (1, 1))]}
+    scenarios.apply_dirichlet(g, data)
+    cases["beam_nh_cubic_musl_10"] = case_from_objects(g, [so], MUSL(1.0), data, 10, basis=2)
+    g, s, alg, data = scenarios.taylor_bar(h=1e-3, radius=2e-3, length=6e-3, width=8e-3, height=10e-3,
+                                           gap=0.0, speed=300.0)
+    scenarios.apply_dirichlet(g, data)
+    cases["taylor_mini_quad_musl_8"] = case_from_objects(g, s, MUSL(0.99), data, 8, basis=1)
 
     for name, cin in cases.items():
         if only and name not in only:

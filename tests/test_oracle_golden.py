@@ -29,12 +29,14 @@ def test_oracle_matches_golden_bitwise(name, oracle_lib):
     np.testing.assert_array_equal(f, z["grid_force"])
 
 
-@pytest.mark.parametrize("name", ["two_disks_elastic_20", "taylor_mini_j2_6"])
+@pytest.mark.parametrize("name", ["two_disks_elastic_20", "taylor_mini_j2_6", "two_disks_quad_12",
+                                  "spheres_nh_cubic_8"])
 def test_oracle_threads_agree(name, oracle_lib):
-    """Slab-coloured parallel P2G re-associates node sums only (differences at rounding level)."""
+    """Slab-coloured parallel P2G re-associates node sums only (differences at rounding level);
+    slabs are as wide as a particle's support (2, 3 or 4 nodes)."""
     grid, solids, tol, bf, dt, nsteps, z = load_golden(name)
-    a = oracle_lib.OracleContext(descriptors(grid, solids, tol, bf, dt), threads=1)
-    b = oracle_lib.OracleContext(descriptors(grid, solids, tol, bf, dt), threads=4)
+    a = oracle_lib.OracleContext(descriptors(grid, solids, tol, bf, dt, **golden_kw(z)), threads=1)
+    b = oracle_lib.OracleContext(descriptors(grid, solids, tol, bf, dt, **golden_kw(z)), threads=4)
     a.step(nsteps)
     b.step(nsteps)
     for sa, sb in zip(a.download_all(), b.download_all()):
