@@ -29,15 +29,15 @@ class BasisType:
 
 
 class LinearBasis(BasisType):
-    """Linear hat functions (Basis.jl:39): the only basis of the accelerated path."""
+    """Linear hat functions (Basis.jl:39), 2 nodes per axis."""
 
 
 class QuadBsplineBasis(BasisType):
-    pass
+    """Modified quadratic B-splines, 3 nodes per axis (Basis.jl:374-592, Bsplines.jl:18-80)."""
 
 
 class CubicBsplineBasis(BasisType):
-    pass
+    """Modified cubic B-splines, 4 nodes per axis (Basis.jl:594-820, Bsplines.jl:86-172)."""
 
 
 class BodyForceType:

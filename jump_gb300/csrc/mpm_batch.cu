@@ -582,6 +582,7 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       dx[a] = (d.grid.xmax[a] - d.grid.xmin[a]) / (double(d.grid.nodes[a]) - 1.0);  // Grid.jl:105
       I.g.xmin[a] = d.grid.xmin[a];
       I.g.dxI[a] = 1.0 / dx[a];
+      I.g.dx[a] = dx[a];
       I.g.nn[a] = nn[a];
     }
     I.g.nx = nn[0];

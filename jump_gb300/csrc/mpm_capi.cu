@@ -266,22 +266,23 @@ void enqueue_musl(mpm_ctx* c, cudaEvent_t* ev) {
   else Launchers<3>::clear(c->stream, c->nd);
   cudaMemsetAsync(c->nd.bcount, 0, sizeof(uint32_t), c->stream);
   if (ev) cudaEventRecord(ev[0], c->stream);
+  const int basis = c->prm.basis;
   for (int b = 0; b < c->nb; ++b) {
-    if (D == 2) Launchers<2>::musl_p2g(c->stream, c->g, c->nd, c->part(b), c->prm.body_force, c->status);
-    else Launchers<3>::musl_p2g(c->stream, c->g, c->nd, c->part(b), c->prm.body_force, c->status);
+    if (D == 2) Launchers<2>::musl_p2g(c->stream, c->g, c->nd, c->part(b), c->prm.body_force, c->status, basis);
+    else Launchers<3>::musl_p2g(c->stream, c->g, c->nd, c->part(b), c->prm.body_force, c->status, basis);
   }
   if (ev) cudaEventRecord(ev[1], c->stream);
-  if (D == 2) Launchers<2>::musl_grid(c->stream, c->nd, c->cg, c->prm.dt, c->prm.alpha, c->status);
-  else Launchers<3>::musl_grid(c->stream, c->nd, c->cg, c->prm.dt, c->prm.alpha, c->status);
+  if (D == 2) Launchers<2>::musl_grid(c->stream, c->nd, c->cg, c->prm.dt, c->prm.alpha, c->status, basis);
+  else Launchers<3>::musl_grid(c->stream, c->nd, c->cg, c->prm.dt, c->prm.alpha, c->status, basis);
   if (ev) cudaEventRecord(ev[2], c->stream);
   for (int b = 0; b < c->nb; ++b) {
-    if (D == 2) Launchers<2>::musl_g2p1(c->stream, c->g, c->nd, c->part(b), c->prm.alpha, c->status);
-    else Launchers<3>::musl_g2p1(c->stream, c->g, c->nd, c->part(b), c->prm.alpha, c->status);
+    if (D == 2) Launchers<2>::musl_g2p1(c->stream, c->g, c->nd, c->part(b), c->prm.alpha, c->status, basis);
+    else Launchers<3>::musl_g2p1(c->stream, c->g, c->nd, c->part(b), c->prm.alpha, c->status, basis);
   }
   if (D == 3) Launchers<3>::musl_vg(c->stream, c->nd, c->prm.dt);
   for (int b = 0; b < c->nb; ++b) {
-    if (D == 2) Launchers<2>::musl_g2p2(c->stream, c->g, c->nd, c->part(b), c->mats[b], c->status);
-    else Launchers<3>::musl_g2p2(c->stream, c->g, c->nd, c->part(b), c->mats[b], c->status);
+    if (D == 2) Launchers<2>::musl_g2p2(c->stream, c->g, c->nd, c->part(b), c->mats[b], c->status, basis);
+    else Launchers<3>::musl_g2p2(c->stream, c->g, c->nd, c->part(b), c->mats[b], c->status, basis);
   }
   if (ev) cudaEventRecord(ev[3], c->stream);
 }
@@ -302,9 +303,16 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
   }
   cudaMemsetAsync(c->nd.bcount, 0, sizeof(uint32_t), c->stream);
   if (ev) cudaEventRecord(ev[0], c->stream);
+  const int basis = c->prm.basis;
   for (int b = 0; b < c->nb; ++b) {
-    if (D == 2) Launchers<2>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
-    else Launchers<3>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
+    if (basis != MPM_BASIS_LINEAR) {
+      if (D == 2) Launchers<2>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
+      else Launchers<3>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
+    } else if (D == 2) {
+      Launchers<2>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
+    } else {
+      Launchers<3>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
+    }
   }
   if (ev) cudaEventRecord(ev[1], c->stream);
   if (contact) {
@@ -321,8 +329,14 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
   }
   if (ev) cudaEventRecord(ev[2], c->stream);
   for (int b = 0; b < c->nb; ++b) {
-    if (D == 2) Launchers<2>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
-    else Launchers<3>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+    if (basis != MPM_BASIS_LINEAR) {
+      if (D == 2) Launchers<2>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
+      else Launchers<3>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
+    } else if (D == 2) {
+      Launchers<2>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+    } else {
+      Launchers<3>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+    }
   }
   if (ev) cudaEventRecord(ev[3], c->stream);
 }
@@ -371,6 +385,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     dx[a] = (gd->xmax[a] - gd->xmin[a]) / (double(gd->nodes[a]) - 1.0);
     c->g.xmin[a] = gd->xmin[a];
     c->g.dxI[a] = 1.0 / dx[a];
+    c->g.dx[a] = dx[a];
     c->g.nn[a] = nn[a];
   }
   c->g.nx = nn[0];
@@ -450,8 +465,10 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     }
   }
   if (prm->algorithm == MPM_ALG_MUSL) {
-    // 3D: p2 (D) | vg (D); 2D: mass stencil (9) | vg (D) | CG x, r, p, q of four right-hand sides
-    const size_t per = D == 3 ? size_t(2 * D) : size_t(9 + D + 16);
+    // 3D: p2 (D) | vg (D); 2D: mass stencil (W*W, W = 2K - 1 for K support nodes per axis) | vg (D) |
+    // CG x, r, p, q of four right-hand sides
+    const int W = 2 * basis_nodes(prm->basis) - 1;
+    const size_t per = D == 3 ? size_t(2 * D) : size_t(W * W + D + 16);
     CUDA_TRY(cudaMalloc(&c->muslbuf, size_t(Nn) * per * sizeof(double)));
     CUDA_TRY(cudaMemset(c->muslbuf, 0, size_t(Nn) * per * sizeof(double)));
     if (D == 3) {
@@ -459,8 +476,9 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
       c->nd.vg = c->muslbuf + Nn * D;
     } else {
       c->nd.mc = c->muslbuf;
-      c->nd.vg = c->muslbuf + Nn * 9;
-      double* v = c->muslbuf + Nn * (9 + D);
+      c->nd.nmc = W * W;
+      c->nd.vg = c->muslbuf + Nn * (W * W);
+      double* v = c->muslbuf + Nn * (W * W + D);
       for (int k = 0; k < 4; ++k) {
         c->cg.x[k] = v + Nn * (0 + k);
         c->cg.r[k] = v + Nn * (4 + k);
@@ -596,6 +614,12 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
   if (params->sort_interval < 0) return fail(MPM_ERR_ARG, "mpm_create: sort_interval < 0");
   if (params->algorithm != MPM_ALG_USL && params->algorithm != MPM_ALG_MUSL)
     return fail(MPM_ERR_ARG, "mpm_create: unknown algorithm");
+  if (params->basis != MPM_BASIS_LINEAR && params->basis != MPM_BASIS_QUAD_BSPLINE &&
+      params->basis != MPM_BASIS_CUBIC_BSPLINE)
+    return fail(MPM_ERR_ARG, "mpm_create: unknown basis");
+  for (int a = 0; a < grid->dim; ++a)
+    if (params->basis != MPM_BASIS_LINEAR && grid->nodes[a] < basis_nodes(params->basis))
+      return fail(MPM_ERR_ARG, "mpm_create: B-spline bases need 3 (quadratic) or 4 (cubic) nodes per axis");
   if (params->algorithm == MPM_ALG_MUSL && (params->precision != MPM_PREC_F64 || params->contact))
     return fail(MPM_ERR_UNSUPPORTED, "mpm_create: MUSL runs FP64 with one velocity field");
   if (!(params->dt > 0.0) || !std::isfinite(params->dt)) return fail(MPM_ERR_ARG, "mpm_create: dt must be > 0");
@@ -827,9 +851,10 @@ int mpm_profile_stages(mpm_ctx* c, int64_t nsteps, double* stage_ms) {
 int mpm_fwd_checkpointed(mpm_ctx* c, int64_t nsteps, int32_t every) {
   if (!c) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: null context");
   if (nsteps < 1 || every < 1) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: need nsteps >= 1, every >= 1");
-  if (c->f32 || c->prm.contact || c->prm.sort_interval > 0 || c->prm.algorithm != MPM_ALG_USL)
-    return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode needs USL, FP64 particles, one velocity "
-                                     "field and no sorting");
+  if (c->f32 || c->prm.contact || c->prm.sort_interval > 0 || c->prm.algorithm != MPM_ALG_USL ||
+      c->prm.basis != MPM_BASIS_LINEAR)
+    return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode needs USL with the linear basis, FP64 "
+                                     "particles, one velocity field and no sorting");
   for (const MatParams& m : c->mats)
     if (m.type != MPM_MAT_NEOHOOKEAN)
       return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode is built for neo-Hookean bodies");

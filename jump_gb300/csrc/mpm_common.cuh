@@ -65,6 +65,7 @@ struct MatParams {
 struct GridP {
   double xmin[3];
   double dxI[3];
+  double dx[3];        // node spacing (xmax - xmin)/(n - 1), Grid.jl:105-107
   int64_t nn[3];       // nodes per axis
   int64_t nx, nxy, nodeCount;
   const double* coord[3];  // node coordinate per axis (xmin + i*dx, Grid.jl:149-152)
@@ -95,6 +96,7 @@ struct NodeP {
   double* p2;
   double* vg;
   double* mc;
+  int nmc;               // entries of the mass stencil per node ((2K - 1)^2 for K support nodes per axis)
 };
 
 // 2D MUSL mass solve: CG vectors of the four right-hand sides (p0_x, p0_y,

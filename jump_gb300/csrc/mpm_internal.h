@@ -95,15 +95,27 @@ struct Launchers {
   // the consistent mass stencil; 3D: no body force); musl_grid: compaction + grid
   // update (3D lumped) or mass solve + node outputs (2D); musl_g2p1: velocity
   // blend (3D: + P2G-2); musl_vg: 3D gradient velocities; musl_g2p2: kinematics.
+  // basis: MPM_BASIS_* of the context (the 2D solve's stencil grows with it)
   static void musl_p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const double* grav,
-                       unsigned* status);
-  static void musl_grid(cudaStream_t s, const NodeP& nd, const CgP& cg, double dt, double alpha, unsigned* status);
+                       unsigned* status, int basis);
+  static void musl_grid(cudaStream_t s, const NodeP& nd, const CgP& cg, double dt, double alpha, unsigned* status,
+                        int basis);
   static void musl_g2p1(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, double alpha,
-                        unsigned* status);
+                        unsigned* status, int basis);
   static void musl_vg(cudaStream_t s, const NodeP& nd, double dt);
   static void musl_g2p2(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const MatParams& mp,
-                        unsigned* status);
+                        unsigned* status, int basis);
+  // USL over the quadratic / cubic B-spline bases (mpm_bspline.cuh)
+  static void bs_p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32, const double* grav,
+                     unsigned* status, int basis);
+  static void bs_g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32, const MatParams& mp,
+                     unsigned* status, int basis);
 };
+
+// nodes per axis of a particle's support
+inline int basis_nodes(int basis) {
+  return basis == MPM_BASIS_QUAD_BSPLINE ? 3 : (basis == MPM_BASIS_CUBIC_BSPLINE ? 4 : 2);
+}
 
 constexpr int kEnergyBlocks = 304;  // 2 x 152 SMs
 

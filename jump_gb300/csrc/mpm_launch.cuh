@@ -4,6 +4,9 @@
 #include "mpm_internal.h"
 #include "mpm_kernels.cuh"
 #include "mpm_musl.cuh"
+#include "mpm_bspline.cuh"
+
+#include <type_traits>
 
 namespace jmpm {
 
@@ -87,25 +90,67 @@ void Launchers<D>::clear(cudaStream_t s, const NodeP& nd) {
   clear_blocks_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd);
 }
 
+// f(std::integral_constant<int, MAT>) for a material type (Johnson-Cook and Voce in 3D only)
+template <int D, class Fn>
+static inline void with_material(int type, Fn&& f) {
+  switch (type) {
+    case MPM_MAT_ELASTIC: f(std::integral_constant<int, MPM_MAT_ELASTIC>{}); break;
+    case MPM_MAT_NEOHOOKEAN: f(std::integral_constant<int, MPM_MAT_NEOHOOKEAN>{}); break;
+    case MPM_MAT_JOHNSON_COOK:
+      if constexpr (D == 3) f(std::integral_constant<int, MPM_MAT_JOHNSON_COOK>{});
+      break;
+    case MPM_MAT_VOCE:
+      if constexpr (D == 3) f(std::integral_constant<int, MPM_MAT_VOCE>{});
+      break;
+    default: f(std::integral_constant<int, MPM_MAT_J2>{}); break;
+  }
+}
+
+// f(std::integral_constant<int, K>) for a B-spline basis (K = 3 or 4 nodes per axis)
+template <class Fn>
+static inline void with_bspline(int basis, Fn&& f) {
+  if (basis == MPM_BASIS_QUAD_BSPLINE) f(std::integral_constant<int, 3>{});
+  else f(std::integral_constant<int, 4>{});
+}
+
 template <int D>
 void Launchers<D>::musl_p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const double* grav,
-                            unsigned* status) {
+                            unsigned* status, int basis) {
   if (pp.count <= 0) return;
   const unsigned nb = blocks_for(pp.count, 256);
+  const bool gr = grav[0] != 0.0 || grav[1] != 0.0;
   if constexpr (D == 2) {
-    if (grav[0] != 0.0 || grav[1] != 0.0) musl2d_p2g_kernel<true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], status);
-    else musl2d_p2g_kernel<false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, status);
+    if (basis == MPM_BASIS_LINEAR) {
+      if (gr) musl2d_p2g_kernel<true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], status);
+      else musl2d_p2g_kernel<false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, status);
+    } else {
+      with_bspline(basis, [&](auto Kc) {
+        constexpr int K = decltype(Kc)::value;
+        if (gr) bs_musl2d_p2g_kernel<K, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], status);
+        else bs_musl2d_p2g_kernel<K, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, status);
+      });
+    }
   } else {
-    p2g_kernel<D, double, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
+    // the 3D MUSL applies no body force
+    if (basis == MPM_BASIS_LINEAR) {
+      p2g_kernel<D, double, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
+    } else {
+      with_bspline(basis, [&](auto Kc) {
+        bs_p2g_kernel<D, double, decltype(Kc)::value, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
+      });
+    }
   }
 }
 
 template <int D>
 void Launchers<D>::musl_grid(cudaStream_t s, const NodeP& nd, const CgP& cg, double dt, double alpha,
-                             unsigned* status) {
+                             unsigned* status, int basis) {
   compact_blocks_kernel<<<blocks_for(nd.nblk, 256), 256, 0, s>>>(nd);
   if constexpr (D == 2) {
-    musl2d_cg_kernel<<<4, 1024, 0, s>>>(nd, cg, dt, status);
+    const int K = basis_nodes(basis);
+    if (K == 2) musl2d_cg_kernel<2><<<4, 1024, 0, s>>>(nd, cg, dt, status);
+    else if (K == 3) musl2d_cg_kernel<3><<<4, 1024, 0, s>>>(nd, cg, dt, status);
+    else musl2d_cg_kernel<4><<<4, 1024, 0, s>>>(nd, cg, dt, status);
     musl2d_node_kernel<<<sparse_ctas(nd), 256, 0, s>>>(nd, cg, dt, alpha);
   } else {
     musl_lumped_grid_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd, dt, alpha);
@@ -114,9 +159,16 @@ void Launchers<D>::musl_grid(cudaStream_t s, const NodeP& nd, const CgP& cg, dou
 
 template <int D>
 void Launchers<D>::musl_g2p1(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, double alpha,
-                             unsigned* status) {
+                             unsigned* status, int basis) {
   if (pp.count <= 0) return;
-  musl_g2p1_kernel<D, D == 3><<<blocks_for(pp.count, 256), 256, 0, s>>>(g, nd, pp, alpha, status);
+  const unsigned nb = blocks_for(pp.count, 256);
+  if (basis == MPM_BASIS_LINEAR) {
+    musl_g2p1_kernel<D, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, alpha, status);
+  } else {
+    with_bspline(basis, [&](auto Kc) {
+      bs_musl_g2p1_kernel<D, decltype(Kc)::value, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, alpha, status);
+    });
+  }
 }
 
 template <int D>
@@ -126,22 +178,52 @@ void Launchers<D>::musl_vg(cudaStream_t s, const NodeP& nd, double dt) {
 
 template <int D>
 void Launchers<D>::musl_g2p2(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, const MatParams& mp,
-                             unsigned* status) {
+                             unsigned* status, int basis) {
   if (pp.count <= 0) return;
   const unsigned nb = blocks_for(pp.count, 256);
-  switch (mp.type) {
-    case MPM_MAT_ELASTIC: musl_g2p2_kernel<D, MPM_MAT_ELASTIC, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status); break;
-    case MPM_MAT_NEOHOOKEAN:
-      musl_g2p2_kernel<D, MPM_MAT_NEOHOOKEAN, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
-      break;
-    case MPM_MAT_JOHNSON_COOK:
-      if constexpr (D == 3) musl_g2p2_kernel<D, MPM_MAT_JOHNSON_COOK, true><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
-      break;
-    case MPM_MAT_VOCE:
-      if constexpr (D == 3) musl_g2p2_kernel<D, MPM_MAT_VOCE, true><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
-      break;
-    default: musl_g2p2_kernel<D, MPM_MAT_J2, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status); break;
-  }
+  with_material<D>(mp.type, [&](auto Mc) {
+    constexpr int M = decltype(Mc)::value;
+    if (basis == MPM_BASIS_LINEAR) {
+      musl_g2p2_kernel<D, M, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+    } else {
+      with_bspline(basis, [&](auto Kc) {
+        bs_musl_g2p2_kernel<D, decltype(Kc)::value, M, D == 3><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+      });
+    }
+  });
+}
+
+template <int D>
+void Launchers<D>::bs_p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
+                          const double* grav, unsigned* status, int basis) {
+  if (pp.count <= 0) return;
+  const unsigned nb = blocks_for(pp.count, 256);
+  const bool gr = grav[0] != 0.0 || grav[1] != 0.0 || (D == 3 && grav[2] != 0.0);
+  with_bspline(basis, [&](auto Kc) {
+    constexpr int K = decltype(Kc)::value;
+    if (f32) {
+      if (gr) bs_p2g_kernel<D, float, K, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+      else bs_p2g_kernel<D, float, K, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
+    } else {
+      if (gr) bs_p2g_kernel<D, double, K, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+      else bs_p2g_kernel<D, double, K, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
+    }
+  });
+}
+
+template <int D>
+void Launchers<D>::bs_g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
+                          const MatParams& mp, unsigned* status, int basis) {
+  if (pp.count <= 0) return;
+  const unsigned nb = blocks_for(pp.count, 256);
+  with_material<D>(mp.type, [&](auto Mc) {
+    constexpr int M = decltype(Mc)::value;
+    with_bspline(basis, [&](auto Kc) {
+      constexpr int K = decltype(Kc)::value;
+      if (f32) bs_g2p_kernel<D, float, K, M><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+      else bs_g2p_kernel<D, double, K, M><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+    });
+  });
 }
 
 template <int D>

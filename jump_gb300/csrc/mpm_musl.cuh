@@ -10,7 +10,7 @@
 //   velocity gradient transposed, :187-189), F, J, V, strain, stress.
 // 2D, blended consistent mass (SolveExplicitSolidMechanics2D.jl:24-329):
 //   P2G with body force plus the consistent mass stencil M_ij = sum m N_i N_j
-//   (9 entries per node) -> v0 = B \ p0 and dv = B \ (dt f) per component with
+//   (9 entries per node for the linear basis, (2K-1)^2 for K nodes per axis) -> v0 = B \ p0 and dv = B \ (dt f) per component with
 //   B = 0.1 diag(m) + 0.9 M (massless rows: 1 on the diagonal), by Jacobi-
 //   preconditioned conjugate gradients, one CTA per right-hand side ->
 //   gv = v0 + dv; dv_node = gv - alpha v0, vdt = vg = gv dt where m > 0 ->
@@ -193,30 +193,37 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;
 }
 
-// (B v)_i with B = 0.1 diag(m) + 0.9 M, massless rows the identity
+// (B v)_i with B = 0.1 diag(m) + 0.9 M, massless rows the identity.  K nodes per
+// axis in a particle's support: M couples nodes up to K-1 apart per axis, so
+// its stencil has W x W entries, W = 2K - 1 (o = (dx + K - 1) + W (dy + K - 1)).
+template <int K>
 __device__ __forceinline__ double musl2d_apply(const NodeP& nd, const double* v, int64_t i) {
+  constexpr int W = 2 * K - 1;
   const int64_t Nn = nd.nodeCount, nx = nd.nn[0], ny = nd.nn[1];
   const double m = nd.m[i];
   if (!(m != 0.0)) return v[i];
   const int64_t ix = i % nx, iy = i / nx;
   double s = (0.1 * m) * v[i];
 #pragma unroll
-  for (int o = 0; o < 9; ++o) {
+  for (int o = 0; o < W * W; ++o) {
     const double c = nd.mc[o * Nn + i];
-    const int64_t jx = ix + (o % 3) - 1, jy = iy + (o / 3) - 1;
+    const int64_t jx = ix + (o % W) - (K - 1), jy = iy + (o / W) - (K - 1);
     if (c != 0.0 && jx >= 0 && jx < nx && jy >= 0 && jy < ny) s += (0.9 * c) * v[jx + nx * jy];
   }
   return s;
 }
 
+template <int K>
 __device__ __forceinline__ double musl2d_diag(const NodeP& nd, int64_t i) {
+  constexpr int W = 2 * K - 1;
   const double m = nd.m[i];
-  return m != 0.0 ? 0.1 * m + 0.9 * nd.mc[4 * nd.nodeCount + i] : 1.0;
+  return m != 0.0 ? 0.1 * m + 0.9 * nd.mc[((K - 1) * (W + 1)) * nd.nodeCount + i] : 1.0;
 }
 
 // One CTA per right-hand side over the nodes of the listed blocks; bounded by
 // kCgMaxIt iterations, after which ST_SOLVER is set.
-static __global__ void __launch_bounds__(1024) musl2d_cg_kernel(NodeP nd, CgP cg, double dt, unsigned* status) {
+template <int K>
+__global__ void __launch_bounds__(1024) musl2d_cg_kernel(NodeP nd, CgP cg, double dt, unsigned* status) {
   __shared__ double sh[32];
   const int rhs = blockIdx.x;
   const int64_t Nn = nd.nodeCount;
@@ -232,7 +239,7 @@ static __global__ void __launch_bounds__(1024) musl2d_cg_kernel(NodeP nd, CgP cg
     const int64_t i = block_node<2>(nd, nd.blist[w >> 6], int(w & 63));
     if (i < 0) continue;
     const double b = bscale * bsrc[i];
-    const double z = b / musl2d_diag(nd, i);
+    const double z = b / musl2d_diag<K>(nd, i);
     x[i] = 0.0;
     r[i] = b;
     p[i] = z;
@@ -253,7 +260,7 @@ static __global__ void __launch_bounds__(1024) musl2d_cg_kernel(NodeP nd, CgP cg
     for (int64_t w = threadIdx.x; w < work; w += blockDim.x) {
       const int64_t i = block_node<2>(nd, nd.blist[w >> 6], int(w & 63));
       if (i < 0) continue;
-      q[i] = musl2d_apply(nd, p, i);
+      q[i] = musl2d_apply<K>(nd, p, i);
       pq += p[i] * q[i];
     }
     pq = block_sum(pq, sh);
@@ -264,7 +271,7 @@ static __global__ void __launch_bounds__(1024) musl2d_cg_kernel(NodeP nd, CgP cg
       if (i < 0) continue;
       x[i] += alpha * p[i];
       r[i] -= alpha * q[i];
-      const double z = r[i] / musl2d_diag(nd, i);
+      const double z = r[i] / musl2d_diag<K>(nd, i);
       rzn += r[i] * z;
       rrn += r[i] * r[i];
     }
@@ -277,7 +284,7 @@ static __global__ void __launch_bounds__(1024) musl2d_cg_kernel(NodeP nd, CgP cg
     for (int64_t w = threadIdx.x; w < work; w += blockDim.x) {
       const int64_t i = block_node<2>(nd, nd.blist[w >> 6], int(w & 63));
       if (i < 0) continue;
-      p[i] = r[i] / musl2d_diag(nd, i) + beta * p[i];
+      p[i] = r[i] / musl2d_diag<K>(nd, i) + beta * p[i];
     }
   }
   if (!done && !(rr <= (kCgTol * kCgTol) * bb) && threadIdx.x == 0) atomicOr(status, ST_SOLVER);

@@ -87,8 +87,7 @@ __global__ void __launch_bounds__(256) clear_blocks_kernel(NodeP nd) {
       if (nd.p2) nd.p2[a * Nn + i] = 0.0;
     }
     if (nd.mc)
-#pragma unroll
-      for (int o = 0; o < 9; ++o) nd.mc[o * Nn + i] = 0.0;
+      for (int o = 0; o < nd.nmc; ++o) nd.mc[o * Nn + i] = 0.0;
   }
 }
 

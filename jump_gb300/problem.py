@@ -1,4 +1,5 @@
-"""solve_explicit_dynamics_2D / 3D for USL or MUSL + LinearBasis: the drop-in
+"""solve_explicit_dynamics_2D / 3D for USL or MUSL with the linear, quadratic or
+cubic B-spline basis: the drop-in
 for Problem.solve_explicit_dynamics_2D (USL SolveExplicitSolidMechanics2D.jl:335-585,
 MUSL :24-329) and solve_explicit_dynamics_3D (USL
 SolveExplicitSolidMechanics3D.jl:230-378, MUSL :14-223).
@@ -19,7 +20,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _capi
-from .algorithm import MUSL, USL, LinearBasis
+from .algorithm import MUSL, USL, CubicBsplineBasis, LinearBasis, QuadBsplineBasis
 from .dirichlet import fix_Dirichlet_grid
 from .engine import Descriptors, MPMContext
 from .fix import EnergiesFix, as_list, closeFile
@@ -63,8 +64,11 @@ def write_back(solids, states):
 
 
 def _solve(dim, grid, solids, basis, alg, output, fixes, data):
-    if not isinstance(basis, LinearBasis):
-        raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED, "the accelerated path supports LinearBasis only")
+    if not isinstance(basis, (LinearBasis, QuadBsplineBasis, CubicBsplineBasis)):
+        raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED,
+                             "the accelerated path supports LinearBasis, QuadBsplineBasis and CubicBsplineBasis")
+    basis_name = ("quad" if isinstance(basis, QuadBsplineBasis) else
+                  "cubic" if isinstance(basis, CubicBsplineBasis) else "linear")
     if not isinstance(alg, (USL, MUSL)):
         raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED, "the accelerated path supports USL and MUSL")
     musl = isinstance(alg, MUSL)
@@ -81,7 +85,8 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
                        precision=data.get("precision", "f64"), contact=bool(data.get("contact", False)),
                        friction=float(data.get("friction", 0.0)),
                        sort_interval=int(data.get("sort_interval", 0)),
-                       algorithm="musl" if musl else "usl", alpha=alg.alpha if musl else 1.0)
+                       algorithm="musl" if musl else "usl", alpha=alg.alpha if musl else 1.0,
+                       basis=basis_name)
     fl = as_list(fixes)
     need_particles = output.needs_particles or any(f.needs_particles for f in fl)
     times = step_times(t, Tf, dt)
