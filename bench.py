@@ -66,10 +66,11 @@ def launches_per_run(args, nbodies):
 
 
 def scheme_kw(args):
-    """Descriptor arguments of the update scheme under test."""
+    """Descriptor arguments of the update scheme and basis under test."""
+    kw = {"basis": args.basis} if args.basis != "linear" else {}
     if args.algorithm == "musl":
-        return {"algorithm": "musl", "alpha": args.alpha}
-    return {}
+        kw.update(algorithm="musl", alpha=args.alpha)
+    return kw
 
 
 def load_peaks():
@@ -281,7 +282,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (geometry-generated particles)",
-        "config": dict(cfg, algorithm=args.algorithm if args.algorithm == "usl" else f"musl(alpha={args.alpha})"),
+        "config": dict(cfg, algorithm=args.algorithm if args.algorithm == "usl" else f"musl(alpha={args.alpha})",
+                       basis=args.basis),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full {args.algorithm.upper()} steps of the workload after {args.warmup} warm-up "
                                    f"steps; C++ restatement of the Julia loops (Julia is not installed on the "
@@ -392,6 +394,7 @@ def run_ours(args):
             "data": "synthetic (geometry-generated particles, no dataset)",
             "config": dict(cfg, precision=args.precision, sort_interval=args.sort_interval,
                            algorithm=args.algorithm if args.algorithm == "usl" else f"musl(alpha={args.alpha})",
+                           basis=args.basis,
                            parallelism=f"replicas{world}" if world > 1 else "single-gpu"),
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "stage_ms_per_step": per,
@@ -637,6 +640,8 @@ def main():
     ap.add_argument("--algorithm", default="usl", choices=["usl", "musl"],
                     help="update scheme: USL (the headline) or MUSL (FLIP/PIC blend --alpha)")
     ap.add_argument("--alpha", type=float, default=1.0, help="MUSL FLIP/PIC blend")
+    ap.add_argument("--basis", default="linear", choices=["linear", "quad", "cubic"],
+                    help="shape functions: linear hat (the headline), quadratic or cubic B-splines")
     ap.add_argument("--material", default="j2", choices=["j2", "jc"],
                     help="Taylor bar material: J2 linear hardening (the headline) or Johnson-Cook")
     ap.add_argument("--sort-interval", type=int, default=0,
