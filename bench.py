@@ -539,6 +539,15 @@ def run_adjoint(args):
     g = c.bwd(loss_grad(x))
     both = time.perf_counter() - t0
     c.close()
+    # the same with every step's state and node buffer kept (no recompute)
+    c = make_context(problem, E, v0)
+    t0 = time.perf_counter()
+    c.fwd_checkpointed(nsteps, 1)
+    x1 = final_positions(c)
+    g1 = c.bwd(loss_grad(x1))
+    both_all = time.perf_counter() - t0
+    c.close()
+    store_all_dev = float(np.max(np.abs(g1["E"] - g["E"])) / np.max(np.abs(g["E"])))
     loss = lambda xx: float(np.sum((xx[tip] - target) ** 2))
     rng = np.random.default_rng(11)
     ids = rng.choice(npart, 32, replace=False)
@@ -563,6 +572,10 @@ def run_adjoint(args):
                       "checkpoint_every": every, "loss": "squared tip displacement error (top 5% in x)"},
            "forward_particle_updates_per_s": npart * nsteps / fwd,
            "fwd_adj_over_fwd_throughput": fwd / both,
+           "store_every_step": {"fwd_adj_over_fwd_throughput": fwd / both_all,
+                                "particle_updates_per_s": npart * nsteps / both_all,
+                                "device_memory_gb": round(nsteps * (npart * 25 * 8 + 4745 * 9 * 8) / 1e9, 2),
+                                "grad_max_rel_diff_vs_checkpointed": store_all_dev},
            "fd_check": {"params": 32, "norm_rel_err": float(np.linalg.norm(ad - fd) / np.linalg.norm(fd)),
                         "max_rel_err": float(np.max(np.abs(ad - fd)) / np.max(np.abs(fd))),
                         "step": "1e-4 relative, central, GPU forward runs"}}

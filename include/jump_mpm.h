@@ -202,7 +202,10 @@ int mpm_destroy(mpm_ctx* ctx);
  * cells (the hat basis has kinks at nodes and cell faces).
  * ------------------------------------------------------------------------- */
 /* Advance nsteps steps keeping a snapshot of the particle state every
-   `checkpoint_every` steps (and the final state) in device memory. */
+   `checkpoint_every` steps (and the final state) in device memory.  With
+   checkpoint_every = 1 every step's state and node buffer are kept
+   (nsteps x (state + node buffer) bytes of device memory) and mpm_bwd
+   recomputes nothing. */
 int mpm_fwd_checkpointed(mpm_ctx* ctx, int64_t nsteps, int32_t checkpoint_every);
 /* Reverse sweep over the last mpm_fwd_checkpointed run: each segment is
    recomputed from its snapshot, then differentiated step by step.

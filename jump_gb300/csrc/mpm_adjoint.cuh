@@ -218,14 +218,17 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, 
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     double p0b = 0.0, fb = 0.0;
+    const double vdtb = na.vdtb[a * Nn + i], dvb = na.dvb[a * Nn + i];
     if (m > tol && !(fx & (1u << a))) {
-      const double vdtb = na.vdtb[a * Nn + i], dvb = na.dvb[a * Nn + i];
       p0b = dt * vdtb / m;
       fb = (dt * dt * vdtb + dt * dvb) / m;
       mb -= (vdtb * gr.vdt[a * Nn + i] + dvb * gr.dv[a * Nn + i]) / m;
     }
     na.p0b[a * Nn + i] = p0b;
     na.fb[a * Nn + i] = fb;
+    // consumed: zero for the previous step's G2P adjoint, which accumulates into them
+    na.vdtb[a * Nn + i] = 0.0;
+    na.dvb[a * Nn + i] = 0.0;
   }
   na.mb[i] = mb;
 }

@@ -94,6 +94,8 @@ struct mpm_ctx {
   double* contactbuf = nullptr;
   float* contactbuf_f = nullptr;
   double* nodebuf = nullptr;
+  double* fullrec = nullptr;  // reverse mode, checkpoint every step: every step's node buffer
+  int64_t fullrec_steps = 0;
   double* muslbuf = nullptr;  // MUSL: 3D p2 | vg; 2D mass stencil (9) | vg | CG vectors (16)
   CgP cg{};
   float* nodebuf_f = nullptr;
@@ -147,6 +149,7 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->coords);
   cudaFree(c->fixed);
   cudaFree(c->nodebuf);
+  cudaFree(c->fullrec);
   cudaFree(c->muslbuf);
   cudaFree(c->nodebuf_f);
   cudaFree(c->blockbuf);
@@ -258,7 +261,7 @@ CompMapH full_from_sym(int dim) {
 }
 
 // The launches of one USL step; ev (optional) gets an event recorded after each stage.
-// rec (optional): receives this step's grid outputs m | vdt (D) | dv (D) for the adjoint
+// rec (optional): receives this step's node buffer m | p0 | f | vdt | dv for the adjoint
 // One MUSL step (mpm_musl.cuh); ev as enqueue_step.
 void enqueue_musl(mpm_ctx* c, cudaEvent_t* ev) {
   const int D = c->dim;
@@ -323,9 +326,9 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
     else Launchers<3>::grid(c->stream, c->nd, c->prm.dt, c->prm.tolerance, c->f32);
   }
   if (rec) {
+    // the node buffer m | p0 | f | vdt | dv in one copy (the adjoint reads m, vdt, dv)
     const size_t Nn = size_t(c->nd.nodeCount);
-    cudaMemcpyAsync(rec, c->nd.m, Nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-    cudaMemcpyAsync(rec + Nn, c->nd.vdt, 2 * D * Nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(rec, c->nodebuf, Nn * (1 + 4 * D) * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   }
   if (ev) cudaEventRecord(ev[2], c->stream);
   for (int b = 0; b < c->nb; ++b) {
@@ -867,12 +870,32 @@ int mpm_fwd_checkpointed(mpm_ctx* c, int64_t nsteps, int32_t every) {
     CUDA_TRY(cudaMalloc(&c->ckpt, bytes * size_t(slots)));
     c->ckpt_slots = slots;
   }
+  // every == 1: every state is kept anyway, so each step's node buffer is kept
+  // too and the reverse sweep recomputes nothing
+  const int64_t Nn = c->nd.nodeCount;
+  const size_t recbytes = size_t(Nn) * (1 + 4 * c->dim) * sizeof(double);
+  if (every == 1) {
+    if (c->fullrec_steps != nsteps) {
+      cudaFree(c->fullrec);
+      c->fullrec = nullptr;
+      c->fullrec_steps = 0;
+      CUDA_TRY(cudaMalloc(&c->fullrec, recbytes * size_t(nsteps)));
+      c->fullrec_steps = nsteps;
+    }
+  } else if (c->fullrec) {
+    cudaFree(c->fullrec);
+    c->fullrec = nullptr;
+    c->fullrec_steps = 0;
+  }
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CUDA_TRY(cudaMemcpyAsync(c->ckpt, c->P, bytes, cudaMemcpyDeviceToDevice, c->stream));
   int r;
   if ((r = build_step_graph(c))) return r;
   for (int64_t k = 1; k <= nsteps; ++k) {
     CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
+    if (every == 1)
+      CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(c->fullrec) + recbytes * size_t(k - 1), c->nodebuf, recbytes,
+                               cudaMemcpyDeviceToDevice, c->stream));
     if (k % every == 0 && k < nsteps)
       CUDA_TRY(cudaMemcpyAsync(c->ckpt + bytes * size_t(k / every), c->P, bytes, cudaMemcpyDeviceToDevice,
                                c->stream));
@@ -910,7 +933,7 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
     c->gridrec = nullptr;
     c->segbuf_slots = 0;
     CUDA_TRY(cudaMalloc(&c->segbuf, bytes * size_t(every)));
-    CUDA_TRY(cudaMalloc(&c->gridrec, size_t(Nn) * (1 + 2 * D) * sizeof(double) * size_t(every)));
+    CUDA_TRY(cudaMalloc(&c->gridrec, size_t(Nn) * (1 + 4 * D) * sizeof(double) * size_t(every)));
     c->segbuf_slots = every;
   }
   if (!c->adjbuf) {
@@ -943,17 +966,18 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
   na.fb = c->nodeadj + Nn * (1 + 3 * D);
   const int64_t nseg = c->ckpt_slots - 1;
   void* Pwork = c->P;
+  CUDA_TRY(cudaMemsetAsync(c->nodeadj, 0, size_t(Nn) * 2 * D * sizeof(double), c->stream));
   // One segment: recompute `len` steps from the state in P, recording each
   // step's particle state and grid outputs, then the reverse sweep over them.
   auto enqueue_segment = [&](int len) {
     for (int j = 0; j < len; ++j) {
       cudaMemcpyAsync(c->segbuf + bytes * size_t(j), Pwork, bytes, cudaMemcpyDeviceToDevice, c->stream);
-      enqueue_step(c, nullptr, c->gridrec + size_t(Nn) * (1 + 2 * D) * size_t(j));
+      enqueue_step(c, nullptr, c->gridrec + size_t(Nn) * (1 + 4 * D) * size_t(j));
     }
     for (int j = len - 1; j >= 0; --j) {
-      const double* rec = c->gridrec + size_t(Nn) * (1 + 2 * D) * size_t(j);
-      const GridRec gr{rec, rec + Nn, rec + Nn * (1 + D)};
-      cudaMemsetAsync(c->nodeadj, 0, size_t(Nn) * 2 * D * sizeof(double), c->stream);
+      const double* rec = c->gridrec + size_t(Nn) * (1 + 4 * D) * size_t(j);
+      const GridRec gr{rec, rec + Nn * (1 + 2 * D), rec + Nn * (1 + 3 * D)};
+      // the node adjoints vdt_bar, dv_bar are zero here: set once below, then zeroed by grid_adj
       for (int b = 0; b < c->nb; ++b) {
         const PartP ps{c->segbuf + bytes * size_t(j), c->np, c->off[b], c->cnt[b]};
         if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
@@ -995,7 +1019,31 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
     *out = c->seg_exec[slot];
     return MPM_OK;
   };
-  for (int64_t seg = nseg - 1; seg >= 0; --seg) {
+  if (every == 1 && c->fullrec) {
+    // every state and node buffer of the forward run is stored: the reverse
+    // sweep is three kernels per step
+    const size_t recd = size_t(Nn) * (1 + 4 * D);
+    for (int64_t k = nsteps; k >= 1; --k) {
+      const double* rec = c->fullrec + recd * size_t(k - 1);
+      const GridRec gr{rec, rec + Nn * (1 + 2 * D), rec + Nn * (1 + 3 * D)};
+      char* state = reinterpret_cast<char*>(c->ckpt) + bytes * size_t(k - 1);
+      for (int b = 0; b < c->nb; ++b) {
+        const PartP ps{state, c->np, c->off[b], c->cnt[b]};
+        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
+        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
+      }
+      if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
+      else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
+      for (int b = 0; b < c->nb; ++b) {
+        const PartP ps{state, c->np, c->off[b], c->cnt[b]};
+        const double nu = c->nus[b];
+        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
+        if (D == 2) Launchers<2>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
+        else Launchers<3>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
+      }
+    }
+  }
+  for (int64_t seg = (every == 1 && c->fullrec) ? -1 : nseg - 1; seg >= 0; --seg) {
     const int64_t n0 = seg * every;
     const int len = int(std::min<int64_t>(every, nsteps - n0));
     CUDA_TRY(cudaMemcpyAsync(Pwork, c->ckpt + bytes * size_t(seg), bytes, cudaMemcpyDeviceToDevice, c->stream));

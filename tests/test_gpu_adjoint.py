@@ -131,3 +131,14 @@ def test_inverse_problem_reduces_loss():
         gl = g["E"] * E  # gradient with respect to log E
         E = E * np.exp(-0.3 * gl / (np.max(np.abs(gl)) + 1e-300))
     assert losses[-1] < 0.5 * losses[0], losses
+
+
+def test_store_every_step_matches_checkpointing():
+    """checkpoint_every = 1 (every state and node buffer kept, no recompute)
+    gives the gradients of the checkpointed sweep."""
+    problem, E, v0, tip = setup_case(2)
+    x_a, ga = rollout_grad(problem, E, v0, NSTEPS, EVERY, lambda x: np.where(tip[:, None], x, 0.0))
+    x_b, gb = rollout_grad(problem, E, v0, NSTEPS, 1, lambda x: np.where(tip[:, None], x, 0.0))
+    assert np.max(np.abs(x_a - x_b)) <= 1e-12 * np.max(np.abs(x_a))
+    for k in ("E", "v0"):
+        assert np.max(np.abs(ga[k] - gb[k])) <= 1e-9 * np.max(np.abs(ga[k])), k
