@@ -53,6 +53,9 @@ BYTES_MUSL = {"p2g": 112 + 7, "g2p": 80 + 3 + 496 + 6, "step": 720}
 # Johnson-Cook, FP64: G2P reads x3 v3 V0 F9 eps6 sigma6 alpha alphadot (30 doubles)
 # and writes x3 v3 V F9 eps6 sigma6 alpha alphadot vm (31 doubles) -> 488 B
 BYTES_JC = {"p2g": 112 + 7, "g2p": 488 + 6, "step": 560}
+# Johnson-Cook with damage, FP64: as Johnson-Cook plus damage_init, damage and
+# temperature read and written and vm read (kept by failed particles) -> 544 B
+BYTES_JCD = {"p2g": 112 + 7, "g2p": 544 + 6, "step": 616}
 
 
 def launches_per_run(args, nbodies):
@@ -82,9 +85,22 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str, precision: str):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_taylor_bar_{precision}.txt")
+def variant_tag(args):
+    """Profile-name tag of the update scheme, basis and material under test ("" for
+    USL, the linear basis and J2, the default workload)."""
+    tag = ""
+    if args.algorithm == "musl":
+        tag += "_musl"
+    if args.basis != "linear":
+        tag += f"_{args.basis}"
+    if args.material != "j2":
+        tag += f"_{args.material}"
+    return tag
+
+
+def ncu_traffic(kernel: str, precision: str, tag: str = ""):
+    """DRAM bytes per launch from the committed ncu summary of this exact variant, if one exists."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_taylor_bar{tag}_{precision}.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -145,6 +161,16 @@ def workload(name: str, material: str = "j2"):
             s[0].mat = JohnsonCookMaterial(115e9, 0.31, 8940.0, 65e6, 356e6, 0.0, 0.37, 1e-3, 0.0, 0.0, 0.0,
                                            2.5e-4, s[0].parCount)
             label = "Johnson-Cook (A 65 MPa, B 356 MPa, n 0.37, C 0)"
+        elif material == "jcdamage":
+            # the steel of the reference's Taylor-bar fracture driver (Main_Taylor_Bar_Frac_FEMP.jl:41-61)
+            # in SI units, on the copper bar's geometry and time step
+            from jump_gb300.material import JohnsonCookDamage, JohnsonCookMaterial, JohnsonCookMaterialWithDamage
+            n = s[0].parCount
+            st = JohnsonCookMaterial(200e9, 0.33, 7850.0, 490e6, 383e6, 0.0123, 0.45, 0.5, 0.94, 0.9, 452.0,
+                                     2.5e-4, n)
+            s[0].mat = JohnsonCookMaterialWithDamage(st, JohnsonCookDamage(0.0705, 1.732, -0.54, 0.015, 0.0, 0.5,
+                                                                           293.0, 1800.0, n))
+            label = "Johnson-Cook with damage (steel: A 490 MPa, B 383 MPa, n 0.45, C 0.0123; D1-D4)"
         cfg = {"workload": f"taylor_bar_3d_{material}", "particles": int(s[0].parCount), "grid_nodes": [65, 65, 161],
                "h_m": 2.5e-4, "particles_per_cell": 8, "material": label,
                "dt_s": data["dt"], "l2": "inputs larger than L2 (~230 MB resident)"}
@@ -221,7 +247,7 @@ def pinned_like(a: np.ndarray) -> np.ndarray:
 
 PARTICLE_ARRAYS = ("pos", "velocity", "mass", "volume", "volumeInitial", "deformationGradient", "strain",
                    "stress", "youngs")
-MATERIAL_ARRAYS = ("alpha", "pstrain", "pstrain_3D", "alphadot")
+MATERIAL_ARRAYS = ("alpha", "pstrain", "pstrain_3D", "alphadot", "vmStr", "damage_init", "dam")
 
 
 def pin_solids(solids):
@@ -236,7 +262,7 @@ def pin_solids(solids):
 
 
 def pin_state(st):
-    for k in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot"):
+    for k in st.FIELDS:
         setattr(st, k, pinned_like(getattr(st, k)))
     return st
 
@@ -328,11 +354,12 @@ def run_ours(args):
     per = {k: v / nprof for k, v in st.items()}
     dom = max(("p2g", "g2p"), key=lambda k: per[k])
     peak, peak_kind = load_peaks()
-    table = BYTES_MUSL if args.algorithm == "musl" else (BYTES_JC if args.material == "jc" and args.precision == "f64"
+    table = BYTES_MUSL if args.algorithm == "musl" else (BYTES_JCD if args.material == "jcdamage" and args.precision == "f64" else
+                                                         BYTES_JC if args.material == "jc" and args.precision == "f64"
                                                          else BYTES[args.precision])
     bts = table[dom] * npart
     achieved = bts / (per[dom] * 1e-3) / 1e9
-    traffic = ncu_traffic(dom, args.precision)
+    traffic = ncu_traffic(dom, args.precision, variant_tag(args))
     step_bytes = table["step"] * npart
     ctx.close()
 
@@ -363,8 +390,7 @@ def run_ours(args):
              "download_ms": 1e3 * (e2e_ctx_t0 + e2e_wall - t2)}
     c2.close()
     h2d = sum(a.nbytes for a in desc._keep)
-    d2h = sum(sum(getattr(stt, k).nbytes for k in ("pos", "velocity", "volume", "F", "strain", "stress",
-                                                   "alpha", "pstrain", "vmstr", "alphadot")) for stt in states)
+    d2h = sum(sum(getattr(stt, k).nbytes for k in stt.FIELDS) for stt in states)
     e2e_t = allreduce_max(dist, e2e_wall)
     e2e_value = total_updates / e2e_t
 
@@ -655,8 +681,9 @@ def main():
     ap.add_argument("--alpha", type=float, default=1.0, help="MUSL FLIP/PIC blend")
     ap.add_argument("--basis", default="linear", choices=["linear", "quad", "cubic"],
                     help="shape functions: linear hat (the headline), quadratic or cubic B-splines")
-    ap.add_argument("--material", default="j2", choices=["j2", "jc"],
-                    help="Taylor bar material: J2 linear hardening (the headline) or Johnson-Cook")
+    ap.add_argument("--material", default="j2", choices=["j2", "jc", "jcdamage"],
+                    help="Taylor bar material: J2 linear hardening (the headline), Johnson-Cook, or Johnson-Cook "
+                         "with damage")
     ap.add_argument("--sort-interval", type=int, default=0,
                     help="counting-sort particles by cell every N steps (0: never)")
     ap.add_argument("--workload", default="taylor_bar",

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 5
+#define JUMP_MPM_ABI_VERSION 6
 
 /* status codes */
 #define MPM_OK               0
@@ -57,6 +57,7 @@ extern "C" {
 #define MPM_MAT_J2          2   /* ElastoPlasticMaterial, Material.jl:128-275 */
 #define MPM_MAT_JOHNSON_COOK 3  /* JohnsonCookMaterial, Material.jl:279-330, 386-443 (3D) */
 #define MPM_MAT_VOCE        4   /* VoceMaterial, Material.jl:336-383, 445-493 (3D) */
+#define MPM_MAT_JOHNSON_COOK_DAMAGE 5  /* JohnsonCookMaterialWithDamage, Material.jl:495-646 (3D) */
 
 /* particle precision (grid accumulation is always FP64) */
 #define MPM_PREC_F64        0   /* every particle field and every operation in FP64 */
@@ -93,6 +94,13 @@ typedef struct mpm_material_desc {
      Voce: A - B exp(-C ep) (n, epsdot0 unused); both: plastic strain rate filter
      time 1000 cellsize / sqrt((lambda + 2 mu)/density) */
   double  A, B, C, n, epsdot0, cellsize;
+  /* Johnson-Cook with damage only: thermal softening exponent m, Taylor-Quinney
+     coefficient chi and specific heat Cp of the strength part (temperature rise
+     chi/(density Cp) x flow stress x plastic strain increment; Cp > 0), and the
+     damage part JohnsonCookDamage(d1..d5, epsdot0, Tr, Tm): failure strain
+     (d1 + d2 exp(d3 triaxiality))(1 + d4 ln(epdot/depsdot0))(1 + d5 (T - Tr)/(Tm - Tr)) */
+  double  m, chi, Cp;
+  double  d1, d2, d3, d4, d5, depsdot0, Tr, Tm;
 } mpm_material_desc;
 
 /* Particle arrays of one Solid2D/Solid3D (Solid.jl:67-125, 267-297), read at create time. */
@@ -111,6 +119,11 @@ typedef struct mpm_body_desc {
   const double* pstrain;            /* J2: 3 (2D Voigt) or 9 (3D) per particle, or NULL */
   const double* youngs;             /* optional per-particle Young's modulus, or NULL */
   const double* alphadot;           /* Johnson-Cook/Voce: plastic strain rate, or NULL (zeros) */
+  const double* damage_init;        /* Johnson-Cook with damage: damage_init, or NULL (zeros) */
+  const double* damage;             /*   dam, or NULL (zeros) */
+  const double* temperature;        /*   damage_part.temp, or NULL (Tr) */
+  const double* vmstr;              /* the material's vmStr, or NULL (zeros): state for Johnson-Cook with
+                                       damage, whose failed particles keep it; recomputed by the others */
 } mpm_body_desc;
 
 /* Writable views for mpm_download; any pointer may be NULL to skip that field. */
@@ -125,6 +138,9 @@ typedef struct mpm_body_view {
   double* pstrain;
   double* vmstr;                    /* von Mises stress written by Elastic-3D and J2 updates */
   double* alphadot;                 /* Johnson-Cook/Voce plastic strain rate, or NULL */
+  double* damage_init;              /* Johnson-Cook with damage state, or NULL */
+  double* damage;
+  double* temperature;
 } mpm_body_view;
 
 typedef struct mpm_params {

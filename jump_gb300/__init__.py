@@ -13,7 +13,7 @@ from .algorithm import (USL, MUSL, LinearBasis, QuadBsplineBasis, CubicBsplineBa
                         ConstantBodyForce2D, ConstantBodyForce3D)
 from .grid import Grid2D, Grid3D, to_1D_index
 from .material import (ElasticMaterial, NeoHookeanMaterial, ElastoPlasticMaterial, JohnsonCookMaterial,
-                       VoceMaterial, RigidMaterial)
+                       VoceMaterial, RigidMaterial, JohnsonCookDamage, JohnsonCookMaterialWithDamage)
 from .solid import (Solid2D, Solid3D, assign_velocity, move, julia_range, buildParticleForCircle,
                     buildParticleForRing, buildParticleForSphere, buildParticleForCylinder,
                     buildParticleForRectangle, buildParticleForBlock)

@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-ABI_VERSION = 5  # JUMP_MPM_ABI_VERSION of the structures below
+ABI_VERSION = 6  # JUMP_MPM_ABI_VERSION of the structures below
 
 MPM_OK = 0
 MPM_ERR_ARG = 1
@@ -42,6 +42,7 @@ MPM_MAT_NEOHOOKEAN = 1
 MPM_MAT_J2 = 2
 MPM_MAT_JOHNSON_COOK = 3
 MPM_MAT_VOCE = 4
+MPM_MAT_JOHNSON_COOK_DAMAGE = 5
 
 MPM_PREC_F64 = 0
 MPM_PREC_F32 = 1
@@ -87,6 +88,17 @@ class MaterialDesc(C.Structure):
         ("n", C.c_double),
         ("epsdot0", C.c_double),
         ("cellsize", C.c_double),
+        ("m", C.c_double),
+        ("chi", C.c_double),
+        ("Cp", C.c_double),
+        ("d1", C.c_double),
+        ("d2", C.c_double),
+        ("d3", C.c_double),
+        ("d4", C.c_double),
+        ("d5", C.c_double),
+        ("depsdot0", C.c_double),
+        ("Tr", C.c_double),
+        ("Tm", C.c_double),
     ]
 
 
@@ -106,6 +118,10 @@ class BodyDesc(C.Structure):
         ("pstrain", _dp),
         ("youngs", _dp),
         ("alphadot", _dp),
+        ("damage_init", _dp),
+        ("damage", _dp),
+        ("temperature", _dp),
+        ("vmstr", _dp),
     ]
 
 
@@ -121,6 +137,9 @@ class BodyView(C.Structure):
         ("pstrain", _dp),
         ("vmstr", _dp),
         ("alphadot", _dp),
+        ("damage_init", _dp),
+        ("damage", _dp),
+        ("temperature", _dp),
     ]
 
 

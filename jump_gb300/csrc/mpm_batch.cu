@@ -317,6 +317,11 @@ int launch_m(mpm_batch* b, void* P, int64_t n, int th, int per) {
         return b->grav ? launch_t<D, R, MPM_MAT_VOCE, true>(b, P, n, th, per)
                        : launch_t<D, R, MPM_MAT_VOCE, false>(b, P, n, th, per);
       return fail(MPM_ERR_ARG, "mpm_batch: Voce is a 3D material");
+    case MPM_MAT_JOHNSON_COOK_DAMAGE:
+      if constexpr (D == 3)
+        return b->grav ? launch_t<D, R, MPM_MAT_JOHNSON_COOK_DAMAGE, true>(b, P, n, th, per)
+                       : launch_t<D, R, MPM_MAT_JOHNSON_COOK_DAMAGE, false>(b, P, n, th, per);
+      return fail(MPM_ERR_ARG, "mpm_batch: Johnson-Cook with damage is a 3D material");
     default:
       return b->grav ? launch_t<D, R, MPM_MAT_J2, true>(b, P, n, th, per)
                      : launch_t<D, R, MPM_MAT_J2, false>(b, P, n, th, per);
@@ -737,7 +742,19 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       if ((r = upload(b, pp, d.stress, D * D, L::SIG, sym_from_full(D, b->d_status, ST_ASYM_STRESS)))) return r;
       if ((r = upload(b, pp, d.alpha, 1, L::ALPHA, ident(1)))) return r;
       if ((r = upload(b, pp, d.alphadot, 1, L::ALPHAD, ident(1)))) return r;
-      if (d.pstrain) {
+      if ((r = upload(b, pp, d.vmstr, 1, L::VM, ident(1)))) return r;
+      if (D == 3 && d.mat.type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+        // damage state in the plastic strain slots; temperatures start at Tr (Material.jl:507)
+        if ((r = upload(b, pp, d.damage_init, 1, L::EP, ident(1)))) return r;
+        if ((r = upload(b, pp, d.damage, 1, L::EP + 1, ident(1)))) return r;
+        std::vector<double> Tr;
+        const double* T = d.temperature;
+        if (!T) {
+          Tr.assign(size_t(d.count), d.mat.Tr);
+          T = Tr.data();
+        }
+        if ((r = upload(b, pp, T, 1, L::EP + 2, ident(1)))) return r;
+      } else if (d.pstrain) {
         r = D == 2 ? upload(b, pp, d.pstrain, 3, L::EP, ident(3)) : upload(b, pp, d.pstrain, 9, L::EP, sym_from_full(3, b->d_status, ST_ASYM_PSTRAIN));
         if (r) return r;
       }
@@ -818,6 +835,8 @@ int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t prec
         return fail(MPM_ERR_ARG, "mpm_batch_create: pos, velocity, mass, volume and volume_initial are required");
       if (!material_ok(bd.mat.type, D))
         return fail(MPM_ERR_ARG, "mpm_batch_create: unknown material type");
+      if (!material_params_ok(bd.mat))
+        return fail(MPM_ERR_ARG, "mpm_batch_create: Johnson-Cook with damage needs density > 0 and Cp > 0");
       mixed = mixed || (mat >= 0 && bd.mat.type != mat);
       mat = bd.mat.type;
     }
@@ -895,8 +914,14 @@ int mpm_batch_download(mpm_batch* b, int32_t instance, int32_t body, const mpm_b
   if ((r = download(b, pp, v->stress, D * D, SIG, full_from_sym(D)))) return r;
   if ((r = download(b, pp, v->alpha, 1, ALPHA, ident(1)))) return r;
   if ((r = download(b, pp, v->alphadot, 1, D == 2 ? Layout<2>::ALPHAD : Layout<3>::ALPHAD, ident(1)))) return r;
-  if ((r = D == 2 ? download(b, pp, v->pstrain, 3, EP, ident(3)) : download(b, pp, v->pstrain, 9, EP, full_from_sym(3))))
+  if (D == 3 && b->inst[instance].mp[body].type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+    if ((r = download(b, pp, v->damage_init, 1, EP, ident(1)))) return r;
+    if ((r = download(b, pp, v->damage, 1, EP + 1, ident(1)))) return r;
+    if ((r = download(b, pp, v->temperature, 1, EP + 2, ident(1)))) return r;
+  } else if ((r = D == 2 ? download(b, pp, v->pstrain, 3, EP, ident(3))
+                        : download(b, pp, v->pstrain, 9, EP, full_from_sym(3)))) {
     return r;
+  }
   if (v->vmstr && pp.count > 0) {
     if (b->inst[instance].mp[body].type == MPM_MAT_J2) {
       if (D == 2) Launchers<2>::j2_vm(b->stream, pp, b->f32, b->staging);

@@ -564,7 +564,19 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
       return r;
     if (d.alpha && (r = upload(c, b, d.alpha, 1, fi.ALPHA, ident(1)))) return r;
     if (d.alphadot && (r = upload(c, b, d.alphadot, 1, fi.ALPHAD, ident(1)))) return r;
-    if (d.pstrain) {
+    if (d.vmstr && (r = upload(c, b, d.vmstr, 1, fi.VM, ident(1)))) return r;
+    if (D == 3 && d.mat.type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+      // damage state in the plastic strain slots; temperatures start at Tr (Material.jl:507)
+      if (d.damage_init && (r = upload(c, b, d.damage_init, 1, fi.EP, ident(1)))) return r;
+      if (d.damage && (r = upload(c, b, d.damage, 1, fi.EP + 1, ident(1)))) return r;
+      std::vector<double> Tr;
+      const double* T = d.temperature;
+      if (!T) {
+        Tr.assign(size_t(n), d.mat.Tr);
+        T = Tr.data();
+      }
+      if ((r = upload(c, b, T, 1, fi.EP + 2, ident(1)))) return r;
+    } else if (d.pstrain) {
       if (D == 2) r = upload(c, b, d.pstrain, 3, fi.EP, ident(3));
       else r = upload(c, b, d.pstrain, 9, fi.EP, sym_from_full(3, c->status, ST_ASYM_PSTRAIN));
       if (r) return r;
@@ -639,7 +651,10 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
     if (d.count > 0 && (!d.pos || !d.velocity || !d.mass || !d.volume || !d.volume_initial))
       return fail(MPM_ERR_ARG, "mpm_create: pos, velocity, mass, volume and volume_initial are required");
     if (!material_ok(d.mat.type, D))
-      return fail(MPM_ERR_ARG, "mpm_create: unknown material type (Johnson-Cook and Voce are 3D)");
+      return fail(MPM_ERR_ARG, "mpm_create: unknown material type (Johnson-Cook, Voce and Johnson-Cook with "
+                               "damage are 3D)");
+    if (!material_params_ok(d.mat))
+      return fail(MPM_ERR_ARG, "mpm_create: Johnson-Cook with damage needs density > 0 and Cp > 0");
   }
   mpm_ctx* c = new mpm_ctx();
   int r = create_impl(grid, bodies, nbodies, params, c);
@@ -690,9 +705,15 @@ int mpm_download(mpm_ctx* c, int32_t body, const mpm_body_view* v) {
   if ((r = download(c, body, v->stress, D * D, fi.SIG, full_from_sym(D)))) return r;
   if ((r = download(c, body, v->alpha, 1, fi.ALPHA, ident(1)))) return r;
   if ((r = download(c, body, v->alphadot, 1, fi.ALPHAD, ident(1)))) return r;
-  if (D == 2) r = download(c, body, v->pstrain, 3, fi.EP, ident(3));
-  else r = download(c, body, v->pstrain, 9, fi.EP, full_from_sym(3));
-  if (r) return r;
+  if (D == 3 && c->mats[body].type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+    if ((r = download(c, body, v->damage_init, 1, fi.EP, ident(1)))) return r;
+    if ((r = download(c, body, v->damage, 1, fi.EP + 1, ident(1)))) return r;
+    if ((r = download(c, body, v->temperature, 1, fi.EP + 2, ident(1)))) return r;
+  } else {
+    if (D == 2) r = download(c, body, v->pstrain, 3, fi.EP, ident(3));
+    else r = download(c, body, v->pstrain, 9, fi.EP, full_from_sym(3));
+    if (r) return r;
+  }
   if (v->vmstr && c->cnt[body] > 0) {
     if (c->mats[body].type == MPM_MAT_J2) {
       // J2 vmStr is a function of the stored stress (Material.jl:223-224, 273-274)

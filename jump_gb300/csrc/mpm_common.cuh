@@ -41,6 +41,11 @@ struct Layout {
   static constexpr int MU = LAM + 1;
   static constexpr int ALPHAD = MU + 1;        // Johnson-Cook/Voce plastic strain rate
   static constexpr int NF = ALPHAD + 1;
+  // Johnson-Cook with damage (3D) keeps its state in the plastic strain slots,
+  // which only J2 uses: damage_init, damage, temperature
+  static constexpr int DINIT = EP;
+  static constexpr int DAM = EP + 1;
+  static constexpr int TEMP = EP + 2;
 };
 
 // symmetric index (i, j) -> storage slot
@@ -59,6 +64,9 @@ struct MatParams {
   // Johnson-Cook / Voce: hardening constants, rate filter time 1000 cellsize /
   // signal velocity, and the step dt it is applied with
   double A, B, C, n, epsdot0, tav, dtime;
+  // Johnson-Cook with damage: thermal softening exponent, temperature rise per
+  // unit plastic work chi/(density Cp), damage constants, Tm - Tr
+  double m, delta, d1, d2, d3, d4, d5, depsdot0, Tr, Tm, Tmr;
 };
 
 // Grid description shared by all kernels.

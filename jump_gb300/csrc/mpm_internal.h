@@ -31,9 +31,22 @@ inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, 
   mp.C = m.C;
   mp.n = m.n;
   mp.epsdot0 = m.epsdot0;
-  if (m.type == MPM_MAT_JOHNSON_COOK || m.type == MPM_MAT_VOCE) {
+  if (m.type == MPM_MAT_JOHNSON_COOK || m.type == MPM_MAT_VOCE || m.type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
     const double velo = std::sqrt((mp.lambda + 2 * mp.mu) / m.density);  // Material.jl:317
     mp.tav = 1000 * m.cellsize / velo;                                   // Material.jl:428
+  }
+  if (m.type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+    mp.m = m.m;
+    mp.delta = m.chi / (m.density * m.Cp);  // Material.jl:323
+    mp.d1 = m.d1;
+    mp.d2 = m.d2;
+    mp.d3 = m.d3;
+    mp.d4 = m.d4;
+    mp.d5 = m.d5;
+    mp.depsdot0 = m.depsdot0;
+    mp.Tr = m.Tr;
+    mp.Tm = m.Tm;
+    mp.Tmr = m.Tm - m.Tr;  // Material.jl:507
   }
   mp.dtime = dt;
   return mp;
@@ -42,7 +55,14 @@ inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, 
 // material model types a context or batch accepts in dimension dim
 inline bool material_ok(int type, int dim) {
   if (type == MPM_MAT_ELASTIC || type == MPM_MAT_NEOHOOKEAN || type == MPM_MAT_J2) return true;
-  return dim == 3 && (type == MPM_MAT_JOHNSON_COOK || type == MPM_MAT_VOCE);
+  return dim == 3 && (type == MPM_MAT_JOHNSON_COOK || type == MPM_MAT_VOCE || type == MPM_MAT_JOHNSON_COOK_DAMAGE);
+}
+
+// material parameters a context or batch accepts: the damage model's
+// temperature rise chi/(density Cp) needs density Cp > 0
+inline bool material_params_ok(const mpm_material_desc& m) {
+  if (m.type != MPM_MAT_JOHNSON_COOK_DAMAGE) return true;
+  return m.density > 0 && m.Cp > 0;
 }
 
 struct CompMapH {

@@ -500,6 +500,88 @@ __device__ __forceinline__ void jc_voce_3d(const MatParams& mp, R mu, R kappa, c
   for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? d[c] + p : d[c];
 }
 
+// Johnson-Cook with damage, 3D (Material.jl:566-646 with compute_damage,
+// :511-549).  A fully damaged particle (damage >= 1) carries the pressure
+// kappa tr(eps) only and keeps its state.  Otherwise: Johnson-Cook yield of the
+// equivalent plastic strain, its filtered rate and the temperature (thermal
+// softening for Tr <= T < Tm, zero at and above Tm), shear modulus and yield
+// scaled by (1 - damage), radial return as in jc_voce_3d, then the failure
+// strain of the returned stress's triaxiality, rate and temperature, the
+// damage_init / damage update, and the temperature rise delta x flow x dp.
+// The reference method reads mat.damage and mat.strength, fields its type
+// names damage_part and strength_part; this is what those lines compute on
+// the fields they evidently mean.
+template <class R>
+__device__ __forceinline__ void jc_damage_3d(const MatParams& mp, R mu, R kappa, const R* sig_old, const R* deps,
+                                             const R* eps, R* sig, R* alpha, R* alphad, R* vm, R* dinit, R* dam,
+                                             R* temp) {
+  const R damage = *dam;
+  const R pH = kappa * ((eps[0] + eps[1]) + eps[2]);
+  if (damage >= R(1)) {  // Material.jl:572-576
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? pH : R(0);
+    return;
+  }
+  const R ep = *alpha;
+  R T = *temp;
+  R yieldS;
+  if (ep < R(1.0e-10)) {
+    yieldS = R(mp.A);
+  } else if (T < R(mp.Tm)) {
+    const R ratio = fmax(*alphad / R(mp.epsdot0), R(1));
+    const R base = R(mp.A) + R(mp.B) * pow(ep, R(mp.n));
+    yieldS = mp.C != 0.0 ? base * pow(R(1) + ratio, R(mp.C)) : base;
+    if (mp.m != 0.0 && T >= R(mp.Tr)) yieldS *= R(1) - pow((T - R(mp.Tr)) / R(mp.Tmr), R(mp.m));
+  } else {
+    yieldS = R(0);
+  }
+  R Gd = mu;
+  if (damage > R(0)) {
+    Gd *= (R(1) - damage);
+    yieldS *= (R(1) - damage);
+  }
+  R d[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) d[c] = sig_old[c] + R(2) * Gd * deps[c];
+  const R third = R(0.333333333) * ((d[0] + d[1]) + d[2]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) d[c] = d[c] - third;
+  const R q0 = ((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + R(2) * ((d[3] * d[3] + d[5] * d[5]) + d[4] * d[4]);
+  const R J2 = R(1.224744871391589) * sqrt(q0);
+  R dp = R(0);
+  if (!(J2 < yieldS)) {
+    dp = (J2 - yieldS) / (R(3) * Gd);
+    const R sc = yieldS / J2;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) d[c] = d[c] * sc;
+  }
+  *alpha = ep + dp;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? d[c] + pH : d[c];
+  const R tav = R(mp.tav);
+  R ad = *alphad;
+  ad = ad - ad * R(mp.dtime) / tav;
+  ad = ad + dp / tav;
+  ad = fmax(R(0), ad);
+  *alphad = ad;
+  const R q = ((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + R(2) * ((d[3] * d[3] + d[5] * d[5]) + d[4] * d[4]);
+  const R flow = R(1.224744871391589) * sqrt(q);
+  *vm = flow;
+  // compute_damage (Material.jl:511-549), with its own 1.224744871
+  const R vmd = R(1.224744871) * sqrt(q);
+  R triax = R(0);
+  if (pH != R(0) && vmd != R(0)) triax = -pH / (vmd + R(0.01) * fabs(pH));
+  if (triax > R(3)) triax = R(3);
+  R fs = R(mp.d1) + R(mp.d2) * exp(R(mp.d3) * triax);
+  if (mp.d4 > 0.0 && ad > R(mp.depsdot0)) fs *= (R(1) + R(mp.d4) * log(ad / R(mp.depsdot0)));
+  if (mp.d5 > 0.0 && T >= R(mp.Tr)) fs *= R(1) + R(mp.d5) * (T - R(mp.Tr)) / R(mp.Tmr);
+  R di = *dinit + dp / fs;
+  *dinit = di;
+  if (di >= R(1)) *dam = fmin((di - R(1)) * R(10), R(1));
+  T += R(mp.delta) * flow * dp;
+  *temp = T;
+}
+
 // F <- F (I + L dt), J, V = J V0, strain += sym(L dt), update_stress! of particle p
 // (:520-532), given L dt; fin: the particle's new x and v are finite.
 template <int D, class R, int MAT>
@@ -563,6 +645,20 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
     elastic<D, R>(lam, mu, eps, sig);
   } else if (MAT == MPM_MAT_NEOHOOKEAN) {
     neohookean<D, R>(lam, mu, Fn, J, sig);
+  } else if (MAT == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+    if constexpr (D == 3) {
+      R so[6], alpha = *field<R>(pp, L::ALPHA, p), ad = *field<R>(pp, L::ALPHAD, p), vm = *field<R>(pp, L::VM, p);
+      R di = *field<R>(pp, L::DINIT, p), dm = *field<R>(pp, L::DAM, p), T = *field<R>(pp, L::TEMP, p);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) so[c] = *field<R>(pp, L::SIG + c, p);
+      jc_damage_3d<R>(mp, mu, kappa, so, deps, eps, sig, &alpha, &ad, &vm, &di, &dm, &T);
+      *field<R>(pp, L::ALPHA, p) = alpha;
+      *field<R>(pp, L::ALPHAD, p) = ad;
+      *field<R>(pp, L::VM, p) = vm;
+      *field<R>(pp, L::DINIT, p) = di;
+      *field<R>(pp, L::DAM, p) = dm;
+      *field<R>(pp, L::TEMP, p) = T;
+    }
   } else if (MAT == MPM_MAT_JOHNSON_COOK || MAT == MPM_MAT_VOCE) {
     if constexpr (D == 3) {
       R so[6], alpha = *field<R>(pp, L::ALPHA, p), ad = *field<R>(pp, L::ALPHAD, p), vm;

@@ -102,6 +102,9 @@ static inline void with_material(int type, Fn&& f) {
     case MPM_MAT_VOCE:
       if constexpr (D == 3) f(std::integral_constant<int, MPM_MAT_VOCE>{});
       break;
+    case MPM_MAT_JOHNSON_COOK_DAMAGE:
+      if constexpr (D == 3) f(std::integral_constant<int, MPM_MAT_JOHNSON_COOK_DAMAGE>{});
+      break;
     default: f(std::integral_constant<int, MPM_MAT_J2>{}); break;
   }
 }
@@ -238,6 +241,7 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
       case MPM_MAT_NEOHOOKEAN: JMPM_G2P(float, MPM_MAT_NEOHOOKEAN); break;
       case MPM_MAT_JOHNSON_COOK: if constexpr (D == 3) JMPM_G2P(float, MPM_MAT_JOHNSON_COOK); break;
       case MPM_MAT_VOCE: if constexpr (D == 3) JMPM_G2P(float, MPM_MAT_VOCE); break;
+      case MPM_MAT_JOHNSON_COOK_DAMAGE: if constexpr (D == 3) JMPM_G2P(float, MPM_MAT_JOHNSON_COOK_DAMAGE); break;
       default: JMPM_G2P(float, MPM_MAT_J2); break;
     }
   } else {
@@ -246,6 +250,7 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
       case MPM_MAT_NEOHOOKEAN: JMPM_G2P(double, MPM_MAT_NEOHOOKEAN); break;
       case MPM_MAT_JOHNSON_COOK: if constexpr (D == 3) JMPM_G2P(double, MPM_MAT_JOHNSON_COOK); break;
       case MPM_MAT_VOCE: if constexpr (D == 3) JMPM_G2P(double, MPM_MAT_VOCE); break;
+      case MPM_MAT_JOHNSON_COOK_DAMAGE: if constexpr (D == 3) JMPM_G2P(double, MPM_MAT_JOHNSON_COOK_DAMAGE); break;
       default: JMPM_G2P(double, MPM_MAT_J2); break;
     }
   }

@@ -96,6 +96,9 @@ __global__ void __launch_bounds__(256) wide_g2p_kernel(const WideBody* __restric
     case MPM_MAT_VOCE:
       if constexpr (D == 3) g2p_particle<D, R, MPM_MAT_VOCE>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st);
       break;
+    case MPM_MAT_JOHNSON_COOK_DAMAGE:
+      if constexpr (D == 3) g2p_particle<D, R, MPM_MAT_JOHNSON_COOK_DAMAGE>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st);
+      break;
     default: g2p_particle<D, R, MPM_MAT_J2>(sG, sB.nd, sB.pp, t, sB.mp, sDt, st); break;
   }
 }

@@ -60,6 +60,12 @@ class Descriptors:
             b.mat.fy, b.mat.k1 = getattr(m, "fy", 0.0), getattr(m, "k1", 0.0)
             for k in ("A", "B", "C", "n", "epsdot0", "cellsize"):
                 setattr(b.mat, k, float(getattr(m, k, 0.0)))
+            dmg = getattr(m, "damage_part", None)
+            if dmg is not None:  # JohnsonCookMaterialWithDamage
+                b.mat.m, b.mat.chi, b.mat.Cp = m.m, m.chi, m.Cp
+                for k in ("d1", "d2", "d3", "d4", "d5", "Tr", "Tm"):
+                    setattr(b.mat, k, getattr(dmg, k))
+                b.mat.depsdot0 = dmg.epsdot0
             arrs = {
                 "pos": np.ascontiguousarray(sol.pos, dtype=np.float64),
                 "velocity": np.ascontiguousarray(sol.velocity, dtype=np.float64),
@@ -81,6 +87,12 @@ class Descriptors:
             if getattr(m, "alphadot", None) is not None:  # Johnson-Cook / Voce state
                 arrs["alpha"] = np.ascontiguousarray(m.alpha[: sol.parCount], dtype=np.float64)
                 arrs["alphadot"] = np.ascontiguousarray(m.alphadot[: sol.parCount], dtype=np.float64)
+            if getattr(m, "vmStr", None) is not None:
+                arrs["vmstr"] = np.ascontiguousarray(m.vmStr[: sol.parCount], dtype=np.float64)
+            if dmg is not None:
+                arrs["damage_init"] = np.ascontiguousarray(m.damage_init[: sol.parCount], dtype=np.float64)
+                arrs["damage"] = np.ascontiguousarray(m.dam[: sol.parCount], dtype=np.float64)
+                arrs["temperature"] = np.ascontiguousarray(dmg.temp[: sol.parCount], dtype=np.float64)
             for k, v in arrs.items():
                 self._keep.append(v)
                 setattr(b, k, _capi.dptr(v))
@@ -121,10 +133,16 @@ class BodyState:
         self.pstrain = np.zeros(n * (3 if d == 2 else 9))
         self.vmstr = np.zeros(n)
         self.alphadot = np.zeros(n)
+        self.damage_init = np.zeros(n)
+        self.damage = np.zeros(n)
+        self.temperature = np.zeros(n)
+
+    FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot",
+              "damage_init", "damage", "temperature")
 
     def view(self) -> _capi.BodyView:
         v = _capi.BodyView()
-        for k in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot"):
+        for k in self.FIELDS:
             setattr(v, k, _capi.dptr(getattr(self, k)))
         return v
 

@@ -118,6 +118,42 @@ class VoceMaterial(MaterialType):
         self.k1 = 0.0
 
 
+class JohnsonCookDamage:
+    """JohnsonCookDamage(d1,d2,d3,d4,d5,epsdot0,Tr,Tm,parCount), Material.jl:495-509:
+    Johnson-Cook failure strain constants, reference and melting temperatures,
+    and the per-particle temperature ``temp`` (starts at Tr)."""
+
+    def __init__(self, d1, d2, d3, d4, d5, epsdot0, Tr, Tm, parCount):
+        self.d1, self.d2, self.d3, self.d4, self.d5 = (float(d1), float(d2), float(d3), float(d4), float(d5))
+        self.epsdot0, self.Tr, self.Tm = float(epsdot0), float(Tr), float(Tm)
+        self.Tmr = self.Tm - self.Tr
+        self.temp = np.full(int(parCount), self.Tr)
+
+
+class JohnsonCookMaterialWithDamage(MaterialType):
+    """JohnsonCookMaterialWithDamage(strength, damage), Material.jl:551-564; 3D stress
+    update Material.jl:566-646 with compute_damage (:511-549).  State per
+    particle: the strength part's alpha, alphadot and vmStr, ``damage_init``,
+    ``dam`` and the damage part's ``temp``.  The strength part's constants
+    (E, nu, A, B, C, n, ...) are reachable on this object too."""
+    kind = _capi.MPM_MAT_JOHNSON_COOK_DAMAGE
+
+    def __init__(self, strength, damage):
+        if not isinstance(strength, JohnsonCookMaterial) or not isinstance(damage, JohnsonCookDamage):
+            raise TypeError("JohnsonCookMaterialWithDamage(strength::JohnsonCookMaterial, damage::JohnsonCookDamage)")
+        self.strength_part = strength
+        self.damage_part = damage
+        n = len(strength.alpha)
+        self.damage_init = np.zeros(n)
+        self.dam = np.zeros(n)
+        self.density = strength.density
+
+    def __getattr__(self, name):
+        if name in ("strength_part", "damage_part"):
+            raise AttributeError(name)
+        return getattr(self.strength_part, name)
+
+
 class ElastoPlasticMaterial(MaterialType):
     """J2 plasticity with linear hardening, ElastoPlasticMaterial(E,nu,density,fy,k1,parCount),
     Material.jl:128-171.  State per particle: alpha, pstrain (2D Voigt) and pstrain_3D."""

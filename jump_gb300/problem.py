@@ -57,10 +57,14 @@ def write_back(solids, states):
             m.vmStr[:n] = st.vmstr
         elif isinstance(m, ElasticMaterial) and solid.dim == 3:
             m.vmStr[:n] = st.vmstr
-        elif getattr(m, "alphadot", None) is not None:  # Johnson-Cook / Voce
+        elif getattr(m, "alphadot", None) is not None:  # Johnson-Cook / Voce / Johnson-Cook with damage
             m.alpha[:n] = st.alpha
             m.alphadot[:n] = st.alphadot
             m.vmStr[:n] = st.vmstr
+            if getattr(m, "damage_part", None) is not None:
+                m.damage_init[:n] = st.damage_init
+                m.dam[:n] = st.damage
+                m.damage_part.temp[:n] = st.temperature
 
 
 def _solve(dim, grid, solids, basis, alg, output, fixes, data):

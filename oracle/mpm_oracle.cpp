@@ -70,6 +70,9 @@ struct Material {
   // Johnson-Cook / Voce (Material.jl:279-383): hardening constants, cellsize and
   // the signal velocity sqrt((lambda + 2 mu)/density) of the rate filter
   double A = 0, B = 0, C = 0, n = 0, epsdot0 = 0, cellsize = 0, velo = 0;
+  // JohnsonCookMaterialWithDamage (Material.jl:495-564): the strength part's m
+  // and delta = chi/(density*Cp), and the JohnsonCookDamage constants
+  double m = 0, delta = 0, d1 = 0, d2 = 0, d3 = 0, d4 = 0, d5 = 0, depsdot0 = 0, Tr = 0, Tm = 0, Tmr = 0;
 };
 
 Material make_material(const mpm_material_desc& d) {
@@ -91,6 +94,17 @@ Material make_material(const mpm_material_desc& d) {
   m.epsdot0 = d.epsdot0;
   m.cellsize = d.cellsize;
   m.velo = std::sqrt((m.lambda + 2 * m.mu) / m.density);  // Material.jl:317
+  m.m = d.m;
+  m.delta = d.chi / (d.density * d.Cp);  // Material.jl:323
+  m.d1 = d.d1;
+  m.d2 = d.d2;
+  m.d3 = d.d3;
+  m.d4 = d.d4;
+  m.d5 = d.d5;
+  m.depsdot0 = d.depsdot0;
+  m.Tr = d.Tr;
+  m.Tm = d.Tm;
+  m.Tmr = d.Tm - d.Tr;  // Material.jl:507
   return m;
 }
 
@@ -100,6 +114,7 @@ struct Body {
   Material mat;
   std::vector<double> mass, vol0, vol, pos, vel, F, strain, stress;
   std::vector<double> alpha, pstrain, vmstr, youngs, alphadot;
+  std::vector<double> damage_init, dam, temp;  // JohnsonCookMaterialWithDamage state
   bool has_youngs = false;
 };
 
@@ -325,11 +340,110 @@ inline void matmul(const double* A, const double* B, double* C) {
     }
 }
 
+// compute_damage (Material.jl:511-549): damage_init and damage after a plastic
+// strain increment dp, given the pressure pH, the returned stress deviator Sdev
+// (column-major 3x3), the plastic strain rate and the temperature.
+inline void compute_damage(double* damage_init, double* damage, double pH, const double* Sdev, double epsdot,
+                           double dp, double T, const Material& mat) {
+  auto sq = [](double x) { return x * x; };
+  const double vm = 1.224744871 * std::sqrt(sq(Sdev[0]) + sq(Sdev[4]) + sq(Sdev[8]) +
+                                            2 * (sq(Sdev[3]) + sq(Sdev[6]) + sq(Sdev[7])));
+  double triax = 0.0;
+  if (pH != 0.0 && vm != 0.0) triax = -pH / (vm + 0.01 * std::fabs(pH));
+  if (triax > 3.0) triax = 3.0;
+  double jc_failure_strain = mat.d1 + mat.d2 * std::exp(mat.d3 * triax);
+  if (mat.d4 > 0.0) {
+    if (epsdot > mat.depsdot0) {
+      const double epdot_ratio = epsdot / mat.depsdot0;
+      jc_failure_strain *= (1.0 + mat.d4 * std::log(epdot_ratio));
+    }
+  }
+  if (mat.d5 > 0.0 && T >= mat.Tr) jc_failure_strain *= 1. + mat.d5 * (T - mat.Tr) / mat.Tmr;
+  *damage_init += dp / jc_failure_strain;
+  if (*damage_init >= 1.0) *damage = std::min((*damage_init - 1.0) * 10, 1.0);
+}
+
+// update_stress! of JohnsonCookMaterialWithDamage (Material.jl:566-646), 3D,
+// column-major; sig holds the old stress on entry and the new one on exit.
+// The reference method reads mat.damage.Tm, mat.damage.temp (the type's field
+// is damage_part) and dispatches on MMatrix while the solvers pass SMatrix and
+// assign its return value: restated on the fields it evidently means, with
+// the stress returned.
+inline void jc_damage_update(const Material& mat, double mu, double kappa, double* sig, const double* eps0,
+                             const double* strain_increment, double dtime, double* alpha, double* alphadot,
+                             double* vmstr, double* damage_init, double* dam, double* temp) {
+  const double damage = *dam;
+  if (damage >= 1.0) {
+    const double pH = kappa * (eps0[0] + eps0[4] + eps0[8]);
+    for (int k = 0; k < 9; ++k) sig[k] = 0.0;
+    sig[0] = sig[4] = sig[8] = pH;
+    return;
+  }
+  const double eff_plastic_strain = *alpha;
+  double epsdot_ratio = *alphadot / mat.epsdot0;
+  epsdot_ratio = std::max(epsdot_ratio, 1.0);
+  double T = *temp;
+  double yieldStress;
+  if (eff_plastic_strain < 1.0e-10) {
+    yieldStress = mat.A;
+  } else if (T < mat.Tm) {
+    if (mat.C != 0)
+      yieldStress = (mat.A + mat.B * std::pow(eff_plastic_strain, mat.n)) * std::pow(1.0 + epsdot_ratio, mat.C);
+    else
+      yieldStress = mat.A + mat.B * std::pow(eff_plastic_strain, mat.n);
+    if (mat.m != 0 && T >= mat.Tr) yieldStress *= 1.0 - std::pow((T - mat.Tr) / mat.Tmr, mat.m);
+  } else {
+    yieldStress = 0.;
+  }
+  double Gd = mu;
+  if (damage > 0) {
+    Gd *= (1 - damage);
+    yieldStress *= (1 - damage);
+  }
+  double dev[9];
+  for (int k = 0; k < 9; ++k) dev[k] = sig[k] + 2.0 * Gd * strain_increment[k];
+  const double tr = 0.333333333 * (dev[0] + dev[4] + dev[8]);
+  dev[0] -= tr;
+  dev[4] -= tr;
+  dev[8] -= tr;
+  auto sq = [](double x) { return x * x; };
+  const double J2 = 1.224744871391589 * std::sqrt(sq(dev[0]) + sq(dev[4]) + sq(dev[8]) +
+                                                  2 * (sq(dev[3]) + sq(dev[6]) + sq(dev[7])));
+  double dp;
+  if (J2 < yieldStress) {
+    dp = 0.0;
+  } else {
+    dp = (J2 - yieldStress) / (3.0 * Gd);
+    for (int k = 0; k < 9; ++k) dev[k] *= (yieldStress / J2);
+  }
+  *alpha = eff_plastic_strain + dp;
+  const double pH = kappa * (eps0[0] + eps0[4] + eps0[8]);
+  for (int k = 0; k < 9; ++k) sig[k] = dev[k];
+  sig[0] += pH;
+  sig[4] += pH;
+  sig[8] += pH;
+  const double tav = 1000 * mat.cellsize / mat.velo;
+  *alphadot -= *alphadot * dtime / tav;
+  *alphadot += dp / tav;
+  *alphadot = std::max(0.0, *alphadot);
+  const double flow_stress = 1.224744871391589 * std::sqrt(sq(dev[0]) + sq(dev[4]) + sq(dev[8]) +
+                                                          2 * (sq(dev[3]) + sq(dev[6]) + sq(dev[7])));
+  *vmstr = flow_stress;
+  compute_damage(damage_init, dam, pH, dev, *alphadot, dp, T, mat);
+  T += mat.delta * flow_stress * dp;
+  *temp = T;
+}
+
 // update_stress!: returns the new stress in sig (column-major D*D).
 template <int D>
 void update_stress(const Material& mat, double lambda, double mu, double kappa, double* sig,
                    const double* eps, const double* F, double J, double* alpha,
-                   double* pstrain, double* vmstr, const double* deps, double dtime, double* alphadot) {
+                   double* pstrain, double* vmstr, const double* deps, double dtime, double* alphadot,
+                   double* damage_init, double* dam, double* temp) {
+  if (D == 3 && mat.type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+    jc_damage_update(mat, mu, kappa, sig, eps, deps, dtime, alpha, alphadot, vmstr, damage_init, dam, temp);
+    return;
+  }
   if (D == 3 && (mat.type == MPM_MAT_JOHNSON_COOK || mat.type == MPM_MAT_VOCE)) {
     // Material.jl:386-443 (Johnson-Cook), 445-493 (Voce); column-major 3x3
     const double ep = *alpha;
@@ -616,7 +730,8 @@ inline void kin_stress(Body<D>& b, int64_t ip, const double* L, double dt, int* 
   double deps[D * D];  // strain_increment = dtime*D (SolveExplicitSolidMechanics3D.jl:208, 363)
   for (int k = 0; k < D * D; ++k) deps[k] = dt * Dm[k];
   update_stress<D>(b.mat, lambda, mu, kappa, &b.stress[D * D * ip], eps, F, J, &b.alpha[ip],
-                   &b.pstrain[PS * ip], &b.vmstr[ip], deps, dt, &b.alphadot[ip]);
+                   &b.pstrain[PS * ip], &b.vmstr[ip], deps, dt, &b.alphadot[ip], &b.damage_init[ip], &b.dam[ip],
+                   &b.temp[ip]);
   if (!(J > 0.0) && *status == MPM_OK) *status = MPM_ERR_NEGATIVE_J;
 }
 
@@ -1075,8 +1190,13 @@ int create(const mpm_grid_desc* gd, const mpm_body_desc* bd, int nb, const mpm_p
     cp(b.stress, d.stress, D * D, 0.0);
     cp(b.alpha, d.alpha, 1, 0.0);
     cp(b.alphadot, d.alphadot, 1, 0.0);
-    cp(b.pstrain, d.pstrain, PS, 0.0);
-    b.vmstr.assign(b.n, 0.0);
+    const bool dmg = D == 3 && d.mat.type == MPM_MAT_JOHNSON_COOK_DAMAGE;
+    cp(b.pstrain, dmg ? nullptr : d.pstrain, PS, 0.0);
+    // JohnsonCookDamage starts every particle at Tr (Material.jl:507)
+    cp(b.damage_init, dmg ? d.damage_init : nullptr, 1, 0.0);
+    cp(b.dam, dmg ? d.damage : nullptr, 1, 0.0);
+    cp(b.temp, dmg ? d.temperature : nullptr, 1, dmg ? d.mat.Tr : 0.0);
+    cp(b.vmstr, d.vmstr, 1, 0.0);
     b.has_youngs = d.youngs != nullptr;
     if (b.has_youngs) cp(b.youngs, d.youngs, 1, 0.0);
     c->bodies.push_back(std::move(b));
@@ -1140,7 +1260,13 @@ static int download_impl(Ctx<D>* c, int body, const mpm_body_view* v) {
   put(v->strain, b.strain, D * D);
   put(v->stress, b.stress, D * D);
   put(v->alpha, b.alpha, 1);
-  put(v->pstrain, b.pstrain, PS);
+  if (D == 3 && b.mat.type == MPM_MAT_JOHNSON_COOK_DAMAGE) {
+    put(v->damage_init, b.damage_init, 1);
+    put(v->damage, b.dam, 1);
+    put(v->temperature, b.temp, 1);
+  } else {
+    put(v->pstrain, b.pstrain, PS);
+  }
   put(v->vmstr, b.vmstr, 1);
   put(v->alphadot, b.alphadot, 1);
   return MPM_OK;

@@ -10,14 +10,15 @@ from jump_gb300 import _capi
 from jump_gb300.algorithm import USL, ConstantBodyForce2D, ConstantBodyForce3D
 from jump_gb300.engine import Descriptors, colmajor, from_colmajor
 from jump_gb300.grid import Grid2D, Grid3D
-from jump_gb300.material import (ElasticMaterial, ElastoPlasticMaterial, JohnsonCookMaterial, NeoHookeanMaterial,
-                                 VoceMaterial)
+from jump_gb300.material import (ElasticMaterial, ElastoPlasticMaterial, JohnsonCookDamage, JohnsonCookMaterial,
+                                 JohnsonCookMaterialWithDamage, NeoHookeanMaterial, VoceMaterial)
 from jump_gb300.solid import Solid2D, Solid3D
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 
-FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot")
+FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr", "alphadot",
+          "damage_init", "damage", "temperature")
 
 
 def load_golden(name):
@@ -44,6 +45,14 @@ def load_golden(name):
         elif int(typ) == _capi.MPM_MAT_VOCE:
             A, Bh, Ch, nh, e0, cs = z[f"b{b}_matx"]
             mat = VoceMaterial(E, nu, rho, A, Bh, Ch, 0.0, 0.0, cs, n)
+        elif int(typ) == _capi.MPM_MAT_JOHNSON_COOK_DAMAGE:
+            A, Bh, Ch, nh, e0, cs = z[f"b{b}_matx"]
+            m_, chi, Cp, d1, d2, d3, d4, d5, de0, Tr, Tm = z[f"b{b}_matd"]
+            mat = JohnsonCookMaterialWithDamage(JohnsonCookMaterial(E, nu, rho, A, Bh, Ch, nh, e0, m_, chi, Cp, cs, n),
+                                                JohnsonCookDamage(d1, d2, d3, d4, d5, de0, Tr, Tm, n))
+            mat.damage_init[:] = z[f"b{b}_in_dinit"]
+            mat.dam[:] = z[f"b{b}_in_dam"]
+            mat.damage_part.temp[:] = z[f"b{b}_in_temp"]
         else:
             mat = ElastoPlasticMaterial(E, nu, rho, fy, k1, n)
         s = (Solid2D if d == 2 else Solid3D)(pos, mat)
@@ -54,7 +63,7 @@ def load_golden(name):
         s.deformationGradient[:] = from_colmajor(z[f"b{b}_in_F"].ravel(), n, d)
         s.strain[:] = from_colmajor(z[f"b{b}_in_strain"].ravel(), n, d)
         s.stress[:] = from_colmajor(z[f"b{b}_in_stress"].ravel(), n, d)
-        if isinstance(mat, (JohnsonCookMaterial, VoceMaterial)):
+        if isinstance(mat, (JohnsonCookMaterial, VoceMaterial, JohnsonCookMaterialWithDamage)):
             mat.alpha[:] = z[f"b{b}_in_alpha"]
             mat.alphadot[:] = z[f"b{b}_in_alphadot"]
         if isinstance(mat, ElastoPlasticMaterial):
@@ -93,6 +102,10 @@ def golden_expected(z, b):
     }
     if f"b{b}_out_alphadot" in z:
         out["alphadot"] = z[f"b{b}_out_alphadot"]
+    if f"b{b}_out_dinit" in z:
+        out["damage_init"] = z[f"b{b}_out_dinit"]
+        out["damage"] = z[f"b{b}_out_dam"]
+        out["temperature"] = z[f"b{b}_out_temp"]
     return out
 
 

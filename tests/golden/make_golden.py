@@ -259,11 +259,91 @@ def det(A, d):
     return x0[0] * cr[0] + x0[1] * cr[1] + x0[2] * cr[2]
 
 
+def jc_failure(mat, damage_init, damage, pH, Sdev, epsdot, dp, T):
+    """compute_damage, Material.jl:511-549: (damage_init, damage) after a plastic
+    strain increment dp."""
+    vm = 1.224744871 * math.sqrt(Sdev[0] * Sdev[0] + Sdev[4] * Sdev[4] + Sdev[8] * Sdev[8] +
+                                 2 * (Sdev[3] * Sdev[3] + Sdev[6] * Sdev[6] + Sdev[7] * Sdev[7]))
+    triax = 0.0
+    if pH != 0.0 and vm != 0.0:
+        triax = -pH / (vm + 0.01 * abs(pH))
+    if triax > 3.0:
+        triax = 3.0
+    fs = mat["d1"] + mat["d2"] * math.exp(mat["d3"] * triax)
+    if mat["d4"] > 0.0 and epsdot > mat["depsdot0"]:
+        fs *= (1.0 + mat["d4"] * math.log(epsdot / mat["depsdot0"]))
+    if mat["d5"] > 0.0 and T >= mat["Tr"]:
+        fs *= 1. + mat["d5"] * (T - mat["Tr"]) / (mat["Tm"] - mat["Tr"])
+    damage_init += dp / fs
+    if damage_init >= 1.0:
+        damage = min((damage_init - 1.0) * 10, 1.0)
+    return damage_init, damage
+
+
+def jc_damage_stress(mat, sig, eps, state):
+    """update_stress! of JohnsonCookMaterialWithDamage, Material.jl:566-646, on the
+    fields the method means (damage_part, strength_part), returning the stress."""
+    lam, mu, kappa = mat["lambda"], mat["mu"], mat["kappa"]
+    damage = state["dam"]
+    if damage >= 1.0:
+        pH = kappa * (eps[0] + eps[4] + eps[8])
+        return [pH, 0.0, 0.0, 0.0, pH, 0.0, 0.0, 0.0, pH]
+    ep = state["alpha"]
+    ratio = max(state["alphadot"] / mat["epsdot0"], 1.0)
+    T = state["temp"]
+    if ep < 1.0e-10:
+        ys = mat["A"]
+    elif T < mat["Tm"]:
+        if mat["C"] != 0:
+            ys = (mat["A"] + mat["B"] * ep ** mat["n"]) * (1.0 + ratio) ** mat["C"]
+        else:
+            ys = mat["A"] + mat["B"] * ep ** mat["n"]
+        if mat["m"] != 0 and T >= mat["Tr"]:
+            ys *= 1.0 - ((T - mat["Tr"]) / (mat["Tm"] - mat["Tr"])) ** mat["m"]
+    else:
+        ys = 0.
+    Gd = mu
+    if damage > 0:
+        Gd *= (1 - damage)
+        ys *= (1 - damage)
+    trial = [sig[k] + 2.0 * Gd * state["deps"][k] for k in range(9)]
+    third = 0.333333333 * (trial[0] + trial[4] + trial[8])
+    dev = list(trial)
+    for k in (0, 4, 8):
+        dev[k] = trial[k] - third
+    J2 = 1.224744871391589 * math.sqrt(dev[0] * dev[0] + dev[4] * dev[4] + dev[8] * dev[8] +
+                                       2 * (dev[3] * dev[3] + dev[6] * dev[6] + dev[7] * dev[7]))
+    if J2 < ys:
+        dp = 0.0
+    else:
+        dp = (J2 - ys) / (3.0 * Gd)
+        dev = [x * (ys / J2) for x in dev]
+    state["alpha"] = ep + dp
+    pH = kappa * (eps[0] + eps[4] + eps[8])
+    out = list(dev)
+    for k in (0, 4, 8):
+        out[k] = dev[k] + pH
+    tav = 1000 * mat["cellsize"] / math.sqrt((lam + 2 * mu) / mat["density"])
+    ad = state["alphadot"]
+    ad -= ad * state["dt"] / tav
+    ad += dp / tav
+    state["alphadot"] = max(0.0, ad)
+    flow = 1.224744871391589 * math.sqrt(dev[0] * dev[0] + dev[4] * dev[4] + dev[8] * dev[8] +
+                                         2 * (dev[3] * dev[3] + dev[6] * dev[6] + dev[7] * dev[7]))
+    state["vm"] = flow
+    state["dinit"], state["dam"] = jc_failure(mat, state["dinit"], state["dam"], pH, dev, state["alphadot"], dp, T)
+    T += mat["chi"] / (mat["density"] * mat["Cp"]) * flow * dp
+    state["temp"] = T
+    return out
+
+
 def stress_update(mat, d, sig, eps, F, J, state):
     """update_stress! for one particle; returns the new stress (column-major).
     state carries alpha, ep, vm and, for Johnson-Cook/Voce, alphadot, the strain
     increment deps = dt D and dt."""
     typ, lam, mu = mat["type"], mat["lambda"], mat["mu"]
+    if typ == 5:  # JohnsonCookMaterialWithDamage (3D)
+        return jc_damage_stress(mat, sig, eps, state)
     if typ in (3, 4):  # JohnsonCookMaterial / VoceMaterial, Material.jl:386-493 (3D)
         ep = state["alpha"]
         if ep < 1.0e-10:
@@ -466,10 +546,12 @@ def usl_steps(case, nsteps):
                     m2["mu"] = E / 2 / (1 + nu)
                     m2["kappa"] = m2["lambda"] + m2["mu"]
                 state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip],
-                         "alphadot": B["alphadot"][ip], "deps": [dt * x for x in D_], "dt": dt}
+                         "alphadot": B["alphadot"][ip], "deps": [dt * x for x in D_], "dt": dt,
+                         "dinit": B["dinit"][ip], "dam": B["dam"][ip], "temp": B["temp"][ip]}
                 B["stress"][ip] = stress_update(m2, d, B["stress"][ip], B["strain"][ip], F, J, state)
                 B["alpha"][ip], B["ep"][ip], B["vm"][ip] = state["alpha"], state["ep"], state["vm"]
                 B["alphadot"][ip] = state["alphadot"]
+                B["dinit"][ip], B["dam"][ip], B["temp"][ip] = state["dinit"], state["dam"], state["temp"]
     case["grid_out"] = (mass, mom0, mom, force)
     return case
 
@@ -493,10 +575,12 @@ def _kinematics(B, ip, L, d, dt):
         m2["mu"] = E / 2 / (1 + nu)
         m2["kappa"] = m2["lambda"] + m2["mu"]
     state = {"alpha": B["alpha"][ip], "ep": B["ep"][ip], "vm": B["vm"][ip],
-             "alphadot": B["alphadot"][ip], "deps": [dt * x for x in D_], "dt": dt}
+             "alphadot": B["alphadot"][ip], "deps": [dt * x for x in D_], "dt": dt,
+             "dinit": B["dinit"][ip], "dam": B["dam"][ip], "temp": B["temp"][ip]}
     B["stress"][ip] = stress_update(m2, d, B["stress"][ip], B["strain"][ip], F, J, state)
     B["alpha"][ip], B["ep"][ip], B["vm"][ip] = state["alpha"], state["ep"], state["vm"]
     B["alphadot"][ip] = state["alphadot"]
+    B["dinit"][ip], B["dam"][ip], B["temp"][ip] = state["dinit"], state["dam"], state["temp"]
 
 
 def _cholesky_solve_band(A, n, w, rhs):
@@ -659,6 +743,12 @@ def case_from_objects(grid, solids, alg, data, nsteps, basis=0):
         for k in ("A", "B", "C", "n", "epsdot0", "cellsize"):
             mat[k] = float(getattr(m, k, 0.0))
         n = s.parCount
+        dinit, dam, temp = np.zeros(n), np.zeros(n), np.zeros(n)
+        dp_ = getattr(m, "damage_part", None)
+        if dp_ is not None:
+            mat.update(m=m.m, chi=m.chi, Cp=m.Cp, d1=dp_.d1, d2=dp_.d2, d3=dp_.d3, d4=dp_.d4, d5=dp_.d5,
+                       depsdot0=dp_.epsdot0, Tr=dp_.Tr, Tm=dp_.Tm)
+            dinit, dam, temp = m.damage_init[:n].copy(), m.dam[:n].copy(), dp_.temp[:n].copy()
         ps = 3 if d == 2 else 9
         ep = np.zeros((n, ps))
         alpha = np.zeros(n)
@@ -679,6 +769,7 @@ def case_from_objects(grid, solids, alg, data, nsteps, basis=0):
             "stress": [list(map(float, r)) for r in colmajor(s.stress).reshape(n, d * d)],
             "alpha": list(map(float, alpha)), "ep": [list(map(float, r)) for r in ep],
             "vm": [0.0] * n, "alphadot": list(map(float, alphadot)),
+            "dinit": list(map(float, dinit)), "dam": list(map(float, dam)), "temp": list(map(float, temp)),
             "youngs": None if s.youngs is None else list(map(float, s.youngs)),
         })
     musl = hasattr(alg, "alpha")
@@ -714,6 +805,12 @@ def save_case(name, case_in, case_out):
             arrs[f"b{b}_in_youngs"] = np.array(Bi["youngs"], dtype=np.float64)
         for k in ("pos", "vel", "vol", "F", "strain", "stress", "alpha", "ep", "vm", "alphadot"):
             arrs[f"b{b}_out_{k}"] = np.array(Bo[k], dtype=np.float64)
+        if m["type"] == 5:  # Johnson-Cook with damage: its constants and state
+            arrs[f"b{b}_matd"] = np.array([m[k] for k in ("m", "chi", "Cp", "d1", "d2", "d3", "d4", "d5",
+                                                          "depsdot0", "Tr", "Tm")])
+            for k in ("dinit", "dam", "temp"):
+                arrs[f"b{b}_in_{k}"] = np.array(Bi[k], dtype=np.float64)
+                arrs[f"b{b}_out_{k}"] = np.array(Bo[k], dtype=np.float64)
     mass, mom0, mom, force = case_out["grid_out"]
     arrs["grid_mass"] = np.array(mass)
     arrs["grid_momentum0"] = np.array(mom0)
@@ -825,6 +922,29 @@ def main(only=None):
         scenarios.apply_dirichlet(g, data)
         algo = USL(1e-3 * float(s[0].mass[0])) if kind == "jc" else MUSL(0.99)
         cases[f"taylor_mini_{kind}_10"] = case_from_objects(g, s, algo, data, 10)
+
+    # 9. Johnson-Cook with damage (USL and MUSL 0.99): copper strength with a
+    #    small failure strain and a melting point just above Tr, so that within
+    #    a few steps particles initiate damage, fail completely, soften thermally
+    #    and pass Tm
+    from jump_gb300.material import JohnsonCookDamage, JohnsonCookMaterialWithDamage
+    for scheme, steps, d1, d2, Tm in (("usl", 12, 0.002, 0.004, 294.0), ("musl", 10, 0.0002, 0.0004, 293.02)):
+        g, s, alg, data = scenarios.taylor_bar(h=1e-3, radius=2e-3, length=6e-3, width=8e-3, height=10e-3,
+                                               gap=0.0, speed=300.0)
+        n = s[0].parCount
+        st = JohnsonCookMaterial(115e9, 0.31, 8940.0, 65e6, 356e6, 0.013, 0.37, 1e-3, 1.09, 0.9, 383.0, 1e-3, n)
+        s[0].mat = JohnsonCookMaterialWithDamage(st, JohnsonCookDamage(d1, d2, -0.54, 0.015, 0.2, 1e-3,
+                                                                       293.0, Tm, n))
+        # seeded starting states: every 5th particle above Tm, every 7th with damage
+        # initiated (damage_init 0.5), every 11th partly damaged (damage 0.3)
+        m = s[0].mat
+        m.damage_part.temp[::5] = Tm + 1.0
+        m.damage_init[::7] = 0.5
+        m.damage_init[::11] = 1.03
+        m.dam[::11] = 0.3
+        scenarios.apply_dirichlet(g, data)
+        algo = USL(1e-3 * float(s[0].mass[0])) if scheme == "usl" else MUSL(0.99)
+        cases[f"taylor_mini_jcdamage_{scheme}_{steps}"] = case_from_objects(g, s, algo, data, steps)
 
     # 8. B-spline bases: the two-disk collision with quadratic B-splines and USL
     #    (Main_TwoDisks.jl:53, 116); 3D neo-Hookean spheres with cubic B-splines

@@ -1,7 +1,8 @@
-"""Johnson-Cook and Voce materials (3D) on the GPU against the oracle: USL and
-MUSL Taylor bars that yield, the FP32 variant's stated bound, batched
-problems under both strategies, the plastic-strain-rate state round trip,
-and the 2D rejection."""
+"""Johnson-Cook, Voce and Johnson-Cook-with-damage materials (3D) on the GPU
+against the oracle: USL and MUSL Taylor bars that yield (and, with damage,
+fail), the FP32 variant's stated bound, batched problems under both
+strategies, the state round trips, the solver entry point, and the
+rejections (2D; damage without a heat capacity)."""
 import ctypes as C
 
 import numpy as np
@@ -11,7 +12,8 @@ from cases import descriptors, field_errors
 from jump_gb300 import _capi, scenarios
 from jump_gb300.batch import Ensemble
 from jump_gb300.engine import MPMContext
-from jump_gb300.material import JohnsonCookMaterial, VoceMaterial
+from jump_gb300.material import (JohnsonCookDamage, JohnsonCookMaterial, JohnsonCookMaterialWithDamage,
+                                 VoceMaterial)
 
 pytestmark = pytest.mark.gpu
 
@@ -101,3 +103,135 @@ def test_jc_rejected_in_2d():
     L = _capi.lib()
     h = C.c_void_p()
     assert L.mpm_create(C.byref(d.grid), d.bodies, d.nbodies, C.byref(d.params), C.byref(h)) == _capi.MPM_ERR_ARG
+
+
+# ---------------------------------------------------------------------------
+# The plastic strain increment dp = (J2 - yield) / (3 G (1 - damage)) subtracts
+# nearly equal stresses and divides by the degraded shear modulus, so rounding
+# differences (the B-spline P2G's atomics add in a run-dependent order: ~1e-16 in
+# positions) reach ~1e-10 relative in the plastic state of nearly failed
+# particles; kinematics and stress stay within FP64_TOL.
+KINEMATIC = ("pos", "velocity", "volume", "F", "strain", "stress")
+DAMAGE_STATE = ("alpha", "alphadot", "vmstr", "damage_init", "damage", "temperature")
+DAMAGE_STATE_TOL = 1e-8
+
+# Johnson-Cook with damage: copper strength, a small failure strain and a
+# melting point 1 K above Tr; seeded starting states put some particles above
+# Tm, some with damage initiated and some partly damaged, so every branch of
+# the update runs.
+def taylor_damage(speed=300.0, Tm=294.0, d1=0.002, d2=0.004):
+    g, s, alg, data = scenarios.taylor_bar(h=1e-3, radius=2e-3, length=6e-3, width=8e-3, height=10e-3,
+                                           speed=speed)
+    n = s[0].parCount
+    st = JohnsonCookMaterial(115e9, 0.31, 8940.0, 65e6, 356e6, 0.013, 0.37, 1e-3, 1.09, 0.9, 383.0, 1e-3, n)
+    m = JohnsonCookMaterialWithDamage(st, JohnsonCookDamage(d1, d2, -0.54, 0.015, 0.2, 1e-3, 293.0, Tm, n))
+    m.damage_part.temp[::5] = Tm + 1.0
+    m.damage_init[::7] = 0.5
+    m.damage_init[::11] = 1.03
+    m.dam[::11] = 0.3
+    s[0].mat = m
+    scenarios.apply_dirichlet(g, data)
+    return g, s, alg, data
+
+
+@pytest.mark.parametrize("basis", ["linear", "quad"])
+@pytest.mark.parametrize("scheme", ["usl", "musl"])
+def test_jc_damage_vs_oracle(scheme, basis, oracle_lib):
+    g, s, alg, data = taylor_damage()
+    kw = {"algorithm": "musl", "alpha": 0.99} if scheme == "musl" else {}
+    mk = lambda: descriptors(g, s, alg.tolerance, data.get("bodyforce"), data["dt"], basis=basis, **kw)
+    dg, do = MPMContext(mk()), oracle_lib.OracleContext(mk())
+    dg.step(60)
+    do.step(60)
+    so = do.download_all()
+    dm = so[0].damage
+    assert (dm == 1.0).sum() > 0 and ((dm > 0) & (dm < 1)).sum() > 0, "particles must fail and partly fail"
+    assert (so[0].damage_init > s[0].mat.damage_init).sum() > 0 and so[0].temperature.max() > 294.0
+    sg = dg.download_all()
+    errs = field_errors(sg, so, fields=KINEMATIC)
+    assert max(errs.values()) <= FP64_TOL, worst(errs)
+    errs = field_errors(sg, so, fields=DAMAGE_STATE)
+    assert max(errs.values()) <= DAMAGE_STATE_TOL, worst(errs)
+
+
+def test_jc_damage_fp32_bound(oracle_lib):
+    g, s, alg, data = taylor_damage()
+    mk = lambda **k: descriptors(g, s, alg.tolerance, data.get("bodyforce"), data["dt"], **k)
+    d32, do = MPMContext(mk(precision="f32")), oracle_lib.OracleContext(mk())
+    d32.step(60)
+    do.step(60)
+    errs = field_errors(d32.download_all(), do.download_all(), fields=("pos", "velocity", "F", "damage"))
+    assert max(errs.values()) <= 2e-3, worst(errs)  # stated FP32 bound, damaged Taylor bar
+
+
+@pytest.mark.parametrize("strategy", ["persistent", "wide"])
+def test_jc_damage_batch_matches_single(strategy):
+    probs = [taylor_damage(speed=v) for v in (200.0, 300.0, 400.0)]
+    ens = Ensemble(probs)
+    ens.set_strategy(strategy)
+    ens.step(40)
+    for i, (g, s, alg, data) in enumerate(probs):
+        c = MPMContext(descriptors(g, s, alg.tolerance, data.get("bodyforce"), data["dt"]))
+        c.step(40)
+        got, exp = ens.download(i), c.download_all()
+        errs = field_errors(got, exp, fields=KINEMATIC)
+        assert max(errs.values()) <= FP64_TOL, (i, worst(errs))
+        errs = field_errors(got, exp, fields=DAMAGE_STATE)
+        assert max(errs.values()) <= DAMAGE_STATE_TOL, (i, worst(errs))
+
+
+def test_jc_damage_state_round_trip():
+    """damage_init, damage and temperature (with alpha/alphadot/vmStr) written back
+    into the material after 30 steps and uploaded into a fresh context continue
+    exactly like 60 uninterrupted steps."""
+    import copy
+    from jump_gb300.problem import write_back
+    g, s, alg, data = taylor_damage()
+    mk = lambda sols: descriptors(g, sols, alg.tolerance, data.get("bodyforce"), data["dt"])
+    a = MPMContext(mk(s))
+    a.step(30)
+    s2 = copy.deepcopy(s)
+    write_back(s2, [a.download_body(0)])
+    assert (s2[0].mat.dam == 1.0).sum() > 0 and s2[0].mat.damage_part.temp.max() > 294.0
+    b = MPMContext(mk(s2))
+    a.step(30)
+    b.step(30)
+    sa, sb = a.download_all(), b.download_all()
+    errs = field_errors(sb, sa, fields=KINEMATIC)
+    assert max(errs.values()) <= 1e-12, worst(errs)
+    errs = field_errors(sb, sa, fields=DAMAGE_STATE)
+    assert max(errs.values()) <= 1e-10, worst(errs)
+
+
+def test_jc_damage_solver_entry(oracle_lib):
+    """solve_explicit_dynamics_3D with JohnsonCookMaterialWithDamage: the
+    material's damage_init, dam and damage_part.temp are updated in place."""
+    from jump_gb300 import EmptyOutput, LinearBasis, solve_explicit_dynamics_3D
+    from jump_gb300.problem import step_times
+    g, s, alg, data = taylor_damage()
+    data["total_time"] = 20 * data["dt"]
+    o = oracle_lib.OracleContext(descriptors(g, s, alg.tolerance, data.get("bodyforce"), data["dt"]))
+    o.step(len(step_times(data.get("time", 0.0), data["total_time"], data["dt"])))
+    solve_explicit_dynamics_3D(g, s, LinearBasis(), alg, EmptyOutput(1000), [], data)
+    st = o.download_all()[0]
+    m = s[0].mat
+    for got, exp in ((s[0].pos, st.pos), (m.damage_init, st.damage_init), (m.dam, st.damage),
+                     (m.damage_part.temp, st.temperature), (m.alpha, st.alpha)):
+        assert np.max(np.abs(got - exp)) <= 1e-10 * max(1.0, np.max(np.abs(exp)))
+
+
+def test_jc_damage_rejected_in_2d_and_without_heat_capacity():
+    L = _capi.lib()
+    h = C.c_void_p()
+    grid, solids, alg, data = scenarios.two_disks(nodes=11)
+    scenarios.apply_dirichlet(grid, data)
+    n = solids[0].parCount
+    st = JohnsonCookMaterial(1e3, 0.3, 1000.0, 1.0, 1.0, 0.0, 0.5, 1e-3, 0.0, 0.9, 400.0, 0.05, n)
+    solids[0].mat = JohnsonCookMaterialWithDamage(st, JohnsonCookDamage(0.1, 0.1, 0.0, 0.0, 0.0, 1e-3, 293.0, 900.0, n))
+    d = descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"])
+    assert L.mpm_create(C.byref(d.grid), d.bodies, d.nbodies, C.byref(d.params), C.byref(h)) == _capi.MPM_ERR_ARG
+    g, s, alg, data = taylor_damage()
+    s[0].mat.strength_part.Cp = 0.0
+    d = descriptors(g, s, alg.tolerance, data.get("bodyforce"), data["dt"])
+    assert L.mpm_create(C.byref(d.grid), d.bodies, d.nbodies, C.byref(d.params), C.byref(h)) == _capi.MPM_ERR_ARG
+    assert b"Cp" in L.mpm_last_error()
