@@ -173,6 +173,17 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
    *t_inout += dt once per step, in FP64, exactly like `t += dtime` (:580). */
 int mpm_step(mpm_ctx* ctx, int64_t nsteps, double* t_inout);
 
+/* nsteps steps as mpm_step, with the EnergiesFix sums (Fix.jl:248-270;
+   mpm_energies) taken after local steps first, first + every, first + 2 every,
+   ... < nsteps -- the hook schedule `counter % interval == 0` of
+   SolveExplicitSolidMechanics2D.jl:574-578 when first = (-counter0) mod every.
+   Record r goes to out[(2 + dim) r ...]: kinetic energy, strain energy, momentum
+   (dim).  Every record is copied to pinned host memory as soon as its sums are
+   formed, with no host synchronisation between steps; the call returns after
+   the last step, like mpm_step.  out may be any host memory
+   ((nsteps - 1 - first)/every + 1 records when nsteps > first). */
+int mpm_step_energies(mpm_ctx* ctx, int64_t nsteps, int64_t every, int64_t first, double* t_inout, double* out);
+
 /* Copy one body's particle state back into caller-owned host arrays
    (original particle order, the layouts of mpm_body_desc). */
 int mpm_download(mpm_ctx* ctx, int32_t body, const mpm_body_view* out);

@@ -184,6 +184,7 @@ SIGNATURES = {
     "mpm_create": (C.c_int, [C.POINTER(GridDesc), C.POINTER(BodyDesc), C.c_int32,
                              C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "mpm_step": (C.c_int, [C.c_void_p, C.c_int64, _dp]),
+    "mpm_step_energies": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, _dp, C.c_void_p]),
     "mpm_download": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(BodyView)]),
     "mpm_download_grid": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
     "mpm_energies": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),

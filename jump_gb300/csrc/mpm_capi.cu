@@ -105,6 +105,8 @@ struct mpm_ctx {
   double* red = nullptr;
   double* staging = nullptr;
   size_t staging_n = 0;
+  double* rec_host = nullptr;   // pinned EnergiesFix records of mpm_step_energies
+  int64_t rec_cap = 0;          // records it holds
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaGraph_t graph[2] = {nullptr, nullptr};       // one step, per physical buffer
@@ -133,6 +135,7 @@ namespace {
 
 void destroy_ctx(mpm_ctx* c) {
   if (!c) return;
+  cudaFreeHost(c->rec_host);
   for (int i = 0; i < 2; ++i) {
     if (c->exec[i]) cudaGraphExecDestroy(c->exec[i]);
     if (c->graph[i]) cudaGraphDestroy(c->graph[i]);
@@ -688,6 +691,55 @@ int mpm_step(mpm_ctx* c, int64_t nsteps, double* t_inout) {
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
   c->last_ms = ms;
+  return status_to_code(st);
+}
+
+int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, double* t_inout, double* out) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_step_energies: null context");
+  if (nsteps < 0 || every < 1 || first < 0)
+    return fail(MPM_ERR_ARG, "mpm_step_energies: nsteps < 0, every < 1 or first < 0");
+  const int D = c->dim;
+  const int64_t nrec = nsteps > first ? (nsteps - 1 - first) / every + 1 : 0;
+  if (nrec > 0 && !out) return fail(MPM_ERR_ARG, "mpm_step_energies: null output");
+  if (nrec > c->rec_cap) {
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    CUDA_TRY(cudaFreeHost(c->rec_host));
+    c->rec_host = nullptr;
+    c->rec_cap = 0;
+    CUDA_TRY(cudaHostAlloc(&c->rec_host, size_t(nrec) * (2 + D) * sizeof(double), cudaHostAllocDefault));
+    c->rec_cap = nrec;
+  }
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  CUDA_TRY(cudaEventRecord(c->e0, c->stream));
+  int64_t j = 0;
+  for (int64_t k = 0; k < nsteps; ++k) {
+    int r;
+    if (c->Palt && c->since_sort >= c->prm.sort_interval && (r = enqueue_sort(c))) return r;
+    if ((r = build_step_graph(c))) return r;
+    CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
+    ++c->since_sort;
+    if (t_inout) *t_inout += c->prm.dt;
+    if (k >= first && (k - first) % every == 0) {
+      double* dst = c->rec_host + size_t(j) * (2 + D);
+      if (c->np > 0) {
+        if (D == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, c->red);
+        else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, c->red);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(dst, c->red, (2 + D) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      } else {
+        for (int q = 0; q < 2 + D; ++q) dst[q] = 0.0;
+      }
+      ++j;
+    }
+  }
+  CUDA_TRY(cudaEventRecord(c->e1, c->stream));
+  unsigned st = 0;
+  CUDA_TRY(cudaMemcpyAsync(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  c->last_ms = ms;
+  if (nrec > 0) std::memcpy(out, c->rec_host, size_t(nrec) * (2 + D) * sizeof(double));
   return status_to_code(st);
 }
 

@@ -193,6 +193,19 @@ class MPMContext(_ContextBase):
             _capi.check(rc, self.L)
         return tt.value if t is not None else rc
 
+    def step_energies(self, nsteps: int, every: int = 1, first: int = 0, t: float | None = None,
+                      check: bool = True):
+        """nsteps steps with the EnergiesFix sums after local steps first, first + every, ...;
+        returns (records, t or status): records is (n, 2 + dim) = [KE, SE, momentum...]."""
+        nrec = (nsteps - 1 - first) // every + 1 if nsteps > first else 0
+        out = np.zeros((max(nrec, 0), 2 + self.dim))
+        tt = C.c_double(0.0 if t is None else t)
+        rc = self.L.mpm_step_energies(self.h, int(nsteps), int(every), int(first), C.byref(tt),
+                                      _capi.dptr(out) if nrec > 0 else None)
+        if check:
+            _capi.check(rc, self.L)
+        return out, (tt.value if t is not None else rc)
+
     def _download(self, s, view):
         _capi.check(self.L.mpm_download(self.h, int(s), C.byref(view)), self.L)
 

@@ -27,6 +27,9 @@ from .fix import EnergiesFix, as_list, closeFile
 from .material import ElastoPlasticMaterial, ElasticMaterial
 
 
+HOOK_CHUNK = 4096  # EnergiesFix records per mpm_step_energies call
+
+
 def step_times(t: float, Tf: float, dt: float):
     """The `t` of every iteration of `while t < Tf ... t += dtime` (:373, :580)."""
     ts = []
@@ -102,7 +105,24 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
         done = 0
         nsteps = len(times)
         states = None  # host arrays of the downloads, reused from hook to hook
+        efix = [f for f in fl if isinstance(f, EnergiesFix)]
         while done < nsteps:
+            if not need_particles:
+                # no hook reads particle arrays: the remaining steps in calls of at most
+                # HOOK_CHUNK hooks, the EnergiesFix sums of each hook step copied back
+                # as they form, with no host round trip between steps
+                first = (-done) % interval
+                run = min(nsteps - done, first + HOOK_CHUNK * interval)
+                if efix:
+                    recs, _ = ctx.step_energies(run, interval, first)
+                    for j, r in enumerate(recs):
+                        th = times[done + first + j * interval]
+                        for f in efix:
+                            f.record(th, r[0], r[1])
+                else:
+                    ctx.step(run)
+                done += run
+                continue
             # next hook step: the first counter >= done with counter % interval == 0
             nxt = ((done + interval - 1) // interval) * interval
             run = min(nsteps, nxt + 1) - done
@@ -111,17 +131,11 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
             counter = done - 1
             if counter % interval == 0:
                 th = times[counter]
-                if need_particles:
-                    states = ctx.download_all(states)
-                    write_back(solids, states)
-                    output.plot(solids, lims, ncells, counter)
-                    for f in fl:
-                        f.compute(th)
-                else:
-                    ke, se, _ = ctx.energies()
-                    for f in fl:
-                        if isinstance(f, EnergiesFix):
-                            f.record(th, ke, se)
+                states = ctx.download_all(states)
+                write_back(solids, states)
+                output.plot(solids, lims, ncells, counter)
+                for f in fl:
+                    f.compute(th)
         write_back(solids, ctx.download_all(states))
         m, p0, p, f = ctx.download_grid(grid.nodeCount)
         grid.mass[:] = m

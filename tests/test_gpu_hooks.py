@@ -1,0 +1,73 @@
+"""EnergiesFix sums taken inside a multi-step call (mpm_step_energies) against
+the same sums taken between single steps and against the oracle, and the
+solver's hook schedule (counter % interval == 0) when no hook reads particle
+arrays."""
+import numpy as np
+import pytest
+
+from cases import descriptors, field_errors
+from jump_gb300 import EmptyOutput, EnergiesFix, LinearBasis, scenarios, solve_explicit_dynamics_2D
+from jump_gb300.engine import MPMContext
+from jump_gb300.problem import step_times
+
+pytestmark = pytest.mark.gpu
+
+
+def disks():
+    grid, solids, alg, data = scenarios.two_disks(nodes=21)
+    scenarios.apply_dirichlet(grid, data)
+    return grid, solids, alg, data
+
+
+@pytest.mark.parametrize("every,first", [(1, 0), (3, 1), (5, 4)])
+def test_step_energies_matches_step_then_energies(every, first):
+    grid, solids, alg, data = disks()
+    mk = lambda: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"])
+    a, b = MPMContext(mk()), MPMContext(mk())
+    n = 25
+    recs, t = a.step_energies(n, every, first, t=0.5)
+    assert t == pytest.approx(0.5 + n * data["dt"], abs=1e-15)
+    want = []
+    for k in range(n):
+        b.step(1)
+        if k >= first and (k - first) % every == 0:
+            ke, se, mom = b.energies()
+            want.append([ke, se, *mom])
+    want = np.array(want)
+    assert recs.shape == want.shape == ((n - 1 - first) // every + 1, 4)
+    assert np.max(np.abs(recs - want)) <= 1e-12 * np.max(np.abs(want))
+    errs = field_errors(a.download_all(), b.download_all())
+    assert max(errs.values()) <= 1e-12, errs
+
+
+def test_step_energies_without_records():
+    grid, solids, alg, data = disks()
+    c = MPMContext(descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"]))
+    recs, _ = c.step_energies(3, 2, 5)
+    assert recs.shape == (0, 4)
+
+
+@pytest.mark.parametrize("interval", [1, 7])
+def test_solver_energies_fix_vs_oracle(interval, oracle_lib, tmp_path):
+    grid, solids, alg, data = disks()
+    data["total_time"] = 0.06
+    o = oracle_lib.OracleContext(descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"]))
+    times = step_times(data["time"], data["total_time"], data["dt"])
+    want_t, want = [], []
+    for c in range(len(times)):
+        o.step(1)
+        if c % interval == 0:
+            ke, se, _ = o.energies()
+            want_t.append(times[c])
+            want.append((ke, se))
+    fix = EnergiesFix(solids, str(tmp_path / "energies.txt"))
+    solve_explicit_dynamics_2D(grid, solids, LinearBasis(), alg, EmptyOutput(interval), [fix], data)
+    assert fix.recordTime == want_t
+    got = np.array([fix.kinEnergy, fix.strEnergy]).T
+    want = np.array(want)
+    assert np.max(np.abs(got - want)) <= 1e-10 * np.max(np.abs(want))
+    lines = open(tmp_path / "energies.txt").read().splitlines()
+    assert len(lines) == len(want_t)
+    assert float(lines[-1].split()[0]) == want_t[-1]
+    for s, st in zip(solids, o.download_all()):
+        assert np.max(np.abs(s.pos - st.pos)) <= 1e-12
