@@ -154,23 +154,9 @@ def workload(name: str, material: str = "j2"):
     from jump_gb300 import scenarios
     if name == "taylor_bar":
         g, s, alg, data = scenarios.taylor_bar()
-        label = "J2 linear hardening"
-        if material == "jc":
-            # the Johnson-Cook copper of the reference's Taylor-bar driver (Main_TaylorBar.jl:43-56), SI units
-            from jump_gb300.material import JohnsonCookMaterial
-            s[0].mat = JohnsonCookMaterial(115e9, 0.31, 8940.0, 65e6, 356e6, 0.0, 0.37, 1e-3, 0.0, 0.0, 0.0,
-                                           2.5e-4, s[0].parCount)
-            label = "Johnson-Cook (A 65 MPa, B 356 MPa, n 0.37, C 0)"
-        elif material == "jcdamage":
-            # the steel of the reference's Taylor-bar fracture driver (Main_Taylor_Bar_Frac_FEMP.jl:41-61)
-            # in SI units, on the copper bar's geometry and time step
-            from jump_gb300.material import JohnsonCookDamage, JohnsonCookMaterial, JohnsonCookMaterialWithDamage
-            n = s[0].parCount
-            st = JohnsonCookMaterial(200e9, 0.33, 7850.0, 490e6, 383e6, 0.0123, 0.45, 0.5, 0.94, 0.9, 452.0,
-                                     2.5e-4, n)
-            s[0].mat = JohnsonCookMaterialWithDamage(st, JohnsonCookDamage(0.0705, 1.732, -0.54, 0.015, 0.0, 0.5,
-                                                                           293.0, 1800.0, n))
-            label = "Johnson-Cook with damage (steel: A 490 MPa, B 383 MPa, n 0.45, C 0.0123; D1-D4)"
+        # the J2 copper, or the Johnson-Cook copper / Johnson-Cook steel with damage of
+        # the reference's Taylor-bar drivers, on the copper bar's geometry and time step
+        label = scenarios.taylor_material(s[0], material, 2.5e-4)
         cfg = {"workload": f"taylor_bar_3d_{material}", "particles": int(s[0].parCount), "grid_nodes": [65, 65, 161],
                "h_m": 2.5e-4, "particles_per_cell": 8, "material": label,
                "dt_s": data["dt"], "l2": "inputs larger than L2 (~230 MB resident)"}

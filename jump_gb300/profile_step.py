@@ -1,7 +1,9 @@
-"""Run a workload for a few USL steps, for profiling the step kernels.
+"""Run a workload for a few steps, for profiling the step kernels.
 
   python -m jump_gb300.profile_step [--workload taylor_bar] [--precision f64]
                                     [--warmup 2] [--steps 2] [--h 2.5e-4]
+                                    [--algorithm usl|musl] [--alpha 0.99]
+                                    [--basis linear|quad|cubic] [--material j2|jc|jcdamage]
 
 Launch order per step: p2g_kernel, grid_kernel, g2p_kernel (one each per body),
 after the aos_to_soa upload launches of context creation.
@@ -22,22 +24,29 @@ def main():
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--h", type=float, default=2.5e-4)
+    ap.add_argument("--algorithm", default="usl", choices=["usl", "musl"])
+    ap.add_argument("--alpha", type=float, default=0.99)
+    ap.add_argument("--basis", default="linear", choices=["linear", "quad", "cubic"])
+    ap.add_argument("--material", default="j2", choices=list(scenarios.TAYLOR_MATERIALS))
     a = ap.parse_args()
     if a.workload == "taylor_bar":
         g, s, alg, data = scenarios.taylor_bar(h=a.h)
+        scenarios.taylor_material(s[0], a.material, a.h)
     elif a.workload == "two_disks":
         g, s, alg, data = scenarios.two_disks()
     else:
         g, s, alg, data = scenarios.cantilever()
     scenarios.apply_dirichlet(g, data)
+    musl = a.algorithm == "musl"
     ctx = MPMContext(Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"),
-                                 dt=data["dt"], precision=a.precision))
+                                 dt=data["dt"], precision=a.precision, algorithm=a.algorithm,
+                                 alpha=a.alpha if musl else 1.0, basis=a.basis))
     ctx.step(a.warmup)
     t0 = time.perf_counter()
     ctx.step(a.steps)
     dt = time.perf_counter() - t0
     n = sum(x.parCount for x in s)
-    print(f"{a.workload} {a.precision}: {n} particles, {a.steps} steps, {1e3 * dt / max(a.steps, 1):.3f} ms/step, "
+    print(f"{a.workload} {a.precision} {a.algorithm} {a.basis} {a.material}: {n} particles, {a.steps} steps, {1e3 * dt / max(a.steps, 1):.3f} ms/step, "
           f"device {ctx.last_step_ms() / max(a.steps, 1):.3f} ms/step")
     ctx.close()
 

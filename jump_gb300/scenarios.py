@@ -84,6 +84,31 @@ def taylor_bar(h: float = 2.5e-4, ppc: int = 2, radius: float = 3.2e-3, length: 
     return grid, [s], USL(1e-3 * float(s.mass[0])), data
 
 
+TAYLOR_MATERIALS = ("j2", "jc", "jcdamage")
+
+
+def taylor_material(solid, material: str, h: float = 2.5e-4) -> str:
+    """Replace the Taylor bar's J2 copper by another of the reference drivers'
+    materials (SI units, cellsize one grid cell h); returns a label.
+
+    jc:       the Johnson-Cook copper of Main_TaylorBar.jl:43-56
+    jcdamage: the Johnson-Cook steel with damage of Main_Taylor_Bar_Frac_FEMP.jl:41-61
+    """
+    from .material import JohnsonCookDamage, JohnsonCookMaterial, JohnsonCookMaterialWithDamage
+    n = solid.parCount
+    if material == "j2":
+        return "J2 linear hardening"
+    if material == "jc":
+        solid.mat = JohnsonCookMaterial(115e9, 0.31, 8940.0, 65e6, 356e6, 0.0, 0.37, 1e-3, 0.0, 0.0, 0.0, h, n)
+        return "Johnson-Cook (A 65 MPa, B 356 MPa, n 0.37, C 0)"
+    if material == "jcdamage":
+        st = JohnsonCookMaterial(200e9, 0.33, 7850.0, 490e6, 383e6, 0.0123, 0.45, 0.5, 0.94, 0.9, 452.0, h, n)
+        solid.mat = JohnsonCookMaterialWithDamage(st, JohnsonCookDamage(0.0705, 1.732, -0.54, 0.015, 0.0, 0.5,
+                                                                        293.0, 1800.0, n))
+        return "Johnson-Cook with damage (steel: A 490 MPa, B 383 MPa, n 0.45, C 0.0123; D1-D4)"
+    raise ValueError(f"unknown Taylor-bar material {material}")
+
+
 def cantilever(h: float = 0.0625, ppc: int = 4, length: float = 4.0, depth: float = 1.0,
                E_range=(0.5e6, 2e6), nu: float = 0.3, rho: float = 1050.0, g: float = -10.0,
                dt: float = 1e-4, seed: int = 0):
