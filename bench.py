@@ -99,13 +99,21 @@ def variant_tag(args):
 
 
 def ncu_traffic(kernel: str, precision: str, tag: str = ""):
-    """DRAM bytes per launch from the committed ncu summary of this exact variant, if one exists."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_taylor_bar{tag}_{precision}.txt")
-    if not os.path.exists(path):
+    """DRAM bytes per launch from the committed ncu summary of this exact variant, if one exists:
+    the per-kernel file of the default workload, or the keyed line of the variants table."""
+    if not tag:
+        path = os.path.join(ROOT, "profiles", f"{kernel}_taylor_bar_{precision}.txt")
+        if os.path.exists(path):
+            for line in open(path):
+                if line.startswith("traffic_bytes_per_launch_full_size:"):
+                    return float(line.split(":", 1)[1])
         return None
-    for line in open(path):
-        if line.startswith("traffic_bytes_per_launch_full_size:"):
-            return float(line.split(":", 1)[1])
+    path = os.path.join(ROOT, "profiles", f"kernels_taylor_bar_variants_{precision}.txt")
+    key = f"traffic[{kernel}{tag}]:"
+    if os.path.exists(path):
+        for line in open(path):
+            if line.startswith(key):
+                return float(line.split(":", 1)[1])
     return None
 
 
