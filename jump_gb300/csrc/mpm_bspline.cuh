@@ -20,7 +20,8 @@ namespace jmpm {
 template <int K>
 struct BsAxis {
   int64_t first;    // 0-based index of the first support node on this axis
-  double N[K], dN[K];  // 1D values and derivatives in the normalised distance r
+  double N[K];      // 1D values
+  double G[K];      // 1D derivatives along the axis: dN/dr x dxI
 };
 
 // Bsplines.jl:18-80 (t = 1..4)
@@ -107,28 +108,31 @@ __device__ __forceinline__ bool bs_axes(const GridP& g, const double* x, BsAxis<
       const double r = a == 0 ? __dmul_rn(__dsub_rn(x[0], g.coord[0][id - 1]), g.dxI[0])
                               : __dmul_rn(__dsub_rn(x[a], __dmul_rn(double(id - 1), g.dx[a])), g.dxI[a]);
       const int t = (id == 1 || id == nn) ? 1 : (id == 2 ? 2 : (id == nn - 1 ? 4 : 3));
-      if (K == 3) quad_bs(t, r, ax[a].N[i], ax[a].dN[i]);
-      else cubic_bs(t, r, ax[a].N[i], ax[a].dN[i]);
+      double dNr;
+      if (K == 3) quad_bs(t, r, ax[a].N[i], dNr);
+      else cubic_bs(t, r, ax[a].N[i], dNr);
+      ax[a].G[i] = dNr * g.dxI[a];
     }
   }
   return true;
 }
 
-// node index, value and gradient of support entry (i, j, k), in the reference's
-// operation order: N = Nx Ny (Nz), dN_x = dNx dxI Ny (Nz), ...
+// node index, value and gradient of support entry (i, j, k): N = Nx Ny (Nz),
+// grad N = (Gx Ny (Nz), Nx Gy (Nz), Nx Ny Gz)
 template <int D, int K>
 __device__ __forceinline__ int64_t bs_entry(const GridP& g, const BsAxis<K>* ax, int i, int j, int k, double& N,
                                            double* dN) {
   if constexpr (D == 2) {
     N = ax[0].N[i] * ax[1].N[j];
-    dN[0] = ax[0].dN[i] * g.dxI[0] * ax[1].N[j];
-    dN[1] = ax[1].dN[j] * g.dxI[1] * ax[0].N[i];
+    dN[0] = ax[0].G[i] * ax[1].N[j];
+    dN[1] = ax[0].N[i] * ax[1].G[j];
     return (ax[0].first + i) + g.nx * (ax[1].first + j);
   } else {
-    N = ax[0].N[i] * ax[1].N[j] * ax[2].N[k];
-    dN[0] = ax[0].dN[i] * g.dxI[0] * ax[1].N[j] * ax[2].N[k];
-    dN[1] = ax[1].dN[j] * g.dxI[1] * ax[0].N[i] * ax[2].N[k];
-    dN[2] = ax[2].dN[k] * g.dxI[2] * ax[0].N[i] * ax[1].N[j];
+    const double nxy = ax[0].N[i] * ax[1].N[j];
+    N = nxy * ax[2].N[k];
+    dN[0] = (ax[0].G[i] * ax[1].N[j]) * ax[2].N[k];
+    dN[1] = (ax[0].N[i] * ax[1].G[j]) * ax[2].N[k];
+    dN[2] = nxy * ax[2].G[k];
     return (ax[0].first + i) + g.nx * (ax[1].first + j) + g.nxy * (ax[2].first + k);
   }
 }
@@ -153,7 +157,11 @@ __device__ __forceinline__ void bs_mark(const NodeP& nd, const BsAxis<K>* ax) {
 
 // ---- USL ---------------------------------------------------------------------
 // P2G over the support (SolveExplicitSolidMechanics2D.jl:391-423): m, p0, f
-// (+ body force), and the contact normals where the field has them.
+// (+ body force), and the contact normals where the field has them.  In 3D the
+// per-node work is factored along z: with Nxy = Nx Ny, the force of node
+// (i, j, k) is f_a = Nz_k P_a(i,j) + Gz_k Q_a(i,j), where
+// P_a = s_a0 Gx Ny + s_a1 Nx Gy (+ m g_a Nxy) and Q_a = s_a2 Nxy with s = -V sigma,
+// and its mass m Nxy Nz_k -- about ten FP64 operations per node.
 template <int D, class R, int K, bool GRAV>
 __global__ void __launch_bounds__(256) bs_p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy, double gz,
                                                      unsigned* status) {
@@ -171,37 +179,84 @@ __global__ void __launch_bounds__(256) bs_p2g_kernel(GridP g, NodeP nd, PartP pp
   }
   if (nd.bflag) bs_mark<D, K>(nd, ax);
   const double m = double(*field<R>(pp, L::M, p)), V = double(*field<R>(pp, L::VOL, p));
-  double mv[D], ms[L::S];
+  double v[D], ms[L::S], mg[D];
   const double grav[3] = {gx, gy, gz};
 #pragma unroll
-  for (int a = 0; a < D; ++a) mv[a] = m * double(*field<R>(pp, L::V + a, p));
+  for (int a = 0; a < D; ++a) {
+    v[a] = double(*field<R>(pp, L::V + a, p));
+    mg[a] = m * grav[a];
+  }
 #pragma unroll
   for (int c = 0; c < L::S; ++c) ms[c] = -V * double(*field<R>(pp, L::SIG + c, p));
   const int64_t Nn = nd.nodeCount;
-  for (int i = 0; i < K; ++i)
-    for (int j = 0; j < K; ++j)
-      for (int k = 0; k < (D == 3 ? K : 1); ++k) {
-        double N, dN[D];
-        const int64_t n = bs_entry<D, K>(g, ax, i, j, k, N, dN);
-        atomicAdd(nd.m + n, N * m);
+  const bool NRM = nd.nrm != nullptr;
+  if constexpr (D == 2) {
+#pragma unroll 1
+    for (int i = 0; i < K; ++i)
 #pragma unroll
-        for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, N * mv[a]);
+      for (int j = 0; j < K; ++j) {
+        double N, dN[2];
+        const int64_t n = bs_entry<2, K>(g, ax, i, j, 0, N, dN);
+        const double Nm = N * m;
+        atomicAdd(nd.m + n, Nm);
 #pragma unroll
-        for (int a = 0; a < D; ++a) {
-          double fa = ms[sym<D>(a, 0)] * dN[0];
+        for (int a = 0; a < 2; ++a) atomicAdd(nd.p0 + a * Nn + n, Nm * v[a]);
 #pragma unroll
-          for (int b = 1; b < D; ++b) fa += ms[sym<D>(a, b)] * dN[b];
-          if (GRAV) fa += (m * grav[a]) * N;
+        for (int a = 0; a < 2; ++a) {
+          double fa = ms[sym<2>(a, 0)] * dN[0] + ms[sym<2>(a, 1)] * dN[1];
+          if (GRAV) fa += mg[a] * N;
           atomicAdd(nd.f + a * Nn + n, fa);
         }
-        if (nd.nrm)
+        if (NRM)
 #pragma unroll
-          for (int a = 0; a < D; ++a) atomicAdd(nd.nrm + a * Nn + n, m * dN[a]);
+          for (int a = 0; a < 2; ++a) atomicAdd(nd.nrm + a * Nn + n, m * dN[a]);
       }
+  } else {
+    double mNz[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) mNz[k] = m * ax[2].N[k];
+    // outer (i, j) loops rolled: unrolling them lets the compiler hold every
+    // node's values at once and spill
+#pragma unroll 1
+    for (int i = 0; i < K; ++i)
+#pragma unroll 1
+      for (int j = 0; j < K; ++j) {
+        const double Nxy = ax[0].N[i] * ax[1].N[j];
+        const double GxNy = ax[0].G[i] * ax[1].N[j];
+        const double NxGy = ax[0].N[i] * ax[1].G[j];
+        double P[3], Q[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          P[a] = ms[sym<3>(a, 0)] * GxNy + ms[sym<3>(a, 1)] * NxGy;
+          if (GRAV) P[a] += mg[a] * Nxy;
+          Q[a] = ms[sym<3>(a, 2)] * Nxy;
+        }
+        const int64_t nij = (ax[0].first + i) + g.nx * (ax[1].first + j) + g.nxy * ax[2].first;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const int64_t n = nij + g.nxy * k;
+          const double Nm = Nxy * mNz[k];
+          atomicAdd(nd.m + n, Nm);
+#pragma unroll
+          for (int a = 0; a < 3; ++a) atomicAdd(nd.p0 + a * Nn + n, Nm * v[a]);
+#pragma unroll
+          for (int a = 0; a < 3; ++a) atomicAdd(nd.f + a * Nn + n, P[a] * ax[2].N[k] + Q[a] * ax[2].G[k]);
+          if (NRM) {
+            // m grad N (SolveExplicitFEMP3DContact.jl)
+            atomicAdd(nd.nrm + n, GxNy * mNz[k]);
+            atomicAdd(nd.nrm + Nn + n, NxGy * mNz[k]);
+            atomicAdd(nd.nrm + 2 * Nn + n, (m * Nxy) * ax[2].G[k]);
+          }
+        }
+      }
+  }
 }
 
 // G2P over the support (:485-532): v += N dv, x += N vdt, L dt += vdt (x) grad N,
-// then the shared kinematics and constitutive update.
+// then the shared kinematics and constitutive update.  The sums are factored
+// along the last axis: per (i(, j)) the node values are first contracted with
+// that axis's N and G (Z0 = sum Nz vdt, Z1 = sum Gz vdt, W = sum Nz dv), then
+// x += Nxy Z0, v += Nxy W, L dt += (Gx Ny Z0, Nx Gy Z0, Nxy Z1).
 template <int D, class R, int K, int MAT>
 __global__ void __launch_bounds__(256) bs_g2p_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, unsigned* status) {
   using L = Layout<D>;
@@ -225,20 +280,41 @@ __global__ void __launch_bounds__(256) bs_g2p_kernel(GridP g, NodeP nd, PartP pp
   for (int a = 0; a < D; ++a)
 #pragma unroll
     for (int b = 0; b < D; ++b) Ld[a][b] = 0.0;
-  for (int i = 0; i < K; ++i)
-    for (int j = 0; j < K; ++j)
-      for (int k = 0; k < (D == 3 ? K : 1); ++k) {
-        double N, dN[D];
-        const int64_t n = bs_entry<D, K>(g, ax, i, j, k, N, dN);
+  constexpr int NO = D == 3 ? K * K : K;  // outer entries (i, j) in 3D, i in 2D
+#pragma unroll 1
+  for (int o = 0; o < NO; ++o) {
+    const int i = D == 3 ? o / K : o, j = D == 3 ? o % K : 0;
+    // outer weights: value and the in-plane gradient factors
+    const double No = D == 3 ? ax[0].N[i] * ax[1].N[j] : ax[0].N[i];
+    const double Go0 = D == 3 ? ax[0].G[i] * ax[1].N[j] : ax[0].G[i];
+    const double Go1 = D == 3 ? ax[0].N[i] * ax[1].G[j] : 0.0;
+    const BsAxis<K>& in = ax[D - 1];
+    const int64_t no = D == 3 ? (ax[0].first + i) + g.nx * (ax[1].first + j) + g.nxy * in.first
+                              : (ax[0].first + i) + g.nx * in.first;
+    const int64_t stride = D == 3 ? g.nxy : g.nx;
+    double Z0[D], Z1[D], W[D];
 #pragma unroll
-        for (int a = 0; a < D; ++a) {
-          const double vd = __ldg(nd.vdt + a * Nn + n);
-          v[a] += N * __ldg(nd.dv + a * Nn + n);
-          x[a] += N * vd;
+    for (int a = 0; a < D; ++a) Z0[a] = Z1[a] = W[a] = 0.0;
 #pragma unroll
-          for (int b = 0; b < D; ++b) Ld[a][b] += vd * dN[b];
-        }
+    for (int k = 0; k < K; ++k) {
+      const int64_t n = no + stride * k;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const double vd = __ldg(nd.vdt + a * Nn + n);
+        Z0[a] += in.N[k] * vd;
+        Z1[a] += in.G[k] * vd;
+        W[a] += in.N[k] * __ldg(nd.dv + a * Nn + n);
       }
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      x[a] += No * Z0[a];
+      v[a] += No * W[a];
+      Ld[a][0] += Go0 * Z0[a];
+      if (D == 3) Ld[a][1] += Go1 * Z0[a];
+      Ld[a][D - 1] += No * Z1[a];
+    }
+  }
   R Ldt[D][D];
   bool fin = true;
 #pragma unroll
