@@ -279,4 +279,17 @@ __device__ __forceinline__ void corners(const GridP& g, const Hat<D, R>& h, Corn
   }
 }
 
+// node indices of the corners only (for kernels that form N and grad N from
+// the per-axis factors themselves)
+template <int D, class R>
+__device__ __forceinline__ void corner_nodes(const GridP& g, const Hat<D, R>& h, Corners<D, R>& cr) {
+  int64_t base = int64_t(h.c[0]) + g.nx * int64_t(h.c[1]);
+  if (D == 3) base += g.nxy * int64_t(h.c[D == 3 ? 2 : 0]);
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) {
+    const int bx = k & 1, by = (k >> 1) & 1, bz = (k >> 2) & 1;
+    cr.node[k] = base + bx + g.nx * by + (D == 3 ? g.nxy * bz : 0);
+  }
+}
+
 }  // namespace jmpm

@@ -37,7 +37,7 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
   R x[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
-  Hat<D, R> h;
+  Hat<D, R> h{};  // zeros on lanes whose cell lies outside (they add nothing)
   const bool ok = hat<D, R>(g, x, h);
   if (!ok) {
     atomicOr(status, ST_OUT_OF_GRID);
@@ -46,7 +46,8 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
   Corners<D, R> cr;
   R m = R(0), V = R(0), v[D], ms[L::S];
   if (ok) {
-    corners<D, R>(g, h, cr);
+    if (D == 3) corner_nodes<D, R>(g, h, cr);  // N and grad N are formed per z pair below
+    else corners<D, R>(g, h, cr);
     m = *field<R>(pp, L::M, p);
     V = *field<R>(pp, L::VOL, p);
   }
@@ -77,26 +78,9 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
     while ((1u << levels) < run) ++levels;
   }
   const int64_t Nn = nd.nodeCount;
-#pragma unroll
-  for (int k = 0; k < (1 << D); ++k) {
-    R val[NV];
-    R N = ok ? cr.N[k] : R(0);
-    R Nm = N * m;
-    val[0] = Nm;
-#pragma unroll
-    for (int a = 0; a < D; ++a) val[1 + a] = Nm * v[a];
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      R fa = ok ? ms[sym<D>(a, 0)] * cr.dN[k][0] : R(0);
-#pragma unroll
-      for (int j = 1; j < D; ++j) fa += ok ? ms[sym<D>(a, j)] * cr.dN[k][j] : R(0);
-      if (GRAV) fa += mg[a] * N;
-      val[1 + D + a] = fa;
-    }
-    // normals of the contact correction: sum m_p grad N (SolveExplicitFEMP2DContact.jl:237)
-    if (NRM)
-#pragma unroll
-      for (int a = 0; a < D; ++a) val[1 + 2 * D + a] = ok ? m * cr.dN[k][a] : R(0);
+  // one node's values: the FP32 run sum, then the FP64 atomics (k: corner index,
+  // bit 0 +x, bit 1 +y, bit 2 +z)
+  auto emit = [&](int k, R* val) {
     if (WARP_SUM) {
       const int nv = NRM ? NV : 1 + 2 * D;
       for (int l = 0; l < levels; ++l) {
@@ -110,8 +94,7 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
       }
     }
     if (ok && head) {
-      if (k == 0 && nd.bflag) mark_blocks<D>(nd, h.c);
-      int64_t n = cr.node[k];
+      const int64_t n = cr.node[k];
       atomicAdd(nd.m + n, to_f64(val[0]));
 #pragma unroll
       for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, to_f64(val[1 + a]));
@@ -120,6 +103,68 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
       if (NRM)
 #pragma unroll
         for (int a = 0; a < D; ++a) atomicAdd(nd.nrm + a * Nn + n, to_f64(val[1 + 2 * D + a]));
+    }
+  };
+  if (ok && head && nd.bflag) mark_blocks<D>(nd, h.c);
+  if constexpr (D == 3) {
+    // factored along z: per (x, y) corner pair the force coefficients
+    // P_a = s_a0 Gx Ny + s_a1 Nx Gy (+ m g_a Nx Ny) and Q_a = s_a2 Nx Ny (s = -V sigma)
+    // give f_a = Nz P_a + Gz Q_a at both z corners
+    const R mNz[2] = {m * h.Nl[2], m * h.Nh[2]};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int bx = q & 1, by = q >> 1;
+      const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
+      const R Gx = bx ? h.gh[0] : h.gl[0], Gy = by ? h.gh[1] : h.gl[1];
+      const R Nxy = Nx * Ny, GxNy = Gx * Ny, NxGy = Nx * Gy;
+      R P[3], Q[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        P[a] = ms[sym<3>(a, 0)] * GxNy + ms[sym<3>(a, 1)] * NxGy;
+        if (GRAV) P[a] += mg[a] * Nxy;
+        Q[a] = ms[sym<3>(a, 2)] * Nxy;
+      }
+#pragma unroll
+      for (int bz = 0; bz < 2; ++bz) {
+        const R Nz = bz ? h.Nh[2] : h.Nl[2], Gz = bz ? h.gh[2] : h.gl[2];
+        R val[NV];
+        const R Nm = Nxy * mNz[bz];
+        val[0] = Nm;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) val[1 + a] = Nm * v[a];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) val[4 + a] = P[a] * Nz + Q[a] * Gz;
+        // normals of the contact correction: sum m_p grad N (SolveExplicitFEMP3DContact.jl)
+        if (NRM) {
+          val[7] = GxNy * mNz[bz];
+          val[8] = NxGy * mNz[bz];
+          val[9] = (m * Nxy) * Gz;
+        }
+        emit(q + 4 * bz, val);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < (1 << D); ++k) {
+      R val[NV];
+      R N = ok ? cr.N[k] : R(0);
+      R Nm = N * m;
+      val[0] = Nm;
+#pragma unroll
+      for (int a = 0; a < D; ++a) val[1 + a] = Nm * v[a];
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        R fa = ok ? ms[sym<D>(a, 0)] * cr.dN[k][0] : R(0);
+#pragma unroll
+        for (int j = 1; j < D; ++j) fa += ok ? ms[sym<D>(a, j)] * cr.dN[k][j] : R(0);
+        if (GRAV) fa += mg[a] * N;
+        val[1 + D + a] = fa;
+      }
+      // normals of the contact correction: sum m_p grad N (SolveExplicitFEMP2DContact.jl:237)
+      if (NRM)
+#pragma unroll
+        for (int a = 0; a < D; ++a) val[1 + 2 * D + a] = ok ? m * cr.dN[k][a] : R(0);
+      emit(k, val);
     }
   }
 }
@@ -708,7 +753,8 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
     return;
   }
   Corners<D, R> cr;
-  corners<D, R>(g, h, cr);
+  if (D == 3) corner_nodes<D, R>(g, h, cr);
+  else corners<D, R>(g, h, cr);
   R v[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) v[a] = *field<R>(pp, L::V + a, p);
@@ -720,8 +766,34 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
   const R* vdt_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.vdt) : reinterpret_cast<const R*>(nd.vdt_f);
   const R* dv_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.dv) : reinterpret_cast<const R*>(nd.dv_f);
   const int64_t Nn = nd.nodeCount;
+  if constexpr (D == 3) {
+    // factored along z: per (x, y) corner pair, Z0 = sum Nz vdt, Z1 = sum Gz vdt,
+    // W = sum Nz dv over the two z corners, then x += Nx Ny Z0, v += Nx Ny W,
+    // L dt += (Gx Ny Z0, Nx Gy Z0, Nx Ny Z1)
 #pragma unroll
-  for (int k = 0; k < (1 << D); ++k) {
+    for (int q = 0; q < 4; ++q) {
+      const int bx = q & 1, by = q >> 1;
+      const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
+      const R Gx = bx ? h.gh[0] : h.gl[0], Gy = by ? h.gh[1] : h.gl[1];
+      const R Nxy = Nx * Ny, GxNy = Gx * Ny, NxGy = Nx * Gy;
+      const int64_t n0 = cr.node[q], n1 = cr.node[q + 4];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const R vd0 = nload<CG>(vdt_n + a * Nn + n0), vd1 = nload<CG>(vdt_n + a * Nn + n1);
+        const R dv0 = nload<CG>(dv_n + a * Nn + n0), dv1 = nload<CG>(dv_n + a * Nn + n1);
+        const R Z0 = h.Nl[2] * vd0 + h.Nh[2] * vd1;
+        const R Z1 = h.gl[2] * vd0 + h.gh[2] * vd1;
+        const R W = h.Nl[2] * dv0 + h.Nh[2] * dv1;
+        x[a] += Nxy * Z0;
+        v[a] += Nxy * W;
+        Ldt[a][0] += GxNy * Z0;
+        Ldt[a][1] += NxGy * Z0;
+        Ldt[a][2] += Nxy * Z1;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < (D == 3 ? 0 : 1 << D); ++k) {
     int64_t n = cr.node[k];
     R N = cr.N[k];
     R vd[D], dvv[D];
