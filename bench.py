@@ -329,6 +329,13 @@ def run_ours(args):
     mk = lambda: Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
                              precision=args.precision, sort_interval=args.sort_interval, **scheme_kw(args))
     ctx = MPMContext(mk())
+    tuning = None
+    if args.tune:
+        # the context's autotuner picks the P2G strategy, CTA size and sort interval
+        # (outside the timed region; the simulation does not advance)
+        tuning = ctx.tune(3)
+    launch = ctx.launch()
+    args.sort_interval = launch["sort_interval"]
     ctx.step(args.warmup)
     sampler = ClockSampler()
     if dist is not None:
@@ -375,6 +382,7 @@ def run_ours(args):
     e2e_ctx_t0 = time.perf_counter()
     desc = mk_pin()
     c2 = MPMContext(desc)
+    c2.set_launch(**launch)
     t1 = time.perf_counter()
     recs, _ = c2.step_energies(args.steps, 1, 0)
     t2 = time.perf_counter()
@@ -415,8 +423,10 @@ def run_ours(args):
             "data": "synthetic (geometry-generated particles, no dataset)",
             "config": dict(cfg, precision=args.precision, sort_interval=args.sort_interval,
                            algorithm=args.algorithm if args.algorithm == "usl" else f"musl(alpha={args.alpha})",
-                           basis=args.basis,
+                           basis=args.basis, p2g=launch["p2g"], threads=launch["threads"],
+                           launch_chosen_by="mpm_tune" if tuning else "defaults",
                            parallelism=f"replicas{world}" if world > 1 else "single-gpu"),
+            "tuning": tuning,
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "stage_ms_per_step": per,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -681,7 +691,9 @@ def main():
                     help="Taylor bar material: J2 linear hardening (the headline), Johnson-Cook, or Johnson-Cook "
                          "with damage")
     ap.add_argument("--sort-interval", type=int, default=0,
-                    help="counting-sort particles by cell every N steps (0: never)")
+                    help="counting-sort particles by cell every N steps (0: never; with --tune the tuner's choice)")
+    ap.add_argument("--tune", action=argparse.BooleanOptionalAction, default=True,
+                    help="run the context's autotuner (P2G strategy, CTA size, sort interval) before timing")
     ap.add_argument("--workload", default="taylor_bar",
                     choices=["taylor_bar", "two_disks", "ensemble", "impact_ensemble", "impact_jvp", "adjoint"])
     ap.add_argument("--instances", type=int, default=None,

@@ -54,6 +54,10 @@ MPM_BASIS_LINEAR = 0
 MPM_BASIS_QUAD_BSPLINE = 1
 MPM_BASIS_CUBIC_BSPLINE = 2
 
+MPM_TUNE_CANDIDATES = 16
+MPM_P2G_ATOMIC = 0
+MPM_P2G_WARP = 1
+
 MPM_BATCH_PERSISTENT = 0
 MPM_BATCH_WIDE = 1
 MPM_BATCH_MAX_BODIES = 4
@@ -185,6 +189,10 @@ SIGNATURES = {
                              C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "mpm_step": (C.c_int, [C.c_void_p, C.c_int64, _dp]),
     "mpm_step_energies": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, _dp, C.c_void_p]),
+    "mpm_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "mpm_get_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "mpm_tune": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                           C.POINTER(C.c_int32), _dp, _dp]),
     "mpm_download": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(BodyView)]),
     "mpm_download_grid": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
     "mpm_energies": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),

@@ -105,6 +105,8 @@ struct mpm_ctx {
   double* red = nullptr;
   double* staging = nullptr;
   size_t staging_n = 0;
+  int p2g_strategy = MPM_P2G_ATOMIC;  // linear-basis USL P2G (mpm_set_launch)
+  int threads = 256;                  // CTA size of the linear-basis P2G and G2P
   double* rec_host = nullptr;   // pinned EnergiesFix records of mpm_step_energies
   int64_t rec_cap = 0;          // records it holds
   cudaStream_t stream = nullptr;
@@ -187,6 +189,37 @@ void launch_aos_to_soa(mpm_ctx* c, const PartP& pp, const double* src, int per, 
 void launch_soa_to_aos(mpm_ctx* c, const PartP& pp, double* dst, int per, int f0, const CompMapH& cm) {
   if (c->dim == 2) Launchers<2>::soa_to_aos_perm(c->stream, pp, c->f32, c->orig, dst, per, f0, cm);
   else Launchers<3>::soa_to_aos_perm(c->stream, pp, c->f32, c->orig, dst, per, f0, cm);
+}
+
+// second particle buffer + key/rank/count arrays of the counting sort
+int alloc_sort(mpm_ctx* c) {
+  if (c->Palt || c->np == 0) return MPM_OK;
+  if (int64_t(c->nb) * (int64_t(c->ncells) + 1) >= (int64_t(1) << 32))
+    return fail(MPM_ERR_ARG, "too many (body, cell) keys for the particle sort");
+  CUDA_TRY(cudaMalloc(&c->Palt, size_t(c->NF) * size_t(c->np) * c->esz));
+  CUDA_TRY(cudaMalloc(&c->orig_alt, size_t(c->np) * sizeof(int64_t)));
+  c->sp.nkeys = int64_t(c->nb) * (int64_t(c->ncells) + 1);
+  CUDA_TRY(cudaMalloc(&c->sp.key, size_t(c->np) * sizeof(uint32_t)));
+  CUDA_TRY(cudaMalloc(&c->sp.rank, size_t(c->np) * sizeof(uint32_t)));
+  CUDA_TRY(cudaMalloc(&c->sp.count, size_t(c->sp.nkeys) * sizeof(uint32_t)));
+  CUDA_TRY(cudaMalloc(&c->sp.offset, size_t(c->sp.nkeys) * sizeof(uint32_t)));
+  CUDA_TRY(cudaMalloc(&c->sp.blocksum, size_t((c->sp.nkeys + 1023) / 1024) * sizeof(uint32_t)));
+  return MPM_OK;
+}
+
+// drop the captured step graphs (the launch configuration changed)
+void invalidate_graphs(mpm_ctx* c) {
+  for (int i = 0; i < 2; ++i) {
+    if (c->exec[i]) cudaGraphExecDestroy(c->exec[i]);
+    if (c->graph[i]) cudaGraphDestroy(c->graph[i]);
+    c->exec[i] = nullptr;
+    c->graph[i] = nullptr;
+    if (c->seg_exec[i]) cudaGraphExecDestroy(c->seg_exec[i]);
+    if (c->seg_graph[i]) cudaGraphDestroy(c->seg_graph[i]);
+    c->seg_exec[i] = nullptr;
+    c->seg_graph[i] = nullptr;
+    c->seg_len[i] = 0;
+  }
 }
 
 // Counting sort of all particles by (body, cell) into the other buffer; swaps buffers.
@@ -315,9 +348,11 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
       if (D == 2) Launchers<2>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
       else Launchers<3>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
     } else if (D == 2) {
-      Launchers<2>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
+      Launchers<2>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status,
+                        c->p2g_strategy, c->threads);
     } else {
-      Launchers<3>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status);
+      Launchers<3>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status,
+                        c->p2g_strategy, c->threads);
     }
   }
   if (ev) cudaEventRecord(ev[1], c->stream);
@@ -339,9 +374,11 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
       if (D == 2) Launchers<2>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
       else Launchers<3>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
     } else if (D == 2) {
-      Launchers<2>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+      Launchers<2>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status,
+                        c->threads);
     } else {
-      Launchers<3>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status);
+      Launchers<3>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status,
+                        c->threads);
     }
   }
   if (ev) cudaEventRecord(ev[3], c->stream);
@@ -523,16 +560,10 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   }
   c->ncells = 1;
   for (int a = 0; a < D; ++a) c->ncells *= uint32_t(nn[a] - 1);
+  c->p2g_strategy = c->f32 ? MPM_P2G_WARP : MPM_P2G_ATOMIC;
   if (prm->sort_interval > 0 && c->np > 0) {
-    // second particle buffer + key/rank/count arrays of the counting sort
-    CUDA_TRY(cudaMalloc(&c->Palt, ptot * c->esz));
-    CUDA_TRY(cudaMalloc(&c->orig_alt, size_t(c->np) * sizeof(int64_t)));
-    c->sp.nkeys = int64_t(nbodies) * (int64_t(c->ncells) + 1);
-    CUDA_TRY(cudaMalloc(&c->sp.key, size_t(c->np) * sizeof(uint32_t)));
-    CUDA_TRY(cudaMalloc(&c->sp.rank, size_t(c->np) * sizeof(uint32_t)));
-    CUDA_TRY(cudaMalloc(&c->sp.count, size_t(c->sp.nkeys) * sizeof(uint32_t)));
-    CUDA_TRY(cudaMalloc(&c->sp.offset, size_t(c->sp.nkeys) * sizeof(uint32_t)));
-    CUDA_TRY(cudaMalloc(&c->sp.blocksum, size_t((c->sp.nkeys + 1023) / 1024) * sizeof(uint32_t)));
+    int r = alloc_sort(c);
+    if (r != MPM_OK) return r;
     c->since_sort = prm->sort_interval;  // sort before the first step
   }
   c->staging_n = size_t(maxn > 0 ? maxn : 1) * 9;
@@ -671,6 +702,18 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
   return MPM_OK;
 }
 
+// enqueue one step: the cell sort when it is due, then the step graph of the
+// buffer in use (captured on first use)
+static int launch_one_step(mpm_ctx* c) {
+  int r;
+  if (c->Palt && c->prm.sort_interval > 0 && c->since_sort >= c->prm.sort_interval && (r = enqueue_sort(c)))
+    return r;
+  if ((r = build_step_graph(c))) return r;
+  CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
+  ++c->since_sort;
+  return MPM_OK;
+}
+
 int mpm_step(mpm_ctx* c, int64_t nsteps, double* t_inout) {
   if (!c) return fail(MPM_ERR_ARG, "mpm_step: null context");
   if (nsteps < 0) return fail(MPM_ERR_ARG, "mpm_step: nsteps < 0");
@@ -678,10 +721,7 @@ int mpm_step(mpm_ctx* c, int64_t nsteps, double* t_inout) {
   CUDA_TRY(cudaEventRecord(c->e0, c->stream));
   for (int64_t k = 0; k < nsteps; ++k) {
     int r;
-    if (c->Palt && c->since_sort >= c->prm.sort_interval && (r = enqueue_sort(c))) return r;
-    if ((r = build_step_graph(c))) return r;
-    CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
-    ++c->since_sort;
+    if ((r = launch_one_step(c))) return r;
     if (t_inout) *t_inout += c->prm.dt;
   }
   CUDA_TRY(cudaEventRecord(c->e1, c->stream));
@@ -714,10 +754,7 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
   int64_t j = 0;
   for (int64_t k = 0; k < nsteps; ++k) {
     int r;
-    if (c->Palt && c->since_sort >= c->prm.sort_interval && (r = enqueue_sort(c))) return r;
-    if ((r = build_step_graph(c))) return r;
-    CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
-    ++c->since_sort;
+    if ((r = launch_one_step(c))) return r;
     if (t_inout) *t_inout += c->prm.dt;
     if (k >= first && (k - first) % every == 0) {
       double* dst = c->rec_host + size_t(j) * (2 + D);
@@ -741,6 +778,117 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
   c->last_ms = ms;
   if (nrec > 0) std::memcpy(out, c->rec_host, size_t(nrec) * (2 + D) * sizeof(double));
   return status_to_code(st);
+}
+
+int mpm_set_launch(mpm_ctx* c, int32_t p2g_strategy, int32_t threads, int32_t sort_interval) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_set_launch: null context");
+  if (p2g_strategy >= 0 && p2g_strategy != MPM_P2G_ATOMIC && p2g_strategy != MPM_P2G_WARP)
+    return fail(MPM_ERR_ARG, "mpm_set_launch: unknown P2G strategy");
+  if (threads >= 0 && (threads < 32 || threads > 256 || threads % 32 != 0))
+    return fail(MPM_ERR_ARG, "mpm_set_launch: threads must be a multiple of 32 in 32 .. 256");
+  if (sort_interval > 0 && !c->Palt) {
+    int r = alloc_sort(c);
+    if (r != MPM_OK) return r;
+  }
+  CUDA_TRY(cudaStreamSynchronize(c->stream));  // captured graphs may still run
+  if (p2g_strategy >= 0) c->p2g_strategy = p2g_strategy;
+  if (threads >= 0) c->threads = threads;
+  if (sort_interval >= 0) {
+    if (sort_interval > 0 && c->prm.sort_interval != sort_interval) c->since_sort = sort_interval;  // sort next step
+    c->prm.sort_interval = sort_interval;
+  }
+  invalidate_graphs(c);
+  return MPM_OK;
+}
+
+int mpm_get_launch(mpm_ctx* c, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval) {
+  if (!c) return fail(MPM_ERR_ARG, "mpm_get_launch: null context");
+  if (p2g_strategy) *p2g_strategy = c->p2g_strategy;
+  if (threads) *threads = c->threads;
+  if (sort_interval) *sort_interval = c->prm.sort_interval;
+  return MPM_OK;
+}
+
+int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval,
+             double* ms_per_step, double* all_ms) {
+  if (!c || probe_steps < 1) return fail(MPM_ERR_ARG, "mpm_tune: null context or probe_steps < 1");
+  if (c->np == 0) return fail(MPM_ERR_ARG, "mpm_tune: no particles");
+  // the particle state (and its slot -> particle map) every probe starts from
+  const size_t pbytes = size_t(c->NF) * size_t(c->np) * c->esz, obytes = size_t(c->np) * sizeof(int64_t);
+  void* snap = nullptr;
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cudaMalloc(&snap, pbytes + obytes));
+  char* sp = static_cast<char*>(snap);
+  int rc = MPM_OK;
+  auto restore = [&]() -> int {
+    CUDA_TRY(cudaMemcpyAsync(c->P, sp, pbytes, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->orig, sp + pbytes, obytes, cudaMemcpyDeviceToDevice, c->stream));
+    return MPM_OK;
+  };
+  const int saved_s = c->p2g_strategy, saved_t = c->threads, saved_i = c->prm.sort_interval;
+  const int64_t saved_since = c->since_sort;
+  if (cudaMemcpyAsync(sp, c->P, pbytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess ||
+      cudaMemcpyAsync(sp + pbytes, c->orig, obytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+    rc = fail(MPM_ERR_CUDA, "mpm_tune: snapshot copy failed");
+  const bool can_sort = rc == MPM_OK && alloc_sort(c) == MPM_OK;
+  const int strategies[] = {MPM_P2G_ATOMIC, MPM_P2G_WARP};
+  const int thread_list[] = {128, 256};
+  const int sort_list[] = {0, 1, 4, 16};
+  double best = 1e300;
+  int bs = saved_s, bt = saved_t, bi = saved_i;
+  if (all_ms)
+    for (int q = 0; q < MPM_TUNE_CANDIDATES; ++q) all_ms[q] = -1.0;
+  int idx = -1;
+  for (int s : strategies) {
+    for (int th : thread_list) {
+      for (int si : sort_list) {
+        ++idx;
+        if (rc != MPM_OK) break;
+        if (si > 0 && !can_sort) continue;
+        c->p2g_strategy = s;
+        c->threads = th;
+        c->prm.sort_interval = si;
+        c->since_sort = si;  // a probe with sorting starts sorted
+        invalidate_graphs(c);
+        if ((rc = restore())) break;
+        if ((rc = launch_one_step(c))) break;  // captures the graphs outside the timed region
+        CUDA_TRY(cudaEventRecord(c->e0, c->stream));
+        for (int64_t k = 0; k < probe_steps && rc == MPM_OK; ++k) rc = launch_one_step(c);
+        CUDA_TRY(cudaEventRecord(c->e1, c->stream));
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) rc = fail(MPM_ERR_CUDA, std::string("mpm_tune: ") + cudaGetErrorString(e));
+        if (rc != MPM_OK) break;
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
+        const double per = double(ms) / double(probe_steps);
+        if (all_ms) all_ms[idx] = per;
+        if (per < best) {
+          best = per;
+          bs = s;
+          bt = th;
+          bi = si;
+        }
+      }
+    }
+  }
+  // the chosen configuration, on the state the call started from
+  c->p2g_strategy = rc == MPM_OK ? bs : saved_s;
+  c->threads = rc == MPM_OK ? bt : saved_t;
+  c->prm.sort_interval = rc == MPM_OK ? bi : saved_i;
+  c->since_sort = c->prm.sort_interval > 0 ? c->prm.sort_interval : saved_since;
+  invalidate_graphs(c);
+  int r2 = restore();
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
+  cudaFree(snap);
+  if (rc != MPM_OK) return rc;
+  if (r2 != MPM_OK) return r2;
+  if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_tune: ") + cudaGetErrorString(e));
+  if (p2g_strategy) *p2g_strategy = c->p2g_strategy;
+  if (threads) *threads = c->threads;
+  if (sort_interval) *sort_interval = c->prm.sort_interval;
+  if (ms_per_step) *ms_per_step = best;
+  return MPM_OK;
 }
 
 int mpm_download(mpm_ctx* c, int32_t body, const mpm_body_view* v) {

@@ -76,8 +76,10 @@ struct CompMapH {
 
 template <int D>
 struct Launchers {
+  // strategy: MPM_P2G_ATOMIC / MPM_P2G_WARP, or -1 for the precision's default
+  // (FP64: atomic, FP32: warp); threads per CTA (<= 256), 0 for 256
   static void p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
-                  const double* grav, unsigned* status);
+                  const double* grav, unsigned* status, int strategy = -1, int threads = 0);
   // compaction of the flagged node blocks + grid update over them
   static void grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy);
   // zero the accumulators of the blocks listed by the previous grid stage
@@ -93,7 +95,7 @@ struct Launchers {
   static void contact_grid(cudaStream_t s, const NodeP& nd, const ContactP& cp, double dt, double tol,
                            bool f32copy);
   static void g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
-                  const MatParams& mp, double dt, unsigned* status);
+                  const MatParams& mp, double dt, unsigned* status, int threads = 0);
   static void energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,
                        double* out);
   static void aos_to_soa(cudaStream_t s, const PartP& pp, bool f32, const double* src, int per, int f0,

@@ -23,12 +23,14 @@ __device__ __forceinline__ R* field(const PartP& pp, int f, int64_t p) {
 // ---------------------------------------------------------------------------
 // P2G of particle pp.begin + t.  All 32 lanes of a warp call it together
 // (t consecutive across the warp); lanes with t >= pp.count do nothing.
-template <int D, class R, bool GRAV>
+// WARP_SUM (MPM_P2G_WARP): lanes with the same base node first add their
+// values by a segmented shuffle reduction and one lane per run issues the
+// atomics; otherwise (MPM_P2G_ATOMIC) every lane issues its own.
+template <int D, class R, bool GRAV, bool WARP_SUM = (sizeof(R) == 4)>
 __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
                                              double gx, double gy, double gz, unsigned* status) {
   using L = Layout<D>;
   constexpr int NV = 1 + 3 * D;  // per node: m, p0 (D), f (D), normal (D, contact mode)
-  constexpr bool WARP_SUM = sizeof(R) == 4;
   const bool NRM = nd.nrm != nullptr;
   // lanes of this warp holding a particle (a contiguous low range)
   const unsigned mask = __ballot_sync(0xffffffffu, t < pp.count);
@@ -61,9 +63,9 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
     mg[1] = m * R(gy);
     if (D == 3) mg[2] = m * R(gz);
   }
-  // FP32 particles: lanes with the same base node (runs of consecutive lanes,
-  // long after the cell sort) add their contributions with a segmented
-  // shuffle reduction, and only the run's first lane issues the FP64 atomics.
+  // WARP_SUM: lanes with the same base node (runs of consecutive lanes, long
+  // after the cell sort) add their contributions with a segmented shuffle
+  // reduction, and only the run's first lane issues the FP64 atomics.
   const int lane = threadIdx.x & 31;
   bool head = true;
   int end = lane + 1, levels = 0;
@@ -169,10 +171,11 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
   }
 }
 
-template <int D, class R, bool GRAV>
+template <int D, class R, bool GRAV, bool WARP_SUM = (sizeof(R) == 4)>
 __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
                                                   double gz, unsigned* status) {
-  p2g_particle<D, R, GRAV>(g, nd, pp, int64_t(blockIdx.x) * blockDim.x + threadIdx.x, gx, gy, gz, status);
+  p2g_particle<D, R, GRAV, WARP_SUM>(g, nd, pp, int64_t(blockIdx.x) * blockDim.x + threadIdx.x, gx, gy, gz,
+                                     status);
 }
 
 // ---------------------------------------------------------------------------

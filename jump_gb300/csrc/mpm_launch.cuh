@@ -30,17 +30,22 @@ static inline CompMap to_dev(const CompMapH& h) {
 
 template <int D>
 void Launchers<D>::p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
-                       const double* grav, unsigned* status) {
+                       const double* grav, unsigned* status, int strategy, int threads) {
   if (pp.count <= 0) return;
   bool has_g = grav[0] != 0.0 || grav[1] != 0.0 || (D == 3 && grav[2] != 0.0);
-  unsigned nb = blocks_for(pp.count, 256);
+  if (strategy < 0) strategy = f32 ? MPM_P2G_WARP : MPM_P2G_ATOMIC;
+  const int th = threads > 0 ? threads : 256;
+  unsigned nb = blocks_for(pp.count, th);
+#define JMPM_P2G(R, G, W) p2g_kernel<D, R, G, W><<<nb, th, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status)
+  const bool w = strategy == MPM_P2G_WARP;
   if (f32) {
-    if (has_g) p2g_kernel<D, float, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
-    else p2g_kernel<D, float, false><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+    if (has_g) { if (w) JMPM_P2G(float, true, true); else JMPM_P2G(float, true, false); }
+    else { if (w) JMPM_P2G(float, false, true); else JMPM_P2G(float, false, false); }
   } else {
-    if (has_g) p2g_kernel<D, double, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
-    else p2g_kernel<D, double, false><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+    if (has_g) { if (w) JMPM_P2G(double, true, true); else JMPM_P2G(double, true, false); }
+    else { if (w) JMPM_P2G(double, false, true); else JMPM_P2G(double, false, false); }
   }
+#undef JMPM_P2G
 }
 
 // sparse grid stages: a fixed grid of CTAs strides over the listed blocks
@@ -231,10 +236,11 @@ void Launchers<D>::bs_g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const
 
 template <int D>
 void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
-                       const MatParams& mp, double dt, unsigned* status) {
+                       const MatParams& mp, double dt, unsigned* status, int threads) {
   if (pp.count <= 0) return;
-  unsigned nb = blocks_for(pp.count, 256);
-#define JMPM_G2P(R, M) g2p_kernel<D, R, M><<<nb, 256, 0, s>>>(g, nd, pp, mp, dt, status)
+  const int th = threads > 0 ? threads : 256;
+  unsigned nb = blocks_for(pp.count, th);
+#define JMPM_G2P(R, M) g2p_kernel<D, R, M><<<nb, th, 0, s>>>(g, nd, pp, mp, dt, status)
   if (f32) {
     switch (mp.type) {
       case MPM_MAT_ELASTIC: JMPM_G2P(float, MPM_MAT_ELASTIC); break;

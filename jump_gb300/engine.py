@@ -206,6 +206,34 @@ class MPMContext(_ContextBase):
             _capi.check(rc, self.L)
         return out, (tt.value if t is not None else rc)
 
+    P2G_STRATEGIES = {"atomic": _capi.MPM_P2G_ATOMIC, "warp": _capi.MPM_P2G_WARP}
+
+    def set_launch(self, p2g: str | None = None, threads: int | None = None, sort_interval: int | None = None):
+        """P2G strategy ("atomic" / "warp"), CTA size of P2G and G2P, cell-sort interval; None keeps a setting."""
+        s = -1 if p2g is None else self.P2G_STRATEGIES[p2g]
+        _capi.check(self.L.mpm_set_launch(self.h, s, -1 if threads is None else int(threads),
+                                          -1 if sort_interval is None else int(sort_interval)), self.L)
+
+    def launch(self) -> dict:
+        s, t, i = C.c_int32(), C.c_int32(), C.c_int32()
+        _capi.check(self.L.mpm_get_launch(self.h, C.byref(s), C.byref(t), C.byref(i)), self.L)
+        names = {v: k for k, v in self.P2G_STRATEGIES.items()}
+        return {"p2g": names[s.value], "threads": t.value, "sort_interval": i.value}
+
+    def tune(self, probe_steps: int = 5) -> dict:
+        """Time every P2G strategy x CTA size x sort interval from the current state, keep the
+        fastest; the simulation does not advance.  ``probes`` maps "p2g/threads/sort" to ms per step."""
+        s, t, i, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
+        allms = np.zeros(_capi.MPM_TUNE_CANDIDATES)
+        _capi.check(self.L.mpm_tune(self.h, int(probe_steps), C.byref(s), C.byref(t), C.byref(i), C.byref(ms),
+                                    _capi.dptr(allms)), self.L)
+        probes = {}
+        for q, v in enumerate(allms):
+            p2g, th, si = ("atomic", "warp")[q // 8], (128, 256)[(q // 4) % 2], (0, 1, 4, 16)[q % 4]
+            if v >= 0:
+                probes[f"{p2g}/{th}/{si}"] = float(v)
+        return dict(self.launch(), ms_per_step=ms.value, probes=probes)
+
     def _download(self, s, view):
         _capi.check(self.L.mpm_download(self.h, int(s), C.byref(view)), self.L)
 
