@@ -142,3 +142,46 @@ def test_store_every_step_matches_checkpointing():
     assert np.max(np.abs(x_a - x_b)) <= 1e-12 * np.max(np.abs(x_a))
     for k in ("E", "v0"):
         assert np.max(np.abs(ga[k] - gb[k])) <= 1e-9 * np.max(np.abs(ga[k])), k
+
+
+def test_inverse_problem_recovers_initial_velocity():
+    """Recover a smooth initial velocity field of the cantilever from the final
+    positions of all its particles: adjoint gradient steps from rest, with a
+    backtracking step length (each trial one GPU forward rollout), cut the
+    misfit by 100x and the velocity error by 3x."""
+    problem, E, v_rest, tip = setup_case(2)
+    x0 = np.concatenate([s.pos for s in problem[1]])
+    v_true = np.zeros_like(v_rest)
+    v_true[:, 1] = 0.05 * np.sin(0.5 * np.pi * x0[:, 0] / x0[:, 0].max())
+    ctx = make_context(problem, E, v_true)
+    ctx.step(NSTEPS)
+    target = final_positions(ctx)
+    ctx.close()
+
+    def misfit(v):
+        c = make_context(problem, E, v)
+        c.step(NSTEPS)
+        x = final_positions(c)
+        c.close()
+        return float(np.sum((x - target) ** 2))
+
+    v = np.zeros_like(v_true)
+    t = None
+    losses = []
+    for _ in range(8):
+        x, g = rollout_grad(problem, E, v, NSTEPS, EVERY, lambda x: 2.0 * (x - target))
+        L0 = float(np.sum((x - target) ** 2))
+        losses.append(L0)
+        gv = np.asarray(g["v0"]).reshape(v.shape)
+        if t is None:
+            t = 0.01 / np.max(np.abs(gv))  # first trial: a 1 cm/s change where the gradient is largest
+        for _ in range(20):  # backtracking: halve until the misfit drops
+            if misfit(v - t * gv) < L0:
+                break
+            t *= 0.5
+        v = v - t * gv
+        t *= 2.0
+    losses.append(misfit(v))
+    err0, err1 = np.linalg.norm(v_true), np.linalg.norm(v - v_true)
+    assert losses[-1] < 0.01 * losses[0], losses
+    assert err1 < err0 / 3.0, (err1, err0)
