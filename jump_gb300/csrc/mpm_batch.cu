@@ -510,6 +510,8 @@ int run_steps(mpm_batch* b, int64_t nsteps) {
   return launch(b, b->P, nsteps, b->threads, b->ctas_per_sm);
 }
 
+// stream-ordered (the next copy into staging waits for this transpose); the
+// create synchronises once after the last upload
 int upload(mpm_batch* b, const PartP& pp, const double* host, int per, int f0, const CompMapH& cm) {
   size_t n = size_t(pp.count) * per;
   if (n == 0 || !host) return MPM_OK;
@@ -517,7 +519,6 @@ int upload(mpm_batch* b, const PartP& pp, const double* host, int per, int f0, c
   if (b->dim == 2) Launchers<2>::aos_to_soa(b->stream, pp, b->f32, b->staging, per, f0, cm);
   else Launchers<3>::aos_to_soa(b->stream, pp, b->f32, b->staging, per, f0, cm);
   BATCH_TRY(cudaGetLastError());
-  BATCH_TRY(cudaStreamSynchronize(b->stream));
   return MPM_OK;
 }
 
@@ -772,7 +773,8 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
   }
   // the uploads compared the mirrored entries of every symmetric input (flag: problem 0's status word)
   unsigned st = 0;
-  BATCH_TRY(cudaMemcpy(&st, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  BATCH_TRY(cudaMemcpyAsync(&st, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+  BATCH_TRY(cudaStreamSynchronize(b->stream));
   if (st & ST_ASYM_STRESS) return fail(MPM_ERR_ARG, "mpm_batch_create: strain and stress must be symmetric");
   if (st & ST_ASYM_PSTRAIN) return fail(MPM_ERR_ARG, "mpm_batch_create: pstrain must be symmetric");
   BATCH_TRY(cudaMemset(b->d_status, 0, sizeof(unsigned)));

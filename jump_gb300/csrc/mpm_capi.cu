@@ -135,6 +135,12 @@ struct mpm_ctx {
 
 namespace {
 
+// orig[i] = i
+__global__ void iota_kernel(int64_t* p, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    p[i] = i;
+}
+
 void destroy_ctx(mpm_ctx* c) {
   if (!c) return;
   cudaFreeHost(c->rec_host);
@@ -242,23 +248,28 @@ int enqueue_sort(mpm_ctx* c) {
 }
 
 // host AoS array -> staging -> SoA fields [f0, f0 + cm.n)
+// host AoS array -> staging -> SoA fields [f0, f0 + cm.n).  Stream-ordered:
+// the next copy into staging waits for this transpose; the caller
+// synchronises once after the last upload, before its host arrays go.  (A
+// transpose reading page-locked host arrays in place was slower: its strided
+// accesses cross the host link in partial lines.)
 int upload(mpm_ctx* c, int b, const double* host, int per, int f0, const CompMapH& cm) {
   size_t n = size_t(c->cnt[b]) * per;
   if (n == 0) return MPM_OK;
   CUDA_TRY(cudaMemcpyAsync(c->staging, host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   launch_aos_to_soa(c, c->part(b), c->staging, per, f0, cm);
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(c->stream));
   return MPM_OK;
 }
 
+// SoA fields -> staging (creation order) -> host AoS array.  Stream-ordered
+// like upload; mpm_download synchronises once at its end.
 int download(mpm_ctx* c, int b, double* host, int per, int f0, const CompMapH& cm) {
   size_t n = size_t(c->cnt[b]) * per;
   if (n == 0 || !host) return MPM_OK;
   launch_soa_to_aos(c, c->part(b), c->staging, per, f0, cm);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(host, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(cudaStreamSynchronize(c->stream));
   return MPM_OK;
 }
 
@@ -448,10 +459,15 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
 
   // Dirichlet mask (grid.fixedNodes, set by fix_Dirichlet_grid, Dirichlet.jl:28-78)
   c->fixed_h.assign(Nn, 0);
-  if (gd->fixed_nodes)
-    for (int64_t i = 0; i < Nn; ++i)
-      for (int a = 0; a < D; ++a)
-        if (gd->fixed_nodes[a + D * i] == 1) c->fixed_h[i] |= uint8_t(1u << a);
+  if (gd->fixed_nodes) {
+    const int64_t* f = gd->fixed_nodes;
+    uint8_t* mk = c->fixed_h.data();
+    if (D == 3)
+      for (int64_t i = 0; i < Nn; ++i)
+        mk[i] = uint8_t(int(f[3 * i] == 1) | (int(f[3 * i + 1] == 1) << 1) | (int(f[3 * i + 2] == 1) << 2));
+    else
+      for (int64_t i = 0; i < Nn; ++i) mk[i] = uint8_t(int(f[2 * i] == 1) | (int(f[2 * i + 1] == 1) << 1));
+  }
   CUDA_TRY(cudaMalloc(&c->fixed, Nn));
   CUDA_TRY(cudaMemcpy(c->fixed, c->fixed_h.data(), Nn, cudaMemcpyHostToDevice));
 
@@ -553,10 +569,10 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   CUDA_TRY(cudaMemset(c->P, 0, ptot * c->esz));
   {
     // identity permutation: slot i holds particle i until the first sort
-    std::vector<int64_t> iota(size_t(c->np > 0 ? c->np : 1));
-    for (size_t i = 0; i < iota.size(); ++i) iota[i] = int64_t(i);
-    CUDA_TRY(cudaMalloc(&c->orig, iota.size() * sizeof(int64_t)));
-    CUDA_TRY(cudaMemcpy(c->orig, iota.data(), iota.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    const int64_t n = c->np > 0 ? c->np : 1;
+    CUDA_TRY(cudaMalloc(&c->orig, size_t(n) * sizeof(int64_t)));
+    iota_kernel<<<unsigned((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, c->stream>>>(c->orig, n);
+    CUDA_TRY(cudaGetLastError());
   }
   c->ncells = 1;
   for (int a = 0; a < D; ++a) c->ncells *= uint32_t(nn[a] - 1);
@@ -628,7 +644,8 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   }
   // the uploads compared the mirrored entries of every symmetric input
   unsigned st = 0;
-  CUDA_TRY(cudaMemcpy(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpyAsync(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
   if (st & ST_ASYM_STRESS) return fail(MPM_ERR_ARG, "mpm_create: strain and stress must be symmetric");
   if (st & ST_ASYM_PSTRAIN) return fail(MPM_ERR_ARG, "mpm_create: pstrain must be symmetric");
   CUDA_TRY(cudaMemset(c->status, 0, sizeof(unsigned)));
@@ -922,11 +939,11 @@ int mpm_download(mpm_ctx* c, int32_t body, const mpm_body_view* v) {
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaMemcpyAsync(v->vmstr, c->staging, size_t(c->cnt[body]) * sizeof(double),
                                cudaMemcpyDeviceToHost, c->stream));
-      CUDA_TRY(cudaStreamSynchronize(c->stream));
     } else if ((r = download(c, body, v->vmstr, 1, fi.VM, ident(1)))) {
       return r;
     }
   }
+  CUDA_TRY(cudaStreamSynchronize(c->stream));  // every copy into the caller's arrays has landed
   return MPM_OK;
 }
 
