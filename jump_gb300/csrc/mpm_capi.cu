@@ -835,6 +835,10 @@ int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* th
   void* snap = nullptr;
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   CUDA_TRY(cudaMalloc(&snap, pbytes + obytes));
+  struct FreeOnExit {
+    void* p;
+    ~FreeOnExit() { cudaFree(p); }  // every return path, after the stream's work on it
+  } guard{snap};
   char* sp = static_cast<char*>(snap);
   int rc = MPM_OK;
   auto restore = [&]() -> int {
@@ -897,7 +901,6 @@ int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* th
   int r2 = restore();
   cudaError_t e = cudaStreamSynchronize(c->stream);
   cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
-  cudaFree(snap);
   if (rc != MPM_OK) return rc;
   if (r2 != MPM_OK) return r2;
   if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_tune: ") + cudaGetErrorString(e));
