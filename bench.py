@@ -17,6 +17,7 @@ Prints one JSON line on rank 0.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -96,6 +97,22 @@ def variant_tag(args):
     if args.material != "j2":
         tag += f"_{args.material}"
     return tag
+
+
+def ncu_fp64_inst(stage: str, tag: str):
+    """FP64-pipe instructions per particle of a stage's kernels (ncu, committed variants
+    table; MUSL's g2p stage is G2P-1 + G2P-2), or None when the table has no such row."""
+    name = {"": "j2", "_jc": "jc", "_jcdamage": "jcdamage", "_musl": "musl", "_quad": "quad",
+            "_cubic": "cubic"}.get(tag)
+    path = os.path.join(ROOT, "profiles", "kernels_taylor_bar_variants_f64.txt")
+    if name is None or not os.path.exists(path):
+        return None
+    total = None
+    for line in open(path):
+        cols = [c.strip() for c in line.split("|")]
+        if len(cols) > 8 and cols[0] == name and stage in cols[1]:
+            total = (total or 0.0) + float(cols[8])
+    return total
 
 
 def ncu_traffic(kernel: str, precision: str, tag: str = ""):
@@ -361,6 +378,16 @@ def run_ours(args):
     bts = table[dom] * npart
     achieved = bts / (per[dom] * 1e-3) / 1e9
     traffic = ncu_traffic(dom, args.precision, variant_tag(args))
+    # FP64 roofline: the stage's FP64-pipe instructions (ncu count per particle) over
+    # its live CUDA-event time, against the FP64 FMA rate measured in this run
+    fp64 = None
+    inst = ncu_fp64_inst(dom, variant_tag(args)) if args.precision == "f64" else None
+    fma = C.c_double(0.0)
+    if inst is not None and _capi.lib().mpm_probe_rates(C.byref(fma), None, None) == 0 and fma.value > 0:
+        ach = inst * npart / (per[dom] * 1e-3)
+        fp64 = {"bound": "fp64_pipe", "kernel": dom, "fp64_pipe_inst_per_particle": inst, "achieved": ach,
+                "peak": fma.value, "unit": "FP64 inst/s", "frac": ach / fma.value,
+                "peak_source": "mpm_probe_rates (FP64 FMA throughput, this run)"}
     step_bytes = table["step"] * npart
     ctx.close()
 
@@ -432,7 +459,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": bts,
-                         "step_frac": step_bytes / (t_max / args.steps) / 1e9 / peak},
+                         "step_frac": step_bytes / (t_max / args.steps) / 1e9 / peak, "fp64": fp64},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps + recs.itemsize * recs.shape[1], "host_memory": "pinned",
                     "how": f"create from host arrays, {args.steps} steps each with its energies copied to the host "

@@ -244,6 +244,12 @@ int mpm_tune(mpm_ctx* ctx, int64_t probe_steps, int32_t* p2g_strategy, int32_t* 
 
 int mpm_destroy(mpm_ctx* ctx);
 
+/* Measurement aid (no counterpart in the reference): throughput of FP64 fused
+   multiply-adds, FP64 divisions and FP64 atomic additions (executed in L2, at
+   distinct coalesced addresses) on the current device, per second; the FP64
+   roofline of the step kernels.  Any output pointer may be NULL. */
+int mpm_probe_rates(double* fp64_fma_per_s, double* fp64_div_per_s, double* fp64_atomics_per_s);
+
 /* ---------------------------------------------------------------------------
  * Reverse mode (no counterpart in the reference): gradients of a loss on the
  * final particle state with respect to the initial velocities and positions

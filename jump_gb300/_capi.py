@@ -190,6 +190,7 @@ SIGNATURES = {
     "mpm_step": (C.c_int, [C.c_void_p, C.c_int64, _dp]),
     "mpm_step_energies": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, _dp, C.c_void_p]),
     "mpm_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "mpm_probe_rates": (C.c_int, [_dp, _dp, _dp]),
     "mpm_get_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "mpm_tune": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                            C.POINTER(C.c_int32), _dp, _dp]),

@@ -26,7 +26,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-O2",
 ]
 
-SOURCES = ["mpm_k2d.cu", "mpm_k3d.cu", "mpm_capi.cu", "mpm_static.cu", "mpm_batch.cu"]
+SOURCES = ["mpm_k2d.cu", "mpm_k3d.cu", "mpm_capi.cu", "mpm_static.cu", "mpm_batch.cu", "mpm_probe.cu"]
 HEADERS = ["mpm_common.cuh", "mpm_kernels.cuh", "mpm_launch.cuh", "mpm_internal.h", "mpm_sparse.cuh",
            "mpm_adjoint.cuh", "mpm_wide.cuh", "mpm_tangent.cuh", "mpm_musl.cuh", "mpm_bspline.cuh"]
 
