@@ -222,7 +222,8 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
    (MPM_P2G_ATOMIC, the FP64 default), or lanes of a warp that share a base
    node first add their values with a segmented shuffle reduction and one lane
    per run issues them (MPM_P2G_WARP, the FP32 default).  threads: CTA size of
-   the P2G and G2P launches (32 .. 256, a multiple of 32).  sort_interval: the
+   the P2G and G2P launches (32 .. 256, a multiple of 32; default 256, halved
+   down to 64 while the largest body would fill fewer than two CTAs per SM).  sort_interval: the
    counting sort by cell every that many steps (0: never); its second particle
    buffer is allocated on first use.  A negative argument keeps that setting.
    Results differ between settings only by the summation order of node sums. */
@@ -231,14 +232,14 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
 int mpm_set_launch(mpm_ctx* ctx, int32_t p2g_strategy, int32_t threads, int32_t sort_interval);
 int mpm_get_launch(mpm_ctx* ctx, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval);
 /* Times probe_steps steps of every combination of P2G strategy {atomic, warp},
-   threads {128, 256} and sort interval {0, 1, 4, 16}, each from the same saved
+   threads {64, 128, 256} and sort interval {0, 1, 4, 16}, each from the same saved
    particle state, keeps the fastest (reported through the non-NULL pointers,
    with its ms per step) and puts the particle state back: the simulation does
    not advance.  Uses a temporary device copy of the particle state.  If
    all_ms is not NULL it receives the ms per step of all MPM_TUNE_CANDIDATES
-   combinations, index (strategy * 2 + threads index) * 4 + sort index (a
+   combinations, index (strategy * 3 + threads index) * 4 + sort index (a
    negative value: not probed).  The reverse mode needs sort_interval 0. */
-#define MPM_TUNE_CANDIDATES 16
+#define MPM_TUNE_CANDIDATES 24
 int mpm_tune(mpm_ctx* ctx, int64_t probe_steps, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval,
              double* ms_per_step, double* all_ms);
 

@@ -54,7 +54,7 @@ MPM_BASIS_LINEAR = 0
 MPM_BASIS_QUAD_BSPLINE = 1
 MPM_BASIS_CUBIC_BSPLINE = 2
 
-MPM_TUNE_CANDIDATES = 16
+MPM_TUNE_CANDIDATES = 24
 MPM_P2G_ATOMIC = 0
 MPM_P2G_WARP = 1
 

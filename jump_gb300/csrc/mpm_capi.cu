@@ -577,6 +577,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   c->ncells = 1;
   for (int a = 0; a < D; ++a) c->ncells *= uint32_t(nn[a] - 1);
   c->p2g_strategy = c->f32 ? MPM_P2G_WARP : MPM_P2G_ATOMIC;
+  c->threads = spread_threads(maxn);  // small bodies: smaller CTAs, spread over the SMs
   if (prm->sort_interval > 0 && c->np > 0) {
     int r = alloc_sort(c);
     if (r != MPM_OK) return r;
@@ -853,7 +854,7 @@ int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* th
     rc = fail(MPM_ERR_CUDA, "mpm_tune: snapshot copy failed");
   const bool can_sort = rc == MPM_OK && alloc_sort(c) == MPM_OK;
   const int strategies[] = {MPM_P2G_ATOMIC, MPM_P2G_WARP};
-  const int thread_list[] = {128, 256};
+  const int thread_list[] = {64, 128, 256};
   const int sort_list[] = {0, 1, 4, 16};
   double best = 1e300;
   int bs = saved_s, bt = saved_t, bi = saved_i;

@@ -52,6 +52,23 @@ inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, 
   return mp;
 }
 
+// CTA size for n independent threads: 256, halved (down to 64) while that
+// leaves fewer than two CTAs per SM, so small problems spread over the GPU
+inline int spread_threads(int64_t n) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) ==
+                                                  cudaSuccess && v > 0)
+      sms = v;
+    else
+      sms = 152;
+  }
+  int th = 256;
+  while (th > 64 && (n + th - 1) / th < 2 * int64_t(sms)) th /= 2;
+  return th;
+}
+
 // material model types a context or batch accepts in dimension dim
 inline bool material_ok(int type, int dim) {
   if (type == MPM_MAT_ELASTIC || type == MPM_MAT_NEOHOOKEAN || type == MPM_MAT_J2) return true;

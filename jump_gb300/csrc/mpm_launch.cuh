@@ -73,21 +73,24 @@ template <int D>
 void Launchers<D>::g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, const PartP& pp, const AdjP& ad,
                            const NodeAdjP& na) {
   if (pp.count <= 0) return;
-  g2p_adj_kernel<D><<<blocks_for(pp.count, 256), 256, 0, s>>>(g, gr, pp, ad, na);
+  const int th = spread_threads(pp.count);
+  g2p_adj_kernel<D><<<blocks_for(pp.count, th), th, 0, s>>>(g, gr, pp, ad, na);
 }
 
 template <int D>
 void Launchers<D>::grid_adj(cudaStream_t s, const GridRec& gr, const NodeAdjP& na, const uint8_t* fixed, double dt,
                             double tol) {
-  grid_adj_kernel<D><<<blocks_for(na.nodeCount, 256), 256, 0, s>>>(gr, na, fixed, dt, tol);
+  const int th = spread_threads(na.nodeCount);
+  grid_adj_kernel<D><<<blocks_for(na.nodeCount, th), th, 0, s>>>(gr, na, fixed, dt, tol);
 }
 
 template <int D>
 void Launchers<D>::p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, const AdjP& ad, const NodeAdjP& na,
                            const MatParams& mp, double c1, double c2, const double* grav) {
   if (pp.count <= 0) return;
-  p2g_adj_kernel<D><<<blocks_for(pp.count, 256), 256, 0, s>>>(g, pp, ad, na, mp, c1, c2, grav[0], grav[1],
-                                                                D == 3 ? grav[2] : 0.0);
+  const int th = spread_threads(pp.count);
+  p2g_adj_kernel<D><<<blocks_for(pp.count, th), th, 0, s>>>(g, pp, ad, na, mp, c1, c2, grav[0], grav[1],
+                                                              D == 3 ? grav[2] : 0.0);
 }
 
 template <int D>

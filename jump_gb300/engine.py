@@ -229,7 +229,7 @@ class MPMContext(_ContextBase):
                                     _capi.dptr(allms)), self.L)
         probes = {}
         for q, v in enumerate(allms):
-            p2g, th, si = ("atomic", "warp")[q // 8], (128, 256)[(q // 4) % 2], (0, 1, 4, 16)[q % 4]
+            p2g, th, si = ("atomic", "warp")[q // 12], (64, 128, 256)[(q // 4) % 3], (0, 1, 4, 16)[q % 4]
             if v >= 0:
                 probes[f"{p2g}/{th}/{si}"] = float(v)
         return dict(self.launch(), ms_per_step=ms.value, probes=probes)

@@ -4,6 +4,7 @@
                                     [--warmup 2] [--steps 2] [--h 2.5e-4]
                                     [--algorithm usl|musl] [--alpha 0.99]
                                     [--basis linear|quad|cubic] [--material j2|jc|jcdamage]
+                                    [--sort-interval 0] [--energies]
 
 Launch order per step: p2g_kernel, grid_kernel, g2p_kernel (one each per body),
 after the aos_to_soa upload launches of context creation.
@@ -28,6 +29,8 @@ def main():
     ap.add_argument("--alpha", type=float, default=0.99)
     ap.add_argument("--basis", default="linear", choices=["linear", "quad", "cubic"])
     ap.add_argument("--material", default="j2", choices=list(scenarios.TAYLOR_MATERIALS))
+    ap.add_argument("--sort-interval", type=int, default=0)
+    ap.add_argument("--energies", action="store_true", help="take the EnergiesFix sums after every step")
     a = ap.parse_args()
     if a.workload == "taylor_bar":
         g, s, alg, data = scenarios.taylor_bar(h=a.h)
@@ -40,10 +43,13 @@ def main():
     musl = a.algorithm == "musl"
     ctx = MPMContext(Descriptors(g, s, tolerance=alg.tolerance, body_force=data.get("bodyforce"),
                                  dt=data["dt"], precision=a.precision, algorithm=a.algorithm,
-                                 alpha=a.alpha if musl else 1.0, basis=a.basis))
+                                 alpha=a.alpha if musl else 1.0, basis=a.basis, sort_interval=a.sort_interval))
     ctx.step(a.warmup)
     t0 = time.perf_counter()
-    ctx.step(a.steps)
+    if a.energies:
+        ctx.step_energies(a.steps, 1, 0)
+    else:
+        ctx.step(a.steps)
     dt = time.perf_counter() - t0
     n = sum(x.parCount for x in s)
     print(f"{a.workload} {a.precision} {a.algorithm} {a.basis} {a.material}: {n} particles, {a.steps} steps, {1e3 * dt / max(a.steps, 1):.3f} ms/step, "
