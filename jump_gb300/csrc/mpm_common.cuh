@@ -64,6 +64,8 @@ struct MatParams {
   // Johnson-Cook / Voce: hardening constants, rate filter time 1000 cellsize /
   // signal velocity, and the step dt it is applied with
   double A, B, C, n, epsdot0, tav, dtime;
+  // J2: 1 / (2 mu + k1) of the material (0 with per-particle Lame constants)
+  double rtmuk1;
   // Johnson-Cook with damage: thermal softening exponent, temperature rise per
   // unit plastic work chi/(density Cp), damage constants, Tm - Tr
   double m, delta, d1, d2, d3, d4, d5, depsdot0, Tr, Tm, Tmr;
@@ -219,7 +221,7 @@ __device__ __forceinline__ bool hat(const GridP& g, const R* x, Hat<D, R>& h) {
     R xl = R(g.coord[a][c]), xh = R(g.coord[a][c + 1]);
     R dl = sub_rn(x[a], xl), dh = sub_rn(x[a], xh);
     h.Nl[a] = sub_rn(R(1), mul_rn(fabs(dl), dxI));
-    h.Nh[a] = sub_rn(R(1), mul_rn(fabs(dh), dxI));
+    h.Nh[a] = sub_rn(R(1), h.Nl[a]);  // 1 - |x - xh| dxI for xl <= x <= xh
     h.gl[a] = neg_sign_scale(dl, dxI);
     h.gh[a] = neg_sign_scale(dh, dxI);
   }

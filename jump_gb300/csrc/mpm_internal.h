@@ -26,6 +26,7 @@ inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, 
   mp.kappa = mp.lambda + mp.mu;  // Material.jl:161, 315
   mp.fy = m.fy;
   mp.k1 = m.k1;
+  mp.rtmuk1 = per_particle ? 0.0 : 1.0 / (2 * mp.mu + m.k1);
   mp.A = m.A;
   mp.B = m.B;
   mp.C = m.C;

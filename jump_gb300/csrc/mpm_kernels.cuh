@@ -398,7 +398,7 @@ __device__ __forceinline__ R sqr(R a) {
 // J2 radial return, 3D (Material.jl:228-275)
 template <class R>
 __device__ __forceinline__ void j2_3d(R lam, R mu, R kappa, R fy, R k1, const R* eps, R* sig,
-                                      R* alpha, R* ep, R* vm) {
+                                      R* alpha, R* ep, R* vm, R rtmuk1 = R(0)) {
   (void)lam;
   R tr = (eps[0] + eps[1]) + eps[2];
   R tt = R(0.333333333) * tr;
@@ -407,7 +407,10 @@ __device__ __forceinline__ void j2_3d(R lam, R mu, R kappa, R fy, R k1, const R*
 #pragma unroll
   for (int c = 0; c < 6; ++c) s[c] = tmu * ((c < 3 ? eps[c] - tt : eps[c]) - ep[c]);
   // sqrt(s11^2 + s22^2 + s33^2 + 2.0*(s12^2 + s23^2 + s13^2))
-  R ns = sqrt(((sqr(s[0]) + sqr(s[1])) + sqr(s[2])) + R(2) * ((sqr(s[3]) + sqr(s[4])) + sqr(s[5])));
+  // |s| and 1/|s| from one reciprocal square root (|s| = 0: no plastic flow)
+  const R q = ((sqr(s[0]) + sqr(s[1])) + sqr(s[2])) + R(2) * ((sqr(s[3]) + sqr(s[4])) + sqr(s[5]));
+  const R rq = rsqrt(q);
+  R ns = q > R(0) ? q * rq : R(0);
   R kt = kappa * tr;
   R a0 = *alpha;
   R f_trial = ns - (k1 * a0 + fy);
@@ -415,8 +418,8 @@ __device__ __forceinline__ void j2_3d(R lam, R mu, R kappa, R fy, R k1, const R*
 #pragma unroll
   for (int c = 0; c < 6; ++c) sg[c] = c < 3 ? s[c] + kt : s[c];  // sigma_trial
   if (!(f_trial <= R(0))) {
-    R inv = R(1) / ns;
-    R lamp = ((ns - k1 * a0) - fy) / (tmu + k1);
+    R inv = rq;
+    R lamp = rtmuk1 != R(0) ? ((ns - k1 * a0) - fy) * rtmuk1 : ((ns - k1 * a0) - fy) / (tmu + k1);
     a0 += lamp;
     R cc = tmu * lamp;
 #pragma unroll
@@ -637,20 +640,17 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
                                                   const MatParams& mp, bool fin, unsigned* status) {
   using L = Layout<D>;
   // F <- F (I + L dt)   (:523)
-  R F[D * D], Fn[D * D], A[D][D];
+  R F[D * D], Fn[D * D];
 #pragma unroll
   for (int c = 0; c < D * D; ++c) F[c] = *field<R>(pp, L::F + c, p);
-#pragma unroll
-  for (int k = 0; k < D; ++k)
-#pragma unroll
-    for (int j = 0; j < D; ++j) A[k][j] = (k == j) ? Ldt[k][j] + R(1) : Ldt[k][j];  // I + L dt
+  // F (I + L dt) = F + F (L dt)
 #pragma unroll
   for (int j = 0; j < D; ++j)
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      R s = F[i] * A[0][j];
+      R s = F[i + D * j];
 #pragma unroll
-      for (int k = 1; k < D; ++k) s += F[i + D * k] * A[k][j];
+      for (int k = 0; k < D; ++k) s += F[i + D * k] * Ldt[k][j];
       Fn[i + D * j] = s;
     }
   double Fd[D * D];
@@ -724,7 +724,7 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
     for (int c = 0; c < L::PS; ++c) ep[c] = *field<R>(pp, L::EP + c, p);
     R vm;
     if (D == 3)
-      j2_3d<R>(lam, mu, kappa, R(mp.fy), R(mp.k1), eps, sig, &alpha, ep, &vm);
+      j2_3d<R>(lam, mu, kappa, R(mp.fy), R(mp.k1), eps, sig, &alpha, ep, &vm, R(mp.rtmuk1));
     else
       j2_2d<R>(lam, mu, kappa, R(mp.fy), R(mp.k1), eps, sig, &alpha, ep, &vm);
     *field<R>(pp, L::ALPHA, p) = alpha;
