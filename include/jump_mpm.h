@@ -248,7 +248,8 @@ int mpm_destroy(mpm_ctx* ctx);
 /* Measurement aid (no counterpart in the reference): throughput of FP64 fused
    multiply-adds, FP64 divisions and FP64 atomic additions (executed in L2, at
    distinct coalesced addresses) on the current device, per second; the FP64
-   roofline of the step kernels.  Any output pointer may be NULL. */
+   roofline of the step kernels.  Only the rates whose output pointer is not
+   NULL are measured. */
 int mpm_probe_rates(double* fp64_fma_per_s, double* fp64_div_per_s, double* fp64_atomics_per_s);
 
 /* ---------------------------------------------------------------------------

@@ -89,13 +89,20 @@ extern "C" int mpm_probe_rates(double* fp64_fma_per_s, double* fp64_div_per_s, d
   const double nthreads = double(blocks) * threads;
   int bad = 0;
   float ms = 0.f;
-  const int fma_iters = 16384, div_iters = 256, atom_iters = 1024;
-  bad |= time_launch(s, [&] { fma_probe_kernel<<<blocks, threads, 0, s>>>(fma_iters, 0.999999, 1e-9, buf); }, &ms);
-  if (!bad && fp64_fma_per_s) *fp64_fma_per_s = nthreads * fma_iters * kChains / (ms * 1e-3);
-  bad |= time_launch(s, [&] { div_probe_kernel<<<blocks, threads, 0, s>>>(div_iters, 3.0, buf); }, &ms);
-  if (!bad && fp64_div_per_s) *fp64_div_per_s = nthreads * div_iters * 4 / (ms * 1e-3);
-  bad |= time_launch(s, [&] { atomic_probe_kernel<<<blocks, threads, 0, s>>>(atom_iters, buf, nbuf - 1); }, &ms);
-  if (!bad && fp64_atomics_per_s) *fp64_atomics_per_s = nthreads * atom_iters / (ms * 1e-3);
+  const int fma_iters = 4096, div_iters = 256, atom_iters = 1024;
+  // only the rates asked for (non-NULL outputs) are measured
+  if (fp64_fma_per_s) {
+    bad |= time_launch(s, [&] { fma_probe_kernel<<<blocks, threads, 0, s>>>(fma_iters, 0.999999, 1e-9, buf); }, &ms);
+    if (!bad) *fp64_fma_per_s = nthreads * fma_iters * kChains / (ms * 1e-3);
+  }
+  if (fp64_div_per_s && !bad) {
+    bad |= time_launch(s, [&] { div_probe_kernel<<<blocks, threads, 0, s>>>(div_iters, 3.0, buf); }, &ms);
+    if (!bad) *fp64_div_per_s = nthreads * div_iters * 4 / (ms * 1e-3);
+  }
+  if (fp64_atomics_per_s && !bad) {
+    bad |= time_launch(s, [&] { atomic_probe_kernel<<<blocks, threads, 0, s>>>(atom_iters, buf, nbuf - 1); }, &ms);
+    if (!bad) *fp64_atomics_per_s = nthreads * atom_iters / (ms * 1e-3);
+  }
   cudaStreamSynchronize(s);
   cudaFree(buf);
   cudaStreamDestroy(s);
