@@ -70,3 +70,32 @@ def test_material_constants():
     assert m.lambda_ == 1000.0 * 0.3 / 1.3 / (1 - 0.6) and getattr(m, "lambda") == m.lambda_
     p = J.ElastoPlasticMaterial(117e9, 0.35, 8930, 400e6, 100e6, 2)
     assert p.kappa == p.lambda_ + p.mu
+
+
+def test_johnson_cook_with_damage_descriptor():
+    """JohnsonCookMaterialWithDamage(strength, damage) packs as material type 5 with
+    the strength part's constants, chi, Cp, m and the damage constants, and passes
+    its state arrays (damage_init, dam, damage_part.temp starting at Tr, vmStr)."""
+    import ctypes as C
+    from jump_gb300 import _capi
+    from jump_gb300.engine import Descriptors
+    g, s, alg, data = scenarios.taylor_bar(h=1e-3, radius=2e-3, length=6e-3, width=8e-3, height=10e-3)
+    scenarios.apply_dirichlet(g, data)
+    n = s[0].parCount
+    st = J.JohnsonCookMaterial(200e9, 0.33, 7850.0, 490e6, 383e6, 0.0123, 0.45, 0.5, 0.94, 0.9, 452.0, 1e-3, n)
+    s[0].mat = J.JohnsonCookMaterialWithDamage(st, J.JohnsonCookDamage(0.07, 1.7, -0.5, 0.015, 0.1, 0.5,
+                                                                       293.0, 1800.0, n))
+    assert s[0].mat.E == 200e9 and s[0].mat.alpha is st.alpha  # the strength part's constants and state
+    assert np.all(s[0].mat.damage_part.temp == 293.0) and s[0].mat.damage_part.Tmr == 1800.0 - 293.0
+    d = Descriptors(g, s, tolerance=alg.tolerance, dt=data["dt"])
+    m = d.bodies[0].mat
+    assert m.type == _capi.MPM_MAT_JOHNSON_COOK_DAMAGE == 5
+    assert (m.E, m.nu, m.density, m.A, m.B, m.C, m.n, m.epsdot0) == (200e9, 0.33, 7850.0, 490e6, 383e6, 0.0123,
+                                                                     0.45, 0.5)
+    assert (m.m, m.chi, m.Cp) == (0.94, 0.9, 452.0)
+    assert (m.d1, m.d2, m.d3, m.d4, m.d5, m.depsdot0, m.Tr, m.Tm) == (0.07, 1.7, -0.5, 0.015, 0.1, 0.5, 293.0, 1800.0)
+    b = d.bodies[0]
+    for k in ("damage_init", "damage", "temperature", "alpha", "alphadot", "vmstr"):
+        assert C.cast(getattr(b, k), C.c_void_p).value is not None, k
+    assert b.temperature[0] == 293.0
+    assert not b.pstrain  # the damage state replaces J2's plastic strain
