@@ -540,6 +540,8 @@ def run_ensemble(args):
     clocks = sampler.stop()
     dev, _, batched = aggregate(dist, ens.last_ms() / 1e3, float(len(mine)))
     npart = allreduce_sum(dist, float(ens.particles))
+    acc_idx = list(range(0, len(probs), max(1, len(probs) // 16)))[:16]
+    got = [ens.download(i) for i in acc_idx] if args.precision == "f32" and world == 1 else None
     ens.close()
     if rank != 0 or world > 1:
         if rank == 0:
@@ -561,11 +563,30 @@ def run_ensemble(args):
         t_one += time.perf_counter() - t1
         c.close()
     one_by_one = n / (t_one * n / len(sample))
+    accuracy = None
+    if got is not None:
+        # the error the FP32 batch's solves/s come at: against an FP64 batch of the same
+        # problems after the same steps (max |difference| / max |FP64 value| per field)
+        ref = Ensemble([member(mine[i]) for i in acc_idx], precision="f64")
+        ref.step(args.warmup + steps)
+        diff, size = {}, {}
+        for j in range(len(acc_idx)):
+            for a, b in zip(got[j], ref.download(j)):
+                for f in ("pos", "velocity", "F", "stress"):
+                    diff[f] = max(diff.get(f, 0.0), float(np.max(np.abs(getattr(a, f) - getattr(b, f)))))
+                    size[f] = max(size.get(f, 0.0), float(np.max(np.abs(getattr(b, f)))))
+        ref.close()
+        # normalised by the field's largest FP64 magnitude over the sampled problems (a problem
+        # whose stress is still rounding noise, before its bodies touch, would otherwise divide
+        # noise by noise)
+        accuracy = {"fields": {f: diff[f] / (size[f] or 1.0) for f in diff}, "problems": len(acc_idx),
+                    "how": "FP32 batch against an FP64 batch of the same problems after the same steps: "
+                           "max |difference| / max |FP64 value| over the sampled problems, per field"}
     print(json.dumps(ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks,
-                                   (one_by_one, len(sample)), world)))
+                                   (one_by_one, len(sample)), world, accuracy)))
 
 
-def ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks, one_by_one, world):
+def ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks, one_by_one, world, accuracy=None):
     out = {"metric": "solves/s", "value": batched, "unit": "solves/s", "n_gpus": world, "steps": steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * dev / steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": args.precision, "data": "synthetic (seeded ensemble)",
@@ -578,6 +599,8 @@ def ensemble_line(args, n, steps, dev, batched, npart, tune, wall, clocks, one_b
         out["one_by_one"] = {"value": v, "unit": "solves/s", "sample": ns,
                              "how": "same problems, one context each, step graph replayed per step"}
         out["speedup_vs_one_by_one"] = batched / v
+    if accuracy is not None:
+        out["error_vs_fp64"] = accuracy
     return out
 
 
