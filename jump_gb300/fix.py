@@ -11,6 +11,8 @@ import os
 
 import numpy as np
 
+from .output import jfloat
+
 
 class FixBase:
     needs_particles = True
@@ -61,23 +63,25 @@ class EnergiesFix(FixBase):
         self.kinEnergy.append(KE)
         self.strEnergy.append(SE)
         self.recordTime.append(time)
-        self.file.write(f"{time} {KE} {SE}\n")
+        self.file.write(f"{jfloat(time)} {jfloat(KE)} {jfloat(SE)}\n")
 
 
 class DisplacementFix(FixBase):
     """Position minus initial position of the particle found at ``point``
-    (Fix.jl:37-102, 214-218)."""
+    (Fix.jl:37-102, 214-218).  As in the reference, the match uses x and y
+    only, takes the first matching particle of a solid, and a later solid with
+    a match replaces an earlier one."""
 
     def __init__(self, solids, point, dir):
         point = np.asarray(point, dtype=np.float64)
         self.solids = solids
         self.index = None
         for s, solid in enumerate(solids):
-            dist = np.sqrt(np.sum((solid.pos - point[None, :]) ** 2, axis=1))
-            hit = np.nonzero(dist < 1e-10)[0]
+            dx = solid.pos[:, 0] - point[0]
+            dy = solid.pos[:, 1] - point[1]
+            hit = np.nonzero(np.sqrt(dx * dx + dy * dy) < 1e-10)[0]
             if hit.size:
                 self.index = (s, int(hit[0]))
-                break
         if self.index is None:
             raise ValueError("No particle with that position found\n")
         self.file = _open_fresh(os.path.join(dir, "recorded-position.txt"))
@@ -86,7 +90,7 @@ class DisplacementFix(FixBase):
         s, p = self.index
         solid = self.solids[s]
         x = solid.pos[p] - solid.pos0[p]
-        self.file.write(f"{time} {x[0]} {x[1]}\n")
+        self.file.write(f"{jfloat(time)} {jfloat(x[0])} {jfloat(x[1])}\n")
 
 
 def compute(fixes, time):

@@ -105,6 +105,12 @@ def plotParticles_2D(plot: OvitoOutput, solids, lims, ncells, counter: int):
                         f.write(f"{jfloat(vel[p, 0])}  ")
                     elif v == "vy":
                         f.write(f"{jfloat(vel[p, 1])}  ")
+                    elif v == "damage":
+                        f.write(f"{jfloat(solid.damage[p])}  ")
+                    elif v == "crackforce":
+                        f.write(f"{jfloat(solid.crackForce[p])}  ")
+                    elif v == "color":
+                        f.write(f"{jfloat(solid.color[p])}  ")
                 f.write("\n")
 
 

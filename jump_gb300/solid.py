@@ -134,6 +134,11 @@ class _SolidBase:
         self.stress = matrix_array(n, d)
         self.rigid = isinstance(mat, RigidMaterial)
         self.youngs = None
+        # Solid.jl:93-96: surface classification, damage and crack force of the
+        # TLMPM/phase-field solvers; written by the 2D dump, zeros here
+        self.color = np.zeros(n)
+        self.damage = np.zeros(n)
+        self.crackForce = np.zeros(n)
 
 
 class Solid2D(_SolidBase):

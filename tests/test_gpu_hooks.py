@@ -71,3 +71,41 @@ def test_solver_energies_fix_vs_oracle(interval, oracle_lib, tmp_path):
     assert float(lines[-1].split()[0]) == want_t[-1]
     for s, st in zip(solids, o.download_all()):
         assert np.max(np.abs(s.pos - st.pos)) <= 1e-12
+
+
+def test_solver_dumps_and_fixes_vs_oracle(oracle_lib, tmp_path):
+    """solve_explicit_dynamics_2D with OvitoOutput, DisplacementFix and EnergiesFix:
+    the LAMMPS dump of every hook step (counter % 10 == 0) holds the oracle's
+    particle state after that step, the displacement file the tracked
+    particle's displacement, the energies file the sums of the downloaded state."""
+    from jump_gb300 import DisplacementFix, OvitoOutput
+    grid, solids, alg, data = disks()
+    data["total_time"] = 0.025
+    o = oracle_lib.OracleContext(descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"]))
+    times = step_times(data["time"], data["total_time"], data["dt"])
+    want = {}
+    for c in range(len(times)):
+        o.step(1)
+        if c % 10 == 0:
+            want[c] = o.download_all()
+    track = solids[1].pos[5].copy()
+    out = OvitoOutput(10, str(tmp_path) + "/", ["sigmaxx", "sigmayy", "vx", "vy"])
+    disp = DisplacementFix(solids, track, str(tmp_path))
+    en = EnergiesFix(solids, str(tmp_path / "energies.txt"))
+    solve_explicit_dynamics_2D(grid, solids, LinearBasis(), alg, out, [disp, en], data)
+    for c, st in want.items():
+        rows = [r.split() for r in open(tmp_path / f"dump_p.{c}.LAMMPS").read().splitlines()[9:]]
+        vals = np.array([[float(v) for v in r] for r in rows])
+        x = np.concatenate([b.pos for b in st])
+        v = np.concatenate([b.velocity for b in st])
+        sxx = np.concatenate([b.stress.reshape(-1, 2, 2)[:, 0, 0] for b in st])
+        assert vals.shape == (len(x), 9) and np.array_equal(vals[:, 0], np.arange(1, len(x) + 1))
+        assert np.max(np.abs(vals[:, 2:4] - x)) <= 1e-10 * np.max(np.abs(x))
+        assert np.max(np.abs(vals[:, 7:9] - v)) <= 1e-10 * np.max(np.abs(v))
+        assert np.max(np.abs(vals[:, 5] - sxx)) <= 1e-10 * max(np.max(np.abs(sxx)), 1.0)  # noise before contact
+    dlines = open(tmp_path / "recorded-position.txt").read().splitlines()
+    assert [float(l.split()[0]) for l in dlines] == [times[c] for c in sorted(want)]
+    last = np.array([float(t) for t in dlines[-1].split()[1:]])
+    ref = want[max(want)][1].pos[5] - track
+    assert np.max(np.abs(last - ref)) <= 1e-10 * max(np.max(np.abs(ref)), 1e-300)
+    assert len(open(tmp_path / "energies.txt").read().splitlines()) == len(want)

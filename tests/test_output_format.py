@@ -1,0 +1,56 @@
+"""LAMMPS dumps and fix files in the reference's text formats, on hand-set
+particle states: plotParticles_2D/3D (Output.jl:146-290; header, column order,
+the two-space columns, elastic materials' zero plastic columns), EnergiesFix
+(Fix.jl:248-270) and DisplacementFix (Fix.jl:37-102, 214-218), with Julia's
+Float64 printing."""
+import numpy as np
+
+import jump_gb300 as J
+from jump_gb300.output import OvitoOutput, plotParticles_2D, plotParticles_3D
+
+
+def test_dump_2d(tmp_path):
+    s1 = J.Solid2D(np.array([[0.25, 0.5], [0.75, 0.125]]), J.ElasticMaterial(1e3, 0.3, 1000.0, 2))
+    s2 = J.Solid2D(np.array([[0.5, 0.5]]), J.ElastoPlasticMaterial(1e3, 0.3, 1000.0, 1.0, 0.0, 1))
+    s1.stress[0] = [[1.5, 0.25], [0.25, -2.0]]
+    s1.velocity[1] = [1e-5, 3.0]
+    s2.mat.alpha[0] = 0.125
+    s2.mat.vmStr[0] = 2.5
+    s2.stress[0] = [[0.5, 0.0], [0.0, 0.25]]
+    s2.damage[0] = 0.5
+    outs = ["pstrain", "vonMises", "sigmaxx", "sigmayy", "pressure", "vx", "vy", "damage"]
+    plotParticles_2D(OvitoOutput(10, str(tmp_path) + "/", outs), [s1, s2], [1.0, 2.0], [10, 20], 30)
+    assert open(tmp_path / "dump_p.30.LAMMPS").read() == (
+        "ITEM: TIMESTEP \n0\nITEM: NUMBER OF ATOMS\n3 \nITEM: BOX BOUNDS sm sm sm\n0 1.0\n0 2.0\n0 0\n"
+        "ITEM: ATOMS id type x y z pstrain vonMises sigmaxx sigmayy pressure vx vy damage \n"
+        "1 1 0.25 0.5 0 0 0 1.5 -2.0 -0.5 0.0  0.0  0.0  \n"
+        "2 1 0.75 0.125 0 0 0 0.0 0.0 0.0 1.0e-5  3.0  0.0  \n"
+        "3 2 0.5 0.5 0 0.125 2.5 0.5 0.25 0.75 0.0  0.0  0.5  \n")
+
+
+def test_dump_3d(tmp_path):
+    s = J.Solid3D(np.array([[0.25, 0.5, 0.75]]), J.ElastoPlasticMaterial(1e3, 0.3, 1000.0, 1.0, 0.0, 1))
+    s.mat.alpha[0] = 0.25
+    s.velocity[0] = [1.0, -2.0, 0.5]
+    s.stress[0] = np.diag([1.0, 2.0, 4.0])
+    out = OvitoOutput(5, str(tmp_path) + "/", ["pstrain", "vonMises", "vx", "vy", "vz", "pressure"])
+    plotParticles_3D(out, [s], [1.0, 2.0, 3.0], [4, 8, 12], 0)
+    assert open(tmp_path / "dump_p.0.LAMMPS").read() == (
+        "ITEM: TIMESTEP \n0\nITEM: NUMBER OF ATOMS\n1 \nITEM: BOX BOUNDS sm sm sm\n0 1.0\n0 2.0\n0 3.0\n"
+        "ITEM: ATOMS id type x y z pstrain vonMises vx vy vz pressure \n"
+        "1 1 0.25 0.5 0.75 0.25 0.0 1.0  -2.0  0.5  7.0  \n")
+
+
+def test_fix_files(tmp_path):
+    s1 = J.Solid2D(np.array([[0.25, 0.5], [0.75, 0.125]]), J.ElasticMaterial(1e3, 0.3, 1000.0, 2))
+    s2 = J.Solid2D(np.array([[0.5, 0.5], [0.75, 0.125]]), J.ElasticMaterial(1e3, 0.3, 1000.0, 2))
+    e = J.EnergiesFix([s1], str(tmp_path / "energies.txt"))
+    e.record(1e-5, 0.5, 2.0)
+    e.close()
+    assert open(tmp_path / "energies.txt").read() == "1.0e-5 0.5 2.0\n"
+    d = J.DisplacementFix([s1, s2], [0.75, 0.125], str(tmp_path))
+    assert d.index == (1, 1)  # a later solid with a matching particle replaces an earlier one
+    s2.pos[1] += [0.25, -0.125]
+    d.compute(0.5)
+    d.close()
+    assert open(tmp_path / "recorded-position.txt").read() == "0.5 0.25 -0.125\n"
