@@ -51,12 +51,26 @@ class EnergiesFix(FixBase):
         self.kinEnergy, self.strEnergy, self.recordTime = [], [], []
 
     def compute(self, time):
-        KE = 0.0
-        SE = 0.0
+        # the reference's summation order: particles left to right across the solids,
+        # dot(v, v) and sum(stress .* strain) over components in column-major order
+        ke_terms, se_terms = [np.zeros(1)], [np.zeros(1)]
         for solid in self.solids:
-            v = solid.velocity
-            KE += float(np.sum(0.5 * solid.mass * np.einsum("pi,pi->p", v, v)))
-            SE += float(np.sum(0.5 * solid.volume * np.einsum("pij,pij->p", solid.stress, solid.strain)))
+            if solid.parCount == 0:
+                continue
+            v, st, ep = solid.velocity, solid.stress, solid.strain
+            d = v.shape[1]
+            dot = v[:, 0] * v[:, 0]
+            for a in range(1, d):
+                dot = dot + v[:, a] * v[:, a]
+            ke_terms.append(0.5 * solid.mass * dot)
+            se = st[:, 0, 0] * ep[:, 0, 0]
+            for j in range(d):
+                for i in range(d):
+                    if i or j:
+                        se = se + st[:, i, j] * ep[:, i, j]
+            se_terms.append(0.5 * solid.volume * se)
+        KE = float(np.cumsum(np.concatenate(ke_terms))[-1])
+        SE = float(np.cumsum(np.concatenate(se_terms))[-1])
         self.record(time, KE, SE)
 
     def record(self, time, KE, SE):

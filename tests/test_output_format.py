@@ -54,3 +54,30 @@ def test_fix_files(tmp_path):
     d.compute(0.5)
     d.close()
     assert open(tmp_path / "recorded-position.txt").read() == "0.5 0.25 -0.125\n"
+
+
+def test_energies_fix_sums_in_the_reference_order(tmp_path):
+    """KE += 0.5 m dot(v, v), SE += 0.5 V sum(stress .* strain), particle by particle
+    (Fix.jl:248-270): the host EnergiesFix reproduces that loop bit for bit."""
+    rng = np.random.default_rng(3)
+    sols = []
+    for n in (7, 0, 5):
+        s = J.Solid2D(rng.random((n, 2)), J.ElasticMaterial(1e3, 0.3, 1000.0, max(n, 1)))
+        s.mass[:] = rng.random(n)
+        s.volume[:] = rng.random(n)
+        s.velocity[:] = rng.standard_normal((n, 2))
+        s.stress[:] = rng.standard_normal((n, 2, 2))
+        s.strain[:] = rng.standard_normal((n, 2, 2))
+        sols.append(s)
+    KE = SE = 0.0
+    for s in sols:
+        for p in range(s.parCount):
+            v = s.velocity[p]
+            KE += 0.5 * s.mass[p] * (v[0] * v[0] + v[1] * v[1])
+            st, ep = s.stress[p], s.strain[p]
+            SE += 0.5 * s.volume[p] * (((st[0, 0] * ep[0, 0] + st[1, 0] * ep[1, 0]) + st[0, 1] * ep[0, 1])
+                                       + st[1, 1] * ep[1, 1])
+    e = J.EnergiesFix(sols, str(tmp_path / "e.txt"))
+    e.compute(0.25)
+    e.close()
+    assert e.kinEnergy == [KE] and e.strEnergy == [SE]
