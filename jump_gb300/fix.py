@@ -32,11 +32,10 @@ class EmptyFix(FixBase):
 
 
 def _open_fresh(filename):
+    """rm the file if it exists, then open it for appending (Fix.jl:61-67,
+    111-114); a missing directory is an error, as there."""
     if os.path.isfile(filename):
         os.remove(filename)
-    d = os.path.dirname(filename)
-    if d:
-        os.makedirs(d, exist_ok=True)
     return open(filename, "a")
 
 
@@ -98,7 +97,7 @@ class DisplacementFix(FixBase):
                 self.index = (s, int(hit[0]))
         if self.index is None:
             raise ValueError("No particle with that position found\n")
-        self.file = _open_fresh(os.path.join(dir, "recorded-position.txt"))
+        self.file = _open_fresh(dir + "recorded-position.txt")  # string(dir, "recorded-position.txt")
 
     def compute(self, time):
         s, p = self.index

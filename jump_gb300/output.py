@@ -40,7 +40,11 @@ class EmptyOutput(OutputType):
 
 
 class OvitoOutput(OutputType):
-    """OvitoOutput(interval, dir, outs): LAMMPS dumps dump_p.<counter>.LAMMPS."""
+    """OvitoOutput(interval, dir, outs): LAMMPS dumps dir * "dump_p.<counter>.LAMMPS"
+    (Output.jl:40-57).  As in the reference, file names are the plain
+    concatenation of dir and the name (dir normally ends in a separator), an
+    existing dir loses its dir * "*.LAMMPS" files and a missing one is made
+    with a one-level mkdir."""
     needs_particles = True
 
     def __init__(self, interval: int, dir: str, outs):
@@ -48,10 +52,10 @@ class OvitoOutput(OutputType):
         self.dir = dir
         self.outs = list(outs)
         if os.path.isdir(dir):
-            for f in glob.glob(os.path.join(dir, "*.LAMMPS")):
+            for f in glob.glob(glob.escape(dir) + "*.LAMMPS"):
                 os.remove(f)
         else:
-            os.makedirs(dir, exist_ok=True)
+            os.mkdir(dir)
 
     def plot(self, solids, lims, ncells, counter):
         d = solids[0].dim if solids else 2
@@ -81,7 +85,7 @@ def _elastic(mat):
 def plotParticles_2D(plot: OvitoOutput, solids, lims, ncells, counter: int):
     """Output.jl:146-222."""
     n = sum(s.parCount for s in solids)
-    with open(os.path.join(plot.dir, f"dump_p.{int(counter)}.LAMMPS"), "a") as f:
+    with open(plot.dir + f"dump_p.{int(counter)}.LAMMPS", "a") as f:
         _header(f, n, lims, 2, plot.outs)
         pid = 0
         for s, solid in enumerate(solids, start=1):
@@ -117,7 +121,7 @@ def plotParticles_2D(plot: OvitoOutput, solids, lims, ncells, counter: int):
 def plotParticles_3D(plot: OvitoOutput, solids, lims, ncells, counter: int):
     """Output.jl:224-290."""
     n = sum(s.parCount for s in solids)
-    with open(os.path.join(plot.dir, f"dump_p.{int(counter)}.LAMMPS"), "a") as f:
+    with open(plot.dir + f"dump_p.{int(counter)}.LAMMPS", "a") as f:
         _header(f, n, lims, 3, plot.outs)
         pid = 0
         for s, solid in enumerate(solids, start=1):

@@ -90,7 +90,7 @@ def test_solver_dumps_and_fixes_vs_oracle(oracle_lib, tmp_path):
             want[c] = o.download_all()
     track = solids[1].pos[5].copy()
     out = OvitoOutput(10, str(tmp_path) + "/", ["sigmaxx", "sigmayy", "vx", "vy"])
-    disp = DisplacementFix(solids, track, str(tmp_path))
+    disp = DisplacementFix(solids, track, str(tmp_path) + "/")
     en = EnergiesFix(solids, str(tmp_path / "energies.txt"))
     solve_explicit_dynamics_2D(grid, solids, LinearBasis(), alg, out, [disp, en], data)
     for c, st in want.items():

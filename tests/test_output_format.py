@@ -48,7 +48,7 @@ def test_fix_files(tmp_path):
     e.record(1e-5, 0.5, 2.0)
     e.close()
     assert open(tmp_path / "energies.txt").read() == "1.0e-5 0.5 2.0\n"
-    d = J.DisplacementFix([s1, s2], [0.75, 0.125], str(tmp_path))
+    d = J.DisplacementFix([s1, s2], [0.75, 0.125], str(tmp_path) + "/")
     assert d.index == (1, 1)  # a later solid with a matching particle replaces an earlier one
     s2.pos[1] += [0.25, -0.125]
     d.compute(0.5)
@@ -81,3 +81,19 @@ def test_energies_fix_sums_in_the_reference_order(tmp_path):
     e.compute(0.25)
     e.close()
     assert e.kinEnergy == [KE] and e.strEnergy == [SE]
+
+
+def test_paths_are_concatenated_as_in_the_reference(tmp_path):
+    """string(dir, name) (Output.jl:48,155; Fix.jl:61): no separator is added,
+    an existing dir loses only dir * "*.LAMMPS", a missing one is made."""
+    d = tmp_path / "out"
+    d.mkdir()
+    (d / "dump_p.7.LAMMPS").write_text("old")
+    (d / "keep.txt").write_text("kept")
+    OvitoOutput(1, str(d) + "/", ["vx"])
+    assert sorted(p.name for p in d.iterdir()) == ["keep.txt"]
+    s = J.Solid2D(np.array([[0.25, 0.5]]), J.ElasticMaterial(1e3, 0.3, 1000.0, 1))
+    plotParticles_2D(OvitoOutput(1, str(tmp_path / "new") + "/", ["vx"]), [s], [1.0, 1.0], [2, 2], 3)
+    assert (tmp_path / "new" / "dump_p.3.LAMMPS").is_file()
+    J.DisplacementFix([s], [0.25, 0.5], str(tmp_path / "run_")).close()
+    assert (tmp_path / "run_recorded-position.txt").is_file()
