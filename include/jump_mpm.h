@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 6
+#define JUMP_MPM_ABI_VERSION 7
 
 /* status codes */
 #define MPM_OK               0
@@ -221,7 +221,11 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
    P2G strategy of the linear basis: every particle issues its own FP64 atomics
    (MPM_P2G_ATOMIC, the FP64 default), or lanes of a warp that share a base
    node first add their values with a segmented shuffle reduction and one lane
-   per run issues them (MPM_P2G_WARP, the FP32 default).  threads: CTA size of
+   per run issues them (MPM_P2G_WARP, the FP32 default); MPM_P2G_TILE and
+   MPM_P2G_TILE_WARP stage those two forms in a shared-memory tile of the node
+   box a CTA's particles cover and issue one FP64 atomic per node value and CTA
+   (a CTA whose box exceeds the tile, 256 nodes for CTAs of 64 threads, else
+   512, falls back to per-particle atomics).  threads: CTA size of
    the P2G and G2P launches (32 .. 256, a multiple of 32; default 256, halved
    down to 64 while the largest body would fill fewer than two CTAs per SM).  sort_interval: the
    counting sort by cell every that many steps (0: never); its second particle
@@ -229,9 +233,13 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
    Results differ between settings only by the summation order of node sums. */
 #define MPM_P2G_ATOMIC 0
 #define MPM_P2G_WARP   1
+#define MPM_P2G_TILE   2
+#define MPM_P2G_TILE_WARP 3
 int mpm_set_launch(mpm_ctx* ctx, int32_t p2g_strategy, int32_t threads, int32_t sort_interval);
 int mpm_get_launch(mpm_ctx* ctx, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval);
-/* Times probe_steps steps of every combination of P2G strategy {atomic, warp},
+/* Times probe_steps steps (rounded up to whole sort intervals, so that every
+   probe pays its share of sorts) of every combination of P2G strategy
+   {atomic, warp, tile, tile_warp},
    threads {64, 128, 256} and sort interval {0, 1, 4, 16}, each from the same saved
    particle state, keeps the fastest (reported through the non-NULL pointers,
    with its ms per step) and puts the particle state back: the simulation does
@@ -239,7 +247,7 @@ int mpm_get_launch(mpm_ctx* ctx, int32_t* p2g_strategy, int32_t* threads, int32_
    all_ms is not NULL it receives the ms per step of all MPM_TUNE_CANDIDATES
    combinations, index (strategy * 3 + threads index) * 4 + sort index (a
    negative value: not probed).  The reverse mode needs sort_interval 0. */
-#define MPM_TUNE_CANDIDATES 24
+#define MPM_TUNE_CANDIDATES 48
 int mpm_tune(mpm_ctx* ctx, int64_t probe_steps, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval,
              double* ms_per_step, double* all_ms);
 

@@ -800,7 +800,7 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
 
 int mpm_set_launch(mpm_ctx* c, int32_t p2g_strategy, int32_t threads, int32_t sort_interval) {
   if (!c) return fail(MPM_ERR_ARG, "mpm_set_launch: null context");
-  if (p2g_strategy >= 0 && p2g_strategy != MPM_P2G_ATOMIC && p2g_strategy != MPM_P2G_WARP)
+  if (p2g_strategy > MPM_P2G_TILE_WARP)
     return fail(MPM_ERR_ARG, "mpm_set_launch: unknown P2G strategy");
   if (threads >= 0 && (threads < 32 || threads > 256 || threads % 32 != 0))
     return fail(MPM_ERR_ARG, "mpm_set_launch: threads must be a multiple of 32 in 32 .. 256");
@@ -853,7 +853,7 @@ int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* th
       cudaMemcpyAsync(sp + pbytes, c->orig, obytes, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
     rc = fail(MPM_ERR_CUDA, "mpm_tune: snapshot copy failed");
   const bool can_sort = rc == MPM_OK && alloc_sort(c) == MPM_OK;
-  const int strategies[] = {MPM_P2G_ATOMIC, MPM_P2G_WARP};
+  const int strategies[] = {MPM_P2G_ATOMIC, MPM_P2G_WARP, MPM_P2G_TILE, MPM_P2G_TILE_WARP};
   const int thread_list[] = {64, 128, 256};
   const int sort_list[] = {0, 1, 4, 16};
   double best = 1e300;
@@ -874,15 +874,19 @@ int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* th
         invalidate_graphs(c);
         if ((rc = restore())) break;
         if ((rc = launch_one_step(c))) break;  // captures the graphs outside the timed region
+        // a whole number of sort intervals, so that each probe pays its share of
+        // sorts (the warm-up step above sorted: the window's sorts fall on its
+        // steps si, 2 si, ...)
+        const int64_t nprobe = si > 0 ? (probe_steps + si - 1) / si * si : probe_steps;
         CUDA_TRY(cudaEventRecord(c->e0, c->stream));
-        for (int64_t k = 0; k < probe_steps && rc == MPM_OK; ++k) rc = launch_one_step(c);
+        for (int64_t k = 0; k < nprobe && rc == MPM_OK; ++k) rc = launch_one_step(c);
         CUDA_TRY(cudaEventRecord(c->e1, c->stream));
         cudaError_t e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) rc = fail(MPM_ERR_CUDA, std::string("mpm_tune: ") + cudaGetErrorString(e));
         if (rc != MPM_OK) break;
         float ms = 0.f;
         CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
-        const double per = double(ms) / double(probe_steps);
+        const double per = double(ms) / double(nprobe);
         if (all_ms) all_ms[idx] = per;
         if (per < best) {
           best = per;

@@ -9,6 +9,8 @@
 //   energies   EnergiesFix sums (Fix.jl:248-270)
 #pragma once
 
+#include <climits>
+
 #include "mpm_common.cuh"
 #include "mpm_sparse.cuh"
 #include "../../include/jump_mpm.h"
@@ -21,35 +23,26 @@ __device__ __forceinline__ R* field(const PartP& pp, int f, int64_t p) {
 }
 
 // ---------------------------------------------------------------------------
-// P2G of particle pp.begin + t.  All 32 lanes of a warp call it together
-// (t consecutive across the warp); lanes with t >= pp.count do nothing.
-// WARP_SUM (MPM_P2G_WARP): lanes with the same base node first add their
-// values by a segmented shuffle reduction and one lane per run issues the
-// atomics; otherwise (MPM_P2G_ATOMIC) every lane issues its own.
-template <int D, class R, bool GRAV, bool WARP_SUM = (sizeof(R) == 4)>
-__device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
-                                             double gx, double gy, double gz, unsigned* status) {
+// P2G values of particle p (SolveExplicitSolidMechanics2D.jl:391-423) at its
+// 2^D stencil corners, handed to put(k, val) (k: corner index, bit 0 +x,
+// bit 1 +y, bit 2 +z; val: m N, m N v (D), f (D) and, in contact mode, the
+// normal sum m grad N (D)) on the lanes that issue them, and the node blocks
+// of the stencil flagged.  All lanes in `mask` call it together with t
+// consecutive across the warp; lanes with ok == false add nothing.
+// WARP_SUM: lanes with the same base node first add their values by a
+// segmented shuffle reduction and only the run's first lane calls put;
+// otherwise every lane with ok calls put.
+template <int D, class R, bool GRAV, bool WARP_SUM, class Put>
+__device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& nd, const PartP& pp, int64_t p,
+                                                  bool ok, const Hat<D, R>& h, unsigned mask, double gx,
+                                                  double gy, double gz, Put&& put) {
   using L = Layout<D>;
   constexpr int NV = 1 + 3 * D;  // per node: m, p0 (D), f (D), normal (D, contact mode)
   const bool NRM = nd.nrm != nullptr;
-  // lanes of this warp holding a particle (a contiguous low range)
-  const unsigned mask = __ballot_sync(0xffffffffu, t < pp.count);
-  if (t >= pp.count) return;
-  int64_t p = pp.begin + t;
-  R x[D];
-#pragma unroll
-  for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
-  Hat<D, R> h{};  // zeros on lanes whose cell lies outside (they add nothing)
-  const bool ok = hat<D, R>(g, x, h);
-  if (!ok) {
-    atomicOr(status, ST_OUT_OF_GRID);
-    if (!WARP_SUM) return;
-  }
   Corners<D, R> cr;
   R m = R(0), V = R(0), v[D], ms[L::S];
   if (ok) {
-    if (D == 3) corner_nodes<D, R>(g, h, cr);  // N and grad N are formed per z pair below
-    else corners<D, R>(g, h, cr);
+    if (D == 2) corners<D, R>(g, h, cr);  // in 3D N and grad N are formed per z pair below
     m = *field<R>(pp, L::M, p);
     V = *field<R>(pp, L::VOL, p);
   }
@@ -65,12 +58,13 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
   }
   // WARP_SUM: lanes with the same base node (runs of consecutive lanes, long
   // after the cell sort) add their contributions with a segmented shuffle
-  // reduction, and only the run's first lane issues the FP64 atomics.
+  // reduction, and only the run's first lane issues them.
   const int lane = threadIdx.x & 31;
   bool head = true;
   int end = lane + 1, levels = 0;
   if (WARP_SUM) {
-    long long key = ok ? (long long)cr.node[0] : -1ll - lane;
+    long long key = ok ? (long long)(int64_t(h.c[0]) + g.nx * int64_t(h.c[1]) + (D == 3 ? g.nxy * int64_t(h.c[D - 1]) : 0))
+                       : -1ll - lane;
     long long kprev = __shfl_up_sync(mask, key, 1);
     head = lane == 0 || kprev != key;
     unsigned heads = __ballot_sync(mask, head);
@@ -79,9 +73,6 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
     unsigned run = __reduce_max_sync(mask, head ? unsigned(end - lane) : 0u);
     while ((1u << levels) < run) ++levels;
   }
-  const int64_t Nn = nd.nodeCount;
-  // one node's values: the FP32 run sum, then the FP64 atomics (k: corner index,
-  // bit 0 +x, bit 1 +y, bit 2 +z)
   auto emit = [&](int k, R* val) {
     if (WARP_SUM) {
       const int nv = NRM ? NV : 1 + 2 * D;
@@ -95,17 +86,7 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
         }
       }
     }
-    if (ok && head) {
-      const int64_t n = cr.node[k];
-      atomicAdd(nd.m + n, to_f64(val[0]));
-#pragma unroll
-      for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, to_f64(val[1 + a]));
-#pragma unroll
-      for (int a = 0; a < D; ++a) atomicAdd(nd.f + a * Nn + n, to_f64(val[1 + D + a]));
-      if (NRM)
-#pragma unroll
-        for (int a = 0; a < D; ++a) atomicAdd(nd.nrm + a * Nn + n, to_f64(val[1 + 2 * D + a]));
-    }
+    if (ok && head) put(k, val);
   };
   if (ok && head && nd.bflag) mark_blocks<D>(nd, h.c);
   if constexpr (D == 3) {
@@ -171,11 +152,154 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
   }
 }
 
+// node value q of node n: m (q = 0), p0 (1 .. D), f (D+1 .. 2D), normal (2D+1 .. 3D)
+template <int D>
+__device__ __forceinline__ double* node_value(const NodeP& nd, int q, int64_t n) {
+  const int64_t Nn = nd.nodeCount;
+  if (q == 0) return nd.m + n;
+  if (q <= D) return nd.p0 + (q - 1) * Nn + n;
+  if (q <= 2 * D) return nd.f + (q - 1 - D) * Nn + n;
+  return nd.nrm + (q - 1 - 2 * D) * Nn + n;
+}
+
+// FP64 atomics of one corner's values at global node n
+template <int D, class R>
+__device__ __forceinline__ void add_node_values(const NodeP& nd, int64_t n, const R* val) {
+  const int64_t Nn = nd.nodeCount;
+  atomicAdd(nd.m + n, to_f64(val[0]));
+#pragma unroll
+  for (int a = 0; a < D; ++a) atomicAdd(nd.p0 + a * Nn + n, to_f64(val[1 + a]));
+#pragma unroll
+  for (int a = 0; a < D; ++a) atomicAdd(nd.f + a * Nn + n, to_f64(val[1 + D + a]));
+  if (nd.nrm)
+#pragma unroll
+    for (int a = 0; a < D; ++a) atomicAdd(nd.nrm + a * Nn + n, to_f64(val[1 + 2 * D + a]));
+}
+
+// global node index of corner k of base node `base`
+template <int D>
+__device__ __forceinline__ int64_t corner_node(const GridP& g, int64_t base, int k) {
+  return base + (k & 1) + g.nx * ((k >> 1) & 1) + (D == 3 ? g.nxy * (k >> 2) : 0);
+}
+
+// P2G of particle pp.begin + t with FP64 atomics at L2: one per lane and node
+// value (MPM_P2G_ATOMIC) or one per run of lanes sharing a base node
+// (WARP_SUM, MPM_P2G_WARP).  All 32 lanes of a warp call it together
+// (t consecutive across the warp); lanes with t >= pp.count do nothing.
+template <int D, class R, bool GRAV, bool WARP_SUM = (sizeof(R) == 4)>
+__device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
+                                             double gx, double gy, double gz, unsigned* status) {
+  using L = Layout<D>;
+  // lanes of this warp holding a particle (a contiguous low range)
+  const unsigned mask = __ballot_sync(0xffffffffu, t < pp.count);
+  if (t >= pp.count) return;
+  int64_t p = pp.begin + t;
+  R x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
+  Hat<D, R> h{};  // zeros on lanes whose cell lies outside (they add nothing)
+  const bool ok = hat<D, R>(g, x, h);
+  if (!ok) {
+    atomicOr(status, ST_OUT_OF_GRID);
+    if (!WARP_SUM) return;
+  }
+  const int64_t base = int64_t(h.c[0]) + g.nx * int64_t(h.c[1]) + (D == 3 ? g.nxy * int64_t(h.c[D - 1]) : 0);
+  p2g_corner_values<D, R, GRAV, WARP_SUM>(g, nd, pp, p, ok, h, mask, gx, gy, gz, [&](int k, const R* val) {
+    add_node_values<D, R>(nd, corner_node<D>(g, base, k), val);
+  });
+}
+
 template <int D, class R, bool GRAV, bool WARP_SUM = (sizeof(R) == 4)>
 __global__ void __launch_bounds__(256) p2g_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
                                                   double gz, unsigned* status) {
   p2g_particle<D, R, GRAV, WARP_SUM>(g, nd, pp, int64_t(blockIdx.x) * blockDim.x + threadIdx.x, gx, gy, gz,
                                      status);
+}
+
+// ---------------------------------------------------------------------------
+// P2G staged in a shared-memory grid tile (MPM_P2G_TILE, MPM_P2G_TILE_WARP).
+// The CTA finds the box of nodes its particles' stencils cover (min/max base
+// cell per axis); if the box holds at most `cap` nodes, the particles add their
+// corner values into an FP64 tile of the box in shared memory (shared atomics;
+// after the warp-segmented sum under WARP_SUM) and the CTA then adds each
+// non-zero tile value to its node with one global FP64 atomic, so a node gets
+// one L2 atomic per value and CTA instead of one per particle.  A CTA whose box
+// is larger (particles far apart, as without the cell sort) falls back to the
+// per-particle global atomics.  Adding a zero is skipped: node accumulators
+// start at +0 and x + 0 == x, so the sums are those of the other strategies up
+// to summation order.  Dynamic shared memory: cap * (1 + 2D, or 1 + 3D in
+// contact mode) doubles.  blockDim.x is a multiple of 32 and at most 256.
+template <int D, class R, bool GRAV, bool WARP_SUM>
+__global__ void __launch_bounds__(256) p2g_tile_kernel(GridP g, NodeP nd, PartP pp, double gx, double gy,
+                                                       double gz, unsigned* status, int cap) {
+  using L = Layout<D>;
+  extern __shared__ double tile[];
+  __shared__ int wlo[8][3], whi[8][3];
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t p = pp.begin + t;
+  Hat<D, R> h{};
+  bool ok = false;
+  if (t < pp.count) {
+    R x[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
+    ok = hat<D, R>(g, x, h);
+    if (!ok) atomicOr(status, ST_OUT_OF_GRID);
+  }
+  // the box of base cells, per warp then over the CTA
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const int wl = __reduce_min_sync(0xffffffffu, ok ? h.c[a] : INT_MAX);
+    const int wh = __reduce_max_sync(0xffffffffu, ok ? h.c[a] : INT_MIN);
+    if (lane == 0) {
+      wlo[warp][a] = wl;
+      whi[warp][a] = wh;
+    }
+  }
+  __syncthreads();
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // axis 2 stays 0 in 2D
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    lo[a] = INT_MAX;
+    hi[a] = INT_MIN;
+    for (int w = 0; w < nwarps; ++w) {
+      lo[a] = min(lo[a], wlo[w][a]);
+      hi[a] = max(hi[a], whi[w][a]);
+    }
+  }
+  if (lo[0] > hi[0]) return;  // no particle of this CTA inside the grid (uniform)
+  const int e0 = hi[0] - lo[0] + 2, e1 = hi[1] - lo[1] + 2, e2 = D == 3 ? hi[2] - lo[2] + 2 : 1;
+  // box volume in 64 bits: a spread-out CTA can cover most of a large grid
+  const int64_t vol64 = int64_t(e0) * e1 * e2;
+  const bool use = vol64 <= int64_t(cap);  // uniform over the CTA
+  const int vol = use ? int(vol64) : 0;
+  const int nv = nd.nrm ? 1 + 3 * D : 1 + 2 * D;
+  if (use) {
+    for (int i = threadIdx.x; i < vol * nv; i += blockDim.x) tile[i] = 0.0;
+    __syncthreads();
+  }
+  const int64_t base = int64_t(h.c[0]) + g.nx * int64_t(h.c[1]) + (D == 3 ? g.nxy * int64_t(h.c[D - 1]) : 0);
+  const int lbase = use ? (h.c[0] - lo[0]) + e0 * ((h.c[1] - lo[1]) + (D == 3 ? e1 * (h.c[D - 1] - lo[D - 1]) : 0)) : 0;
+  p2g_corner_values<D, R, GRAV, WARP_SUM>(g, nd, pp, p, ok, h, 0xffffffffu, gx, gy, gz, [&](int k, const R* val) {
+    if (use) {
+      // ok lanes only: lo <= c <= hi per axis, so 0 <= l < vol
+      const int l = lbase + (k & 1) + e0 * ((k >> 1) & 1) + (D == 3 ? e0 * e1 * (k >> 2) : 0);
+      for (int q = 0; q < nv; ++q) atomicAdd(tile + q * vol + l, to_f64(val[q]));
+    } else {
+      add_node_values<D, R>(nd, corner_node<D>(g, base, k), val);
+    }
+  });
+  if (!use) return;  // uniform
+  __syncthreads();
+  for (int l = threadIdx.x; l < vol; l += blockDim.x) {
+    const int ix = l % e0, iy = (l / e0) % e1, iz = l / (e0 * e1);
+    const int64_t n = int64_t(lo[0] + ix) + g.nx * int64_t(lo[1] + iy) + (D == 3 ? g.nxy * int64_t(lo[2] + iz) : 0);
+    for (int q = 0; q < nv; ++q) {
+      const double s = tile[q * vol + l];
+      if (s != 0.0) atomicAdd(node_value<D>(nd, q, n), s);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

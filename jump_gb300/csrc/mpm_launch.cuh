@@ -36,8 +36,25 @@ void Launchers<D>::p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
   if (strategy < 0) strategy = f32 ? MPM_P2G_WARP : MPM_P2G_ATOMIC;
   const int th = threads > 0 ? threads : 256;
   unsigned nb = blocks_for(pp.count, th);
+  const bool w = strategy == MPM_P2G_WARP || strategy == MPM_P2G_TILE_WARP;
+  if (strategy == MPM_P2G_TILE || strategy == MPM_P2G_TILE_WARP) {
+    // tile of at most cap nodes: 40 KB at most (512 nodes x 10 values), under
+    // the default 48 KB of dynamic shared memory
+    const int cap = th <= 64 ? 256 : 512;
+    const size_t smem = size_t(cap) * size_t(nd.nrm ? 1 + 3 * D : 1 + 2 * D) * sizeof(double);
+#define JMPM_P2GT(R, G, W) \
+  p2g_tile_kernel<D, R, G, W><<<nb, th, smem, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status, cap)
+    if (f32) {
+      if (has_g) { if (w) JMPM_P2GT(float, true, true); else JMPM_P2GT(float, true, false); }
+      else { if (w) JMPM_P2GT(float, false, true); else JMPM_P2GT(float, false, false); }
+    } else {
+      if (has_g) { if (w) JMPM_P2GT(double, true, true); else JMPM_P2GT(double, true, false); }
+      else { if (w) JMPM_P2GT(double, false, true); else JMPM_P2GT(double, false, false); }
+    }
+#undef JMPM_P2GT
+    return;
+  }
 #define JMPM_P2G(R, G, W) p2g_kernel<D, R, G, W><<<nb, th, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status)
-  const bool w = strategy == MPM_P2G_WARP;
   if (f32) {
     if (has_g) { if (w) JMPM_P2G(float, true, true); else JMPM_P2G(float, true, false); }
     else { if (w) JMPM_P2G(float, false, true); else JMPM_P2G(float, false, false); }

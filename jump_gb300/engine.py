@@ -206,10 +206,12 @@ class MPMContext(_ContextBase):
             _capi.check(rc, self.L)
         return out, (tt.value if t is not None else rc)
 
-    P2G_STRATEGIES = {"atomic": _capi.MPM_P2G_ATOMIC, "warp": _capi.MPM_P2G_WARP}
+    P2G_STRATEGIES = {"atomic": _capi.MPM_P2G_ATOMIC, "warp": _capi.MPM_P2G_WARP, "tile": _capi.MPM_P2G_TILE,
+                      "tile_warp": _capi.MPM_P2G_TILE_WARP}
 
     def set_launch(self, p2g: str | None = None, threads: int | None = None, sort_interval: int | None = None):
-        """P2G strategy ("atomic" / "warp"), CTA size of P2G and G2P, cell-sort interval; None keeps a setting."""
+        """P2G strategy ("atomic", "warp", "tile", "tile_warp"), CTA size of P2G and G2P, cell-sort
+        interval; None keeps a setting."""
         s = -1 if p2g is None else self.P2G_STRATEGIES[p2g]
         _capi.check(self.L.mpm_set_launch(self.h, s, -1 if threads is None else int(threads),
                                           -1 if sort_interval is None else int(sort_interval)), self.L)
@@ -229,7 +231,8 @@ class MPMContext(_ContextBase):
                                     _capi.dptr(allms)), self.L)
         probes = {}
         for q, v in enumerate(allms):
-            p2g, th, si = ("atomic", "warp")[q // 12], (64, 128, 256)[(q // 4) % 3], (0, 1, 4, 16)[q % 4]
+            p2g, th, si = ("atomic", "warp", "tile", "tile_warp")[q // 12], (64, 128, 256)[(q // 4) % 3], \
+                (0, 1, 4, 16)[q % 4]
             if v >= 0:
                 probes[f"{p2g}/{th}/{si}"] = float(v)
         return dict(self.launch(), ms_per_step=ms.value, probes=probes)

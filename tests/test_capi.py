@@ -34,7 +34,7 @@ def test_every_declared_symbol_is_exported(L):
 
 
 def test_abi_version(L):
-    assert L.mpm_abi_version() == _capi.ABI_VERSION == 6
+    assert L.mpm_abi_version() == _capi.ABI_VERSION == 7
 
 
 def test_argument_errors_without_gpu(L):
@@ -55,3 +55,16 @@ def test_argument_errors_without_gpu(L):
     assert L.mpm_create(C.byref(g), None, 0, C.byref(p), C.byref(h)) == _capi.MPM_ERR_ARG
     assert L.mpm_step(None, 1, None) == _capi.MPM_ERR_ARG
     assert L.mpm_destroy(None) == _capi.MPM_OK
+
+
+def test_python_constants_match_the_header():
+    """Every integer #define of include/jump_mpm.h that _capi also names has the
+    header's value (strategies, tuner candidates, materials, error codes)."""
+    import os
+    import re
+    hdr = os.path.join(os.path.dirname(__file__), "..", "include", "jump_mpm.h")
+    defs = dict(re.findall(r"^#define\s+(MPM_\w+)\s+\(?(-?\d+)\)?\s*$", open(hdr).read(), re.M))
+    shared = [k for k in defs if hasattr(_capi, k)]
+    assert {"MPM_P2G_TILE", "MPM_P2G_TILE_WARP", "MPM_TUNE_CANDIDATES", "MPM_OK"} <= set(shared)
+    for k in shared:
+        assert getattr(_capi, k) == int(defs[k]), k
