@@ -63,7 +63,7 @@ def test_python_constants_match_the_header():
     import os
     import re
     hdr = os.path.join(os.path.dirname(__file__), "..", "include", "jump_mpm.h")
-    defs = dict(re.findall(r"^#define\s+(MPM_\w+)\s+\(?(-?\d+)\)?\s*$", open(hdr).read(), re.M))
+    defs = dict(re.findall(r"^#define\s+(MPM_\w+)\s+\(?(-?\d+)\)?(?:\s*/\*.*)?\s*$", open(hdr).read(), re.M))
     shared = [k for k in defs if hasattr(_capi, k)]
     assert {"MPM_P2G_TILE", "MPM_P2G_TILE_WARP", "MPM_TUNE_CANDIDATES", "MPM_OK"} <= set(shared)
     for k in shared:
