@@ -43,8 +43,11 @@ METRIC = "particle-updates/s"
 #        writes x3 v3 V F9 eps6 sigma6 alpha ep6 vm  = 36 doubles -> 520 B
 # plus the grid share (8 particles per active node): P2G 7 doubles/node, G2P 6
 # doubles/node gathered, grid update 13 doubles/node -> 600 B per particle-update.
+# FP64 particles add the hat cache (per axis a cell code, int32, and the lower hat
+# value, double): P2G writes it and the G2P of the same step reads it, 36 B each.
+HAT = 36
 BYTES = {
-    "f64": {"p2g": 112 + 7, "g2p": 520 + 6, "step": 600},
+    "f64": {"p2g": 112 + HAT + 7, "g2p": 520 + HAT + 6, "step": 600 + 2 * HAT},
     "f32": {"p2g": 56 + 7, "g2p": 260 + 3, "step": 330},
 }
 # MUSL, FP64, 3D J2: P2G as above; the G2P stage is G2P-1 (reads x3 v3 m, writes v3
@@ -53,10 +56,10 @@ BYTES = {
 BYTES_MUSL = {"p2g": 112 + 7, "g2p": 80 + 3 + 496 + 6, "step": 720}
 # Johnson-Cook, FP64: G2P reads x3 v3 V0 F9 eps6 sigma6 alpha alphadot (30 doubles)
 # and writes x3 v3 V F9 eps6 sigma6 alpha alphadot vm (31 doubles) -> 488 B
-BYTES_JC = {"p2g": 112 + 7, "g2p": 488 + 6, "step": 560}
+BYTES_JC = {"p2g": 112 + HAT + 7, "g2p": 488 + HAT + 6, "step": 560 + 2 * HAT}
 # Johnson-Cook with damage, FP64: as Johnson-Cook plus damage_init, damage and
 # temperature read and written and vm read (kept by failed particles) -> 544 B
-BYTES_JCD = {"p2g": 112 + 7, "g2p": 544 + 6, "step": 616}
+BYTES_JCD = {"p2g": 112 + HAT + 7, "g2p": 544 + HAT + 6, "step": 616 + 2 * HAT}
 
 
 def launches_per_run(args, nbodies):
@@ -399,6 +402,9 @@ def run_ours(args):
     table = BYTES_MUSL if args.algorithm == "musl" else (BYTES_JCD if args.material == "jcdamage" and args.precision == "f64" else
                                                          BYTES_JC if args.material == "jc" and args.precision == "f64"
                                                          else BYTES[args.precision])
+    if args.basis != "linear" and args.precision == "f64" and args.algorithm != "musl":
+        # the B-spline kernels compute their weights in place: no hat cache
+        table = {k: v - (HAT if k in ("p2g", "g2p") else 2 * HAT) for k, v in table.items()}
     bts = table[dom] * npart
     achieved = bts / (per[dom] * 1e-3) / 1e9
     traffic = ncu_traffic(dom, args.precision, variant_tag(args))

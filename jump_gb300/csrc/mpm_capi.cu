@@ -65,6 +65,8 @@ struct mpm_ctx {
   FieldIdx fi{};
   void* P = nullptr;          // particle SoA in use
   void* Palt = nullptr;       // the other buffer of the counting sort (sort_interval > 0)
+  int32_t* hat_c = nullptr;   // hat cache of the linear USL step (PartP::hat_c), dim * np
+  void* hat_nl = nullptr;     // and its lower hat values (particle type), dim * np
   int64_t* orig = nullptr;    // orig[slot]: original (creation-order) index of the particle in slot
   int64_t* orig_alt = nullptr;
   int cur = 0;                // which physical buffer P is (selects the captured graph)
@@ -123,6 +125,18 @@ struct mpm_ctx {
     pp.count = cnt[b];
     return pp;
   }
+  // the linear USL step's P2G and G2P: part(b) with the hat cache, for FP64
+  // particles (the G2P saves the FP64 work of the hat: 0.270 -> 0.239 ms per
+  // step on the Taylor bar, net 0.464 -> 0.447 ms; with FP32 particles the hat
+  // is FP32 work and reading it back was slower than recomputing it)
+  PartP step_part(int b) const {
+    PartP pp = part(b);
+    if (!f32) {
+      pp.hat_c = hat_c;
+      pp.hat_nl = hat_nl;
+    }
+    return pp;
+  }
   PartP all() const {
     PartP pp;
     pp.base = P;
@@ -150,6 +164,7 @@ void destroy_ctx(mpm_ctx* c) {
   }
   cudaFree(c->P);
   cudaFree(c->Palt);
+  cudaFree(c->hat_c);
   cudaFree(c->orig);
   cudaFree(c->orig_alt);
   cudaFree(c->sp.key);
@@ -359,10 +374,10 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
       if (D == 2) Launchers<2>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
       else Launchers<3>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
     } else if (D == 2) {
-      Launchers<2>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status,
+      Launchers<2>::p2g(c->stream, c->g, field_of(b), c->step_part(b), c->f32, c->prm.body_force, c->status,
                         c->p2g_strategy, c->threads);
     } else {
-      Launchers<3>::p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status,
+      Launchers<3>::p2g(c->stream, c->g, field_of(b), c->step_part(b), c->f32, c->prm.body_force, c->status,
                         c->p2g_strategy, c->threads);
     }
   }
@@ -385,10 +400,10 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
       if (D == 2) Launchers<2>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
       else Launchers<3>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
     } else if (D == 2) {
-      Launchers<2>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status,
+      Launchers<2>::g2p(c->stream, c->g, field_of(b), c->step_part(b), c->f32, c->mats[b], c->prm.dt, c->status,
                         c->threads);
     } else {
-      Launchers<3>::g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->prm.dt, c->status,
+      Launchers<3>::g2p(c->stream, c->g, field_of(b), c->step_part(b), c->f32, c->mats[b], c->prm.dt, c->status,
                         c->threads);
     }
   }
@@ -567,6 +582,15 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   size_t ptot = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1);
   CUDA_TRY(cudaMalloc(&c->P, ptot * c->esz));
   CUDA_TRY(cudaMemset(c->P, 0, ptot * c->esz));
+  if (!c->f32 && c->np > 0 && c->g.nn[0] < (1 << 27) && c->g.nn[1] < (1 << 27) && c->g.nn[2] < (1 << 27)) {
+    // hat cache: int32 codes, then the lower hat values (one allocation)
+    const size_t nc = size_t(c->dim) * size_t(c->np);
+    const size_t cbytes = (nc * sizeof(int32_t) + 15) / 16 * 16;
+    char* hb = nullptr;
+    CUDA_TRY(cudaMalloc(&hb, cbytes + nc * c->esz));
+    c->hat_c = reinterpret_cast<int32_t*>(hb);
+    c->hat_nl = hb + cbytes;
+  }
   {
     // identity permutation: slot i holds particle i until the first sort
     const int64_t n = c->np > 0 ? c->np : 1;

@@ -131,6 +131,11 @@ struct PartP {
   int64_t pitch;   // elements per field
   int64_t begin;   // first particle of this launch
   int64_t count;   // particles of this launch
+  // Optional hat cache (hat_put / hat_get): the linear P2G stores each
+  // particle's hat and the G2P of the same step reads it back, since both see
+  // the positions before the G2P moves them.  Null: the G2P recomputes it.
+  int32_t* hat_c = nullptr;  // D * pitch: cell | bit 27 gl == 0 | bit 28 gl < 0 | bit 29 gh == 0 | bit 30 gh < 0; -1 outside
+  void* hat_nl = nullptr;    // D * pitch values of the particle type: the hat value at the lower node
 };
 
 // Buffers of the counting sort by (body, cell).
@@ -224,6 +229,44 @@ __device__ __forceinline__ bool hat(const GridP& g, const R* x, Hat<D, R>& h) {
     h.Nh[a] = sub_rn(R(1), h.Nl[a]);  // 1 - |x - xh| dxI for xl <= x <= xh
     h.gl[a] = neg_sign_scale(dl, dxI);
     h.gh[a] = neg_sign_scale(dh, dxI);
+  }
+  return true;
+}
+
+// Hat cache of particle p (PartP::hat_c / hat_nl).  The gradient factors are
+// 0 or -+dxI (neg_sign_scale), so two bits each restore them exactly, and the
+// upper value is recomputed with hat()'s rounding: hat_get gives bit for bit
+// the Hat that hat() computes from the same position, without its FP64 work.
+template <int D, class R>
+__device__ __forceinline__ void hat_put(const PartP& pp, int64_t p, bool ok, const Hat<D, R>& h) {
+  if constexpr (sizeof(R) != 8) return;  // FP64 particles only: an FP32 hat is cheaper to recompute
+  if (!pp.hat_c) return;
+  R* nl = static_cast<R*>(pp.hat_nl);
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    int32_t code = -1;
+    if (ok) {
+      code = h.c[a] | (int32_t(is_zero_bits(h.gl[a])) << 27) | (int32_t(is_neg_bits(h.gl[a])) << 28) |
+             (int32_t(is_zero_bits(h.gh[a])) << 29) | (int32_t(is_neg_bits(h.gh[a])) << 30);
+      nl[a * pp.pitch + p] = h.Nl[a];
+    }
+    pp.hat_c[a * pp.pitch + p] = code;
+  }
+}
+
+template <int D, class R>
+__device__ __forceinline__ bool hat_get(const GridP& g, const PartP& pp, int64_t p, Hat<D, R>& h) {
+  const R* nl = static_cast<const R*>(pp.hat_nl);
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const int32_t code = pp.hat_c[a * pp.pitch + p];
+    if (code < 0) return false;
+    const R dxI = R(g.dxI[a]);
+    h.c[a] = code & ((1 << 27) - 1);
+    h.Nl[a] = nl[a * pp.pitch + p];
+    h.Nh[a] = sub_rn(R(1), h.Nl[a]);
+    h.gl[a] = ((code >> 27) & 1) ? R(0) : (((code >> 28) & 1) ? -dxI : dxI);
+    h.gh[a] = ((code >> 29) & 1) ? R(0) : (((code >> 30) & 1) ? -dxI : dxI);
   }
   return true;
 }

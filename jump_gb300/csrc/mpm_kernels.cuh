@@ -200,6 +200,7 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
   Hat<D, R> h{};  // zeros on lanes whose cell lies outside (they add nothing)
   const bool ok = hat<D, R>(g, x, h);
   if (!ok) {
+    hat_put<D, R>(pp, p, false, h);  // the G2P of this step skips it too
     atomicOr(status, ST_OUT_OF_GRID);
     if (!WARP_SUM) return;
   }
@@ -207,6 +208,7 @@ __device__ __forceinline__ void p2g_particle(const GridP& g, const NodeP& nd, co
   p2g_corner_values<D, R, GRAV, WARP_SUM>(g, nd, pp, p, ok, h, mask, gx, gy, gz, [&](int k, const R* val) {
     add_node_values<D, R>(nd, corner_node<D>(g, base, k), val);
   });
+  if (ok) hat_put<D, R>(pp, p, true, h);  // for the G2P of this step
 }
 
 template <int D, class R, bool GRAV, bool WARP_SUM = (sizeof(R) == 4)>
@@ -244,6 +246,7 @@ __global__ void __launch_bounds__(256) p2g_tile_kernel(GridP g, NodeP nd, PartP 
 #pragma unroll
     for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
     ok = hat<D, R>(g, x, h);
+    hat_put<D, R>(pp, p, ok, h);
     if (!ok) atomicOr(status, ST_OUT_OF_GRID);
   }
   // the box of base cells, per warp then over the CTA
@@ -875,7 +878,9 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
 #pragma unroll
   for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
   Hat<D, R> h;
-  if (!hat<D, R>(g, x, h)) {
+  // the hat the P2G of this step stored (same positions), else computed here
+  const bool ok = (sizeof(R) == 8 && pp.hat_c) ? hat_get<D, R>(g, pp, p, h) : hat<D, R>(g, x, h);
+  if (!ok) {
     atomicOr(status, ST_OUT_OF_GRID);
     return;
   }
