@@ -126,8 +126,8 @@ struct mpm_ctx {
     return pp;
   }
   // the linear USL step's P2G and G2P: part(b) with the hat cache, for FP64
-  // particles (the G2P saves the FP64 work of the hat: 0.270 -> 0.239 ms per
-  // step on the Taylor bar, net 0.464 -> 0.447 ms; with FP32 particles the hat
+  // particles (the G2P saves the FP64 work of the hat: 0.270 -> 0.238 ms per
+  // step on the Taylor bar, net 0.464 -> 0.438 ms; with FP32 particles the hat
   // is FP32 work and reading it back was slower than recomputing it)
   PartP step_part(int b) const {
     PartP pp = part(b);
