@@ -471,13 +471,28 @@ __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt,
   }
 }
 
-// grid update over the nodes of the listed blocks
+// The list compaction and the grid update of the plain step in one launch:
+// CTAs of 256 threads stride over all node blocks, four at a time (64 threads
+// per block).  A flagged block goes on the list (which the next step's clear
+// reads), its flag is reset, and its nodes are updated (grid_node).
+// Saves the compact_blocks launch; the list order is immaterial (as with the
+// warp-aggregated appends of compact_blocks).  blockDim.x must be 256.
 template <int D, bool F32COPY>
-__global__ void __launch_bounds__(256) grid_kernel(NodeP nd, double dt, double tol) {
-  const int64_t work = int64_t(*nd.bcount) * 64;
-  for (int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < work; w += int64_t(gridDim.x) * blockDim.x) {
-    int64_t i = block_node<D>(nd, nd.blist[w >> 6], int(w & 63));
-    if (i >= 0) grid_node<D, F32COPY>(nd, i, dt, tol);
+__global__ void __launch_bounds__(256) grid_scan_kernel(NodeP nd, double dt, double tol) {
+  const int sub = threadIdx.x >> 6, l = threadIdx.x & 63;
+  const int64_t stride = int64_t(gridDim.x) * 4;
+  for (int64_t b0 = int64_t(blockIdx.x) * 4; b0 < nd.nblk; b0 += stride) {  // same trip count CTA-wide
+    const int64_t blk = b0 + sub;
+    const bool on = blk < nd.nblk && nd.bflag[blk] != 0u;
+    __syncthreads();  // the block's 64 threads have read its flag before it is reset
+    if (on && l == 0) {
+      nd.bflag[blk] = 0u;
+      nd.blist[atomicAdd(nd.bcount, 1u)] = uint32_t(blk);
+    }
+    if (on) {
+      const int64_t i = block_node<D>(nd, uint32_t(blk), l);
+      if (i >= 0) grid_node<D, F32COPY>(nd, i, dt, tol);
+    }
   }
 }
 

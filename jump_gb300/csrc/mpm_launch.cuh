@@ -73,9 +73,11 @@ static inline unsigned sparse_ctas(const NodeP& nd) {
 
 template <int D>
 void Launchers<D>::grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy) {
-  compact_blocks_kernel<<<blocks_for(nd.nblk, 256), 256, 0, s>>>(nd);
-  if (f32copy) grid_kernel<D, true><<<sparse_ctas(nd), 256, 0, s>>>(nd, dt, tol);
-  else grid_kernel<D, false><<<sparse_ctas(nd), 256, 0, s>>>(nd, dt, tol);
+  // list compaction and grid update in one launch (grid_scan_kernel)
+  const int64_t quads = (nd.nblk + 3) / 4;
+  const unsigned ctas = unsigned(quads < 152 * 8 ? (quads > 0 ? quads : 1) : 152 * 8);
+  if (f32copy) grid_scan_kernel<D, true><<<ctas, 256, 0, s>>>(nd, dt, tol);
+  else grid_scan_kernel<D, false><<<ctas, 256, 0, s>>>(nd, dt, tol);
 }
 
 template <int D>
