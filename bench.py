@@ -63,11 +63,12 @@ BYTES_JCD = {"p2g": 112 + HAT + 7, "g2p": 544 + HAT + 6, "step": 616 + 2 * HAT}
 
 
 def launches_per_run(args, nbodies):
-    """Kernels of the timed steps: USL clear + P2G per body + compaction + grid
-    update + G2P per body; MUSL adds G2P-1 per body and, in 3D, the gradient
+    """Kernels of the timed steps: USL clear + P2G per body + grid update (which
+    lists the node blocks in the same launch) + G2P per body; MUSL: clear, P2G,
+    compaction, its grid update, G2P-1 per body and, in 3D, the gradient
     velocity pass (2D: the solve and the node pass in place of the grid update);
     a cell sort is a key pass per body, three scan passes and the scatter."""
-    per_step = 3 + 2 * nbodies if args.algorithm == "usl" else 4 + 3 * nbodies
+    per_step = 2 + 2 * nbodies if args.algorithm == "usl" else 4 + 3 * nbodies
     sorts = args.steps // args.sort_interval if args.sort_interval > 0 else 0
     return args.steps * per_step + sorts * (nbodies + 4)
 
