@@ -1,8 +1,9 @@
 """Edge cases of the step on the GPU against the oracle: an empty body among
 others, a single-particle body, the smallest grid (two nodes per axis), a
 particle that leaves the grid (frozen, MPM_ERR_OUT_OF_GRID), det F <= 0
-(MPM_ERR_NEGATIVE_J, the state still advanced) and a non-finite stress
-(MPM_ERR_NONFINITE)."""
+(MPM_ERR_NEGATIVE_J, the state still advanced), a non-finite stress
+(MPM_ERR_NONFINITE) and particles exactly on grid nodes (zero gradient
+factors)."""
 import numpy as np
 import pytest
 
@@ -116,3 +117,32 @@ def test_nonfinite_stress_reported():
     with pytest.raises(_capi.MPMError) as e:
         c.step(1)
     assert e.value.code in (_capi.MPM_ERR_NONFINITE, _capi.MPM_ERR_OUT_OF_GRID)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_particles_on_grid_nodes(dim, oracle_lib):
+    """A lattice of particles on grid nodes, cell faces and cell midpoints (node
+    spacing 0.25, particle spacing 0.125, exact in binary): x - x_lower == 0
+    makes a gradient factor exactly zero, a case the step's hat (stored by P2G,
+    reused by G2P with FP64 particles) must carry through; an expansion moves
+    them off the nodes over the run."""
+    from jump_gb300.grid import Grid3D
+    from jump_gb300.solid import Solid3D
+    ax = np.arange(0.25, 0.76, 0.125)
+    if dim == 2:
+        grid = Grid2D(0.0, 1.0, 0.0, 1.0, 5, 5)
+        xs = np.array([[a, b] for a in ax for b in ax])
+    else:
+        grid = Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, 5, 5, 5)
+        xs = np.array([[a, b, c] for a in ax for b in ax for c in ax])
+    vol = 0.125 ** dim
+    s = (Solid2D if dim == 2 else Solid3D)(xs, ElasticMaterial(1e3, 0.3, 1000.0, len(xs)))
+    s.mass[:] = 1000.0 * vol
+    s.volume[:] = vol
+    s.volumeInitial[:] = vol
+    s.velocity[:] = 0.01 * (xs - 0.5)
+    g, o, rg, ro = run_pair(grid, [s], 0.0, 1e-3, oracle_lib, 10)
+    assert rg == ro == _capi.MPM_OK
+    sg, so = g.download_all(), o.download_all()
+    assert np.abs(so[0].strain).max() > 1e-5
+    close(sg, so)
