@@ -215,14 +215,15 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, 
   const double m = gr.m[i];
   double mb = 0.0;
   const unsigned fx = fixed[i];
+  const double im = m > tol ? 1.0 / m : 0.0;  // one FP64 division per node
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     double p0b = 0.0, fb = 0.0;
     const double vdtb = na.vdtb[a * Nn + i], dvb = na.dvb[a * Nn + i];
     if (m > tol && !(fx & (1u << a))) {
-      p0b = dt * vdtb / m;
-      fb = (dt * dt * vdtb + dt * dvb) / m;
-      mb -= (vdtb * gr.vdt[a * Nn + i] + dvb * gr.dv[a * Nn + i]) / m;
+      p0b = (dt * vdtb) * im;
+      fb = (dt * dt * vdtb + dt * dvb) * im;
+      mb -= (vdtb * gr.vdt[a * Nn + i] + dvb * gr.dv[a * Nn + i]) * im;
     }
     na.p0b[a * Nn + i] = p0b;
     na.fb[a * Nn + i] = fb;
