@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 7
+#define JUMP_MPM_ABI_VERSION 8
 
 /* status codes */
 #define MPM_OK               0
@@ -47,7 +47,7 @@ extern "C" {
 #define MPM_ERR_NEGATIVE_J   3  /* det F <= 0 at some particle (state still advanced) */
 #define MPM_ERR_NONFINITE    4  /* NaN/Inf in a particle's velocity, position or stress */
 #define MPM_ERR_OUT_OF_GRID  5  /* a particle's cell lies outside the grid; it was frozen */
-#define MPM_ERR_TIMEOUT      6  /* a bounded device-side wait gave up */
+/* 6 is not used: no kernel of this library waits on another, so no wait can time out */
 #define MPM_ERR_UNSUPPORTED  7  /* feature not available in this build */
 #define MPM_ERR_SOLVER       8  /* the 2D MUSL mass solve did not converge in its iteration cap */
 
@@ -58,6 +58,19 @@ extern "C" {
 #define MPM_MAT_JOHNSON_COOK 3  /* JohnsonCookMaterial, Material.jl:279-330, 386-443 (3D) */
 #define MPM_MAT_VOCE        4   /* VoceMaterial, Material.jl:336-383, 445-493 (3D) */
 #define MPM_MAT_JOHNSON_COOK_DAMAGE 5  /* JohnsonCookMaterialWithDamage, Material.jl:495-646 (3D) */
+/* Rigid body (RigidMaterial, Material.jl:29-31, with the fields the USL solver
+   reads from it, SolveExplicitSolidMechanics2D.jl:448-479, 539-551: vx, vy and
+   fixed; vz in 3D).  Its particles add nothing in P2G.  After the grid update
+   and its Dirichlet conditions, every node of a rigid particle's linear-basis
+   cell gets nodal momentum and old momentum m_I v_rigid in each component
+   where v_rigid is non-zero (m_I: the deformable bodies' nodal mass), or zero
+   in every component when `fixed`; rigid bodies later in the body list
+   override earlier ones at shared nodes.  After G2P the rigid particles move
+   by dt v_rigid; their other fields are never updated.  USL with one velocity
+   field only (MUSL, contact, batches and the reverse mode reject it); at most
+   MPM_MAX_RIGID_BODIES per context. */
+#define MPM_MAT_RIGID       6
+#define MPM_MAX_RIGID_BODIES 32
 
 /* particle precision (grid accumulation is always FP64) */
 #define MPM_PREC_F64        0   /* every particle field and every operation in FP64 */
@@ -101,6 +114,12 @@ typedef struct mpm_material_desc {
      (d1 + d2 exp(d3 triaxiality))(1 + d4 ln(epdot/depsdot0))(1 + d5 (T - Tr)/(Tm - Tr)) */
   double  m, chi, Cp;
   double  d1, d2, d3, d4, d5, depsdot0, Tr, Tm;
+  /* MPM_MAT_RIGID only: the body's prescribed velocity (vx, vy, vz; vz unused
+     in 2D) and `fixed` (non-zero: every nodal momentum component under the
+     body is zeroed instead) */
+  double  v_rigid[3];
+  int32_t fixed;
+  int32_t reserved2;
 } mpm_material_desc;
 
 /* Particle arrays of one Solid2D/Solid3D (Solid.jl:67-125, 267-297), read at create time. */
@@ -372,11 +391,14 @@ int mpm_batch_destroy(mpm_batch* batch);
      out       device, 2+dim doubles: KE, SE, momentum
      stream    a cudaStream_t of this process, or NULL for the default stream
    The work is enqueued on `stream` and the call returns without waiting.
-   The first call on each device looks up the scratch array's device address
-   (cudaGetSymbolAddress) with that device current, so make that first call
-   before any stream capture.  Calls share the one scratch array: calls that
-   overlap on the GPU (other streams, other threads) race and must be
-   serialised by the caller. */
+   The scratch array's device address belongs to a CUDA context: the first
+   call in each context (the device's primary context, a context the caller
+   made current, or the primary context re-created after cudaDeviceReset)
+   looks it up (cudaGetSymbolAddress) with that context current and caches it
+   under the context's unique id, so make the first call in a context before
+   any stream capture in it.  Calls share the one scratch array of their
+   context: calls that overlap on the GPU (other streams, other threads) race
+   and must be serialised by the caller. */
 #define MPM_STATIC_MAX_PARTICLES 4194304
 int mpm_energies_static(int32_t dim, int64_t count, const double* mass, const double* velocity,
                         const double* volume, const double* stress, const double* strain, double* out,

@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-ABI_VERSION = 7  # JUMP_MPM_ABI_VERSION of the structures below
+ABI_VERSION = 8  # JUMP_MPM_ABI_VERSION of the structures below
 
 MPM_OK = 0
 MPM_ERR_ARG = 1
@@ -22,7 +22,6 @@ MPM_ERR_CUDA = 2
 MPM_ERR_NEGATIVE_J = 3
 MPM_ERR_NONFINITE = 4
 MPM_ERR_OUT_OF_GRID = 5
-MPM_ERR_TIMEOUT = 6
 MPM_ERR_UNSUPPORTED = 7
 MPM_ERR_SOLVER = 8
 
@@ -32,7 +31,6 @@ ERR_NAMES = {
     MPM_ERR_NEGATIVE_J: "MPM_ERR_NEGATIVE_J",
     MPM_ERR_NONFINITE: "MPM_ERR_NONFINITE",
     MPM_ERR_OUT_OF_GRID: "MPM_ERR_OUT_OF_GRID",
-    MPM_ERR_TIMEOUT: "MPM_ERR_TIMEOUT",
     MPM_ERR_UNSUPPORTED: "MPM_ERR_UNSUPPORTED",
     MPM_ERR_SOLVER: "MPM_ERR_SOLVER",
 }
@@ -43,6 +41,8 @@ MPM_MAT_J2 = 2
 MPM_MAT_JOHNSON_COOK = 3
 MPM_MAT_VOCE = 4
 MPM_MAT_JOHNSON_COOK_DAMAGE = 5
+MPM_MAT_RIGID = 6
+MPM_MAX_RIGID_BODIES = 32
 
 MPM_PREC_F64 = 0
 MPM_PREC_F32 = 1
@@ -105,6 +105,9 @@ class MaterialDesc(C.Structure):
         ("depsdot0", C.c_double),
         ("Tr", C.c_double),
         ("Tm", C.c_double),
+        ("v_rigid", C.c_double * 3),
+        ("fixed", C.c_int32),
+        ("reserved2", C.c_int32),
     ]
 
 

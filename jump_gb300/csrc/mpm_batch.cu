@@ -835,6 +835,8 @@ int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t prec
       if (bd.count < 0) return fail(MPM_ERR_ARG, "mpm_batch_create: negative particle count");
       if (bd.count > 0 && (!bd.pos || !bd.velocity || !bd.mass || !bd.volume || !bd.volume_initial))
         return fail(MPM_ERR_ARG, "mpm_batch_create: pos, velocity, mass, volume and volume_initial are required");
+      if (bd.mat.type == MPM_MAT_RIGID)
+        return fail(MPM_ERR_UNSUPPORTED, "mpm_batch_create: rigid solids run in single contexts only");
       if (!material_ok(bd.mat.type, D))
         return fail(MPM_ERR_ARG, "mpm_batch_create: unknown material type");
       if (!material_params_ok(bd.mat))

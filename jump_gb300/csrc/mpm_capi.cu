@@ -102,6 +102,13 @@ struct mpm_ctx {
   CgP cg{};
   float* nodebuf_f = nullptr;
   std::vector<uint8_t> fixed_h;
+  // rigid bodies (MPM_MAT_RIGID): rigid ordinal of each body (-1: deformable),
+  // the per-node marks and the {fixed, vx, vy, vz} table (device and host)
+  std::vector<int> rigid_bit;
+  uint32_t* rmask = nullptr;
+  double* rtab = nullptr;
+  std::vector<double> rtab_h;
+  bool rigid(int b) const { return rigid_bit[b] >= 0; }
   unsigned* status = nullptr;
   double* partial = nullptr;
   double* red = nullptr;
@@ -179,6 +186,8 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->muslbuf);
   cudaFree(c->nodebuf_f);
   cudaFree(c->blockbuf);
+  cudaFree(c->rmask);
+  cudaFree(c->rtab);
   for (int i = 0; i < 2; ++i) {
     if (c->seg_exec[i]) cudaGraphExecDestroy(c->seg_exec[i]);
     if (c->seg_graph[i]) cudaGraphDestroy(c->seg_graph[i]);
@@ -370,6 +379,7 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
   if (ev) cudaEventRecord(ev[0], c->stream);
   const int basis = c->prm.basis;
   for (int b = 0; b < c->nb; ++b) {
+    if (c->rigid(b)) continue;  // rigid solids add nothing (:394)
     if (basis != MPM_BASIS_LINEAR) {
       if (D == 2) Launchers<2>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
       else Launchers<3>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
@@ -380,6 +390,13 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
       Launchers<3>::p2g(c->stream, c->g, field_of(b), c->step_part(b), c->f32, c->prm.body_force, c->status,
                         c->p2g_strategy, c->threads);
     }
+  }
+  // rigid solids: mark the nodes the grid update overrides, then move them
+  for (int b = 0; b < c->nb; ++b) {
+    if (!c->rigid(b)) continue;
+    const double* v = c->rtab_h.data() + 4 * c->rigid_bit[b] + 1;
+    if (D == 2) Launchers<2>::rigid(c->stream, c->g, c->nd, c->part(b), c->f32, c->rigid_bit[b], v, c->prm.dt, c->status);
+    else Launchers<3>::rigid(c->stream, c->g, c->nd, c->part(b), c->f32, c->rigid_bit[b], v, c->prm.dt, c->status);
   }
   if (ev) cudaEventRecord(ev[1], c->stream);
   if (contact) {
@@ -396,6 +413,7 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
   }
   if (ev) cudaEventRecord(ev[2], c->stream);
   for (int b = 0; b < c->nb; ++b) {
+    if (c->rigid(b)) continue;  // rigid solids take no G2P (:488)
     if (basis != MPM_BASIS_LINEAR) {
       if (D == 2) Launchers<2>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
       else Launchers<3>::bs_g2p(c->stream, c->g, field_of(b), c->part(b), c->f32, c->mats[b], c->status, basis);
@@ -510,6 +528,28 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     c->nd.bflag = c->blockbuf;
     c->nd.blist = c->blockbuf + c->nd.nblk;
     c->nd.bcount = c->blockbuf + 2 * c->nd.nblk;
+  }
+  {
+    // rigid bodies: their ordinal among the rigid bodies, node marks and velocity table
+    int nr = 0;
+    for (int b = 0; b < nbodies; ++b) {
+      const bool r = bd[b].mat.type == MPM_MAT_RIGID;
+      c->rigid_bit.push_back(r ? nr : -1);
+      if (r) {
+        const mpm_material_desc& m = bd[b].mat;
+        c->rtab_h.insert(c->rtab_h.end(), {m.fixed != 0 ? 1.0 : 0.0, m.v_rigid[0], m.v_rigid[1],
+                                           D == 3 ? m.v_rigid[2] : 0.0});
+        ++nr;
+      }
+    }
+    if (nr > 0) {
+      CUDA_TRY(cudaMalloc(&c->rmask, size_t(Nn) * sizeof(uint32_t)));
+      CUDA_TRY(cudaMemset(c->rmask, 0, size_t(Nn) * sizeof(uint32_t)));
+      CUDA_TRY(cudaMalloc(&c->rtab, c->rtab_h.size() * sizeof(double)));
+      CUDA_TRY(cudaMemcpy(c->rtab, c->rtab_h.data(), c->rtab_h.size() * sizeof(double), cudaMemcpyHostToDevice));
+      c->nd.rmask = c->rmask;
+      c->nd.rtab = c->rtab;
+    }
   }
   if (prm->contact) {
     // per body: m | p0 (D) | f (D) | normal (D) | vdt (D) | dv (D), sharing mask and block list
@@ -721,11 +761,21 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
                                  " bodies");
   if (params->contact && !(params->friction >= 0.0)) return fail(MPM_ERR_ARG, "mpm_create: friction < 0");
   const int D = grid->dim;
+  int nrigid = 0;
   for (int b = 0; b < nbodies; ++b) {
     const mpm_body_desc& d = bodies[b];
     if (d.count < 0) return fail(MPM_ERR_ARG, "mpm_create: negative particle count");
     if (d.count > 0 && (!d.pos || !d.velocity || !d.mass || !d.volume || !d.volume_initial))
       return fail(MPM_ERR_ARG, "mpm_create: pos, velocity, mass, volume and volume_initial are required");
+    if (d.mat.type == MPM_MAT_RIGID) {
+      if (params->algorithm != MPM_ALG_USL || params->contact)
+        return fail(MPM_ERR_UNSUPPORTED, "mpm_create: rigid solids need USL with one velocity field");
+      if (++nrigid > MPM_MAX_RIGID_BODIES)
+        return fail(MPM_ERR_ARG, "mpm_create: more than MPM_MAX_RIGID_BODIES rigid solids");
+      for (int a = 0; a < D; ++a)
+        if (!std::isfinite(d.mat.v_rigid[a])) return fail(MPM_ERR_ARG, "mpm_create: non-finite rigid velocity");
+      continue;
+    }
     if (!material_ok(d.mat.type, D))
       return fail(MPM_ERR_ARG, "mpm_create: unknown material type (Johnson-Cook, Voce and Johnson-Cook with "
                                "damage are 3D)");
@@ -1005,22 +1055,45 @@ int mpm_download_grid(mpm_ctx* c, double* mass, double* momentum0, double* momen
     return MPM_OK;
   }
   CUDA_TRY(cudaMemcpy(h.data(), c->nodebuf, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> rm;
+  if (c->rmask) {
+    rm.resize(size_t(Nn));
+    CUDA_TRY(cudaMemcpy(rm.data(), c->rmask, size_t(Nn) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  }
   const double* m = h.data();
   const double* p0 = m + Nn;
   const double* f = p0 + Nn * D;
   const double dt = c->prm.dt;
   for (int64_t i = 0; i < Nn; ++i) {
     if (mass) mass[i] = m[i];
+    double q0[3], q[3];
     for (int a = 0; a < D; ++a) {
-      double q0 = p0[a * Nn + i], fa = f[a * Nn + i];
-      double q = q0 + fa * dt;  // grid update (:430), then the Dirichlet mask (:433-441)
+      q0[a] = p0[a * Nn + i];
+      q[a] = q0[a] + f[a * Nn + i] * dt;  // grid update (:430), then the Dirichlet mask (:433-441)
       if (c->fixed_h[i] & (1u << a)) {
-        q0 = 0.0;
-        q = 0.0;
+        q0[a] = 0.0;
+        q[a] = 0.0;
       }
-      if (momentum0) momentum0[D * i + a] = q0;
-      if (momentum) momentum[D * i + a] = q;
-      if (force) force[D * i + a] = fa;
+    }
+    // the rigid-body override of the last step (:448-479), in body order
+    for (uint32_t bits = rm.empty() ? 0u : rm[size_t(i)]; bits; bits &= bits - 1u) {
+      int k = 0;
+      while (!((bits >> k) & 1u)) ++k;
+      const double* rt = c->rtab_h.data() + 4 * k;
+      for (int a = 0; a < D; ++a) {
+        if (rt[0] != 0.0) {
+          q0[a] = 0.0;
+          q[a] = 0.0;
+        } else if (rt[1 + a] != 0.0) {
+          q0[a] = m[i] * rt[1 + a];
+          q[a] = q0[a];
+        }
+      }
+    }
+    for (int a = 0; a < D; ++a) {
+      if (momentum0) momentum0[D * i + a] = q0[a];
+      if (momentum) momentum[D * i + a] = q[a];
+      if (force) force[D * i + a] = f[a * Nn + i];
     }
   }
   return MPM_OK;

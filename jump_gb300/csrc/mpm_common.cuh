@@ -107,6 +107,12 @@ struct NodeP {
   double* vg;
   double* mc;
   int nmc;               // entries of the mass stencil per node ((2K - 1)^2 for K support nodes per axis)
+  // rigid bodies (MPM_MAT_RIGID): per node, bit k set when a particle of rigid
+  // body k (in body order) has the node in its linear cell this step; zeroed
+  // with the accumulators of the listed blocks.  rtab: per rigid body
+  // {fixed, vx, vy, vz}.  Both null without rigid bodies.
+  uint32_t* rmask;
+  const double* rtab;
 };
 
 // 2D MUSL mass solve: CG vectors of the four right-hand sides (p0_x, p0_y,

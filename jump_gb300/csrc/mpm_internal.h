@@ -70,7 +70,8 @@ inline int spread_threads(int64_t n) {
   return th;
 }
 
-// material model types a context or batch accepts in dimension dim
+// deformable material model types a context or batch accepts in dimension dim
+// (rigid bodies, MPM_MAT_RIGID, are checked separately: contexts only)
 inline bool material_ok(int type, int dim) {
   if (type == MPM_MAT_ELASTIC || type == MPM_MAT_NEOHOOKEAN || type == MPM_MAT_J2) return true;
   return dim == 3 && (type == MPM_MAT_JOHNSON_COOK || type == MPM_MAT_VOCE || type == MPM_MAT_JOHNSON_COOK_DAMAGE);
@@ -98,6 +99,9 @@ struct Launchers {
   // (FP64: atomic, FP32: warp); threads per CTA (<= 256), 0 for 256
   static void p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
                   const double* grav, unsigned* status, int strategy = -1, int threads = 0);
+  // rigid body `bit`: mark its particles' linear-cell nodes and move them by dt v (v: 3 doubles)
+  static void rigid(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32, int bit,
+                    const double* v, double dt, unsigned* status);
   // compaction of the flagged node blocks + grid update over them
   static void grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy);
   // zero the accumulators of the blocks listed by the previous grid stage

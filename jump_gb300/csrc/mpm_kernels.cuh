@@ -427,6 +427,32 @@ __device__ __forceinline__ T nload(const T* p) {
   else return __ldg(p);
 }
 
+// Rigid bodies after the grid update and its Dirichlet mask
+// (SolveExplicitSolidMechanics2D.jl:448-479): for every rigid body marked at
+// node i, in body order, both momenta become m v_rigid in the components where
+// v_rigid is non-zero, or zero in every component for a fixed body.
+template <int D>
+__device__ __forceinline__ void rigid_override(const NodeP& nd, int64_t i, double m, double* p0, double* p) {
+  unsigned bits = nd.rmask[i];
+  while (bits) {
+    const int k = __ffs(bits) - 1;
+    bits &= bits - 1u;
+    const double* rt = nd.rtab + 4 * k;
+    const bool fixed = rt[0] != 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      if (fixed) {
+        p0[a] = 0.0;
+        p[a] = 0.0;
+      } else if (rt[1 + a] != 0.0) {
+        const double q = m * rt[1 + a];
+        p0[a] = q;
+        p[a] = q;
+      }
+    }
+  }
+}
+
 template <int D, bool F32COPY, bool CG = false>
 __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt, double tol) {
   const int64_t Nn = nd.nodeCount;
@@ -445,20 +471,23 @@ __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt,
     return;
   }
   const unsigned fx = nd.fixed[i];
-  double vdt[D], dv[D];
-  const bool live = true;
+  double vdt[D], dv[D], p0[D], p[D];
   double invM = 1.0 / m;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    double p0 = CG ? __ldcg(nd.p0 + a * Nn + i) : nd.p0[a * Nn + i];
+    p0[a] = CG ? __ldcg(nd.p0 + a * Nn + i) : nd.p0[a * Nn + i];
     double fa = CG ? __ldcg(nd.f + a * Nn + i) : nd.f[a * Nn + i];
-    double p = __dadd_rn(p0, __dmul_rn(fa, dt));  // p = p0 + f*dt
+    p[a] = __dadd_rn(p0[a], __dmul_rn(fa, dt));  // p = p0 + f*dt
     if (fx & (1u << a)) {
-      p0 = 0.0;
-      p = 0.0;
+      p0[a] = 0.0;
+      p[a] = 0.0;
     }
-    vdt[a] = live ? (p * invM) * dt : 0.0;
-    dv[a] = live ? (p - p0) * invM : 0.0;
+  }
+  if (nd.rmask) rigid_override<D>(nd, i, m, p0, p);
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    vdt[a] = (p[a] * invM) * dt;
+    dv[a] = (p[a] - p0[a]) * invM;
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) {
@@ -973,6 +1002,39 @@ __global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, M
                                                   unsigned* status) {
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t < pp.count) g2p_particle<D, R, MAT>(g, nd, pp, t, mp, dt, status);
+}
+
+// ---------------------------------------------------------------------------
+// Rigid body `bit` (in body order among the rigid bodies) of one step: every
+// particle marks the nodes of its linear cell (getAdjacentGridPoints with the
+// linear basis, SolveExplicitSolidMechanics2D.jl:456) and their blocks for the
+// grid update's override, then moves by dt v_rigid (:539-551).  The reference
+// moves rigid particles after G2P; nothing between this launch (after P2G)
+// and the end of the step reads their positions, so marking with the old
+// position and moving here is the same.  A particle outside the grid is
+// reported and frozen.
+template <int D, class R>
+__global__ void __launch_bounds__(256) rigid_kernel(GridP g, NodeP nd, PartP pp, int bit, double vx, double vy,
+                                                    double vz, double dt, unsigned* status) {
+  using L = Layout<D>;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= pp.count) return;
+  const int64_t p = pp.begin + t;
+  R x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
+  Hat<D, R> h;
+  if (!hat<D, R>(g, x, h)) {
+    atomicOr(status, ST_OUT_OF_GRID);
+    return;
+  }
+  const int64_t base = int64_t(h.c[0]) + g.nx * int64_t(h.c[1]) + (D == 3 ? g.nxy * int64_t(h.c[D - 1]) : 0);
+#pragma unroll
+  for (int k = 0; k < (1 << D); ++k) atomicOr(nd.rmask + corner_node<D>(g, base, k), 1u << bit);
+  mark_blocks<D>(nd, h.c);
+  const double v[3] = {vx, vy, vz};
+#pragma unroll
+  for (int a = 0; a < D; ++a) *field<R>(pp, L::X + a, p) = R(to_f64(x[a]) + dt * v[a]);
 }
 
 // ---------------------------------------------------------------------------

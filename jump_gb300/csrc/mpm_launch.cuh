@@ -113,6 +113,14 @@ void Launchers<D>::p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, cons
 }
 
 template <int D>
+void Launchers<D>::rigid(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32, int bit,
+                         const double* v, double dt, unsigned* status) {
+  if (pp.count <= 0) return;
+  if (f32) rigid_kernel<D, float><<<blocks_for(pp.count, 256), 256, 0, s>>>(g, nd, pp, bit, v[0], v[1], v[2], dt, status);
+  else rigid_kernel<D, double><<<blocks_for(pp.count, 256), 256, 0, s>>>(g, nd, pp, bit, v[0], v[1], v[2], dt, status);
+}
+
+template <int D>
 void Launchers<D>::clear(cudaStream_t s, const NodeP& nd) {
   clear_blocks_kernel<D><<<sparse_ctas(nd), 256, 0, s>>>(nd);
 }

@@ -69,8 +69,8 @@ __device__ __forceinline__ int64_t block_node(const NodeP& nd, uint32_t blk, int
   return ix + nd.nn[0] * (iy + nd.nn[1] * iz);
 }
 
-// zero the accumulators (m, p0, f and, where present, normals, MUSL p2 and
-// mass stencil) of the listed blocks before the next P2G
+// zero the accumulators (m, p0, f and, where present, normals, MUSL p2, mass
+// stencil and rigid-body node marks) of the listed blocks before the next P2G
 template <int D>
 __global__ void __launch_bounds__(256) clear_blocks_kernel(NodeP nd) {
   const int64_t Nn = nd.nodeCount;
@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(256) clear_blocks_kernel(NodeP nd) {
     }
     if (nd.mc)
       for (int o = 0; o < nd.nmc; ++o) nd.mc[o * Nn + i] = 0.0;
+    if (nd.rmask) nd.rmask[i] = 0u;
   }
 }
 

@@ -16,6 +16,7 @@
 #include <mutex>
 #include <string>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "../../include/jump_mpm.h"
@@ -36,25 +37,75 @@ __device__ __align__(256) double g_static_partials[kMaxBlocks * kMaxQ];
 
 int fail(int code, const std::string& msg) { return jmpm::set_last_error(code, msg); }
 
-// Device address of g_static_partials, resolved once per device.
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_ptr[kMaxDevices] = {nullptr};
+// Device address of g_static_partials in the calling thread's current CUDA
+// context.  A module's device symbols live in one context: a non-primary
+// context made current by the caller, or the primary context re-created after
+// cudaDeviceReset, loads the module again at another address.  So the cache is
+// keyed by the context's unique id (cuCtxGetId, never reused within a process),
+// not by the device ordinal.  The two driver calls are fetched through the
+// runtime (cudaGetDriverEntryPointByVersion), so the library still links
+// against nothing but the driver the runtime loads.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-int scratch_for_current_device(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(MPM_ERR_ARG, "device ordinal beyond the supported range");
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_static_partials);
-    if (e != cudaSuccess)
-      return fail(MPM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_ptr[dev] = static_cast<double*>(p);
+constexpr int kCacheEntries = 64;
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  double* ptr;
+};
+std::mutex g_mu;
+ScratchEntry g_cache[kCacheEntries] = {};
+int g_cache_next = 0;  // round-robin replacement once all entries are used
+CtxGetCurrentFn g_get_current = nullptr;
+CtxGetIdFn g_get_id = nullptr;
+
+// the id of the current context, or 0 when none is current (lock held)
+int current_context_id(unsigned long long* id) {
+  if (!g_get_current || !g_get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return fail(MPM_ERR_CUDA, "mpm_energies_static: cuCtxGetCurrent/cuCtxGetId not available from the driver");
+    g_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_get_id = reinterpret_cast<CtxGetIdFn>(f2);
   }
-  *out = g_ptr[dev];
+  CUcontext ctx = nullptr;
+  if (g_get_current(&ctx) != CUDA_SUCCESS)
+    return fail(MPM_ERR_CUDA, "mpm_energies_static: cuCtxGetCurrent failed");
+  *id = 0;
+  if (ctx && g_get_id(ctx, id) != CUDA_SUCCESS) return fail(MPM_ERR_CUDA, "mpm_energies_static: cuCtxGetId failed");
+  return MPM_OK;
+}
+
+int scratch_for_current_context(double** out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  unsigned long long id = 0;
+  int rc = current_context_id(&id);
+  if (rc != MPM_OK) return rc;
+  if (id != 0)
+    for (const ScratchEntry& e : g_cache)
+      if (e.ctx_id == id) {
+        *out = e.ptr;
+        return MPM_OK;
+      }
+  // first call in this context: look the address up with it current (this also
+  // makes the device's primary context current when no context was)
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_partials);
+  if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  if (id == 0) {
+    rc = current_context_id(&id);
+    if (rc != MPM_OK) return rc;
+  }
+  if (id != 0) {
+    g_cache[g_cache_next] = ScratchEntry{id, static_cast<double*>(p)};
+    g_cache_next = (g_cache_next + 1) % kCacheEntries;
+  }
+  *out = static_cast<double*>(p);
   return MPM_OK;
 }
 
@@ -141,7 +192,7 @@ int mpm_energies_static(int32_t dim, int64_t count, const double* mass, const do
   if (!out || (count > 0 && (!mass || !velocity || !volume || !stress || !strain)))
     return fail(MPM_ERR_ARG, "mpm_energies_static: null array");
   double* scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
+  int rc = scratch_for_current_context(&scratch);
   if (rc != MPM_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int nblocks = int((count + kPerBlock - 1) / kPerBlock);

@@ -49,13 +49,13 @@ class Descriptors:
         self.grid = g
         bodies = (_capi.BodyDesc * max(1, len(solids)))()
         for s, sol in enumerate(solids):
-            if isinstance(sol.mat, RigidMaterial) or getattr(sol, "rigid", False):
-                raise _capi.MPMError(_capi.MPM_ERR_UNSUPPORTED,
-                                     "rigid solids are not supported by the accelerated USL path")
             b = bodies[s]
             b.count = sol.parCount
             m = sol.mat
             b.mat.type = m.kind
+            if isinstance(m, RigidMaterial):
+                b.mat.v_rigid[0], b.mat.v_rigid[1], b.mat.v_rigid[2] = m.vx, m.vy, m.vz
+                b.mat.fixed = 1 if m.fixed else 0
             b.mat.E, b.mat.nu, b.mat.density = m.E, m.nu, m.density
             b.mat.fy, b.mat.k1 = getattr(m, "fy", 0.0), getattr(m, "k1", 0.0)
             for k in ("A", "B", "C", "n", "epsdot0", "cellsize"):

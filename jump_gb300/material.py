@@ -32,10 +32,29 @@ def _lame(E, nu):
 
 
 class RigidMaterial(MaterialType):
-    """RigidMaterial(density), Material.jl:29-31 (not supported by the solver)."""
+    """A rigid solid: RigidMaterial(vx, vy, density) as the reference drivers build it
+    (Main_LateralCompressionTube.jl:116-117), with the fields the USL solver reads
+    (SolveExplicitSolidMechanics2D.jl:453-461: vx, vy, fixed); vz for 3D.  The
+    reference type itself holds only the density (Material.jl:29-31).
 
-    def __init__(self, density):
-        self.density = float(density)
+    RigidMaterial(vx, vy, density) or RigidMaterial(vx, vy, vz, density), and
+    ``fixed=True`` for a body that zeroes every nodal momentum component under it.
+    """
+    kind = _capi.MPM_MAT_RIGID
+
+    def __init__(self, *args, fixed: bool = False):
+        if len(args) == 1:  # RigidMaterial(density), the reference type
+            self.vx = self.vy = self.vz = 0.0
+            self.density = float(args[0])
+        elif len(args) == 3:
+            self.vx, self.vy, self.density = (float(a) for a in args)
+            self.vz = 0.0
+        elif len(args) == 4:
+            self.vx, self.vy, self.vz, self.density = (float(a) for a in args)
+        else:
+            raise TypeError("RigidMaterial(vx, vy[, vz], density) or RigidMaterial(density)")
+        self.fixed = bool(fixed)
+        self.E = self.nu = 0.0
 
 
 class ElasticMaterial(MaterialType):

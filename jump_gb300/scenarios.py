@@ -235,3 +235,51 @@ def block_3d(h: float = 0.125, ppc: int = 2, size=(1.0, 0.25, 0.25), E_range=(0.
     data = {"total_time": 200 * dt, "dt": dt, "time": 0.0, "bodyforce": ConstantBodyForce3D([0.0, g, 0.0]),
             "dirichlet_grid": [("left", (1, 1, 1))]}
     return grid, [s], USL(1e-9), data
+
+
+def rigid_punch(dim: int = 2, h: float = 0.025, ppc: int = 2, radius: float = 0.2, speed: float = 0.1,
+                E: float = 1000.0, nu: float = 0.3, rho: float = 1000.0, dt: float = 1e-3,
+                material: str = "elastic"):
+    """A rigid plate striking a deformable disk (sphere in 3D) that rests on a fixed
+    rigid base, in the manner of the reference's lateral-compression drivers
+    (Main_LateralCompressionTube.jl:116-117: a moving RigidMaterial punch and a
+    still one).  The base fills y in [h, 3h] and is ``fixed`` (zero nodal momentum
+    under it); the disk sits half a cell above it; the punch, 4h thick, starts
+    1.5 cells above the disk and moves along -y at ``speed``.  Unit domain,
+    h-spaced grid, every face fixed in every direction."""
+    from .material import RigidMaterial
+    from .solid import buildParticleForBlock, buildParticleForSphere
+    n = int(round(1.0 / h)) + 1
+    off = h / ppc
+    cy = 3.5 * h + radius
+    py = cy + radius + 1.5 * h + 2 * h
+    if dim == 2:
+        grid = Grid2D(0.0, 1.0, 0.0, 1.0, n, n)
+        cd = buildParticleForCircle([0.5, cy], radius, off)
+        cp = buildParticleForRectangle([0.5, py], 0.5, 4 * h, off)
+        cb = buildParticleForRectangle([0.5, 2 * h], 0.6, 2 * h, off)
+        S, v = Solid2D, [0.0, -speed]
+        base = RigidMaterial(0.0, 0.0, 7800.0, fixed=True)
+        punch = RigidMaterial(0.0, -speed, 7800.0)
+        faces = [("bottom", (1, 1)), ("top", (1, 1)), ("left", (1, 1)), ("right", (1, 1))]
+    else:
+        grid = Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, n, n, n)
+        cd = buildParticleForSphere([0.5, cy, 0.5], radius, off)
+        cp = buildParticleForBlock([0.5, py, 0.5], 0.5, 4 * h, 0.5, off)
+        cb = buildParticleForBlock([0.5, 2 * h, 0.5], 0.6, 2 * h, 0.6, off)
+        S, v = Solid3D, [0.0, -speed, 0.0]
+        base = RigidMaterial(0.0, 0.0, 0.0, 7800.0, fixed=True)
+        punch = RigidMaterial(0.0, -speed, 0.0, 7800.0)
+        faces = [("bottom", (1, 1, 1)), ("top", (1, 1, 1)), ("left", (1, 1, 1)), ("right", (1, 1, 1)),
+                 ("front", (1, 1, 1)), ("back", (1, 1, 1))]
+    if material == "elastic":
+        mat = ElasticMaterial(E, nu, rho, len(cd))
+    else:
+        mat = NeoHookeanMaterial(E, nu, rho, len(cd))
+    disk, pl, bs = S(cd, mat), S(cp, punch), S(cb, base)
+    for s in (disk, pl, bs):
+        _scale(s, off, dim)
+    assign_velocity(pl, v)  # the punch's particles carry its velocity (energy records)
+    bf = ConstantBodyForce2D([0.0, 0.0]) if dim == 2 else ConstantBodyForce3D([0.0, 0.0, 0.0])
+    data = {"total_time": 200 * dt, "dt": dt, "time": 0.0, "bodyforce": bf, "dirichlet_grid": faces}
+    return grid, [disk, pl, bs], USL(1e-9), data

@@ -51,6 +51,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <type_traits>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -116,6 +117,9 @@ struct Body {
   std::vector<double> alpha, pstrain, vmstr, youngs, alphadot;
   std::vector<double> damage_init, dam, temp;  // JohnsonCookMaterialWithDamage state
   bool has_youngs = false;
+  // RigidMaterial as the USL solver reads it (SolveExplicitSolidMechanics2D.jl:453-461)
+  bool rigid = false, rigid_fixed = false;
+  double vr[3] = {0, 0, 0};
 };
 
 template <int D>
@@ -808,6 +812,56 @@ void g2p_body(Ctx<D>& c, int s, const double* mass, const double* mom0, const do
 #endif
 }
 
+// Rigid solids after the grid update (SolveExplicitSolidMechanics2D.jl:448-479):
+// for every rigid particle, in body and particle order, the nodes of its cell
+// found with the linear basis (getAdjacentGridPoints with linBasis, :456)
+// get momentum and momentum0 m_I v in each component with v != 0, or zero in
+// every component for a fixed body (the field RigidMaterial lacks, see the
+// header).  A particle outside the grid is reported and skipped.
+template <int D>
+void rigid_override(Ctx<D>& c) {
+  Grid<D>& g = c.g;
+  int64_t near[kMaxSupport];
+  double N[kMaxSupport], dN[kMaxSupport * D];
+  for (Body<D>& b : c.bodies) {
+    if (!b.rigid) continue;
+    for (int64_t ip = 0; ip < b.n; ++ip) {
+      if (shape<D>(g, &b.pos[D * ip], near, N, dN) == false) {
+        c.status = MPM_ERR_OUT_OF_GRID;
+        continue;
+      }
+      for (int i = 0; i < (1 << D); ++i) {
+        const int64_t id = near[i];
+        const double mi = g.mass[id];
+        for (int a = 0; a < D; ++a) {
+          if (b.rigid_fixed) {
+            g.momentum[D * id + a] = 0.;
+            g.momentum0[D * id + a] = 0.;
+          } else if (b.vr[a] != 0.) {
+            g.momentum[D * id + a] = mi * b.vr[a];
+            g.momentum0[D * id + a] = mi * b.vr[a];
+          }
+        }
+      }
+    }
+  }
+}
+
+// xx[ip] += dtime * v (:539-551); particles outside the grid stay where they are
+template <int D>
+void rigid_advance(Ctx<D>& c) {
+  int64_t near[kMaxSupport];
+  double N[kMaxSupport], dN[kMaxSupport * D];
+  for (Body<D>& b : c.bodies) {
+    if (!b.rigid) continue;
+    for (int64_t ip = 0; ip < b.n; ++ip) {
+      // the position the override saw, before this step's move
+      if (!shape<D>(c.g, &b.pos[D * ip], near, N, dN)) continue;
+      for (int a = 0; a < D; ++a) b.pos[D * ip + a] += c.p.dt * b.vr[a];
+    }
+  }
+}
+
 // One USL step with a single velocity field (the reference).
 template <int D>
 void step_single(Ctx<D>& c) {
@@ -815,9 +869,13 @@ void step_single(Ctx<D>& c) {
   zero<D>(g.mass);
   zero<D>(g.momentum0);
   zero<D>(g.force);
-  std::vector<int> all(c.bodies.size());
-  for (size_t s = 0; s < all.size(); ++s) all[s] = int(s);
-  p2g_bodies<D>(c, all, g.mass.data(), g.momentum0.data(), g.force.data(), nullptr);
+  std::vector<int> deformable;
+  bool any_rigid = false;
+  for (size_t s = 0; s < c.bodies.size(); ++s) {
+    if (c.bodies[s].rigid) any_rigid = true;  // rigid solids take no P2G (:394) and no G2P (:488)
+    else deformable.push_back(int(s));
+  }
+  p2g_bodies<D>(c, deformable, g.mass.data(), g.momentum0.data(), g.force.data(), nullptr);
   double dt = c.p.dt;
   for (int64_t i = 0; i < g.nodeCount; ++i) {
     for (int a = 0; a < D; ++a)
@@ -828,8 +886,9 @@ void step_single(Ctx<D>& c) {
         g.momentum[D * i + a] = 0.;
       }
   }
-  for (size_t s = 0; s < c.bodies.size(); ++s)
-    g2p_body<D>(c, int(s), g.mass.data(), g.momentum0.data(), g.momentum.data(), 0);
+  if (any_rigid) rigid_override<D>(c);
+  for (int s : deformable) g2p_body<D>(c, s, g.mass.data(), g.momentum0.data(), g.momentum.data(), 0);
+  if (any_rigid) rigid_advance<D>(c);
 }
 
 // ---------------------------------------------------------------------------
@@ -1199,6 +1258,11 @@ int create(const mpm_grid_desc* gd, const mpm_body_desc* bd, int nb, const mpm_p
     cp(b.vmstr, d.vmstr, 1, 0.0);
     b.has_youngs = d.youngs != nullptr;
     if (b.has_youngs) cp(b.youngs, d.youngs, 1, 0.0);
+    if (d.mat.type == MPM_MAT_RIGID) {
+      b.rigid = true;
+      b.rigid_fixed = d.mat.fixed != 0;
+      for (int a = 0; a < D; ++a) b.vr[a] = d.mat.v_rigid[a];
+    }
     c->bodies.push_back(std::move(b));
   }
   if (p->algorithm == MPM_ALG_MUSL) {
@@ -1324,6 +1388,9 @@ int oracle_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_
   for (int a = 0; params && a < grid->dim; ++a)
     if (grid->nodes[a] < (params->basis == MPM_BASIS_CUBIC_BSPLINE ? 4 : 3) && params->basis != MPM_BASIS_LINEAR)
       return fail(MPM_ERR_ARG, "oracle_create: B-spline bases need 3 (quadratic) or 4 (cubic) nodes per axis");
+  for (int s = 0; s < nbodies; ++s)
+    if (bodies[s].mat.type == MPM_MAT_RIGID && (params->algorithm != MPM_ALG_USL || params->contact))
+      return fail(MPM_ERR_UNSUPPORTED, "oracle_create: rigid solids need USL with one velocity field");
   Handle* h = new Handle{grid->dim, nullptr};
   if (grid->dim == 2) {
     Ctx<2>* c;
@@ -1356,6 +1423,40 @@ int oracle_max_threads(void) {
 #else
   return 1;
 #endif
+}
+
+// The shape functions of one point (getShapeAndGradient, Basis.jl:219-251,
+// 292-332 and the B-spline forms :374-820) on the grid a descriptor describes:
+// fills near[] (0-based node ids), N[] and dN[] (dim per node) and returns the
+// support size, 0 when the point's cell lies outside the grid.  For the
+// known-answer tests of the basis.
+int oracle_shape(const mpm_grid_desc* gd, int32_t basis, const double* x, int64_t* near, double* N, double* dN) {
+  if (!gd || !x || !near || !N || !dN || (gd->dim != 2 && gd->dim != 3)) return -1;
+  auto run = [&](auto dimtag) -> int {
+    constexpr int D = decltype(dimtag)::value;
+    Grid<D> g;
+    g.basis = basis;
+    for (int a = 0; a < D; ++a) {
+      g.xmin[a] = gd->xmin[a];
+      g.nn[a] = gd->nodes[a];
+      g.dx[a] = (gd->xmax[a] - gd->xmin[a]) / (double(gd->nodes[a]) - 1.0);
+      g.dxI[a] = 1.0 / g.dx[a];
+    }
+    g.nodeCountXY = g.nn[0] * g.nn[1];
+    g.nodeCount = g.nodeCountXY * (D == 3 ? g.nn[2] : 1);
+    g.pos.assign(size_t(D) * g.nodeCount, 0.0);
+    for (int64_t k = 0; k < (D == 3 ? g.nn[2] : 1); ++k)
+      for (int64_t j = 0; j < g.nn[1]; ++j)
+        for (int64_t i = 0; i < g.nn[0]; ++i) {
+          int64_t idx = g.nodeCountXY * k + g.nn[0] * j + i;
+          g.pos[D * idx + 0] = g.xmin[0] + double(i) * g.dx[0];
+          g.pos[D * idx + 1] = g.xmin[1] + double(j) * g.dx[1];
+          if (D == 3) g.pos[D * idx + 2] = g.xmin[2] + double(k) * g.dx[2];
+        }
+    return support<D>(g, x, near, N, dN);
+  };
+  if (gd->dim == 2) return run(std::integral_constant<int, 2>{});
+  return run(std::integral_constant<int, 3>{});
 }
 
 
