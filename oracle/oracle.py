@@ -57,6 +57,8 @@ def lib():
         L.oracle_set_threads.argtypes = [vp, C.c_int32]
         L.oracle_last_error.restype = C.c_char_p
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_shape.argtypes = [C.POINTER(_capi.GridDesc), C.c_int32, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -113,8 +115,23 @@ class OracleContext(_ContextBase):
             pass
 
 
+def shape(grid_desc, basis: int, x):
+    """(node ids, N, dN (support x dim)) of point x: the oracle's shape functions
+    (Basis.jl getShapeAndGradient) for known-answer tests; None outside the grid."""
+    d = int(grid_desc.dim)
+    xp = np.ascontiguousarray(x, dtype=np.float64)
+    near = np.zeros(64, dtype=np.int64)
+    N = np.zeros(64)
+    dN = np.zeros(64 * d)
+    n = lib().oracle_shape(C.byref(grid_desc), int(basis), _capi.dptr(xp), near.ctypes.data_as(C.POINTER(C.c_int64)),
+                           _capi.dptr(N), _capi.dptr(dN))
+    if n <= 0:
+        return None
+    return near[:n].copy(), N[:n].copy(), dN[: n * d].reshape(n, d).copy()
+
+
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
 
 
-__all__ = ["OracleContext", "BodyState", "build", "lib", "max_threads"]
+__all__ = ["OracleContext", "BodyState", "build", "lib", "max_threads", "shape"]

@@ -1,0 +1,174 @@
+"""Known answers that do not come from a restatement of the reference: closed
+forms of the constitutive updates, the hat basis's algebraic properties,
+conservation laws of the USL step and a manufactured-solution convergence rate.
+Shared by the oracle pins (CPU) and the GPU pins; every check runs the same
+driver surface (engine.MPMContext or oracle.OracleContext)."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from jump_gb300 import scenarios
+from jump_gb300.algorithm import ConstantBodyForce2D, ConstantBodyForce3D
+from jump_gb300.engine import Descriptors
+from jump_gb300.grid import Grid2D, Grid3D
+from jump_gb300.material import ElasticMaterial, ElastoPlasticMaterial, NeoHookeanMaterial
+from jump_gb300.solid import Solid2D, Solid3D, buildParticleForRectangle
+
+
+def lame(E, nu):
+    return E * nu / (1 + nu) / (1 - 2 * nu), E / 2 / (1 + nu)
+
+
+# ---------------------------------------------------------------------------
+# one material point: its constitutive update evaluated at a prescribed state.
+# A single particle at rest on a unit grid, stepped once with dt = 1e-14: the
+# nodal velocities its own stress produces are O(dt), so the strain and F it
+# takes into update_stress! differ from the prescribed ones by O(dt^2) ~ 1e-23
+# relative, far below the 1e-12 tolerance of the checks.
+
+DT_POINT = 1e-14
+
+
+def point_state(ctx_cls, dim, mat, F=None, strain=None, alpha=0.0, pstrain=None):
+    """(stress, alpha, pstrain, vmstr) after one step of a single particle of
+    material `mat` whose F and strain are prescribed (d x d)."""
+    grid = Grid2D(0.0, 1.0, 0.0, 1.0, 3, 3) if dim == 2 else Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, 3, 3, 3)
+    x = np.full((1, dim), 0.37)
+    s = (Solid2D if dim == 2 else Solid3D)(x, mat)
+    s.volume[:] = 1e-3
+    s.volumeInitial[:] = 1e-3
+    s.mass[:] = mat.density * 1e-3
+    if F is not None:
+        s.deformationGradient[0] = np.asarray(F, dtype=np.float64)
+    if strain is not None:
+        s.strain[0] = np.asarray(strain, dtype=np.float64)
+    if isinstance(mat, ElastoPlasticMaterial):
+        mat.alpha[0] = alpha
+        if pstrain is not None:
+            if dim == 2:
+                mat.pstrain[0] = pstrain
+            else:
+                mat.pstrain_3D[0] = pstrain
+    bf = ConstantBodyForce2D([0.0, 0.0]) if dim == 2 else ConstantBodyForce3D([0.0, 0.0, 0.0])
+    c = ctx_cls(Descriptors(grid, [s], tolerance=0.0, body_force=bf, dt=DT_POINT))
+    c.step(1)
+    st = c.download_body(0)
+    c.close()
+    _, _, sig = st.matrices()
+    ps = st.pstrain.copy() if dim == 2 else st.pstrain.reshape(3, 3).T.copy()
+    return sig[0].copy(), float(st.alpha[0]), ps, float(st.vmstr[0])
+
+
+def elastic_closed_form(E, nu, eps):
+    lam, mu = lame(E, nu)
+    eps = np.asarray(eps, dtype=np.float64)
+    return lam * np.trace(eps) * np.eye(eps.shape[0]) + 2 * mu * eps
+
+
+def neohookean_uniaxial(E, nu, stretch, dim):
+    """sigma of F = diag(stretch, 1(, 1)): sigma_11 = (mu (s^2 - 1) + lambda ln s)/s,
+    the lateral components lambda ln s / s"""
+    lam, mu = lame(E, nu)
+    s = stretch
+    out = np.zeros((dim, dim))
+    out[0, 0] = (mu * (s * s - 1) + lam * math.log(s)) / s
+    for a in range(1, dim):
+        out[a, a] = lam * math.log(s) / s
+    return out
+
+
+def j2_shear_closed_form(E, nu, fy, k1, eps12):
+    """Radial return with linear hardening under monotonic pure shear strain
+    eps12 (so the deviatoric strain norm is sqrt(2) eps12 in the reference's
+    norm |s| = sqrt(s11^2 + s22^2 + s33^2 + 2 (s12^2 + s23^2 + s13^2))): along a
+    proportional path every return lands on alpha = (2 mu sqrt(2) eps12 - fy)/
+    (2 mu + k1) whatever the increments, and sigma_12 = 2 mu (eps12 - alpha/sqrt(2));
+    below yield alpha = 0 and sigma_12 = 2 mu eps12.  Returns (alpha, sigma_12)."""
+    _, mu = lame(E, nu)
+    a = max(0.0, (2 * mu * math.sqrt(2.0) * eps12 - fy) / (2 * mu + k1))
+    return a, 2 * mu * (eps12 - a / math.sqrt(2.0))
+
+
+def j2_shear_history(ctx_cls, dim, E, nu, rho, fy, k1, eps12s):
+    """Drive one J2 material point through the monotonic shear history eps12s,
+    carrying alpha and the plastic strain from each point to the next."""
+    alpha, ps, out = 0.0, None, []
+    for e in eps12s:
+        mat = ElastoPlasticMaterial(E, nu, rho, fy, k1, 1)
+        strain = np.zeros((dim, dim))
+        strain[0, 1] = strain[1, 0] = e
+        sig, alpha, ps, _ = point_state(ctx_cls, dim, mat, strain=strain, alpha=alpha, pstrain=ps)
+        out.append((alpha, sig[0, 1], sig))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# the two-disk collision (Main_TwoDisks.jl) without boundary conditions: the
+# USL step conserves linear momentum exactly up to rounding (the grid forces
+# sum to zero because sum_I grad N_I = 0 for every particle off the node lines)
+
+def two_disks_free(ctx_cls, steps, record_every=100, threads=None):
+    grid, solids, alg, data = scenarios.two_disks(fixed_boundary=False)
+    kw = {} if threads is None else {"threads": threads}
+    c = ctx_cls(Descriptors(grid, solids, tolerance=0.0, body_force=data["bodyforce"], dt=data["dt"]), **kw)
+    recs = [c.energies()]
+    mass = sum(float(np.sum(s.mass)) for s in solids)
+    pscale = sum(float(np.sum(s.mass * np.linalg.norm(s.velocity, axis=1))) for s in solids)
+    done = 0
+    while done < steps:
+        n = min(record_every, steps - done)
+        c.step(n)
+        done += n
+        recs.append(c.energies())
+    m_grid = c.download_grid(grid.nodeCount)[0]
+    c.close()
+    return recs, mass, pscale, float(np.sum(m_grid))
+
+
+# ---------------------------------------------------------------------------
+# manufactured solution: the standing wave u_x = G sin(pi x) sin(c pi t) of the
+# reference's 1D MMS (Main_MMS_1D.jl:26-77, BodyForce.jl:68-75).  The reference
+# drives a neo-Hookean bar and adds the body force that balances its
+# nonlinearity; for the linear elastic material this u is an exact solution with
+# no body force (c^2 = (lambda + 2 mu)/rho in plane strain with u_y = 0), which the
+# accelerated path's constant body force can express.  A strip [0, 1] x [0, 2h],
+# x fixed at x = 0 and 1, every node fixed in y, initial velocity pi c G sin(pi x).
+
+MMS = {"E": 1e7, "nu": 0.3, "rho": 1000.0, "G": 1e-4}
+
+
+def mms_errors(ctx_cls, ncell, cfl=0.1, ppc=2):
+    """RMS displacement and velocity errors (relative to G and pi c G) at t = 0.3/c."""
+    E, nu, rho, G = MMS["E"], MMS["nu"], MMS["rho"], MMS["G"]
+    lam, mu = lame(E, nu)
+    c = math.sqrt((lam + 2 * mu) / rho)
+    h = 1.0 / ncell
+    grid = Grid2D(0.0, 1.0, 0.0, 2 * h, ncell + 1, 3)
+    off = h / ppc
+    pts = buildParticleForRectangle([0.5, h], 1.0, 2 * h, off)
+    s = Solid2D(pts, ElasticMaterial(E, nu, rho, len(pts)))
+    s.mass *= off * off
+    s.volume[:] = off * off
+    s.volumeInitial[:] = off * off
+    x = s.pos[:, 0].copy()
+    s.velocity[:, 0] = math.pi * c * G * np.sin(math.pi * x)
+    fx = np.zeros_like(grid.fixedNodes)
+    fx[1, :] = 1
+    xs = np.tile(np.linspace(0.0, 1.0, ncell + 1), 3)
+    fx[0, np.isclose(xs, 0.0) | np.isclose(xs, 1.0)] = 1
+    grid.fixedNodes[:, :] = fx
+    T = 0.3 / c
+    n = int(round(T / (cfl * h / c)))
+    dt = T / n
+    ctx = ctx_cls(Descriptors(grid, [s], tolerance=0.0, body_force=ConstantBodyForce2D([0.0, 0.0]), dt=dt))
+    ctx.step(n)
+    st = ctx.download_body(0)
+    ctx.close()
+    t = n * dt
+    u_ex = G * np.sin(math.pi * x) * math.sin(c * math.pi * t)
+    v_ex = math.pi * c * G * np.sin(math.pi * x) * math.cos(c * math.pi * t)
+    eu = math.sqrt(float(np.mean((st.pos[:, 0] - x - u_ex) ** 2))) / G
+    ev = math.sqrt(float(np.mean((st.velocity[:, 0] - v_ex) ** 2))) / (math.pi * c * G)
+    return eu, ev
