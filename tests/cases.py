@@ -130,3 +130,51 @@ def field_errors(states_a, states_b, fields=FIELDS):
         for f in fields:
             errs[(s, f)] = rel_err(getattr(A, f), getattr(B, f))
     return errs
+
+
+# Per-particle metric: |a_p - b_p| / max(|b_p|, floor_f) per particle entry, with
+# the absolute floor of field f a stated fraction of that field's scale (its
+# largest magnitude, over the states compared or a given set of states).  Values
+# smaller than the floor are compared at the floor's level: a particle whose
+# component is zero by symmetry, or rounding noise of a rigidly moving body,
+# would otherwise divide noise by noise.
+PP_FLOOR = 1e-3
+
+
+def field_scales(states, fields=FIELDS):
+    return {f: max((float(np.max(np.abs(getattr(s, f)))) if getattr(s, f).size else 0.0) for s in states)
+            for f in fields}
+
+
+def particle_errors(states_a, states_b, fields=FIELDS, floor=PP_FLOOR, scales=None):
+    """{field: max per-particle error} over all bodies, floor_f = floor * scale_f."""
+    sc = scales or field_scales(states_b, fields)
+    out = {}
+    for f in fields:
+        worst = 0.0
+        fl = floor * sc[f]
+        for A, B in zip(states_a, states_b):
+            a = np.asarray(getattr(A, f), dtype=np.float64).ravel()
+            b = np.asarray(getattr(B, f), dtype=np.float64).ravel()
+            if b.size == 0:
+                continue
+            d = np.abs(a - b)
+            den = np.maximum(np.abs(b), fl)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                r = np.where(den > 0, d / den, np.where(d > 0, np.inf, 0.0))
+            worst = max(worst, float(np.max(r)))
+        out[f] = worst
+    return out
+
+
+def scaled_field_errors(states_a, states_b, fields=FIELDS, scales=None):
+    """{field: max |a - b| / scale_f} over all bodies (the field-max metric with a
+    shared scale, e.g. an ensemble's)."""
+    sc = scales or field_scales(states_b, fields)
+    out = {}
+    for f in fields:
+        num = max((float(np.max(np.abs(np.asarray(getattr(A, f)) - np.asarray(getattr(B, f)))))
+                   if getattr(B, f).size else 0.0) for A, B in zip(states_a, states_b))
+        out[f] = num / sc[f] if sc[f] > 0 else num
+    return out
+
