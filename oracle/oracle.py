@@ -1,4 +1,5 @@
-"""ctypes binding of the CPU oracle (oracle/mpm_oracle.cpp).
+"""ctypes binding of the CPU oracle (oracle/mpm_oracle.cpp) and of its
+dual-number restatement for gradients (oracle/mpm_dual.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and bench.py's
 CPU-baseline leg, never by the jump_gb300 package.  It consumes the same
@@ -20,24 +21,33 @@ from jump_gb300.engine import BodyState, Descriptors, _ContextBase
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "mpm_oracle.cpp")
 LIB = os.path.join(HERE, "_build", "libmpm_oracle.so")
+DUAL_SRC = os.path.join(HERE, "mpm_dual.cpp")
+DUAL_LIB = os.path.join(HERE, "_build", "libmpm_dual.so")
 
 _lib = None
+_dual = None
+
+
+def _compile(src: str, out: str, force: bool, openmp: bool) -> str:
+    hdr = os.path.join(HERE, "..", "include", "jump_mpm.h")
+    if (not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src)
+            and os.path.getmtime(out) >= os.path.getmtime(hdr)):
+        return out
+    base = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", src, "-o", out]
+    r = subprocess.run(base[:6] + ["-fopenmp"] + base[6:], capture_output=True, text=True) if openmp else None
+    if r is None or r.returncode != 0:
+        r = subprocess.run(base, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"oracle build failed ({os.path.basename(src)}):\n" + r.stderr)
+    return out
 
 
 def build(force: bool = False) -> str:
-    """g++ -O3 -ffp-contract=off (no FMA contraction), OpenMP when available."""
+    """g++ -O3 -ffp-contract=off (no FMA contraction), OpenMP when available; both the
+    oracle and its dual-number (forward-mode gradient) restatement."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    hdr = os.path.join(HERE, "..", "include", "jump_mpm.h")
-    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC)
-            and os.path.getmtime(LIB) >= os.path.getmtime(hdr)):
-        return LIB
-    base = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", SRC, "-o", LIB]
-    r = subprocess.run(base[:6] + ["-fopenmp"] + base[6:], capture_output=True, text=True)
-    if r.returncode != 0:
-        r = subprocess.run(base, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("oracle build failed:\n" + r.stderr)
-    return LIB
+    _compile(DUAL_SRC, DUAL_LIB, force, openmp=False)
+    return _compile(SRC, LIB, force, openmp=True)
 
 
 def lib():
@@ -130,8 +140,51 @@ def shape(grid_desc, basis: int, x):
     return near[:n].copy(), N[:n].copy(), dN[: n * d].reshape(n, d).copy()
 
 
+def dual_lib():
+    global _dual
+    if _dual is None:
+        if not os.path.exists(DUAL_LIB):
+            build()
+        L = C.CDLL(DUAL_LIB)
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int64)
+        L.dual_grad.argtypes = [C.POINTER(_capi.GridDesc), C.POINTER(_capi.BodyDesc), C.c_int32,
+                                C.POINTER(_capi.Params), C.c_int64, C.c_int32, ip, C.c_int32, dp, dp]
+        L.dual_run.argtypes = [C.POINTER(_capi.GridDesc), C.POINTER(_capi.BodyDesc), C.c_int32,
+                               C.POINTER(_capi.Params), C.c_int64, dp, dp]
+        _dual = L
+    return _dual
+
+
+def dual_gradient(desc: Descriptors, nsteps: int, kind: str, ids, xbar) -> np.ndarray:
+    """d(xbar . x_final)/d(parameter) by forward-mode dual numbers through the
+    templated restatement (oracle/mpm_dual.cpp): kind "E" (ids: particles, their
+    Young's modulus) or "v0" (ids: particle * dim + component of the initial
+    velocity).  USL, linear basis, one velocity field; elastic, neo-Hookean, J2."""
+    ids = np.ascontiguousarray(ids, dtype=np.int64)
+    xb = np.ascontiguousarray(xbar, dtype=np.float64).ravel()
+    out = np.zeros(len(ids))
+    rc = dual_lib().dual_grad(C.byref(desc.grid), desc.bodies, desc.nbodies, C.byref(desc.params), int(nsteps),
+                              {"E": 0, "v0": 1}[kind], ids.ctypes.data_as(C.POINTER(C.c_int64)), len(ids),
+                              _capi.dptr(xb), _capi.dptr(out))
+    if rc != 0:
+        raise _capi.MPMError(rc, "dual_grad failed")
+    return out
+
+
+def dual_values(desc: Descriptors, nsteps: int):
+    """(positions, stresses) of the templated restatement run with plain doubles."""
+    n = sum(desc.bodies[s].count for s in range(desc.nbodies))
+    d = desc.dim
+    pos, sig = np.zeros(n * d), np.zeros(n * d * d)
+    rc = dual_lib().dual_run(C.byref(desc.grid), desc.bodies, desc.nbodies, C.byref(desc.params), int(nsteps),
+                             _capi.dptr(pos), _capi.dptr(sig))
+    if rc != 0:
+        raise _capi.MPMError(rc, "dual_run failed")
+    return pos.reshape(n, d), sig
+
+
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
 
 
-__all__ = ["OracleContext", "BodyState", "build", "lib", "max_threads", "shape"]
+__all__ = ["OracleContext", "BodyState", "build", "lib", "max_threads", "shape", "dual_gradient", "dual_values"]
