@@ -1,6 +1,11 @@
 // mpm_adjoint.cuh -- reverse-mode (adjoint) kernels of one USL step, FP64,
-// single velocity field, neo-Hookean bodies (the material of the inverse
-// problems this serves), D = 2, 3.
+// single velocity field, neo-Hookean, linear elastic and J2 bodies, D = 2, 3.
+// The neo-Hookean stress is a function of F, so its P2G adjoint maps the
+// stress adjoint onto F directly (below).  The elastic and J2 stresses are
+// particle state formed by the previous G2P's update_stress!: the P2G adjoint
+// stores the stress adjoint, and the previous step's G2P adjoint runs it back
+// through the constitutive update (stress_adj) onto the strain, the plastic
+// state and the moduli.
 //
 // State of a step n: (x, v, F) per particle, with sigma = NH(F; lambda_p,
 // mu_p) and V = det(F) V0 derived from F.  The forward step (mpm_kernels.cuh)
@@ -26,10 +31,15 @@
 namespace jmpm {
 
 // particle adjoints, SoA (component-major) with pitch = particle count:
-// x_ (D) | v_ (D) | F_ (D*D, column-major) | E_ (1)
+// x_ (D) | v_ (D) | F_ (D*D, column-major) | E_ (1), and for the materials whose
+// stress is state (linear elastic, J2): strain_ (S) | sigma_ (S) | pstrain_ (S)
+// | alpha_ (1), adjoints of the stored symmetric components
 template <int D>
 struct AdjLayout {
-  static constexpr int XB = 0, VB = D, FB = 2 * D, EB = 2 * D + D * D, NF = 2 * D + D * D + 1;
+  static constexpr int S = (D == 2) ? 3 : 6;
+  static constexpr int XB = 0, VB = D, FB = 2 * D, EB = 2 * D + D * D;
+  static constexpr int EPSB = EB + 1, SIGB = EPSB + S, EPB = SIGB + S, ALB = EPB + S;
+  static constexpr int NF = ALB + 1;
 };
 
 struct AdjP {
@@ -112,8 +122,139 @@ __device__ __forceinline__ double* adj(const AdjP& ad, int f, int64_t p) {
   return ad.base + int64_t(f) * ad.pitch + p;
 }
 
-template <int D>
-__global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, PartP pp, AdjP ad, NodeAdjP na) {
+// ---------------------------------------------------------------------------
+// Reverse of update_stress! for the materials whose stress is particle state
+// (linear elastic, Material.jl:68-81; J2 radial return, :174-275), at the
+// strain eps' = eps + sym(L dt) the forward G2P formed.  In: the adjoints of its
+// outputs sigma' (sb), alpha' (ab), pstrain' (pb) in stored symmetric
+// components; out: the adjoint of eps' (added to eb), of the incoming pstrain
+// and alpha (written to pb, ab), and of the moduli (G = 2 mu, lambda, kappa)
+// as dL/dmu and dL/dlambda.  Forward as in mpm_kernels.cuh (j2_3d: deviator
+// with 0.333333333, |s| = sqrt(sum w s^2) with w = 2 off the diagonal,
+// kappa = lambda + mu, linear hardening k1; j2_2d: the Voigt form).
+template <int D, int MAT>
+__device__ __forceinline__ void stress_adj(const double* eps, double lam, double mu, const MatParams& mp,
+                                           const double* ep_in, double alpha_in, const double* sb, double* eb,
+                                           double* pb, double& ab, double& mub, double& lamb) {
+  constexpr int S = Layout<D>::S;
+  const double G = 2.0 * mu;
+  if (MAT == MPM_MAT_ELASTIC) {
+    // sigma_c = G eps_c + lambda tr (c < D)
+    double tr = 0.0, strb = 0.0, Gb = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      tr += eps[c];
+      strb += sb[c];
+    }
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      eb[c] += G * sb[c] + (c < D ? lam * strb : 0.0);
+      Gb += sb[c] * eps[c];
+    }
+    mub += 2.0 * Gb;
+    lamb += tr * strb;
+    return;
+  }
+  const double kappa = lam + mu, k1 = mp.k1, fy = mp.fy;
+  double d[S], s[S], w[S], sv[S];
+  double tr;
+  if constexpr (D == 3) {
+    tr = (eps[0] + eps[1]) + eps[2];
+    const double tt = 0.333333333 * tr;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      d[c] = c < 3 ? eps[c] - tt : eps[c];
+      s[c] = G * (d[c] - ep_in[c]);
+      w[c] = c < 3 ? 1.0 : 2.0;
+      sv[c] = 1.0;  // sigma_c = s_c (+ kt) - G lamp n_c
+    }
+  } else {
+    // Voigt: e = (xx, yy, 2 xy), deviator (e0 - e1)/2, (e1 - e0)/2, e2
+    const double e0 = eps[0], e1 = eps[1], e2 = 2.0 * eps[2];
+    tr = e0 + e1;
+    d[0] = 0.5 * e0 + (-0.5) * e1;
+    d[1] = -0.5 * e0 + 0.5 * e1;
+    d[2] = e2;
+    s[0] = G * (d[0] - ep_in[0]);
+    s[1] = G * (d[1] - ep_in[1]);
+    s[2] = 0.5 * (G * (d[2] - ep_in[2]));
+    w[0] = w[1] = 1.0;
+    w[2] = 2.0;
+    sv[0] = sv[1] = sv[2] = 1.0;
+  }
+  double q = 0.0;
+#pragma unroll
+  for (int c = 0; c < S; ++c) q += w[c] * s[c] * s[c];
+  const double ns = sqrt(q);
+  double sbar[S], kt_b = 0.0, Gb = 0.0;
+#pragma unroll
+  for (int c = 0; c < S; ++c) sbar[c] = sb[c];
+#pragma unroll
+  for (int c = 0; c < D; ++c) kt_b += sb[c];
+  double alpha_b = ab;  // alpha' = alpha (+ lamp)
+  double epb_pass[S];   // pstrain' = pstrain (+ lamp n, times 2 for the 2D shear)
+#pragma unroll
+  for (int c = 0; c < S; ++c) epb_pass[c] = pb[c];
+  const double ftrial = ns - (k1 * alpha_in + fy);
+  if (!(ftrial <= 0.0) && ns > 0.0) {
+    const double r = 1.0 / (G + k1);
+    const double lamp = ((ns - k1 * alpha_in) - fy) * r;
+    const double ins = 1.0 / ns;
+    double n[S], lampb = ab, nsb = 0.0;
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      n[c] = s[c] * ins;
+      const double ew = (D == 2 && c == 2) ? 2.0 : 1.0;  // 2D pstrain shear takes 2 n (Iinv)
+      lampb += pb[c] * ew * n[c] - G * sb[c] * n[c];
+      Gb -= lamp * sb[c] * n[c];
+    }
+    Gb -= lampb * lamp * r;  // lamp = (ns - k1 alpha - fy) / (G + k1)
+    double nb[S];
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      const double ew = (D == 2 && c == 2) ? 2.0 : 1.0;
+      nb[c] = lamp * pb[c] * ew - G * lamp * sb[c];
+      nsb -= nb[c] * s[c] * ins * ins;
+    }
+    nsb += lampb * r;
+#pragma unroll
+    for (int c = 0; c < S; ++c) sbar[c] += nb[c] * ins + nsb * w[c] * s[c] * ins;
+    alpha_b -= k1 * r * lampb;
+  }
+  (void)sv;
+  // s_c = G (d_c - ep_c)  (2D shear: 0.5 G (d_2 - ep_2))
+  double db[S];
+#pragma unroll
+  for (int c = 0; c < S; ++c) {
+    const double h = (D == 2 && c == 2) ? 0.5 : 1.0;
+    db[c] = h * G * sbar[c];
+    epb_pass[c] -= h * G * sbar[c];
+    Gb += h * sbar[c] * (d[c] - ep_in[c]);
+  }
+  const double kappab = kt_b * tr;
+  if constexpr (D == 3) {
+    const double ttb = -((db[0] + db[1]) + db[2]);
+    const double trb = 0.333333333 * ttb + kappa * kt_b;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) eb[c] += db[c] + (c < 3 ? trb : 0.0);
+  } else {
+    double e0b = 0.5 * db[0] - 0.5 * db[1] + kappa * kt_b;
+    double e1b = -0.5 * db[0] + 0.5 * db[1] + kappa * kt_b;
+    eb[0] += e0b;
+    eb[1] += e1b;
+    eb[2] += 2.0 * db[2];
+  }
+#pragma unroll
+  for (int c = 0; c < S; ++c) pb[c] = epb_pass[c];
+  ab = alpha_b;
+  // G = 2 mu, kappa = lambda + mu
+  mub += 2.0 * Gb + kappab;
+  lamb += kappab;
+}
+
+template <int D, int MAT>
+__global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, PartP pp, AdjP ad, NodeAdjP na,
+                                                      MatParams mp, double c1, double c2) {
   using L = Layout<D>;
   using A = AdjLayout<D>;
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -165,6 +306,56 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, Part
       for (int i = 0; i < D; ++i) s += F[i + D * k] * Fb[i + D * j];
       Ab[k][j] = s;
     }
+  if constexpr (MAT != MPM_MAT_NEOHOOKEAN) {
+    // the strain and stress update of this G2P: eps' = eps + sym(Ldt), then
+    // update_stress! at eps' (its adjoint from the next step's P2G and G2P)
+    constexpr int S = Layout<D>::S;
+    double eps[S], ep_in[S], sb[S], eb[S], pb[S];
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = i; j < D; ++j) {
+        const int c = sym<D>(i, j);
+        const double de = i == j ? Ldt[i][i] : 0.5 * (Ldt[i][j] + Ldt[j][i]);
+        eps[c] = P[int64_t(L::EPS + c) * pp.pitch + p] + de;
+      }
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      ep_in[c] = MAT == MPM_MAT_J2 ? P[int64_t(L::EP + c) * pp.pitch + p] : 0.0;
+      sb[c] = *adj<D>(ad, A::SIGB + c, p);
+      eb[c] = *adj<D>(ad, A::EPSB + c, p);
+      pb[c] = *adj<D>(ad, A::EPB + c, p);
+    }
+    double ab = *adj<D>(ad, A::ALB, p);
+    const double alpha_in = MAT == MPM_MAT_J2 ? P[int64_t(L::ALPHA) * pp.pitch + p] : 0.0;
+    double lam = mp.lambda, mu = mp.mu;
+    if (mp.per_particle) {
+      lam = P[int64_t(L::LAM) * pp.pitch + p];
+      mu = P[int64_t(L::MU) * pp.pitch + p];
+    }
+    double mub = 0.0, lamb = 0.0;
+    stress_adj<D, MAT>(eps, lam, mu, mp, ep_in, alpha_in, sb, eb, pb, ab, mub, lamb);
+    // eps' = eps + sym(Ldt): eps_ passes through, Ldt_ += the symmetric part
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = i; j < D; ++j) {
+        const int c = sym<D>(i, j);
+        if (i == j) {
+          Ab[i][i] += eb[c];
+        } else {
+          Ab[i][j] += 0.5 * eb[c];
+          Ab[j][i] += 0.5 * eb[c];
+        }
+      }
+#pragma unroll
+    for (int c = 0; c < S; ++c) {
+      *adj<D>(ad, A::EPSB + c, p) = eb[c];
+      *adj<D>(ad, A::EPB + c, p) = pb[c];
+    }
+    *adj<D>(ad, A::ALB, p) = ab;
+    *adj<D>(ad, A::EB, p) += c1 * lamb + c2 * mub;
+  }
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
@@ -260,7 +451,7 @@ __device__ __forceinline__ void inv_det(const double* F, double* Fi, double& J) 
   }
 }
 
-template <int D>
+template <int D, int MAT>
 __global__ void __launch_bounds__(256) p2g_adj_kernel(GridP gp, PartP pp, AdjP ad, NodeAdjP na, MatParams mp,
                                                       double c1, double c2, double bx, double by, double bz) {
   using L = Layout<D>;
@@ -330,11 +521,31 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(GridP gp, PartP pp, AdjP a
     }
     add_shape_adj<D>(xb, c, k, wb, gb);
   }
-  // sigma = NH(F) = (mu (F F^T - I) + lambda ln J I) / J ;  V = J V0
   double F[D * D], Fi[D * D], J;
 #pragma unroll
   for (int q = 0; q < D * D; ++q) F[q] = fld(L::F + q);
   inv_det<D>(F, Fi, J);
+  if constexpr (MAT != MPM_MAT_NEOHOOKEAN) {
+    // the stress is particle state: its adjoint (stored symmetric components)
+    // goes to the G2P adjoint of the previous step, which formed it; V = J V0
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = i; j < D; ++j)
+        *adj<D>(ad, A::SIGB + sym<D>(i, j), p) = i == j ? sb[i][i] : sb[i][j] + sb[j][i];
+    const double cV = Vb * V0 * J;
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+      for (int q = 0; q < D; ++q) *adj<D>(ad, A::FB + a + D * q, p) += cV * Fi[q + D * a];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      *adj<D>(ad, A::XB + a, p) = xb[a];
+      *adj<D>(ad, A::VB + a, p) = vb[a];
+    }
+    return;
+  }
+  // sigma = NH(F) = (mu (F F^T - I) + lambda ln J I) / J ;  V = J V0
   double lam = mp.lambda, mu = mp.mu;
   if (mp.per_particle) {
     lam = fld(L::LAM);

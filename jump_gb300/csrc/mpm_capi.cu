@@ -1202,8 +1202,9 @@ int mpm_fwd_checkpointed(mpm_ctx* c, int64_t nsteps, int32_t every) {
     return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode needs USL with the linear basis, FP64 "
                                      "particles, one velocity field and no sorting");
   for (const MatParams& m : c->mats)
-    if (m.type != MPM_MAT_NEOHOOKEAN)
-      return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode is built for neo-Hookean bodies");
+    if (m.type != MPM_MAT_NEOHOOKEAN && m.type != MPM_MAT_ELASTIC && m.type != MPM_MAT_J2)
+      return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode is built for neo-Hookean, linear "
+                                       "elastic and J2 bodies");
   const size_t bytes = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1) * c->esz;
   const int64_t slots = (nsteps + every - 1) / every + 1;  // steps 0, every, ... and the final state
   if (slots != c->ckpt_slots) {
@@ -1323,8 +1324,10 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
       // the node adjoints vdt_bar, dv_bar are zero here: set once below, then zeroed by grid_adj
       for (int b = 0; b < c->nb; ++b) {
         const PartP ps{c->segbuf + bytes * size_t(j), c->np, c->off[b], c->cnt[b]};
-        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
-        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
+        const double nu = c->nus[b];
+        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);  // dlambda/dE, dmu/dE
+        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
+        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
       }
       if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
       else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
@@ -1372,8 +1375,10 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
       char* state = reinterpret_cast<char*>(c->ckpt) + bytes * size_t(k - 1);
       for (int b = 0; b < c->nb; ++b) {
         const PartP ps{state, c->np, c->off[b], c->cnt[b]};
-        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
-        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na);
+        const double nu = c->nus[b];
+        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
+        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
+        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
       }
       if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
       else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);

@@ -106,9 +106,10 @@ struct Launchers {
   static void grid(cudaStream_t s, const NodeP& nd, double dt, double tol, bool f32copy);
   // zero the accumulators of the blocks listed by the previous grid stage
   static void clear(cudaStream_t s, const NodeP& nd);
-  // adjoint of one step (mpm_adjoint.cuh), FP64 particles
+  // adjoint of one step (mpm_adjoint.cuh), FP64 particles; mp.type selects the
+  // material (neo-Hookean, linear elastic, J2); c1, c2 = dlambda/dE, dmu/dE
   static void g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, const PartP& pp, const AdjP& ad,
-                      const NodeAdjP& na);
+                      const NodeAdjP& na, const MatParams& mp, double c1, double c2);
   static void grid_adj(cudaStream_t s, const GridRec& gr, const NodeAdjP& na, const uint8_t* fixed, double dt,
                        double tol);
   static void p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, const AdjP& ad, const NodeAdjP& na,

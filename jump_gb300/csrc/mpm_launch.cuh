@@ -90,10 +90,16 @@ void Launchers<D>::contact_grid(cudaStream_t s, const NodeP& nd, const ContactP&
 
 template <int D>
 void Launchers<D>::g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, const PartP& pp, const AdjP& ad,
-                           const NodeAdjP& na) {
+                           const NodeAdjP& na, const MatParams& mp, double c1, double c2) {
   if (pp.count <= 0) return;
   const int th = spread_threads(pp.count);
-  g2p_adj_kernel<D><<<blocks_for(pp.count, th), th, 0, s>>>(g, gr, pp, ad, na);
+  const unsigned nb = blocks_for(pp.count, th);
+  if (mp.type == MPM_MAT_ELASTIC)
+    g2p_adj_kernel<D, MPM_MAT_ELASTIC><<<nb, th, 0, s>>>(g, gr, pp, ad, na, mp, c1, c2);
+  else if (mp.type == MPM_MAT_J2)
+    g2p_adj_kernel<D, MPM_MAT_J2><<<nb, th, 0, s>>>(g, gr, pp, ad, na, mp, c1, c2);
+  else
+    g2p_adj_kernel<D, MPM_MAT_NEOHOOKEAN><<<nb, th, 0, s>>>(g, gr, pp, ad, na, mp, c1, c2);
 }
 
 template <int D>
@@ -108,8 +114,14 @@ void Launchers<D>::p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, cons
                            const MatParams& mp, double c1, double c2, const double* grav) {
   if (pp.count <= 0) return;
   const int th = spread_threads(pp.count);
-  p2g_adj_kernel<D><<<blocks_for(pp.count, th), th, 0, s>>>(g, pp, ad, na, mp, c1, c2, grav[0], grav[1],
-                                                              D == 3 ? grav[2] : 0.0);
+  const unsigned nb = blocks_for(pp.count, th);
+  const double gz = D == 3 ? grav[2] : 0.0;
+  if (mp.type == MPM_MAT_ELASTIC)
+    p2g_adj_kernel<D, MPM_MAT_ELASTIC><<<nb, th, 0, s>>>(g, pp, ad, na, mp, c1, c2, grav[0], grav[1], gz);
+  else if (mp.type == MPM_MAT_J2)
+    p2g_adj_kernel<D, MPM_MAT_J2><<<nb, th, 0, s>>>(g, pp, ad, na, mp, c1, c2, grav[0], grav[1], gz);
+  else
+    p2g_adj_kernel<D, MPM_MAT_NEOHOOKEAN><<<nb, th, 0, s>>>(g, pp, ad, na, mp, c1, c2, grav[0], grav[1], gz);
 }
 
 template <int D>

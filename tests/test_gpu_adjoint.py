@@ -1,9 +1,16 @@
-"""Reverse mode: gradients of a tip-displacement loss with respect to
-per-particle Young's modulus and initial velocity, from the adjoint kernels
-on the GPU, against central finite differences of the deterministic CPU
-oracle (cross-implementation check), on a short 2D neo-Hookean cantilever
-and a small 3D neo-Hookean block (400 steps, long enough for the clamp to be
-felt at the tip)."""
+"""Reverse mode: gradients of a loss on the final positions with respect to
+per-particle Young's modulus and initial velocity, from the adjoint kernels on
+the GPU, against
+
+* forward-mode dual numbers through the templated restatement of the step
+  (oracle/mpm_dual.cpp) for neo-Hookean, linear elastic and J2 bodies in 2D and
+  3D (bound 1e-8, norm-relative), and
+* central finite differences of the deterministic CPU oracle on a 2D
+  neo-Hookean cantilever and a 3D neo-Hookean block (400 steps, long enough
+  for the clamp to be felt at the tip);
+
+and the inverse problems the gradients serve: recovering a stiffness field and
+an initial velocity field from final positions."""
 import copy
 
 import numpy as np
@@ -95,6 +102,66 @@ def test_adjoint_matches_finite_differences(dim, oracle_lib):
         ad_v.append(g["v0"][p, a])
     fd_v, ad_v = np.array(fd_v), np.array(ad_v)
     assert np.linalg.norm(ad_v - fd_v) <= 1e-5 * np.linalg.norm(fd_v), (ad_v, fd_v)
+
+
+def _desc_for(problem, E, v0):
+    grid, solids, alg, data = problem
+    solids = copy.deepcopy(solids)
+    off = 0
+    for s in solids:
+        n = s.parCount
+        s.youngs = np.asarray(E[off:off + n], dtype=np.float64).copy()
+        s.velocity = np.asarray(v0[off:off + n]).reshape(n, s.dim).copy()
+        off += n
+    scenarios.apply_dirichlet(grid, data)
+    return Descriptors(grid, solids, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"])
+
+
+DUAL_CASES = {
+    # name: (problem, steps, checkpoint interval)
+    "cantilever_nh_2d": (lambda: scenarios.cantilever(h=0.0625, ppc=2, length=1.0, depth=0.25), 400, 50),
+    "disks_elastic_2d": (lambda: scenarios.two_disks(centers=((0.3, 0.3), (0.585, 0.585))), 150, 25),
+    "disks_j2_2d": (lambda: scenarios.two_disks(material="j2", centers=((0.3, 0.3), (0.585, 0.585))), 150, 25),
+    "block_nh_3d": (lambda: scenarios.block_3d(), 200, 50),
+    "taylor_j2_3d": (lambda: scenarios.taylor_bar(h=1e-3), 30, 10),
+}
+
+
+@pytest.mark.parametrize("name", sorted(DUAL_CASES))
+def test_adjoint_matches_dual_numbers(name, oracle_lib):
+    """dL/dE and dL/dv0 of L = xbar . x_final: the GPU adjoint against forward-mode
+    dual numbers through the restatement, on the same seeded inputs."""
+    make, nsteps, every = DUAL_CASES[name]
+    problem = make()
+    scenarios.apply_dirichlet(problem[0], problem[3])
+    solids = problem[1]
+    rng = np.random.default_rng(3)
+    E = np.concatenate([np.full(s.parCount, s.mat.E) if getattr(s, "youngs", None) is None else s.youngs
+                        for s in solids])
+    E = E * np.exp(rng.uniform(-0.2, 0.2, len(E)))  # per-particle moduli
+    v0 = np.concatenate([s.velocity for s in solids])
+    n, d = v0.shape
+    xbar = rng.normal(size=(n, d))
+    ctx = make_context(problem, E, v0)
+    ctx.fwd_checkpointed(nsteps, every)
+    g = ctx.bwd(xbar)
+    ctx.close()
+    o = oracle_lib.OracleContext(_desc_for(problem, E, v0))
+    o.step(nsteps)
+    st = o.download_all()
+    o.close()
+    if name.startswith(("disks_j2", "taylor_j2")):
+        assert max(float(np.max(s.alpha)) for s in st) > 0, "the J2 case must yield"
+    # half the checked particles among the most strained (where E matters), half at random
+    strain = np.concatenate([np.abs(s.strain.reshape(s.n, -1)).max(axis=1) for s in st])
+    ids = np.unique(np.concatenate([np.argsort(strain)[-8:], rng.choice(n, 8, replace=False)]))
+    dual = oracle_lib.dual_gradient(_desc_for(problem, E, v0), nsteps, "E", ids, xbar)
+    ad = g["E"][ids]
+    assert np.linalg.norm(ad - dual) <= 1e-8 * np.linalg.norm(dual), (ad, dual)
+    vid = rng.choice(n * d, 16, replace=False)
+    dual_v = oracle_lib.dual_gradient(_desc_for(problem, E, v0), nsteps, "v0", vid, xbar)
+    ad_v = g["v0"].ravel()[vid]
+    assert np.linalg.norm(ad_v - dual_v) <= 1e-8 * np.linalg.norm(dual_v), (ad_v, dual_v)
 
 
 def test_checkpointed_forward_is_the_forward():
