@@ -85,10 +85,11 @@ struct mpm_ctx {
   int32_t adj_every = 0;
   char* segbuf = nullptr;
   int32_t segbuf_slots = 0;
-  // captured reverse segment (recompute + reverse sweep), per segment length
-  cudaGraph_t seg_graph[2] = {nullptr, nullptr};
-  cudaGraphExec_t seg_exec[2] = {nullptr, nullptr};
-  int seg_len[2] = {0, 0};
+  // captured reverse-mode segments: [kind: 0 recompute, 1 reverse sweep][segment
+  // buffer][full or last (shorter) segment length]
+  cudaGraph_t seg_graph[2][2][2] = {};
+  cudaGraphExec_t seg_exec[2][2][2] = {};
+  int seg_len[2][2][2] = {};
   double* gridrec = nullptr;
   double* adjbuf = nullptr;
   double* nodeadj = nullptr;
@@ -120,6 +121,10 @@ struct mpm_ctx {
   int64_t rec_cap = 0;          // records it holds
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  // reverse mode: the second stream the reverse sweep runs on while the first
+  // recomputes the next segment, and the events that order the two
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_adj[2] = {nullptr, nullptr}, ev_sync = nullptr;
   cudaGraph_t graph[2] = {nullptr, nullptr};       // one step, per physical buffer
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   double last_ms = 0.0;
@@ -162,6 +167,19 @@ __global__ void iota_kernel(int64_t* p, int64_t n) {
     p[i] = i;
 }
 
+// drop the captured reverse-mode segment graphs (their buffers changed)
+void drop_seg_graphs(mpm_ctx* c) {
+  for (int k = 0; k < 2; ++k)
+    for (int b = 0; b < 2; ++b)
+      for (int l = 0; l < 2; ++l) {
+        if (c->seg_exec[k][b][l]) cudaGraphExecDestroy(c->seg_exec[k][b][l]);
+        if (c->seg_graph[k][b][l]) cudaGraphDestroy(c->seg_graph[k][b][l]);
+        c->seg_exec[k][b][l] = nullptr;
+        c->seg_graph[k][b][l] = nullptr;
+        c->seg_len[k][b][l] = 0;
+      }
+}
+
 void destroy_ctx(mpm_ctx* c) {
   if (!c) return;
   cudaFreeHost(c->rec_host);
@@ -188,10 +206,7 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->blockbuf);
   cudaFree(c->rmask);
   cudaFree(c->rtab);
-  for (int i = 0; i < 2; ++i) {
-    if (c->seg_exec[i]) cudaGraphExecDestroy(c->seg_exec[i]);
-    if (c->seg_graph[i]) cudaGraphDestroy(c->seg_graph[i]);
-  }
+  drop_seg_graphs(c);
   cudaFree(c->ckpt);
   cudaFree(c->segbuf);
   cudaFree(c->gridrec);
@@ -205,6 +220,12 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->staging);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
+  for (int i = 0; i < 2; ++i) {
+    if (c->ev_rec[i]) cudaEventDestroy(c->ev_rec[i]);
+    if (c->ev_adj[i]) cudaEventDestroy(c->ev_adj[i]);
+  }
+  if (c->ev_sync) cudaEventDestroy(c->ev_sync);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -244,12 +265,8 @@ void invalidate_graphs(mpm_ctx* c) {
     if (c->graph[i]) cudaGraphDestroy(c->graph[i]);
     c->exec[i] = nullptr;
     c->graph[i] = nullptr;
-    if (c->seg_exec[i]) cudaGraphExecDestroy(c->seg_exec[i]);
-    if (c->seg_graph[i]) cudaGraphDestroy(c->seg_graph[i]);
-    c->seg_exec[i] = nullptr;
-    c->seg_graph[i] = nullptr;
-    c->seg_len[i] = 0;
   }
+  drop_seg_graphs(c);
 }
 
 // Counting sort of all particles by (body, cell) into the other buffer; swaps buffers.
@@ -482,11 +499,20 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   std::vector<double> coords_h;
   for (int a = 0; a < D; ++a)
     for (int64_t i = 0; i < nn[a]; ++i) coords_h.push_back(gd->xmin[a] + double(i) * dx[a]);
-  CUDA_TRY(cudaMalloc(&c->coords, coords_h.size() * sizeof(double)));
-  CUDA_TRY(cudaMemcpy(c->coords, coords_h.data(), coords_h.size() * sizeof(double), cudaMemcpyHostToDevice));
+  // node coordinates in FP64, then the same rounded to float for FP32 particles
+  const size_t ncoord = coords_h.size();
+  std::vector<float> coords_f(ncoord);
+  for (size_t i = 0; i < ncoord; ++i) coords_f[i] = float(coords_h[i]);
+  CUDA_TRY(cudaMalloc(&c->coords, ncoord * (sizeof(double) + sizeof(float))));
+  CUDA_TRY(cudaMemcpy(c->coords, coords_h.data(), ncoord * sizeof(double), cudaMemcpyHostToDevice));
+  float* coordf = reinterpret_cast<float*>(c->coords + ncoord);
+  CUDA_TRY(cudaMemcpy(coordf, coords_f.data(), ncoord * sizeof(float), cudaMemcpyHostToDevice));
   int64_t o = 0;
   for (int a = 0; a < 3; ++a) {
     c->g.coord[a] = a < D ? c->coords + o : c->coords;
+    c->g.coordf[a] = a < D ? coordf + o : coordf;
+    c->g.xminf[a] = float(c->g.xmin[a]);
+    c->g.dxIf[a] = float(c->g.dxI[a]);
     if (a < D) o += nn[a];
   }
 
@@ -602,10 +628,15 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     }
   }
   if (c->f32) {
-    CUDA_TRY(cudaMalloc(&c->nodebuf_f, size_t(Nn) * 2 * D * sizeof(float)));
-    CUDA_TRY(cudaMemset(c->nodebuf_f, 0, size_t(Nn) * 2 * D * sizeof(float)));
+    // the linear-basis USL G2P reads interleaved per-node records (NodeP::nf4);
+    // the B-spline G2P the component-major copies
+    const bool inter = prm->basis == MPM_BASIS_LINEAR && !prm->contact && prm->algorithm == MPM_ALG_USL;
+    const size_t per = inter ? size_t(D == 2 ? 4 : 8) : size_t(2 * D);
+    CUDA_TRY(cudaMalloc(&c->nodebuf_f, size_t(Nn) * per * sizeof(float)));
+    CUDA_TRY(cudaMemset(c->nodebuf_f, 0, size_t(Nn) * per * sizeof(float)));
     c->nd.vdt_f = c->nodebuf_f;
     c->nd.dv_f = c->nodebuf_f + Nn * D;
+    c->nd.nf4 = inter ? reinterpret_cast<float4*>(c->nodebuf_f) : nullptr;
   }
 
   // particles
@@ -1263,22 +1294,26 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
   const size_t bytes = size_t(c->NF) * size_t(c->np > 0 ? c->np : 1) * c->esz;
   const int ANF = D == 2 ? AdjLayout<2>::NF : AdjLayout<3>::NF;
   const int XB = 0, VB = D, EB = 2 * D + D * D;
+  // two segment buffers: the reverse sweep reads one while the next segment is
+  // recomputed into the other
   if (c->segbuf_slots < every) {
-    for (int i = 0; i < 2; ++i) {  // captured segments point into the old buffers
-      if (c->seg_exec[i]) cudaGraphExecDestroy(c->seg_exec[i]);
-      if (c->seg_graph[i]) cudaGraphDestroy(c->seg_graph[i]);
-      c->seg_exec[i] = nullptr;
-      c->seg_graph[i] = nullptr;
-      c->seg_len[i] = 0;
-    }
+    drop_seg_graphs(c);  // captured segments point into the old buffers
     cudaFree(c->segbuf);
     cudaFree(c->gridrec);
     c->segbuf = nullptr;
     c->gridrec = nullptr;
     c->segbuf_slots = 0;
-    CUDA_TRY(cudaMalloc(&c->segbuf, bytes * size_t(every)));
-    CUDA_TRY(cudaMalloc(&c->gridrec, size_t(Nn) * (1 + 4 * D) * sizeof(double) * size_t(every)));
+    CUDA_TRY(cudaMalloc(&c->segbuf, bytes * size_t(2 * every)));
+    CUDA_TRY(cudaMalloc(&c->gridrec, size_t(Nn) * (1 + 4 * D) * sizeof(double) * size_t(2 * every)));
     c->segbuf_slots = every;
+  }
+  if (!c->stream2) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      CUDA_TRY(cudaEventCreateWithFlags(&c->ev_rec[i], cudaEventDisableTiming));
+      CUDA_TRY(cudaEventCreateWithFlags(&c->ev_adj[i], cudaEventDisableTiming));
+    }
+    CUDA_TRY(cudaEventCreateWithFlags(&c->ev_sync, cudaEventDisableTiming));
   }
   if (!c->adjbuf) {
     CUDA_TRY(cudaMalloc(&c->adjbuf, size_t(ANF) * size_t(c->np > 0 ? c->np : 1) * sizeof(double)));
@@ -1311,19 +1346,26 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
   const int64_t nseg = c->ckpt_slots - 1;
   void* Pwork = c->P;
   CUDA_TRY(cudaMemsetAsync(c->nodeadj, 0, size_t(Nn) * 2 * D * sizeof(double), c->stream));
-  // One segment: recompute `len` steps from the state in P, recording each
-  // step's particle state and grid outputs, then the reverse sweep over them.
-  auto enqueue_segment = [&](int len) {
+  // Segment buffer X (0, 1) holds `every` particle states and node records.
+  // Recompute: `len` steps from the state in P, recording each step's particle
+  // state and grid outputs in buffer X.  Reverse: the adjoint of those steps,
+  // last first, from buffer X.
+  const size_t recd = size_t(Nn) * (1 + 4 * D);
+  auto seg_state = [&](int X, int j) { return c->segbuf + bytes * size_t(X * every + j); };
+  auto seg_rec = [&](int X, int j) { return c->gridrec + recd * size_t(X * every + j); };
+  auto enqueue_recompute = [&](int X, int len) {
     for (int j = 0; j < len; ++j) {
-      cudaMemcpyAsync(c->segbuf + bytes * size_t(j), Pwork, bytes, cudaMemcpyDeviceToDevice, c->stream);
-      enqueue_step(c, nullptr, c->gridrec + size_t(Nn) * (1 + 4 * D) * size_t(j));
+      cudaMemcpyAsync(seg_state(X, j), Pwork, bytes, cudaMemcpyDeviceToDevice, c->stream);
+      enqueue_step(c, nullptr, seg_rec(X, j));
     }
+  };
+  auto enqueue_reverse = [&](int X, int len) {
     for (int j = len - 1; j >= 0; --j) {
-      const double* rec = c->gridrec + size_t(Nn) * (1 + 4 * D) * size_t(j);
+      const double* rec = seg_rec(X, j);
       const GridRec gr{rec, rec + Nn * (1 + 2 * D), rec + Nn * (1 + 3 * D)};
       // the node adjoints vdt_bar, dv_bar are zero here: set once below, then zeroed by grid_adj
       for (int b = 0; b < c->nb; ++b) {
-        const PartP ps{c->segbuf + bytes * size_t(j), c->np, c->off[b], c->cnt[b]};
+        const PartP ps{seg_state(X, j), c->np, c->off[b], c->cnt[b]};
         const double nu = c->nus[b];
         const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);  // dlambda/dE, dmu/dE
         if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
@@ -1332,37 +1374,39 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
       if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
       else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
       for (int b = 0; b < c->nb; ++b) {
-        const PartP ps{c->segbuf + bytes * size_t(j), c->np, c->off[b], c->cnt[b]};
+        const PartP ps{seg_state(X, j), c->np, c->off[b], c->cnt[b]};
         const double nu = c->nus[b];
-        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);  // dlambda/dE, dmu/dE
+        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
         if (D == 2) Launchers<2>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
         else Launchers<3>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
       }
     }
   };
-  // captured once per segment length (full segments, and a shorter last one)
-  auto segment_exec = [&](int len, cudaGraphExec_t* out) -> int {
-    for (int i = 0; i < 2; ++i)
-      if (c->seg_exec[i] && c->seg_len[i] == len) {
-        *out = c->seg_exec[i];
+  // captured once per (kind, buffer, segment length: full or the shorter last one),
+  // on the context's stream; launched on either stream
+  auto segment_exec = [&](int kind, int X, int len, cudaGraphExec_t* out) -> int {
+    for (int l = 0; l < 2; ++l)
+      if (c->seg_exec[kind][X][l] && c->seg_len[kind][X][l] == len) {
+        *out = c->seg_exec[kind][X][l];
         return MPM_OK;
       }
-    int slot = c->seg_exec[0] ? 1 : 0;
-    if (c->seg_exec[slot]) {
-      cudaGraphExecDestroy(c->seg_exec[slot]);
-      cudaGraphDestroy(c->seg_graph[slot]);
-      c->seg_exec[slot] = nullptr;
-      c->seg_graph[slot] = nullptr;
+    const int l = c->seg_exec[kind][X][0] ? 1 : 0;
+    if (c->seg_exec[kind][X][l]) {
+      cudaGraphExecDestroy(c->seg_exec[kind][X][l]);
+      cudaGraphDestroy(c->seg_graph[kind][X][l]);
+      c->seg_exec[kind][X][l] = nullptr;
+      c->seg_graph[kind][X][l] = nullptr;
     }
     CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_segment(len);
+    if (kind == 0) enqueue_recompute(X, len);
+    else enqueue_reverse(X, len);
     cudaError_t le = cudaGetLastError();
-    cudaError_t ee = cudaStreamEndCapture(c->stream, &c->seg_graph[slot]);
+    cudaError_t ee = cudaStreamEndCapture(c->stream, &c->seg_graph[kind][X][l]);
     if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_bwd launch: ") + cudaGetErrorString(le));
     if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_bwd capture: ") + cudaGetErrorString(ee));
-    CUDA_TRY(cudaGraphInstantiate(&c->seg_exec[slot], c->seg_graph[slot], 0));
-    c->seg_len[slot] = len;
-    *out = c->seg_exec[slot];
+    CUDA_TRY(cudaGraphInstantiate(&c->seg_exec[kind][X][l], c->seg_graph[kind][X][l], 0));
+    c->seg_len[kind][X][l] = len;
+    *out = c->seg_exec[kind][X][l];
     return MPM_OK;
   };
   if (every == 1 && c->fullrec) {
@@ -1391,14 +1435,41 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
       }
     }
   }
-  for (int64_t seg = (every == 1 && c->fullrec) ? -1 : nseg - 1; seg >= 0; --seg) {
-    const int64_t n0 = seg * every;
-    const int len = int(std::min<int64_t>(every, nsteps - n0));
-    CUDA_TRY(cudaMemcpyAsync(Pwork, c->ckpt + bytes * size_t(seg), bytes, cudaMemcpyDeviceToDevice, c->stream));
-    cudaGraphExec_t ex = nullptr;
-    int r = segment_exec(len, &ex);
-    if (r) return r;
-    CUDA_TRY(cudaGraphLaunch(ex, c->stream));
+  if (!(every == 1 && c->fullrec) && nseg > 0) {
+    // Checkpointed: segment seg - 1 is recomputed on the context's stream while
+    // the reverse sweep of segment seg runs on the second stream, in the other
+    // segment buffer.  A small problem (the 16,384-particle cantilever fills 5%
+    // of the warp slots) leaves most SMs idle in either pass, so the two
+    // overlap.  Stream order: recompute X -> ev_rec[X] -> reverse X ->
+    // ev_adj[X] -> the next recompute into X.
+    auto seg_len_of = [&](int64_t seg) { return int(std::min<int64_t>(every, nsteps - seg * every)); };
+    CUDA_TRY(cudaEventRecord(c->ev_sync, c->stream));  // adjoint inputs are set
+    CUDA_TRY(cudaStreamWaitEvent(c->stream2, c->ev_sync, 0));
+    bool used[2] = {false, false};
+    auto recompute = [&](int64_t seg, int X) -> int {
+      if (used[X]) CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_adj[X], 0));
+      CUDA_TRY(cudaMemcpyAsync(Pwork, c->ckpt + bytes * size_t(seg), bytes, cudaMemcpyDeviceToDevice, c->stream));
+      cudaGraphExec_t ex = nullptr;
+      int r = segment_exec(0, X, seg_len_of(seg), &ex);
+      if (r) return r;
+      CUDA_TRY(cudaGraphLaunch(ex, c->stream));
+      CUDA_TRY(cudaEventRecord(c->ev_rec[X], c->stream));
+      used[X] = true;
+      return MPM_OK;
+    };
+    int X = 0, r;
+    if ((r = recompute(nseg - 1, X))) return r;
+    for (int64_t seg = nseg - 1; seg >= 0; --seg) {
+      if (seg > 0 && (r = recompute(seg - 1, 1 - X))) return r;
+      cudaGraphExec_t ex = nullptr;
+      if ((r = segment_exec(1, X, seg_len_of(seg), &ex))) return r;
+      CUDA_TRY(cudaStreamWaitEvent(c->stream2, c->ev_rec[X], 0));
+      CUDA_TRY(cudaGraphLaunch(ex, c->stream2));
+      CUDA_TRY(cudaEventRecord(c->ev_adj[X], c->stream2));
+      X = 1 - X;
+    }
+    CUDA_TRY(cudaEventRecord(c->ev_sync, c->stream2));  // the context's stream waits for the sweep
+    CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_sync, 0));
   }
   CUDA_TRY(cudaGetLastError());
   // gradients in original particle order (no sorting in reverse mode)
