@@ -79,6 +79,11 @@ struct GridP {
   int64_t nn[3];       // nodes per axis
   int64_t nx, nxy, nodeCount;
   const double* coord[3];  // node coordinate per axis (xmin + i*dx, Grid.jl:149-152)
+  // FP32 particles: the same constants rounded to float once (the hat of an FP32
+  // particle needs them in float; converting per particle costs FP64-pipe work);
+  // coordf null: convert on the fly
+  float xminf[3], dxIf[3];
+  const float* coordf[3];
 };
 
 // Node arrays (FP64).  Accumulators m, p0 (D), f (D); grid-update outputs
@@ -91,6 +96,10 @@ struct NodeP {
   double* dv;
   float* vdt_f;  // FP32 copies for the FP32 particle path
   float* dv_f;
+  // or, for the linear-basis USL G2P of a single context, one interleaved FP32
+  // record per node (2D: vdt x y, dv x y = one float4; 3D: vdt x y z 0, dv x y z 0
+  // = two float4), so that a corner's six values come in two 16-byte loads
+  float4* nf4;
   const uint8_t* fixed;  // bit a set: dof a is fixed (grid.fixedNodes)
   int64_t nodeCount;
   int64_t nn[3];         // nodes per axis (1 for the unused axis in 2D)
@@ -221,15 +230,16 @@ struct Hat {
 // (Basis.jl:63-78, 104-137, 219-251, 292-332).  False if outside the grid.
 template <int D, class R>
 __device__ __forceinline__ bool hat(const GridP& g, const R* x, Hat<D, R>& h) {
+  const bool fc = sizeof(R) == 4 && g.coordf[0] != nullptr;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    R xmin = R(g.xmin[a]), dxI = R(g.dxI[a]);
+    R xmin = fc ? R(g.xminf[a]) : R(g.xmin[a]), dxI = fc ? R(g.dxIf[a]) : R(g.dxI[a]);
     R t = add_rn(mul_rn(sub_rn(x[a], xmin), dxI), R(1));
     int i1 = floor_to_int(t);  // 1-based base node
     if (i1 < 1 || i1 > int(g.nn[a] - 1)) return false;
     int c = i1 - 1;
     h.c[a] = c;
-    R xl = R(g.coord[a][c]), xh = R(g.coord[a][c + 1]);
+    R xl = fc ? R(g.coordf[a][c]) : R(g.coord[a][c]), xh = fc ? R(g.coordf[a][c + 1]) : R(g.coord[a][c + 1]);
     R dl = sub_rn(x[a], xl), dh = sub_rn(x[a], xh);
     h.Nl[a] = sub_rn(R(1), mul_rn(fabs(dl), dxI));
     h.Nh[a] = sub_rn(R(1), h.Nl[a]);  // 1 - |x - xh| dxI for xl <= x <= xh

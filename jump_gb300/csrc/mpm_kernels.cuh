@@ -463,10 +463,15 @@ __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt,
     for (int a = 0; a < D; ++a) {
       nd.vdt[a * Nn + i] = 0.0;
       nd.dv[a * Nn + i] = 0.0;
-      if (F32COPY) {
+      if (F32COPY && !nd.nf4) {
         nd.vdt_f[a * Nn + i] = 0.f;
         nd.dv_f[a * Nn + i] = 0.f;
       }
+    }
+    if (F32COPY && nd.nf4) {
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      nd.nf4[(D == 2 ? 1 : 2) * i] = z;
+      if (D == 3) nd.nf4[2 * i + 1] = z;
     }
     return;
   }
@@ -493,9 +498,17 @@ __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt,
   for (int a = 0; a < D; ++a) {
     nd.vdt[a * Nn + i] = vdt[a];
     nd.dv[a * Nn + i] = dv[a];
-    if (F32COPY) {
+    if (F32COPY && !nd.nf4) {
       nd.vdt_f[a * Nn + i] = float(vdt[a]);
       nd.dv_f[a * Nn + i] = float(dv[a]);
+    }
+  }
+  if (F32COPY && nd.nf4) {
+    if (D == 2) {
+      nd.nf4[i] = make_float4(float(vdt[0]), float(vdt[1]), float(dv[0]), float(dv[D - 1]));
+    } else {
+      nd.nf4[2 * i] = make_float4(float(vdt[0]), float(vdt[1]), float(vdt[D - 1]), 0.f);
+      nd.nf4[2 * i + 1] = make_float4(float(dv[0]), float(dv[1]), float(dv[D - 1]), 0.f);
     }
   }
 }
@@ -942,7 +955,57 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
   const R* vdt_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.vdt) : reinterpret_cast<const R*>(nd.vdt_f);
   const R* dv_n = sizeof(R) == 8 ? reinterpret_cast<const R*>(nd.dv) : reinterpret_cast<const R*>(nd.dv_f);
   const int64_t Nn = nd.nodeCount;
-  if constexpr (D == 3) {
+  if (sizeof(R) == 4 && !CG && nd.nf4) {
+    // FP32 particles, interleaved node records: all corner loads issued first
+    // (two 16-byte loads per corner in 3D, one in 2D), then the same sums
+    constexpr int NC = 1 << D;
+    float4 rv[NC], rd[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      if (D == 3) {
+        rv[k] = __ldg(nd.nf4 + 2 * cr.node[k]);
+        rd[k] = __ldg(nd.nf4 + 2 * cr.node[k] + 1);
+      } else {
+        rv[k] = __ldg(nd.nf4 + cr.node[k]);
+      }
+    }
+    if constexpr (D == 3) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int bx = q & 1, by = q >> 1;
+        const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
+        const R Gx = bx ? h.gh[0] : h.gl[0], Gy = by ? h.gh[1] : h.gl[1];
+        const R Nxy = Nx * Ny, GxNy = Gx * Ny, NxGy = Nx * Gy;
+        const float4 a0 = rv[q], a1 = rv[q + 4], b0 = rd[q], b1 = rd[q + 4];
+        const R vd0[3] = {R(a0.x), R(a0.y), R(a0.z)}, vd1[3] = {R(a1.x), R(a1.y), R(a1.z)};
+        const R dv0[3] = {R(b0.x), R(b0.y), R(b0.z)}, dv1[3] = {R(b1.x), R(b1.y), R(b1.z)};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const R Z0 = h.Nl[2] * vd0[a] + h.Nh[2] * vd1[a];
+          const R Z1 = h.gl[2] * vd0[a] + h.gh[2] * vd1[a];
+          const R W = h.Nl[2] * dv0[a] + h.Nh[2] * dv1[a];
+          x[a] += Nxy * Z0;
+          v[a] += Nxy * W;
+          Ldt[a][0] += GxNy * Z0;
+          Ldt[a][1] += NxGy * Z0;
+          Ldt[a][2] += Nxy * Z1;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < NC; ++k) {
+        const R N = cr.N[k];
+        const R vd[2] = {R(rv[k].x), R(rv[k].y)}, dvv[2] = {R(rv[k].z), R(rv[k].w)};
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          v[a] += N * dvv[a];
+          x[a] += N * vd[a];
+#pragma unroll
+          for (int j = 0; j < D; ++j) Ldt[a][j] += vd[a] * cr.dN[k][j];
+        }
+      }
+    }
+  } else if constexpr (D == 3) {
     // factored along z: per (x, y) corner pair, Z0 = sum Nz vdt, Z1 = sum Gz vdt,
     // W = sum Nz dv over the two z corners, then x += Nx Ny Z0, v += Nx Ny W,
     // L dt += (Gx Ny Z0, Nx Gy Z0, Nx Ny Z1)
@@ -967,23 +1030,24 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
         Ldt[a][2] += Nxy * Z1;
       }
     }
-  }
+  } else {
 #pragma unroll
-  for (int k = 0; k < (D == 3 ? 0 : 1 << D); ++k) {
-    int64_t n = cr.node[k];
-    R N = cr.N[k];
-    R vd[D], dvv[D];
+    for (int k = 0; k < (1 << D); ++k) {
+      int64_t n = cr.node[k];
+      R N = cr.N[k];
+      R vd[D], dvv[D];
 #pragma unroll
-    for (int a = 0; a < D; ++a) {
-      vd[a] = nload<CG>(vdt_n + a * Nn + n);
-      dvv[a] = nload<CG>(dv_n + a * Nn + n);
-    }
+      for (int a = 0; a < D; ++a) {
+        vd[a] = nload<CG>(vdt_n + a * Nn + n);
+        dvv[a] = nload<CG>(dv_n + a * Nn + n);
+      }
 #pragma unroll
-    for (int a = 0; a < D; ++a) {
-      v[a] += N * dvv[a];
-      x[a] += N * vd[a];
+      for (int a = 0; a < D; ++a) {
+        v[a] += N * dvv[a];
+        x[a] += N * vd[a];
 #pragma unroll
-      for (int j = 0; j < D; ++j) Ldt[a][j] += vd[a] * cr.dN[k][j];
+        for (int j = 0; j < D; ++j) Ldt[a][j] += vd[a] * cr.dN[k][j];
+      }
     }
   }
 #pragma unroll

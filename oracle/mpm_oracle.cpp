@@ -4,10 +4,17 @@
 // against; it is never linked into, loaded by or called from the product
 // library.  Only tests/, the smoke check and bench.py's CPU-baseline leg use it.
 //
-// PARITY STATUS: unpinned.  The reference is Julia and cannot run in this
-// environment (no Julia toolchain), and it ships no golden vectors or tests.
-// This restatement is cross-checked against an independent pure-Python
-// restatement (tests/golden/make_golden.py) and against closed-form cases.
+// PARITY STATUS: not pinned to reference outputs.  The reference is Julia and
+// cannot run in this environment (no Julia toolchain), and it ships no golden
+// vectors or tests.  This restatement is checked against an independent
+// pure-Python restatement (tests/golden/make_golden.py, bit for bit) and against
+// known answers that come from no restatement (tests/test_oracle_pins.py): the
+// hat basis's partition of unity, zero gradient sum, linear reproduction and
+// sign(0) gradient on node lines; B-spline partition of unity; elastic,
+// neo-Hookean (uniaxial stretch) and J2 (monotonic shear, linear hardening)
+// closed forms of one material point; mass and momentum conservation on the
+// free two-disk collision; second-order convergence of a standing-wave
+// manufactured solution.
 //
 // It follows the reference loops statement by statement, in the same loop and
 // summation order (solids, then particles, then the nodes of a particle in

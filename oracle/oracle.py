@@ -4,8 +4,10 @@ dual-number restatement for gradients (oracle/mpm_dual.cpp).
 TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and bench.py's
 CPU-baseline leg, never by the jump_gb300 package.  It consumes the same
 descriptors as the CUDA library (jump_gb300.engine.Descriptors) so both run
-on identical inputs.  Parity status: unpinned (the Julia reference cannot
-run here and ships no golden data).
+on identical inputs.  Parity status: not pinned to reference outputs (the
+Julia reference cannot run here and ships no golden data); pinned instead by
+known answers (tests/test_oracle_pins.py) and by an independent Python
+restatement (tests/golden/).
 """
 from __future__ import annotations
 

@@ -176,28 +176,87 @@ def test_checkpointed_forward_is_the_forward():
     assert np.max(np.abs(final_positions(a) - xa)) == 0.0  # context left at the final state
 
 
-def test_inverse_problem_reduces_loss():
-    """Recover a stiffness field from final tip displacements: a few scaled
-    gradient steps on log E reduce the misfit."""
-    problem, E_true, v0, tip = setup_case(2)
+def _segments_case():
+    problem, _, v0, _ = setup_case(2)
+    x0 = np.concatenate([s.pos for s in problem[1]])
+    xs = x0[:, 0] / x0[:, 0].max()
+    return problem, v0, xs
+
+
+def test_inverse_problem_recovers_stiffness_segments():
+    """Recover the Young's moduli of four segments of the cantilever (the
+    particles' E piecewise constant along x) from the final positions of all
+    particles: L-BFGS on the log moduli, each gradient the sum of the adjoint's
+    per-particle dL/dE over a segment.  From a uniform start 30-60% off, every
+    segment's modulus comes back within the stated tolerance."""
+    opt = pytest.importorskip("scipy.optimize")
+    problem, v0, xs = _segments_case()
+    nseg = 4
+    seg = np.minimum((xs * nseg).astype(int), nseg - 1)
+    E_true_seg = 1e6 * np.array([1.6, 0.7, 1.3, 0.9])
+    ctx = make_context(problem, E_true_seg[seg], v0)
+    ctx.step(NSTEPS)
+    target = final_positions(ctx)
+    ctx.close()
+    scale = 1e6
+
+    def f(a):
+        E = np.exp(a)[seg]
+        x, g = rollout_grad(problem, E, v0, NSTEPS, EVERY, lambda x: 2.0 * (x - target))
+        L = float(np.sum((x - target) ** 2))
+        ga = np.array([np.sum(g["E"][seg == k] * E[seg == k]) for k in range(nseg)])
+        return L * scale, ga * scale
+
+    a0 = np.full(nseg, np.log(1e6))
+    L0 = f(a0)[0]
+    res = opt.minimize(f, a0, jac=True, method="L-BFGS-B", options={"maxiter": 60, "ftol": 1e-16, "gtol": 1e-14})
+    err = np.abs(np.exp(res.x) / E_true_seg - 1)
+    print("\nstiffness segments", np.exp(res.x) / E_true_seg, "misfit", L0, "->", res.fun, "iterations", res.nit)
+    assert res.fun <= 1e-6 * L0, (L0, res.fun)
+    assert np.max(err) <= 0.01, err
+
+
+def test_inverse_problem_per_particle_stiffness_error_falls():
+    """Per-particle Young's modulus (a smooth field along x) from the final
+    positions of all particles, by scaled gradient steps on log E with a
+    backtracking step length: the misfit falls 100x and the RMS error of log E
+    falls by a quarter (the field is only partly identifiable: particles near
+    the free end carry little stress)."""
+    problem, v0, xs = _segments_case()
+    E_true = 1e6 * np.exp(0.4 * np.sin(2 * np.pi * xs))
     ctx = make_context(problem, E_true, v0)
     ctx.step(NSTEPS)
-    target = final_positions(ctx)[tip]
+    target = final_positions(ctx)
     ctx.close()
-    E = np.full_like(E_true, np.exp(np.mean(np.log(E_true))) * 0.7)
 
-    def loss_grad(x):
-        g = np.zeros_like(x)
-        g[tip] = 2.0 * (x[tip] - target)
-        return g
+    def misfit(E):
+        c = make_context(problem, E, v0)
+        c.step(NSTEPS)
+        x = final_positions(c)
+        c.close()
+        return float(np.sum((x - target) ** 2))
 
-    losses = []
-    for _ in range(6):
-        x, g = rollout_grad(problem, E, v0, NSTEPS, EVERY, loss_grad)
-        losses.append(float(np.sum((x[tip] - target) ** 2)))
-        gl = g["E"] * E  # gradient with respect to log E
-        E = E * np.exp(-0.3 * gl / (np.max(np.abs(gl)) + 1e-300))
-    assert losses[-1] < 0.5 * losses[0], losses
+    la = np.full(len(xs), np.log(1e6))
+    err0 = float(np.sqrt(np.mean((la - np.log(E_true)) ** 2)))
+    t, losses = None, []
+    for _ in range(30):
+        E = np.exp(la)
+        x, g = rollout_grad(problem, E, v0, NSTEPS, EVERY, lambda x: 2.0 * (x - target))
+        L0 = float(np.sum((x - target) ** 2))
+        losses.append(L0)
+        gl = g["E"] * E  # dL/d log E
+        if t is None:
+            t = 0.1 / np.max(np.abs(gl))
+        for _ in range(30):
+            if misfit(np.exp(la - t * gl)) < L0:
+                break
+            t *= 0.5
+        la = la - t * gl
+        t *= 2.0
+    err1 = float(np.sqrt(np.mean((la - np.log(E_true)) ** 2)))
+    print("\nper-particle log-E error", err0, "->", err1, "misfit", losses[0], "->", losses[-1])
+    assert losses[-1] < 0.01 * losses[0], losses
+    assert err1 < 0.75 * err0, (err0, err1)
 
 
 def test_store_every_step_matches_checkpointing():
