@@ -284,7 +284,9 @@ int mpm_probe_rates(double* fp64_fma_per_s, double* fp64_div_per_s, double* fp64
  * final particle state with respect to the initial velocities and positions
  * and to a per-particle Young's modulus, through hand-written adjoint
  * kernels of every stage.  Built for FP64 contexts with one velocity field,
- * no sorting and neo-Hookean bodies; otherwise MPM_ERR_UNSUPPORTED.
+ * no sorting and neo-Hookean, linear elastic or J2 bodies; otherwise
+ * MPM_ERR_UNSUPPORTED.  The backward pass recomputes one checkpoint segment
+ * on the context's stream while it differentiates the next on a second one.
  * The derivative is that of the discrete map inside the particles' current
  * cells (the hat basis has kinks at nodes and cell faces).
  * ------------------------------------------------------------------------- */

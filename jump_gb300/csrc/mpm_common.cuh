@@ -69,7 +69,17 @@ struct MatParams {
   // Johnson-Cook with damage: thermal softening exponent, temperature rise per
   // unit plastic work chi/(density Cp), damage constants, Tm - Tr
   double m, delta, d1, d2, d3, d4, d5, depsdot0, Tr, Tm, Tmr;
+  // FP32 particles: lambda, mu, kappa, fy, k1 and rtmuk1 rounded to float once
+  // on the host (a per-particle conversion is FP64-pipe work)
+  float f_lambda, f_mu, f_kappa, f_fy, f_k1, f_rtmuk1;
 };
+
+// a material constant in the particle precision: the FP64 value, or its float copy
+template <class R>
+__device__ __forceinline__ R mat_const(double d, float f) {
+  if constexpr (sizeof(R) == 4) return f;
+  else return d;
+}
 
 // Grid description shared by all kernels.
 struct GridP {

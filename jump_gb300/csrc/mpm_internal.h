@@ -50,6 +50,12 @@ inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, 
     mp.Tmr = m.Tm - m.Tr;  // Material.jl:507
   }
   mp.dtime = dt;
+  mp.f_lambda = float(mp.lambda);
+  mp.f_mu = float(mp.mu);
+  mp.f_kappa = float(mp.kappa);
+  mp.f_fy = float(mp.fy);
+  mp.f_k1 = float(mp.k1);
+  mp.f_rtmuk1 = float(mp.rtmuk1);
   return mp;
 }
 

@@ -858,7 +858,8 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
       eps[c] = e;
       *field<R>(pp, L::EPS + c, p) = e;
     }
-  R lam = R(mp.lambda), mu = R(mp.mu), kappa = R(mp.kappa);
+  R lam = mat_const<R>(mp.lambda, mp.f_lambda), mu = mat_const<R>(mp.mu, mp.f_mu);
+  R kappa = mat_const<R>(mp.kappa, mp.f_kappa);
   if (mp.per_particle) {
     lam = *field<R>(pp, L::LAM, p);
     mu = *field<R>(pp, L::MU, p);
@@ -908,9 +909,11 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
     for (int c = 0; c < L::PS; ++c) ep[c] = *field<R>(pp, L::EP + c, p);
     R vm;
     if (D == 3)
-      j2_3d<R>(lam, mu, kappa, R(mp.fy), R(mp.k1), eps, sig, &alpha, ep, &vm, R(mp.rtmuk1));
+      j2_3d<R>(lam, mu, kappa, mat_const<R>(mp.fy, mp.f_fy), mat_const<R>(mp.k1, mp.f_k1), eps, sig, &alpha, ep,
+               &vm, mat_const<R>(mp.rtmuk1, mp.f_rtmuk1));
     else
-      j2_2d<R>(lam, mu, kappa, R(mp.fy), R(mp.k1), eps, sig, &alpha, ep, &vm);
+      j2_2d<R>(lam, mu, kappa, mat_const<R>(mp.fy, mp.f_fy), mat_const<R>(mp.k1, mp.f_k1), eps, sig, &alpha, ep,
+               &vm);
     *field<R>(pp, L::ALPHA, p) = alpha;
 #pragma unroll
     for (int c = 0; c < L::PS; ++c) *field<R>(pp, L::EP + c, p) = ep[c];
@@ -1061,8 +1064,12 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
   kinematics_stress<D, R, MAT>(pp, p, Ldt, mp, fin, status);
 }
 
+// FP32 particles: at most 48 registers (five 256-thread CTAs per SM); the
+// latency-bound FP32 G2P gains more from the extra resident warps than it
+// loses to 16-20 bytes of spills (43.0 -> 39.9 us on the Taylor bar).  The
+// FP64 kernel keeps its natural register count.
 template <int D, class R, int MAT>
-__global__ void __launch_bounds__(256) g2p_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, double dt,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 0) g2p_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, double dt,
                                                   unsigned* status) {
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t < pp.count) g2p_particle<D, R, MAT>(g, nd, pp, t, mp, dt, status);
