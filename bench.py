@@ -470,13 +470,15 @@ def run_ours(args):
         late = late_window(args, ctx, npart, args.warmup + args.steps + nprof)
     ctx.close()
 
-    # End to end through the public API.  The caller's particle arrays (inputs)
-    # and the arrays it downloads into (outputs) sit in pinned host memory
-    # before the clock starts, like a solver's own Solid arrays.  Timed: packing
-    # the descriptors, mpm_create (every host->device copy), K steps with the
-    # EnergiesFix sums of every step copied back to the host as they form
-    # (mpm_step_energies, the solver's path when no hook reads particle arrays),
-    # and the download of every field.
+    # End to end through the public API: one solve of max(K, --e2e-steps) steps
+    # from host arrays.  The caller's particle arrays (inputs) and the arrays it
+    # downloads into (outputs) sit in pinned host memory before the clock
+    # starts, like a solver's own Solid arrays.  Timed: packing the
+    # descriptors, mpm_create (every host->device copy), the steps with the
+    # EnergiesFix sums of every step (mpm_step_energies, the solver's path when
+    # no hook reads particle arrays: each step's record formed on the device,
+    # all of them copied to the host at the end of the call), and the download
+    # of every field.
     import copy
     from jump_gb300.engine import BodyState
     s_pin = pin_solids(copy.deepcopy(s))
@@ -490,9 +492,10 @@ def run_ours(args):
     c2 = MPMContext(desc)
     c2.set_launch(**launch)
     t1 = time.perf_counter()
-    recs, _ = c2.step_energies(args.steps, 1, 0)
+    e2e_steps = max(args.steps, args.e2e_steps)
+    recs, _ = c2.step_energies(e2e_steps, 1, 0)
     t2 = time.perf_counter()
-    assert recs.shape[0] == args.steps and np.all(np.isfinite(recs))
+    assert recs.shape[0] == e2e_steps and np.all(np.isfinite(recs))
     states = c2.download_all(out_states)
     e2e_wall = time.perf_counter() - e2e_ctx_t0
     parts = {"create_ms": 1e3 * (t1 - e2e_ctx_t0), "steps_ms": 1e3 * (t2 - t1),
@@ -501,7 +504,7 @@ def run_ours(args):
     h2d = sum(a.nbytes for a in desc._keep)
     d2h = sum(sum(getattr(stt, k).nbytes for k in stt.FIELDS) for stt in states)
     e2e_t = allreduce_max(dist, e2e_wall)
-    e2e_value = total_updates / e2e_t
+    e2e_value = allreduce_sum(dist, float(npart * e2e_steps)) / e2e_t
 
     extras = {}
     if world == 1 and args.extras and args.workload == "taylor_bar" and args.precision == "f64":
@@ -550,10 +553,12 @@ def run_ours(args):
                                                                else 0},
                          "step_frac": step_bytes / (t_max / args.steps) / 1e9 / peak, "fp64": fp64},
             "late_window": late,
-            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / args.steps,
-                    "d2h_bytes_per_step": d2h / args.steps + recs.itemsize * recs.shape[1], "host_memory": "pinned",
-                    "how": f"create from host arrays, {args.steps} steps each with its energies copied to the host "
-                           "(mpm_step_energies), download all",
+            "e2e": {"value": e2e_value, "unit": METRIC, "steps": e2e_steps,
+                    "h2d_bytes_per_step": h2d / e2e_steps,
+                    "d2h_bytes_per_step": d2h / e2e_steps + recs.itemsize * recs.shape[1], "host_memory": "pinned",
+                    "how": f"one solve: create from host arrays, {e2e_steps} steps each with its EnergiesFix record "
+                           "(mpm_step_energies: formed on the device, all records copied to the host at the end), "
+                           "download all",
                     **parts},
             "gpu_launches": launches_per_run(args, len(s)),
             "clocks": clocks,
@@ -713,7 +718,15 @@ def measure_adjoint(args, nsteps):
     tip-displacement loss against central differences on 32 random parameters
     (GPU forward runs)."""
     from jump_gb300 import scenarios
-    from jump_gb300.adjoint import final_positions, make_context
+    from jump_gb300.adjoint import final_positions
+    from jump_gb300.adjoint import make_context as _make
+
+    def make_context(*a):
+        c = _make(*a)
+        if args.adjoint_p2g is not None:  # a tile strategy selects the tiled adjoint scatter too
+            c.set_launch(p2g=args.adjoint_p2g)
+        return c
+
     problem = scenarios.cantilever()
     grid, solids, alg, data = problem
     scenarios.apply_dirichlet(grid, data)
@@ -789,6 +802,7 @@ def measure_adjoint(args, nsteps):
             "n_gpus": 1, "steps": nsteps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded per-particle E)",
             "config": {"workload": "cantilever_2d_neohookean_adjoint", "particles": npart,
+                       "p2g": args.adjoint_p2g or "atomic",
                        "checkpoint_every": every, "loss": "squared tip displacement error (top 5% in x)"},
             "forward_particle_updates_per_s": npart * nsteps / fwd,
             "fwd_adj_over_fwd_throughput": fwd / both,
@@ -917,6 +931,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--late-steps", type=int, default=1000,
                     help="Taylor bar: steps advanced before the late-window measurement (0: none)")
+    ap.add_argument("--adjoint-p2g", default=None, choices=["atomic", "warp", "tile", "tile_warp"],
+                    help="adjoint: P2G strategy of its contexts (a tile one selects the tiled adjoint scatter)")
+    ap.add_argument("--e2e-steps", type=int, default=1000,
+                    help="Taylor bar: steps of the end-to-end solve (at least --steps)")
     ap.add_argument("--extras", action=argparse.BooleanOptionalAction, default=True,
                     help="Taylor bar, FP64, 1 GPU: add the ensemble, adjoint and impact-jvp sub-results")
     args = ap.parse_args()

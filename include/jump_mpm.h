@@ -197,9 +197,9 @@ int mpm_step(mpm_ctx* ctx, int64_t nsteps, double* t_inout);
    ... < nsteps -- the hook schedule `counter % interval == 0` of
    SolveExplicitSolidMechanics2D.jl:574-578 when first = (-counter0) mod every.
    Record r goes to out[(2 + dim) r ...]: kinetic energy, strain energy, momentum
-   (dim).  Every record is copied to pinned host memory as soon as its sums are
-   formed, with no host synchronisation between steps; the call returns after
-   the last step, like mpm_step.  out may be any host memory
+   (dim).  Each record is formed on the device in its own slot, with no host
+   synchronisation between steps, and all of them are copied to the host in
+   one transfer after the last step; the call returns then, like mpm_step.  out may be any host memory
    ((nsteps - 1 - first)/every + 1 records when nsteps > first). */
 int mpm_step_energies(mpm_ctx* ctx, int64_t nsteps, int64_t every, int64_t first, double* t_inout, double* out);
 
@@ -239,8 +239,9 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
 /* Launch configuration and its autotuner (no counterpart in the reference).
    P2G strategy of the linear basis: every particle issues its own FP64 atomics
    (MPM_P2G_ATOMIC, the FP64 default), or lanes of a warp that share a base
-   node first add their values with a segmented shuffle reduction and one lane
-   per run issues them (MPM_P2G_WARP, the FP32 default); MPM_P2G_TILE and
+   node (the group __match_any_sync finds) first add their values with a
+   shuffle reduction and one lane per group issues them (MPM_P2G_WARP, the
+   FP32 default); MPM_P2G_TILE and
    MPM_P2G_TILE_WARP stage those two forms in a shared-memory tile of the node
    box a CTA's particles cover and issue one FP64 atomic per node value and CTA
    (a CTA whose box exceeds the tile, 256 nodes for CTAs of 64 threads, else
@@ -302,6 +303,9 @@ int mpm_fwd_checkpointed(mpm_ctx* ctx, int64_t nsteps, int32_t checkpoint_every)
                    all bodies in order, dim doubles per particle
      E_bar         out: dL/dE per particle (count doubles), or NULL
      v0_bar, x0_bar out: dL/dv, dL/dx at the initial step, or NULL
+   The G2P adjoint scatters its node adjoints with FP64 atomics per particle
+   at L2, or, when the context's P2G strategy is MPM_P2G_TILE or
+   MPM_P2G_TILE_WARP, through a shared-memory tile of each CTA's node box.
    The context is left at the final state of the forward run. */
 int mpm_bwd(mpm_ctx* ctx, const double* x_bar, const double* v_bar, double* E_bar, double* v0_bar,
             double* x0_bar);

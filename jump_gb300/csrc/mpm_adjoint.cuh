@@ -252,20 +252,16 @@ __device__ __forceinline__ void stress_adj(const double* eps, double lam, double
   lamb += kappab;
 }
 
-template <int D, int MAT>
-__global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, PartP pp, AdjP ad, NodeAdjP na,
-                                                      MatParams mp, double c1, double c2) {
+// G2P adjoint of particle p inside the grid (hat h): reads its adjoints,
+// writes x_, F_ (and the constitutive adjoints, with E_ += dL/dE), and hands
+// each corner k's node adjoints (vdt_ (D), dv_ (D)) to put(k, node, val).
+template <int D, int MAT, class Put>
+__device__ __forceinline__ void g2p_adj_particle(const GridP& gp, const GridRec& gr, const PartP& pp, const AdjP& ad,
+                                                 const NodeAdjP& na, const MatParams& mp, double c1, double c2,
+                                                 int64_t p, const Hat<D, double>& h, Put&& put) {
   using L = Layout<D>;
   using A = AdjLayout<D>;
-  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= pp.count) return;
-  const int64_t p = pp.begin + t;
   const double* P = static_cast<const double*>(pp.base);
-  double x[D];
-#pragma unroll
-  for (int a = 0; a < D; ++a) x[a] = P[int64_t(L::X + a) * pp.pitch + p];
-  Hat<D, double> h;
-  if (!hat<D, double>(gp, x, h)) return;  // frozen particle: its adjoints pass through unchanged
   CornersFull<D> c;
   corners_full<D>(gp, h, c);
   const int64_t Nn = na.nodeCount;
@@ -380,21 +376,105 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, Part
       for (int a = 0; a < D; ++a) s += Ab[a][b] * vdt[k][a];
       gb[b] = s;
     }
-    const int64_t n = c.node[k];
+    double val[2 * D];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       double s = c.N[k] * xb[a];
 #pragma unroll
       for (int b = 0; b < D; ++b) s += Ab[a][b] * c.g[k][b];
-      atomicAdd(na.vdtb + a * Nn + n, s);
-      atomicAdd(na.dvb + a * Nn + n, c.N[k] * vb[a]);
+      val[a] = s;
+      val[D + a] = c.N[k] * vb[a];
     }
+    put(k, c.node[k], val);
     add_shape_adj<D>(xn, c, k, wb, gb);
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) *adj<D>(ad, A::XB + a, p) = xn[a];
 #pragma unroll
   for (int q = 0; q < D * D; ++q) *adj<D>(ad, A::FB + q, p) = Fn[q];
+}
+
+
+// The G2P adjoint.  Its scatter of the node adjoints vdt_ and dv_:
+// TILE = false: FP64 atomics per particle, corner and value at L2;
+// TILE = true: staged in a shared-memory tile of the node box the CTA's
+//   particles cover (the box as in the P2G tile kernel): shared FP64 atomics
+//   per particle and corner, then one global atomic per non-zero node value and
+//   CTA; a CTA whose box holds more than cap nodes adds per particle to global
+//   memory.  Dynamic shared memory: cap * 2D doubles.
+// blockDim.x is a multiple of 32 and at most 256.
+template <int D, int MAT, bool TILE>
+__global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, PartP pp, AdjP ad, NodeAdjP na,
+                                                      MatParams mp, double c1, double c2, int cap) {
+  using L = Layout<D>;
+  constexpr int NV = 2 * D;
+  extern __shared__ double tile[];
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t p = pp.begin + t;
+  const int64_t Nn = na.nodeCount;
+  if constexpr (!TILE) {
+    if (t >= pp.count) return;
+    double x[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) x[a] = static_cast<const double*>(pp.base)[int64_t(L::X + a) * pp.pitch + p];
+    Hat<D, double> h;
+    if (!hat<D, double>(gp, x, h)) return;  // frozen particle: its adjoints pass through unchanged
+    g2p_adj_particle<D, MAT>(gp, gr, pp, ad, na, mp, c1, c2, p, h, [&](int, int64_t n, const double* val) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        atomicAdd(na.vdtb + a * Nn + n, val[a]);
+        atomicAdd(na.dvb + a * Nn + n, val[D + a]);
+      }
+    });
+    return;
+  }
+  Hat<D, double> h{};
+  bool ok = false;  // false: outside the grid, a frozen particle whose adjoints pass through unchanged
+  if (t < pp.count) {
+    double x[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) x[a] = static_cast<const double*>(pp.base)[int64_t(L::X + a) * pp.pitch + p];
+    ok = hat<D, double>(gp, x, h);
+  }
+  int lo[3], hi[3];
+  cta_cell_box<D>(ok, h.c, lo, hi);
+  if (lo[0] > hi[0]) return;  // uniform
+  const int e0 = hi[0] - lo[0] + 2, e1 = hi[1] - lo[1] + 2, e2 = D == 3 ? hi[2] - lo[2] + 2 : 1;
+  const int64_t vol64 = int64_t(e0) * e1 * e2;
+  const bool use = vol64 <= int64_t(cap);  // uniform
+  const int vol = use ? int(vol64) : 0;
+  if (use) {
+    for (int i = threadIdx.x; i < vol * NV; i += blockDim.x) tile[i] = 0.0;
+    __syncthreads();
+  }
+  if (ok) {
+    const int lbase = use ? (h.c[0] - lo[0]) + e0 * ((h.c[1] - lo[1]) + (D == 3 ? e1 * (h.c[D - 1] - lo[D - 1]) : 0)) : 0;
+    g2p_adj_particle<D, MAT>(gp, gr, pp, ad, na, mp, c1, c2, p, h, [&](int k, int64_t n, const double* val) {
+      if (use) {
+        // lo <= c <= hi per axis, so 0 <= l < vol
+        const int l = lbase + (k & 1) + e0 * ((k >> 1) & 1) + (D == 3 ? e0 * e1 * (k >> 2) : 0);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) atomicAdd(tile + q * vol + l, val[q]);
+      } else {
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          atomicAdd(na.vdtb + a * Nn + n, val[a]);
+          atomicAdd(na.dvb + a * Nn + n, val[D + a]);
+        }
+      }
+    });
+  }
+  if (!use) return;  // uniform
+  __syncthreads();
+  for (int l = threadIdx.x; l < vol; l += blockDim.x) {
+    const int ix = l % e0, iy = (l / e0) % e1, iz = l / (e0 * e1);
+    const int64_t n = int64_t(lo[0] + ix) + gp.nx * int64_t(lo[1] + iy) + (D == 3 ? gp.nxy * int64_t(lo[2] + iz) : 0);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const double v = tile[q * vol + l];
+      if (v != 0.0) atomicAdd((q < D ? na.vdtb + q * Nn : na.dvb + (q - D) * Nn) + n, v);
+    }
+  }
 }
 
 template <int D>

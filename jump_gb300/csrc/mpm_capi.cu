@@ -118,7 +118,8 @@ struct mpm_ctx {
   int p2g_strategy = MPM_P2G_ATOMIC;  // linear-basis USL P2G (mpm_set_launch)
   int threads = 256;                  // CTA size of the linear-basis P2G and G2P
   double* rec_host = nullptr;   // pinned EnergiesFix records of mpm_step_energies
-  int64_t rec_cap = 0;          // records it holds
+  double* rec_dev = nullptr;    // the same records as the steps form them, on the device
+  int64_t rec_cap = 0;          // records each holds
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   // reverse mode: the second stream the reverse sweep runs on while the first
@@ -183,6 +184,7 @@ void drop_seg_graphs(mpm_ctx* c) {
 void destroy_ctx(mpm_ctx* c) {
   if (!c) return;
   cudaFreeHost(c->rec_host);
+  cudaFree(c->rec_dev);
   for (int i = 0; i < 2; ++i) {
     if (c->exec[i]) cudaGraphExecDestroy(c->exec[i]);
     if (c->graph[i]) cudaGraphDestroy(c->graph[i]);
@@ -682,7 +684,9 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   CUDA_TRY(cudaMalloc(&c->staging, c->staging_n * sizeof(double)));
   CUDA_TRY(cudaMalloc(&c->status, sizeof(unsigned)));
   CUDA_TRY(cudaMemset(c->status, 0, sizeof(unsigned)));
-  CUDA_TRY(cudaMalloc(&c->partial, size_t(kEnergyBlocks) * 5 * sizeof(double)));
+  // the energies' partial sums and, after them, the zeroed ticket of their fold
+  CUDA_TRY(cudaMalloc(&c->partial, (size_t(kEnergyBlocks) * 5 + 1) * sizeof(double)));
+  CUDA_TRY(cudaMemsetAsync(c->partial + size_t(kEnergyBlocks) * 5, 0, sizeof(double), c->stream));
   CUDA_TRY(cudaMalloc(&c->red, 8 * sizeof(double)));
 
   const FieldIdx& fi = c->fi;
@@ -867,9 +871,12 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
   if (nrec > c->rec_cap) {
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     CUDA_TRY(cudaFreeHost(c->rec_host));
+    CUDA_TRY(cudaFree(c->rec_dev));
     c->rec_host = nullptr;
+    c->rec_dev = nullptr;
     c->rec_cap = 0;
     CUDA_TRY(cudaHostAlloc(&c->rec_host, size_t(nrec) * (2 + D) * sizeof(double), cudaHostAllocDefault));
+    CUDA_TRY(cudaMalloc(&c->rec_dev, size_t(nrec) * (2 + D) * sizeof(double)));
     c->rec_cap = nrec;
   }
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
@@ -880,18 +887,22 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
     if ((r = launch_one_step(c))) return r;
     if (t_inout) *t_inout += c->prm.dt;
     if (k >= first && (k - first) % every == 0) {
-      double* dst = c->rec_host + size_t(j) * (2 + D);
+      // the record is formed on the device, in its slot; all records cross to
+      // the host in one copy after the steps
+      double* dst = c->rec_dev + size_t(j) * (2 + D);
       if (c->np > 0) {
-        if (D == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, c->red);
-        else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, c->red);
+        if (D == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, dst);
+        else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, dst);
         CUDA_TRY(cudaGetLastError());
-        CUDA_TRY(cudaMemcpyAsync(dst, c->red, (2 + D) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
       } else {
-        for (int q = 0; q < 2 + D; ++q) dst[q] = 0.0;
+        CUDA_TRY(cudaMemsetAsync(dst, 0, (2 + D) * sizeof(double), c->stream));
       }
       ++j;
     }
   }
+  if (nrec > 0)
+    CUDA_TRY(cudaMemcpyAsync(c->rec_host, c->rec_dev, size_t(nrec) * (2 + D) * sizeof(double),
+                             cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaEventRecord(c->e1, c->stream));
   unsigned st = 0;
   CUDA_TRY(cudaMemcpyAsync(&st, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
@@ -1345,6 +1356,8 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
   na.fb = c->nodeadj + Nn * (1 + 3 * D);
   const int64_t nseg = c->ckpt_slots - 1;
   void* Pwork = c->P;
+  // a tile P2G strategy selects the G2P adjoint's tiled scatter too
+  const bool adj_tile = c->p2g_strategy == MPM_P2G_TILE || c->p2g_strategy == MPM_P2G_TILE_WARP;
   CUDA_TRY(cudaMemsetAsync(c->nodeadj, 0, size_t(Nn) * 2 * D * sizeof(double), c->stream));
   // Segment buffer X (0, 1) holds `every` particle states and node records.
   // Recompute: `len` steps from the state in P, recording each step's particle
@@ -1368,8 +1381,8 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
         const PartP ps{seg_state(X, j), c->np, c->off[b], c->cnt[b]};
         const double nu = c->nus[b];
         const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);  // dlambda/dE, dmu/dE
-        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
-        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
+        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
+        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
       }
       if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
       else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
@@ -1421,8 +1434,8 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
         const PartP ps{state, c->np, c->off[b], c->cnt[b]};
         const double nu = c->nus[b];
         const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
-        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
-        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2);
+        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
+        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
       }
       if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
       else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);

@@ -7,6 +7,7 @@
 // grid (nodeCount = nx*ny*nz, node index i + nx*j + nx*ny*k, 0-based).
 #pragma once
 
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -360,6 +361,38 @@ __device__ __forceinline__ void corner_nodes(const GridP& g, const Hat<D, R>& h,
   for (int k = 0; k < (1 << D); ++k) {
     const int bx = k & 1, by = (k >> 1) & 1, bz = (k >> 2) & 1;
     cr.node[k] = base + bx + g.nx * by + (D == 3 ? g.nxy * bz : 0);
+  }
+}
+
+// The box [lo, hi] (per axis) of the base cells of the CTA's lanes with ok,
+// for the shared-memory node tiles of the P2G and of the G2P adjoint: a
+// reduction per warp, then over the CTA's warps.  Every thread of the CTA
+// calls it once per launch (it synchronises the CTA); lo[0] > hi[0] when no
+// lane has ok; axis 2 stays [0, 0] in 2D.  blockDim.x is a multiple of 32 and
+// at most 256.
+template <int D>
+__device__ __forceinline__ void cta_cell_box(bool ok, const int* c, int (&lo)[3], int (&hi)[3]) {
+  __shared__ int wlo[8][3], whi[8][3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const int wl = __reduce_min_sync(0xffffffffu, ok ? c[a] : INT_MAX);
+    const int wh = __reduce_max_sync(0xffffffffu, ok ? c[a] : INT_MIN);
+    if (lane == 0) {
+      wlo[warp][a] = wl;
+      whi[warp][a] = wh;
+    }
+  }
+  __syncthreads();
+  lo[2] = hi[2] = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    lo[a] = INT_MAX;
+    hi[a] = INT_MIN;
+    for (int w = 0; w < nwarps; ++w) {
+      lo[a] = min(lo[a], wlo[w][a]);
+      hi[a] = max(hi[a], whi[w][a]);
+    }
   }
 }
 

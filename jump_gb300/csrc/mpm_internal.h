@@ -114,8 +114,10 @@ struct Launchers {
   static void clear(cudaStream_t s, const NodeP& nd);
   // adjoint of one step (mpm_adjoint.cuh), FP64 particles; mp.type selects the
   // material (neo-Hookean, linear elastic, J2); c1, c2 = dlambda/dE, dmu/dE
+  // tile: the node adjoints scattered through a shared-memory node tile (the
+  // contexts whose P2G strategy is a tile one), else per particle at L2
   static void g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, const PartP& pp, const AdjP& ad,
-                      const NodeAdjP& na, const MatParams& mp, double c1, double c2);
+                      const NodeAdjP& na, const MatParams& mp, double c1, double c2, bool tile);
   static void grid_adj(cudaStream_t s, const GridRec& gr, const NodeAdjP& na, const uint8_t* fixed, double dt,
                        double tol);
   static void p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, const AdjP& ad, const NodeAdjP& na,
@@ -125,6 +127,9 @@ struct Launchers {
                            bool f32copy);
   static void g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
                   const MatParams& mp, double dt, unsigned* status, int threads = 0);
+  // EnergiesFix sums into out[0 .. 2 + D): partial holds nblocks x 5 doubles
+  // and one more slot, the fold's ticket, zero before the first launch (each
+  // launch leaves it zero)
   static void energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,
                        double* out);
   static void aos_to_soa(cudaStream_t s, const PartP& pp, bool f32, const double* src, int per, int f0,

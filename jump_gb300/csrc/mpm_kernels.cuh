@@ -30,8 +30,8 @@ __device__ __forceinline__ R* field(const PartP& pp, int f, int64_t p) {
 // of the stencil flagged.  All lanes in `mask` call it together with t
 // consecutive across the warp; lanes with ok == false add nothing.
 // WARP_SUM: lanes with the same base node first add their values by a
-// segmented shuffle reduction and only the run's first lane calls put;
-// otherwise every lane with ok calls put.
+// shuffle reduction over the group __match_any_sync finds, and only the
+// group's lowest lane calls put; otherwise every lane with ok calls put.
 template <int D, class R, bool GRAV, bool WARP_SUM, class Put>
 __device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& nd, const PartP& pp, int64_t p,
                                                   bool ok, const Hat<D, R>& h, unsigned mask, double gx,
@@ -56,33 +56,46 @@ __device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& n
     mg[1] = m * R(gy);
     if (D == 3) mg[2] = m * R(gz);
   }
-  // WARP_SUM: lanes with the same base node (runs of consecutive lanes, long
-  // after the cell sort) add their contributions with a segmented shuffle
-  // reduction, and only the run's first lane issues them.
+  // WARP_SUM: the lanes with the same base node, wherever they sit in the warp
+  // (__match_any_sync), add their contributions by a tree reduction over the
+  // group's members in lane order, and only the group's lowest lane issues
+  // them.  At level l the member of group rank r (r a multiple of 2^(l+1))
+  // adds the partial sum held by the member of rank r + 2^l, whose lane is
+  // src[l]; take bit l says whether this lane has such a partner.
   const int lane = threadIdx.x & 31;
   bool head = true;
-  int end = lane + 1, levels = 0;
+  int levels = 0, src[5];
+  unsigned take = 0;
   if (WARP_SUM) {
     long long key = ok ? (long long)(int64_t(h.c[0]) + g.nx * int64_t(h.c[1]) + (D == 3 ? g.nxy * int64_t(h.c[D - 1]) : 0))
                        : -1ll - lane;
-    long long kprev = __shfl_up_sync(mask, key, 1);
-    head = lane == 0 || kprev != key;
-    unsigned heads = __ballot_sync(mask, head);
-    unsigned later = heads & ~((2u << lane) - 1u);
-    end = later ? __ffs(later) - 1 : 32 - __clz(mask);
-    unsigned run = __reduce_max_sync(mask, head ? unsigned(end - lane) : 0u);
-    while ((1u << levels) < run) ++levels;
+    const unsigned grp = __match_any_sync(mask, key);
+    const int r = __popc(grp & ((1u << lane) - 1u));  // rank in the group
+    head = r == 0;
+    const unsigned nmax = __reduce_max_sync(mask, unsigned(__popc(grp)));
+    while ((1u << levels) < nmax) ++levels;
+    unsigned after = grp & ~((2u << lane) - 1u);  // members of higher rank, lowest bit = rank r + 1
+#pragma unroll
+    for (int l = 0; l < 5; ++l) {
+      src[l] = after ? __ffs(after) - 1 : lane;
+      if (after && (r & ((2 << l) - 1)) == 0) take |= 1u << l;
+      if (l < 4) {  // drop 2^l members: the lowest bit becomes rank r + 2^(l+1)
+#pragma unroll
+        for (int s = 0; s < (1 << l); ++s) after &= after - 1u;
+      }
+    }
   }
   auto emit = [&](int k, R* val) {
     if (WARP_SUM) {
       const int nv = NRM ? NV : 1 + 2 * D;
-      for (int l = 0; l < levels; ++l) {
-        const int off = 1 << l;
+#pragma unroll
+      for (int l = 0; l < 5; ++l) {
+        if (l >= levels) break;
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
           if (q >= nv) break;
-          R o = __shfl_down_sync(mask, val[q], off);
-          if (lane + off < end) val[q] += o;
+          R o = __shfl_sync(mask, val[q], src[l]);
+          if ((take >> l) & 1u) val[q] += o;
         }
       }
     }
@@ -183,7 +196,7 @@ __device__ __forceinline__ int64_t corner_node(const GridP& g, int64_t base, int
 }
 
 // P2G of particle pp.begin + t with FP64 atomics at L2: one per lane and node
-// value (MPM_P2G_ATOMIC) or one per run of lanes sharing a base node
+// value (MPM_P2G_ATOMIC) or one per group of lanes sharing a base node
 // (WARP_SUM, MPM_P2G_WARP).  All 32 lanes of a warp call it together
 // (t consecutive across the warp); lanes with t >= pp.count do nothing.
 template <int D, class R, bool GRAV, bool WARP_SUM = (sizeof(R) == 4)>
@@ -236,7 +249,6 @@ __global__ void __launch_bounds__(256) p2g_tile_kernel(GridP g, NodeP nd, PartP 
                                                        double gz, unsigned* status, int cap) {
   using L = Layout<D>;
   extern __shared__ double tile[];
-  __shared__ int wlo[8][3], whi[8][3];
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t p = pp.begin + t;
   Hat<D, R> h{};
@@ -249,28 +261,8 @@ __global__ void __launch_bounds__(256) p2g_tile_kernel(GridP g, NodeP nd, PartP 
     hat_put<D, R>(pp, p, ok, h);
     if (!ok) atomicOr(status, ST_OUT_OF_GRID);
   }
-  // the box of base cells, per warp then over the CTA
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    const int wl = __reduce_min_sync(0xffffffffu, ok ? h.c[a] : INT_MAX);
-    const int wh = __reduce_max_sync(0xffffffffu, ok ? h.c[a] : INT_MIN);
-    if (lane == 0) {
-      wlo[warp][a] = wl;
-      whi[warp][a] = wh;
-    }
-  }
-  __syncthreads();
-  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // axis 2 stays 0 in 2D
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    lo[a] = INT_MAX;
-    hi[a] = INT_MIN;
-    for (int w = 0; w < nwarps; ++w) {
-      lo[a] = min(lo[a], wlo[w][a]);
-      hi[a] = max(hi[a], whi[w][a]);
-    }
-  }
+  int lo[3], hi[3];
+  cta_cell_box<D>(ok, h.c, lo, hi);
   if (lo[0] > hi[0]) return;  // no particle of this CTA inside the grid (uniform)
   const int e0 = hi[0] - lo[0] + 2, e1 = hi[1] - lo[1] + 2, e2 = D == 3 ? hi[2] - lo[2] + 2 : 1;
   // box volume in 64 bits: a spread-out CTA can cover most of a large grid
@@ -1109,10 +1101,16 @@ __global__ void __launch_bounds__(256) rigid_kernel(GridP g, NodeP nd, PartP pp,
 }
 
 // ---------------------------------------------------------------------------
-// EnergiesFix sums: per-block partials [KE, SE, P_0..P_{D-1}], then one block
-// folds the partials in a fixed order (deterministic).
+// EnergiesFix sums (Fix.jl:248-270): kinetic energy, strain energy and
+// momentum (D) over the particles, in one launch.  Each CTA writes its sums
+// to partial[block]; the CTA that finishes last (a ticket counter after a
+// fence) folds the partials into out in a fixed order -- lane l of its first
+// warp adds blocks l, l + 32, ..., then a fixed shuffle tree -- so the result
+// does not depend on which CTA finishes last, and resets the ticket to zero
+// for the next launch.  The 1/2 factors are applied once to the folded sums
+// (a power-of-two scaling, exact).
 template <int D, class R>
-__global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial) {
+__global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial, unsigned* ticket, double* out) {
   using L = Layout<D>;
   constexpr int NQ = 2 + D;
   double q[NQ];
@@ -1129,18 +1127,19 @@ __global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial
       v[a] = *field<R>(pp, L::V + a, p);
       vv += v[a] * v[a];
     }
-    q[0] += 0.5 * m * vv;
+    q[0] += m * vv;
     double se = 0.0;
 #pragma unroll
     for (int c = 0; c < L::S; ++c) {
       double w = (c < D) ? 1.0 : 2.0;  // off-diagonal entries appear twice in sigma:eps
       se += w * double(*field<R>(pp, L::SIG + c, p)) * double(*field<R>(pp, L::EPS + c, p));
     }
-    q[1] += 0.5 * double(*field<R>(pp, L::VOL, p)) * se;
+    q[1] += double(*field<R>(pp, L::VOL, p)) * se;
 #pragma unroll
     for (int a = 0; a < D; ++a) q[2 + a] += m * v[a];
   }
   __shared__ double sh[NQ][256];
+  __shared__ bool last;
 #pragma unroll
   for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] = q[k];
   __syncthreads();
@@ -1150,28 +1149,32 @@ __global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial
       for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NQ; ++k) partial[int64_t(blockIdx.x) * NQ + k] = sh[k][0];
-}
-
-template <int NQ>
-__global__ void fold_kernel(const double* partial, int nblocks, double* out) {
-  // one warp: lane l sums blocks l, l+32, ... then a fixed shuffle tree, so the
-  // result does not depend on timing
-  int lane = threadIdx.x;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x >= 32) return;
+  __threadfence();
+  const int lane = threadIdx.x;
   double acc[NQ];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) acc[k] = 0.0;
-  for (int b = lane; b < nblocks; b += 32)
+  for (int b = lane; b < int(gridDim.x); b += 32)
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) acc[k] += partial[int64_t(b) * NQ + k];
+    for (int k = 0; k < NQ; ++k) acc[k] += __ldcg(partial + int64_t(b) * NQ + k);
 #pragma unroll
   for (int k = 0; k < NQ; ++k)
     for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
-  if (lane == 0)
+  if (lane == 0) {
+    out[0] = 0.5 * acc[0];
+    out[1] = 0.5 * acc[1];
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) out[k] = acc[k];
+    for (int k = 2; k < NQ; ++k) out[k] = acc[k];
+    *ticket = 0u;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -90,16 +90,22 @@ void Launchers<D>::contact_grid(cudaStream_t s, const NodeP& nd, const ContactP&
 
 template <int D>
 void Launchers<D>::g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, const PartP& pp, const AdjP& ad,
-                           const NodeAdjP& na, const MatParams& mp, double c1, double c2) {
+                           const NodeAdjP& na, const MatParams& mp, double c1, double c2, bool tile) {
   if (pp.count <= 0) return;
   const int th = spread_threads(pp.count);
   const unsigned nb = blocks_for(pp.count, th);
-  if (mp.type == MPM_MAT_ELASTIC)
-    g2p_adj_kernel<D, MPM_MAT_ELASTIC><<<nb, th, 0, s>>>(g, gr, pp, ad, na, mp, c1, c2);
-  else if (mp.type == MPM_MAT_J2)
-    g2p_adj_kernel<D, MPM_MAT_J2><<<nb, th, 0, s>>>(g, gr, pp, ad, na, mp, c1, c2);
-  else
-    g2p_adj_kernel<D, MPM_MAT_NEOHOOKEAN><<<nb, th, 0, s>>>(g, gr, pp, ad, na, mp, c1, c2);
+  // node tile of the scatter: at most 512 nodes x 2D doubles (24 KB in 3D)
+  const int cap = tile ? (th <= 64 ? 256 : 512) : 0;
+  const size_t smem = size_t(cap) * 2 * D * sizeof(double);
+#define JMPM_G2PA(MAT)                                                                       \
+  do {                                                                                       \
+    if (tile) g2p_adj_kernel<D, MAT, true><<<nb, th, smem, s>>>(g, gr, pp, ad, na, mp, c1, c2, cap); \
+    else g2p_adj_kernel<D, MAT, false><<<nb, th, 0, s>>>(g, gr, pp, ad, na, mp, c1, c2, 0);         \
+  } while (0)
+  if (mp.type == MPM_MAT_ELASTIC) JMPM_G2PA(MPM_MAT_ELASTIC);
+  else if (mp.type == MPM_MAT_J2) JMPM_G2PA(MPM_MAT_J2);
+  else JMPM_G2PA(MPM_MAT_NEOHOOKEAN);
+#undef JMPM_G2PA
 }
 
 template <int D>
@@ -308,9 +314,10 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
 template <int D>
 void Launchers<D>::energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,
                             double* out) {
-  if (f32) energies_kernel<D, float><<<nblocks, 256, 0, s>>>(pp, partial);
-  else energies_kernel<D, double><<<nblocks, 256, 0, s>>>(pp, partial);
-  fold_kernel<2 + D><<<1, 32, 0, s>>>(partial, nblocks, out);
+  // the ticket of the last-CTA fold sits after the nblocks x 5 partial sums
+  unsigned* ticket = reinterpret_cast<unsigned*>(partial + size_t(nblocks) * 5);
+  if (f32) energies_kernel<D, float><<<nblocks, 256, 0, s>>>(pp, partial, ticket, out);
+  else energies_kernel<D, double><<<nblocks, 256, 0, s>>>(pp, partial, ticket, out);
 }
 
 template <int D>

@@ -109,8 +109,9 @@ def _solve(dim, grid, solids, basis, alg, output, fixes, data):
         while done < nsteps:
             if not need_particles:
                 # no hook reads particle arrays: the remaining steps in calls of at most
-                # HOOK_CHUNK hooks, the EnergiesFix sums of each hook step copied back
-                # as they form, with no host round trip between steps
+                # HOOK_CHUNK hooks, the EnergiesFix sums of each hook step formed on
+                # the device and copied back once per call, with no host round trip
+                # between steps
                 first = (-done) % interval
                 run = min(nsteps - done, first + HOOK_CHUNK * interval)
                 if efix:
