@@ -383,8 +383,9 @@ def late_window(args, ctx, npart, advanced_before):
     the return-mapping branch, disordered particles), with the tuner re-run there.
     The default 1000 steps (about 11 us of the impact) stays inside the run's healthy
     range: with the linear hat basis the crushed impact corner reaches det F <= 0 near
-    step 1500 and loses a particle off the grid near step 2000, in the oracle as on
-    the GPU."""
+    step 1450 and loses a particle off the grid near step 2000, in the oracle as on
+    the GPU.  With FP32 particles det F <= 0 comes near step 925, so the FP32 default
+    is 600 steps."""
     ctx.step(args.late_steps)  # untimed
     tuning = ctx.tune(3) if args.tune else None
     launch = ctx.launch()
@@ -929,17 +930,20 @@ def main():
                     help="ensembles: steps per solve (default 1000 two-disk, 200 impact); adjoint: steps (2000)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--late-steps", type=int, default=1000,
-                    help="Taylor bar: steps advanced before the late-window measurement (0: none)")
+    ap.add_argument("--late-steps", type=int, default=None,
+                    help="Taylor bar: steps advanced before the late-window measurement (0: none; default "
+                         "1000 with FP64 particles, 600 with FP32)")
     ap.add_argument("--adjoint-p2g", default=None, choices=["atomic", "warp", "tile", "tile_warp"],
                     help="adjoint: P2G strategy of its contexts (a tile one selects the tiled adjoint scatter)")
-    ap.add_argument("--e2e-steps", type=int, default=1000,
+    ap.add_argument("--e2e-steps", type=int, default=500,
                     help="Taylor bar: steps of the end-to-end solve (at least --steps)")
     ap.add_argument("--extras", action=argparse.BooleanOptionalAction, default=True,
                     help="Taylor bar, FP64, 1 GPU: add the ensemble, adjoint and impact-jvp sub-results")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.late_steps is None:
+        args.late_steps = 600 if args.precision == "f32" else 1000
     if args.impl == "reference":
         run_reference(args)
     elif args.workload in ENSEMBLES:

@@ -128,6 +128,12 @@ struct mpm_ctx {
   cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_adj[2] = {nullptr, nullptr}, ev_sync = nullptr;
   cudaGraph_t graph[2] = {nullptr, nullptr};       // one step, per physical buffer
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  // the same step followed by its EnergiesFix sums, written through the
+  // device record cursor en_rec (mpm_step_energies)
+  cudaGraph_t graph_en[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec_en[2] = {nullptr, nullptr};
+  EnRec* en_rec = nullptr;    // device record cursor of the captured energies
+  EnRec* en_rec_h = nullptr;  // pinned host copy it is set from
   double last_ms = 0.0;
 
   PartP part(int b) const {
@@ -188,7 +194,11 @@ void destroy_ctx(mpm_ctx* c) {
   for (int i = 0; i < 2; ++i) {
     if (c->exec[i]) cudaGraphExecDestroy(c->exec[i]);
     if (c->graph[i]) cudaGraphDestroy(c->graph[i]);
+    if (c->exec_en[i]) cudaGraphExecDestroy(c->exec_en[i]);
+    if (c->graph_en[i]) cudaGraphDestroy(c->graph_en[i]);
   }
+  cudaFree(c->en_rec);
+  cudaFreeHost(c->en_rec_h);
   cudaFree(c->P);
   cudaFree(c->Palt);
   cudaFree(c->hat_c);
@@ -265,8 +275,10 @@ void invalidate_graphs(mpm_ctx* c) {
   for (int i = 0; i < 2; ++i) {
     if (c->exec[i]) cudaGraphExecDestroy(c->exec[i]);
     if (c->graph[i]) cudaGraphDestroy(c->graph[i]);
-    c->exec[i] = nullptr;
-    c->graph[i] = nullptr;
+    if (c->exec_en[i]) cudaGraphExecDestroy(c->exec_en[i]);
+    if (c->graph_en[i]) cudaGraphDestroy(c->graph_en[i]);
+    c->exec[i] = c->exec_en[i] = nullptr;
+    c->graph[i] = c->graph_en[i] = nullptr;
   }
   drop_seg_graphs(c);
 }
@@ -380,7 +392,8 @@ void enqueue_musl(mpm_ctx* c, cudaEvent_t* ev) {
   if (ev) cudaEventRecord(ev[3], c->stream);
 }
 
-void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
+// The launches of one step's kernels (enqueue_step).
+static void enqueue_step_kernels(mpm_ctx* c, cudaEvent_t* ev, double* rec) {
   if (c->prm.algorithm == MPM_ALG_MUSL) {
     enqueue_musl(c, ev);
     return;
@@ -447,17 +460,29 @@ void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr) {
   if (ev) cudaEventRecord(ev[3], c->stream);
 }
 
-// The step graph of the buffer currently in use (captured on first use).
-int build_step_graph(mpm_ctx* c) {
+// en: the step's EnergiesFix sums follow it, written through the record cursor
+// c->en_rec (a captured step fills successive records)
+void enqueue_step(mpm_ctx* c, cudaEvent_t* ev, double* rec = nullptr, bool en = false) {
+  enqueue_step_kernels(c, ev, rec);
+  if (!en || c->np == 0) return;
+  if (c->dim == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, nullptr, c->en_rec);
+  else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, nullptr, c->en_rec);
+}
+
+// The step graph of the buffer currently in use (captured on first use); en:
+// the step followed by its EnergiesFix record.
+int build_step_graph(mpm_ctx* c, bool en = false) {
   const int k = c->cur;
-  if (c->exec[k]) return MPM_OK;
+  cudaGraphExec_t& ex = en ? c->exec_en[k] : c->exec[k];
+  cudaGraph_t& gr = en ? c->graph_en[k] : c->graph[k];
+  if (ex) return MPM_OK;
   CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  enqueue_step(c, nullptr);
+  enqueue_step(c, nullptr, nullptr, en);
   cudaError_t le = cudaGetLastError();
-  cudaError_t ee = cudaStreamEndCapture(c->stream, &c->graph[k]);
+  cudaError_t ee = cudaStreamEndCapture(c->stream, &gr);
   if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(le));
   if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
-  CUDA_TRY(cudaGraphInstantiate(&c->exec[k], c->graph[k], 0));
+  CUDA_TRY(cudaGraphInstantiate(&ex, gr, 0));
   return MPM_OK;
 }
 
@@ -831,12 +856,12 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
 
 // enqueue one step: the cell sort when it is due, then the step graph of the
 // buffer in use (captured on first use)
-static int launch_one_step(mpm_ctx* c) {
+static int launch_one_step(mpm_ctx* c, bool en = false) {
   int r;
   if (c->Palt && c->prm.sort_interval > 0 && c->since_sort >= c->prm.sort_interval && (r = enqueue_sort(c)))
     return r;
-  if ((r = build_step_graph(c))) return r;
-  CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));
+  if ((r = build_step_graph(c, en))) return r;
+  CUDA_TRY(cudaGraphLaunch(en ? c->exec_en[c->cur] : c->exec[c->cur], c->stream));
   ++c->since_sort;
   return MPM_OK;
 }
@@ -879,26 +904,29 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
     CUDA_TRY(cudaMalloc(&c->rec_dev, size_t(nrec) * (2 + D) * sizeof(double)));
     c->rec_cap = nrec;
   }
+  // a recording step is one graph: the step, then its sums written through
+  // the record cursor (set here to the first record slot)
+  const bool in_graph = nrec > 0 && c->np > 0;
+  if (in_graph) {
+    if (!c->en_rec) {
+      CUDA_TRY(cudaMalloc(&c->en_rec, sizeof(EnRec)));
+      CUDA_TRY(cudaHostAlloc(&c->en_rec_h, sizeof(EnRec), cudaHostAllocDefault));
+    }
+    c->en_rec_h->base = c->rec_dev;
+    c->en_rec_h->idx = 0;
+    CUDA_TRY(cudaMemcpyAsync(c->en_rec, c->en_rec_h, sizeof(EnRec), cudaMemcpyHostToDevice, c->stream));
+  }
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CUDA_TRY(cudaEventRecord(c->e0, c->stream));
   int64_t j = 0;
   for (int64_t k = 0; k < nsteps; ++k) {
     int r;
-    if ((r = launch_one_step(c))) return r;
+    const bool recd = k >= first && (k - first) % every == 0;
+    if ((r = launch_one_step(c, in_graph && recd))) return r;
     if (t_inout) *t_inout += c->prm.dt;
-    if (k >= first && (k - first) % every == 0) {
-      // the record is formed on the device, in its slot; all records cross to
-      // the host in one copy after the steps
-      double* dst = c->rec_dev + size_t(j) * (2 + D);
-      if (c->np > 0) {
-        if (D == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, dst);
-        else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, dst);
-        CUDA_TRY(cudaGetLastError());
-      } else {
-        CUDA_TRY(cudaMemsetAsync(dst, 0, (2 + D) * sizeof(double), c->stream));
-      }
-      ++j;
-    }
+    if (recd && !in_graph)  // no particles: zero sums
+      CUDA_TRY(cudaMemsetAsync(c->rec_dev + size_t(j) * (2 + D), 0, (2 + D) * sizeof(double), c->stream));
+    if (recd) ++j;
   }
   if (nrec > 0)
     CUDA_TRY(cudaMemcpyAsync(c->rec_host, c->rec_dev, size_t(nrec) * (2 + D) * sizeof(double),

@@ -164,6 +164,13 @@ struct PartP {
   void* hat_nl = nullptr;    // D * pitch values of the particle type: the hat value at the lower node
 };
 
+// Record cursor of the EnergiesFix sums of captured steps (energies_kernel):
+// the records' base and the next record's index, in device memory.
+struct EnRec {
+  double* base;
+  long long idx;
+};
+
 // Buffers of the counting sort by (body, cell).
 struct SortP {
   uint32_t* key;       // per particle

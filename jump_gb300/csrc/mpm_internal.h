@@ -127,11 +127,12 @@ struct Launchers {
                            bool f32copy);
   static void g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
                   const MatParams& mp, double dt, unsigned* status, int threads = 0);
-  // EnergiesFix sums into out[0 .. 2 + D): partial holds nblocks x 5 doubles
-  // and one more slot, the fold's ticket, zero before the first launch (each
-  // launch leaves it zero)
+  // EnergiesFix sums into out[0 .. 2 + D), or with a record cursor rec into
+  // rec->base[rec->idx] (the cursor advances): partial holds nblocks x 5
+  // doubles and one more slot, the fold's ticket, zero before the first
+  // launch (each launch leaves it zero)
   static void energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,
-                       double* out);
+                       double* out, EnRec* rec = nullptr);
   static void aos_to_soa(cudaStream_t s, const PartP& pp, bool f32, const double* src, int per, int f0,
                          const CompMapH& cm);
   static void soa_to_aos(cudaStream_t s, const PartP& pp, bool f32, double* dst, int per, int f0,
@@ -173,7 +174,7 @@ inline int basis_nodes(int basis) {
   return basis == MPM_BASIS_QUAD_BSPLINE ? 3 : (basis == MPM_BASIS_CUBIC_BSPLINE ? 4 : 2);
 }
 
-constexpr int kEnergyBlocks = 304;  // 2 x 152 SMs
+constexpr int kEnergyBlocks = 608;  // 4 x 152 SMs
 
 // Records msg as the calling thread's mpm_last_error() text; returns code.
 int set_last_error(int code, const std::string& msg);

@@ -1108,9 +1108,12 @@ __global__ void __launch_bounds__(256) rigid_kernel(GridP g, NodeP nd, PartP pp,
 // warp adds blocks l, l + 32, ..., then a fixed shuffle tree -- so the result
 // does not depend on which CTA finishes last, and resets the ticket to zero
 // for the next launch.  The 1/2 factors are applied once to the folded sums
-// (a power-of-two scaling, exact).
+// (a power-of-two scaling, exact).  With a record cursor rec the sums go to
+// rec->base[rec->idx] and the cursor advances (a captured step graph fills
+// successive records); else to out.
 template <int D, class R>
-__global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial, unsigned* ticket, double* out) {
+__global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial, unsigned* ticket, double* out,
+                                                       EnRec* rec) {
   using L = Layout<D>;
   constexpr int NQ = 2 + D;
   double q[NQ];
@@ -1128,13 +1131,15 @@ __global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial
       vv += v[a] * v[a];
     }
     q[0] += m * vv;
-    double se = 0.0;
+    // sigma:eps with the off-diagonal entries twice: diagonal + 2 off-diagonal
+    double sd = 0.0, so = 0.0;
 #pragma unroll
     for (int c = 0; c < L::S; ++c) {
-      double w = (c < D) ? 1.0 : 2.0;  // off-diagonal entries appear twice in sigma:eps
-      se += w * double(*field<R>(pp, L::SIG + c, p)) * double(*field<R>(pp, L::EPS + c, p));
+      const double e = double(*field<R>(pp, L::SIG + c, p)) * double(*field<R>(pp, L::EPS + c, p));
+      if (c < D) sd += e;
+      else so += e;
     }
-    q[1] += double(*field<R>(pp, L::VOL, p)) * se;
+    q[1] += double(*field<R>(pp, L::VOL, p)) * (sd + 2.0 * so);
 #pragma unroll
     for (int a = 0; a < D; ++a) q[2 + a] += m * v[a];
   }
@@ -1169,6 +1174,10 @@ __global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial
   for (int k = 0; k < NQ; ++k)
     for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
   if (lane == 0) {
+    if (rec) {  // the record cursor of a captured step: the next record slot
+      out = rec->base + rec->idx * NQ;
+      rec->idx += 1;
+    }
     out[0] = 0.5 * acc[0];
     out[1] = 0.5 * acc[1];
 #pragma unroll

@@ -313,11 +313,11 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
 
 template <int D>
 void Launchers<D>::energies(cudaStream_t s, const PartP& pp, bool f32, double* partial, int nblocks,
-                            double* out) {
+                            double* out, EnRec* rec) {
   // the ticket of the last-CTA fold sits after the nblocks x 5 partial sums
   unsigned* ticket = reinterpret_cast<unsigned*>(partial + size_t(nblocks) * 5);
-  if (f32) energies_kernel<D, float><<<nblocks, 256, 0, s>>>(pp, partial, ticket, out);
-  else energies_kernel<D, double><<<nblocks, 256, 0, s>>>(pp, partial, ticket, out);
+  if (f32) energies_kernel<D, float><<<nblocks, 256, 0, s>>>(pp, partial, ticket, out, rec);
+  else energies_kernel<D, double><<<nblocks, 256, 0, s>>>(pp, partial, ticket, out, rec);
 }
 
 template <int D>

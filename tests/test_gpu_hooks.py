@@ -40,6 +40,42 @@ def test_step_energies_matches_step_then_energies(every, first):
     assert max(errs.values()) <= 1e-12, errs
 
 
+@pytest.mark.parametrize("precision,sort,threads", [("f64", 0, 128), ("f32", 3, 32), ("f64", 2, 256)])
+def test_step_energies_taylor_bar_captured(precision, sort, threads):
+    """The 3D J2 bar, whose recording steps run as one captured graph each (the
+    step, then the EnergiesFix sums through the device record cursor): records
+    of two calls (the second needs more record slots than the first) against
+    mpm_energies after single steps, FP64 and FP32, with the cell sort
+    switching buffers (two captured graphs) and at several CTA sizes."""
+    grid, solids, alg, data = scenarios.taylor_bar(h=1e-3)
+    scenarios.apply_dirichlet(grid, data)
+    mk = lambda: descriptors(grid, solids, alg.tolerance, data.get("bodyforce"), data["dt"], precision=precision)
+    a, b = MPMContext(mk()), MPMContext(mk())
+    for c in (a, b):
+        c.set_launch(threads=threads, sort_interval=sort)
+    calls = [(7, 1, 0), (20, 2, 1)]
+    got = [a.step_energies(n, e, f)[0] for n, e, f in calls]
+    want = []
+    for n, e, f in calls:
+        w = []
+        for k in range(n):
+            b.step(1)
+            if k >= f and (k - f) % e == 0:
+                ke, se, mom = b.energies()
+                w.append([ke, se, *mom])
+        want.append(np.array(w))
+    for g, w in zip(got, want):
+        assert g.shape == w.shape
+        scale = np.max(np.abs(w), axis=0)
+        scale[2:] = scale[2:].max()  # momentum components against the momentum's size
+        # FP32: two runs of the same FP32 problem differ at FP32's resolution
+        # (summation order of the FP32 warp sums); FP64: at FP64's
+        tol = 2e-6 if precision == "f32" else 1e-11
+        assert np.all(np.abs(g - w) <= tol * scale), (g, w)
+    a.close()
+    b.close()
+
+
 def test_step_energies_without_records():
     grid, solids, alg, data = disks()
     c = MPMContext(descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"]))
