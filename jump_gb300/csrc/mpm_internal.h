@@ -174,7 +174,7 @@ inline int basis_nodes(int basis) {
   return basis == MPM_BASIS_QUAD_BSPLINE ? 3 : (basis == MPM_BASIS_CUBIC_BSPLINE ? 4 : 2);
 }
 
-constexpr int kEnergyBlocks = 608;  // 4 x 152 SMs
+constexpr int kEnergyBlocks = 304;  // 2 x 152 SMs
 
 // Records msg as the calling thread's mpm_last_error() text; returns code.
 int set_last_error(int code, const std::string& msg);

@@ -1110,7 +1110,8 @@ __global__ void __launch_bounds__(256) rigid_kernel(GridP g, NodeP nd, PartP pp,
 // for the next launch.  The 1/2 factors are applied once to the folded sums
 // (a power-of-two scaling, exact).  With a record cursor rec the sums go to
 // rec->base[rec->idx] and the cursor advances (a captured step graph fills
-// successive records); else to out.
+// successive records); else to out.  kEnergyBlocks CTAs: one wave at the two
+// CTAs per SM its registers allow.
 template <int D, class R>
 __global__ void __launch_bounds__(256) energies_kernel(PartP pp, double* partial, unsigned* ticket, double* out,
                                                        EnRec* rec) {
