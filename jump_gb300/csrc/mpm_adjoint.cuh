@@ -395,6 +395,28 @@ __device__ __forceinline__ void g2p_adj_particle(const GridP& gp, const GridRec&
 }
 
 
+// G2P adjoint of particle pp.begin + t (t < pp.count) with its node adjoints
+// added by FP64 atomics per corner and value at L2
+template <int D, int MAT>
+__device__ __forceinline__ void g2p_adj_atomic(const GridP& gp, const GridRec& gr, const PartP& pp, const AdjP& ad,
+                                               const NodeAdjP& na, const MatParams& mp, double c1, double c2,
+                                               int64_t t) {
+  using L = Layout<D>;
+  const int64_t p = pp.begin + t, Nn = na.nodeCount;
+  double x[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) x[a] = static_cast<const double*>(pp.base)[int64_t(L::X + a) * pp.pitch + p];
+  Hat<D, double> h;
+  if (!hat<D, double>(gp, x, h)) return;  // frozen particle: its adjoints pass through unchanged
+  g2p_adj_particle<D, MAT>(gp, gr, pp, ad, na, mp, c1, c2, p, h, [&](int, int64_t n, const double* val) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      atomicAdd(na.vdtb + a * Nn + n, val[a]);
+      atomicAdd(na.dvb + a * Nn + n, val[D + a]);
+    }
+  });
+}
+
 // The G2P adjoint.  Its scatter of the node adjoints vdt_ and dv_:
 // TILE = false: FP64 atomics per particle, corner and value at L2;
 // TILE = true: staged in a shared-memory tile of the node box the CTA's
@@ -413,19 +435,7 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, Part
   const int64_t p = pp.begin + t;
   const int64_t Nn = na.nodeCount;
   if constexpr (!TILE) {
-    if (t >= pp.count) return;
-    double x[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) x[a] = static_cast<const double*>(pp.base)[int64_t(L::X + a) * pp.pitch + p];
-    Hat<D, double> h;
-    if (!hat<D, double>(gp, x, h)) return;  // frozen particle: its adjoints pass through unchanged
-    g2p_adj_particle<D, MAT>(gp, gr, pp, ad, na, mp, c1, c2, p, h, [&](int, int64_t n, const double* val) {
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        atomicAdd(na.vdtb + a * Nn + n, val[a]);
-        atomicAdd(na.dvb + a * Nn + n, val[D + a]);
-      }
-    });
+    if (t < pp.count) g2p_adj_atomic<D, MAT>(gp, gr, pp, ad, na, mp, c1, c2, t);
     return;
   }
   Hat<D, double> h{};
@@ -477,12 +487,11 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(GridP gp, GridRec gr, Part
   }
 }
 
+// grid adjoint of node i (see the header)
 template <int D>
-__global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, const uint8_t* fixed, double dt,
-                                                       double tol) {
-  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void grid_adj_node(const GridRec& gr, const NodeAdjP& na, const uint8_t* fixed, double dt,
+                                              double tol, int64_t i) {
   const int64_t Nn = na.nodeCount;
-  if (i >= Nn) return;
   const double m = gr.m[i];
   double mb = 0.0;
   const unsigned fx = fixed[i];
@@ -490,7 +499,7 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, 
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     double p0b = 0.0, fb = 0.0;
-    const double vdtb = na.vdtb[a * Nn + i], dvb = na.dvb[a * Nn + i];
+    const double vdtb = __ldcg(na.vdtb + a * Nn + i), dvb = __ldcg(na.dvb + a * Nn + i);
     if (m > tol && !(fx & (1u << a))) {
       p0b = (dt * vdtb) * im;
       fb = (dt * dt * vdtb + dt * dvb) * im;
@@ -503,6 +512,13 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, 
     na.dvb[a * Nn + i] = 0.0;
   }
   na.mb[i] = mb;
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, const uint8_t* fixed, double dt,
+                                                       double tol) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < na.nodeCount) grid_adj_node<D>(gr, na, fixed, dt, tol, i);
 }
 
 template <int D>
@@ -531,13 +547,13 @@ __device__ __forceinline__ void inv_det(const double* F, double* Fi, double& J) 
   }
 }
 
+// P2G adjoint of particle pp.begin + t (t < pp.count; see the header)
 template <int D, int MAT>
-__global__ void __launch_bounds__(256) p2g_adj_kernel(GridP gp, PartP pp, AdjP ad, NodeAdjP na, MatParams mp,
-                                                      double c1, double c2, double bx, double by, double bz) {
+__device__ __forceinline__ void p2g_adj_particle(const GridP& gp, const PartP& pp, const AdjP& ad, const NodeAdjP& na,
+                                                 const MatParams& mp, double c1, double c2, double bx, double by,
+                                                 double bz, int64_t t) {
   using L = Layout<D>;
   using A = AdjLayout<D>;
-  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= pp.count) return;
   const int64_t p = pp.begin + t;
   const double* P = static_cast<const double*>(pp.base);
   auto fld = [&](int f) { return P[int64_t(f) * pp.pitch + p]; };
@@ -569,12 +585,14 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(GridP gp, PartP pp, AdjP a
 #pragma unroll
   for (int k = 0; k < (1 << D); ++k) {
     const int64_t n = c.node[k];
-    const double mb = na.mb[n];
+    // node adjoints through L2 (__ldcg): in the fused reverse step other CTAs
+    // wrote them in this launch
+    const double mb = __ldcg(na.mb + n);
     double p0b[D], fb[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      p0b[a] = na.p0b[a * Nn + n];
-      fb[a] = na.fb[a * Nn + n];
+      p0b[a] = __ldcg(na.p0b + a * Nn + n);
+      fb[a] = __ldcg(na.fb + a * Nn + n);
     }
     double wb = mpart * mb, gb[D];
 #pragma unroll
@@ -661,6 +679,83 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(GridP gp, PartP pp, AdjP a
     *adj<D>(ad, A::XB + a, p) = xb[a];
     *adj<D>(ad, A::VB + a, p) = vb[a];
   }
+}
+
+template <int D, int MAT>
+__global__ void __launch_bounds__(256) p2g_adj_kernel(GridP gp, PartP pp, AdjP ad, NodeAdjP na, MatParams mp,
+                                                      double c1, double c2, double bx, double by, double bz) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t < pp.count) p2g_adj_particle<D, MAT>(gp, pp, ad, na, mp, c1, c2, bx, by, bz, t);
+}
+
+// ---------------------------------------------------------------------------
+// One reversed step of a single-body context in one cooperative launch: the G2P
+// adjoint (per-particle atomics), a grid barrier, the grid adjoint of every
+// node, a grid barrier, the P2G adjoint -- the three kernels above without two
+// launches and the grid adjoint's own launch latency.  Thread t handles
+// particle t in the particle stages and nodes t, t + gridDim.x blockDim.x, ...
+// in the grid stage, so no thread leaves before a barrier.
+struct RevStepP {
+  GridP gp;
+  GridRec gr;
+  PartP pp;
+  AdjP ad;
+  NodeAdjP na;
+  MatParams mp;
+  double c1, c2, dt, tol;
+  double grav[3];
+  const uint8_t* fixed;
+  unsigned* bar;  // [0] arrivals, [1] generation: zero before the first launch, left consistent by each
+  unsigned* err;  // bit 0: a barrier wait gave up
+};
+
+// Grid-wide barrier of a cooperative launch (every CTA resident).  Thread 0 of
+// each CTA arrives on bar[0]; the last to arrive resets it and advances the
+// generation bar[1]; the others wait for the generation to change, at most
+// about one second (globaltimer), after which the wait sets err bit 0 and
+// returns false and the kernel ends without its remaining stages.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned* gen = bar + 1;
+    const unsigned g = *gen;  // read before arriving: it cannot advance until this CTA has arrived
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x * gridDim.y * gridDim.z - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned long long t0, t1;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (*gen == g) {
+        __nanosleep(64);
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        if (t1 - t0 > 1000000000ull) {
+          atomicOr(err, 1u);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <int D, int MAT>
+__global__ void __launch_bounds__(256) reverse_step_kernel(RevStepP r) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t nth = int64_t(gridDim.x) * blockDim.x;
+  if (*reinterpret_cast<volatile unsigned*>(r.err)) return;  // an earlier barrier gave up: the sweep is void
+  if (t < r.pp.count) g2p_adj_atomic<D, MAT>(r.gp, r.gr, r.pp, r.ad, r.na, r.mp, r.c1, r.c2, t);
+  if (!grid_barrier(r.bar, r.err)) return;
+  for (int64_t i = t; i < r.na.nodeCount; i += nth) grid_adj_node<D>(r.gr, r.na, r.fixed, r.dt, r.tol, i);
+  if (!grid_barrier(r.bar, r.err)) return;
+  if (t < r.pp.count)
+    p2g_adj_particle<D, MAT>(r.gp, r.pp, r.ad, r.na, r.mp, r.c1, r.c2, r.grav[0], r.grav[1], r.grav[2], t);
 }
 
 }  // namespace jmpm

@@ -93,6 +93,8 @@ struct mpm_ctx {
   double* gridrec = nullptr;
   double* adjbuf = nullptr;
   double* nodeadj = nullptr;
+  unsigned* revbar = nullptr;  // fused reverse step: barrier arrivals, generation, error flag
+  bool coop_off = false;       // the fused reverse step could not be captured: three kernels per step
   ContactP cp{};                 // contact mode: per-body node fields
   double* contactbuf = nullptr;
   float* contactbuf_f = nullptr;
@@ -224,6 +226,7 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->gridrec);
   cudaFree(c->adjbuf);
   cudaFree(c->nodeadj);
+  cudaFree(c->revbar);
   cudaFree(c->contactbuf);
   cudaFree(c->contactbuf_f);
   cudaFree(c->status);
@@ -1400,27 +1403,61 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
       enqueue_step(c, nullptr, seg_rec(X, j));
     }
   };
+  // One reversed step from a particle state and its node record, on the
+  // context's stream.  A single body with the per-particle scatter runs it as
+  // one cooperative launch (reverse_step_kernel), else three kernels.  The
+  // node adjoints vdt_bar, dv_bar are zero on entry: set once below, then
+  // zeroed by the grid adjoint as it consumes them.
+  bool coop = c->nb == 1 && !adj_tile && !c->coop_off &&
+              (D == 2 ? Launchers<2>::reverse_step_fits(c->cnt[0], c->mats[0].type)
+                      : Launchers<3>::reverse_step_fits(c->cnt[0], c->mats[0].type));
+  if (coop) {
+    if (!c->revbar) CUDA_TRY(cudaMalloc(&c->revbar, 4 * sizeof(unsigned)));
+    CUDA_TRY(cudaMemsetAsync(c->revbar, 0, 4 * sizeof(unsigned), c->stream));
+  }
+  auto reverse_one = [&](const GridRec& gr, void* state) {
+    if (coop) {
+      const double nu = c->nus[0];
+      RevStepP r{};
+      r.gp = c->g;
+      r.gr = gr;
+      r.pp = PartP{state, c->np, c->off[0], c->cnt[0]};
+      r.ad = ad;
+      r.na = na;
+      r.mp = c->mats[0];
+      r.c1 = nu / (1 + nu) / (1 - 2 * nu);  // dlambda/dE
+      r.c2 = 1.0 / 2.0 / (1 + nu);          // dmu/dE
+      r.dt = c->prm.dt;
+      r.tol = c->prm.tolerance;
+      for (int a = 0; a < 3; ++a) r.grav[a] = (a < D) ? c->prm.body_force[a] : 0.0;
+      r.fixed = c->fixed;
+      r.bar = c->revbar;
+      r.err = c->revbar + 2;
+      if (D == 2) Launchers<2>::reverse_step(c->stream, r);
+      else Launchers<3>::reverse_step(c->stream, r);
+      return;
+    }
+    for (int b = 0; b < c->nb; ++b) {
+      const PartP ps{state, c->np, c->off[b], c->cnt[b]};
+      const double nu = c->nus[b];
+      const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);  // dlambda/dE, dmu/dE
+      if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
+      else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
+    }
+    if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
+    else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
+    for (int b = 0; b < c->nb; ++b) {
+      const PartP ps{state, c->np, c->off[b], c->cnt[b]};
+      const double nu = c->nus[b];
+      const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
+      if (D == 2) Launchers<2>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
+      else Launchers<3>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
+    }
+  };
   auto enqueue_reverse = [&](int X, int len) {
     for (int j = len - 1; j >= 0; --j) {
       const double* rec = seg_rec(X, j);
-      const GridRec gr{rec, rec + Nn * (1 + 2 * D), rec + Nn * (1 + 3 * D)};
-      // the node adjoints vdt_bar, dv_bar are zero here: set once below, then zeroed by grid_adj
-      for (int b = 0; b < c->nb; ++b) {
-        const PartP ps{seg_state(X, j), c->np, c->off[b], c->cnt[b]};
-        const double nu = c->nus[b];
-        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);  // dlambda/dE, dmu/dE
-        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
-        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
-      }
-      if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
-      else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
-      for (int b = 0; b < c->nb; ++b) {
-        const PartP ps{seg_state(X, j), c->np, c->off[b], c->cnt[b]};
-        const double nu = c->nus[b];
-        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
-        if (D == 2) Launchers<2>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
-        else Launchers<3>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
-      }
+      reverse_one(GridRec{rec, rec + Nn * (1 + 2 * D), rec + Nn * (1 + 3 * D)}, seg_state(X, j));
     }
   };
   // captured once per (kind, buffer, segment length: full or the shorter last one),
@@ -1443,6 +1480,18 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
     else enqueue_reverse(X, len);
     cudaError_t le = cudaGetLastError();
     cudaError_t ee = cudaStreamEndCapture(c->stream, &c->seg_graph[kind][X][l]);
+    if (kind == 1 && coop && (le != cudaSuccess || ee != cudaSuccess)) {
+      // the cooperative launch was not captured: three kernels per step from now on
+      if (c->seg_graph[kind][X][l]) cudaGraphDestroy(c->seg_graph[kind][X][l]);
+      c->seg_graph[kind][X][l] = nullptr;
+      cudaGetLastError();
+      coop = false;
+      c->coop_off = true;
+      CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_reverse(X, len);
+      le = cudaGetLastError();
+      ee = cudaStreamEndCapture(c->stream, &c->seg_graph[kind][X][l]);
+    }
     if (le != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_bwd launch: ") + cudaGetErrorString(le));
     if (ee != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("mpm_bwd capture: ") + cudaGetErrorString(ee));
     CUDA_TRY(cudaGraphInstantiate(&c->seg_exec[kind][X][l], c->seg_graph[kind][X][l], 0));
@@ -1456,24 +1505,8 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
     const size_t recd = size_t(Nn) * (1 + 4 * D);
     for (int64_t k = nsteps; k >= 1; --k) {
       const double* rec = c->fullrec + recd * size_t(k - 1);
-      const GridRec gr{rec, rec + Nn * (1 + 2 * D), rec + Nn * (1 + 3 * D)};
-      char* state = reinterpret_cast<char*>(c->ckpt) + bytes * size_t(k - 1);
-      for (int b = 0; b < c->nb; ++b) {
-        const PartP ps{state, c->np, c->off[b], c->cnt[b]};
-        const double nu = c->nus[b];
-        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
-        if (D == 2) Launchers<2>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
-        else Launchers<3>::g2p_adj(c->stream, c->g, gr, ps, ad, na, c->mats[b], c1, c2, adj_tile);
-      }
-      if (D == 2) Launchers<2>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
-      else Launchers<3>::grid_adj(c->stream, gr, na, c->fixed, c->prm.dt, c->prm.tolerance);
-      for (int b = 0; b < c->nb; ++b) {
-        const PartP ps{state, c->np, c->off[b], c->cnt[b]};
-        const double nu = c->nus[b];
-        const double c1 = nu / (1 + nu) / (1 - 2 * nu), c2 = 1.0 / 2.0 / (1 + nu);
-        if (D == 2) Launchers<2>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
-        else Launchers<3>::p2g_adj(c->stream, c->g, ps, ad, na, c->mats[b], c1, c2, c->prm.body_force);
-      }
+      reverse_one(GridRec{rec, rec + Nn * (1 + 2 * D), rec + Nn * (1 + 3 * D)},
+                  reinterpret_cast<char*>(c->ckpt) + bytes * size_t(k - 1));
     }
   }
   if (!(every == 1 && c->fullrec) && nseg > 0) {
@@ -1513,6 +1546,12 @@ int mpm_bwd(mpm_ctx* c, const double* x_bar, const double* v_bar, double* E_bar,
     CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_sync, 0));
   }
   CUDA_TRY(cudaGetLastError());
+  if (coop) {
+    unsigned err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, c->revbar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (err) return fail(MPM_ERR_CUDA, "mpm_bwd: a grid barrier of the fused reverse step gave up after one second");
+  }
   // gradients in original particle order (no sorting in reverse mode)
   base = 0;
   for (int b = 0; b < c->nb; ++b) {

@@ -118,6 +118,11 @@ struct Launchers {
   // contexts whose P2G strategy is a tile one), else per particle at L2
   static void g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, const PartP& pp, const AdjP& ad,
                       const NodeAdjP& na, const MatParams& mp, double c1, double c2, bool tile);
+  // one reversed step of a single-body context in one cooperative launch
+  // (reverse_step_kernel); reverse_step_fits: the device takes cooperative
+  // launches and every CTA of count particles' launch can be resident at once
+  static bool reverse_step_fits(int64_t count, int mat);
+  static cudaError_t reverse_step(cudaStream_t s, const RevStepP& r);
   static void grid_adj(cudaStream_t s, const GridRec& gr, const NodeAdjP& na, const uint8_t* fixed, double dt,
                        double tol);
   static void p2g_adj(cudaStream_t s, const GridP& g, const PartP& pp, const AdjP& ad, const NodeAdjP& na,

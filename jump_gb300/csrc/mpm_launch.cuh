@@ -109,6 +109,34 @@ void Launchers<D>::g2p_adj(cudaStream_t s, const GridP& g, const GridRec& gr, co
 }
 
 template <int D>
+static const void* reverse_step_fn(int mat) {
+  if (mat == MPM_MAT_ELASTIC) return reinterpret_cast<const void*>(reverse_step_kernel<D, MPM_MAT_ELASTIC>);
+  if (mat == MPM_MAT_J2) return reinterpret_cast<const void*>(reverse_step_kernel<D, MPM_MAT_J2>);
+  return reinterpret_cast<const void*>(reverse_step_kernel<D, MPM_MAT_NEOHOOKEAN>);
+}
+
+template <int D>
+bool Launchers<D>::reverse_step_fits(int64_t count, int mat) {
+  int dev = 0, coop = 0, sms = 0, per = 0;
+  if (count <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || !coop)
+    return false;
+  const int th = spread_threads(count);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, reverse_step_fn<D>(mat), th, 0) != cudaSuccess) return false;
+  return int64_t(per) * sms >= int64_t(blocks_for(count, th));
+}
+
+template <int D>
+cudaError_t Launchers<D>::reverse_step(cudaStream_t s, const RevStepP& r) {
+  const int th = spread_threads(r.pp.count);
+  RevStepP a = r;
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel(reverse_step_fn<D>(r.mp.type), dim3(blocks_for(r.pp.count, th)), dim3(th), args,
+                                     0, s);
+}
+
+template <int D>
 void Launchers<D>::grid_adj(cudaStream_t s, const GridRec& gr, const NodeAdjP& na, const uint8_t* fixed, double dt,
                             double tol) {
   const int th = spread_threads(na.nodeCount);
