@@ -307,8 +307,8 @@ function gpu_solve(grid, solids, basis, alg::Union{USL,MUSL}, output, fixes, dat
 end
 
 # With only EnergiesFix hooks nothing reads the particle arrays between hooks:
-# many hook intervals run in one call, each hook's sums formed on the device and
-# copied back while later steps run (mpm_step_energies).
+# many hook intervals run in one call, each hook's sums formed on the device
+# after its step and all of them copied back at the end (mpm_step_energies).
 function gpu_energies_run!(ctx, fix::EnergiesFix, dim, n, interval, counter0, times)
     first = mod(-counter0, interval)
     nrec = n > first ? div(n - 1 - first, interval) + 1 : 0
