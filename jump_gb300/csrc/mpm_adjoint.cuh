@@ -522,10 +522,10 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(GridRec gr, NodeAdjP na, 
 }
 
 template <int D>
-__device__ __forceinline__ void inv_det(const double* F, double* Fi, double& J) {
+__device__ __forceinline__ void inv_det(const double* F, double* Fi, double& J, double& iJ) {
   if constexpr (D == 2) {
     J = F[0] * F[3] - F[2] * F[1];
-    const double iJ = 1.0 / J;
+    iJ = 1.0 / J;
     Fi[0] = F[3] * iJ;
     Fi[3] = F[0] * iJ;
     Fi[2] = -F[2] * iJ;
@@ -533,7 +533,7 @@ __device__ __forceinline__ void inv_det(const double* F, double* Fi, double& J) 
   } else {
     const double c00 = F[4] * F[8] - F[7] * F[5], c02 = F[1] * F[5] - F[4] * F[2];
     J = F[0] * c00 - F[3] * (F[1] * F[8] - F[2] * F[7]) + F[6] * c02;
-    const double iJ = 1.0 / J;
+    iJ = 1.0 / J;
     // inverse via the adjugate (column-major: Fi[i + 3 j] = (F^-1)_ij)
     Fi[0] = c00 * iJ;
     Fi[1] = -(F[1] * F[8] - F[2] * F[7]) * iJ;
@@ -573,13 +573,24 @@ __device__ __forceinline__ void p2g_adj_particle(const GridP& gp, const PartP& p
 #pragma unroll
     for (int b = 0; b < D; ++b) sig[a][b] = fld(L::SIG + sym<D>(a, b));
   const double grav[3] = {bx, by, bz};
+  // per particle once: -V sigma, m v, m g; per corner the sum T = sum_k f_ (x) grad N_k,
+  // from which sigma_ = -V T and V_ = -sigma : T after the corners
+  double sV[D][D], mv[D], mg[D], T[D][D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    mv[a] = mpart * v[a];
+    mg[a] = mpart * grav[a];
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      sV[a][b] = -V * sig[a][b];
+      T[a][b] = 0.0;
+    }
+  }
   double xb[D], vb[D], sb[D][D], Vb = 0.0;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     xb[a] = *adj<D>(ad, A::XB + a, p);
     vb[a] = *adj<D>(ad, A::VB + a, p);
-#pragma unroll
-    for (int b = 0; b < D; ++b) sb[a][b] = 0.0;
   }
   const int64_t Nn = na.nodeCount;
 #pragma unroll
@@ -595,34 +606,36 @@ __device__ __forceinline__ void p2g_adj_particle(const GridP& gp, const PartP& p
       fb[a] = __ldcg(na.fb + a * Nn + n);
     }
     double wb = mpart * mb, gb[D];
+    const double mN = mpart * c.N[k];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      wb += mpart * (v[a] * p0b[a] + grav[a] * fb[a]);
-      vb[a] += mpart * c.N[k] * p0b[a];
+      wb += mv[a] * p0b[a] + mg[a] * fb[a];
+      vb[a] += mN * p0b[a];
     }
 #pragma unroll
     for (int b = 0; b < D; ++b) {
       double s = 0.0;
 #pragma unroll
-      for (int a = 0; a < D; ++a) s += sig[a][b] * fb[a];
-      gb[b] = -V * s;
+      for (int a = 0; a < D; ++a) s += sV[a][b] * fb[a];
+      gb[b] = s;
     }
 #pragma unroll
-    for (int a = 0; a < D; ++a) {
-      double sg = 0.0;
+    for (int a = 0; a < D; ++a)
 #pragma unroll
-      for (int b = 0; b < D; ++b) {
-        sb[a][b] -= V * fb[a] * c.g[k][b];
-        sg += sig[a][b] * c.g[k][b];
-      }
-      Vb -= fb[a] * sg;
-    }
+      for (int b = 0; b < D; ++b) T[a][b] += fb[a] * c.g[k][b];
     add_shape_adj<D>(xb, c, k, wb, gb);
   }
-  double F[D * D], Fi[D * D], J;
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+#pragma unroll
+    for (int b = 0; b < D; ++b) {
+      sb[a][b] = -V * T[a][b];
+      Vb -= sig[a][b] * T[a][b];
+    }
+  double F[D * D], Fi[D * D], J, iJ;
 #pragma unroll
   for (int q = 0; q < D * D; ++q) F[q] = fld(L::F + q);
-  inv_det<D>(F, Fi, J);
+  inv_det<D>(F, Fi, J, iJ);
   if constexpr (MAT != MPM_MAT_NEOHOOKEAN) {
     // the stress is particle state: its adjoint (stored symmetric components)
     // goes to the G2P adjoint of the previous step, which formed it; V = J V0
@@ -649,7 +662,7 @@ __device__ __forceinline__ void p2g_adj_particle(const GridP& gp, const PartP& p
     lam = fld(L::LAM);
     mu = fld(L::MU);
   }
-  const double lnJ = log(J), iJ = 1.0 / J;
+  const double lnJ = log(J);
   double trS = 0.0, SB = 0.0;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
