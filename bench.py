@@ -713,7 +713,8 @@ def run_ensemble(args):
 def measure_adjoint(args, nsteps):
     """Differentiable cantilever (16,384 particles, neo-Hookean, per-particle E,
     nsteps steps at dt = 1e-4, checkpoint every 50): forward throughput against
-    forward + adjoint throughput, the store-every-step mode, end to end (context
+    forward + adjoint throughput (medians of three alternating runs of each),
+    the store-every-step mode, end to end (context
     from host arrays, forward with checkpoints, final positions downloaded, the
     reverse sweep, gradients in host memory), and the gradient of the
     tip-displacement loss against central differences on 32 random parameters
@@ -750,20 +751,25 @@ def measure_adjoint(args, nsteps):
     c = make_context(problem, E, v0)
     c.step(args.warmup)
     c.close()
-    c = make_context(problem, E, v0)
-    t0 = time.perf_counter()
-    c.step(nsteps)
-    fwd = time.perf_counter() - t0
-    c.close()
-    c = make_context(problem, E, v0)
+    # forward and forward + adjoint, three of each, alternating, each on a fresh
+    # context from the same initial state; the medians are reported
+    fwd_s, both_s = [], []
     sampler = ClockSampler()
-    t0 = time.perf_counter()
-    c.fwd_checkpointed(nsteps, every)
-    x = final_positions(c)
-    g = c.bwd(loss_grad(x))
-    both = time.perf_counter() - t0
+    for _ in range(3):
+        c = make_context(problem, E, v0)
+        t0 = time.perf_counter()
+        c.step(nsteps)
+        fwd_s.append(time.perf_counter() - t0)
+        c.close()
+        c = make_context(problem, E, v0)
+        t0 = time.perf_counter()
+        c.fwd_checkpointed(nsteps, every)
+        x = final_positions(c)
+        g = c.bwd(loss_grad(x))
+        both_s.append(time.perf_counter() - t0)
+        c.close()
     clocks = sampler.stop()
-    c.close()
+    fwd, both = float(np.median(fwd_s)), float(np.median(both_s))
     # end to end: the same with the context built from the host arrays inside the clock
     t0 = time.perf_counter()
     c = make_context(problem, E, v0)
@@ -807,6 +813,7 @@ def measure_adjoint(args, nsteps):
                        "checkpoint_every": every, "loss": "squared tip displacement error (top 5% in x)"},
             "forward_particle_updates_per_s": npart * nsteps / fwd,
             "fwd_adj_over_fwd_throughput": fwd / both,
+            "samples_s": {"forward": fwd_s, "forward_adjoint": both_s, "reported": "medians"},
             "clocks": clocks,
             "e2e": {"value": npart * nsteps / e2e, "unit": "particle-updates/s",
                     "h2d_bytes_per_step": (npart * (2 * d + 3 + 3 * d * d + 1) * 8 + x.nbytes) / nsteps,

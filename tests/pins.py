@@ -109,10 +109,25 @@ def j2_shear_history(ctx_cls, dim, E, nu, rho, fy, k1, eps12s):
 # USL step conserves linear momentum exactly up to rounding (the grid forces
 # sum to zero because sum_I grad N_I = 0 for every particle off the node lines)
 
-def two_disks_free(ctx_cls, steps, record_every=100, threads=None):
+# Nodal mass cutoffs of the pin.  Linear momentum is conserved to rounding only
+# without a cutoff (a cut node drops its share); but then a node reached only
+# by a particle's far corner can keep a mass small enough for f dt / m to
+# invert a particle late in the run, in some summation orders: the oracle with
+# its particles permuted (each node sum re-associated) reaches det F <= 0 after
+# step 2275 in some orders, with no cutoff or with the reference driver's 1e-9
+# (Main_TwoDisks.jl:107).  At 1e-6 (particle masses 0.625) every order gives the
+# same energy history.  The GPU's atomics choose a summation order per run, so
+# mass and momentum are checked without a cutoff over the first 2000 steps
+# (through the collision's strain-energy peak near step 1900) and the energy
+# band at 1e-6 over the configuration's 3001 steps.
+MOMENTUM_STEPS = 2000
+ENERGY_TOL = 1e-6
+
+
+def two_disks_free(ctx_cls, steps, tol, record_every=100, threads=None):
     grid, solids, alg, data = scenarios.two_disks(fixed_boundary=False)
     kw = {} if threads is None else {"threads": threads}
-    c = ctx_cls(Descriptors(grid, solids, tolerance=0.0, body_force=data["bodyforce"], dt=data["dt"]), **kw)
+    c = ctx_cls(Descriptors(grid, solids, tolerance=tol, body_force=data["bodyforce"], dt=data["dt"]), **kw)
     recs = [c.energies()]
     mass = sum(float(np.sum(s.mass)) for s in solids)
     pscale = sum(float(np.sum(s.mass * np.linalg.norm(s.velocity, axis=1))) for s in solids)

@@ -3,7 +3,8 @@
 * The Taylor bar of the headline benchmark: 511,784 particles, J2 plasticity,
   100 steps from the impact, every particle field of the GPU run against the
   oracle (OpenMP: its node sums are re-associated slab by slab, which by itself
-  moves the results by ~1e-14).
+  moves the results by ~1e-14); and the FP32-particle variant's error on the
+  same run.
 * The 512-problem two-disk ensemble (seeded instances, 132..9,096 particles,
   20^2..80^2 cells) over the configuration's 1000 steps in one batched launch,
   both batch strategies, against the oracle for 16 problems that span the
@@ -29,20 +30,28 @@ J2_FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pst
 DISK_FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress")
 
 
-def test_taylor_bar_full_size_100_steps_vs_oracle(oracle_lib):
+@pytest.fixture(scope="module")
+def bar_100(oracle_lib):
+    """The headline bar's descriptor factory and the oracle's state after 100 steps."""
     grid, solids, alg, data = scenarios.taylor_bar()
     scenarios.apply_dirichlet(grid, data)
     assert solids[0].parCount == 511784
-    mk = lambda: Descriptors(grid, solids, tolerance=alg.tolerance, body_force=data["bodyforce"], dt=data["dt"])
-    g = MPMContext(mk())
-    g.step(100)
-    sg = g.download_all()
-    g.close()
+    mk = lambda **kw: Descriptors(grid, solids, tolerance=alg.tolerance, body_force=data["bodyforce"],
+                                  dt=data["dt"], **kw)
     o = oracle_lib.OracleContext(mk(), threads=oracle_lib.max_threads())
     o.step(100)
     so = o.download_all()
     o.close()
     assert np.max(so[0].alpha) > 0, "the bar must yield"
+    return mk, so
+
+
+def test_taylor_bar_full_size_100_steps_vs_oracle(bar_100):
+    mk, so = bar_100
+    g = MPMContext(mk())
+    g.step(100)
+    sg = g.download_all()
+    g.close()
     fm = {f: e for (_, f), e in field_errors(sg, so, fields=J2_FIELDS).items()}
     pp = particle_errors(sg, so, fields=J2_FIELDS)
     print("\ntaylor_bar_full_100", json.dumps({"field_max": fm, "per_particle_floor_1e-3": pp}))
@@ -50,6 +59,20 @@ def test_taylor_bar_full_size_100_steps_vs_oracle(oracle_lib):
     # stated per-particle bound at this size: 2e-8 (floor 1e-3 of the field scale;
     # measured 5.0e-9, stress)
     assert max(pp.values()) <= 2e-8, pp
+
+
+def test_taylor_bar_full_size_fp32_error_stated(bar_100):
+    """The FP32-particle variant (FP64 nodes) on the same 100 steps against the
+    FP64 oracle: its error, per field, printed and bounded."""
+    mk, so = bar_100
+    g = MPMContext(mk(precision="f32"))
+    g.step(100)
+    sg = g.download_all()
+    g.close()
+    fm = {f: e for (_, f), e in field_errors(sg, so, fields=J2_FIELDS).items()}
+    pp = particle_errors(sg, so, fields=J2_FIELDS)
+    print("\ntaylor_bar_full_100_fp32", json.dumps({"field_max": fm, "per_particle_floor_1e-3": pp}))
+    assert max(fm.values()) <= 1e-2, fm
 
 
 @pytest.fixture(scope="module")
