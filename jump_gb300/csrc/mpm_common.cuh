@@ -267,6 +267,19 @@ __device__ __forceinline__ bool hat(const GridP& g, const R* x, Hat<D, R>& h) {
   return true;
 }
 
+// True when every axis has gl = -dxI and gh = +dxI exactly: the particle lies
+// strictly inside its cell (neither on a node line nor rounded past one), so
+// sums over the two nodes of an axis weighted by the gradient are dxI times a
+// difference.  Integer tests of the sign and zero bits.
+template <int D, class R>
+__device__ __forceinline__ bool hat_interior(const Hat<D, R>& h) {
+  bool in = true;
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+    in = in && is_neg_bits(h.gl[a]) && !is_zero_bits(h.gl[a]) && !is_neg_bits(h.gh[a]) && !is_zero_bits(h.gh[a]);
+  return in;
+}
+
 // Hat cache of particle p (PartP::hat_c / hat_nl).  The gradient factors are
 // 0 or -+dxI (neg_sign_scale), so two bits each restore them exactly, and the
 // upper value is recomputed with hat()'s rounding: hat_get gives bit for bit

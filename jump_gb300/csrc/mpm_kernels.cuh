@@ -10,6 +10,7 @@
 #pragma once
 
 #include <climits>
+#include <type_traits>
 
 #include "mpm_common.cuh"
 #include "mpm_sparse.cuh"
@@ -105,40 +106,71 @@ __device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& n
   if constexpr (D == 3) {
     // factored along z: per (x, y) corner pair the force coefficients
     // P_a = s_a0 Gx Ny + s_a1 Nx Gy (+ m g_a Nx Ny) and Q_a = s_a2 Nx Ny (s = -V sigma)
-    // give f_a = Nz P_a + Gz Q_a at both z corners
+    // give f_a = Nz P_a + Gz Q_a at both z corners.
+    // FAST (every lane of the warp strictly inside its cell, hat_interior, and no
+    // contact normals): the gradients are -dxI and +dxI, so s is scaled by dxI
+    // once per particle (c_ab = s_ab dxI_b), P_a = +-c_a0 Ny +- c_a1 Nx and
+    // Q_a = c_a2 Nx Ny, and each corner's force is the one FMA Nz P_a +- Q_a.
+    // The branch is uniform over the warp, so the shuffles of emit stay in step.
     const R mNz[2] = {m * h.Nl[2], m * h.Nh[2]};
+    auto corners3 = [&](auto fast_c) {
+      constexpr bool FAST = decltype(fast_c)::value;
+      R cs[3][3];
+      if constexpr (FAST) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int bx = q & 1, by = q >> 1;
-      const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
-      const R Gx = bx ? h.gh[0] : h.gl[0], Gy = by ? h.gh[1] : h.gl[1];
-      const R Nxy = Nx * Ny, GxNy = Gx * Ny, NxGy = Nx * Gy;
-      R P[3], Q[3];
+        for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        P[a] = ms[sym<3>(a, 0)] * GxNy + ms[sym<3>(a, 1)] * NxGy;
-        if (GRAV) P[a] += mg[a] * Nxy;
-        Q[a] = ms[sym<3>(a, 2)] * Nxy;
+          for (int b = 0; b < 3; ++b) cs[a][b] = ms[sym<3>(a, b)] * h.gh[b];  // gh = +dxI here
       }
 #pragma unroll
-      for (int bz = 0; bz < 2; ++bz) {
-        const R Nz = bz ? h.Nh[2] : h.Nl[2], Gz = bz ? h.gh[2] : h.gl[2];
-        R val[NV];
-        const R Nm = Nxy * mNz[bz];
-        val[0] = Nm;
+      for (int q = 0; q < 4; ++q) {
+        const int bx = q & 1, by = q >> 1;
+        const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
+        const R Gx = bx ? h.gh[0] : h.gl[0], Gy = by ? h.gh[1] : h.gl[1];
+        const R Nxy = Nx * Ny;
+        R P[3], Q[3], GxNy = R(0), NxGy = R(0);
+        if constexpr (FAST) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) val[1 + a] = Nm * v[a];
+          for (int a = 0; a < 3; ++a) {
+            P[a] = (bx ? cs[a][0] : -cs[a][0]) * Ny + (by ? cs[a][1] : -cs[a][1]) * Nx;
+            if (GRAV) P[a] += mg[a] * Nxy;
+            Q[a] = cs[a][2] * Nxy;
+          }
+        } else {
+          GxNy = Gx * Ny;
+          NxGy = Nx * Gy;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) val[4 + a] = P[a] * Nz + Q[a] * Gz;
-        // normals of the contact correction: sum m_p grad N (SolveExplicitFEMP3DContact.jl)
-        if (NRM) {
-          val[7] = GxNy * mNz[bz];
-          val[8] = NxGy * mNz[bz];
-          val[9] = (m * Nxy) * Gz;
+          for (int a = 0; a < 3; ++a) {
+            P[a] = ms[sym<3>(a, 0)] * GxNy + ms[sym<3>(a, 1)] * NxGy;
+            if (GRAV) P[a] += mg[a] * Nxy;
+            Q[a] = ms[sym<3>(a, 2)] * Nxy;
+          }
         }
-        emit(q + 4 * bz, val);
+#pragma unroll
+        for (int bz = 0; bz < 2; ++bz) {
+          const R Nz = bz ? h.Nh[2] : h.Nl[2], Gz = bz ? h.gh[2] : h.gl[2];
+          R val[NV];
+          const R Nm = Nxy * mNz[bz];
+          val[0] = Nm;
+#pragma unroll
+          for (int a = 0; a < 3; ++a) val[1 + a] = Nm * v[a];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            if constexpr (FAST) val[4 + a] = P[a] * Nz + (bz ? Q[a] : -Q[a]);
+            else val[4 + a] = P[a] * Nz + Q[a] * Gz;
+          }
+          // normals of the contact correction: sum m_p grad N (SolveExplicitFEMP3DContact.jl)
+          if (!FAST && NRM) {
+            val[7] = GxNy * mNz[bz];
+            val[8] = NxGy * mNz[bz];
+            val[9] = (m * Nxy) * Gz;
+          }
+          emit(q + 4 * bz, val);
+        }
       }
-    }
+    };
+    if (__all_sync(mask, !NRM && hat_interior<3, R>(h))) corners3(std::true_type{});
+    else corners3(std::false_type{});
   } else {
 #pragma unroll
     for (int k = 0; k < (1 << D); ++k) {
@@ -1003,26 +1035,57 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
   } else if constexpr (D == 3) {
     // factored along z: per (x, y) corner pair, Z0 = sum Nz vdt, Z1 = sum Gz vdt,
     // W = sum Nz dv over the two z corners, then x += Nx Ny Z0, v += Nx Ny W,
-    // L dt += (Gx Ny Z0, Nx Gy Z0, Nx Ny Z1)
+    // L dt += (Gx Ny Z0, Nx Gy Z0, Nx Ny Z1).
+    // Strictly inside the cell (hat_interior: gl = -dxI, gh = +dxI per axis):
+    // Z0 = vd0 + Nh_z (vd1 - vd0), Z1 = dxI_z (vd1 - vd0), and the gradient
+    // sums are signed sums of Ny Z0, Nx Z0 and Nx Ny (vd1 - vd0), each scaled by
+    // its dxI once after the corners.
+    if (hat_interior<3, R>(h)) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int bx = q & 1, by = q >> 1;
-      const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
-      const R Gx = bx ? h.gh[0] : h.gl[0], Gy = by ? h.gh[1] : h.gl[1];
-      const R Nxy = Nx * Ny, GxNy = Gx * Ny, NxGy = Nx * Gy;
-      const int64_t n0 = cr.node[q], n1 = cr.node[q + 4];
+      for (int q = 0; q < 4; ++q) {
+        const int bx = q & 1, by = q >> 1;
+        const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
+        const R Nxy = Nx * Ny;
+        const int64_t n0 = cr.node[q], n1 = cr.node[q + 4];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const R vd0 = nload<CG>(vdt_n + a * Nn + n0), vd1 = nload<CG>(vdt_n + a * Nn + n1);
-        const R dv0 = nload<CG>(dv_n + a * Nn + n0), dv1 = nload<CG>(dv_n + a * Nn + n1);
-        const R Z0 = h.Nl[2] * vd0 + h.Nh[2] * vd1;
-        const R Z1 = h.gl[2] * vd0 + h.gh[2] * vd1;
-        const R W = h.Nl[2] * dv0 + h.Nh[2] * dv1;
-        x[a] += Nxy * Z0;
-        v[a] += Nxy * W;
-        Ldt[a][0] += GxNy * Z0;
-        Ldt[a][1] += NxGy * Z0;
-        Ldt[a][2] += Nxy * Z1;
+        for (int a = 0; a < 3; ++a) {
+          const R vd0 = nload<CG>(vdt_n + a * Nn + n0), vd1 = nload<CG>(vdt_n + a * Nn + n1);
+          const R dv0 = nload<CG>(dv_n + a * Nn + n0), dv1 = nload<CG>(dv_n + a * Nn + n1);
+          const R dz = vd1 - vd0;
+          const R Z0 = vd0 + h.Nh[2] * dz;
+          const R W = h.Nl[2] * dv0 + h.Nh[2] * dv1;
+          x[a] += Nxy * Z0;
+          v[a] += Nxy * W;
+          Ldt[a][0] += (bx ? Ny : -Ny) * Z0;
+          Ldt[a][1] += (by ? Nx : -Nx) * Z0;
+          Ldt[a][2] += Nxy * dz;
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Ldt[a][j] *= h.gh[j];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int bx = q & 1, by = q >> 1;
+        const R Nx = bx ? h.Nh[0] : h.Nl[0], Ny = by ? h.Nh[1] : h.Nl[1];
+        const R Gx = bx ? h.gh[0] : h.gl[0], Gy = by ? h.gh[1] : h.gl[1];
+        const R Nxy = Nx * Ny, GxNy = Gx * Ny, NxGy = Nx * Gy;
+        const int64_t n0 = cr.node[q], n1 = cr.node[q + 4];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const R vd0 = nload<CG>(vdt_n + a * Nn + n0), vd1 = nload<CG>(vdt_n + a * Nn + n1);
+          const R dv0 = nload<CG>(dv_n + a * Nn + n0), dv1 = nload<CG>(dv_n + a * Nn + n1);
+          const R Z0 = h.Nl[2] * vd0 + h.Nh[2] * vd1;
+          const R Z1 = h.gl[2] * vd0 + h.gh[2] * vd1;
+          const R W = h.Nl[2] * dv0 + h.Nh[2] * dv1;
+          x[a] += Nxy * Z0;
+          v[a] += Nxy * W;
+          Ldt[a][0] += GxNy * Z0;
+          Ldt[a][1] += NxGy * Z0;
+          Ldt[a][2] += Nxy * Z1;
+        }
       }
     }
   } else {
