@@ -205,6 +205,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# Steps each Taylor-bar variant runs from the impact before the first error
+# (det F <= 0 at the crushed corner, or a particle leaving the grid), measured
+# on the GPU in steps of 25 (the FP64 J2 bar fails at the same step in the
+# oracle).  MUSL and the B-spline bases ran 2200 steps without one.  The late
+# window and the end-to-end solve stay within 80% of it.
+HEALTHY_STEPS = {("j2", "f64"): 1450, ("j2", "f32"): 925, ("jc", "f64"): 1250, ("jc", "f32"): 1250,
+                 ("jcdamage", "f64"): 200, ("jcdamage", "f32"): 100}
+
+
+def healthy_steps(args):
+    """Steps the workload runs before its first error, or None if it has no such limit here."""
+    if args.workload != "taylor_bar":
+        return None
+    if args.algorithm != "usl" or args.basis != "linear":
+        return 2200
+    return HEALTHY_STEPS.get((args.material, args.precision))
+
+
 def workload(name: str, material: str = "j2"):
     from jump_gb300 import scenarios
     if name == "taylor_bar":
@@ -382,10 +400,9 @@ def late_window(args, ctx, npart, advanced_before):
     mushrooming, plastically flowing phase (more active node blocks, more particles on
     the return-mapping branch, disordered particles), with the tuner re-run there.
     The default 1000 steps (about 11 us of the impact) stays inside the run's healthy
-    range: with the linear hat basis the crushed impact corner reaches det F <= 0 near
-    step 1450 and loses a particle off the grid near step 2000, in the oracle as on
-    the GPU.  With FP32 particles det F <= 0 comes near step 925, so the FP32 default
-    is 600 steps."""
+    range: with the linear hat basis the crushed impact corner of the J2 bar reaches
+    det F <= 0 near step 1450, in the oracle as on the GPU; other variants are capped
+    by HEALTHY_STEPS."""
     ctx.step(args.late_steps)  # untimed
     tuning = ctx.tune(3) if args.tune else None
     launch = ctx.launch()
@@ -468,7 +485,15 @@ def run_ours(args):
     step_bytes = table["step"] * npart
     late = None
     if world == 1 and args.workload == "taylor_bar" and args.late_steps > 0:
-        late = late_window(args, ctx, npart, args.warmup + args.steps + nprof)
+        used = args.warmup + args.steps + nprof
+        limit = healthy_steps(args)
+        room = int(0.8 * limit) - used - args.warmup - args.steps if limit else args.late_steps
+        if room >= 100:
+            args.late_steps = min(args.late_steps, room)
+            late = late_window(args, ctx, npart, used)
+        else:
+            late = {"skipped": f"the variant reaches its first error (det F <= 0 or a particle leaving the grid) "
+                               f"near step {limit}, too early for a late window"}
     ctx.close()
 
     # End to end through the public API: one solve of max(K, --e2e-steps) steps
@@ -493,7 +518,8 @@ def run_ours(args):
     c2 = MPMContext(desc)
     c2.set_launch(**launch)
     t1 = time.perf_counter()
-    e2e_steps = max(args.steps, args.e2e_steps)
+    limit = healthy_steps(args)
+    e2e_steps = max(args.steps, min(args.e2e_steps, int(0.8 * limit)) if limit else args.e2e_steps)
     recs, _ = c2.step_energies(e2e_steps, 1, 0)
     t2 = time.perf_counter()
     assert recs.shape[0] == e2e_steps and np.all(np.isfinite(recs))
@@ -937,20 +963,19 @@ def main():
                     help="ensembles: steps per solve (default 1000 two-disk, 200 impact); adjoint: steps (2000)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--late-steps", type=int, default=None,
-                    help="Taylor bar: steps advanced before the late-window measurement (0: none; default "
-                         "1000 with FP64 particles, 600 with FP32)")
+    ap.add_argument("--late-steps", type=int, default=1000,
+                    help="Taylor bar: steps advanced before the late-window measurement (0: none; capped so the "
+                         "window ends within 80%% of the steps the variant runs before its first error)")
     ap.add_argument("--adjoint-p2g", default=None, choices=["atomic", "warp", "tile", "tile_warp"],
                     help="adjoint: P2G strategy of its contexts (a tile one selects the tiled adjoint scatter)")
     ap.add_argument("--e2e-steps", type=int, default=500,
-                    help="Taylor bar: steps of the end-to-end solve (at least --steps)")
+                    help="Taylor bar: steps of the end-to-end solve (at least --steps; at most 80%% of the steps "
+                         "the variant runs before its first error)")
     ap.add_argument("--extras", action=argparse.BooleanOptionalAction, default=True,
                     help="Taylor bar, FP64, 1 GPU: add the ensemble, adjoint and impact-jvp sub-results")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.late_steps is None:
-        args.late_steps = 600 if args.precision == "f32" else 1000
     if args.impl == "reference":
         run_reference(args)
     elif args.workload in ENSEMBLES:
