@@ -306,6 +306,9 @@ int mpm_fwd_checkpointed(mpm_ctx* ctx, int64_t nsteps, int32_t checkpoint_every)
    The G2P adjoint scatters its node adjoints with FP64 atomics per particle
    at L2, or, when the context's P2G strategy is MPM_P2G_TILE or
    MPM_P2G_TILE_WARP, through a shared-memory tile of each CTA's node box.
+   A single-body context with the per-particle scatter runs each reversed step
+   as one cooperative launch whose grid barriers wait at most about one second
+   each; a wait that gives up makes the call return MPM_ERR_CUDA.
    The context is left at the final state of the forward run. */
 int mpm_bwd(mpm_ctx* ctx, const double* x_bar, const double* v_bar, double* E_bar, double* v0_bar,
             double* x0_bar);
