@@ -107,8 +107,8 @@ __device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& n
     // factored along z: per (x, y) corner pair the force coefficients
     // P_a = s_a0 Gx Ny + s_a1 Nx Gy (+ m g_a Nx Ny) and Q_a = s_a2 Nx Ny (s = -V sigma)
     // give f_a = Nz P_a + Gz Q_a at both z corners.
-    // FAST (every lane of the warp strictly inside its cell, hat_interior, and no
-    // contact normals): the gradients are -dxI and +dxI, so s is scaled by dxI
+    // FAST (every lane of the warp strictly inside its cell, hat_interior): the
+    // gradients are -dxI and +dxI, so s is scaled by dxI
     // once per particle (c_ab = s_ab dxI_b), P_a = +-c_a0 Ny +- c_a1 Nx and
     // Q_a = c_a2 Nx Ny, and each corner's force is the one FMA Nz P_a +- Q_a.
     // The branch is uniform over the warp, so the shuffles of emit stay in step.
@@ -136,6 +136,10 @@ __device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& n
             if (GRAV) P[a] += mg[a] * Nxy;
             Q[a] = cs[a][2] * Nxy;
           }
+          if (NRM) {  // the contact normals still take the gradient products
+            GxNy = Gx * Ny;
+            NxGy = Nx * Gy;
+          }
         } else {
           GxNy = Gx * Ny;
           NxGy = Nx * Gy;
@@ -160,7 +164,7 @@ __device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& n
             else val[4 + a] = P[a] * Nz + Q[a] * Gz;
           }
           // normals of the contact correction: sum m_p grad N (SolveExplicitFEMP3DContact.jl)
-          if (!FAST && NRM) {
+          if (NRM) {
             val[7] = GxNy * mNz[bz];
             val[8] = NxGy * mNz[bz];
             val[9] = (m * Nxy) * Gz;
@@ -169,7 +173,7 @@ __device__ __forceinline__ void p2g_corner_values(const GridP& g, const NodeP& n
         }
       }
     };
-    if (__all_sync(mask, !NRM && hat_interior<3, R>(h))) corners3(std::true_type{});
+    if (__all_sync(mask, hat_interior<3, R>(h))) corners3(std::true_type{});
     else corners3(std::false_type{});
   } else {
 #pragma unroll
