@@ -65,12 +65,15 @@ BYTES_JC = {"p2g": 112 + 7, "g2p": 488 + 6, "step": 560}
 BYTES_JCD = {"p2g": 112 + 7, "g2p": 544 + 6, "step": 616}
 
 
-def launches_per_run(args, nbodies):
+def launches_per_run(args, nbodies, p2g=None):
     """Kernels of the timed steps: USL clear + P2G per body + grid update (which
     lists the node blocks in the same launch) + G2P per body; MUSL: clear, P2G,
     compaction, its grid update, G2P-1 per body and, in 3D, the gradient
     velocity pass (2D: the solve and the node pass in place of the grid update);
-    a cell sort is a key pass per body, three scan passes and the scatter."""
+    a cell sort is a key pass per body, three scan passes and the scatter.  The
+    fused strategy runs all timed steps in one launch."""
+    if p2g == "fused":
+        return 1
     per_step = 2 + 2 * nbodies if args.algorithm == "usl" else 4 + 3 * nbodies
     sorts = args.steps // args.sort_interval if args.sort_interval > 0 else 0
     return args.steps * per_step + sorts * (nbodies + 4)
@@ -587,7 +590,7 @@ def run_ours(args):
                            "(mpm_step_energies: formed on the device, all records copied to the host at the end), "
                            "download all",
                     **parts},
-            "gpu_launches": launches_per_run(args, len(s)),
+            "gpu_launches": launches_per_run(args, len(s), launch["p2g"]),
             "clocks": clocks,
             "cpu_baseline": cpu,
             **extras,

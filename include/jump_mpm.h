@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 8
+#define JUMP_MPM_ABI_VERSION 9
 
 /* status codes */
 #define MPM_OK               0
@@ -250,24 +250,36 @@ int mpm_profile_stages(mpm_ctx* ctx, int64_t nsteps, double* stage_ms);
    down to 64 while the largest body would fill fewer than two CTAs per SM).  sort_interval: the
    counting sort by cell every that many steps (0: never); its second particle
    buffer is allocated on first use.  A negative argument keeps that setting.
+   MPM_P2G_FUSED runs every stage of every step of an mpm_step call in one
+   cooperative launch, the stages separated by grid barriers (each wait
+   bounded at about one second, after which the call returns MPM_ERR_CUDA),
+   with a dense reset of all nodes each step; it is for small problems, where a
+   step's four launches cost more than its work, and the default where it
+   applies: FP64, linear basis, USL, one velocity field, no rigid bodies, no
+   sort, at most MPM_BATCH_MAX_BODIES bodies of one type (linear elastic,
+   neo-Hookean or J2), at most MPM_FUSED_MAX_PARTICLES particles (elsewhere
+   MPM_ERR_ARG).
    Results differ between settings only by the summation order of node sums. */
 #define MPM_P2G_ATOMIC 0
 #define MPM_P2G_WARP   1
 #define MPM_P2G_TILE   2
 #define MPM_P2G_TILE_WARP 3
+#define MPM_P2G_FUSED 4
+#define MPM_FUSED_MAX_PARTICLES 2048
 int mpm_set_launch(mpm_ctx* ctx, int32_t p2g_strategy, int32_t threads, int32_t sort_interval);
 int mpm_get_launch(mpm_ctx* ctx, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval);
 /* Times probe_steps steps (rounded up to whole sort intervals, so that every
    probe pays its share of sorts) of every combination of P2G strategy
-   {atomic, warp, tile, tile_warp},
+   {atomic, warp, tile, tile_warp} (and MPM_P2G_FUSED where it applies),
    threads {64, 128, 256} and sort interval {0, 1, 4, 16}, each from the same saved
    particle state, keeps the fastest (reported through the non-NULL pointers,
    with its ms per step) and puts the particle state back: the simulation does
    not advance.  Uses a temporary device copy of the particle state.  If
    all_ms is not NULL it receives the ms per step of all MPM_TUNE_CANDIDATES
    combinations, index (strategy * 3 + threads index) * 4 + sort index (a
-   negative value: not probed).  The reverse mode needs sort_interval 0. */
-#define MPM_TUNE_CANDIDATES 48
+   negative value: not probed), and at index 48 that of MPM_P2G_FUSED
+   where it applies.  The reverse mode needs sort_interval 0. */
+#define MPM_TUNE_CANDIDATES 49
 int mpm_tune(mpm_ctx* ctx, int64_t probe_steps, int32_t* p2g_strategy, int32_t* threads, int32_t* sort_interval,
              double* ms_per_step, double* all_ms);
 

@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-ABI_VERSION = 8  # JUMP_MPM_ABI_VERSION of the structures below
+ABI_VERSION = 9  # JUMP_MPM_ABI_VERSION of the structures below
 
 MPM_OK = 0
 MPM_ERR_ARG = 1
@@ -54,11 +54,13 @@ MPM_BASIS_LINEAR = 0
 MPM_BASIS_QUAD_BSPLINE = 1
 MPM_BASIS_CUBIC_BSPLINE = 2
 
-MPM_TUNE_CANDIDATES = 48
+MPM_TUNE_CANDIDATES = 49
 MPM_P2G_ATOMIC = 0
 MPM_P2G_WARP = 1
 MPM_P2G_TILE = 2
 MPM_P2G_TILE_WARP = 3
+MPM_P2G_FUSED = 4
+MPM_FUSED_MAX_PARTICLES = 2048
 
 MPM_BATCH_PERSISTENT = 0
 MPM_BATCH_WIDE = 1

@@ -801,6 +801,125 @@ int status_code(unsigned st) {
 
 }  // namespace
 
+namespace jmpm {
+
+// MPM_P2G_FUSED: nsteps USL steps of one small FP64 problem of a context in a
+// single cooperative launch.  Per step: P2G, grid update, G2P (with the reset
+// of the node accumulators for the next step), separated by grid barriers
+// (grid_barrier: bounded waits that set q.bar[2] and end the kernel).  Thread
+// t handles particles t, t + nthreads, ... in both particle stages, so a
+// particle's fields are only ever read on the SM that wrote them; node values
+// written in the launch by other CTAs are read through L2 (grid_node and
+// g2p_particle with CG, P2G through atomics).
+struct FusedP {
+  GridP g;
+  NodeP nd;
+  void* P;
+  int64_t pitch, np;
+  int nb;
+  int64_t bbeg[MPM_BATCH_MAX_BODIES];
+  MatParams mp[MPM_BATCH_MAX_BODIES];
+  double dt, tol, grav[3];
+  unsigned* status;
+  unsigned* bar;  // [0] arrivals, [1] generation, [2] a barrier wait gave up
+};
+
+template <int D, int MAT, bool GRAV>
+__global__ void __launch_bounds__(128) fused_steps_kernel(FusedP q, int64_t nsteps) {
+  const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t nth = int64_t(gridDim.x) * blockDim.x;
+  unsigned* err = q.bar + 2;
+  if (*reinterpret_cast<volatile unsigned*>(err)) return;  // an earlier wait gave up
+  const PartP all{q.P, q.pitch, 0, q.np};
+  const int64_t Nn = q.nd.nodeCount;
+  auto reset = [&]() {
+    for (int64_t i = tid; i < Nn; i += nth) {
+      q.nd.m[i] = 0.0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        q.nd.p0[a * Nn + i] = 0.0;
+        q.nd.f[a * Nn + i] = 0.0;
+      }
+    }
+  };
+  reset();
+  if (!grid_barrier(q.bar, err)) return;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    // P2G: every lane of a warp calls it the same number of times
+    for (int64_t base = 0; base < q.np; base += nth)
+      p2g_particle<D, double, GRAV, false>(q.g, q.nd, all, base + tid, q.grav[0], q.grav[1], q.grav[2], q.status);
+    if (!grid_barrier(q.bar, err)) return;
+    for (int64_t i = tid; i < Nn; i += nth) grid_node<D, false, true>(q.nd, i, q.dt, q.tol);
+    if (!grid_barrier(q.bar, err)) return;
+    for (int64_t p = tid; p < q.np; p += nth) {
+      int b = 0;
+      while (b + 1 < q.nb && p >= q.bbeg[b + 1]) ++b;
+      const PartP pb{q.P, q.pitch, q.bbeg[b], q.np - q.bbeg[b]};
+      g2p_particle<D, double, MAT, true>(q.g, q.nd, pb, p - q.bbeg[b], q.mp[b], q.dt, q.status);
+    }
+    if (s + 1 < nsteps) reset();  // G2P reads vdt and dv only: the accumulators are free
+    if (!grid_barrier(q.bar, err)) return;
+  }
+}
+
+template <int D, int MAT, bool GRAV>
+static const void* fused_fn() {
+  return reinterpret_cast<const void*>(fused_steps_kernel<D, MAT, GRAV>);
+}
+
+static const void* fused_kernel_for(int dim, int mat, bool grav) {
+#define JMPM_FK(D)                                                                                   \
+  (mat == MPM_MAT_ELASTIC ? (grav ? fused_fn<D, MPM_MAT_ELASTIC, true>() : fused_fn<D, MPM_MAT_ELASTIC, false>()) \
+   : mat == MPM_MAT_NEOHOOKEAN                                                                       \
+       ? (grav ? fused_fn<D, MPM_MAT_NEOHOOKEAN, true>() : fused_fn<D, MPM_MAT_NEOHOOKEAN, false>())   \
+       : (grav ? fused_fn<D, MPM_MAT_J2, true>() : fused_fn<D, MPM_MAT_J2, false>()))
+  return dim == 2 ? JMPM_FK(2) : JMPM_FK(3);
+#undef JMPM_FK
+}
+
+size_t fused_bytes() { return 4 * sizeof(unsigned); }
+
+int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
+                int nb, const int64_t* bbeg, const int64_t* bcnt, const MatParams* mp, double dt, double tol,
+                const double* grav, int64_t nsteps, unsigned* status) {
+  if (nb < 1 || nb > MPM_BATCH_MAX_BODIES) return fail(MPM_ERR_ARG, "fused_steps: body count");
+  FusedP q{};
+  q.g = g;
+  q.nd = nd;
+  q.nd.bflag = nullptr;  // the dense reset of every step needs no block list
+  q.nd.rmask = nullptr;
+  q.P = P;
+  q.pitch = pitch;
+  q.np = 0;
+  q.nb = nb;
+  for (int b = 0; b < nb; ++b) {
+    q.bbeg[b] = bbeg[b];
+    q.mp[b] = mp[b];
+    q.np += bcnt[b];
+  }
+  q.dt = dt;
+  q.tol = tol;
+  for (int a = 0; a < 3; ++a) q.grav[a] = grav[a];
+  q.status = status;
+  q.bar = static_cast<unsigned*>(dev);
+  const bool gr = grav[0] != 0.0 || grav[1] != 0.0 || (dim == 3 && grav[2] != 0.0);
+  const void* fn = fused_kernel_for(dim, mp[0].type, gr);
+  // 64-thread CTAs, one per SM at most, no more than the particles need
+  int devid = 0, sms = 0, per = 0;
+  BATCH_TRY(cudaGetDevice(&devid));
+  BATCH_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, devid));
+  BATCH_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 64, 0));
+  if (per < 1) return fail(MPM_ERR_CUDA, "fused_steps: the kernel does not fit on an SM");
+  const int64_t want = std::max<int64_t>(1, (q.np + 63) / 64);
+  const unsigned nblk = unsigned(std::min<int64_t>(want, int64_t(sms)));
+  BATCH_TRY(cudaMemsetAsync(q.bar, 0, 3 * sizeof(unsigned), s));
+  void* args[] = {&q, &nsteps};
+  BATCH_TRY(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(64), args, 0, s));
+  return MPM_OK;
+}
+
+}  // namespace jmpm
+
 extern "C" {
 
 int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t precision, mpm_batch** out) {

@@ -94,6 +94,8 @@ struct mpm_ctx {
   double* adjbuf = nullptr;
   double* nodeadj = nullptr;
   unsigned* revbar = nullptr;  // fused reverse step: barrier arrivals, generation, error flag
+  void* fused = nullptr;       // barrier words of the fused steps (MPM_P2G_FUSED)
+  bool full_clear = false;     // the node accumulators need a dense clear before the next graph step
   bool coop_off = false;       // the fused reverse step could not be captured: three kernels per step
   ContactP cp{};                 // contact mode: per-body node fields
   double* contactbuf = nullptr;
@@ -227,6 +229,7 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->adjbuf);
   cudaFree(c->nodeadj);
   cudaFree(c->revbar);
+  cudaFree(c->fused);
   cudaFree(c->contactbuf);
   cudaFree(c->contactbuf_f);
   cudaFree(c->status);
@@ -395,6 +398,13 @@ void enqueue_musl(mpm_ctx* c, cudaEvent_t* ev) {
   if (ev) cudaEventRecord(ev[3], c->stream);
 }
 
+// P2G strategy of the per-stage launches: MPM_P2G_FUSED contexts that take
+// the per-stage path (checkpointed forward, stage profiling, the reverse
+// sweep's recompute) use per-particle atomics there
+static int graph_strategy(const mpm_ctx* c) {
+  return c->p2g_strategy == MPM_P2G_FUSED ? MPM_P2G_ATOMIC : c->p2g_strategy;
+}
+
 // The launches of one step's kernels (enqueue_step).
 static void enqueue_step_kernels(mpm_ctx* c, cudaEvent_t* ev, double* rec) {
   if (c->prm.algorithm == MPM_ALG_MUSL) {
@@ -420,10 +430,10 @@ static void enqueue_step_kernels(mpm_ctx* c, cudaEvent_t* ev, double* rec) {
       else Launchers<3>::bs_p2g(c->stream, c->g, field_of(b), c->part(b), c->f32, c->prm.body_force, c->status, basis);
     } else if (D == 2) {
       Launchers<2>::p2g(c->stream, c->g, field_of(b), c->step_part(b), c->f32, c->prm.body_force, c->status,
-                        c->p2g_strategy, c->threads);
+                        graph_strategy(c), c->threads);
     } else {
       Launchers<3>::p2g(c->stream, c->g, field_of(b), c->step_part(b), c->f32, c->prm.body_force, c->status,
-                        c->p2g_strategy, c->threads);
+                        graph_strategy(c), c->threads);
     }
   }
   // rigid solids: mark the nodes the grid update overrides, then move them
@@ -701,7 +711,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   }
   c->ncells = 1;
   for (int a = 0; a < D; ++a) c->ncells *= uint32_t(nn[a] - 1);
-  c->p2g_strategy = c->f32 ? MPM_P2G_WARP : MPM_P2G_ATOMIC;
+  c->p2g_strategy = c->f32 ? MPM_P2G_WARP : MPM_P2G_ATOMIC;  // MPM_P2G_FUSED where it fits: set at the end
   c->threads = spread_threads(maxn);  // small bodies: smaller CTAs, spread over the SMs
   if (prm->sort_interval > 0 && c->np > 0) {
     int r = alloc_sort(c);
@@ -788,6 +798,8 @@ int mpm_abi_version(void) { return JUMP_MPM_ABI_VERSION; }
 
 const char* mpm_last_error(void) { return g_err.c_str(); }
 
+static bool fused_fits(const mpm_ctx* c, int sort_interval);
+
 int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t nbodies,
                const mpm_params* params, mpm_ctx** out) {
   if (!grid || !params || !out) return fail(MPM_ERR_ARG, "mpm_create: null argument");
@@ -853,7 +865,56 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
     g_err = msg;
     return r;
   }
+  if (fused_fits(c, c->prm.sort_interval)) c->p2g_strategy = MPM_P2G_FUSED;
   *out = c;
+  return MPM_OK;
+}
+
+// MPM_P2G_FUSED applies to small FP64 problems whose whole step costs less
+// than its four launches: linear-basis USL, one velocity field, no rigid
+// bodies, no cell sort (sort_interval as given), at most MPM_BATCH_MAX_BODIES
+// bodies of one material type (linear elastic, neo-Hookean or J2), at most
+// MPM_FUSED_MAX_PARTICLES particles.  mpm_step and mpm_step_energies then run
+// their steps in one cooperative launch (fused_steps), whose reset of every
+// step is dense.
+static bool fused_fits(const mpm_ctx* c, int sort_interval) {
+  if (c->f32 || c->np == 0 || c->np > MPM_FUSED_MAX_PARTICLES || c->prm.algorithm != MPM_ALG_USL ||
+      c->prm.basis != MPM_BASIS_LINEAR || c->prm.contact || sort_interval > 0 || c->nb > MPM_BATCH_MAX_BODIES)
+    return false;
+  const int t0 = c->mats[0].type;
+  for (int b = 0; b < c->nb; ++b) {
+    const int t = c->mats[b].type;
+    if (c->rigid(b) || t != t0 || (t != MPM_MAT_ELASTIC && t != MPM_MAT_NEOHOOKEAN && t != MPM_MAT_J2)) return false;
+  }
+  return true;
+}
+
+// n steps on the fused path; the next per-stage step clears every node first
+static int fused_run(mpm_ctx* c, int64_t n) {
+  if (n <= 0) return MPM_OK;
+  if (!c->fused) CUDA_TRY(cudaMalloc(&c->fused, fused_bytes()));
+  int r = fused_steps(c->dim, c->stream, c->fused, c->g, c->nd, c->P, c->np, c->nb, c->off.data(), c->cnt.data(),
+                      c->mats.data(), c->prm.dt, c->prm.tolerance, c->prm.body_force, n, c->status);
+  c->full_clear = true;
+  return r;
+}
+
+// after the fused steps' barrier words: MPM_ERR_CUDA if a wait gave up (the
+// stream has synchronised)
+static int fused_check(mpm_ctx* c) {
+  if (!c->fused) return MPM_OK;
+  unsigned w[3] = {0, 0, 0};
+  CUDA_TRY(cudaMemcpy(w, c->fused, sizeof(w), cudaMemcpyDeviceToHost));
+  if (w[2]) return fail(MPM_ERR_CUDA, "a grid barrier of the fused steps gave up after one second");
+  return MPM_OK;
+}
+
+// after fused steps the block list of the sparse clear is stale: clear
+// m, p0 and f of every node before the next step that uses it
+static int clear_if_stale(mpm_ctx* c) {
+  if (!c->full_clear) return MPM_OK;
+  CUDA_TRY(cudaMemsetAsync(c->nodebuf, 0, size_t(c->nd.nodeCount) * (1 + 2 * c->dim) * sizeof(double), c->stream));
+  c->full_clear = false;
   return MPM_OK;
 }
 
@@ -861,6 +922,7 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
 // buffer in use (captured on first use)
 static int launch_one_step(mpm_ctx* c, bool en = false) {
   int r;
+  if ((r = clear_if_stale(c))) return r;
   if (c->Palt && c->prm.sort_interval > 0 && c->since_sort >= c->prm.sort_interval && (r = enqueue_sort(c)))
     return r;
   if ((r = build_step_graph(c, en))) return r;
@@ -874,10 +936,17 @@ int mpm_step(mpm_ctx* c, int64_t nsteps, double* t_inout) {
   if (nsteps < 0) return fail(MPM_ERR_ARG, "mpm_step: nsteps < 0");
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CUDA_TRY(cudaEventRecord(c->e0, c->stream));
-  for (int64_t k = 0; k < nsteps; ++k) {
+  if (c->p2g_strategy == MPM_P2G_FUSED) {
     int r;
-    if ((r = launch_one_step(c))) return r;
-    if (t_inout) *t_inout += c->prm.dt;
+    if ((r = fused_run(c, nsteps))) return r;
+    if (t_inout)
+      for (int64_t k = 0; k < nsteps; ++k) *t_inout += c->prm.dt;
+  } else {
+    for (int64_t k = 0; k < nsteps; ++k) {
+      int r;
+      if ((r = launch_one_step(c))) return r;
+      if (t_inout) *t_inout += c->prm.dt;
+    }
   }
   CUDA_TRY(cudaEventRecord(c->e1, c->stream));
   unsigned st = 0;
@@ -886,6 +955,10 @@ int mpm_step(mpm_ctx* c, int64_t nsteps, double* t_inout) {
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
   c->last_ms = ms;
+  if (c->p2g_strategy == MPM_P2G_FUSED) {
+    int r = fused_check(c);
+    if (r) return r;
+  }
   return status_to_code(st);
 }
 
@@ -922,14 +995,31 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CUDA_TRY(cudaEventRecord(c->e0, c->stream));
   int64_t j = 0;
+  const bool one = c->p2g_strategy == MPM_P2G_FUSED;
+  int64_t pending = 0;  // fused steps not yet launched (one launch per run between records)
   for (int64_t k = 0; k < nsteps; ++k) {
     int r;
     const bool recd = k >= first && (k - first) % every == 0;
-    if ((r = launch_one_step(c, in_graph && recd))) return r;
+    if (one) {
+      ++pending;
+      if (recd) {
+        if ((r = fused_run(c, pending))) return r;
+        pending = 0;
+        if (D == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, nullptr, c->en_rec);
+        else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, nullptr, c->en_rec);
+        CUDA_TRY(cudaGetLastError());
+      }
+    } else if ((r = launch_one_step(c, in_graph && recd))) {
+      return r;
+    }
     if (t_inout) *t_inout += c->prm.dt;
     if (recd && !in_graph)  // no particles: zero sums
       CUDA_TRY(cudaMemsetAsync(c->rec_dev + size_t(j) * (2 + D), 0, (2 + D) * sizeof(double), c->stream));
     if (recd) ++j;
+  }
+  if (one && pending > 0) {
+    int r;
+    if ((r = fused_run(c, pending))) return r;
   }
   if (nrec > 0)
     CUDA_TRY(cudaMemcpyAsync(c->rec_host, c->rec_dev, size_t(nrec) * (2 + D) * sizeof(double),
@@ -941,22 +1031,33 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
   c->last_ms = ms;
+  if (one) {
+    int r = fused_check(c);
+    if (r) return r;
+  }
   if (nrec > 0) std::memcpy(out, c->rec_host, size_t(nrec) * (2 + D) * sizeof(double));
   return status_to_code(st);
 }
 
 int mpm_set_launch(mpm_ctx* c, int32_t p2g_strategy, int32_t threads, int32_t sort_interval) {
   if (!c) return fail(MPM_ERR_ARG, "mpm_set_launch: null context");
-  if (p2g_strategy > MPM_P2G_TILE_WARP)
+  if (p2g_strategy > MPM_P2G_FUSED)
     return fail(MPM_ERR_ARG, "mpm_set_launch: unknown P2G strategy");
   if (threads >= 0 && (threads < 32 || threads > 256 || threads % 32 != 0))
     return fail(MPM_ERR_ARG, "mpm_set_launch: threads must be a multiple of 32 in 32 .. 256");
+  const int new_sort = sort_interval >= 0 ? sort_interval : c->prm.sort_interval;
+  if (p2g_strategy == MPM_P2G_FUSED && !fused_fits(c, new_sort))
+    return fail(MPM_ERR_ARG, "mpm_set_launch: MPM_P2G_FUSED needs an FP64 linear-basis USL problem of at most "
+                             "MPM_FUSED_MAX_PARTICLES particles, one velocity field, no rigid bodies, no sort and "
+                             "one material type (linear elastic, neo-Hookean or J2)");
   if (sort_interval > 0 && !c->Palt) {
     int r = alloc_sort(c);
     if (r != MPM_OK) return r;
   }
   CUDA_TRY(cudaStreamSynchronize(c->stream));  // captured graphs may still run
   if (p2g_strategy >= 0) c->p2g_strategy = p2g_strategy;
+  // a sort switched on under the default fused strategy: per-stage launches
+  if (c->p2g_strategy == MPM_P2G_FUSED && !fused_fits(c, new_sort)) c->p2g_strategy = MPM_P2G_ATOMIC;
   if (threads >= 0) c->threads = threads;
   if (sort_interval >= 0) {
     if (sort_interval > 0 && c->prm.sort_interval != sort_interval) c->since_sort = sort_interval;  // sort next step
@@ -1041,6 +1142,31 @@ int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* th
           bt = th;
           bi = si;
         }
+      }
+    }
+  }
+  // MPM_P2G_FUSED where it fits (candidate 48), from the same saved state
+  if (rc == MPM_OK && fused_fits(c, 0)) {
+    c->prm.sort_interval = 0;
+    if ((rc = restore()) == MPM_OK) rc = fused_run(c, 1);  // allocates its scratch outside the clock
+    if (rc == MPM_OK) {
+      CUDA_TRY(cudaEventRecord(c->e0, c->stream));
+      rc = fused_run(c, probe_steps);
+      CUDA_TRY(cudaEventRecord(c->e1, c->stream));
+      cudaError_t e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) rc = fail(MPM_ERR_CUDA, std::string("mpm_tune: ") + cudaGetErrorString(e));
+      if (rc == MPM_OK) rc = fused_check(c);
+    }
+    if (rc == MPM_OK) {
+      float ms = 0.f;
+      CUDA_TRY(cudaEventElapsedTime(&ms, c->e0, c->e1));
+      const double per = double(ms) / double(probe_steps);
+      if (all_ms) all_ms[48] = per;
+      if (per < best) {
+        best = per;
+        bs = MPM_P2G_FUSED;
+        bt = saved_t;
+        bi = 0;
       }
     }
   }
@@ -1241,7 +1367,7 @@ int mpm_profile_stages(mpm_ctx* c, int64_t nsteps, double* stage_ms) {
   cudaEvent_t ev[5];
   for (int i = 0; i < 5; ++i) CUDA_TRY(cudaEventCreate(&ev[i]));
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
-  int rc = MPM_OK;
+  int rc = clear_if_stale(c);
   for (int64_t k = 0; k < nsteps && rc == MPM_OK; ++k) {
     cudaEventRecord(ev[4], c->stream);
     enqueue_step(c, ev);
@@ -1307,6 +1433,7 @@ int mpm_fwd_checkpointed(mpm_ctx* c, int64_t nsteps, int32_t every) {
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CUDA_TRY(cudaMemcpyAsync(c->ckpt, c->P, bytes, cudaMemcpyDeviceToDevice, c->stream));
   int r;
+  if ((r = clear_if_stale(c))) return r;
   if ((r = build_step_graph(c))) return r;
   for (int64_t k = 1; k <= nsteps; ++k) {
     CUDA_TRY(cudaGraphLaunch(c->exec[c->cur], c->stream));

@@ -76,6 +76,17 @@ inline int spread_threads(int64_t n) {
   return th;
 }
 
+// MPM_P2G_FUSED (mpm_batch.cu): nsteps USL steps of one FP64 problem of a
+// context in one cooperative launch, stages separated by bounded grid
+// barriers: linear basis, one velocity field, no rigid bodies, every body
+// linear elastic, neo-Hookean or J2 of one type, at most MPM_BATCH_MAX_BODIES
+// bodies.  dev: device scratch of fused_bytes() bytes, whose third word is set
+// when a barrier wait gave up (read it after the stream synchronises).
+size_t fused_bytes();
+int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
+                int nb, const int64_t* bbeg, const int64_t* bcnt, const MatParams* mp, double dt, double tol,
+                const double* grav, int64_t nsteps, unsigned* status);
+
 // deformable material model types a context or batch accepts in dimension dim
 // (rigid bodies, MPM_MAT_RIGID, are checked separately: contexts only)
 inline bool material_ok(int type, int dim) {

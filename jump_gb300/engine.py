@@ -207,11 +207,12 @@ class MPMContext(_ContextBase):
         return out, (tt.value if t is not None else rc)
 
     P2G_STRATEGIES = {"atomic": _capi.MPM_P2G_ATOMIC, "warp": _capi.MPM_P2G_WARP, "tile": _capi.MPM_P2G_TILE,
-                      "tile_warp": _capi.MPM_P2G_TILE_WARP}
+                      "tile_warp": _capi.MPM_P2G_TILE_WARP, "fused": _capi.MPM_P2G_FUSED}
 
     def set_launch(self, p2g: str | None = None, threads: int | None = None, sort_interval: int | None = None):
-        """P2G strategy ("atomic", "warp", "tile", "tile_warp"), CTA size of P2G and G2P, cell-sort
-        interval; None keeps a setting."""
+        """P2G strategy ("atomic", "warp", "tile", "tile_warp"; "fused": every stage of every step in
+        one cooperative launch, for small problems), CTA size of P2G and G2P, cell-sort interval;
+        None keeps a setting."""
         s = -1 if p2g is None else self.P2G_STRATEGIES[p2g]
         _capi.check(self.L.mpm_set_launch(self.h, s, -1 if threads is None else int(threads),
                                           -1 if sort_interval is None else int(sort_interval)), self.L)
@@ -230,11 +231,13 @@ class MPMContext(_ContextBase):
         _capi.check(self.L.mpm_tune(self.h, int(probe_steps), C.byref(s), C.byref(t), C.byref(i), C.byref(ms),
                                     _capi.dptr(allms)), self.L)
         probes = {}
-        for q, v in enumerate(allms):
+        for q, v in enumerate(allms[:48]):
             p2g, th, si = ("atomic", "warp", "tile", "tile_warp")[q // 12], (64, 128, 256)[(q // 4) % 3], \
                 (0, 1, 4, 16)[q % 4]
             if v >= 0:
                 probes[f"{p2g}/{th}/{si}"] = float(v)
+        if allms[48] >= 0:
+            probes["fused"] = float(allms[48])
         return dict(self.launch(), ms_per_step=ms.value, probes=probes)
 
     def _download(self, s, view):

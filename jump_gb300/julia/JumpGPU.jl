@@ -29,7 +29,7 @@ using Grid, Solid, Material, Algorithm, Basis, Fix, Dirichlet, Output
 import Problem
 
 const lib = normpath(joinpath(@__DIR__, "..", "lib", "libjumpmpm.so"))
-const ABI = 8  # JUMP_MPM_ABI_VERSION of the structures below
+const ABI = 9  # JUMP_MPM_ABI_VERSION of the structures below
 
 function __init__()
     v = ccall((:mpm_abi_version, lib), Cint, ())

@@ -34,7 +34,7 @@ def test_every_declared_symbol_is_exported(L):
 
 
 def test_abi_version(L):
-    assert L.mpm_abi_version() == _capi.ABI_VERSION == 8
+    assert L.mpm_abi_version() == _capi.ABI_VERSION == 9
 
 
 def test_argument_errors_without_gpu(L):

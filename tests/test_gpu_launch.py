@@ -1,6 +1,7 @@
 """Launch configuration and its tuner: the P2G strategies (per-lane atomics,
-warp-segmented sums, and both staged in shared-memory node tiles, with the
-per-particle fallback of a CTA whose box exceeds the tile), CTA sizes and
+warp sums over __match_any_sync groups, and both staged in shared-memory node
+tiles, with the per-particle fallback of a CTA whose box exceeds the tile; and
+for small problems every stage of every step in one cooperative launch), CTA sizes and
 cell-sort intervals change only the
 summation order of node sums, so every combination matches the oracle; the
 sort can be switched on at run time; mpm_tune keeps the fastest combination
@@ -131,8 +132,9 @@ def test_tune_keeps_the_state(precision):
     a.step(10)
     before = a.download_all()
     res = a.tune(3)
-    assert res["p2g"] in ("atomic", "warp", "tile", "tile_warp") and res["threads"] in (64, 128, 256)
-    assert len(res["probes"]) == 48
+    assert res["p2g"] in ("atomic", "warp", "tile", "tile_warp", "fused") and res["threads"] in (64, 128, 256)
+    # the fused candidate where it applies (FP64 problems of at most 2048 particles)
+    assert len(res["probes"]) == (49 if precision == "f64" else 48)
     assert res["sort_interval"] in (0, 1, 4, 16) and res["ms_per_step"] > 0
     errs = field_errors(a.download_all(), before)
     assert max(errs.values()) == 0.0, worst(errs)  # tuning does not advance the simulation
@@ -145,9 +147,59 @@ def test_tune_keeps_the_state(precision):
 def test_set_launch_rejects_bad_arguments():
     c = MPMContext(mk(disks()))
     before = c.launch()
-    assert before == {"p2g": "atomic", "threads": 64, "sort_interval": 0}  # 416 particles: small CTAs
+    assert before == {"p2g": "fused", "threads": 64, "sort_interval": 0}  # 416 particles: the fused default
     L = _capi.lib()
     assert L.mpm_set_launch(c.h, 7, -1, -1) == _capi.MPM_ERR_ARG
     assert L.mpm_set_launch(c.h, -1, 100, -1) == _capi.MPM_ERR_ARG
     assert L.mpm_set_launch(c.h, -1, 512, -1) == _capi.MPM_ERR_ARG
     assert c.launch() == before
+
+
+def test_fused_strategy_default_and_vs_oracle(oracle_lib):
+    """A small FP64 problem defaults to the fused strategy (every stage of
+    every step in one cooperative launch); it matches the oracle, and the per-stage
+    launches on the same problem to summation order."""
+    prob = disks()
+    c, a, o = MPMContext(mk(prob)), MPMContext(mk(prob)), oracle_lib.OracleContext(mk(prob))
+    assert c.launch()["p2g"] == "fused"
+    a.set_launch(p2g="atomic")
+    for ctx in (c, a, o):
+        ctx.step(60)
+    so = o.download_all()
+    errs = field_errors(c.download_all(), so)
+    assert max(errs.values()) <= FP64_TOL, worst(errs)
+    errs = field_errors(c.download_all(), a.download_all())
+    assert max(errs.values()) <= 1e-12, worst(errs)
+    # the grid arrays after a fused step equal those after per-stage steps
+    ng = prob[0].nodeCount
+    for x, y in zip(c.download_grid(ng), a.download_grid(ng)):
+        assert np.max(np.abs(x - y)) <= 1e-12 * max(np.max(np.abs(y)), 1e-300)
+
+
+def test_fused_then_per_stage_steps(oracle_lib):
+    """Steps alternating between the fused strategy and per-stage launches
+    (the dense reset of the fused steps leaves the per-stage block list stale;
+    the next per-stage step clears every node first) match the oracle."""
+    prob = disks()
+    c, o = MPMContext(mk(prob)), oracle_lib.OracleContext(mk(prob))
+    for k, p2g in enumerate(("fused", "atomic", "fused", "warp", "fused", "tile")):
+        c.set_launch(p2g=p2g)
+        c.step(10 + k)
+        o.step(10 + k)
+    errs = field_errors(c.download_all(), o.download_all())
+    assert max(errs.values()) <= FP64_TOL, worst(errs)
+
+
+def test_fused_rules():
+    """The fused strategy is refused where it does not apply; a sort
+    switched on under it moves the context to per-stage launches."""
+    f32 = MPMContext(mk(bar(), precision="f32"))  # FP32 particles: per-stage launches only
+    assert f32.launch()["p2g"] != "fused"
+    with pytest.raises(_capi.MPMError):
+        f32.set_launch(p2g="fused")
+    small = MPMContext(mk(disks()))
+    small.set_launch(sort_interval=3)
+    assert small.launch() == {"p2g": "atomic", "threads": small.launch()["threads"], "sort_interval": 3}
+    with pytest.raises(_capi.MPMError):
+        small.set_launch(p2g="fused")
+    small.step(5)
