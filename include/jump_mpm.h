@@ -198,8 +198,9 @@ int mpm_step(mpm_ctx* ctx, int64_t nsteps, double* t_inout);
    SolveExplicitSolidMechanics2D.jl:574-578 when first = (-counter0) mod every.
    Record r goes to out[(2 + dim) r ...]: kinetic energy, strain energy, momentum
    (dim).  Each record is formed on the device in its own slot, with no host
-   synchronisation between steps, and all of them are copied to the host in
-   one transfer after the last step; the call returns then, like mpm_step.  out may be any host memory
+   synchronisation between steps (under MPM_P2G_FUSED every step and record of
+   the call in one launch), and all of them are copied to the host in one
+   transfer after the last step; the call returns then, like mpm_step.  out may be any host memory
    ((nsteps - 1 - first)/every + 1 records when nsteps > first). */
 int mpm_step_energies(mpm_ctx* ctx, int64_t nsteps, int64_t every, int64_t first, double* t_inout, double* out);
 

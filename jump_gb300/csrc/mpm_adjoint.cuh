@@ -740,15 +740,18 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err) {
       __threadfence();
       atomicAdd(bar + 1, 1u);
     } else {
+      // spin on the generation; the clock is read every 16 polls
       unsigned long long t0, t1;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      unsigned polls = 0;
       while (*gen == g) {
-        __nanosleep(64);
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
-        if (t1 - t0 > 1000000000ull) {
-          atomicOr(err, 1u);
-          ok = 0;
-          break;
+        if ((++polls & 15u) == 0u) {
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+          if (t1 - t0 > 1000000000ull) {
+            atomicOr(err, 1u);
+            ok = 0;
+            break;
+          }
         }
       }
     }

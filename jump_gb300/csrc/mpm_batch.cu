@@ -822,6 +822,11 @@ struct FusedP {
   double dt, tol, grav[3];
   unsigned* status;
   unsigned* bar;  // [0] arrivals, [1] generation, [2] a barrier wait gave up
+  // EnergiesFix records after steps first, first + every, ... (rec non-null):
+  // per-CTA partial sums, folded by CTA 0 in a fixed order into rec->base[rec->idx++]
+  EnRec* rec;
+  int64_t first, every;
+  double* partial;  // (2 + D) doubles per CTA
 };
 
 template <int D, int MAT, bool GRAV>
@@ -859,6 +864,63 @@ __global__ void __launch_bounds__(128) fused_steps_kernel(FusedP q, int64_t nste
     }
     if (s + 1 < nsteps) reset();  // G2P reads vdt and dv only: the accumulators are free
     if (!grid_barrier(q.bar, err)) return;
+    if (q.rec && s >= q.first && (s - q.first) % q.every == 0) {
+      // EnergiesFix sums of the particles this thread updated (Fix.jl:248-270):
+      // m v.v, V sigma:eps (diagonal + 2 off-diagonal), m v; a fixed CTA tree,
+      // a barrier, then CTA 0 folds the CTAs' sums in block order
+      constexpr int NQ = 2 + D;
+      using L = Layout<D>;
+      double e[NQ];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) e[k] = 0.0;
+      for (int64_t p = tid; p < q.np; p += nth) {
+        const double m = *field<double>(all, L::M, p);
+        double vv = 0.0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          const double v = *field<double>(all, L::V + a, p);
+          vv += v * v;
+          e[2 + a] += m * v;
+        }
+        e[0] += m * vv;
+        double sd = 0.0, so = 0.0;
+#pragma unroll
+        for (int c = 0; c < L::S; ++c) {
+          const double x = *field<double>(all, L::SIG + c, p) * *field<double>(all, L::EPS + c, p);
+          if (c < D) sd += x;
+          else so += x;
+        }
+        e[1] += *field<double>(all, L::VOL, p) * (sd + 2.0 * so);
+      }
+      __shared__ double sh[NQ][128];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] = e[k];
+      __syncthreads();
+      for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) q.partial[int64_t(blockIdx.x) * NQ + k] = sh[k][0];
+      if (!grid_barrier(q.bar, err)) return;
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double t[NQ];
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) t[k] = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b)
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) t[k] += __ldcg(q.partial + int64_t(b) * NQ + k);
+        double* out = q.rec->base + q.rec->idx * NQ;
+        out[0] = 0.5 * t[0];
+        out[1] = 0.5 * t[1];
+#pragma unroll
+        for (int k = 2; k < NQ; ++k) out[k] = t[k];
+        q.rec->idx += 1;
+      }
+    }
   }
 }
 
@@ -877,11 +939,12 @@ static const void* fused_kernel_for(int dim, int mat, bool grav) {
 #undef JMPM_FK
 }
 
-size_t fused_bytes() { return 4 * sizeof(unsigned); }
+// barrier words, then the partial sums of up to 152 CTAs (5 doubles each)
+size_t fused_bytes() { return 4 * sizeof(unsigned) + 152 * 5 * sizeof(double); }
 
 int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
                 int nb, const int64_t* bbeg, const int64_t* bcnt, const MatParams* mp, double dt, double tol,
-                const double* grav, int64_t nsteps, unsigned* status) {
+                const double* grav, int64_t nsteps, unsigned* status, EnRec* rec, int64_t first, int64_t every) {
   if (nb < 1 || nb > MPM_BATCH_MAX_BODIES) return fail(MPM_ERR_ARG, "fused_steps: body count");
   FusedP q{};
   q.g = g;
@@ -902,6 +965,10 @@ int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP&
   for (int a = 0; a < 3; ++a) q.grav[a] = grav[a];
   q.status = status;
   q.bar = static_cast<unsigned*>(dev);
+  q.rec = rec;
+  q.first = first;
+  q.every = every > 0 ? every : 1;
+  q.partial = reinterpret_cast<double*>(static_cast<char*>(dev) + 4 * sizeof(unsigned));
   const bool gr = grav[0] != 0.0 || grav[1] != 0.0 || (dim == 3 && grav[2] != 0.0);
   const void* fn = fused_kernel_for(dim, mp[0].type, gr);
   // 64-thread CTAs, one per SM at most, no more than the particles need
@@ -911,7 +978,7 @@ int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP&
   BATCH_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 64, 0));
   if (per < 1) return fail(MPM_ERR_CUDA, "fused_steps: the kernel does not fit on an SM");
   const int64_t want = std::max<int64_t>(1, (q.np + 63) / 64);
-  const unsigned nblk = unsigned(std::min<int64_t>(want, int64_t(sms)));
+  const unsigned nblk = unsigned(std::min<int64_t>(std::min<int64_t>(want, int64_t(sms)), 152));
   BATCH_TRY(cudaMemsetAsync(q.bar, 0, 3 * sizeof(unsigned), s));
   void* args[] = {&q, &nsteps};
   BATCH_TRY(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(64), args, 0, s));

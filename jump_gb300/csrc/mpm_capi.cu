@@ -889,12 +889,15 @@ static bool fused_fits(const mpm_ctx* c, int sort_interval) {
   return true;
 }
 
-// n steps on the fused path; the next per-stage step clears every node first
-static int fused_run(mpm_ctx* c, int64_t n) {
+// n steps on the fused path, with the EnergiesFix records of local steps
+// first, first + every, ... through c->en_rec when rec; the next per-stage
+// step clears every node first
+static int fused_run(mpm_ctx* c, int64_t n, bool rec = false, int64_t first = 0, int64_t every = 1) {
   if (n <= 0) return MPM_OK;
   if (!c->fused) CUDA_TRY(cudaMalloc(&c->fused, fused_bytes()));
   int r = fused_steps(c->dim, c->stream, c->fused, c->g, c->nd, c->P, c->np, c->nb, c->off.data(), c->cnt.data(),
-                      c->mats.data(), c->prm.dt, c->prm.tolerance, c->prm.body_force, n, c->status);
+                      c->mats.data(), c->prm.dt, c->prm.tolerance, c->prm.body_force, n, c->status,
+                      rec ? c->en_rec : nullptr, first, every);
   c->full_clear = true;
   return r;
 }
@@ -996,30 +999,21 @@ int mpm_step_energies(mpm_ctx* c, int64_t nsteps, int64_t every, int64_t first, 
   CUDA_TRY(cudaEventRecord(c->e0, c->stream));
   int64_t j = 0;
   const bool one = c->p2g_strategy == MPM_P2G_FUSED;
-  int64_t pending = 0;  // fused steps not yet launched (one launch per run between records)
-  for (int64_t k = 0; k < nsteps; ++k) {
+  if (one) {
+    // every step and every record of the call in one cooperative launch
+    int r;
+    if ((r = fused_run(c, nsteps, in_graph, first, every))) return r;
+    if (t_inout)
+      for (int64_t k = 0; k < nsteps; ++k) *t_inout += c->prm.dt;
+  }
+  for (int64_t k = 0; k < nsteps && !one; ++k) {
     int r;
     const bool recd = k >= first && (k - first) % every == 0;
-    if (one) {
-      ++pending;
-      if (recd) {
-        if ((r = fused_run(c, pending))) return r;
-        pending = 0;
-        if (D == 2) Launchers<2>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, nullptr, c->en_rec);
-        else Launchers<3>::energies(c->stream, c->all(), c->f32, c->partial, kEnergyBlocks, nullptr, c->en_rec);
-        CUDA_TRY(cudaGetLastError());
-      }
-    } else if ((r = launch_one_step(c, in_graph && recd))) {
-      return r;
-    }
+    if ((r = launch_one_step(c, in_graph && recd))) return r;
     if (t_inout) *t_inout += c->prm.dt;
     if (recd && !in_graph)  // no particles: zero sums
       CUDA_TRY(cudaMemsetAsync(c->rec_dev + size_t(j) * (2 + D), 0, (2 + D) * sizeof(double), c->stream));
     if (recd) ++j;
-  }
-  if (one && pending > 0) {
-    int r;
-    if ((r = fused_run(c, pending))) return r;
   }
   if (nrec > 0)
     CUDA_TRY(cudaMemcpyAsync(c->rec_host, c->rec_dev, size_t(nrec) * (2 + D) * sizeof(double),

@@ -83,9 +83,12 @@ inline int spread_threads(int64_t n) {
 // bodies.  dev: device scratch of fused_bytes() bytes, whose third word is set
 // when a barrier wait gave up (read it after the stream synchronises).
 size_t fused_bytes();
+// rec (may be null): the EnergiesFix record cursor, one record after local
+// steps first, first + every, ... of the call
 int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
                 int nb, const int64_t* bbeg, const int64_t* bcnt, const MatParams* mp, double dt, double tol,
-                const double* grav, int64_t nsteps, unsigned* status);
+                const double* grav, int64_t nsteps, unsigned* status, EnRec* rec = nullptr, int64_t first = 0,
+                int64_t every = 1);
 
 // deformable material model types a context or batch accepts in dimension dim
 // (rigid bodies, MPM_MAT_RIGID, are checked separately: contexts only)
