@@ -847,14 +847,20 @@ __device__ __forceinline__ void jc_damage_3d(const MatParams& mp, R mu, R kappa,
 
 // F <- F (I + L dt), J, V = J V0, strain += sym(L dt), update_stress! of particle p
 // (:520-532), given L dt; fin: the particle's new x and v are finite.
+// pre (J2 only, may be null): this thread's prefetched inputs in shared
+// memory, slot k at pre[k * blockDim.x]: F (D*D), strain (S), plastic strain
+// (PS), alpha, V0 (g2p_prefetch)
 template <int D, class R, int MAT>
 __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, const R (&Ldt)[D][D],
-                                                  const MatParams& mp, bool fin, unsigned* status) {
+                                                  const MatParams& mp, bool fin, unsigned* status,
+                                                  const R* pre = nullptr) {
   using L = Layout<D>;
+  const int bs = blockDim.x;
+  constexpr int PF = 0, PE = D * D, PP = D * D + L::S, PA = D * D + L::S + L::PS, PV = PA + 1;
   // F <- F (I + L dt)   (:523)
   R F[D * D], Fn[D * D];
 #pragma unroll
-  for (int c = 0; c < D * D; ++c) F[c] = *field<R>(pp, L::F + c, p);
+  for (int c = 0; c < D * D; ++c) F[c] = pre ? pre[(PF + c) * bs] : *field<R>(pp, L::F + c, p);
   // F (I + L dt) = F + F (L dt)
 #pragma unroll
   for (int j = 0; j < D; ++j)
@@ -872,7 +878,7 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
     *field<R>(pp, L::F + c, p) = Fn[c];
   }
   double J = det_d<D>(Fd);  // det F in FP64 for both precisions
-  *field<R>(pp, L::VOL, p) = R(J * to_f64(*field<R>(pp, L::VOL0, p)));
+  *field<R>(pp, L::VOL, p) = R(J * to_f64(pre ? pre[PV * bs] : *field<R>(pp, L::VOL0, p)));
   // strain += dt * 0.5*(L + L')
   R eps[L::S], deps[L::S];
 #pragma unroll
@@ -880,7 +886,7 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
 #pragma unroll
     for (int j = i; j < D; ++j) {
       int c = sym<D>(i, j);
-      R e = *field<R>(pp, L::EPS + c, p);
+      R e = pre ? pre[(PE + c) * bs] : *field<R>(pp, L::EPS + c, p);
       deps[c] = (i == j) ? Ldt[i][i] : R(0.5) * (Ldt[i][j] + Ldt[j][i]);
       e += deps[c];
       eps[c] = e;
@@ -931,10 +937,10 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
       *field<R>(pp, L::VM, p) = vm;
     }
   } else {
-    R alpha = *field<R>(pp, L::ALPHA, p);
+    R alpha = pre ? pre[PA * bs] : *field<R>(pp, L::ALPHA, p);
     R ep[L::PS];
 #pragma unroll
-    for (int c = 0; c < L::PS; ++c) ep[c] = *field<R>(pp, L::EP + c, p);
+    for (int c = 0; c < L::PS; ++c) ep[c] = pre ? pre[(PP + c) * bs] : *field<R>(pp, L::EP + c, p);
     R vm;
     if (D == 3)
       j2_3d<R>(lam, mu, kappa, mat_const<R>(mp.fy, mp.f_fy), mat_const<R>(mp.k1, mp.f_k1), eps, sig, &alpha, ep,
@@ -955,13 +961,39 @@ __device__ __forceinline__ void kinematics_stress(const PartP& pp, int64_t p, co
   if (st) atomicOr(status, st);
 }
 
+// One 4-byte asynchronous copy global -> shared (cp.async, this thread's own
+// slot), and the wait for all of this thread's copies.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // G2P + kinematics + stress of particle pp.begin + t (t < pp.count).
+// pre (J2 only, may be null): this thread's shared-memory slots (stride
+// blockDim.x) into which the constitutive inputs are copied asynchronously
+// at the start, so that their loads overlap the node gather without holding
+// registers (the layout of kinematics_stress's pre).
 template <int D, class R, int MAT, bool CG = false>
 __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
-                                             const MatParams& mp, double dt, unsigned* status) {
+                                             const MatParams& mp, double dt, unsigned* status, R* pre = nullptr) {
   using L = Layout<D>;
   int64_t p = pp.begin + t;
+  if constexpr (MAT == MPM_MAT_J2) {
+    if (pre) {
+      const int bs = blockDim.x;
+      int k = 0;
+#pragma unroll
+      for (int c = 0; c < D * D; ++c) cp_async4(pre + (k++) * bs, field<R>(pp, L::F + c, p));
+#pragma unroll
+      for (int c = 0; c < L::S; ++c) cp_async4(pre + (k++) * bs, field<R>(pp, L::EPS + c, p));
+#pragma unroll
+      for (int c = 0; c < L::PS; ++c) cp_async4(pre + (k++) * bs, field<R>(pp, L::EP + c, p));
+      cp_async4(pre + (k++) * bs, field<R>(pp, L::ALPHA, p));
+      cp_async4(pre + (k++) * bs, field<R>(pp, L::VOL0, p));
+    }
+  }
   R x[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) x[a] = *field<R>(pp, L::X + a, p);
@@ -969,6 +1001,7 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
   // the hat the P2G of this step stored (same positions), else computed here
   const bool ok = (sizeof(R) == 8 && pp.hat_c) ? hat_get<D, R>(g, pp, p, h) : hat<D, R>(g, x, h);
   if (!ok) {
+    if (pre) cp_async_wait_all();  // no copy into this CTA's shared memory outlives the thread
     atomicOr(status, ST_OUT_OF_GRID);
     return;
   }
@@ -1120,7 +1153,12 @@ __device__ __forceinline__ void g2p_particle(const GridP& g, const NodeP& nd, co
   bool fin = true;
 #pragma unroll
   for (int a = 0; a < D; ++a) fin &= finite_bits(x[a]) & finite_bits(v[a]);
-  kinematics_stress<D, R, MAT>(pp, p, Ldt, mp, fin, status);
+  if (MAT == MPM_MAT_J2 && pre) {
+    cp_async_wait_all();
+    kinematics_stress<D, R, MAT>(pp, p, Ldt, mp, fin, status, pre);
+  } else {
+    kinematics_stress<D, R, MAT>(pp, p, Ldt, mp, fin, status);
+  }
 }
 
 // FP32 particles: at most 48 registers (five 256-thread CTAs per SM); the
@@ -1132,6 +1170,24 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 0) g2p_kernel(GridP 
                                                   unsigned* status) {
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t < pp.count) g2p_particle<D, R, MAT>(g, nd, pp, t, mp, dt, status);
+}
+
+// The J2 G2P with its constitutive inputs (F, strain, plastic strain, alpha,
+// V0) prefetched into shared memory by cp.async: dynamic shared memory of
+// g2p_prefetch_slots<D>() x blockDim.x particle values.
+template <int D>
+constexpr int g2p_prefetch_slots() {
+  return D * D + Layout<D>::S + Layout<D>::PS + 2;
+}
+
+template <int D, class R>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 0) g2p_prefetch_kernel(GridP g, NodeP nd, PartP pp,
+                                                                                  MatParams mp, double dt,
+                                                                                  unsigned* status) {
+  extern __shared__ __align__(16) unsigned char g2p_pre_smem[];
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t < pp.count)
+    g2p_particle<D, R, MPM_MAT_J2>(g, nd, pp, t, mp, dt, status, reinterpret_cast<R*>(g2p_pre_smem) + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------

@@ -317,6 +317,12 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
   const int th = threads > 0 ? threads : 256;
   unsigned nb = blocks_for(pp.count, th);
 #define JMPM_G2P(R, M) g2p_kernel<D, R, M><<<nb, th, 0, s>>>(g, nd, pp, mp, dt, status)
+  if (f32 && nd.nf4 && mp.type == MPM_MAT_J2 && D == 3) {
+    // FP32 J2 with interleaved node records: the constitutive inputs prefetched
+    const size_t smem = size_t(g2p_prefetch_slots<D>()) * size_t(th) * sizeof(float);
+    g2p_prefetch_kernel<D, float><<<nb, th, smem, s>>>(g, nd, pp, mp, dt, status);
+    return;
+  }
   if (f32) {
     switch (mp.type) {
       case MPM_MAT_ELASTIC: JMPM_G2P(float, MPM_MAT_ELASTIC); break;
