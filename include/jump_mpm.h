@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define JUMP_MPM_ABI_VERSION 9
+#define JUMP_MPM_ABI_VERSION 10
 
 /* status codes */
 #define MPM_OK               0
@@ -75,6 +75,19 @@ extern "C" {
 /* particle precision (grid accumulation is always FP64) */
 #define MPM_PREC_F64        0   /* every particle field and every operation in FP64 */
 #define MPM_PREC_F32        1   /* FP32 particle fields and arithmetic; FP64 nodes, det F, energies */
+/* FP64 particle fields and FP64 node accumulators; the arithmetic of the P2G
+   and the G2P with its constitutive update (linear elastic, J2) in
+   double-word FP32: each value a pair of floats hi + lo, about 48 significant
+   bits (2^-49 relative per rounding against FP64's 2^-53), from error-free
+   transforms on the FP32 pipe, which issues 64 times as many operations per
+   clock as the FP64 pipe on GB300.  Every accumulated particle field is its
+   FP64 value plus the step's increment rounded to FP64, and the hat (cell and
+   weights) is the FP64 one, so the results follow the FP64 step to within the
+   FP64 step's own rounding differences.  3D USL on the linear basis with one
+   velocity field and the P2G strategy MPM_P2G_ATOMIC; other configurations:
+   MPM_ERR_UNSUPPORTED (MPM_ERR_ARG for another strategy).  The reverse mode
+   and MPM_P2G_FUSED take FP64 contexts only. */
+#define MPM_PREC_DW         2
 
 /* Shape functions (the `basis` argument of solve_explicit_dynamics_2D/3D) */
 #define MPM_BASIS_LINEAR        0  /* LinearBasis: hat functions, 2^dim nodes (Basis.jl:219-251, 292-332) */
@@ -166,7 +179,7 @@ typedef struct mpm_params {
   double  dt;                  /* data["dt"] */
   double  tolerance;           /* USL.tolerance: nodal mass cutoff in G2P, Algorithm.jl:16-18 */
   double  body_force[3];       /* ConstantBodyForce2D/3D.g, BodyForce.jl:56-62,85-91 */
-  int32_t precision;           /* MPM_PREC_F64 or MPM_PREC_F32 */
+  int32_t precision;           /* MPM_PREC_F64, MPM_PREC_F32 or MPM_PREC_DW */
   int32_t contact;             /* 0: one velocity field (the reference USL); 1: one field per body
                                   with the multi-body contact correction */
   double  friction;            /* Coulomb coefficient for contact (2D only; 0 = frictionless) */
@@ -292,6 +305,25 @@ int mpm_destroy(mpm_ctx* ctx);
    roofline of the step kernels.  Only the rates whose output pointer is not
    NULL are measured. */
 int mpm_probe_rates(double* fp64_fma_per_s, double* fp64_div_per_s, double* fp64_atomics_per_s);
+
+/* Test aid (no counterpart in the reference): the double-word operation op of
+   the MPM_PREC_DW arithmetic on n operand triples (a[i], b[i], c[i]), each
+   first converted FP64 -> double-word; out[2i] and out[2i + 1] receive the
+   result's float parts (hi, lo) as doubles (MPM_DW_OP_TO_F64: the FP64 value
+   of a[i] after the conversion and back, and 0).  MPM_DW_OP_MUL_FLOAT
+   multiplies by the high part of b[i]; MPM_DW_OP_FMA is a[i] b[i] + c[i]. */
+#define MPM_DW_OP_FROM_F64  0
+#define MPM_DW_OP_ADD       1
+#define MPM_DW_OP_SUB       2
+#define MPM_DW_OP_MUL       3
+#define MPM_DW_OP_MUL_FLOAT 4
+#define MPM_DW_OP_FMA       5
+#define MPM_DW_OP_SQR       6
+#define MPM_DW_OP_SQRT      7
+#define MPM_DW_OP_RECIP     8
+#define MPM_DW_OP_ONE_MINUS 9
+#define MPM_DW_OP_TO_F64    10
+int mpm_probe_dw(int32_t op, int64_t n, const double* a, const double* b, const double* c, double* out);
 
 /* ---------------------------------------------------------------------------
  * Reverse mode (no counterpart in the reference): gradients of a loss on the

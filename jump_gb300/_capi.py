@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-ABI_VERSION = 9  # JUMP_MPM_ABI_VERSION of the structures below
+ABI_VERSION = 10  # JUMP_MPM_ABI_VERSION of the structures below
 
 MPM_OK = 0
 MPM_ERR_ARG = 1
@@ -46,6 +46,20 @@ MPM_MAX_RIGID_BODIES = 32
 
 MPM_PREC_F64 = 0
 MPM_PREC_F32 = 1
+MPM_PREC_DW = 2
+
+# double-word operations of mpm_probe_dw
+MPM_DW_OP_FROM_F64 = 0
+MPM_DW_OP_ADD = 1
+MPM_DW_OP_SUB = 2
+MPM_DW_OP_MUL = 3
+MPM_DW_OP_MUL_FLOAT = 4
+MPM_DW_OP_FMA = 5
+MPM_DW_OP_SQR = 6
+MPM_DW_OP_SQRT = 7
+MPM_DW_OP_RECIP = 8
+MPM_DW_OP_ONE_MINUS = 9
+MPM_DW_OP_TO_F64 = 10
 
 MPM_ALG_USL = 0
 MPM_ALG_MUSL = 1
@@ -198,6 +212,7 @@ SIGNATURES = {
     "mpm_step_energies": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, _dp, C.c_void_p]),
     "mpm_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "mpm_probe_rates": (C.c_int, [_dp, _dp, _dp]),
+    "mpm_probe_dw": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp, _dp]),
     "mpm_get_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "mpm_tune": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                            C.POINTER(C.c_int32), _dp, _dp]),

@@ -992,6 +992,7 @@ extern "C" {
 int mpm_batch_create(const mpm_instance_desc* instances, int32_t n, int32_t precision, mpm_batch** out) {
   if (!instances || !out || n < 1) return fail(MPM_ERR_ARG, "mpm_batch_create: need at least one problem");
   *out = nullptr;
+  if (precision == MPM_PREC_DW) return fail(MPM_ERR_UNSUPPORTED, "mpm_batch_create: MPM_PREC_DW is for contexts");
   if (precision != MPM_PREC_F64 && precision != MPM_PREC_F32)
     return fail(MPM_ERR_ARG, "mpm_batch_create: unknown precision");
   const int D = instances[0].grid.dim;

@@ -55,6 +55,7 @@ int jmpm::set_last_error(int code, const std::string& msg) { return fail(code, m
 struct mpm_ctx {
   int dim = 2;
   bool f32 = false;
+  bool dw = false;            // MPM_PREC_DW: FP64 particles, double-word FP32 G2P
   mpm_params prm{};
   int nb = 0;
   std::vector<int64_t> off, cnt;
@@ -106,6 +107,7 @@ struct mpm_ctx {
   double* muslbuf = nullptr;  // MUSL: 3D p2 | vg; 2D mass stencil (9) | vg | CG vectors (16)
   CgP cg{};
   float* nodebuf_f = nullptr;
+  float4* nodebuf_dw = nullptr;  // MPM_PREC_DW: the grid update's double-word node records (NodeP::dw4)
   std::vector<uint8_t> fixed_h;
   // rigid bodies (MPM_MAT_RIGID): rigid ordinal of each body (-1: deformable),
   // the per-node marks and the {fixed, vx, vy, vz} table (device and host)
@@ -219,6 +221,7 @@ void destroy_ctx(mpm_ctx* c) {
   cudaFree(c->fullrec);
   cudaFree(c->muslbuf);
   cudaFree(c->nodebuf_f);
+  cudaFree(c->nodebuf_dw);
   cudaFree(c->blockbuf);
   cudaFree(c->rmask);
   cudaFree(c->rtab);
@@ -513,6 +516,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
   c->dim = D;
   c->prm = *prm;
   c->f32 = prm->precision == MPM_PREC_F32;
+  c->dw = prm->precision == MPM_PREC_DW;
   c->esz = c->f32 ? sizeof(float) : sizeof(double);
   c->NF = num_fields(D);
   c->fi = D == 2 ? make_idx<2>() : make_idx<3>();
@@ -553,6 +557,7 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     c->g.coordf[a] = a < D ? coordf + o : coordf;
     c->g.xminf[a] = float(c->g.xmin[a]);
     c->g.dxIf[a] = float(c->g.dxI[a]);
+    split_dw(c->g.dxI[a], c->g.w_dxI[a]);
     if (a < D) o += nn[a];
   }
 
@@ -677,6 +682,14 @@ int create_impl(const mpm_grid_desc* gd, const mpm_body_desc* bd, int32_t nbodie
     c->nd.vdt_f = c->nodebuf_f;
     c->nd.dv_f = c->nodebuf_f + Nn * D;
     c->nd.nf4 = inter ? reinterpret_cast<float4*>(c->nodebuf_f) : nullptr;
+  }
+
+  if (c->dw) {
+    // three float4 per node (NodeP::dw4), written by every grid update
+    CUDA_TRY(cudaMalloc(&c->nodebuf_dw, size_t(Nn) * 3 * sizeof(float4)));
+    CUDA_TRY(cudaMemset(c->nodebuf_dw, 0, size_t(Nn) * 3 * sizeof(float4)));
+    c->nd.dw4 = c->nodebuf_dw;
+    CUDA_TRY(Launchers<3>::dw_setup());
   }
 
   // particles
@@ -829,8 +842,19 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
   if (params->algorithm == MPM_ALG_MUSL && (params->precision != MPM_PREC_F64 || params->contact))
     return fail(MPM_ERR_UNSUPPORTED, "mpm_create: MUSL runs FP64 with one velocity field");
   if (!(params->dt > 0.0) || !std::isfinite(params->dt)) return fail(MPM_ERR_ARG, "mpm_create: dt must be > 0");
-  if (params->precision != MPM_PREC_F64 && params->precision != MPM_PREC_F32)
+  if (params->precision != MPM_PREC_F64 && params->precision != MPM_PREC_F32 && params->precision != MPM_PREC_DW)
     return fail(MPM_ERR_ARG, "mpm_create: unknown precision");
+  if (params->precision == MPM_PREC_DW) {
+    bool ok = grid->dim == 3 && params->algorithm == MPM_ALG_USL && params->basis == MPM_BASIS_LINEAR &&
+              !params->contact;
+    for (int b = 0; ok && b < nbodies; ++b) {
+      const int t = bodies[b].mat.type;
+      ok = t == MPM_MAT_RIGID || t == MPM_MAT_ELASTIC || t == MPM_MAT_J2;
+    }
+    if (!ok)
+      return fail(MPM_ERR_UNSUPPORTED, "mpm_create: MPM_PREC_DW runs 3D USL on the linear basis with one velocity "
+                                       "field and linear elastic, J2 or rigid bodies");
+  }
   if (params->contact && nbodies > kMaxContactBodies)
     return fail(MPM_ERR_ARG, "mpm_create: contact mode supports at most " + std::to_string(kMaxContactBodies) +
                                  " bodies");
@@ -878,7 +902,7 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
 // their steps in one cooperative launch (fused_steps), whose reset of every
 // step is dense.
 static bool fused_fits(const mpm_ctx* c, int sort_interval) {
-  if (c->f32 || c->np == 0 || c->np > MPM_FUSED_MAX_PARTICLES || c->prm.algorithm != MPM_ALG_USL ||
+  if (c->f32 || c->dw || c->np == 0 || c->np > MPM_FUSED_MAX_PARTICLES || c->prm.algorithm != MPM_ALG_USL ||
       c->prm.basis != MPM_BASIS_LINEAR || c->prm.contact || sort_interval > 0 || c->nb > MPM_BATCH_MAX_BODIES)
     return false;
   const int t0 = c->mats[0].type;
@@ -1040,6 +1064,8 @@ int mpm_set_launch(mpm_ctx* c, int32_t p2g_strategy, int32_t threads, int32_t so
   if (threads >= 0 && (threads < 32 || threads > 256 || threads % 32 != 0))
     return fail(MPM_ERR_ARG, "mpm_set_launch: threads must be a multiple of 32 in 32 .. 256");
   const int new_sort = sort_interval >= 0 ? sort_interval : c->prm.sort_interval;
+  if (c->dw && p2g_strategy > MPM_P2G_ATOMIC)
+    return fail(MPM_ERR_ARG, "mpm_set_launch: MPM_PREC_DW contexts take MPM_P2G_ATOMIC");
   if (p2g_strategy == MPM_P2G_FUSED && !fused_fits(c, new_sort))
     return fail(MPM_ERR_ARG, "mpm_set_launch: MPM_P2G_FUSED needs an FP64 linear-basis USL problem of at most "
                              "MPM_FUSED_MAX_PARTICLES particles, one velocity field, no rigid bodies, no sort and "
@@ -1108,7 +1134,7 @@ int mpm_tune(mpm_ctx* c, int64_t probe_steps, int32_t* p2g_strategy, int32_t* th
       for (int si : sort_list) {
         ++idx;
         if (rc != MPM_OK) break;
-        if (si > 0 && !can_sort) continue;
+        if ((si > 0 && !can_sort) || (c->dw && s != MPM_P2G_ATOMIC)) continue;
         c->p2g_strategy = s;
         c->threads = th;
         c->prm.sort_interval = si;
@@ -1390,10 +1416,10 @@ int mpm_profile_stages(mpm_ctx* c, int64_t nsteps, double* stage_ms) {
 int mpm_fwd_checkpointed(mpm_ctx* c, int64_t nsteps, int32_t every) {
   if (!c) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: null context");
   if (nsteps < 1 || every < 1) return fail(MPM_ERR_ARG, "mpm_fwd_checkpointed: need nsteps >= 1, every >= 1");
-  if (c->f32 || c->prm.contact || c->prm.sort_interval > 0 || c->prm.algorithm != MPM_ALG_USL ||
+  if (c->f32 || c->dw || c->prm.contact || c->prm.sort_interval > 0 || c->prm.algorithm != MPM_ALG_USL ||
       c->prm.basis != MPM_BASIS_LINEAR)
     return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode needs USL with the linear basis, FP64 "
-                                     "particles, one velocity field and no sorting");
+                                     "particles and arithmetic, one velocity field and no sorting");
   for (const MatParams& m : c->mats)
     if (m.type != MPM_MAT_NEOHOOKEAN && m.type != MPM_MAT_ELASTIC && m.type != MPM_MAT_J2)
       return fail(MPM_ERR_UNSUPPORTED, "mpm_fwd_checkpointed: reverse mode is built for neo-Hookean, linear "

@@ -73,6 +73,9 @@ struct MatParams {
   // FP32 particles: lambda, mu, kappa, fy, k1 and rtmuk1 rounded to float once
   // on the host (a per-particle conversion is FP64-pipe work)
   float f_lambda, f_mu, f_kappa, f_fy, f_k1, f_rtmuk1;
+  // double-word G2P (MPM_PREC_DW): lambda, mu, kappa, fy, k1, rtmuk1 and the
+  // deviator's 0.333333333 as {hi, lo} float pairs split once on the host
+  float w_lambda[2], w_mu[2], w_kappa[2], w_fy[2], w_k1[2], w_rtmuk1[2], w_third[2];
 };
 
 // a material constant in the particle precision: the FP64 value, or its float copy
@@ -95,6 +98,7 @@ struct GridP {
   // coordf null: convert on the fly
   float xminf[3], dxIf[3];
   const float* coordf[3];
+  float w_dxI[3][2];   // dxI as {hi, lo} float pairs (double-word G2P)
 };
 
 // Node arrays (FP64).  Accumulators m, p0 (D), f (D); grid-update outputs
@@ -111,6 +115,9 @@ struct NodeP {
   // record per node (2D: vdt x y, dv x y = one float4; 3D: vdt x y z 0, dv x y z 0
   // = two float4), so that a corner's six values come in two 16-byte loads
   float4* nf4;
+  // or, for the double-word G2P (MPM_PREC_DW), three float4 per node:
+  // {vdt x hi, lo, vdt y hi, lo}, {vdt z hi, lo, dv x hi, lo}, {dv y hi, lo, dv z hi, lo}
+  float4* dw4 = nullptr;
   const uint8_t* fixed;  // bit a set: dof a is fixed (grid.fixedNodes)
   int64_t nodeCount;
   int64_t nn[3];         // nodes per axis (1 for the unused axis in 2D)

@@ -17,6 +17,12 @@ namespace jmpm {
 // Kernel parameters of a material (Material.jl:37-172, 279-383): Lame constants
 // as the constructors compute them; for Johnson-Cook/Voce the rate filter time
 // 1000 cellsize / sqrt((lambda + 2 mu)/density) and the step dt.
+// d as a double-word pair: hi = float(d), lo = float(d - hi)
+inline void split_dw(double d, float (&w)[2]) {
+  w[0] = float(d);
+  w[1] = float(d - double(w[0]));
+}
+
 inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, double dt) {
   MatParams mp{};
   mp.type = m.type;
@@ -56,6 +62,13 @@ inline MatParams make_mat_params(const mpm_material_desc& m, bool per_particle, 
   mp.f_fy = float(mp.fy);
   mp.f_k1 = float(mp.k1);
   mp.f_rtmuk1 = float(mp.rtmuk1);
+  split_dw(mp.lambda, mp.w_lambda);
+  split_dw(mp.mu, mp.w_mu);
+  split_dw(mp.kappa, mp.w_kappa);
+  split_dw(mp.fy, mp.w_fy);
+  split_dw(mp.k1, mp.w_k1);
+  split_dw(mp.rtmuk1, mp.w_rtmuk1);
+  split_dw(0.333333333, mp.w_third);  // the deviator's constant (Material.jl:246)
   return mp;
 }
 
@@ -146,6 +159,9 @@ struct Launchers {
                            bool f32copy);
   static void g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const PartP& pp, bool f32,
                   const MatParams& mp, double dt, unsigned* status, int threads = 0);
+  // raises the dynamic shared-memory limit of the double-word G2P (3D), once
+  // per context before its first step (outside any stream capture)
+  static cudaError_t dw_setup();
   // EnergiesFix sums into out[0 .. 2 + D), or with a record cursor rec into
   // rec->base[rec->idx] (the cursor advances): partial holds nblocks x 5
   // doubles and one more slot, the fold's ticket, zero before the first

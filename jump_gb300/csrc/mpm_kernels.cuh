@@ -13,6 +13,7 @@
 #include <type_traits>
 
 #include "mpm_common.cuh"
+#include "mpm_dw.cuh"
 #include "mpm_sparse.cuh"
 #include "../../include/jump_mpm.h"
 
@@ -501,6 +502,7 @@ __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt,
       nd.nf4[(D == 2 ? 1 : 2) * i] = z;
       if (D == 3) nd.nf4[2 * i + 1] = z;
     }
+    if (D == 3 && !F32COPY && nd.dw4) put_node_dw(nd.dw4, i, nullptr, nullptr);
     return;
   }
   const unsigned fx = nd.fixed[i];
@@ -531,6 +533,7 @@ __device__ __forceinline__ void grid_node(const NodeP& nd, int64_t i, double dt,
       nd.dv_f[a * Nn + i] = float(dv[a]);
     }
   }
+  if (D == 3 && !F32COPY && nd.dw4) put_node_dw(nd.dw4, i, vdt, dv);
   if (F32COPY && nd.nf4) {
     if (D == 2) {
       nd.nf4[i] = make_float4(float(vdt[0]), float(vdt[1]), float(dv[0]), float(dv[D - 1]));

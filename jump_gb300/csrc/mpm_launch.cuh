@@ -5,6 +5,7 @@
 #include "mpm_kernels.cuh"
 #include "mpm_musl.cuh"
 #include "mpm_bspline.cuh"
+#include "mpm_step_dw.cuh"
 
 #include <type_traits>
 
@@ -33,6 +34,15 @@ void Launchers<D>::p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
                        const double* grav, unsigned* status, int strategy, int threads) {
   if (pp.count <= 0) return;
   bool has_g = grav[0] != 0.0 || grav[1] != 0.0 || (D == 3 && grav[2] != 0.0);
+  if (!f32 && nd.dw4) {
+    // double-word P2G (MPM_PREC_DW contexts, 3D): per-lane FP64 atomics
+    if constexpr (D == 3) {
+      const int th = threads > 0 ? threads : 256;
+      if (has_g) p2g_dw_kernel<true><<<blocks_for(pp.count, th), th, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+      else p2g_dw_kernel<false><<<blocks_for(pp.count, th), th, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+    }
+    return;
+  }
   if (strategy < 0) strategy = f32 ? MPM_P2G_WARP : MPM_P2G_ATOMIC;
   const int th = threads > 0 ? threads : 256;
   unsigned nb = blocks_for(pp.count, th);
@@ -317,6 +327,17 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
   const int th = threads > 0 ? threads : 256;
   unsigned nb = blocks_for(pp.count, th);
 #define JMPM_G2P(R, M) g2p_kernel<D, R, M><<<nb, th, 0, s>>>(g, nd, pp, mp, dt, status)
+  if (!f32 && nd.dw4) {
+    // double-word G2P (MPM_PREC_DW contexts: 3D, linear elastic or J2 bodies)
+    if constexpr (D == 3) {
+      // the inputs' shared-memory slots: 28 doubles per thread (57 KB at 256
+      // threads; dw_setup raised the kernels' limit)
+      const size_t smem = size_t(DwSlots::N) * size_t(th) * sizeof(double);
+      if (mp.type == MPM_MAT_ELASTIC) g2p_dw_kernel<MPM_MAT_ELASTIC><<<nb, th, smem, s>>>(g, nd, pp, mp, status);
+      else g2p_dw_kernel<MPM_MAT_J2><<<nb, th, smem, s>>>(g, nd, pp, mp, status);
+    }
+    return;
+  }
   if (f32 && nd.nf4 && mp.type == MPM_MAT_J2 && D == 3) {
     // FP32 J2 with interleaved node records: the constitutive inputs prefetched
     const size_t smem = size_t(g2p_prefetch_slots<D>()) * size_t(th) * sizeof(float);
@@ -343,6 +364,18 @@ void Launchers<D>::g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const Pa
     }
   }
 #undef JMPM_G2P
+}
+
+template <int D>
+cudaError_t Launchers<D>::dw_setup() {
+  if constexpr (D == 3) {
+    const int most = int(DwSlots::N * 256 * sizeof(double));
+    cudaError_t e = cudaFuncSetAttribute(g2p_dw_kernel<MPM_MAT_ELASTIC>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(g2p_dw_kernel<MPM_MAT_J2>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    return e;
+  }
+  return cudaSuccess;
 }
 
 template <int D>

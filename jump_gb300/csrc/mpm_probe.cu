@@ -2,13 +2,16 @@
 // kernels are bound by, measured on the device the library runs on: FP64
 // fused multiply-adds, FP64 divisions and FP64 atomic additions executed in
 // L2 (RED.ADD at distinct, coalesced addresses).  A measurement aid for the
-// FP64 roofline that bench.py reports beside the HBM one.
+// FP64 roofline that bench.py reports beside the HBM one.  mpm_probe_dw: the
+// double-word operations of mpm_dw.cuh on given operands, for tests of their
+// error bounds against exact rational arithmetic.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 #include <string>
 
 #include "../../include/jump_mpm.h"
+#include "mpm_dw.cuh"
 
 namespace jmpm {
 int set_last_error(int code, const std::string& msg);  // mpm_capi.cu
@@ -68,7 +71,57 @@ int time_launch(cudaStream_t s, F&& f, float* ms) {
   return e == cudaSuccess ? 0 : 1;
 }
 
+// result i of double-word operation op on operands a[i], b[i], c[i] (each
+// converted FP64 -> DW by dw_from): out[2i] = hi, out[2i + 1] = lo
+__global__ void dw_probe_kernel(int op, int64_t n, const double* a, const double* b, const double* c, double* out) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  using namespace jmpm;
+  const dw x = dw_from(a[i]), y = dw_from(b[i]), z = dw_from(c[i]);
+  dw r = x;
+  switch (op) {
+    case MPM_DW_OP_ADD: r = x + y; break;
+    case MPM_DW_OP_SUB: r = x - y; break;
+    case MPM_DW_OP_MUL: r = x * y; break;
+    case MPM_DW_OP_MUL_FLOAT: r = x * y.hi; break;
+    case MPM_DW_OP_FMA: r = dw_fma(x, y, z); break;
+    case MPM_DW_OP_SQR: r = dw_sqr(x); break;
+    case MPM_DW_OP_SQRT: r = dw_sqrt(x); break;
+    case MPM_DW_OP_RECIP: r = dw_recip(x); break;
+    case MPM_DW_OP_ONE_MINUS: r = dw_one_minus(x); break;
+    case MPM_DW_OP_TO_F64: r = dw_make(float(0), float(0)); break;
+    default: break;  // MPM_DW_OP_FROM_F64: the conversion itself
+  }
+  if (op == MPM_DW_OP_TO_F64) {
+    out[2 * i] = dw_to_f64(x);
+    out[2 * i + 1] = 0.0;
+    return;
+  }
+  out[2 * i] = double(r.hi);
+  out[2 * i + 1] = double(r.lo);
+}
+
 }  // namespace
+
+extern "C" int mpm_probe_dw(int32_t op, int64_t n, const double* a, const double* b, const double* c, double* out) {
+  if (op < MPM_DW_OP_FROM_F64 || op > MPM_DW_OP_TO_F64 || n < 0 || (n > 0 && (!a || !b || !c || !out)))
+    return jmpm::set_last_error(MPM_ERR_ARG, "mpm_probe_dw: bad operation or arrays");
+  if (n == 0) return MPM_OK;
+  double* d = nullptr;
+  const size_t bytes = size_t(n) * sizeof(double);
+  if (cudaMalloc(&d, bytes * 5) != cudaSuccess) return jmpm::set_last_error(MPM_ERR_CUDA, "mpm_probe_dw: allocation");
+  cudaError_t e = cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + 2 * n, c, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    dw_probe_kernel<<<unsigned((n + 255) / 256), 256>>>(op, n, d, d + n, d + 2 * n, d + 3 * n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + 3 * n, 2 * bytes, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return jmpm::set_last_error(MPM_ERR_CUDA, std::string("mpm_probe_dw: ") + cudaGetErrorString(e));
+  return MPM_OK;
+}
 
 extern "C" int mpm_probe_rates(double* fp64_fma_per_s, double* fp64_div_per_s, double* fp64_atomics_per_s) {
   int dev = 0, sms = 0;

@@ -14,7 +14,7 @@ from . import _capi
 from .algorithm import USL, ConstantBodyForce2D, ConstantBodyForce3D
 from .material import ElastoPlasticMaterial, RigidMaterial
 
-PRECISIONS = {"f64": _capi.MPM_PREC_F64, "f32": _capi.MPM_PREC_F32}
+PRECISIONS = {"f64": _capi.MPM_PREC_F64, "f32": _capi.MPM_PREC_F32, "dw": _capi.MPM_PREC_DW}
 
 
 def colmajor(a: np.ndarray) -> np.ndarray:

@@ -29,7 +29,7 @@ using Grid, Solid, Material, Algorithm, Basis, Fix, Dirichlet, Output
 import Problem
 
 const lib = normpath(joinpath(@__DIR__, "..", "lib", "libjumpmpm.so"))
-const ABI = 9  # JUMP_MPM_ABI_VERSION of the structures below
+const ABI = 10  # JUMP_MPM_ABI_VERSION of the structures below
 
 function __init__()
     v = ccall((:mpm_abi_version, lib), Cint, ())
@@ -232,7 +232,7 @@ gravity(data, dim) = haskey(data, "bodyforce") && hasproperty(data["bodyforce"],
 
 function params(alg, basis, data, dim)
     musl = alg isa MUSL
-    prec = get(data, "precision", "f64") == "f32" ? Int32(1) : Int32(0)
+    prec = Int32(get(Dict("f64" => 0, "f32" => 1, "dw" => 2), get(data, "precision", "f64"), 0))
     Params(data["dt"], musl ? 0.0 : alg.tolerance, gravity(data, dim), prec,
            Int32(get(data, "contact", false) ? 1 : 0), Float64(get(data, "friction", 0.0)),
            Int32(get(data, "sort_interval", 0)), Int32(0), musl ? Int32(1) : Int32(0), basiscode(basis),

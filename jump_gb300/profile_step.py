@@ -6,12 +6,13 @@
                                     [--basis linear|quad|cubic] [--material j2|jc|jcdamage]
                                     [--sort-interval 0] [--energies]
                                     [--p2g atomic|warp|tile|tile_warp] [--threads N]
-                                    [--sweep]
+                                    [--sweep] [--stages]
 
 --sweep: instead of the timed steps, the device ms per stage (reset, P2G,
 grid, G2P; individual launches timed with CUDA events, mean of 10 steps) for
 every P2G strategy x CTA size {128, 256} x sort interval {0, 4}, one JSON
-line each.
+line each.  --stages: after the timed steps, the same per-stage ms of the
+configuration as given.
 
 Launch order per step: p2g_kernel, grid_kernel, g2p_kernel (one each per body),
 after the aos_to_soa upload launches of context creation.
@@ -29,7 +30,7 @@ from .engine import Descriptors, MPMContext
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="taylor_bar", choices=["taylor_bar", "two_disks", "cantilever"])
-    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "dw"])
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--h", type=float, default=2.5e-4)
@@ -42,6 +43,7 @@ def main():
     ap.add_argument("--p2g", default=None, choices=list(MPMContext.P2G_STRATEGIES), help="P2G strategy")
     ap.add_argument("--threads", type=int, default=None, help="CTA size of P2G and G2P")
     ap.add_argument("--sweep", action="store_true", help="stage times of every P2G strategy / CTA size / sort")
+    ap.add_argument("--stages", action="store_true", help="then the device ms per stage (mean of 10 steps)")
     a = ap.parse_args()
     if a.workload == "taylor_bar":
         g, s, alg, data = scenarios.taylor_bar(h=a.h)
@@ -78,6 +80,9 @@ def main():
     n = sum(x.parCount for x in s)
     print(f"{a.workload} {a.precision} {a.algorithm} {a.basis} {a.material} {ctx.launch()}: {n} particles, {a.steps} steps, {1e3 * dt / max(a.steps, 1):.3f} ms/step, "
           f"device {ctx.last_step_ms() / max(a.steps, 1):.3f} ms/step")
+    if a.stages:
+        st = ctx.profile_stages(10)
+        print(json.dumps({"stage_ms": {k: round(v / 10, 4) for k, v in st.items()}}))
     ctx.close()
 
 

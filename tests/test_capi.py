@@ -34,7 +34,7 @@ def test_every_declared_symbol_is_exported(L):
 
 
 def test_abi_version(L):
-    assert L.mpm_abi_version() == _capi.ABI_VERSION == 9
+    assert L.mpm_abi_version() == _capi.ABI_VERSION == 10
 
 
 def test_argument_errors_without_gpu(L):
@@ -55,6 +55,34 @@ def test_argument_errors_without_gpu(L):
     assert L.mpm_create(C.byref(g), None, 0, C.byref(p), C.byref(h)) == _capi.MPM_ERR_ARG
     assert L.mpm_step(None, 1, None) == _capi.MPM_ERR_ARG
     assert L.mpm_destroy(None) == _capi.MPM_OK
+
+
+def test_double_word_precision_refusals_without_gpu(L):
+    """MPM_PREC_DW takes 3D USL on the linear basis with linear elastic, J2 or
+    rigid bodies; anything else is refused before any device work."""
+    from jump_gb300 import scenarios
+    from jump_gb300.engine import Descriptors
+
+    h = C.c_void_p()
+    grid, solids, alg, data = scenarios.two_disks(nodes=11)
+    d = Descriptors(grid, solids, tolerance=alg.tolerance, dt=data["dt"], precision="dw")
+    assert L.mpm_create(C.byref(d.grid), d.bodies, len(solids), C.byref(d.params), C.byref(h)) == \
+        _capi.MPM_ERR_UNSUPPORTED  # 2D
+    assert b"MPM_PREC_DW" in L.mpm_last_error()
+    grid, solids, alg, data = scenarios.taylor_bar(h=2e-3)
+    for kw in ({"algorithm": "musl"}, {"basis": "quad"}, {"contact": True}):
+        d = Descriptors(grid, solids, tolerance=alg.tolerance, dt=data["dt"], precision="dw", **kw)
+        assert L.mpm_create(C.byref(d.grid), d.bodies, len(solids), C.byref(d.params), C.byref(h)) == \
+            _capi.MPM_ERR_UNSUPPORTED, kw
+    from jump_gb300.material import NeoHookeanMaterial
+    m = solids[0].mat
+    solids[0].mat = NeoHookeanMaterial(m.E, m.nu, m.density, solids[0].parCount)
+    d = Descriptors(grid, solids, tolerance=alg.tolerance, dt=data["dt"], precision="dw")
+    assert L.mpm_create(C.byref(d.grid), d.bodies, len(solids), C.byref(d.params), C.byref(h)) == \
+        _capi.MPM_ERR_UNSUPPORTED  # neo-Hookean
+    assert not h.value
+    assert L.mpm_batch_create(None, 0, _capi.MPM_PREC_DW, C.byref(h)) == _capi.MPM_ERR_ARG
+    assert L.mpm_probe_dw(99, 1, None, None, None, None) == _capi.MPM_ERR_ARG
 
 
 def test_python_constants_match_the_header():

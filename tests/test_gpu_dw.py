@@ -1,0 +1,245 @@
+"""The double-word G2P (MPM_PREC_DW): FP64 particle fields and P2G; the G2P
+and the constitutive update in pairs of floats hi + lo.
+
+* Each double-word operation (mpm_probe_dw) against exact rational arithmetic
+  on seeded operands spanning the step's magnitudes (1e-12 .. 1e12, both signs,
+  near-cancelling sums): u = 2^-24; relative error (products, square, square
+  root, reciprocal) or error relative to |x| + |y| (sums, c + a b) within the
+  stated multiple of u^2.
+* The FP64 -> double-word conversion: hi is the double rounded to nearest float,
+  hi + lo equals it to u^2 relative, and the conversion back is the correctly
+  rounded FP64 value of hi + lo.
+* The step against the FP64 oracle: the golden 3D J2 and linear elastic cases,
+  the coarse Taylor bar over 100 steps, particles on grid nodes (zero gradient
+  factors), a particle that leaves the grid; the full-size bar is in
+  test_gpu_fullsize.py."""
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from cases import descriptors, field_errors, golden_expected, load_golden, particle_errors, rel_err
+from jump_gb300 import _capi, scenarios
+from jump_gb300.engine import MPMContext
+from jump_gb300.probe import dw_op
+
+pytestmark = pytest.mark.gpu
+
+U2 = Fraction(1, 2 ** 48)  # u^2, u = 2^-24
+FP64_TOL = 1e-10
+J2_FIELDS = ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain", "vmstr")
+
+
+def operands(n, seed, lo=-12, hi=12, positive=False):
+    r = np.random.default_rng(seed)
+    x = r.uniform(1.0, 10.0, n) * 10.0 ** r.uniform(lo, hi, n)
+    if not positive:
+        x *= r.choice([-1.0, 1.0], n)
+    return x
+
+
+def exact(hi, lo):
+    return [Fraction(float(a)) + Fraction(float(b)) for a, b in zip(hi, lo)]
+
+
+def dw_values(a):
+    """the double-word values the device converts a to (exact rationals)"""
+    return exact(*dw_op(_capi.MPM_DW_OP_FROM_F64, a))
+
+
+def worst(errs):
+    return float(max(errs)) if errs else 0.0
+
+
+def test_conversion_from_and_to_f64():
+    a = np.concatenate([operands(4000, 1), [0.0, -0.0, 1.0, -2.5, 1e-30, 3e30]])
+    hi, lo = dw_op(_capi.MPM_DW_OP_FROM_F64, a)
+    np.testing.assert_array_equal(hi, a.astype(np.float32).astype(np.float64))
+    assert np.all(np.abs(lo) <= np.abs(hi) * 2.0 ** -24)
+    errs = [abs(Fraction(float(x)) - v) / abs(Fraction(float(x))) for x, v in zip(a, exact(hi, lo)) if x != 0]
+    assert worst(errs) <= U2, worst(errs)
+    assert np.signbit(hi[a.size - 5]) and hi[a.size - 5] == 0.0  # -0.0 keeps its sign
+    # back to FP64: hi + lo correctly rounded, a low part below the float
+    # normal range (|x| < ~2^-102) flushed to zero
+    back, _ = dw_op(_capi.MPM_DW_OP_TO_F64, a)
+    lo_n = np.where(np.abs(lo) < 2.0 ** -126, 0.0, lo)
+    want = np.array([float(v) for v in exact(hi, lo_n)])
+    np.testing.assert_array_equal(back, want)
+    assert lo[a.size - 2] != 0.0 and back[a.size - 2] == hi[a.size - 2]  # 1e-30: its low part is subnormal
+
+
+@pytest.mark.parametrize("op, bound", [(_capi.MPM_DW_OP_ADD, 4), (_capi.MPM_DW_OP_SUB, 4)])
+def test_sums(op, bound):
+    n = 2000
+    a = operands(n, 2)
+    b = operands(n, 3)
+    b[: n // 4] = -a[: n // 4] * (1.0 + operands(n // 4, 4, lo=-15, hi=-3, positive=True))  # near-cancelling
+    if op == _capi.MPM_DW_OP_SUB:
+        b[: n // 4] = -b[: n // 4]
+    x, y = dw_values(a), dw_values(b)
+    hi, lo = dw_op(op, a, b)
+    sgn = 1 if op == _capi.MPM_DW_OP_ADD else -1
+    errs = [abs(r - (p + sgn * q)) / ((abs(p) + abs(q)) * U2) for r, p, q in zip(exact(hi, lo), x, y)]
+    assert worst(errs) <= bound, worst(errs)
+
+
+@pytest.mark.parametrize("op, bound", [(_capi.MPM_DW_OP_MUL, 5), (_capi.MPM_DW_OP_MUL_FLOAT, 3),
+                                       (_capi.MPM_DW_OP_SQR, 5)])
+def test_products(op, bound):
+    n = 2000
+    a, b = operands(n, 5, -10, 10), operands(n, 6, -10, 10)
+    x, y = dw_values(a), dw_values(b)
+    if op == _capi.MPM_DW_OP_MUL_FLOAT:
+        y = [Fraction(float(np.float32(v))) for v in b]
+    if op == _capi.MPM_DW_OP_SQR:
+        y = x
+    hi, lo = dw_op(op, a, b)
+    errs = [abs(r - p * q) / (abs(p * q) * U2) for r, p, q in zip(exact(hi, lo), x, y)]
+    assert worst(errs) <= bound, worst(errs)
+
+
+def test_fma():
+    n = 2000
+    a, b, c = operands(n, 7, -8, 8), operands(n, 8, -8, 8), operands(n, 9, -8, 8)
+    c[: n // 4] = -a[: n // 4] * b[: n // 4] * (1.0 + operands(n // 4, 10, -15, -3, positive=True))
+    x, y, z = dw_values(a), dw_values(b), dw_values(c)
+    hi, lo = dw_op(_capi.MPM_DW_OP_FMA, a, b, c)
+    errs = [abs(r - (p * q + s)) / ((abs(p * q) + abs(s)) * U2) for r, p, q, s in zip(exact(hi, lo), x, y, z)]
+    assert worst(errs) <= 8, worst(errs)
+
+
+def test_sqrt_and_reciprocal():
+    n = 2000
+    a = operands(n, 11, -20, 20, positive=True)
+    x = dw_values(a)
+    hi, lo = dw_op(_capi.MPM_DW_OP_SQRT, a)
+    # |r^2 - x| / x ~ 2 |r - sqrt x| / sqrt x: relative error of the root from its square
+    errs = [abs(r * r - p) / (2 * p * U2) for r, p in zip(exact(hi, lo), x)]
+    assert worst(errs) <= 4, worst(errs)
+    b = operands(n, 12, -20, 20)
+    y = dw_values(b)
+    hi, lo = dw_op(_capi.MPM_DW_OP_RECIP, b)
+    errs = [abs(r * p - 1) / U2 for r, p in zip(exact(hi, lo), y)]
+    assert worst(errs) <= 6, worst(errs)
+    hi, lo = dw_op(_capi.MPM_DW_OP_SQRT, np.array([0.0, -1.0]))
+    assert np.all(hi == 0.0) and np.all(lo == 0.0)
+
+
+def test_one_minus():
+    a = np.random.default_rng(13).uniform(0.0, 1.0, 2000)
+    a[:5] = [0.0, 1.0, 0.5, 1.0 - 2.0 ** -30, 2.0 ** -40]
+    x = dw_values(a)
+    hi, lo = dw_op(_capi.MPM_DW_OP_ONE_MINUS, a)
+    errs = [abs(r - (1 - p)) / U2 for r, p in zip(exact(hi, lo), x)]
+    assert worst(errs) <= 3, worst(errs)
+
+
+# ---------------------------------------------------------------------------
+# the step
+
+
+@pytest.mark.parametrize("name", ["taylor_mini_j2_6", "spheres_elastic_12"])
+def test_golden_3d_cases(name):
+    grid, solids, tol, bf, dt, nsteps, z = load_golden(name)
+    g = MPMContext(descriptors(grid, solids, tol, bf, dt, precision="dw"))
+    g.step(nsteps)
+    for b, st in enumerate(g.download_all()):
+        for k, v in golden_expected(z, b).items():
+            assert rel_err(getattr(st, k), v) <= FP64_TOL, (name, b, k, rel_err(getattr(st, k), v))
+    g.close()
+
+
+def test_taylor_bar_small_100_steps_vs_oracle(oracle_lib):
+    """The coarse J2 bar (h = 5e-4) over 100 steps from the impact: the
+    double-word G2P against the FP64 oracle at the FP64 path's bound."""
+    grid, solids, alg, data = scenarios.taylor_bar(h=5e-4)
+    scenarios.apply_dirichlet(grid, data)
+    mk = lambda **kw: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], **kw)
+    g, o = MPMContext(mk(precision="dw")), oracle_lib.OracleContext(mk())
+    g.step(100)
+    o.step(100)
+    sg, so = g.download_all(), o.download_all()
+    assert np.max(so[0].alpha) > 0, "the bar must yield"
+    fm = {f: e for (_, f), e in field_errors(sg, so, fields=J2_FIELDS).items()}
+    pp = particle_errors(sg, so, fields=J2_FIELDS)
+    print("\ntaylor_bar_small_100_dw", fm, pp)
+    assert max(fm.values()) <= FP64_TOL, fm
+    g.close()
+    o.close()
+
+
+def test_particles_on_grid_nodes_3d(oracle_lib):
+    """Particles exactly on node lines (zero gradient factors, the general
+    branch of the z factor) and on cell faces."""
+    from jump_gb300.grid import Grid3D
+    from jump_gb300.material import ElasticMaterial
+    from jump_gb300.solid import Solid3D
+    ax = np.arange(0.25, 0.76, 0.125)
+    grid = Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, 5, 5, 5)
+    xs = np.array([[a, b, c] for a in ax for b in ax for c in ax])
+    vol = 0.125 ** 3
+    s = Solid3D(xs, ElasticMaterial(1e3, 0.3, 1000.0, len(xs)))
+    s.mass[:] = 1000.0 * vol
+    s.volume[:] = vol
+    s.volumeInitial[:] = vol
+    s.velocity[:] = 0.01 * (xs - 0.5)
+    mk = lambda **kw: descriptors(grid, [s], 0.0, None, 1e-3, **kw)
+    g, o = MPMContext(mk(precision="dw")), oracle_lib.OracleContext(mk())
+    assert g.step(10, check=False) == o.step(10, check=False) == _capi.MPM_OK
+    sg, so = g.download_all(), o.download_all()
+    assert np.abs(so[0].strain).max() > 1e-5
+    errs = field_errors(sg, so, fields=("pos", "velocity", "volume", "F"))
+    assert max(errs.values()) <= FP64_TOL, errs
+    assert np.max(np.abs(sg[0].strain - so[0].strain)) <= 1e-12
+    assert np.max(np.abs(sg[0].stress - so[0].stress)) <= 1e-12 * 1e3
+    g.close()
+    o.close()
+
+
+def test_particle_leaving_the_grid(oracle_lib):
+    """A particle alone in its cell runs out through x = 1: MPM_ERR_OUT_OF_GRID
+    from both, and it stays frozen where it left."""
+    from jump_gb300.grid import Grid3D
+    from jump_gb300.material import ElasticMaterial
+    from jump_gb300.solid import Solid3D
+    grid = Grid3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0, 11, 11, 11)
+    xs = np.array([[0.45, 0.5, 0.52], [0.55, 0.5, 0.52], [0.95, 0.5, 0.52]])
+    s = Solid3D(xs, ElasticMaterial(1e3, 0.3, 1000.0, 3))
+    s.mass[:] = 1000.0 * 1e-4
+    s.volume[:] = 1e-4
+    s.volumeInitial[:] = 1e-4
+    s.velocity[2] = [60.0, 0.0, 0.0]
+    mk = lambda **kw: descriptors(grid, [s], 0.0, None, 1e-3, **kw)
+    g, o = MPMContext(mk(precision="dw")), oracle_lib.OracleContext(mk())
+    assert g.step(20, check=False) == o.step(20, check=False) == _capi.MPM_ERR_OUT_OF_GRID
+    sg, so = g.download_all(), o.download_all()
+    assert sg[0].pos[2, 0] > 1.0
+    np.testing.assert_allclose(sg[0].pos, so[0].pos, rtol=1e-13)
+    before = sg[0].pos[2].copy()
+    g.step(3, check=False)
+    np.testing.assert_array_equal(g.download_all()[0].pos[2], before)
+    g.close()
+    o.close()
+
+
+def test_launch_settings_and_tuner(oracle_lib):
+    """A double-word context takes the per-lane atomic P2G only: the tuner
+    probes its CTA sizes and sort intervals, another strategy is refused, and
+    a tuned, cell-sorted run still matches the oracle."""
+    grid, solids, alg, data = scenarios.taylor_bar(h=1e-3)
+    scenarios.apply_dirichlet(grid, data)
+    mk = lambda **kw: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], **kw)
+    g = MPMContext(mk(precision="dw"))
+    with pytest.raises(_capi.MPMError) as e:
+        g.set_launch(p2g="warp")
+    assert e.value.code == _capi.MPM_ERR_ARG
+    r = g.tune(probe_steps=2)
+    assert r["probes"] and all(k.startswith("atomic/") for k in r["probes"])
+    g.set_launch(threads=128, sort_interval=4)
+    o = oracle_lib.OracleContext(mk())
+    g.step(30)
+    o.step(30)
+    errs = field_errors(g.download_all(), o.download_all(), fields=J2_FIELDS)
+    assert max(errs.values()) <= FP64_TOL, errs
+    g.close()
+    o.close()

@@ -3,8 +3,8 @@
 * The Taylor bar of the headline benchmark: 511,784 particles, J2 plasticity,
   100 steps from the impact, every particle field of the GPU run against the
   oracle (OpenMP: its node sums are re-associated slab by slab, which by itself
-  moves the results by ~1e-14); and the FP32-particle variant's error on the
-  same run.
+  moves the results by ~1e-14); the FP32-particle variant's error on the same
+  run; and the double-word G2P (MPM_PREC_DW) at the FP64 bounds.
 * The 512-problem two-disk ensemble (seeded instances, 132..9,096 particles,
   20^2..80^2 cells) over the configuration's 1000 steps in one batched launch,
   both batch strategies, against the oracle for 16 problems that span the
@@ -80,6 +80,21 @@ def test_taylor_bar_full_size_fp32_error_stated(bar_100):
     # stated bounds for this configuration: 0.25 per field, 1e-4 for positions
     assert max(fm.values()) <= 0.25, fm
     assert fm["pos"] <= 1e-4, fm
+
+
+def test_taylor_bar_full_size_double_word_vs_oracle(bar_100):
+    """MPM_PREC_DW (FP64 fields and P2G, double-word FP32 G2P) on the same 100
+    steps against the FP64 oracle, with the FP64 path's bounds."""
+    mk, so = bar_100
+    g = MPMContext(mk(precision="dw"))
+    g.step(100)
+    sg = g.download_all()
+    g.close()
+    fm = {f: e for (_, f), e in field_errors(sg, so, fields=J2_FIELDS).items()}
+    pp = particle_errors(sg, so, fields=J2_FIELDS)
+    print("\ntaylor_bar_full_100_dw", json.dumps({"field_max": fm, "per_particle_floor_1e-3": pp}))
+    assert max(fm.values()) <= FP64_TOL, fm
+    assert max(pp.values()) <= 2e-8, pp
 
 
 @pytest.fixture(scope="module")
