@@ -9,8 +9,13 @@ particles.  Inputs are synthetic (generated from the geometry).  The
 particle state (~160 MB) and grid (~70 MB) exceed the 129 MB L2, so no L2
 flush is needed between steps.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision f64|f32]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision f64|f32|dw]
   python bench.py --impl reference ...   # the CPU restatement on the host cores
+
+The default FP64 line also carries "double_word": the MPM_PREC_DW variant of
+the same step (FP64 fields and node sums, P2G and G2P arithmetic in
+double-word FP32) timed the same way, with its roofline and its largest
+relative difference per field from the FP64 run at the same step.
 
 Prints one JSON line on rank 0.
 """
@@ -53,6 +58,8 @@ BYTES = {
     "f64": {"p2g": 112 + 7, "g2p": 520 + 6, "step": 600},
     "f32": {"p2g": 56 + 7, "g2p": 260 + 3, "step": 330},
 }
+# the double-word variant keeps the FP64 fields and nodes: the same bytes
+BYTES["dw"] = BYTES["f64"]
 # MUSL, FP64, 3D J2: P2G as above; the G2P stage is G2P-1 (reads x3 v3 m, writes v3
 # = 80 B, + P2G-2 grid share 3 doubles/node) and G2P-2 (reads x3 v3 V0 F9 eps6 alpha
 # ep6, writes x3 V F9 eps6 sigma6 alpha ep6 vm = 496 B, + 6 doubles/node gathered)
@@ -213,7 +220,7 @@ class ClockSampler:
 # on the GPU in steps of 25 (the FP64 J2 bar fails at the same step in the
 # oracle).  MUSL and the B-spline bases ran 2200 steps without one.  The late
 # window and the end-to-end solve stay within 80% of it.
-HEALTHY_STEPS = {("j2", "f64"): 1450, ("j2", "f32"): 925, ("jc", "f64"): 1250, ("jc", "f32"): 1250,
+HEALTHY_STEPS = {("j2", "f64"): 1450, ("j2", "dw"): 1450, ("j2", "f32"): 925, ("jc", "f64"): 1250, ("jc", "f32"): 1250,
                  ("jcdamage", "f64"): 200, ("jcdamage", "f32"): 100}
 
 
@@ -486,6 +493,10 @@ def run_ours(args):
                 "peak": fma.value, "unit": "FP64 inst/s", "frac": ach / fma.value,
                 "peak_source": "mpm_probe_rates (FP64 FMA throughput, this run)"}
     step_bytes = table["step"] * npart
+    # the FP64 state after warm-up, timed steps and stage profile, for the
+    # double-word variant's comparison (which runs the same sequence)
+    fp64_state = ctx.download_all() if (world == 1 and args.extras and args.workload == "taylor_bar" and
+                                        args.precision == "f64") else None
     late = None
     if world == 1 and args.workload == "taylor_bar" and args.late_steps > 0:
         used = args.warmup + args.steps + nprof
@@ -539,6 +550,7 @@ def run_ours(args):
     extras = {}
     if world == 1 and args.extras and args.workload == "taylor_bar" and args.precision == "f64":
         # the benchmark spec's other three targets, each on its own workload
+        extras["double_word"] = measure_double_word(args, mk, npart, nprof, fp64_state, peak, peak_kind)
         extras["ensemble"] = measure_ensemble(args, "ensemble", "f64", 512, 1000)
         extras["adjoint"] = measure_adjoint(args, 2000)
         extras["impact_jvp"] = measure_impact_jvp(args, 64, 200)
@@ -598,6 +610,45 @@ def run_ours(args):
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def measure_double_word(args, mk_fp64, npart, nprof, fp64_state, peak, peak_kind):
+    """The MPM_PREC_DW variant of the same step (FP64 fields and node sums, the P2G
+    and G2P arithmetic in double-word FP32): the same warm-up, timed steps and
+    stage profile as the FP64 context, its device throughput and HBM roofline,
+    and the largest relative difference per field from the FP64 state at the
+    same step.  Reported beside the FP64 headline, not as it."""
+    from jump_gb300 import _capi
+    from jump_gb300.engine import MPMContext
+    d = mk_fp64()
+    d.params.precision = _capi.MPM_PREC_DW  # the same descriptors
+    ctx = MPMContext(d)
+    ctx.step(args.warmup)
+    ctx.step(args.steps)
+    dev_ms = ctx.last_step_ms()
+    st = ctx.profile_stages(nprof)
+    per = {k: v / nprof for k, v in st.items()}
+    dom = max(("p2g", "g2p"), key=lambda k: per[k])
+    states = ctx.download_all()
+    launch = ctx.launch()
+    ctx.close()
+    err = {}
+    for f in ("pos", "velocity", "volume", "F", "strain", "stress", "alpha", "pstrain"):
+        a = np.concatenate([np.ravel(getattr(x, f)) for x in states])
+        b = np.concatenate([np.ravel(getattr(x, f)) for x in fp64_state])
+        den = float(np.max(np.abs(b))) or 1.0
+        err[f] = float(np.max(np.abs(a - b)) / den)
+    achieved = BYTES["dw"][dom] * npart / (per[dom] * 1e-3) / 1e9
+    return {"precision": "dw", "value": npart * args.steps / (dev_ms * 1e-3), "unit": METRIC,
+            "ms_per_step": dev_ms / args.steps, "stage_ms_per_step": per, "launch": launch,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": ncu_traffic(dom, "dw"),
+                         "step_frac": BYTES["dw"]["step"] * npart / (dev_ms * 1e-3 / args.steps) / 1e9 / peak},
+            "max_rel_diff_vs_fp64_gpu": err,
+            "steps_compared": args.warmup + args.steps + nprof,
+            "what": "FP64 particle fields and node accumulators; P2G and G2P arithmetic in double-word FP32 "
+                    "(float pairs, 2^-49 relative per rounding); not the FP64 headline"}
 
 
 ENSEMBLES = {
@@ -945,7 +996,7 @@ def main():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "dw"])
     ap.add_argument("--algorithm", default="usl", choices=["usl", "musl"],
                     help="update scheme: USL (the headline) or MUSL (FLIP/PIC blend --alpha)")
     ap.add_argument("--alpha", type=float, default=1.0, help="MUSL FLIP/PIC blend")

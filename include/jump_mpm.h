@@ -309,8 +309,8 @@ int mpm_probe_rates(double* fp64_fma_per_s, double* fp64_div_per_s, double* fp64
 /* Test aid (no counterpart in the reference): the double-word operation op of
    the MPM_PREC_DW arithmetic on n operand triples (a[i], b[i], c[i]), each
    first converted FP64 -> double-word; out[2i] and out[2i + 1] receive the
-   result's float parts (hi, lo) as doubles (MPM_DW_OP_TO_F64: the FP64 value
-   of a[i] after the conversion and back, and 0).  MPM_DW_OP_MUL_FLOAT
+   result's float parts (hi, lo) as doubles (MPM_DW_OP_TO_F64: the double-word
+   sum a[i] + b[i] rounded to FP64 by an FP64 add of its exact parts, and 0).  MPM_DW_OP_MUL_FLOAT
    multiplies by the high part of b[i]; MPM_DW_OP_FMA is a[i] b[i] + c[i]. */
 #define MPM_DW_OP_FROM_F64  0
 #define MPM_DW_OP_ADD       1

@@ -93,7 +93,7 @@ __global__ void dw_probe_kernel(int op, int64_t n, const double* a, const double
     default: break;  // MPM_DW_OP_FROM_F64: the conversion itself
   }
   if (op == MPM_DW_OP_TO_F64) {
-    out[2 * i] = dw_to_f64(x);
+    out[2 * i] = dw_to_f64(x + y);
     out[2 * i + 1] = 0.0;
     return;
   }

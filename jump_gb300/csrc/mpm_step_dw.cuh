@@ -164,7 +164,8 @@ __device__ __forceinline__ void p2g_dw_particle(const GridP& g, const NodeP& nd,
 #pragma unroll
       for (int a = 0; a < 3; ++a) atomicAdd(nd.p0 + a * Nn + n, dw_to_f64(Nm * v[a]));
 #pragma unroll
-      for (int a = 0; a < 3; ++a) atomicAdd(nd.f + a * Nn + n, dw_to_f64(dw_fma(P[a], Nz, dw_scale(Q[a], sz))));
+      for (int a = 0; a < 3; ++a)
+        atomicAdd(nd.f + a * Nn + n, dw_to_f64(dw_fma(P[a], Nz, dw_scale(Q[a], sz))));
     }
   }
 }

@@ -59,13 +59,34 @@ def test_conversion_from_and_to_f64():
     errs = [abs(Fraction(float(x)) - v) / abs(Fraction(float(x))) for x, v in zip(a, exact(hi, lo)) if x != 0]
     assert worst(errs) <= U2, worst(errs)
     assert np.signbit(hi[a.size - 5]) and hi[a.size - 5] == 0.0  # -0.0 keeps its sign
-    # back to FP64: hi + lo correctly rounded, a low part below the float
-    # normal range (|x| < ~2^-102) flushed to zero
+    # back to FP64 (the sum with 0): hi + lo correctly rounded, a low part
+    # below the float normal range (|x| < ~2^-102) flushed to zero
     back, _ = dw_op(_capi.MPM_DW_OP_TO_F64, a)
     lo_n = np.where(np.abs(lo) < 2.0 ** -126, 0.0, lo)
     want = np.array([float(v) for v in exact(hi, lo_n)])
     np.testing.assert_array_equal(back, want)
     assert lo[a.size - 2] != 0.0 and back[a.size - 2] == hi[a.size - 2]  # 1e-30: its low part is subnormal
+
+
+def test_rounding_to_f64():
+    """dw_to_f64 against the correctly rounded FP64 value of hi + lo for pairs
+    whose low part lies 24 .. 80 bits below the high part, of either sign, on
+    powers of two (the low part lowering them into the binade below) and on
+    exact ties of the last FP64 place."""
+    r = np.random.default_rng(14)
+    n = 3000
+    a = operands(n, 15, -6, 6)
+    a[:600] = np.ldexp(1.0, r.integers(-20, 20, 600)) * r.choice([-1.0, 1.0], 600)  # powers of two
+    b = a * r.choice([-1.0, 1.0], n) * np.ldexp(r.uniform(1.0, 2.0, n), -r.integers(24, 80, n))
+    # ties: float-exact high parts and low parts of half a unit of their last FP64 place
+    a[600:900] = a[600:900].astype(np.float32).astype(np.float64)
+    b[600:900] = np.ldexp(1.0, np.frexp(a[600:900])[1] - 54) * r.choice([-1.0, 1.0], 300)
+    hi, lo = dw_op(_capi.MPM_DW_OP_ADD, a, b)
+    back, _ = dw_op(_capi.MPM_DW_OP_TO_F64, a, b)
+    lo_n = np.where(np.abs(lo) < 2.0 ** -126, 0.0, lo)
+    want = np.array([float(v) for v in exact(hi, lo_n)])
+    np.testing.assert_array_equal(back, want)
+    assert np.any(lo[:600] * hi[:600] < 0) and np.all(lo[600:900] == b[600:900])
 
 
 @pytest.mark.parametrize("op, bound", [(_capi.MPM_DW_OP_ADD, 4), (_capi.MPM_DW_OP_SUB, 4)])
