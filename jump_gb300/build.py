@@ -27,8 +27,8 @@ NVCC_FLAGS = ARCH + [
 ]
 
 SOURCES = ["mpm_k2d.cu", "mpm_k3d.cu", "mpm_capi.cu", "mpm_static.cu", "mpm_batch.cu", "mpm_probe.cu"]
-HEADERS = ["mpm_common.cuh", "mpm_kernels.cuh", "mpm_launch.cuh", "mpm_internal.h", "mpm_sparse.cuh",
-           "mpm_adjoint.cuh", "mpm_wide.cuh", "mpm_tangent.cuh", "mpm_musl.cuh", "mpm_bspline.cuh"]
+# every header of csrc/ is a dependency of every translation unit
+HEADERS = sorted(f for f in os.listdir(CSRC) if f.endswith((".cuh", ".h")))
 
 
 def nvcc() -> str:

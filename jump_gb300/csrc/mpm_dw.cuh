@@ -101,6 +101,30 @@ __device__ __forceinline__ dw dw_fma(dw a, dw b, dw c) {
   return dw_make(zh, zl);
 }
 
+// A sum of DW products kept as its leading float sum s (each product's
+// leading part added by TwoSum) and the float sum c of every error term, so a
+// term costs TwoProd, two cross FMAs, TwoSum and two adds; one TwoSum turns
+// (s, c) into a DW at the end (s may cancel below c, so not Fast2Sum).  The
+// error stays a small multiple of u^2 times the sum of the terms' magnitudes.
+struct dw_acc {
+  float s, c;
+};
+
+__device__ __forceinline__ void acc_fma(dw_acc& acc, dw a, dw b) {
+  float ph, pl, sh, sl;
+  two_prod(a.hi, b.hi, ph, pl);
+  pl = __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.lo, pl));
+  two_sum(acc.s, ph, sh, sl);
+  acc.s = sh;
+  acc.c = __fadd_rn(acc.c, __fadd_rn(sl, pl));
+}
+
+__device__ __forceinline__ dw acc_value(dw_acc acc) {
+  float zh, zl;
+  two_sum(acc.s, acc.c, zh, zl);
+  return dw_make(zh, zl);
+}
+
 __device__ __forceinline__ dw dw_sqr(dw x) {
   float ph, pl, zh, zl;
   two_prod(x.hi, x.hi, ph, pl);

@@ -10,10 +10,10 @@
 // value plus the step's DW increment rounded to FP64, so the state keeps its
 // 53 bits and only the increment carries the DW rounding; the stress is the
 // FP64 value of its DW result, and V = J V0 that of J V0 with det F in DW.
-// Loads convert FP64 -> DW on the integer pipe.  The P2G's hat is the FP64
-// one (the cell and the zero gradient factors bit for bit those of the FP64
-// step, stored for the G2P in the hat cache), its node values DW, each added
-// to its FP64 node accumulator as an FP64 value.  The grid update writes each
+// Loads convert FP64 -> DW on the integer pipe.  The P2G's hat has the FP64
+// hat's cell and zero gradient factors bit for bit and its weights in DW
+// (hat_dw, stored for the G2P in the hat cache as DW pairs); its node values
+// are DW, each added to its FP64 node accumulator as an FP64 value.  The grid update writes each
 // node's vdt and dv as DW records (NodeP::dw4, three float4 per node), so the
 // G2P's corner gathers need no conversion.  The G2P's particle inputs are
 // copied into the thread's shared-memory slots by cp.async at the start, so
@@ -24,41 +24,87 @@
 
 namespace jmpm {
 
-// The hat of particle p from the cache the P2G of this step stored
-// (PartP::hat_c / hat_nl, FP64): base cells, hat values at the lower and upper
-// node, and the gradient factors as signs (gl = sl dxI, gh = sh dxI with
-// sl, sh in {-1, 0, +1}).  False when the P2G found the particle outside.
+// The hat of particle p from the cache the P2G of this step stored (hat_dw):
+// base cells, hat values at the lower and upper node, and the gradient factors
+// as signs (gl = sl dxI, gh = sh dxI with sl, sh in {-1, 0, +1}).  False when
+// the P2G found the particle outside.
 struct HatDW {
   int c[3];
   dw Nl[3], Nh[3];
   float sl[3], sh[3];
 };
 
+// the sign of an FP64 gradient factor or coordinate difference as a float
+__device__ __forceinline__ float sign_of(double gfac) {
+  return is_zero_bits(gfac) ? 0.f : (is_neg_bits(gfac) ? -1.f : 1.f);
+}
+
+// The hat of particle p at position x (FP64) for the DW step: the cell the
+// FP64 hat() chooses, bit for bit -- its t = (x - xmin) dxI + 1 estimated in
+// FP32 and floored when the estimate lies farther from an integer than its
+// error bound, else formed in FP64 as hat() forms it -- the differences
+// dl = x - x_lower, dh = x - x_upper in FP64 (exact, as in hat()), their signs
+// for the gradient factors, and Nl = 1 - |dl| dxI, Nh = 1 - Nl in DW.
+// The cache (PartP::hat_c codes, hat_nl as DW pairs) is written for the G2P.
+__device__ __forceinline__ bool hat_dw(const GridP& g, const PartP& pp, int64_t p, const double* x, HatDW& h) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float xf = dw_from(x[a]).hi;
+    const float u = __fsub_rn(xf, g.xminf[a]);
+    const float t32 = __fmaf_rn(u, g.dxIf[a], 1.0f);
+    // |t32 - t| <= 4 u32 ((|x| + |xmin|) dxI + t + 1), u32 = 2^-24
+    const float bound = 0x1p-22f * __fmaf_rn(__fadd_rn(fabsf(xf), fabsf(g.xminf[a])), g.dxIf[a], fabsf(t32) + 1.0f);
+    const float fl = floorf(t32);
+    int i1;
+    if (t32 - fl > bound && fl + 1.0f - t32 > bound) {
+      i1 = int(fl);
+    } else {
+      const double t = add_rn(mul_rn(sub_rn(x[a], g.xmin[a]), g.dxI[a]), 1.0);
+      i1 = floor_to_int(t);
+    }
+    if (i1 < 1 || i1 > int(g.nn[a] - 1)) {
+      if (pp.hat_c)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) pp.hat_c[b * pp.pitch + p] = -1;
+      return false;
+    }
+    const int c = i1 - 1;
+    h.c[a] = c;
+    const double dl = sub_rn(x[a], g.coord[a][c]), dh = sub_rn(x[a], g.coord[a][c + 1]);
+    h.sl[a] = -sign_of(dl);
+    h.sh[a] = -sign_of(dh);
+    h.Nl[a] = dw_one_minus(dw_from(fabs(dl)) * dw_c(g.w_dxI[a]));
+    h.Nh[a] = dw_one_minus(h.Nl[a]);
+  }
+  if (pp.hat_c) {
+    float2* nl = static_cast<float2*>(pp.hat_nl);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      pp.hat_c[a * pp.pitch + p] = h.c[a] | (int32_t(h.sl[a] == 0.f) << 27) | (int32_t(h.sl[a] < 0.f) << 28) |
+                                   (int32_t(h.sh[a] == 0.f) << 29) | (int32_t(h.sh[a] < 0.f) << 30);
+      nl[a * pp.pitch + p] = make_float2(h.Nl[a].hi, h.Nl[a].lo);
+    }
+  }
+  return true;
+}
+
+// The hat the P2G of this step cached (hat_dw), or, without a cache, hat_dw
+// of the position.  False when the particle is outside.
 __device__ __forceinline__ bool hat_get_dw(const GridP& g, const PartP& pp, int64_t p, HatDW& h) {
   if (!pp.hat_c) {
-    // no cache: the FP64 hat of the position, converted
-    Hat<3, double> hd;
     double x[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) x[a] = *field<double>(pp, Layout<3>::X + a, p);
-    if (!hat<3, double>(g, x, hd)) return false;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      h.c[a] = hd.c[a];
-      h.Nl[a] = dw_from(hd.Nl[a]);
-      h.Nh[a] = dw_one_minus(h.Nl[a]);
-      h.sl[a] = is_zero_bits(hd.gl[a]) ? 0.f : (is_neg_bits(hd.gl[a]) ? -1.f : 1.f);
-      h.sh[a] = is_zero_bits(hd.gh[a]) ? 0.f : (is_neg_bits(hd.gh[a]) ? -1.f : 1.f);
-    }
-    return true;
+    return hat_dw(g, pp, p, x, h);
   }
-  const double* nl = static_cast<const double*>(pp.hat_nl);
+  const float2* nl = static_cast<const float2*>(pp.hat_nl);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const int32_t code = pp.hat_c[a * pp.pitch + p];
     if (code < 0) return false;
     h.c[a] = code & ((1 << 27) - 1);
-    h.Nl[a] = dw_from(nl[a * pp.pitch + p]);
+    const float2 w = nl[a * pp.pitch + p];
+    h.Nl[a] = dw_make(w.x, w.y);
     h.Nh[a] = dw_one_minus(h.Nl[a]);
     h.sl[a] = ((code >> 27) & 1) ? 0.f : (((code >> 28) & 1) ? -1.f : 1.f);
     h.sh[a] = ((code >> 29) & 1) ? 0.f : (((code >> 30) & 1) ? -1.f : 1.f);
@@ -85,11 +131,6 @@ __device__ __forceinline__ NodeDW node_dw(const float4* r, int64_t n) {
 
 __device__ __forceinline__ void put_f64(const PartP& pp, int f, int64_t p, double v) { *field<double>(pp, f, p) = v; }
 
-// the sign of an FP64 gradient factor (0 or +-dxI) as a float
-__device__ __forceinline__ float sign_of(double gfac) {
-  return is_zero_bits(gfac) ? 0.f : (is_neg_bits(gfac) ? -1.f : 1.f);
-}
-
 // ---------------------------------------------------------------------------
 // P2G of particle pp.begin + t: mass m N, momentum m N v and force
 // -V sigma grad N + m g N at its 8 corners, one FP64 atomic per value at L2.
@@ -105,23 +146,14 @@ __device__ __forceinline__ void p2g_dw_particle(const GridP& g, const NodeP& nd,
   double xd[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) xd[a] = *field<double>(pp, L::X + a, p);
-  Hat<3, double> h{};
-  const bool ok = hat<3, double>(g, xd, h);
-  hat_put<3, double>(pp, p, ok, h);  // for the G2P of this step
-  if (!ok) {
+  HatDW h;
+  if (!hat_dw(g, pp, p, xd, h)) {  // cached for the G2P of this step
     atomicOr(status, ST_OUT_OF_GRID);
     return;
   }
   if (nd.bflag) mark_blocks<3>(nd, h.c);
-  dw Nl[3], Nh[3];
-  float sl[3], sh[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    Nl[a] = dw_from(h.Nl[a]);
-    Nh[a] = dw_from(h.Nh[a]);
-    sl[a] = sign_of(h.gl[a]);
-    sh[a] = sign_of(h.gh[a]);
-  }
+  const dw(&Nl)[3] = h.Nl, (&Nh)[3] = h.Nh;
+  const float(&sl)[3] = h.sl, (&sh)[3] = h.sh;
   const dw m = dw_from(*field<double>(pp, L::M, p)), V = dw_from(*field<double>(pp, L::VOL, p));
   dw v[3], cs[3][3], mg[3];
 #pragma unroll
@@ -220,12 +252,12 @@ __device__ __forceinline__ void g2p_dw_particle(const GridP& g, const NodeP& nd,
   }
   const int64_t base = int64_t(h.c[0]) + g.nx * int64_t(h.c[1]) + g.nxy * int64_t(h.c[2]);
   // increments of x and v, and the gradient sums
-  dw dx[3], dvp[3], Ls[3][3];
+  dw_acc dx[3], dvp[3], Ls[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    dx[a] = dvp[a] = dw_make(0.f, 0.f);
+    dx[a] = dvp[a] = dw_acc{0.f, 0.f};
 #pragma unroll
-    for (int j = 0; j < 3; ++j) Ls[a][j] = dw_make(0.f, 0.f);
+    for (int j = 0; j < 3; ++j) Ls[a][j] = dw_acc{0.f, 0.f};
   }
   // factored along z as in g2p_particle: per (x, y) corner pair
   // Z0 = vd0 + Nh_z (vd1 - vd0), Z1 = sl_z vd0 + sh_z vd1 (= vd1 - vd0 strictly
@@ -248,18 +280,18 @@ __device__ __forceinline__ void g2p_dw_particle(const GridP& g, const NodeP& nd,
       dw Z1 = dz;
       if (!inz) Z1 = dw_scale(r0.vd[a], h.sl[2]) + dw_scale(r1.vd[a], h.sh[2]);
       const dw W = dw_fma(h.Nh[2], r1.dv[a], h.Nl[2] * r0.dv[a]);
-      dx[a] = dw_fma(Nxy, Z0, dx[a]);
-      dvp[a] = dw_fma(Nxy, W, dvp[a]);
-      Ls[a][0] = dw_fma(sNy, Z0, Ls[a][0]);
-      Ls[a][1] = dw_fma(sNx, Z0, Ls[a][1]);
-      Ls[a][2] = dw_fma(Nxy, Z1, Ls[a][2]);
+      acc_fma(dx[a], Nxy, Z0);
+      acc_fma(dvp[a], Nxy, W);
+      acc_fma(Ls[a][0], sNy, Z0);
+      acc_fma(Ls[a][1], sNx, Z0);
+      acc_fma(Ls[a][2], Nxy, Z1);
     }
   }
   cp_async_wait_all();
   bool fin = true;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const double xd = f64_plus_dw(slot(S::X + a), dx[a]), vd = f64_plus_dw(slot(S::V + a), dvp[a]);
+    const double xd = f64_plus_dw(slot(S::X + a), acc_value(dx[a])), vd = f64_plus_dw(slot(S::V + a), acc_value(dvp[a]));
     put_f64(pp, L::X + a, p, xd);
     put_f64(pp, L::V + a, p, vd);
     fin &= finite_bits(xd) & finite_bits(vd);
@@ -269,7 +301,7 @@ __device__ __forceinline__ void g2p_dw_particle(const GridP& g, const NodeP& nd,
   for (int j = 0; j < 3; ++j) {
     const dw s = dw_c(g.w_dxI[j]);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) Ldt[a][j] = Ls[a][j] * s;
+    for (int a = 0; a < 3; ++a) Ldt[a][j] = acc_value(Ls[a][j]) * s;
   }
   // F <- F + F (L dt) (:523), J = det F and V = J V0 (:525-526)
   dw J;
@@ -372,7 +404,7 @@ __device__ __forceinline__ void g2p_dw_particle(const GridP& g, const NodeP& nd,
 
 // dynamic shared memory: DwSlots::N doubles per thread
 template <int MAT>
-__global__ void __launch_bounds__(256) g2p_dw_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, unsigned* status) {
+__global__ void __launch_bounds__(256, 2) g2p_dw_kernel(GridP g, NodeP nd, PartP pp, MatParams mp, unsigned* status) {
   extern __shared__ __align__(16) unsigned char g2p_dw_smem[];
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t < pp.count)
