@@ -589,6 +589,8 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       I.g.xmin[a] = d.grid.xmin[a];
       I.g.dxI[a] = 1.0 / dx[a];
       I.g.dx[a] = dx[a];
+      I.g.xminf[a] = float(I.g.xmin[a]);  // the FP32 estimate of hat()'s base node
+      I.g.dxIf[a] = float(I.g.dxI[a]);
       I.g.nn[a] = nn[a];
     }
     I.g.nx = nn[0];

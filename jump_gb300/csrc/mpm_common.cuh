@@ -243,6 +243,34 @@ __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, 
 __device__ __forceinline__ int floor_to_int(double t) { return __double2int_rd(t); }
 __device__ __forceinline__ int floor_to_int(float t) { return __float2int_rd(t); }
 
+// FP64 -> float by truncation on the integer pipe, for magnitudes in
+// [2^-126, 2^128) (relative error below 2^-23); NaN for any other value,
+// zero included
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned bh = unsigned(__double2hiint(x)), bl = unsigned(__double2loint(x));
+  const unsigned ex = (bh >> 20) & 0x7ffu;
+  if (ex - 897u > 253u) return __uint_as_float(0x7fc00000u);
+  return __uint_as_float((__funnelshift_l(bl, bh, 3) - (0x180u << 23)) | (bh & 0x80000000u));
+}
+
+// The 1-based base node i1 = floor((x - xmin) dxI + 1) of hat(), decided by an
+// FP32 estimate (from the host-rounded float grid constants) when the
+// estimate lies farther from an integer than its error bound
+// |t32 - t| <= 2^-24 (4 (|x| + |xmin|) dxI + |t|): the FP64 expression, whose
+// own error is some 10^8 times smaller, then has the same floor.  False when
+// the caller must form it in FP64 (near a node line, outside the float range,
+// or without float constants: dxIf == 0).
+__device__ __forceinline__ bool base_node_estimate(double x, float xminf, float dxIf, int& i1) {
+  if (!(dxIf > 0.f)) return false;
+  const float xf = f32_trunc(x);
+  const float t32 = __fmaf_rn(__fsub_rn(xf, xminf), dxIf, 1.0f);
+  const float bound = 0x1p-21f * __fmaf_rn(__fadd_rn(fabsf(xf), fabsf(xminf)), dxIf, fabsf(t32) + 1.0f);
+  const float fl = floorf(t32);
+  if (!(t32 - fl > bound && fl + 1.0f - t32 > bound && fabsf(fl) < 1e9f)) return false;
+  i1 = int(fl);
+  return true;
+}
+
 // Per-axis linear hat values and gradient factors of one particle.
 template <int D, class R>
 struct Hat {
@@ -259,8 +287,13 @@ __device__ __forceinline__ bool hat(const GridP& g, const R* x, Hat<D, R>& h) {
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     R xmin = fc ? R(g.xminf[a]) : R(g.xmin[a]), dxI = fc ? R(g.dxIf[a]) : R(g.dxI[a]);
-    R t = add_rn(mul_rn(sub_rn(x[a], xmin), dxI), R(1));
-    int i1 = floor_to_int(t);  // 1-based base node
+    int i1;  // 1-based base node
+    // FP64 particles: the FP32 estimate where it decides the floor (saves
+    // FP64-pipe work), else the FP64 expression
+    if (!(sizeof(R) == 8 && base_node_estimate(double(x[a]), g.xminf[a], g.dxIf[a], i1))) {
+      R t = add_rn(mul_rn(sub_rn(x[a], xmin), dxI), R(1));
+      i1 = floor_to_int(t);
+    }
     if (i1 < 1 || i1 > int(g.nn[a] - 1)) return false;
     int c = i1 - 1;
     h.c[a] = c;

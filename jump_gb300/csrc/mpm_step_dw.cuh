@@ -40,25 +40,16 @@ __device__ __forceinline__ float sign_of(double gfac) {
 }
 
 // The hat of particle p at position x (FP64) for the DW step: the cell the
-// FP64 hat() chooses, bit for bit -- its t = (x - xmin) dxI + 1 estimated in
-// FP32 and floored when the estimate lies farther from an integer than its
-// error bound, else formed in FP64 as hat() forms it -- the differences
+// FP64 hat() chooses, bit for bit (base_node_estimate, else the FP64
+// expression, as hat() decides it) -- the differences
 // dl = x - x_lower, dh = x - x_upper in FP64 (exact, as in hat()), their signs
 // for the gradient factors, and Nl = 1 - |dl| dxI, Nh = 1 - Nl in DW.
 // The cache (PartP::hat_c codes, hat_nl as DW pairs) is written for the G2P.
 __device__ __forceinline__ bool hat_dw(const GridP& g, const PartP& pp, int64_t p, const double* x, HatDW& h) {
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const float xf = dw_from(x[a]).hi;
-    const float u = __fsub_rn(xf, g.xminf[a]);
-    const float t32 = __fmaf_rn(u, g.dxIf[a], 1.0f);
-    // |t32 - t| <= 4 u32 ((|x| + |xmin|) dxI + t + 1), u32 = 2^-24
-    const float bound = 0x1p-22f * __fmaf_rn(__fadd_rn(fabsf(xf), fabsf(g.xminf[a])), g.dxIf[a], fabsf(t32) + 1.0f);
-    const float fl = floorf(t32);
     int i1;
-    if (t32 - fl > bound && fl + 1.0f - t32 > bound) {
-      i1 = int(fl);
-    } else {
+    if (!base_node_estimate(x[a], g.xminf[a], g.dxIf[a], i1)) {
       const double t = add_rn(mul_rn(sub_rn(x[a], g.xmin[a]), g.dxI[a]), 1.0);
       i1 = floor_to_int(t);
     }
