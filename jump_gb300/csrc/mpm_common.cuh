@@ -253,6 +253,13 @@ __device__ __forceinline__ float f32_trunc(double x) {
   return __uint_as_float((__funnelshift_l(bl, bh, 3) - (0x180u << 23)) | (bh & 0x80000000u));
 }
 
+// hat()'s 1-based base node in FP64, floor((x - xmin) dxI + 1) with the
+// reference's roundings; not inlined, so that the compiler cannot evaluate it
+// beside the FP32 estimate on the path where the estimate decides
+static __device__ __noinline__ int base_node_f64(double x, double xmin, double dxI) {
+  return __double2int_rd(__dadd_rn(__dmul_rn(__dsub_rn(x, xmin), dxI), 1.0));
+}
+
 // The 1-based base node i1 = floor((x - xmin) dxI + 1) of hat(), decided by an
 // FP32 estimate (from the host-rounded float grid constants) when the
 // estimate lies farther from an integer than its error bound
@@ -290,9 +297,10 @@ __device__ __forceinline__ bool hat(const GridP& g, const R* x, Hat<D, R>& h) {
     int i1;  // 1-based base node
     // FP64 particles: the FP32 estimate where it decides the floor (saves
     // FP64-pipe work), else the FP64 expression
-    if (!(sizeof(R) == 8 && base_node_estimate(double(x[a]), g.xminf[a], g.dxIf[a], i1))) {
-      R t = add_rn(mul_rn(sub_rn(x[a], xmin), dxI), R(1));
-      i1 = floor_to_int(t);
+    if constexpr (sizeof(R) == 8) {
+      if (!base_node_estimate(x[a], g.xminf[a], g.dxIf[a], i1)) i1 = base_node_f64(x[a], g.xmin[a], g.dxI[a]);
+    } else {
+      i1 = floor_to_int(add_rn(mul_rn(sub_rn(x[a], xmin), dxI), R(1)));
     }
     if (i1 < 1 || i1 > int(g.nn[a] - 1)) return false;
     int c = i1 - 1;

@@ -49,10 +49,7 @@ __device__ __forceinline__ bool hat_dw(const GridP& g, const PartP& pp, int64_t 
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     int i1;
-    if (!base_node_estimate(x[a], g.xminf[a], g.dxIf[a], i1)) {
-      const double t = add_rn(mul_rn(sub_rn(x[a], g.xmin[a]), g.dxI[a]), 1.0);
-      i1 = floor_to_int(t);
-    }
+    if (!base_node_estimate(x[a], g.xminf[a], g.dxIf[a], i1)) i1 = base_node_f64(x[a], g.xmin[a], g.dxI[a]);
     if (i1 < 1 || i1 > int(g.nn[a] - 1)) {
       if (pp.hat_c)
 #pragma unroll
