@@ -623,6 +623,7 @@ def measure_double_word(args, mk_fp64, npart, nprof, fp64_state, peak, peak_kind
     d = mk_fp64()
     d.params.precision = _capi.MPM_PREC_DW  # the same descriptors
     ctx = MPMContext(d)
+    tuning = ctx.tune(3) if args.tune else None  # CTA size and sort interval (its P2G is per-lane atomics)
     ctx.step(args.warmup)
     ctx.step(args.steps)
     dev_ms = ctx.last_step_ms()
@@ -641,6 +642,7 @@ def measure_double_word(args, mk_fp64, npart, nprof, fp64_state, peak, peak_kind
     achieved = BYTES["dw"][dom] * npart / (per[dom] * 1e-3) / 1e9
     return {"precision": "dw", "value": npart * args.steps / (dev_ms * 1e-3), "unit": METRIC,
             "ms_per_step": dev_ms / args.steps, "stage_ms_per_step": per, "launch": launch,
+            "launch_chosen_by": "mpm_tune" if tuning else "defaults",
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": ncu_traffic(dom, "dw"),

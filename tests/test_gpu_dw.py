@@ -264,3 +264,29 @@ def test_launch_settings_and_tuner(oracle_lib):
     assert max(errs.values()) <= FP64_TOL, errs
     g.close()
     o.close()
+
+
+def test_per_particle_moduli_vs_oracle(oracle_lib):
+    """Per-particle Young's moduli (the Lame fields, and the J2 plastic
+    multiplier by a double-word division): a coarse yielding bar with a seeded
+    +-20% modulus field against the oracle, beside the FP64 step on the same
+    case.  The heterogeneous bar amplifies rounding differences more than the
+    uniform one, so the bound is the FP64 step's own distance from the oracle
+    (times 4, and at least 1e-10) per field."""
+    grid, solids, alg, data = scenarios.taylor_bar(h=1e-3)
+    scenarios.apply_dirichlet(grid, data)
+    s = solids[0]
+    s.youngs = s.mat.E * np.random.default_rng(21).uniform(0.8, 1.2, s.parCount)
+    mk = lambda **kw: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], **kw)
+    g, f, o = MPMContext(mk(precision="dw")), MPMContext(mk()), oracle_lib.OracleContext(mk())
+    for c in (g, f, o):
+        c.step(60)
+    so = o.download_all()
+    assert np.max(so[0].alpha) > 0, "the bar must yield"
+    ed = field_errors(g.download_all(), so, fields=J2_FIELDS)
+    ef = field_errors(f.download_all(), so, fields=J2_FIELDS)
+    print("\nper_particle_moduli dw", ed, "\nf64", ef)
+    for k in ed:
+        assert ed[k] <= max(1e-10, 4 * ef[k]), (k, ed[k], ef[k])
+    for c in (g, f, o):
+        c.close()
