@@ -83,9 +83,10 @@ extern "C" {
    clock as the FP64 pipe on GB300.  Every accumulated particle field is its
    FP64 value plus the step's increment rounded to FP64, and the hat (cell and
    weights) is the FP64 one, so the results follow the FP64 step to within the
-   FP64 step's own rounding differences.  3D USL on the linear basis with one
-   velocity field and the P2G strategy MPM_P2G_ATOMIC; other configurations:
-   MPM_ERR_UNSUPPORTED (MPM_ERR_ARG for another strategy).  The reverse mode
+   FP64 step's own rounding differences.  3D USL (linear, quadratic or cubic
+   B-spline basis) with one velocity field and the P2G strategy MPM_P2G_ATOMIC;
+   other configurations: MPM_ERR_UNSUPPORTED (MPM_ERR_ARG for another
+   strategy).  The reverse mode
    and MPM_P2G_FUSED take FP64 contexts only. */
 #define MPM_PREC_DW         2
 

@@ -845,15 +845,14 @@ int mpm_create(const mpm_grid_desc* grid, const mpm_body_desc* bodies, int32_t n
   if (params->precision != MPM_PREC_F64 && params->precision != MPM_PREC_F32 && params->precision != MPM_PREC_DW)
     return fail(MPM_ERR_ARG, "mpm_create: unknown precision");
   if (params->precision == MPM_PREC_DW) {
-    bool ok = grid->dim == 3 && params->algorithm == MPM_ALG_USL && params->basis == MPM_BASIS_LINEAR &&
-              !params->contact;
+    bool ok = grid->dim == 3 && params->algorithm == MPM_ALG_USL && !params->contact;
     for (int b = 0; ok && b < nbodies; ++b) {
       const int t = bodies[b].mat.type;
       ok = t == MPM_MAT_RIGID || t == MPM_MAT_ELASTIC || t == MPM_MAT_J2;
     }
     if (!ok)
-      return fail(MPM_ERR_UNSUPPORTED, "mpm_create: MPM_PREC_DW runs 3D USL on the linear basis with one velocity "
-                                       "field and linear elastic, J2 or rigid bodies");
+      return fail(MPM_ERR_UNSUPPORTED, "mpm_create: MPM_PREC_DW runs 3D USL with one velocity field and linear "
+                                       "elastic, J2 or rigid bodies");
   }
   if (params->contact && nbodies > kMaxContactBodies)
     return fail(MPM_ERR_ARG, "mpm_create: contact mode supports at most " + std::to_string(kMaxContactBodies) +

@@ -6,6 +6,7 @@
 #include "mpm_musl.cuh"
 #include "mpm_bspline.cuh"
 #include "mpm_step_dw.cuh"
+#include "mpm_bspline_dw.cuh"
 
 #include <type_traits>
 
@@ -295,6 +296,14 @@ void Launchers<D>::bs_p2g(cudaStream_t s, const GridP& g, const NodeP& nd, const
   const bool gr = grav[0] != 0.0 || grav[1] != 0.0 || (D == 3 && grav[2] != 0.0);
   with_bspline(basis, [&](auto Kc) {
     constexpr int K = decltype(Kc)::value;
+    if (!f32 && nd.dw4) {
+      // double-word P2G (MPM_PREC_DW contexts, 3D)
+      if constexpr (D == 3) {
+        if (gr) bs_p2g_dw_kernel<K, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
+        else bs_p2g_dw_kernel<K, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
+      }
+      return;
+    }
     if (f32) {
       if (gr) bs_p2g_kernel<D, float, K, true><<<nb, 256, 0, s>>>(g, nd, pp, grav[0], grav[1], grav[2], status);
       else bs_p2g_kernel<D, float, K, false><<<nb, 256, 0, s>>>(g, nd, pp, 0.0, 0.0, 0.0, status);
@@ -314,6 +323,12 @@ void Launchers<D>::bs_g2p(cudaStream_t s, const GridP& g, const NodeP& nd, const
     constexpr int M = decltype(Mc)::value;
     with_bspline(basis, [&](auto Kc) {
       constexpr int K = decltype(Kc)::value;
+      if (!f32 && nd.dw4) {
+        // double-word G2P (MPM_PREC_DW contexts: 3D, linear elastic or J2 bodies)
+        if constexpr (D == 3 && (M == MPM_MAT_ELASTIC || M == MPM_MAT_J2))
+          bs_g2p_dw_kernel<K, M><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
+        return;
+      }
       if (f32) bs_g2p_kernel<D, float, K, M><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
       else bs_g2p_kernel<D, double, K, M><<<nb, 256, 0, s>>>(g, nd, pp, mp, status);
     });

@@ -118,6 +118,7 @@ __device__ __forceinline__ NodeDW node_dw(const float4* r, int64_t n) {
 }
 
 __device__ __forceinline__ void put_f64(const PartP& pp, int f, int64_t p, double v) { *field<double>(pp, f, p) = v; }
+__device__ __forceinline__ dw get_dw(const PartP& pp, int f, int64_t p) { return dw_from(*field<double>(pp, f, p)); }
 
 // ---------------------------------------------------------------------------
 // P2G of particle pp.begin + t: mass m N, momentum m N v and force
@@ -210,6 +211,122 @@ struct DwSlots {
   static constexpr int X = 0, V = 3, F = 6, EPS = 15, EP = 21, SIG = 21, ALPHA = 27, N = 28;
 };
 
+// The G2P after the gather, shared by the bases: x and v (their FP64 values
+// plus the DW increments dx, dv), F <- F + F (L dt) (:523), J = det F and
+// V = J V0 (:525-526), the strain and the constitutive update.  in(k) is the
+// particle's FP64 input of DwSlots slot k.
+template <int MAT, class In>
+__device__ __forceinline__ void dw_finish(const PartP& pp, int64_t p, const MatParams& mp, unsigned* status, In&& in,
+                                          const dw (&dx)[3], const dw (&dvp)[3], const dw (&Ldt)[3][3]) {
+  using L = Layout<3>;
+  using S = DwSlots;
+  bool fin = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double xd = f64_plus_dw(in(S::X + a), dx[a]), vd = f64_plus_dw(in(S::V + a), dvp[a]);
+    put_f64(pp, L::X + a, p, xd);
+    put_f64(pp, L::V + a, p, vd);
+    fin &= finite_bits(xd) & finite_bits(vd);
+  }
+  // F <- F + F (L dt) (:523), J = det F and V = J V0 (:525-526)
+  dw J;
+  {
+    dw F[9], Fn[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) F[c] = dw_from(in(S::F + c));
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        dw s = F[i] * Ldt[0][j];
+#pragma unroll
+        for (int k = 1; k < 3; ++k) s = dw_fma(F[i + 3 * k], Ldt[k][j], s);
+        put_f64(pp, L::F + i + 3 * j, p, f64_plus_dw(in(S::F + i + 3 * j), s));
+        Fn[i + 3 * j] = F[i + 3 * j] + s;
+      }
+    // det = col0 . (col1 x col2), as det_d (column-major F)
+    const dw c0 = dw_fma(Fn[4], Fn[8], -(Fn[5] * Fn[7]));
+    const dw c1 = dw_fma(Fn[5], Fn[6], -(Fn[3] * Fn[8]));
+    const dw c2 = dw_fma(Fn[3], Fn[7], -(Fn[4] * Fn[6]));
+    J = dw_fma(Fn[2], c2, dw_fma(Fn[1], c1, Fn[0] * c0));
+  }
+  put_f64(pp, L::VOL, p, dw_to_f64(J * dw_from(*field<double>(pp, L::VOL0, p))));
+  // strain += dt * 0.5 (L + L')
+  dw eps[6];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      const int c = sym<3>(i, j);
+      const dw de = (i == j) ? Ldt[i][i] : dw_scale(Ldt[i][j] + Ldt[j][i], 0.5f);
+      const double e0 = in(S::EPS + c);
+      eps[c] = dw_from(e0) + de;
+      put_f64(pp, L::EPS + c, p, f64_plus_dw(e0, de));
+    }
+  dw lam = dw_c(mp.w_lambda), mu = dw_c(mp.w_mu), kappa = dw_c(mp.w_kappa);
+  if (mp.per_particle) {
+    lam = dw_from(*field<double>(pp, L::LAM, p));
+    mu = dw_from(*field<double>(pp, L::MU, p));
+    kappa = lam + mu;
+  }
+  const dw tmu = dw_scale(mu, 2.f);
+  const dw tr = (eps[0] + eps[1]) + eps[2];
+  dw sig[6];
+  if (MAT == MPM_MAT_ELASTIC) {
+    // vmStr of the incoming stress (Material.jl:78-79), then
+    // lambda (tr eps) I + 2 mu eps (:68-72, 80)
+    dw so[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) so[c] = dw_from(in(S::SIG + c));
+    const dw qv = ((dw_sqr(so[0]) + dw_sqr(so[1])) + dw_sqr(so[2])) +
+                  dw_scale((dw_sqr(so[3]) + dw_sqr(so[5])) + dw_sqr(so[4]), 2.f);
+    put_f64(pp, L::VM, p, dw_to_f64(dw_sqrt(qv)));
+    const dw lt = lam * tr;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? dw_fma(tmu, eps[c], lt) : tmu * eps[c];
+  } else {
+    // J2 radial return (Material.jl:228-275), as j2_3d
+    dw ep[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) ep[c] = dw_from(in(S::EP + c));
+    const dw tt = tr * dw_c(mp.w_third);
+    dw s[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) s[c] = tmu * ((c < 3 ? eps[c] - tt : eps[c]) - ep[c]);
+    const dw qv = ((dw_sqr(s[0]) + dw_sqr(s[1])) + dw_sqr(s[2])) +
+                  dw_scale((dw_sqr(s[3]) + dw_sqr(s[4])) + dw_sqr(s[5]), 2.f);
+    const dw ns = dw_sqrt(qv);
+    const dw kt = kappa * tr;
+    const dw k1 = dw_c(mp.w_k1);
+    const double a0d = in(S::ALPHA);
+    const dw a0 = dw_from(a0d);
+    const dw f_trial = ns - dw_fma(k1, a0, dw_c(mp.w_fy));
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? s[c] + kt : s[c];
+    if (dw_pos(f_trial)) {
+      // plastic: the increments of alpha and the plastic strain go to their FP64 values
+      const dw inv = dw_recip(ns);
+      const dw lamp = mp.per_particle ? f_trial * dw_recip(tmu + k1) : f_trial * dw_c(mp.w_rtmuk1);
+      const dw cc = tmu * lamp;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const dw nrm = inv * s[c];
+        put_f64(pp, L::EP + c, p, f64_plus_dw(in(S::EP + c), lamp * nrm));
+        sig[c] = dw_fma(-cc, nrm, sig[c]);
+      }
+      put_f64(pp, L::ALPHA, p, f64_plus_dw(a0d, lamp));
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const double sd = dw_to_f64(sig[c]);
+    put_f64(pp, L::SIG + c, p, sd);
+    fin &= finite_bits(sd);
+  }
+  const unsigned st = (dw_pos(J) ? 0u : ST_NEGATIVE_J) | (fin ? 0u : ST_NONFINITE);
+  if (st) atomicOr(status, st);
+}
+
 // MAT: MPM_MAT_J2 or MPM_MAT_ELASTIC; pre: this thread's first slot
 template <int MAT>
 __device__ __forceinline__ void g2p_dw_particle(const GridP& g, const NodeP& nd, const PartP& pp, int64_t t,
@@ -276,118 +393,19 @@ __device__ __forceinline__ void g2p_dw_particle(const GridP& g, const NodeP& nd,
     }
   }
   cp_async_wait_all();
-  bool fin = true;
+  dw dxv[3], dvv[3], Ldt[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const double xd = f64_plus_dw(slot(S::X + a), acc_value(dx[a])), vd = f64_plus_dw(slot(S::V + a), acc_value(dvp[a]));
-    put_f64(pp, L::X + a, p, xd);
-    put_f64(pp, L::V + a, p, vd);
-    fin &= finite_bits(xd) & finite_bits(vd);
+    dxv[a] = acc_value(dx[a]);
+    dvv[a] = acc_value(dvp[a]);
   }
-  dw Ldt[3][3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     const dw s = dw_c(g.w_dxI[j]);
 #pragma unroll
     for (int a = 0; a < 3; ++a) Ldt[a][j] = acc_value(Ls[a][j]) * s;
   }
-  // F <- F + F (L dt) (:523), J = det F and V = J V0 (:525-526)
-  dw J;
-  {
-    dw F[9], Fn[9];
-#pragma unroll
-    for (int c = 0; c < 9; ++c) F[c] = dw_from(slot(S::F + c));
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        dw s = F[i] * Ldt[0][j];
-#pragma unroll
-        for (int k = 1; k < 3; ++k) s = dw_fma(F[i + 3 * k], Ldt[k][j], s);
-        put_f64(pp, L::F + i + 3 * j, p, f64_plus_dw(slot(S::F + i + 3 * j), s));
-        Fn[i + 3 * j] = F[i + 3 * j] + s;
-      }
-    // det = col0 . (col1 x col2), as det_d (column-major F)
-    const dw c0 = dw_fma(Fn[4], Fn[8], -(Fn[5] * Fn[7]));
-    const dw c1 = dw_fma(Fn[5], Fn[6], -(Fn[3] * Fn[8]));
-    const dw c2 = dw_fma(Fn[3], Fn[7], -(Fn[4] * Fn[6]));
-    J = dw_fma(Fn[2], c2, dw_fma(Fn[1], c1, Fn[0] * c0));
-  }
-  put_f64(pp, L::VOL, p, dw_to_f64(J * dw_from(*field<double>(pp, L::VOL0, p))));
-  // strain += dt * 0.5 (L + L')
-  dw eps[6];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = i; j < 3; ++j) {
-      const int c = sym<3>(i, j);
-      const dw de = (i == j) ? Ldt[i][i] : dw_scale(Ldt[i][j] + Ldt[j][i], 0.5f);
-      const double e0 = slot(S::EPS + c);
-      eps[c] = dw_from(e0) + de;
-      put_f64(pp, L::EPS + c, p, f64_plus_dw(e0, de));
-    }
-  dw lam = dw_c(mp.w_lambda), mu = dw_c(mp.w_mu), kappa = dw_c(mp.w_kappa);
-  if (mp.per_particle) {
-    lam = dw_from(*field<double>(pp, L::LAM, p));
-    mu = dw_from(*field<double>(pp, L::MU, p));
-    kappa = lam + mu;
-  }
-  const dw tmu = dw_scale(mu, 2.f);
-  const dw tr = (eps[0] + eps[1]) + eps[2];
-  dw sig[6];
-  if (MAT == MPM_MAT_ELASTIC) {
-    // vmStr of the incoming stress (Material.jl:78-79), then
-    // lambda (tr eps) I + 2 mu eps (:68-72, 80)
-    dw so[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) so[c] = dw_from(slot(S::SIG + c));
-    const dw qv = ((dw_sqr(so[0]) + dw_sqr(so[1])) + dw_sqr(so[2])) +
-                  dw_scale((dw_sqr(so[3]) + dw_sqr(so[5])) + dw_sqr(so[4]), 2.f);
-    put_f64(pp, L::VM, p, dw_to_f64(dw_sqrt(qv)));
-    const dw lt = lam * tr;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? dw_fma(tmu, eps[c], lt) : tmu * eps[c];
-  } else {
-    // J2 radial return (Material.jl:228-275), as j2_3d
-    dw ep[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) ep[c] = dw_from(slot(S::EP + c));
-    const dw tt = tr * dw_c(mp.w_third);
-    dw s[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) s[c] = tmu * ((c < 3 ? eps[c] - tt : eps[c]) - ep[c]);
-    const dw qv = ((dw_sqr(s[0]) + dw_sqr(s[1])) + dw_sqr(s[2])) +
-                  dw_scale((dw_sqr(s[3]) + dw_sqr(s[4])) + dw_sqr(s[5]), 2.f);
-    const dw ns = dw_sqrt(qv);
-    const dw kt = kappa * tr;
-    const dw k1 = dw_c(mp.w_k1);
-    const double a0d = slot(S::ALPHA);
-    const dw a0 = dw_from(a0d);
-    const dw f_trial = ns - dw_fma(k1, a0, dw_c(mp.w_fy));
-#pragma unroll
-    for (int c = 0; c < 6; ++c) sig[c] = c < 3 ? s[c] + kt : s[c];
-    if (dw_pos(f_trial)) {
-      // plastic: the increments of alpha and the plastic strain go to their FP64 values
-      const dw inv = dw_recip(ns);
-      const dw lamp = mp.per_particle ? f_trial * dw_recip(tmu + k1) : f_trial * dw_c(mp.w_rtmuk1);
-      const dw cc = tmu * lamp;
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const dw nrm = inv * s[c];
-        put_f64(pp, L::EP + c, p, f64_plus_dw(slot(S::EP + c), lamp * nrm));
-        sig[c] = dw_fma(-cc, nrm, sig[c]);
-      }
-      put_f64(pp, L::ALPHA, p, f64_plus_dw(a0d, lamp));
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < 6; ++c) {
-    const double sd = dw_to_f64(sig[c]);
-    put_f64(pp, L::SIG + c, p, sd);
-    fin &= finite_bits(sd);
-  }
-  const unsigned st = (dw_pos(J) ? 0u : ST_NEGATIVE_J) | (fin ? 0u : ST_NONFINITE);
-  if (st) atomicOr(status, st);
+  dw_finish<MAT>(pp, p, mp, status, slot, dxv, dvv, Ldt);
 }
 
 // dynamic shared memory: DwSlots::N doubles per thread

@@ -58,8 +58,8 @@ def test_argument_errors_without_gpu(L):
 
 
 def test_double_word_precision_refusals_without_gpu(L):
-    """MPM_PREC_DW takes 3D USL on the linear basis with linear elastic, J2 or
-    rigid bodies; anything else is refused before any device work."""
+    """MPM_PREC_DW takes 3D USL (any basis) with one velocity field and linear
+    elastic, J2 or rigid bodies; anything else is refused before any device work."""
     from jump_gb300 import scenarios
     from jump_gb300.engine import Descriptors
 
@@ -70,7 +70,7 @@ def test_double_word_precision_refusals_without_gpu(L):
         _capi.MPM_ERR_UNSUPPORTED  # 2D
     assert b"MPM_PREC_DW" in L.mpm_last_error()
     grid, solids, alg, data = scenarios.taylor_bar(h=2e-3)
-    for kw in ({"algorithm": "musl"}, {"basis": "quad"}, {"contact": True}):
+    for kw in ({"algorithm": "musl"}, {"contact": True}):
         d = Descriptors(grid, solids, tolerance=alg.tolerance, dt=data["dt"], precision="dw", **kw)
         assert L.mpm_create(C.byref(d.grid), d.bodies, len(solids), C.byref(d.params), C.byref(h)) == \
             _capi.MPM_ERR_UNSUPPORTED, kw

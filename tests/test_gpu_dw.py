@@ -11,7 +11,8 @@ and the constitutive update in pairs of floats hi + lo.
   rounded FP64 value of hi + lo.
 * The step against the FP64 oracle: the golden 3D J2 and linear elastic cases,
   the coarse Taylor bar over 100 steps, particles on grid nodes (zero gradient
-  factors), a particle that leaves the grid; the full-size bar is in
+  factors), a particle that leaves the grid, per-particle moduli, the
+  quadratic and cubic B-spline bases; the full-size bar is in
   test_gpu_fullsize.py."""
 from fractions import Fraction
 
@@ -286,6 +287,34 @@ def test_per_particle_moduli_vs_oracle(oracle_lib):
     ed = field_errors(g.download_all(), so, fields=J2_FIELDS)
     ef = field_errors(f.download_all(), so, fields=J2_FIELDS)
     print("\nper_particle_moduli dw", ed, "\nf64", ef)
+    for k in ed:
+        assert ed[k] <= max(1e-10, 4 * ef[k]), (k, ed[k], ef[k])
+    for c in (g, f, o):
+        c.close()
+
+
+@pytest.mark.parametrize("basis, material", [("quad", "j2"), ("cubic", "j2"), ("quad", "elastic")])
+def test_bspline_bars_vs_oracle(basis, material, oracle_lib):
+    """The quadratic and cubic B-spline bases in double-word: a coarse bar over
+    60 steps against the oracle, beside the FP64 step (bound: the FP64 step's
+    own distance from the oracle times 4, and at least 1e-10, per field)."""
+    from jump_gb300.material import ElasticMaterial
+    grid, solids, alg, data = scenarios.taylor_bar(h=1e-3)
+    scenarios.apply_dirichlet(grid, data)
+    if material == "elastic":
+        m = solids[0].mat
+        solids[0].mat = ElasticMaterial(m.E, m.nu, m.density, solids[0].parCount)
+    mk = lambda **kw: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], basis=basis, **kw)
+    g, f, o = MPMContext(mk(precision="dw")), MPMContext(mk()), oracle_lib.OracleContext(mk())
+    for c in (g, f, o):
+        c.step(60)
+    so = o.download_all()
+    fields = J2_FIELDS if material == "j2" else ("pos", "velocity", "volume", "F", "strain", "stress", "vmstr")
+    if material == "j2":
+        assert np.max(so[0].alpha) > 0, "the bar must yield"
+    ed = field_errors(g.download_all(), so, fields=fields)
+    ef = field_errors(f.download_all(), so, fields=fields)
+    print(f"\nbspline {basis} {material} dw", ed, "\nf64", ef)
     for k in ed:
         assert ed[k] <= max(1e-10, 4 * ef[k]), (k, ed[k], ef[k])
     for c in (g, f, o):
