@@ -12,8 +12,8 @@ and the constitutive update in pairs of floats hi + lo.
 * The step against the FP64 oracle: the golden 3D J2 and linear elastic cases,
   the coarse Taylor bar over 100 steps, particles on grid nodes (zero gradient
   factors), a particle that leaves the grid, per-particle moduli, the
-  quadratic and cubic B-spline bases; the full-size bar is in
-  test_gpu_fullsize.py."""
+  quadratic and cubic B-spline bases, a rigid punch, a snapshot round trip;
+  the full-size bar is in test_gpu_fullsize.py."""
 from fractions import Fraction
 
 import numpy as np
@@ -319,3 +319,44 @@ def test_bspline_bars_vs_oracle(basis, material, oracle_lib):
         assert ed[k] <= max(1e-10, 4 * ef[k]), (k, ed[k], ef[k])
     for c in (g, f, o):
         c.close()
+
+
+def test_rigid_punch_3d_vs_oracle(oracle_lib):
+    """A rigid plate striking an elastic sphere on a fixed rigid base (3D): the
+    rigid override feeds the double-word records; bound as for the B-splines."""
+    grid, solids, alg, data = scenarios.rigid_punch(dim=3, material="elastic", h=0.05)
+    scenarios.apply_dirichlet(grid, data)
+    mk = lambda **kw: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], **kw)
+    g, f, o = MPMContext(mk(precision="dw")), MPMContext(mk()), oracle_lib.OracleContext(mk())
+    for c in (g, f, o):
+        c.step(210)
+    so = o.download_all()
+    assert np.abs(so[0].strain).max() > 0.1, "the punch must load the sphere"
+    fields = ("pos", "velocity", "volume", "F", "strain", "stress")
+    ed = field_errors(g.download_all(), so, fields=fields)
+    ef = field_errors(f.download_all(), so, fields=fields)
+    for k in ed:
+        assert ed[k] <= max(1e-10, 4 * ef[k]), (k, ed[k], ef[k])
+    np.testing.assert_array_equal(g.download_all()[1].pos, so[1].pos)  # the punch moves as the oracle moves it
+    for c in (g, f, o):
+        c.close()
+
+
+def test_save_load_roundtrip():
+    """A double-word context resumes from its snapshot (the FP64 state) and
+    follows the uninterrupted run."""
+    grid, solids, alg, data = scenarios.taylor_bar(h=1e-3)
+    scenarios.apply_dirichlet(grid, data)
+    mk = lambda: descriptors(grid, solids, alg.tolerance, data["bodyforce"], data["dt"], precision="dw")
+    a = MPMContext(mk())
+    a.step(8)
+    snap = a.save()
+    a.step(11)
+    b = MPMContext(mk())
+    b.load(snap)
+    b.step(11)
+    # the node sums' atomic order differs between runs: equal to rounding
+    for x, y in zip(a.download_all(), b.download_all()):
+        assert rel_err(x.pos, y.pos) <= 1e-12 and rel_err(x.stress, y.stress) <= 1e-10
+    a.close()
+    b.close()
