@@ -27,7 +27,9 @@ def from_colmajor(flat: np.ndarray, n: int, d: int) -> np.ndarray:
 
 
 class Descriptors:
-    """Descriptors plus the numpy arrays they point into (kept alive here)."""
+    """Descriptors plus the numpy arrays they point into (kept alive here).
+    precision: "f64", "f32" (FP32 particles, FP64 nodes) or "dw" (FP64 fields
+    and nodes, P2G and G2P arithmetic in double-word FP32; 3D USL)."""
 
     def __init__(self, grid, solids, tolerance=0.0, body_force=None, dt=0.0, precision="f64",
                  contact=False, friction=0.0, sort_interval=0, algorithm="usl", alpha=1.0, basis="linear"):

@@ -12,7 +12,8 @@ the only hooks are EmptyFix/EnergiesFix and a non-writing output, in which case
 the energies are reduced on the device).  The per-step ``@printf`` of the 2D
 reference (:375) is not reproduced.
 
-Extra ``data`` keys (all optional): "precision" ("f64" | "f32"),
+Extra ``data`` keys (all optional): "precision" ("f64" | "f32" | "dw": FP64
+fields with the P2G and G2P arithmetic in double-word FP32, 3D USL),
 "contact" (bool) with "friction" (float), "sort_interval" (int).
 """
 from __future__ import annotations
