@@ -236,7 +236,8 @@ __global__ void __launch_bounds__(256) bs_p2g_dw_kernel(GridP g, NodeP nd, PartP
 #pragma unroll
         for (int a = 0; a < 3; ++a) atomicAdd(nd.p0 + a * Nn + n, dw_to_f64(Nm * v[a]));
 #pragma unroll
-        for (int a = 0; a < 3; ++a) atomicAdd(nd.f + a * Nn + n, dw_to_f64(dw_fma(P[a], ax[2].N[k], Q[a] * ax[2].G[k])));
+        for (int a = 0; a < 3; ++a)
+          atomicAdd(nd.f + a * Nn + n, dw_to_f64(dw_fma(P[a], ax[2].N[k], Q[a] * ax[2].G[k])));
       }
     }
 }
@@ -251,7 +252,8 @@ __device__ __forceinline__ int dw_slot_field(int k) {
                   : (k < S::F ? L::V + (k - S::V)
                               : (k < S::EPS ? L::F + (k - S::F)
                                             : (k < S::EP ? L::EPS + (k - S::EPS)
-                                                         : (k < S::ALPHA ? (MAT == MPM_MAT_J2 ? L::EP : L::SIG) + (k - S::EP)
+                                                         : (k < S::ALPHA ? (MAT == MPM_MAT_J2 ? L::EP : L::SIG) +
+                                                                               (k - S::EP)
                                                                          : L::ALPHA))));
 }
 

@@ -13,11 +13,12 @@
 // Loads convert FP64 -> DW on the integer pipe.  The P2G's hat has the FP64
 // hat's cell and zero gradient factors bit for bit and its weights in DW
 // (hat_dw, stored for the G2P in the hat cache as DW pairs); its node values
-// are DW, each added to its FP64 node accumulator as an FP64 value.  The grid update writes each
-// node's vdt and dv as DW records (NodeP::dw4, three float4 per node), so the
-// G2P's corner gathers need no conversion.  The G2P's particle inputs are
-// copied into the thread's shared-memory slots by cp.async at the start, so
-// their loads overlap the gather.
+// are DW, each added to its FP64 node accumulator as an FP64 value.  The grid
+// update writes each node's vdt and dv as DW records (NodeP::dw4, three float4
+// per node), so the G2P's corner gathers need no conversion.  The G2P's
+// particle inputs are copied into the thread's shared-memory slots by cp.async
+// at the start, so their loads overlap the gather; its tail (dw_finish) is
+// shared with the B-spline G2P of mpm_bspline_dw.cuh.
 #pragma once
 
 #include "mpm_kernels.cuh"
