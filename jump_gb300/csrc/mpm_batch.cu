@@ -824,6 +824,9 @@ struct FusedP {
   double dt, tol, grav[3];
   unsigned* status;
   unsigned* bar;  // [0] arrivals, [1] generation, [2] a barrier wait gave up
+  // the second set of node accumulators (m, p0 (D), f (D)): steps alternate
+  // between it and nd's, ending on nd's
+  double *m2, *p02, *f2;
   // EnergiesFix records after steps first, first + every, ... (rec non-null):
   // per-CTA partial sums, folded by CTA 0 in a fixed order into rec->base[rec->idx++]
   EnRec* rec;
@@ -839,37 +842,51 @@ __global__ void __launch_bounds__(128) fused_steps_kernel(FusedP q, int64_t nste
   if (*reinterpret_cast<volatile unsigned*>(err)) return;  // an earlier wait gave up
   const PartP all{q.P, q.pitch, 0, q.np};
   const int64_t Nn = q.nd.nodeCount;
-  auto reset = [&]() {
+  // two sets of accumulators, A (the context's) and B: step s sums into A when
+  // nsteps - 1 - s is even, so the last step's sums are the context's; while
+  // the grid update of a step reads its set, the other is zeroed for the next
+  // step, so no barrier separates a step's G2P from the next step's P2G (a
+  // thread's P2G reads only the particles its own G2P updated)
+  NodeP nA = q.nd, nB = q.nd;
+  nB.m = q.m2;
+  nB.p0 = q.p02;
+  nB.f = q.f2;
+  auto reset = [&](const NodeP& n) {
     for (int64_t i = tid; i < Nn; i += nth) {
-      q.nd.m[i] = 0.0;
+      n.m[i] = 0.0;
 #pragma unroll
       for (int a = 0; a < D; ++a) {
-        q.nd.p0[a * Nn + i] = 0.0;
-        q.nd.f[a * Nn + i] = 0.0;
+        n.p0[a * Nn + i] = 0.0;
+        n.f[a * Nn + i] = 0.0;
       }
     }
   };
-  reset();
+  reset(nA);
+  reset(nB);
   if (!grid_barrier(q.bar, err)) return;
   for (int64_t s = 0; s < nsteps; ++s) {
+    const bool onA = ((nsteps - 1 - s) & 1) == 0;
+    const NodeP& cur = onA ? nA : nB;
     // P2G: every lane of a warp calls it the same number of times
     for (int64_t base = 0; base < q.np; base += nth)
-      p2g_particle<D, double, GRAV, false>(q.g, q.nd, all, base + tid, q.grav[0], q.grav[1], q.grav[2], q.status);
+      p2g_particle<D, double, GRAV, false>(q.g, cur, all, base + tid, q.grav[0], q.grav[1], q.grav[2], q.status);
     if (!grid_barrier(q.bar, err)) return;
-    for (int64_t i = tid; i < Nn; i += nth) grid_node<D, false, true>(q.nd, i, q.dt, q.tol);
+    for (int64_t i = tid; i < Nn; i += nth) grid_node<D, false, true>(cur, i, q.dt, q.tol);
+    // the other set was last read by the previous step's grid update, before
+    // the barrier above; the next step sums into it after the barrier below
+    if (s + 1 < nsteps) reset(onA ? nB : nA);
     if (!grid_barrier(q.bar, err)) return;
     for (int64_t p = tid; p < q.np; p += nth) {
       int b = 0;
       while (b + 1 < q.nb && p >= q.bbeg[b + 1]) ++b;
       const PartP pb{q.P, q.pitch, q.bbeg[b], q.np - q.bbeg[b]};
-      g2p_particle<D, double, MAT, true>(q.g, q.nd, pb, p - q.bbeg[b], q.mp[b], q.dt, q.status);
+      g2p_particle<D, double, MAT, true>(q.g, cur, pb, p - q.bbeg[b], q.mp[b], q.dt, q.status);
     }
-    if (s + 1 < nsteps) reset();  // G2P reads vdt and dv only: the accumulators are free
-    if (!grid_barrier(q.bar, err)) return;
     if (q.rec && s >= q.first && (s - q.first) % q.every == 0) {
-      // EnergiesFix sums of the particles this thread updated (Fix.jl:248-270):
-      // m v.v, V sigma:eps (diagonal + 2 off-diagonal), m v; a fixed CTA tree,
-      // a barrier, then CTA 0 folds the CTAs' sums in block order
+      // EnergiesFix sums of the particles this thread updated (Fix.jl:248-270;
+      // the G2P's mapping, so they need no barrier first): m v.v, V sigma:eps
+      // (diagonal + 2 off-diagonal), m v; a fixed CTA tree, a barrier, then
+      // CTA 0 folds the CTAs' sums in block order
       constexpr int NQ = 2 + D;
       using L = Layout<D>;
       double e[NQ];
@@ -941,8 +958,11 @@ static const void* fused_kernel_for(int dim, int mat, bool grav) {
 #undef JMPM_FK
 }
 
-// barrier words, then the partial sums of up to 152 CTAs (5 doubles each)
-size_t fused_bytes() { return 4 * sizeof(unsigned) + 152 * 5 * sizeof(double); }
+// barrier words, the partial sums of up to 152 CTAs (5 doubles each), then
+// the second set of node accumulators (1 + 2 dim doubles per node)
+size_t fused_bytes(int dim, int64_t nodes) {
+  return 4 * sizeof(unsigned) + 152 * 5 * sizeof(double) + size_t(1 + 2 * dim) * size_t(nodes) * sizeof(double);
+}
 
 int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
                 int nb, const int64_t* bbeg, const int64_t* bcnt, const MatParams* mp, double dt, double tol,
@@ -971,19 +991,24 @@ int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP&
   q.first = first;
   q.every = every > 0 ? every : 1;
   q.partial = reinterpret_cast<double*>(static_cast<char*>(dev) + 4 * sizeof(unsigned));
+  const int64_t Nn = nd.nodeCount;
+  q.m2 = q.partial + 152 * 5;
+  q.p02 = q.m2 + Nn;
+  q.f2 = q.p02 + int64_t(dim) * Nn;
   const bool gr = grav[0] != 0.0 || grav[1] != 0.0 || (dim == 3 && grav[2] != 0.0);
   const void* fn = fused_kernel_for(dim, mp[0].type, gr);
-  // 64-thread CTAs, one per SM at most, no more than the particles need
+  // kFusedThreads-thread CTAs, one per SM at most, no more than the particles need
+  constexpr int kFusedThreads = 64;
   int devid = 0, sms = 0, per = 0;
   BATCH_TRY(cudaGetDevice(&devid));
   BATCH_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, devid));
-  BATCH_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 64, 0));
+  BATCH_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kFusedThreads, 0));
   if (per < 1) return fail(MPM_ERR_CUDA, "fused_steps: the kernel does not fit on an SM");
-  const int64_t want = std::max<int64_t>(1, (q.np + 63) / 64);
+  const int64_t want = std::max<int64_t>(1, (q.np + kFusedThreads - 1) / kFusedThreads);
   const unsigned nblk = unsigned(std::min<int64_t>(std::min<int64_t>(want, int64_t(sms)), 152));
   BATCH_TRY(cudaMemsetAsync(q.bar, 0, 3 * sizeof(unsigned), s));
   void* args[] = {&q, &nsteps};
-  BATCH_TRY(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(64), args, 0, s));
+  BATCH_TRY(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(kFusedThreads), args, 0, s));
   return MPM_OK;
 }
 

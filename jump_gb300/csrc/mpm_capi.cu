@@ -917,7 +917,7 @@ static bool fused_fits(const mpm_ctx* c, int sort_interval) {
 // step clears every node first
 static int fused_run(mpm_ctx* c, int64_t n, bool rec = false, int64_t first = 0, int64_t every = 1) {
   if (n <= 0) return MPM_OK;
-  if (!c->fused) CUDA_TRY(cudaMalloc(&c->fused, fused_bytes()));
+  if (!c->fused) CUDA_TRY(cudaMalloc(&c->fused, fused_bytes(c->dim, c->nd.nodeCount)));
   int r = fused_steps(c->dim, c->stream, c->fused, c->g, c->nd, c->P, c->np, c->nb, c->off.data(), c->cnt.data(),
                       c->mats.data(), c->prm.dt, c->prm.tolerance, c->prm.body_force, n, c->status,
                       rec ? c->en_rec : nullptr, first, every);

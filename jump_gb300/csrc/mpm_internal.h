@@ -95,7 +95,7 @@ inline int spread_threads(int64_t n) {
 // linear elastic, neo-Hookean or J2 of one type, at most MPM_BATCH_MAX_BODIES
 // bodies.  dev: device scratch of fused_bytes() bytes, whose third word is set
 // when a barrier wait gave up (read it after the stream synchronises).
-size_t fused_bytes();
+size_t fused_bytes(int dim, int64_t nodes);
 // rec (may be null): the EnergiesFix record cursor, one record after local
 // steps first, first + every, ... of the call
 int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
