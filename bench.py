@@ -433,6 +433,41 @@ def late_window(args, ctx, npart, advanced_before):
                    f"{args.warmup})"}
 
 
+def e2e_solve(args, g, s, alg, data, launch, precision):
+    """End to end through the public API: one solve of max(K, --e2e-steps)
+    steps from host arrays.  The caller's particle arrays (inputs) and the
+    arrays it downloads into (outputs) sit in pinned host memory before the
+    clock starts, like a solver's own Solid arrays.  Timed: packing the
+    descriptors, mpm_create (every host->device copy), the steps with the
+    EnergiesFix sums of every step (mpm_step_energies, the solver's path when
+    no hook reads particle arrays: each step's record formed on the device,
+    all of them copied to the host at the end of the call), and the download
+    of every field.  Returns (wall s, steps, host->device bytes, device->host
+    bytes of the fields, record bytes per step, the parts in ms)."""
+    import copy
+    from jump_gb300.engine import BodyState, Descriptors, MPMContext
+    s_pin = pin_solids(copy.deepcopy(s))
+    out_states = [pin_state(BodyState(x.parCount, x.dim)) for x in s]
+    t0 = time.perf_counter()
+    desc = Descriptors(g, s_pin, tolerance=alg.tolerance, body_force=data.get("bodyforce"), dt=data["dt"],
+                       precision=precision, sort_interval=launch["sort_interval"], **scheme_kw(args))
+    c2 = MPMContext(desc)
+    c2.set_launch(**launch)
+    t1 = time.perf_counter()
+    limit = healthy_steps(args)
+    steps = max(args.steps, min(args.e2e_steps, int(0.8 * limit)) if limit else args.e2e_steps)
+    recs, _ = c2.step_energies(steps, 1, 0)
+    t2 = time.perf_counter()
+    assert recs.shape[0] == steps and np.all(np.isfinite(recs))
+    states = c2.download_all(out_states)
+    wall = time.perf_counter() - t0
+    parts = {"create_ms": 1e3 * (t1 - t0), "steps_ms": 1e3 * (t2 - t1), "download_ms": 1e3 * (t0 + wall - t2)}
+    c2.close()
+    h2d = sum(a.nbytes for a in desc._keep)
+    d2h = sum(sum(getattr(stt, k).nbytes for k in stt.FIELDS) for stt in states)
+    return wall, steps, h2d, d2h, recs.itemsize * recs.shape[1], parts
+
+
 def run_ours(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -510,47 +545,15 @@ def run_ours(args):
                                f"near step {limit}, too early for a late window"}
     ctx.close()
 
-    # End to end through the public API: one solve of max(K, --e2e-steps) steps
-    # from host arrays.  The caller's particle arrays (inputs) and the arrays it
-    # downloads into (outputs) sit in pinned host memory before the clock
-    # starts, like a solver's own Solid arrays.  Timed: packing the
-    # descriptors, mpm_create (every host->device copy), the steps with the
-    # EnergiesFix sums of every step (mpm_step_energies, the solver's path when
-    # no hook reads particle arrays: each step's record formed on the device,
-    # all of them copied to the host at the end of the call), and the download
-    # of every field.
-    import copy
-    from jump_gb300.engine import BodyState
-    s_pin = pin_solids(copy.deepcopy(s))
-    out_states = [pin_state(BodyState(x.parCount, x.dim)) for x in s]
-    mk_pin = lambda: Descriptors(g, s_pin, tolerance=alg.tolerance, body_force=data.get("bodyforce"),
-                                 dt=data["dt"], precision=args.precision, sort_interval=args.sort_interval,
-                                 **scheme_kw(args))
-    parts = {}
-    e2e_ctx_t0 = time.perf_counter()
-    desc = mk_pin()
-    c2 = MPMContext(desc)
-    c2.set_launch(**launch)
-    t1 = time.perf_counter()
-    limit = healthy_steps(args)
-    e2e_steps = max(args.steps, min(args.e2e_steps, int(0.8 * limit)) if limit else args.e2e_steps)
-    recs, _ = c2.step_energies(e2e_steps, 1, 0)
-    t2 = time.perf_counter()
-    assert recs.shape[0] == e2e_steps and np.all(np.isfinite(recs))
-    states = c2.download_all(out_states)
-    e2e_wall = time.perf_counter() - e2e_ctx_t0
-    parts = {"create_ms": 1e3 * (t1 - e2e_ctx_t0), "steps_ms": 1e3 * (t2 - t1),
-             "download_ms": 1e3 * (e2e_ctx_t0 + e2e_wall - t2)}
-    c2.close()
-    h2d = sum(a.nbytes for a in desc._keep)
-    d2h = sum(sum(getattr(stt, k).nbytes for k in stt.FIELDS) for stt in states)
+    e2e_wall, e2e_steps, h2d, d2h, rec_bytes, parts = e2e_solve(args, g, s, alg, data, launch, args.precision)
     e2e_t = allreduce_max(dist, e2e_wall)
     e2e_value = allreduce_sum(dist, float(npart * e2e_steps)) / e2e_t
 
     extras = {}
     if world == 1 and args.extras and args.workload == "taylor_bar" and args.precision == "f64":
         # the benchmark spec's other three targets, each on its own workload
-        extras["double_word"] = measure_double_word(args, mk, npart, nprof, fp64_state, peak, peak_kind)
+        extras["double_word"] = measure_double_word(args, (g, s, alg, data), mk, npart, nprof, fp64_state, peak,
+                                                    peak_kind)
         extras["ensemble"] = measure_ensemble(args, "ensemble", "f64", 512, 1000)
         extras["adjoint"] = measure_adjoint(args, 2000)
         extras["impact_jvp"] = measure_impact_jvp(args, 64, 200)
@@ -597,7 +600,7 @@ def run_ours(args):
             "late_window": late,
             "e2e": {"value": e2e_value, "unit": METRIC, "steps": e2e_steps,
                     "h2d_bytes_per_step": h2d / e2e_steps,
-                    "d2h_bytes_per_step": d2h / e2e_steps + recs.itemsize * recs.shape[1], "host_memory": "pinned",
+                    "d2h_bytes_per_step": d2h / e2e_steps + rec_bytes, "host_memory": "pinned",
                     "how": f"one solve: create from host arrays, {e2e_steps} steps each with its EnergiesFix record "
                            "(mpm_step_energies: formed on the device, all records copied to the host at the end), "
                            "download all",
@@ -612,12 +615,13 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def measure_double_word(args, mk_fp64, npart, nprof, fp64_state, peak, peak_kind):
+def measure_double_word(args, problem, mk_fp64, npart, nprof, fp64_state, peak, peak_kind):
     """The MPM_PREC_DW variant of the same step (FP64 fields and node sums, the P2G
     and G2P arithmetic in double-word FP32): the same warm-up, timed steps and
     stage profile as the FP64 context, its device throughput and HBM roofline,
-    and the largest relative difference per field from the FP64 state at the
-    same step.  Reported beside the FP64 headline, not as it."""
+    the largest relative difference per field from the FP64 state at the same
+    step, and the end-to-end solve of the FP64 line on a double-word context.
+    Reported beside the FP64 headline, not as it."""
     from jump_gb300 import _capi
     from jump_gb300.engine import MPMContext
     d = mk_fp64()
@@ -640,7 +644,12 @@ def measure_double_word(args, mk_fp64, npart, nprof, fp64_state, peak, peak_kind
         den = float(np.max(np.abs(b))) or 1.0
         err[f] = float(np.max(np.abs(a - b)) / den)
     achieved = BYTES["dw"][dom] * npart / (per[dom] * 1e-3) / 1e9
-    return {"precision": "dw", "value": npart * args.steps / (dev_ms * 1e-3), "unit": METRIC,
+    g, s, alg, data = problem
+    wall, steps, h2d, d2h, rec_bytes, parts = e2e_solve(args, g, s, alg, data, launch, "dw")
+    e2e = {"value": npart * steps / wall, "unit": METRIC, "steps": steps, "h2d_bytes_per_step": h2d / steps,
+           "d2h_bytes_per_step": d2h / steps + rec_bytes, "host_memory": "pinned",
+           "how": "as the FP64 line's e2e, on a double-word context", **parts}
+    return {"precision": "dw", "value": npart * args.steps / (dev_ms * 1e-3), "unit": METRIC, "e2e": e2e,
             "ms_per_step": dev_ms / args.steps, "stage_ms_per_step": per, "launch": launch,
             "launch_chosen_by": "mpm_tune" if tuning else "defaults",
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
