@@ -143,7 +143,7 @@ struct mpm_ctx {
   double last_ms = 0.0;
 
   PartP part(int b) const {
-    PartP pp;
+    PartP pp{};
     pp.base = P;
     pp.pitch = np;
     pp.begin = off[b];
@@ -163,7 +163,7 @@ struct mpm_ctx {
     return pp;
   }
   PartP all() const {
-    PartP pp;
+    PartP pp{};
     pp.base = P;
     pp.pitch = np;
     pp.begin = 0;

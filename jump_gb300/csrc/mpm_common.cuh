@@ -116,8 +116,10 @@ struct NodeP {
   // = two float4), so that a corner's six values come in two 16-byte loads
   float4* nf4;
   // or, for the double-word G2P (MPM_PREC_DW), three float4 per node:
-  // {vdt x hi, lo, vdt y hi, lo}, {vdt z hi, lo, dv x hi, lo}, {dv y hi, lo, dv z hi, lo}
-  float4* dw4 = nullptr;
+  // {vdt x hi, lo, vdt y hi, lo}, {vdt z hi, lo, dv x hi, lo}, {dv y hi, lo, dv z hi, lo};
+  // null otherwise (every NodeP, and every struct holding one, is
+  // value-initialised on the host; the grid update writes it when non-null)
+  float4* dw4;
   const uint8_t* fixed;  // bit a set: dof a is fixed (grid.fixedNodes)
   int64_t nodeCount;
   int64_t nn[3];         // nodes per axis (1 for the unused axis in 2D)
@@ -166,9 +168,11 @@ struct PartP {
   int64_t count;   // particles of this launch
   // Optional hat cache (hat_put / hat_get): the linear P2G stores each
   // particle's hat and the G2P of the same step reads it back, since both see
-  // the positions before the G2P moves them.  Null: the G2P recomputes it.
-  int32_t* hat_c = nullptr;  // D * pitch: cell | bit 27 gl == 0 | bit 28 gl < 0 | bit 29 gh == 0 | bit 30 gh < 0; -1 outside
-  void* hat_nl = nullptr;    // D * pitch values of the particle type: the hat value at the lower node
+  // the positions before the G2P moves them.  Null: the G2P recomputes it
+  // (every PartP, and every struct holding one, is value-initialised on the
+  // host, so both are null unless set).
+  int32_t* hat_c;  // D * pitch: cell | bit 27 gl == 0 | bit 28 gl < 0 | bit 29 gh == 0 | bit 30 gh < 0; -1 outside
+  void* hat_nl;    // D * pitch values of the particle type: the hat value at the lower node
 };
 
 // Record cursor of the EnergiesFix sums of captured steps (energies_kernel):
