@@ -810,7 +810,8 @@ namespace jmpm {
 // of the node accumulators for the next step), separated by grid barriers
 // (grid_barrier: bounded waits that set q.bar[2] and end the kernel).  Thread
 // t handles particles t, t + nthreads, ... in both particle stages, so a
-// particle's fields are only ever read on the SM that wrote them; node values
+// particle's fields, and the hat its P2G caches for the G2P of the same step,
+// are only ever read by the thread that wrote them; node values
 // written in the launch by other CTAs are read through L2 (grid_node and
 // g2p_particle with CG, P2G through atomics).
 struct FusedP {
@@ -827,6 +828,9 @@ struct FusedP {
   // the second set of node accumulators (m, p0 (D), f (D)): steps alternate
   // between it and nd's, ending on nd's
   double *m2, *p02, *f2;
+  // the hat cache (PartP::hat_c / hat_nl; null: the G2P recomputes each hat)
+  int32_t* hat_c;
+  void* hat_nl;
   // EnergiesFix records after steps first, first + every, ... (rec non-null):
   // per-CTA partial sums, folded by CTA 0 in a fixed order into rec->base[rec->idx++]
   EnRec* rec;
@@ -840,7 +844,7 @@ __global__ void __launch_bounds__(128) fused_steps_kernel(FusedP q, int64_t nste
   const int64_t nth = int64_t(gridDim.x) * blockDim.x;
   unsigned* err = q.bar + 2;
   if (*reinterpret_cast<volatile unsigned*>(err)) return;  // an earlier wait gave up
-  const PartP all{q.P, q.pitch, 0, q.np};
+  const PartP all{q.P, q.pitch, 0, q.np, q.hat_c, q.hat_nl};
   const int64_t Nn = q.nd.nodeCount;
   // two sets of accumulators, A (the context's) and B: step s sums into A when
   // nsteps - 1 - s is even, so the last step's sums are the context's; while
@@ -879,7 +883,7 @@ __global__ void __launch_bounds__(128) fused_steps_kernel(FusedP q, int64_t nste
     for (int64_t p = tid; p < q.np; p += nth) {
       int b = 0;
       while (b + 1 < q.nb && p >= q.bbeg[b + 1]) ++b;
-      const PartP pb{q.P, q.pitch, q.bbeg[b], q.np - q.bbeg[b]};
+      const PartP pb{q.P, q.pitch, q.bbeg[b], q.np - q.bbeg[b], q.hat_c, q.hat_nl};
       g2p_particle<D, double, MAT, true>(q.g, cur, pb, p - q.bbeg[b], q.mp[b], q.dt, q.status);
     }
     if (q.rec && s >= q.first && (s - q.first) % q.every == 0) {
@@ -966,7 +970,8 @@ size_t fused_bytes(int dim, int64_t nodes) {
 
 int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
                 int nb, const int64_t* bbeg, const int64_t* bcnt, const MatParams* mp, double dt, double tol,
-                const double* grav, int64_t nsteps, unsigned* status, EnRec* rec, int64_t first, int64_t every) {
+                const double* grav, int64_t nsteps, unsigned* status, EnRec* rec, int64_t first, int64_t every,
+                int32_t* hat_c, void* hat_nl) {
   if (nb < 1 || nb > MPM_BATCH_MAX_BODIES) return fail(MPM_ERR_ARG, "fused_steps: body count");
   FusedP q{};
   q.g = g;
@@ -986,6 +991,8 @@ int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP&
   q.tol = tol;
   for (int a = 0; a < 3; ++a) q.grav[a] = grav[a];
   q.status = status;
+  q.hat_c = hat_c;
+  q.hat_nl = hat_nl;
   q.bar = static_cast<unsigned*>(dev);
   q.rec = rec;
   q.first = first;

@@ -920,7 +920,7 @@ static int fused_run(mpm_ctx* c, int64_t n, bool rec = false, int64_t first = 0,
   if (!c->fused) CUDA_TRY(cudaMalloc(&c->fused, fused_bytes(c->dim, c->nd.nodeCount)));
   int r = fused_steps(c->dim, c->stream, c->fused, c->g, c->nd, c->P, c->np, c->nb, c->off.data(), c->cnt.data(),
                       c->mats.data(), c->prm.dt, c->prm.tolerance, c->prm.body_force, n, c->status,
-                      rec ? c->en_rec : nullptr, first, every);
+                      rec ? c->en_rec : nullptr, first, every, c->hat_c, c->hat_nl);
   c->full_clear = true;
   return r;
 }

@@ -101,7 +101,7 @@ size_t fused_bytes(int dim, int64_t nodes);
 int fused_steps(int dim, cudaStream_t s, void* dev, const GridP& g, const NodeP& nd, void* P, int64_t pitch,
                 int nb, const int64_t* bbeg, const int64_t* bcnt, const MatParams* mp, double dt, double tol,
                 const double* grav, int64_t nsteps, unsigned* status, EnRec* rec = nullptr, int64_t first = 0,
-                int64_t every = 1);
+                int64_t every = 1, int32_t* hat_c = nullptr, void* hat_nl = nullptr);
 
 // deformable material model types a context or batch accepts in dimension dim
 // (rigid bodies, MPM_MAT_RIGID, are checked separately: contexts only)
