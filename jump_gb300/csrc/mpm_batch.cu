@@ -54,7 +54,8 @@ struct InstanceP {
 
 template <int D, class R, int MAT, bool GRAV>
 __global__ void batch_kernel(const InstanceP* __restrict__ inst, const int* __restrict__ order, int ninst,
-                             int* next, int64_t nsteps, void* P, int64_t pitch, unsigned* status) {
+                             int* next, int64_t nsteps, void* P, int64_t pitch, unsigned* status, int32_t* hat_c,
+                             void* hat_nl) {
   __shared__ int sh_q;
   constexpr bool F32 = sizeof(R) == 4;
   for (;;) {
@@ -65,7 +66,7 @@ __global__ void batch_kernel(const InstanceP* __restrict__ inst, const int* __re
     if (q >= ninst) return;
     const int id = order[q];
     const InstanceP& I = inst[id];
-    const PartP all{P, pitch, I.pbegin, I.pcount};
+    const PartP all{P, pitch, I.pbegin, I.pcount, hat_c, hat_nl};
     unsigned* st = status + id;
     const int64_t Nn = I.nd.nodeCount;
     for (int64_t s = 0; s < nsteps; ++s) {
@@ -86,7 +87,7 @@ __global__ void batch_kernel(const InstanceP* __restrict__ inst, const int* __re
       for (int64_t i = threadIdx.x; i < Nn; i += blockDim.x) grid_node<D, F32, true>(I.nd, i, I.dt, I.tol);
       __syncthreads();
       for (int b = 0; b < I.nb; ++b) {
-        const PartP pb{P, pitch, I.bbeg[b], I.bcnt[b]};
+        const PartP pb{P, pitch, I.bbeg[b], I.bcnt[b], hat_c, hat_nl};
         for (int64_t t = threadIdx.x; t < pb.count; t += blockDim.x)
           g2p_particle<D, R, MAT, true>(I.g, I.nd, pb, t, I.mp[b], I.dt, st);
       }
@@ -188,6 +189,9 @@ struct mpm_batch {
   int NF = 0;
   size_t esz = 8;
   void* P = nullptr;
+  // hat cache of the persistent kernel's FP64 steps (PartP::hat_c / hat_nl), or null
+  int32_t* hat_c = nullptr;
+  void* hat_nl = nullptr;
   double* nodebuf = nullptr;
   float* nodebuf_f = nullptr;
   uint8_t* fixed = nullptr;
@@ -248,6 +252,7 @@ namespace {
 void destroy_batch(mpm_batch* b) {
   if (!b) return;
   cudaFree(b->P);
+  cudaFree(b->hat_c);
   cudaFree(b->nodebuf);
   cudaFree(b->nodebuf_f);
   cudaFree(b->fixed);
@@ -293,7 +298,7 @@ int launch_t(mpm_batch* b, void* P, int64_t nsteps, int threads, int per_sm) {
   int per = per_sm > 0 ? std::min(per_sm, occ) : occ;
   BATCH_TRY(cudaMemsetAsync(b->d_next, 0, sizeof(int), b->stream));
   kern<<<b->sms * per, threads, 0, b->stream>>>(b->d_inst, b->d_order, b->ninst, b->d_next, nsteps, P, b->np,
-                                                b->d_status);
+                                                b->d_status, b->hat_c, b->hat_nl);
   BATCH_TRY(cudaGetLastError());
   return MPM_OK;
 }
@@ -555,6 +560,16 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
   const size_t ptot = size_t(b->NF) * size_t(b->np > 0 ? b->np : 1);
   BATCH_TRY(cudaMalloc(&b->P, ptot * b->esz));
   BATCH_TRY(cudaMemset(b->P, 0, ptot * b->esz));
+  if (!b->f32 && b->np > 0) {
+    // hat cache: int32 codes, then the lower hat values (every axis has at most
+    // 2^20 nodes, so a cell fits the code's 27 bits)
+    const size_t nc = size_t(D) * size_t(b->np);
+    const size_t cbytes = (nc * sizeof(int32_t) + 15) / 16 * 16;
+    char* hb = nullptr;
+    BATCH_TRY(cudaMalloc(&hb, cbytes + nc * sizeof(double)));
+    b->hat_c = reinterpret_cast<int32_t*>(hb);
+    b->hat_nl = hb + cbytes;
+  }
   // per node: m | p0 (D) | f (D) | vdt (D) | dv (D); contact fields add the normals (D)
   if (plain_nodes > 0) {
     BATCH_TRY(cudaMalloc(&b->nodebuf, size_t(plain_nodes) * (1 + 4 * D) * sizeof(double)));
