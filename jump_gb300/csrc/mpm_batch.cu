@@ -706,6 +706,8 @@ int create_t(const mpm_instance_desc* in, int32_t n, mpm_batch* b) {
       for (int k = 0; k < b->inst[i].nb; ++k) {
         WideBody wb{};
         wb.pp = b->body(i, k);
+        wb.pp.hat_c = b->hat_c;  // the wide P2G caches each hat for the wide G2P of the step
+        wb.pp.hat_nl = b->hat_nl;
         wb.nd = W.cp.body[W.contact ? k : 0];
         wb.mp = b->inst[i].mp[k];
         wb.inst = i;
